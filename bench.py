@@ -1,0 +1,350 @@
+"""Throughput of SWAP's hybrid PIC ion step on GB300: ion particle-steps/s.
+
+A step is one full ion step of maind.f:385-479 (three particle passes with
+four moment deposits, the field predictor-corrector with its subcycles and
+the final half move) over every particle of the workload.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--precision f64] [--config 1]
+
+Rank 0 prints one JSON line.  --impl reference times the reference's CPU
+path (the C++ restatement in oracle/, the reference itself has no Fortran
+compiler here) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "ion particle-steps/s on 1 GB300 (FP64 plain step)"
+UNIT = "particle-steps/s"
+
+
+# ---------------------------------------------------------------------------
+# helpers
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int = 0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def barrier_max(value: float, ws: int) -> float:
+    if ws == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws: int):
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+
+        dist.barrier()
+        torch.cuda.synchronize()
+
+
+# Algorithmic (compulsory) HBM bytes per unit for the FP64 drop-in kernels:
+# each reads/writes its particle arrays once; gathered field values and the
+# deposit targets are node data that stay in L2 and are not counted.
+# Units: particles for particle kernels, interior nodes for stencils.
+KERNEL_BYTES_F64 = {
+    "interp_weights": 24 + 12 + 64,            # read xp; write ijk, wght
+    "deposit_np": 12 + 64 + 8,                 # read ijk, wght, beta_p
+    "deposit_u": 12 + 64 + 8 + 48,             # + two velocity arrays (worst case of the modes)
+    "get_Ep": 12 + 64 + 8 + 24,                # read ijk, wght, mrat; write Ep
+    "vplus_vminus": 12 + 64 + 8 + 24 + 24 + 48,  # + Ep, vp; write v+, v-
+    "vp_final": 24 + 24 + 24 + 48,
+    "move_half": 24 + 24 + 24,
+}
+
+
+def cpu_sample_oracle(cfg_full, steps: int, threads: int):
+    """Time the oracle's FP64 ion step on a sub-box of the workload (same ppc,
+    same physics), on `threads` host threads.  Returns (particle-steps/s, info)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+    from swap_gb300.grid import grd6_setup, grd7
+    from swap_gb300.hybrid import RunConfig
+
+    cells = (64, 32, 32)
+    cfg = RunConfig(name="cpu sample", cells=cells, ppc=cfg_full.ppc, vth=cfg_full.vth, u=cfg_full.u,
+                    dt=cfg_full.dt, ntsub=cfg_full.ntsub, nu=cfg_full.nu, seed=cfg_full.seed)
+    nx, ny, nz = cfg.nodes
+    n = cfg.n_particles
+
+    class Host:  # arrays in the layout the oracle binds
+        pass
+
+    h = Host()
+    h.cfg = cfg
+    h.ni_max = n
+    co = grd7(nx, ny, nz)
+    f3 = lambda: np.zeros((n, 3), order="F")
+    h.xp, h.vp, h.vp1, h.Ep, h.vplus, h.vminus = (f3() for _ in range(6))
+    h.mrat, h.beta_p = np.ones(n), np.ones(n)
+    h.ni_tot = np.array([n], dtype=np.int32)
+    for k, v in grd6_setup(co, cfg.b0, cfg.nu).items():
+        setattr(h, k, v)
+    # the same stratified Maxwellian load as the GPU run, made by the product loader
+    from swap_gb300 import abi
+    import ctypes as C
+
+    lib = abi.load()
+    dims = abi.Dims(nx, ny, nz, 0, n)
+    cc = abi.Coords(*[abi.dptr(getattr(co, a)) for a in co.ARRAYS])
+    spec = abi.LoadSpec(cfg.seed, 0, cfg.ppc, cfg.vth, *cfg.u, 1.0, 1.0)
+    cnt = C.c_int64()
+    abi.check(lib, None, lib.swap_load_maxwellian_host(C.byref(dims), C.byref(cc), C.byref(spec), abi.dptr(h.xp),
+                                                        abi.dptr(h.vp), abi.dptr(h.vp1), abi.dptr(h.mrat),
+                                                        abi.dptr(h.beta_p), 0, C.byref(cnt)))
+    o = pyoracle.from_hybrid_arrays(h, precision="f64", nthreads=threads)
+    t0 = time.perf_counter()
+    o.run(steps)
+    dt = time.perf_counter() - t0
+    info = {"sample": f"{cells[0]}x{cells[1]}x{cells[2]}-cell sub-box of the workload at {cfg.ppc} ppc "
+                      f"({n:,} ions), {steps} FP64 ion steps of the oracle",
+            "seconds": dt}
+    return n * steps / dt, info
+
+
+# ---------------------------------------------------------------------------
+# reference arm: the reference's CPU path (restated) on the host cores
+# ---------------------------------------------------------------------------
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from swap_gb300.hybrid import config
+
+    cfg = config(args.config)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_sample_oracle(cfg, 1, threads)
+    vals = []
+    info = None
+    for _ in range(args.steps):
+        v, info = cpu_sample_oracle(cfg, 1, threads)
+        vals.append(v)
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference",
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": cfg.n_particles / value * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": cfg.name, "cells": list(cfg.cells), "ppc": cfg.ppc, "ions": cfg.n_particles,
+                   "subcycles": cfg.ntsub},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": info["sample"]},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+
+def run_ours(args):
+    ws, rank, local = dist_env()
+    import torch
+
+    if ws > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    from swap_gb300.hybrid import Hybrid, config
+
+    cfg = config(args.config)
+    # Each rank runs its own replica of the workload: the particle-decomposed
+    # exchange (an allreduce of the moments after each deposit) is not built.
+    h = Hybrid(cfg, pinned=True)
+    t_load = time.perf_counter()
+    h.load_maxwellian(seed=cfg.seed + 1000 * rank)
+    t_load = time.perf_counter() - t_load
+    N = int(h.ni_tot[0])
+    h.sync_to_device()
+
+    for _ in range(args.warmup):
+        h.run(1)
+    lib, ctx = h.lib, h.ctx
+
+    # ---- timed region: K steps, device-resident, CUDA events on the library stream
+    lib.swap_profile_reset(ctx)
+    lib.swap_profile_enable(ctx, 1)
+    barrier(ws)
+    clocks = ClockSampler(local)
+    clocks.start()
+    import ctypes as C
+
+    ms = C.c_double()
+    h._check(lib.swap_timer_start(ctx))
+    h.run(args.steps)
+    h._check(lib.swap_timer_stop(ctx, C.byref(ms)))
+    clk = clocks.stop()
+    lib.swap_profile_enable(ctx, 0)
+    t_ms = barrier_max(ms.value, ws)
+
+    names = (C.c_char_p * 64)()
+    tot = (C.c_double * 64)()
+    cnt = (C.c_int64 * 64)()
+    n = C.c_int32()
+    lib.swap_profile_read(ctx, 64, names, tot, cnt, C.byref(n))
+    prof = {names[i].decode(): (tot[i], cnt[i]) for i in range(min(n.value, 64))}
+    kernels = {k: v for k, v in prof.items() if not k.startswith("cuda")}
+    launches = int(sum(v[1] for v in kernels.values()))
+    top = max(kernels.items(), key=lambda kv: kv[1][0])
+    top_name, (top_ms, top_n) = top
+    units = N if top_name in KERNEL_BYTES_F64 else (cfg.nodes[0] - 2) * (cfg.nodes[1] - 2) * (cfg.nodes[2] - 2)
+    per_unit = KERNEL_BYTES_F64.get(top_name, 0)
+    avg_s = top_ms / 1e3 / max(top_n, 1)
+    achieved = per_unit * units / avg_s / 1e9 if per_unit else None
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+
+    # ---- end to end through the C-ABI with host buffers (pinned): upload the
+    # whole state, K steps each followed by the per-step Energy_diag read
+    # (maind.f:391-393,503-505), download the whole state.
+    state_arrays = [h.xp, h.vp, h.vp1, h.mrat, h.beta_p]
+    state_bytes_p = N * 8 * 11
+    field_bytes = sum(getattr(h, a).nbytes for a in ("b0", "b1", "b12", "b1p2", "bt", "btc", "np", "up", "aj", "E",
+                                                      "nu"))
+    h.sync_to_host()
+    barrier(ws)
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    h.mark_host_dirty()
+    h.sync_to_device()
+    for _ in range(args.steps):
+        h.run(1)
+        h.energy()
+    h.sync_to_host()
+    torch.cuda.synchronize()
+    e2e_s = barrier_max(time.perf_counter() - w0, ws)
+    del state_arrays
+
+    value = N * args.steps * ws / (t_ms / 1e3)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded stratified Maxwellian load, normalized units)",
+        "config": {"workload": cfg.name, "cells": list(cfg.cells), "ppc": cfg.ppc, "ions": N,
+                   "subcycles": cfg.ntsub, "precision_form": "FP64 drop-in",
+                   "l2": "inputs larger than L2 (particle state %.1f GB)" % (N * 72 / 1e9),
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU"},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "peak_source": "measured" if peaks else "fallback",
+                     "note": "FP64 kernels on GB300 are bound by the FP64 pipe, not HBM"},
+        "kernels_ms_per_step": {k: v[0] / args.steps for k, v in sorted(kernels.items(), key=lambda kv: -kv[1][0])},
+        "e2e": {"value": N * args.steps * ws / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": (state_bytes_p + field_bytes) / args.steps,
+                "d2h_bytes_per_step": (state_bytes_p + field_bytes) / args.steps + 32},
+        "load_seconds": t_load,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        v, info = cpu_sample_oracle(cfg, 1, os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                                "sample": info["sample"]}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    h.close()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,179 @@
+/* swap_gpu.h -- C-ABI of the GB300 (sm_103a) hybrid PIC ion step.
+ *
+ * Drop-in for the particle and field subroutines of SWAP (pdelamere/SWAP):
+ * gutsp.f, gutsf.f, grid_interp.f and boundary.f.  A Fortran caller reaches
+ * these entries through the bind(C) module in swap_gb300/fortran/, whose
+ * wrappers keep the original subroutine names and argument lists; the C
+ * entries take the same arguments in the same order plus a context.
+ *
+ * Data model.
+ *   - Arrays are the caller's host arrays in Fortran layout: grids
+ *     (nx,ny,nz[,3]) column-major, x fastest, component slowest; particles
+ *     (ni_max,3) column-major.  Reals are IEEE double (the reference built with
+ *     -real-size 64); indices are int32 (-i4, makefile:1).
+ *   - Every host array an entry receives must first be registered
+ *     (swap_bind_particles / swap_bind_fields / swap_bind_array).  The context
+ *     keeps a device mirror of each and tracks which copy is current: an entry
+ *     uploads an input whose device copy is stale, runs on the device, and
+ *     marks its outputs device-current.  swap_sync_to_host() brings results
+ *     back; swap_mark_host_dirty() tells the context the caller changed a host
+ *     array.  The implicit COMMON state of the reference (ijkp, wght,
+ *     /dummy/ a,c,ct) lives on the device inside the context.
+ *   - Every entry returns 0 on success and a SWAP_E* code otherwise; the
+ *     message is in swap_last_error(ctx).  No entry aborts, exits or traps.
+ *   - Calls on one context must not run concurrently.  Entries are
+ *     synchronous on return.
+ *   - This library never calls MPI.  In a multi-rank run the deposit entries
+ *     still return the folded, complete moments of the local particles; the
+ *     caller keeps its MPI_ALLREDUCE (gutsp.f:1503,1812-1822).
+ */
+#ifndef SWAP_GPU_H
+#define SWAP_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define SWAP_OK 0
+#define SWAP_EINVAL 1        /* bad argument (null, size, unregistered array) */
+#define SWAP_ECUDA 2         /* CUDA runtime error (allocation, launch)       */
+#define SWAP_EDOMAIN 3       /* a particle lies outside the grid               */
+#define SWAP_ECAPACITY 4     /* ni_tot > ni_max or a work buffer too small     */
+#define SWAP_ENONFINITE 5    /* non-finite value found by swap_check_finite    */
+#define SWAP_ESUBCYCLE 6     /* subcycle count overflow in check_time_step     */
+#define SWAP_EMOVE 7         /* a particle moved more than one cell in a step  */
+#define SWAP_EWAIT 8         /* a device wait reached its iteration limit      */
+
+typedef struct swap_ctx swap_ctx;
+
+/* Grid and particle capacity: dimensions.f:5,9 (nx,ny,nz,Ni_max). */
+typedef struct swap_dims {
+  int32_t nx, ny, nz;
+  int32_t reserved;
+  int64_t ni_max;
+} swap_dims;
+
+/* Scalars of module `inputs`/`global` that the hot path reads. */
+typedef struct swap_params {
+  double dt;         /* ion step (inputs.f:141)                               */
+  double alpha;      /* mu0/1e3*q*q/m (inputs.f:170)                          */
+  double beta;       /* particle scale factor (misc.f:462-475)                */
+  double dx, dy;     /* module dx, dy; dy enters the y cell index (gutsp.f:1404) */
+  double grad_pe;    /* isothermal T_e/m of the electron-pressure extension;
+                        0 = the reference's E (no pressure term)              */
+  int32_t ntsub;     /* field subcycles per ion step (inputs.f:140)           */
+  int32_t flags;     /* reserved, 0                                           */
+} swap_params;
+
+/* The /coords/ COMMON block (global.f:27-38) as 0-based copies of the
+ * 1-based Fortran arrays: qx[0] holds qx(1).  Lengths nx, ny or nz. */
+typedef struct swap_coords {
+  const double *qx, *qy, *qz;
+  const double *dx_grid, *dy_grid, *dz_grid;
+  const double *dx_cell, *dy_cell, *dz_cell;
+  const double *xrat, *yrat, *zrat;
+} swap_coords;
+
+/* ---- lifecycle ---- */
+int swap_init(swap_ctx** ctx, const swap_dims* dims, const swap_params* params, const swap_coords* coords);
+int swap_finalize(swap_ctx* ctx);
+const char* swap_last_error(const swap_ctx* ctx);
+int swap_abi_version(void);
+
+/* ---- array registration and data movement ---- */
+/* The particle arrays of maind.f:54-59 and global.f:44,96,100; ijkp may be
+ * NULL.  ni_tot is the caller's Ni_tot (global.f:41), read at every call. */
+int swap_bind_particles(swap_ctx* ctx, double* xp, double* vp, double* vp1, double* mrat, double* beta_p,
+                        int32_t* ijkp, int32_t* ni_tot);
+/* The grid arrays of maind.f:38-70. */
+int swap_bind_fields(swap_ctx* ctx, double* b0, double* b1, double* b12, double* b1p2, double* bt, double* btc,
+                     double* np, double* up, double* aj, double* E, double* nu);
+/* Any other array an entry is handed (e.g. Ep, vplus, vminus). */
+int swap_bind_array(swap_ctx* ctx, void* host, int64_t bytes);
+/* host = NULL: every registered array. */
+int swap_sync_to_device(swap_ctx* ctx, const void* host);
+int swap_sync_to_host(swap_ctx* ctx, void* host);
+int swap_mark_host_dirty(swap_ctx* ctx, const void* host);
+
+/* ---- one entry per reference subroutine (same arguments, same order) ---- */
+int swap_get_interp_weights(swap_ctx* ctx, const double* xp);                          /* gutsp.f:1378 */
+int swap_update_np(swap_ctx* ctx, double* np);                                          /* gutsp.f:1441 */
+int swap_update_up(swap_ctx* ctx, const double* vp, const double* np, double* up);      /* gutsp.f:1649 */
+int swap_extrapol_up(swap_ctx* ctx, double* up, const double* vp, const double* vp1,
+                     const double* np);                                                 /* gutsp.f:127  */
+int swap_get_Ep(swap_ctx* ctx, double* Ep, double* aj, const double* np, double* up, const double* btc,
+                const double* nu);                                                      /* gutsp.f:155  */
+int swap_get_vplus_vminus(swap_ctx* ctx, const double* Ep, const double* btc, const double* vp,
+                          double* vplus, double* vminus);                               /* gutsp.f:281  */
+int swap_improve_up(swap_ctx* ctx, double* vp1, const double* vplus, const double* vminus, double* up,
+                    const double* np);                                                  /* gutsp.f:407  */
+int swap_get_vp_final(swap_ctx* ctx, const double* Ep, double* vp, double* vp1,
+                      const double* vplus);                                             /* gutsp.f:433  */
+int swap_move_ion_half(swap_ctx* ctx, double* xp, const double* vp, const double* vp1,
+                       double* input_p);                                                /* gutsp.f:454  */
+int swap_curlB(swap_ctx* ctx, double* bt, const double* np, double* aj);                /* gutsf.f:178  */
+int swap_edge_to_center(swap_ctx* ctx, double* bt, double* btc);                        /* grid_interp.f:10 */
+int swap_face_to_center(swap_ctx* ctx, double* v, double* vc);                          /* grid_interp.f:136 */
+int swap_get_E(swap_ctx* ctx, double* E, const double* b0, double* bt, double* aj, const double* up,
+               const double* np, const double* nu);                                     /* gutsf.f:994  */
+/* dtsub is the module variable of global.f:76 that the Fortran reads. */
+int swap_predict_B(swap_ctx* ctx, double* b0, double* b1, double* b12, double* b1p2, double* bt, double* E,
+                   double* aj, double* up, double* np, double* nu, double dtsub);       /* gutsf.f:1115 */
+int swap_correct_B(swap_ctx* ctx, double* b0, double* b1, double* b1p2, double* E, double* aj, double* up,
+                   double* np, double* nu, double dtsub);                               /* gutsf.f:1309 */
+int swap_f_update_tlev(swap_ctx* ctx, double* b1, double* b12, double* b1p2, double* bt,
+                       const double* b0);                                               /* gutsf.f:10   */
+/* dtsub/ntf in and out (global.f:76-77; ntf is real there). */
+int swap_check_time_step(swap_ctx* ctx, const double* bt, const double* np, double* dtsub,
+                         double* ntf);                                                  /* gutsf.f:1776 */
+int swap_periodic(swap_ctx* ctx, double* b);                                            /* boundary.f:9 */
+int swap_periodic_scalar(swap_ctx* ctx, double* b);                                     /* boundary.f:167 */
+
+/* ---- fused, device-resident ion step on the bound arrays ---- */
+int swap_ion_step_pre(swap_ctx* ctx);     /* maind.f:385-413 */
+int swap_field_subcycles(swap_ctx* ctx);  /* maind.f:420-476 */
+int swap_ion_step_post(swap_ctx* ctx);    /* maind.f:479     */
+int swap_ion_step(swap_ctx* ctx);         /* maind.f:385-479 */
+int swap_run(swap_ctx* ctx, int32_t nsteps);
+
+/* ---- diagnostics (FP64, device reductions) ---- */
+/* out[0] kinetic, out[1] |b1-b0|^2 field, out[2] |b1|^2 field, out[3] |E|^2,
+ * in the normalized units of the oracle (part_init.f:14-139 sums the j=2
+ * plane only; this is the full-3D form). */
+int swap_energy(swap_ctx* ctx, double out[4]);
+int swap_max_abs_divB(swap_ctx* ctx, const double* b, double* out);
+/* SWAP_ENONFINITE if any registered array holds a NaN or Inf. */
+int swap_check_finite(swap_ctx* ctx);
+
+/* ---- particle loading (host, product-side; replaces part_init.f:146-232) ---- */
+typedef struct swap_load_spec {
+  uint64_t seed;
+  uint32_t stream;       /* species / population id mixed into the key   */
+  int32_t ppc;           /* particles per physical cell (stratified load) */
+  double vth;            /* reference convention: v = vth*sqrt(-ln U)*cos(pi U') */
+  double ux, uy, uz;     /* bulk flow                                     */
+  double mrat;           /* q/m relative to H+ (global.f:100)             */
+  double beta_p;         /* statistical weight factor (global.f:96)       */
+} swap_load_spec;
+/* Fill particles first .. first+ncell*ppc-1 (0-based) with a stratified
+ * Maxwellian over the physical cells of coords; returns the count in *count. */
+int swap_load_maxwellian_host(const swap_dims* dims, const swap_coords* coords, const swap_load_spec* spec,
+                              double* xp, double* vp, double* vp1, double* mrat, double* beta_p, int64_t first,
+                              int64_t* count);
+
+/* ---- timing (CUDA events on the context's stream) ---- */
+int swap_timer_start(swap_ctx* ctx);
+int swap_timer_stop(swap_ctx* ctx, double* ms);
+/* Per-kernel CUDA-event timing of the fused path; names are static strings. */
+int swap_profile_enable(swap_ctx* ctx, int on);
+int swap_profile_read(swap_ctx* ctx, int32_t max, const char** names, double* total_ms, int64_t* launches,
+                      int32_t* n);
+int swap_profile_reset(swap_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SWAP_GPU_H */

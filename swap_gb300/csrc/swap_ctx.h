@@ -1,0 +1,89 @@
+// swap_ctx.h -- host-side state behind a swap_ctx handle.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/swap_gpu.h"
+#include "k64.cuh"
+
+enum class MirrorKind { Grid, Particle3, Particle1, ParticleI3 };
+enum class Access { In, Out, InOut };
+
+// A caller's host array and its device copy, with which side is current.
+struct Mirror {
+  void* host = nullptr;
+  void* dev = nullptr;
+  std::size_t bytes = 0;
+  MirrorKind kind = MirrorKind::Grid;
+  bool host_valid = true;
+  bool dev_valid = false;
+};
+
+struct ProfEntry {
+  const char* name;
+  double ms;
+  long long launches;
+};
+
+struct swap_ctx {
+  swap_dims dims{};
+  swap_params prm{};
+  swapk::Geo g{};
+  cudaStream_t st = nullptr;
+  int* d_err = nullptr;
+  std::string err;
+
+  // registry of bound host arrays
+  std::unordered_map<const void*, Mirror> reg;
+  std::vector<Mirror*> touched;
+  std::vector<void*> owned;  // device buffers freed at finalize
+
+  // host addresses of the bound arrays (the Fortran's own)
+  double *h_xp = nullptr, *h_vp = nullptr, *h_vp1 = nullptr, *h_mrat = nullptr, *h_beta_p = nullptr;
+  int32_t* h_ijkp = nullptr;
+  int32_t* ni_tot_ptr = nullptr;
+  double *h_b0 = nullptr, *h_b1 = nullptr, *h_b12 = nullptr, *h_b1p2 = nullptr, *h_bt = nullptr, *h_btc = nullptr;
+  double *h_np = nullptr, *h_up = nullptr, *h_aj = nullptr, *h_E = nullptr, *h_nu = nullptr;
+  std::vector<double> h_qx, h_qy, h_qz;
+
+  // device state of the implicit COMMON blocks
+  double *d_mrat = nullptr, *d_beta_p = nullptr;
+  int32_t* d_ijk = nullptr;   // /ion_info/ ijkp
+  double* d_wght = nullptr;   // /weights/ wght
+  bool weights_valid = false;
+
+  // grid scratch: /dummy/ a, c, ct and subroutine locals
+  double *s_a = nullptr, *s_aa = nullptr, *s_c = nullptr, *s_ct = nullptr, *s_btcl = nullptr, *s_btc2 = nullptr;
+  double *s_btmf = nullptr, *s_ajc = nullptr, *s_upc = nullptr, *s_btp1 = nullptr, *s_S = nullptr;
+  double *s_gf = nullptr, *s_gpc = nullptr, *s_dtn = nullptr, *s_red = nullptr;
+  // particle work arrays of the fused step (maind.f locals Ep, vplus, vminus)
+  double *w_Ep = nullptr, *w_vplus = nullptr, *w_vminus = nullptr;
+  double last_dtsub = 0, last_ntf = 0;
+
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+
+  // per-kernel profile (CUDA events), filled by the fused paths
+  bool prof_on = false;
+  std::vector<ProfEntry> prof;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_pending;
+  std::vector<cudaEvent_t> prof_pool;
+
+  int fail(int code, const std::string& msg);
+  int cuda_fail(cudaError_t e, const char* where);
+  double* dalloc(std::size_t n);
+  Mirror* find(const void* host);
+  int add_mirror(void* host, std::size_t bytes, MirrorKind kind);
+  int transfer(Mirror& m, bool to_dev);
+  int use(const void* host, Access acc, double** dev);
+  int begin();
+  int finish();
+  long long ntot() const;
+  swapk::PartDev part_view();
+  void prof_free();
+};

@@ -1,0 +1,234 @@
+"""Host-side mirror of the reference's hot-path interface.
+
+``Hybrid`` owns the arrays that maind.f declares (maind.f:38-70) in Fortran
+layout, registers them with the C-ABI context, and exposes one method per
+reference subroutine with the same name and arguments (gutsp.f, gutsf.f,
+grid_interp.f, boundary.f), so a replay of maind.f reads like the Fortran.
+All computation runs in the sm_103a library; there is no CPU path here.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import abi
+from .grid import Coords, grd6_setup, grd7
+
+
+@dataclass
+class RunConfig:
+    """A workload in normalized units: d_i = 1, Omega_i = 1, v_A = 1, n0 = 1
+    (alpha*n0 = 1, B0 = 1 as a gyrofrequency)."""
+
+    name: str
+    cells: tuple  # physical cells (x, y, z); nodes = cells + 2 ghosts
+    ppc: int
+    vth: float = 0.5
+    u: tuple = (2.0, 0.0, 0.0)
+    b0: float = 1.0
+    n0: float = 1.0
+    dt: float = 0.05
+    ntsub: int = 10
+    nu: float = 0.002  # nu_init_frac of inputs.dat, in units of Omega_i
+    steps: int = 100
+    seed: int = 1
+    grad_pe: float = 0.0
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def nodes(self):
+        return tuple(c + 2 for c in self.cells)
+
+    @property
+    def n_particles(self) -> int:
+        return int(np.prod(self.cells)) * self.ppc
+
+    @property
+    def alpha(self) -> float:
+        return 1.0 / self.n0
+
+    @property
+    def beta(self) -> float:
+        # one macro-particle per cell of volume 1 carries n0/ppc
+        return self.ppc / self.n0
+
+
+def config(n: int, **over) -> RunConfig:
+    """The named workloads: 0 = 64x32x32 cells, 16 ppc (1,048,576 ions; the
+    stated 524,288 is 8 ppc); 1 = 256x128x128 cells, 32 ppc (134,217,728 ions)."""
+    base = {
+        0: dict(name="uniform H+ 64x32x32, 16 ppc", cells=(64, 32, 32), ppc=16, steps=100, seed=1),
+        1: dict(name="uniform H+ 256x128x128, 32 ppc", cells=(256, 128, 128), ppc=32, steps=200, seed=2),
+    }[n]
+    base.update(over)
+    return RunConfig(**base)
+
+
+class Hybrid:
+    """One context on the current GPU with the reference's arrays bound."""
+
+    def __init__(self, cfg: RunConfig, ni_max: int | None = None, coords: Coords | None = None,
+                 pinned: bool = False):
+        self.cfg = cfg
+        self.lib = abi.load()
+        nx, ny, nz = cfg.nodes
+        self.coords = coords or grd7(nx, ny, nz)
+        self.ni_max = int(ni_max if ni_max is not None else cfg.n_particles)
+        NM = self.ni_max
+        self.dims = abi.Dims(nx, ny, nz, 0, NM)
+        self.params = abi.Params(cfg.dt, cfg.alpha, cfg.beta, self.coords.dx, self.coords.dy, cfg.grad_pe, cfg.ntsub, 0)
+        self._coords_c = abi.Coords(*[abi.dptr(getattr(self.coords, n)) for n in Coords.ARRAYS])
+        self._pins = []
+        # particle arrays (maind.f:54-59, global.f:44,96,100)
+        f = (lambda: self._pinned((NM, 3))) if pinned else (lambda: np.zeros((NM, 3), dtype=np.float64, order="F"))
+        self.xp, self.vp, self.vp1 = f(), f(), f()
+        self.Ep, self.vplus, self.vminus = f(), f(), f()
+        self.mrat = np.ones(NM, dtype=np.float64)
+        self.beta_p = np.ones(NM, dtype=np.float64)
+        self.ijkp = np.zeros((NM, 3), dtype=np.int32, order="F")
+        self.ni_tot = np.zeros(1, dtype=np.int32)
+        # fields (maind.f:38-70)
+        flds = grd6_setup(self.coords, cfg.b0, cfg.nu)
+        for k, v in flds.items():
+            setattr(self, k, v)
+        self.input_p = np.zeros(3)
+        ctx = C.c_void_p()
+        abi.check(self.lib, None, self.lib.swap_init(C.byref(ctx), C.byref(self.dims), C.byref(self.params),
+                                                       C.byref(self._coords_c)))
+        self.ctx = ctx
+        self._check(self.lib.swap_bind_particles(ctx, abi.dptr(self.xp), abi.dptr(self.vp), abi.dptr(self.vp1),
+                                                 abi.dptr(self.mrat), abi.dptr(self.beta_p), abi.iptr(self.ijkp),
+                                                 abi.iptr(self.ni_tot)))
+        self._check(self.lib.swap_bind_fields(ctx, *[abi.dptr(getattr(self, n)) for n in (
+            "b0", "b1", "b12", "b1p2", "bt", "btc", "np", "up", "aj", "E", "nu")]))
+        for a in (self.Ep, self.vplus, self.vminus, self.input_p):
+            self._check(self.lib.swap_bind_array(ctx, a.ctypes.data_as(C.c_void_p), a.nbytes))
+
+    # ---- plumbing ----
+    def _pinned(self, shape):
+        """A zeroed float64 Fortran-ordered array in page-locked host memory."""
+        import torch
+
+        t = torch.zeros(int(np.prod(shape)), dtype=torch.float64, pin_memory=True)
+        self._pins.append(t)
+        return np.ndarray(shape, dtype=np.float64, buffer=t.numpy(), order="F")
+
+    def _check(self, code):
+        abi.check(self.lib, self.ctx if hasattr(self, "ctx") else None, code)
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.swap_finalize(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def load_maxwellian(self, vth=None, u=None, ppc=None, seed=None, stream=0, mrat=1.0, beta_p=1.0, first=0):
+        """Stratified Maxwellian load on the host (replaces part_init.f:146-232)."""
+        cfg = self.cfg
+        ux, uy, uz = cfg.u if u is None else u
+        spec = abi.LoadSpec(cfg.seed if seed is None else seed, stream, cfg.ppc if ppc is None else ppc,
+                            cfg.vth if vth is None else vth, ux, uy, uz, mrat, beta_p)
+        cnt = C.c_int64()
+        abi.check(self.lib, None, self.lib.swap_load_maxwellian_host(
+            C.byref(self.dims), C.byref(self._coords_c), C.byref(spec), abi.dptr(self.xp), abi.dptr(self.vp),
+            abi.dptr(self.vp1), abi.dptr(self.mrat), abi.dptr(self.beta_p), first, C.byref(cnt)))
+        self.ni_tot[0] = first + cnt.value
+        self.mark_host_dirty()
+        return cnt.value
+
+    def sync_to_host(self, arr=None):
+        self._check(self.lib.swap_sync_to_host(self.ctx, None if arr is None else arr.ctypes.data_as(C.c_void_p)))
+
+    def sync_to_device(self, arr=None):
+        self._check(self.lib.swap_sync_to_device(self.ctx, None if arr is None else arr.ctypes.data_as(C.c_void_p)))
+
+    def mark_host_dirty(self, arr=None):
+        self._check(self.lib.swap_mark_host_dirty(self.ctx, None if arr is None else arr.ctypes.data_as(C.c_void_p)))
+
+    # ---- gutsp.f ----
+    def get_interp_weights(self, xp):
+        self._check(self.lib.swap_get_interp_weights(self.ctx, abi.dptr(xp)))
+
+    def update_np(self, np_):
+        self._check(self.lib.swap_update_np(self.ctx, abi.dptr(np_)))
+
+    def update_up(self, vp, np_, up):
+        self._check(self.lib.swap_update_up(self.ctx, abi.dptr(vp), abi.dptr(np_), abi.dptr(up)))
+
+    def extrapol_up(self, up, vp, vp1, np_):
+        self._check(self.lib.swap_extrapol_up(self.ctx, abi.dptr(up), abi.dptr(vp), abi.dptr(vp1), abi.dptr(np_)))
+
+    def get_Ep(self, Ep, aj, np_, up, btc, nu):
+        self._check(self.lib.swap_get_Ep(self.ctx, *map(abi.dptr, (Ep, aj, np_, up, btc, nu))))
+
+    def get_vplus_vminus(self, Ep, btc, vp, vplus, vminus):
+        self._check(self.lib.swap_get_vplus_vminus(self.ctx, *map(abi.dptr, (Ep, btc, vp, vplus, vminus))))
+
+    def improve_up(self, vp1, vplus, vminus, up, np_):
+        self._check(self.lib.swap_improve_up(self.ctx, *map(abi.dptr, (vp1, vplus, vminus, up, np_))))
+
+    def get_vp_final(self, Ep, vp, vp1, vplus):
+        self._check(self.lib.swap_get_vp_final(self.ctx, *map(abi.dptr, (Ep, vp, vp1, vplus))))
+
+    def move_ion_half(self, xp, vp, vp1, input_p):
+        self._check(self.lib.swap_move_ion_half(self.ctx, *map(abi.dptr, (xp, vp, vp1, input_p))))
+
+    # ---- gutsf.f / grid_interp.f / boundary.f ----
+    def curlB(self, bt, np_, aj):
+        self._check(self.lib.swap_curlB(self.ctx, *map(abi.dptr, (bt, np_, aj))))
+
+    def edge_to_center(self, bt, btc):
+        self._check(self.lib.swap_edge_to_center(self.ctx, abi.dptr(bt), abi.dptr(btc)))
+
+    def face_to_center(self, v, vc):
+        self._check(self.lib.swap_face_to_center(self.ctx, abi.dptr(v), abi.dptr(vc)))
+
+    def get_E(self, E, b0, bt, aj, up, np_, nu):
+        self._check(self.lib.swap_get_E(self.ctx, *map(abi.dptr, (E, b0, bt, aj, up, np_, nu))))
+
+    def predict_B(self, b0, b1, b12, b1p2, bt, E, aj, up, np_, nu, dtsub):
+        self._check(self.lib.swap_predict_B(self.ctx, *map(abi.dptr, (b0, b1, b12, b1p2, bt, E, aj, up, np_, nu)),
+                                            float(dtsub)))
+
+    def correct_B(self, b0, b1, b1p2, E, aj, up, np_, nu, dtsub):
+        self._check(self.lib.swap_correct_B(self.ctx, *map(abi.dptr, (b0, b1, b1p2, E, aj, up, np_, nu)),
+                                            float(dtsub)))
+
+    def f_update_tlev(self, b1, b12, b1p2, bt, b0):
+        self._check(self.lib.swap_f_update_tlev(self.ctx, *map(abi.dptr, (b1, b12, b1p2, bt, b0))))
+
+    def check_time_step(self, bt, np_, dtsub, ntf):
+        d = C.c_double(dtsub)
+        n = C.c_double(ntf)
+        self._check(self.lib.swap_check_time_step(self.ctx, abi.dptr(bt), abi.dptr(np_), C.byref(d), C.byref(n)))
+        return d.value, n.value
+
+    def periodic(self, b):
+        self._check(self.lib.swap_periodic(self.ctx, abi.dptr(b)))
+
+    # ---- fused step ----
+    def ion_step(self):
+        self._check(self.lib.swap_ion_step(self.ctx))
+
+    def run(self, nsteps: int):
+        self._check(self.lib.swap_run(self.ctx, int(nsteps)))
+
+    def energy(self):
+        out = np.zeros(4)
+        self._check(self.lib.swap_energy(self.ctx, abi.dptr(out)))
+        return out
+
+    def max_abs_divB(self, b):
+        out = C.c_double()
+        self._check(self.lib.swap_max_abs_divB(self.ctx, abi.dptr(b), C.byref(out)))
+        return out.value
+
+    def check_finite(self):
+        self._check(self.lib.swap_check_finite(self.ctx))
