@@ -271,6 +271,12 @@ __global__ void k_weights(Geo g, PartDev p, long long N, int* err) {
   }
 }
 
+// A cell index triple is usable for node addressing only inside
+// [1,n-1] on every axis; anything else is reported and skipped.
+__device__ __forceinline__ bool cell_ok(const Geo& g, int i, int j, int k) {
+  return i >= 1 && i <= g.nx - 1 && j >= 1 && j <= g.ny - 1 && k >= 1 && k <= g.nz - 1;
+}
+
 // The eight corners in the reference's weight order (gutsp.f:1484-1491).
 __device__ __forceinline__ void corners(const Geo& g, int i, int j, int k, long long nd[8]) {
   const long long o = nidx(g, i, j, k), sy = g.nx, sz = (long long)g.nx * g.ny;
@@ -298,9 +304,13 @@ __device__ __forceinline__ void corner_targets(const Geo& g, int i, int j, int k
 }
 
 // update_np deposit (gutsp.f:1461-1493) into the folded node.
-__global__ void k_deposit_np(Geo g, PartDev p, long long N, double beta, double* __restrict__ np) {
+__global__ void k_deposit_np(Geo g, PartDev p, long long N, double beta, double* __restrict__ np, int* err) {
   GRID_STRIDE(l, N) {
     const int i = p.ijk[l], j = p.ijk[l + p.NM], k = p.ijk[l + 2 * p.NM];
+    if (!cell_ok(g, i, j, k)) {
+      set_err(err, KERR_DOMAIN);
+      continue;
+    }
     const double volb = 1.0 / (g.dxg[i] * g.dyg[j] * g.dzg[k] * beta * p.beta_p[l]);
     long long tg[8];
     corner_targets(g, i, j, k, tg);
@@ -312,7 +322,8 @@ __global__ void k_deposit_np(Geo g, PartDev p, long long N, double beta, double*
 // update_up deposit (gutsp.f:1676-1800) without the per-node 1/np factor,
 // which ct_from_sums applies once per node: sum v*w/volb.
 __global__ void k_deposit_u(Geo g, PartDev p, long long N, double beta, int mode, const double* __restrict__ va,
-                            const double* __restrict__ vb, double* __restrict__ out_v1, double* __restrict__ S) {
+                            const double* __restrict__ vb, double* __restrict__ out_v1, double* __restrict__ S,
+                            int* err) {
   const long long C = g.C;
   GRID_STRIDE(l, N) {
     double v[3];
@@ -326,6 +337,10 @@ __global__ void k_deposit_u(Geo g, PartDev p, long long N, double beta, int mode
       }
     }
     const int i = p.ijk[l], j = p.ijk[l + p.NM], k = p.ijk[l + 2 * p.NM];
+    if (!cell_ok(g, i, j, k)) {
+      set_err(err, KERR_DOMAIN);
+      continue;
+    }
     const double volb =
         (g.qx[i + 1] - g.qx[i]) * (g.qy[j + 1] - g.qy[j]) * (g.qz[k + 1] - g.qz[k]) * beta * p.beta_p[l];
     const double ivolb = 1.0 / volb;
@@ -374,10 +389,14 @@ __device__ __forceinline__ double gather8(const double* __restrict__ f, const lo
 // get_Ep particle loop (gutsp.f:189-273).
 __global__ void k_get_Ep(Geo g, PartDev p, long long N, const double* __restrict__ ajc,
                          const double* __restrict__ upc, const double* __restrict__ btc,
-                         const double* __restrict__ gpc, double* __restrict__ Ep) {
+                         const double* __restrict__ gpc, double* __restrict__ Ep, int* err) {
   const long long C = g.C;
   GRID_STRIDE(l, N) {
     const int i = p.ijk[l], j = p.ijk[l + p.NM], k = p.ijk[l + 2 * p.NM];
+    if (!cell_ok(g, i, j, k)) {
+      set_err(err, KERR_DOMAIN);
+      continue;
+    }
     long long nd[8];
     corners(g, i, j, k, nd);
     double aa[3], bb[3];
@@ -403,7 +422,7 @@ __global__ void k_get_Ep(Geo g, PartDev p, long long N, const double* __restrict
 // get_vplus_vminus (gutsp.f:302-399).
 __global__ void k_vplus_vminus(Geo g, PartDev p, long long N, double dt, const double* __restrict__ Ep,
                                const double* __restrict__ btc, const double* __restrict__ vp,
-                               double* __restrict__ vplus, double* __restrict__ vminus) {
+                               double* __restrict__ vplus, double* __restrict__ vminus, int* err) {
   const long long C = g.C, NM = p.NM;
   GRID_STRIDE(l, N) {
     double vm[3];
@@ -412,6 +431,10 @@ __global__ void k_vplus_vminus(Geo g, PartDev p, long long N, double dt, const d
       vminus[l + m * NM] = vm[m];
     }
     const int i = p.ijk[l], j = p.ijk[l + NM], k = p.ijk[l + 2 * NM];
+    if (!cell_ok(g, i, j, k)) {
+      set_err(err, KERR_DOMAIN);
+      continue;
+    }
     long long nd[8];
     corners(g, i, j, k, nd);
     double b3[3];
@@ -606,27 +629,29 @@ cudaError_t interp_weights(const Geo& g, const PartDev& p, long long N, int* err
   if (N <= 0) return cudaSuccess;
   LAUNCH(k_weights, N, g, p, N, err);
 }
-cudaError_t deposit_np(const Geo& g, const PartDev& p, long long N, double beta, double* np, cudaStream_t st) {
+cudaError_t deposit_np(const Geo& g, const PartDev& p, long long N, double beta, double* np, int* err,
+                       cudaStream_t st) {
   if (N <= 0) return cudaSuccess;
-  LAUNCH(k_deposit_np, N, g, p, N, beta, np);
+  LAUNCH(k_deposit_np, N, g, p, N, beta, np, err);
 }
 cudaError_t deposit_u(const Geo& g, const PartDev& p, long long N, double beta, int mode, const double* va,
-                      const double* vb, double* out_v1, double* S, cudaStream_t st) {
+                      const double* vb, double* out_v1, double* S, int* err, cudaStream_t st) {
   if (N <= 0) return cudaSuccess;
-  LAUNCH(k_deposit_u, N, g, p, N, beta, mode, va, vb, out_v1, S);
+  LAUNCH(k_deposit_u, N, g, p, N, beta, mode, va, vb, out_v1, S, err);
 }
 cudaError_t ct_from_sums(const Geo& g, const double* S, const double* np, double* ct, cudaStream_t st) {
   LAUNCH(k_ct_from_sums, n_interior(g), g, S, np, ct);
 }
 cudaError_t get_Ep(const Geo& g, const PartDev& p, long long N, const double* ajc, const double* upc,
-                   const double* btc, const double* gpc, double* Ep, cudaStream_t st) {
+                   const double* btc, const double* gpc, double* Ep, int* err, cudaStream_t st) {
   if (N <= 0) return cudaSuccess;
-  LAUNCH(k_get_Ep, N, g, p, N, ajc, upc, btc, gpc, Ep);
+  LAUNCH(k_get_Ep, N, g, p, N, ajc, upc, btc, gpc, Ep, err);
 }
 cudaError_t vplus_vminus(const Geo& g, const PartDev& p, long long N, double dt, const double* Ep,
-                         const double* btc, const double* vp, double* vplus, double* vminus, cudaStream_t st) {
+                         const double* btc, const double* vp, double* vplus, double* vminus, int* err,
+                         cudaStream_t st) {
   if (N <= 0) return cudaSuccess;
-  LAUNCH(k_vplus_vminus, N, g, p, N, dt, Ep, btc, vp, vplus, vminus);
+  LAUNCH(k_vplus_vminus, N, g, p, N, dt, Ep, btc, vp, vplus, vminus, err);
 }
 cudaError_t vp_final(const PartDev& p, long long N, double dt, const double* Ep, double* vp, double* vp1,
                      const double* vplus, cudaStream_t st) {

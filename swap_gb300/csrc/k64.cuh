@@ -39,15 +39,17 @@ cudaError_t grad_pe_face_int(const Geo& g, const double* np, double grad_pe, dou
 
 // gutsp.f particle operators
 cudaError_t interp_weights(const Geo& g, const PartDev& p, long long N, int* err, cudaStream_t st);
-cudaError_t deposit_np(const Geo& g, const PartDev& p, long long N, double beta, double* np, cudaStream_t st);
+cudaError_t deposit_np(const Geo& g, const PartDev& p, long long N, double beta, double* np, int* err,
+                       cudaStream_t st);
 // mode: 0 = v, 1 = 1.5 v - 0.5 v1 (extrapol_up), 2 = 0.5 (a + b) (improve_up, also stores into out_v1)
 cudaError_t deposit_u(const Geo& g, const PartDev& p, long long N, double beta, int mode, const double* va,
-                      const double* vb, double* out_v1, double* S, cudaStream_t st);
+                      const double* vb, double* out_v1, double* S, int* err, cudaStream_t st);
 cudaError_t ct_from_sums(const Geo& g, const double* S, const double* np, double* ct, cudaStream_t st);
 cudaError_t get_Ep(const Geo& g, const PartDev& p, long long N, const double* ajc, const double* upc,
-                   const double* btc, const double* gpc, double* Ep, cudaStream_t st);
+                   const double* btc, const double* gpc, double* Ep, int* err, cudaStream_t st);
 cudaError_t vplus_vminus(const Geo& g, const PartDev& p, long long N, double dt, const double* Ep,
-                         const double* btc, const double* vp, double* vplus, double* vminus, cudaStream_t st);
+                         const double* btc, const double* vp, double* vplus, double* vminus, int* err,
+                         cudaStream_t st);
 cudaError_t vp_final(const PartDev& p, long long N, double dt, const double* Ep, double* vp, double* vp1,
                      const double* vplus, cudaStream_t st);
 cudaError_t move_half(const Geo& g, const PartDev& p, long long N, double dt, double* xp, const double* vp,

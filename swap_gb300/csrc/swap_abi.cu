@@ -295,11 +295,15 @@ int get_interp_weights(swap_ctx* c, const double* xp) {
   p.xp = const_cast<double*>(xp);
   KL("interp_weights", interp_weights(c->g, p, c->ntot(), c->d_err, c->st));
   c->weights_valid = true;
+  c->weights_n = c->ntot();
   return 0;
 }
 
+// The device ijk/wght cover the particles get_interp_weights saw; a larger
+// Ni_tot since then would address cells never computed.
 int need_weights(swap_ctx* c) {
   if (!c->weights_valid) return c->fail(SWAP_EINVAL, "get_interp_weights has not been called");
+  if (c->ntot() > c->weights_n) return c->fail(SWAP_EINVAL, "Ni_tot grew since get_interp_weights");
   return 0;
 }
 
@@ -307,7 +311,7 @@ int need_weights(swap_ctx* c) {
 int update_np(swap_ctx* c, double* np) {
   TRY(need_weights(c));
   KL("cudaMemsetAsync", cudaMemsetAsync(np, 0, (std::size_t)c->g.C * sizeof(double), c->st));
-  KL("deposit_np", deposit_np(c->g, c->part_view(), c->ntot(), c->prm.beta, np, c->st));
+  KL("deposit_np", deposit_np(c->g, c->part_view(), c->ntot(), c->prm.beta, np, c->d_err, c->st));
   KL("periodic", periodic1(c->g, np, c->st));
   return 0;
 }
@@ -319,7 +323,7 @@ int update_up_mode(swap_ctx* c, int mode, const double* va, const double* vb, do
   TRY(need_weights(c));
   const std::size_t b3 = 3 * (std::size_t)c->g.C * sizeof(double);
   KL("cudaMemsetAsync", cudaMemsetAsync(c->s_S, 0, b3, c->st));
-  KL("deposit_u", deposit_u(c->g, c->part_view(), c->ntot(), c->prm.beta, mode, va, vb, out_v1, c->s_S, c->st));
+  KL("deposit_u", deposit_u(c->g, c->part_view(), c->ntot(), c->prm.beta, mode, va, vb, out_v1, c->s_S, c->d_err, c->st));
   KL("ct_from_sums", ct_from_sums(c->g, c->s_S, np, c->s_ct, c->st));
   KL("periodic", periodic3(c->g, c->s_ct, c->st));
   KL("face_avg_int", face_avg_int(c->g, c->s_ct, up, c->st));
@@ -338,13 +342,13 @@ int get_Ep(swap_ctx* c, double* Ep, double* aj, const double* np, double* up, co
     TRY(face_to_center(c, c->s_gf, c->s_gpc));
     gpc = c->s_gpc;
   }
-  KL("get_Ep", swapk::get_Ep(c->g, c->part_view(), c->ntot(), c->s_ajc, c->s_upc, btc, gpc, Ep, c->st));
+  KL("get_Ep", swapk::get_Ep(c->g, c->part_view(), c->ntot(), c->s_ajc, c->s_upc, btc, gpc, Ep, c->d_err, c->st));
   return 0;
 }
 
 int vpm(swap_ctx* c, const double* Ep, const double* btc, const double* vp, double* vplus, double* vminus) {
   TRY(need_weights(c));
-  KL("vplus_vminus", vplus_vminus(c->g, c->part_view(), c->ntot(), c->prm.dt, Ep, btc, vp, vplus, vminus, c->st));
+  KL("vplus_vminus", vplus_vminus(c->g, c->part_view(), c->ntot(), c->prm.dt, Ep, btc, vp, vplus, vminus, c->d_err, c->st));
   return 0;
 }
 

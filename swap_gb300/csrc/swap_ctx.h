@@ -57,6 +57,7 @@ struct swap_ctx {
   int32_t* d_ijk = nullptr;   // /ion_info/ ijkp
   double* d_wght = nullptr;   // /weights/ wght
   bool weights_valid = false;
+  long long weights_n = 0;
 
   // grid scratch: /dummy/ a, c, ct and subroutine locals
   double *s_a = nullptr, *s_aa = nullptr, *s_c = nullptr, *s_ct = nullptr, *s_btcl = nullptr, *s_btc2 = nullptr;

@@ -1,0 +1,290 @@
+! swap_gpu_iface.f90 -- ISO_C_BINDING face of libswap_gpu.so for the
+! SWAP Fortran driver.  Two modules:
+!
+!   swap_gpu_iface   bind(C) interfaces to include/swap_gpu.h and the one
+!                    context per MPI rank (swap_gpu_ctx);
+!   swap_gpu_calls   wrappers with the reference's subroutine names and
+!                    argument lists (gutsp.f, gutsf.f, grid_interp.f,
+!                    boundary.f) that forward to the C entries and stop on a
+!                    nonzero status, as inputs.f:199 stops on a bad input.
+!
+! Build with the reference compiled at -real-size 64 (REAL = double), e.g.
+!   mpif90 -i4 -real-size 64 -c swap_gpu_iface.f90
+! and link -L<repo>/swap_gb300/_lib -lswap_gpu.  No Fortran compiler exists
+! in the image this file was written in, so it has not been compiled here;
+! the C entries it binds are exercised through ctypes by the test suite.
+module swap_gpu_iface
+  use iso_c_binding
+  implicit none
+
+  type, bind(C) :: swap_dims_t
+     integer(c_int32_t) :: nx, ny, nz, reserved
+     integer(c_int64_t) :: ni_max
+  end type swap_dims_t
+
+  type, bind(C) :: swap_params_t
+     real(c_double) :: dt, alpha, beta, dx, dy, grad_pe
+     integer(c_int32_t) :: ntsub, flags
+  end type swap_params_t
+
+  type, bind(C) :: swap_coords_t
+     type(c_ptr) :: qx, qy, qz, dx_grid, dy_grid, dz_grid
+     type(c_ptr) :: dx_cell, dy_cell, dz_cell, xrat, yrat, zrat
+  end type swap_coords_t
+
+  type(c_ptr), save :: swap_gpu_ctx = c_null_ptr
+
+  interface
+     integer(c_int) function swap_init(ctx, dims, params, coords) bind(C, name="swap_init")
+       import :: c_int, c_ptr, swap_dims_t, swap_params_t, swap_coords_t
+       type(c_ptr) :: ctx
+       type(swap_dims_t) :: dims
+       type(swap_params_t) :: params
+       type(swap_coords_t) :: coords
+     end function swap_init
+     integer(c_int) function swap_finalize(ctx) bind(C, name="swap_finalize")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function swap_finalize
+     type(c_ptr) function swap_last_error(ctx) bind(C, name="swap_last_error")
+       import :: c_ptr
+       type(c_ptr), value :: ctx
+     end function swap_last_error
+     integer(c_int) function swap_bind_particles(ctx, xp, vp, vp1, mrat, beta_p, ijkp, ni_tot) &
+          bind(C, name="swap_bind_particles")
+       import :: c_int, c_ptr, c_double, c_int32_t
+       type(c_ptr), value :: ctx
+       real(c_double) :: xp(*), vp(*), vp1(*), mrat(*), beta_p(*)
+       integer(c_int32_t) :: ijkp(*), ni_tot
+     end function swap_bind_particles
+     integer(c_int) function swap_bind_fields(ctx, b0, b1, b12, b1p2, bt, btc, np, up, aj, E, nu) &
+          bind(C, name="swap_bind_fields")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: b0(*), b1(*), b12(*), b1p2(*), bt(*), btc(*), np(*), up(*), aj(*), E(*), nu(*)
+     end function swap_bind_fields
+     integer(c_int) function swap_bind_array(ctx, a, nbytes) bind(C, name="swap_bind_array")
+       import :: c_int, c_ptr, c_int64_t
+       type(c_ptr), value :: ctx, a
+       integer(c_int64_t), value :: nbytes
+     end function swap_bind_array
+     integer(c_int) function swap_sync_to_host(ctx, a) bind(C, name="swap_sync_to_host")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx, a
+     end function swap_sync_to_host
+     integer(c_int) function swap_mark_host_dirty(ctx, a) bind(C, name="swap_mark_host_dirty")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx, a
+     end function swap_mark_host_dirty
+     ! --- gutsp.f ---
+     integer(c_int) function c_get_interp_weights(ctx, xp) bind(C, name="swap_get_interp_weights")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: xp(*)
+     end function c_get_interp_weights
+     integer(c_int) function c_update_np(ctx, np) bind(C, name="swap_update_np")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: np(*)
+     end function c_update_np
+     integer(c_int) function c_update_up(ctx, vp, np, up) bind(C, name="swap_update_up")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: vp(*), np(*), up(*)
+     end function c_update_up
+     integer(c_int) function c_extrapol_up(ctx, up, vp, vp1, np) bind(C, name="swap_extrapol_up")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: up(*), vp(*), vp1(*), np(*)
+     end function c_extrapol_up
+     integer(c_int) function c_get_Ep(ctx, Ep, aj, np, up, btc, nu) bind(C, name="swap_get_Ep")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: Ep(*), aj(*), np(*), up(*), btc(*), nu(*)
+     end function c_get_Ep
+     integer(c_int) function c_get_vplus_vminus(ctx, Ep, btc, vp, vplus, vminus) bind(C, name="swap_get_vplus_vminus")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: Ep(*), btc(*), vp(*), vplus(*), vminus(*)
+     end function c_get_vplus_vminus
+     integer(c_int) function c_improve_up(ctx, vp1, vplus, vminus, up, np) bind(C, name="swap_improve_up")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: vp1(*), vplus(*), vminus(*), up(*), np(*)
+     end function c_improve_up
+     integer(c_int) function c_get_vp_final(ctx, Ep, vp, vp1, vplus) bind(C, name="swap_get_vp_final")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: Ep(*), vp(*), vp1(*), vplus(*)
+     end function c_get_vp_final
+     integer(c_int) function c_move_ion_half(ctx, xp, vp, vp1, input_p) bind(C, name="swap_move_ion_half")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: xp(*), vp(*), vp1(*), input_p(*)
+     end function c_move_ion_half
+     ! --- gutsf.f / grid_interp.f / boundary.f ---
+     integer(c_int) function c_curlB(ctx, bt, np, aj) bind(C, name="swap_curlB")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: bt(*), np(*), aj(*)
+     end function c_curlB
+     integer(c_int) function c_edge_to_center(ctx, bt, btc) bind(C, name="swap_edge_to_center")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: bt(*), btc(*)
+     end function c_edge_to_center
+     integer(c_int) function c_face_to_center(ctx, v, vc) bind(C, name="swap_face_to_center")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: v(*), vc(*)
+     end function c_face_to_center
+     integer(c_int) function c_get_E(ctx, E, b0, bt, aj, up, np, nu) bind(C, name="swap_get_E")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: E(*), b0(*), bt(*), aj(*), up(*), np(*), nu(*)
+     end function c_get_E
+     integer(c_int) function c_predict_B(ctx, b0, b1, b12, b1p2, bt, E, aj, up, np, nu, dtsub) &
+          bind(C, name="swap_predict_B")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: b0(*), b1(*), b12(*), b1p2(*), bt(*), E(*), aj(*), up(*), np(*), nu(*)
+       real(c_double), value :: dtsub
+     end function c_predict_B
+     integer(c_int) function c_correct_B(ctx, b0, b1, b1p2, E, aj, up, np, nu, dtsub) bind(C, name="swap_correct_B")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: b0(*), b1(*), b1p2(*), E(*), aj(*), up(*), np(*), nu(*)
+       real(c_double), value :: dtsub
+     end function c_correct_B
+     integer(c_int) function c_f_update_tlev(ctx, b1, b12, b1p2, bt, b0) bind(C, name="swap_f_update_tlev")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: b1(*), b12(*), b1p2(*), bt(*), b0(*)
+     end function c_f_update_tlev
+     integer(c_int) function c_check_time_step(ctx, bt, np, dtsub, ntf) bind(C, name="swap_check_time_step")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: bt(*), np(*), dtsub, ntf
+     end function c_check_time_step
+     integer(c_int) function c_periodic(ctx, b) bind(C, name="swap_periodic")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: b(*)
+     end function c_periodic
+     integer(c_int) function c_periodic_scalar(ctx, b) bind(C, name="swap_periodic_scalar")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: b(*)
+     end function c_periodic_scalar
+  end interface
+
+contains
+
+  ! Stop with the library's message on a nonzero status (the reference's
+  ! own error style, inputs.f:199).
+  subroutine swap_check(ierr, where)
+    integer(c_int), intent(in) :: ierr
+    character(*), intent(in) :: where
+    character(kind=c_char), pointer :: msg(:)
+    integer :: n
+    if (ierr == 0) return
+    call c_f_pointer(swap_last_error(swap_gpu_ctx), msg, [256])
+    n = 0
+    do while (n < 256)
+       if (msg(n + 1) == c_null_char) exit
+       n = n + 1
+    end do
+    write(*,*) 'swap_gpu error in ', where, ': ', ierr, ' ', msg(1:n)
+    stop
+  end subroutine swap_check
+
+end module swap_gpu_iface
+
+
+! Wrappers with the reference names.  The makefile links this module's
+! object in place of the bodies of the same subroutines in gutsp.f,
+! gutsf.f, grid_interp.f and boundary.f (INTEGRATION.md); maind.f is
+! unchanged.  Implicit state (dt, dtsub, ijkp, wght) is held by the context.
+module swap_gpu_calls
+  use iso_c_binding
+  use swap_gpu_iface
+  use global, only: dtsub, ntf   ! /timestep/ (global.f:76-77)
+  implicit none
+contains
+  subroutine get_interp_weights(xp)
+    real(c_double) :: xp(*)
+    call swap_check(c_get_interp_weights(swap_gpu_ctx, xp), 'get_interp_weights')
+  end subroutine get_interp_weights
+  subroutine update_np(np)
+    real(c_double) :: np(*)
+    call swap_check(c_update_np(swap_gpu_ctx, np), 'update_np')
+  end subroutine update_np
+  subroutine update_up(vp, np, up)
+    real(c_double) :: vp(*), np(*), up(*)
+    call swap_check(c_update_up(swap_gpu_ctx, vp, np, up), 'update_up')
+  end subroutine update_up
+  subroutine extrapol_up(up, vp, vp1, np)
+    real(c_double) :: up(*), vp(*), vp1(*), np(*)
+    call swap_check(c_extrapol_up(swap_gpu_ctx, up, vp, vp1, np), 'extrapol_up')
+  end subroutine extrapol_up
+  subroutine get_Ep(Ep, aj, np, up, btc, nu)
+    real(c_double) :: Ep(*), aj(*), np(*), up(*), btc(*), nu(*)
+    call swap_check(c_get_Ep(swap_gpu_ctx, Ep, aj, np, up, btc, nu), 'get_Ep')
+  end subroutine get_Ep
+  subroutine get_vplus_vminus(Ep, btc, vp, vplus, vminus)
+    real(c_double) :: Ep(*), btc(*), vp(*), vplus(*), vminus(*)
+    call swap_check(c_get_vplus_vminus(swap_gpu_ctx, Ep, btc, vp, vplus, vminus), 'get_vplus_vminus')
+  end subroutine get_vplus_vminus
+  subroutine improve_up(vp1, vplus, vminus, up, np)
+    real(c_double) :: vp1(*), vplus(*), vminus(*), up(*), np(*)
+    call swap_check(c_improve_up(swap_gpu_ctx, vp1, vplus, vminus, up, np), 'improve_up')
+  end subroutine improve_up
+  subroutine get_vp_final(Ep, vp, vp1, vplus)
+    real(c_double) :: Ep(*), vp(*), vp1(*), vplus(*)
+    call swap_check(c_get_vp_final(swap_gpu_ctx, Ep, vp, vp1, vplus), 'get_vp_final')
+  end subroutine get_vp_final
+  subroutine move_ion_half(xp, vp, vp1, input_p)
+    real(c_double) :: xp(*), vp(*), vp1(*), input_p(*)
+    call swap_check(c_move_ion_half(swap_gpu_ctx, xp, vp, vp1, input_p), 'move_ion_half')
+  end subroutine move_ion_half
+  subroutine curlB(bt, np, aj)
+    real(c_double) :: bt(*), np(*), aj(*)
+    call swap_check(c_curlB(swap_gpu_ctx, bt, np, aj), 'curlB')
+  end subroutine curlB
+  subroutine edge_to_center(bt, btc)
+    real(c_double) :: bt(*), btc(*)
+    call swap_check(c_edge_to_center(swap_gpu_ctx, bt, btc), 'edge_to_center')
+  end subroutine edge_to_center
+  subroutine face_to_center(v, vc)
+    real(c_double) :: v(*), vc(*)
+    call swap_check(c_face_to_center(swap_gpu_ctx, v, vc), 'face_to_center')
+  end subroutine face_to_center
+  subroutine get_E(E, b0, bt, aj, up, np, nu)
+    real(c_double) :: E(*), b0(*), bt(*), aj(*), up(*), np(*), nu(*)
+    call swap_check(c_get_E(swap_gpu_ctx, E, b0, bt, aj, up, np, nu), 'get_E')
+  end subroutine get_E
+  subroutine predict_B(b0, b1, b12, b1p2, bt, E, aj, up, np, nu)
+    real(c_double) :: b0(*), b1(*), b12(*), b1p2(*), bt(*), E(*), aj(*), up(*), np(*), nu(*)
+    call swap_check(c_predict_B(swap_gpu_ctx, b0, b1, b12, b1p2, bt, E, aj, up, np, nu, dtsub), 'predict_B')
+  end subroutine predict_B
+  subroutine correct_B(b0, b1, b1p2, E, aj, up, np, nu)
+    real(c_double) :: b0(*), b1(*), b1p2(*), E(*), aj(*), up(*), np(*), nu(*)
+    call swap_check(c_correct_B(swap_gpu_ctx, b0, b1, b1p2, E, aj, up, np, nu, dtsub), 'correct_B')
+  end subroutine correct_B
+  subroutine f_update_tlev(b1, b12, b1p2, bt, b0)
+    real(c_double) :: b1(*), b12(*), b1p2(*), bt(*), b0(*)
+    call swap_check(c_f_update_tlev(swap_gpu_ctx, b1, b12, b1p2, bt, b0), 'f_update_tlev')
+  end subroutine f_update_tlev
+  subroutine check_time_step(bt, np)
+    real(c_double) :: bt(*), np(*)
+    call swap_check(c_check_time_step(swap_gpu_ctx, bt, np, dtsub, ntf), 'check_time_step')
+  end subroutine check_time_step
+  subroutine periodic(b)
+    real(c_double) :: b(*)
+    call swap_check(c_periodic(swap_gpu_ctx, b), 'periodic')
+  end subroutine periodic
+  subroutine periodic_scalar(b)
+    real(c_double) :: b(*)
+    call swap_check(c_periodic_scalar(swap_gpu_ctx, b), 'periodic_scalar')
+  end subroutine periodic_scalar
+end module swap_gpu_calls
