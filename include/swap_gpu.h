@@ -164,6 +164,33 @@ int swap_load_maxwellian_host(const swap_dims* dims, const swap_coords* coords, 
                               double* xp, double* vp, double* vp1, double* mrat, double* beta_p, int64_t first,
                               int64_t* count);
 
+/* ---- allocation-free deposit (no counterpart in the reference) ---- */
+/* For callers that cannot call cudaMalloc: a host whose device memory is
+ * owned by another allocator, or a caller that cannot let cudaMalloc/cudaFree
+ * synchronize the device inside its step.  Such a caller cannot create a
+ * swap_ctx.  swap_update_up_noalloc computes the same moment as
+ * swap_get_interp_weights + swap_update_up (gutsp.f:1378-1435, 1649-1842)
+ * from the caller's DEVICE arrays xp, vp (ni_max,3), beta_p (ni_max), np
+ * (nx,ny,nz) into the caller's device array up (nx,ny,nz,3), on `stream`
+ * (a cudaStream_t; NULL = default stream), and returns after the stream
+ * finishes.  coords are host arrays, as for swap_init.
+ *   - It allocates nothing.  Its scratch is one file-scope device array of
+ *     SWAP_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds
+ *     until the process exits.
+ *   - The first call on a device resolves that array's address
+ *     (cudaGetSymbolAddress); make the first call before any stream capture.
+ *   - All calls share the array and each call clears the part it uses first;
+ *     calls that overlap on the GPU race, so serialize them.
+ *   - More than SWAP_NOALLOC_MAX_NODES nodes, or more than
+ *     SWAP_NOALLOC_MAX_AXIS nodes on an axis, returns SWAP_ECAPACITY.  A
+ *     particle outside the grid returns SWAP_EDOMAIN. */
+#define SWAP_NOALLOC_MAX_NODES (1 << 20)
+#define SWAP_NOALLOC_MAX_AXIS 4096
+#define SWAP_NOALLOC_SCRATCH_BYTES (8 * (3 * (SWAP_NOALLOC_MAX_AXIS + 1) + 3 * SWAP_NOALLOC_MAX_NODES))
+int swap_update_up_noalloc(const swap_dims* dims, const swap_params* params, const swap_coords* coords,
+                           const double* xp, const double* vp, const double* beta_p, int64_t ni_tot,
+                           const double* np, double* up, void* stream);
+
 /* ---- timing (CUDA events on the context's stream) ---- */
 int swap_timer_start(swap_ctx* ctx);
 int swap_timer_stop(swap_ctx* ctx, double* ms);

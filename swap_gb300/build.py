@@ -32,6 +32,7 @@ UNITS = [
     ("swap_abi.cu", []),
     ("swap_f32.cu", []),
     ("swap_prof.cu", []),
+    ("swap_noalloc.cu", ["--fmad=false"]),
     ("loader.cpp", ["-Xcompiler", "-fopenmp,-ffp-contract=off"]),
 ]
 
