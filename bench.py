@@ -29,7 +29,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-METRIC = "ion particle-steps/s on 1 GB300 (FP64 plain step)"
+METRIC = "ion particle-steps/s on 1 GB300"
 UNIT = "particle-steps/s"
 
 
@@ -122,6 +122,29 @@ KERNEL_BYTES_F64 = {
     "vplus_vminus": 12 + 64 + 8 + 24 + 24 + 48,  # + Ep, vp; write v+, v-
     "vp_final": 24 + 24 + 24 + 48,
     "move_half": 24 + 24 + 24,
+}
+
+
+# Algorithmic bytes per unit for the FP32 form (particles: cell 4 + offsets 12
+# + v 12 + vp1 12 + species 1 = 41 B of state).
+KERNEL_BYTES_F32 = {
+    "f32_P1": 41 + 16,           # read state; write cell + offsets
+    "f32_P2": 29,                # read cell, offsets, v, species
+    "f32_P3": 29 + 40,           # + write v, vp1, cell, offsets
+    "f32_sort_scatter": 41 + 4 + 41,
+    "f32_sort_prep": 4 + 4,
+}
+# per interior node (FP32 fields, FP64 B levels)
+NODE_BYTES_F32 = {
+    "f32_curlB": 12 + 4 + 12,
+    "f32_ct_pred": 36 + 12,
+    "f32_ct_corr": 36 + 12,
+    "f32_E": 28 + 12,
+    "f32_bupd": 12 + 48 + 36,
+    "f32_half": 24 + 12,
+    "f32_kit": 36 + 32,
+    "f32_node_sum": 16 * 2 + 16,
+    "f32_ct_up": 16 + 12,
 }
 
 
@@ -226,6 +249,14 @@ def run_ours(args):
     from swap_gb300.hybrid import Hybrid, config
 
     cfg = config(args.config)
+    if args.cells or args.ppc:
+        over = {}
+        if args.cells:
+            over["cells"] = tuple(args.cells)
+        if args.ppc:
+            over["ppc"] = args.ppc
+        over["name"] = f"{cfg.name} (resized to {over.get('cells', cfg.cells)} cells, {over.get('ppc', cfg.ppc)} ppc)"
+        cfg = config(args.config, **over)
     # Each rank runs its own replica of the workload: the particle-decomposed
     # exchange (an allreduce of the moments after each deposit) is not built.
     h = Hybrid(cfg, pinned=True)
@@ -235,8 +266,14 @@ def run_ours(args):
     N = int(h.ni_tot[0])
     h.sync_to_device()
 
+    f32 = args.precision == "f32"
+    if f32:
+        h.f32_begin()
+        run = h.f32_run
+    else:
+        run = h.run
     for _ in range(args.warmup):
-        h.run(1)
+        run(1)
     lib, ctx = h.lib, h.ctx
 
     # ---- timed region: K steps, device-resident, CUDA events on the library stream
@@ -249,7 +286,7 @@ def run_ours(args):
 
     ms = C.c_double()
     h._check(lib.swap_timer_start(ctx))
-    h.run(args.steps)
+    run(args.steps)
     h._check(lib.swap_timer_stop(ctx, C.byref(ms)))
     clk = clocks.stop()
     lib.swap_profile_enable(ctx, 0)
@@ -265,8 +302,11 @@ def run_ours(args):
     launches = int(sum(v[1] for v in kernels.values()))
     top = max(kernels.items(), key=lambda kv: kv[1][0])
     top_name, (top_ms, top_n) = top
-    units = N if top_name in KERNEL_BYTES_F64 else (cfg.nodes[0] - 2) * (cfg.nodes[1] - 2) * (cfg.nodes[2] - 2)
-    per_unit = KERNEL_BYTES_F64.get(top_name, 0)
+    part_bytes = KERNEL_BYTES_F32 if f32 else KERNEL_BYTES_F64
+    node_bytes = NODE_BYTES_F32 if f32 else {}
+    nodes_int = (cfg.nodes[0] - 2) * (cfg.nodes[1] - 2) * (cfg.nodes[2] - 2)
+    units = N if top_name in part_bytes else nodes_int
+    per_unit = part_bytes.get(top_name, node_bytes.get(top_name, 0))
     avg_s = top_ms / 1e3 / max(top_n, 1)
     achieved = per_unit * units / avg_s / 1e9 if per_unit else None
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
@@ -279,17 +319,24 @@ def run_ours(args):
     state_bytes_p = N * 8 * 11
     field_bytes = sum(getattr(h, a).nbytes for a in ("b0", "b1", "b12", "b1p2", "bt", "btc", "np", "up", "aj", "E",
                                                       "nu"))
+    if f32:
+        h.f32_end()
     h.sync_to_host()
     barrier(ws)
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     w0 = time.perf_counter()
     h.mark_host_dirty()
     h.sync_to_device()
-    for _ in range(args.steps):
-        h.run(1)
-        h.energy()
+    if f32:
+        h.f32_begin()
+        for _ in range(args.steps):
+            h.f32_run(1)
+            h.f32_energy()
+        h.f32_end()
+    else:
+        for _ in range(args.steps):
+            h.run(1)
+            h.energy()
     h.sync_to_host()
     torch.cuda.synchronize()
     e2e_s = barrier_max(time.perf_counter() - w0, ws)
@@ -299,17 +346,20 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic (seeded stratified Maxwellian load, normalized units)",
+        "dtype": "f32" if f32 else "f64", "data": "synthetic (seeded stratified Maxwellian load, normalized units)",
         "config": {"workload": cfg.name, "cells": list(cfg.cells), "ppc": cfg.ppc, "ions": N,
-                   "subcycles": cfg.ntsub, "precision_form": "FP64 drop-in",
-                   "l2": "inputs larger than L2 (particle state %.1f GB)" % (N * 72 / 1e9),
+                   "subcycles": cfg.ntsub,
+                   "precision_form": "FP32 form (int32 cell + FP32 offset, FP32 moments, FP64 B)" if f32
+                   else "FP64 drop-in",
+                   "l2": "inputs larger than L2 (particle state %.1f GB)" % (N * (41 if f32 else 72) / 1e9),
                    "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU"},
         "gpu_launches": launches,
         "clocks": clk,
         "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": None,
                      "peak_source": "measured" if peaks else "fallback",
-                     "note": "FP64 kernels on GB300 are bound by the FP64 pipe, not HBM"},
+                     "bytes_per_unit": per_unit, "units_per_launch": units,
+                     "note": None if f32 else "FP64 kernels on GB300 are bound by the FP64 pipe, not HBM"},
         "kernels_ms_per_step": {k: v[0] / args.steps for k, v in sorted(kernels.items(), key=lambda kv: -kv[1][0])},
         "e2e": {"value": N * args.steps * ws / e2e_s, "unit": UNIT,
                 "h2d_bytes_per_step": (state_bytes_p + field_bytes) / args.steps,
@@ -337,7 +387,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", type=int, default=1)
+    ap.add_argument("--precision", default="f32", choices=["f32", "f64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cells", type=int, nargs=3, default=None, help="override the workload's cells (profiling)")
+    ap.add_argument("--ppc", type=int, default=None, help="override particles per cell (profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

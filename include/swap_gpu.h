@@ -139,6 +139,22 @@ int swap_ion_step_post(swap_ctx* ctx);    /* maind.f:479     */
 int swap_ion_step(swap_ctx* ctx);         /* maind.f:385-479 */
 int swap_run(swap_ctx* ctx, int32_t nsteps);
 
+/* ---- the FP32 form of the fused step ----
+ * Particle positions as int32 cell + FP32 offset, FP32 velocities and
+ * moments, B accumulated in FP64 across subcycles.  Needs a uniform grid with
+ * 8..1024 physical cells per axis in multiples of 4, a uniform b0, at most 16
+ * (mrat, beta_p) species, and |v|*dt < dx per axis (SWAP_EMOVE otherwise).
+ * begin converts the bound FP64 state; end writes it back into the bound
+ * arrays' device mirrors, with the particles in cell-sorted order. */
+int swap_f32_begin(swap_ctx* ctx);
+int swap_f32_run(swap_ctx* ctx, int32_t nsteps);
+int swap_f32_end(swap_ctx* ctx);
+int swap_f32_energy(swap_ctx* ctx, double out[4]);
+/* Validation: move particles idx[q] of the current (sorted) order by one
+ * cell step per axis (dcell[q] = (dx+1) | (dy+1)<<10 | (dz+1)<<20) and run
+ * the stable incremental sort that follows each ion step. */
+int swap_f32_displace_resort(swap_ctx* ctx, int64_t n, const int64_t* idx, const int32_t* dcell);
+
 /* ---- diagnostics (FP64, device reductions) ---- */
 /* out[0] kinetic, out[1] |b1-b0|^2 field, out[2] |b1|^2 field, out[3] |E|^2,
  * in the normalized units of the oracle (part_init.f:14-139 sums the j=2

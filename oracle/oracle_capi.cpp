@@ -288,3 +288,18 @@ void copy_out(const std::vector<R>& v1based, int n, R* out) {
 
 ORACLE_API(double, oracle_)
 ORACLE_API(float, oracle32_)
+
+// Stable counting sort over arbitrary integer keys in [0, nkeys): perm[new] =
+// old, counts[key].  The definition the GPU's incremental sort must match.
+extern "C" int oracle_stable_counting_sort(const std::int64_t* keys, std::int64_t n, std::int64_t nkeys,
+                                           std::int64_t* perm, std::int64_t* counts) {
+  std::vector<std::int64_t> start((std::size_t)nkeys + 1, 0);
+  for (std::int64_t l = 0; l < n; ++l) {
+    if (keys[l] < 0 || keys[l] >= nkeys) return 1;
+    start[(std::size_t)keys[l] + 1]++;
+  }
+  for (std::int64_t k = 0; k < nkeys; ++k) counts[k] = start[(std::size_t)k + 1];
+  for (std::int64_t k = 0; k < nkeys; ++k) start[(std::size_t)k + 1] += start[(std::size_t)k];
+  for (std::int64_t l = 0; l < n; ++l) perm[start[(std::size_t)keys[l]]++] = l;
+  return 0;
+}

@@ -29,6 +29,8 @@
 #include <stdexcept>
 #include <vector>
 
+#include "../swap_gb300/csrc/philox.h"
+
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -1001,6 +1003,237 @@ void counting_sort_perm(const Mesh<R>& g, const std::int32_t* ijkp, std::int64_t
   for (std::size_t c = 0; c < ncell; ++c) start[c + 1] = start[c] + counts[c];
   perm.assign((std::size_t)ni_tot, 0);
   for (std::int64_t l = 0; l < ni_tot; ++l) perm[(std::size_t)start[(std::size_t)key[(std::size_t)l]]++] = l;
+}
+
+}  // namespace swo
+
+// ---------------------------------------------------------------------------
+// Particle sources and sinks (chem_rates.f, gutsp.f:12-46) and the
+// extensions D3-D5 (x inflow/outflow, cloud ionization, charge exchange).
+// The compiler's random_number (misc.f:24) is replaced by Philox4x32-10
+// draws keyed by (seed, stream) with counters (step, slot, draw block), so
+// the CPU and GPU paths consume identical uniforms.
+// ---------------------------------------------------------------------------
+namespace swo {
+
+struct Sources {
+  std::uint64_t seed;
+  double ndot, vsw, beta_pu, mrat_pu, delz_ref;    // Ionize_sw_mp
+  int x_open, inflow_ppc;                          // D3
+  double inflow_vth, inflow_ux, inflow_uy, inflow_uz;
+  double cloud_N0, cloud_r0, cloud_x, cloud_y, cloud_z, nu_ion, mrat_heavy, beta_heavy;  // D4
+  double cx_a, cx_b;                               // D5
+};
+
+enum : std::uint32_t { RNG_IONIZE = 1, RNG_INFLOW = 2, RNG_CLOUD = 3, RNG_CHEX = 4 };
+
+// Four uniforms in (0,1) for (stream, step, a, b).
+inline void draw4(const Sources& s, std::uint32_t stream, std::int64_t step, std::int64_t a, std::uint32_t b,
+                  double u[4]) {
+  swapk::u32x4 c;
+  c.v[0] = (std::uint32_t)step;
+  c.v[1] = (std::uint32_t)a;
+  c.v[2] = (std::uint32_t)((std::uint64_t)a >> 32);
+  c.v[3] = b;
+  const swapk::u32x4 r = swapk::philox4x32_10(c, (std::uint32_t)s.seed ^ (stream * 0x9E3779B9u),
+                                              (std::uint32_t)(s.seed >> 32));
+  for (int q = 0; q < 4; ++q) u[q] = swapk::u01_open(r.v[q]);
+}
+
+// Ionize_sw_mp (chem_rates.f:508-646): dNi = ndot*dt*beta*beta_pu*dx*dy*delz*nz
+// (:553), a Bernoulli trial when below one (:555-560), nint (:562); ring
+// ions v = (vsw + vsw cos th, vsw sin th, 0) placed uniformly in the box
+// (:570-577) with mrat, beta_pu (:606-608), appended after Ni_tot (:567,628).
+template <class R>
+std::int64_t ionize_sw_count(const State<R>& s, const Sources& src, std::int64_t step) {
+  const Mesh<R>& g = s.g;
+  double dNi = src.ndot * (double)s.dt * (double)s.beta * src.beta_pu * (double)g.dx * (double)g.dy * src.delz_ref *
+               (double)g.nz;
+  if (dNi < 1.0) {
+    double u[4];
+    draw4(src, RNG_IONIZE, step, -1, 0, u);
+    if (dNi > u[0]) dNi = 1.0;
+  }
+  return (std::int64_t)std::llround(dNi);  // nint
+}
+
+template <class R>
+std::int64_t ionize_sw(State<R>& s, const Sources& src, std::int64_t step, R* xp, R* vp, R* vp1, R* mrat, R* beta_p,
+                       std::int64_t ni_tot) {
+  const Mesh<R>& g = s.g;
+  const std::int64_t NM = s.ni_max, n = ionize_sw_count(s, src, step);
+  if (ni_tot + n > NM) throw std::runtime_error("Ionize_sw_mp: Ni_max exceeded");
+  const double twopi = 2.0 * 3.14159265358979323846;
+  for (std::int64_t q = 0; q < n; ++q) {
+    double u[4];
+    draw4(src, RNG_IONIZE, step, q, 1, u);
+    const std::int64_t l = ni_tot + q;
+    const R th = (R)(u[0] * twopi);
+    vp[l] = (R)src.vsw + (R)src.vsw * std::cos(th);
+    vp[l + NM] = (R)src.vsw * std::sin(th);
+    vp[l + 2 * NM] = R(0.0);
+    xp[l] = g.qx[1] + (R(1.0) - (R)u[1]) * (g.qx[g.nx - 1] - g.qx[1]);
+    xp[l + NM] = g.qy[1] + (R(1.0) - (R)u[2]) * (g.qy[g.ny - 1] - g.qy[1]);
+    xp[l + 2 * NM] = g.qz[1] + (R(1.0) - (R)u[3]) * (g.qz[g.nz - 1] - g.qz[1]);
+    for (int m = 0; m < 3; ++m) vp1[l + m * NM] = vp[l + m * NM];
+    mrat[l] = (R)src.mrat_pu;
+    beta_p[l] = (R)src.beta_pu;
+  }
+  return n;
+}
+
+// Stable removal of every particle with keep[l] == 0: the bulk form of
+// remove_ion's order-preserving shift (gutsp.f:29-41).  Returns the new count.
+template <class R>
+std::int64_t compact(const State<R>& s, const std::vector<char>& keep, R* xp, R* vp, R* vp1, R* mrat, R* beta_p,
+                     std::int64_t ni_tot) {
+  const std::int64_t NM = s.ni_max;
+  std::int64_t w = 0;
+  for (std::int64_t l = 0; l < ni_tot; ++l) {
+    if (!keep[(std::size_t)l]) continue;
+    if (w != l)
+      for (int m = 0; m < 3; ++m) {
+        xp[w + m * NM] = xp[l + m * NM];
+        vp[w + m * NM] = vp[l + m * NM];
+        vp1[w + m * NM] = vp1[l + m * NM];
+      }
+    mrat[w] = mrat[l];
+    beta_p[w] = beta_p[l];
+    ++w;
+  }
+  return w;
+}
+
+// D3 outflow: after a half move with the x axis open, particles with
+// x > q(nx-1) or x <= q(1) leave the box.
+template <class R>
+std::int64_t remove_outflow_x(const State<R>& s, R* xp, R* vp, R* vp1, R* mrat, R* beta_p, std::int64_t ni_tot) {
+  const Mesh<R>& g = s.g;
+  std::vector<char> keep((std::size_t)ni_tot);
+  for (std::int64_t l = 0; l < ni_tot; ++l) keep[(std::size_t)l] = xp[l] > g.qx[1] && xp[l] <= g.qx[g.nx - 1];
+  return compact(s, keep, xp, vp, vp1, mrat, beta_p, ni_tot);
+}
+
+// D3 inflow: a virtual ghost slab one cell deep before x = q(1).  Each face
+// cell (j,k) holds inflow_ppc particles, stratified like the load, with
+// drifting-Maxwellian velocities of the reference's form; those whose
+// ballistic move over one ion step crosses x = q(1) enter the box at their
+// moved position.  Counts are exact functions of the draws.
+template <class R>
+std::int64_t inflow_x(State<R>& s, const Sources& src, std::int64_t step, R* xp, R* vp, R* vp1, R* mrat, R* beta_p,
+                      std::int64_t ni_tot) {
+  const Mesh<R>& g = s.g;
+  const std::int64_t NM = s.ni_max;
+  const int ncy = g.ny - 2, ncz = g.nz - 2, ppc = src.inflow_ppc;
+  const double pi = 3.14159265358979323846;
+  const R x0 = g.qx[1], dxg = g.dx_grid[1];
+  std::int64_t w = ni_tot;
+  for (int ck = 0; ck < ncz; ++ck)
+    for (int cj = 0; cj < ncy; ++cj)
+      for (int p = 0; p < ppc; ++p) {
+        const std::int64_t slot = ((std::int64_t)ck * ncy + cj) * ppc + p;
+        double u[4], v[4], e[4];
+        draw4(src, RNG_INFLOW, step, slot, 0, u);
+        draw4(src, RNG_INFLOW, step, slot, 1, v);
+        draw4(src, RNG_INFLOW, step, slot, 2, e);
+        const R vx = (R)(src.inflow_ux + src.inflow_vth * std::sqrt(-std::log(u[3])) * std::cos(pi * v[0]));
+        const R vy = (R)(src.inflow_uy + src.inflow_vth * std::sqrt(-std::log(v[1])) * std::cos(pi * v[2]));
+        const R vz = (R)(src.inflow_uz + src.inflow_vth * std::sqrt(-std::log(v[3])) * std::cos(pi * e[0]));
+        const R xg = x0 - dxg + (R)u[0] * dxg;
+        const R xn = xg + s.dt * vx;
+        if (!(xn > x0) || xn > g.qx[g.nx - 1]) continue;
+        if (w >= NM) throw std::runtime_error("inflow: Ni_max exceeded");
+        xp[w] = xn;
+        xp[w + NM] = g.qy[cj + 1] + (R)u[1] * (g.qy[cj + 2] - g.qy[cj + 1]);
+        xp[w + 2 * NM] = g.qz[ck + 1] + (R)u[2] * (g.qz[ck + 2] - g.qz[ck + 1]);
+        vp[w] = vx; vp[w + NM] = vy; vp[w + 2 * NM] = vz;
+        for (int m = 0; m < 3; ++m) vp1[w + m * NM] = vp[w + m * NM];
+        mrat[w] = R(1.0);
+        beta_p[w] = R(1.0);
+        ++w;
+      }
+  return w - ni_tot;
+}
+
+// Neutral cloud density n_n(r) = N0/(1+(r/r0)^2) about (cx,cy,cz).
+inline double cloud_density(const Sources& src, double x, double y, double z) {
+  const double dx = x - src.cloud_x, dy = y - src.cloud_y, dz = z - src.cloud_z;
+  const double r2 = (dx * dx + dy * dy + dz * dz) / (src.cloud_r0 * src.cloud_r0);
+  return src.cloud_N0 / (1.0 + r2);
+}
+
+// D4 cloud ionization, after the per-cell rule of Ionize_pluto_mp
+// (chem_rates.f:346-432): in every physical cell, n_new = vol*beta*beta_h*
+// n_n(centre)*nu_ion*dt; floor plus a Bernoulli trial on the remainder; new
+// heavy ions at rest, uniform in the cell.
+template <class R>
+std::int64_t cloud_count(const State<R>& s, const Sources& src, std::int64_t step, int ci, int cj, int ck) {
+  const Mesh<R>& g = s.g;
+  const double xc = 0.5 * ((double)g.qx[ci + 1] + (double)g.qx[ci + 2]);
+  const double yc = 0.5 * ((double)g.qy[cj + 1] + (double)g.qy[cj + 2]);
+  const double zc = 0.5 * ((double)g.qz[ck + 1] + (double)g.qz[ck + 2]);
+  const double vol = (double)g.dx_grid[ci + 1] * (double)g.dy_grid[cj + 1] * (double)g.dz_grid[ck + 1];
+  const double lam = vol * (double)s.beta * src.beta_heavy * cloud_density(src, xc, yc, zc) * src.nu_ion * (double)s.dt;
+  std::int64_t n = (std::int64_t)std::floor(lam);
+  double u[4];
+  const std::int64_t cell = ((std::int64_t)ck * (g.ny - 2) + cj) * (g.nx - 2) + ci;
+  draw4(src, RNG_CLOUD, step, cell, 0, u);
+  if (u[0] < lam - (double)n) ++n;
+  return n;
+}
+
+template <class R>
+std::int64_t ionize_cloud(State<R>& s, const Sources& src, std::int64_t step, R* xp, R* vp, R* vp1, R* mrat,
+                          R* beta_p, std::int64_t ni_tot) {
+  const Mesh<R>& g = s.g;
+  const std::int64_t NM = s.ni_max;
+  std::int64_t w = ni_tot;
+  for (int ck = 0; ck < g.nz - 2; ++ck)
+    for (int cj = 0; cj < g.ny - 2; ++cj)
+      for (int ci = 0; ci < g.nx - 2; ++ci) {
+        const std::int64_t n = cloud_count(s, src, step, ci, cj, ck);
+        const std::int64_t cell = ((std::int64_t)ck * (g.ny - 2) + cj) * (g.nx - 2) + ci;
+        for (std::int64_t q = 0; q < n; ++q) {
+          if (w >= NM) throw std::runtime_error("cloud ionization: Ni_max exceeded");
+          double u[4];
+          draw4(src, RNG_CLOUD, step, cell, (std::uint32_t)(1 + q), u);
+          xp[w] = g.qx[ci + 1] + (R)u[0] * (g.qx[ci + 2] - g.qx[ci + 1]);
+          xp[w + NM] = g.qy[cj + 1] + (R)u[1] * (g.qy[cj + 2] - g.qy[cj + 1]);
+          xp[w + 2 * NM] = g.qz[ck + 1] + (R)u[2] * (g.qz[ck + 2] - g.qz[ck + 1]);
+          for (int m = 0; m < 3; ++m) { vp[w + m * NM] = R(0); vp1[w + m * NM] = R(0); }
+          mrat[w] = (R)src.mrat_heavy;
+          beta_p[w] = (R)src.beta_heavy;
+          ++w;
+        }
+      }
+  return w - ni_tot;
+}
+
+// D5 charge exchange, after res_chex (chem_rates.f:823-840): each ion with
+// mrat != mrat_heavy exchanges with probability dt*n_n*sigma*v_rel,
+// sigma = a - b ln(v_rel); the new ion is heavy and at rest.  Returns the count.
+template <class R>
+std::int64_t res_chex(State<R>& s, const Sources& src, std::int64_t step, const R* xp, R* vp, R* vp1, R* mrat,
+                      std::int64_t ni_tot) {
+  const std::int64_t NM = s.ni_max;
+  std::int64_t n = 0;
+  for (std::int64_t l = 0; l < ni_tot; ++l) {
+    if (mrat[l] == (R)src.mrat_heavy) continue;
+    const double vx = vp[l], vy = vp[l + NM], vz = vp[l + 2 * NM];
+    const double vrel = std::sqrt(vx * vx + vy * vy + vz * vz);
+    if (!(vrel > 0.0)) continue;
+    const double sigma = src.cx_a - src.cx_b * std::log(vrel);
+    if (!(sigma > 0.0)) continue;
+    const double prob = (double)s.dt * cloud_density(src, xp[l], xp[l + NM], xp[l + 2 * NM]) * sigma * vrel;
+    double u[4];
+    draw4(src, RNG_CHEX, step, l, 0, u);
+    if (u[0] < prob) {
+      for (int m = 0; m < 3; ++m) { vp[l + m * NM] = R(0); vp1[l + m * NM] = R(0); }
+      mrat[l] = (R)src.mrat_heavy;
+      ++n;
+    }
+  }
+  return n;
 }
 
 }  // namespace swo

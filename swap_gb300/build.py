@@ -28,7 +28,6 @@ NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2
 UNITS = [
     ("k64.cu", ["--fmad=false"]),
     ("k32.cu", []),
-    ("kconv.cu", []),
     ("swap_abi.cu", []),
     ("swap_f32.cu", []),
     ("swap_prof.cu", []),

@@ -1,0 +1,972 @@
+// k32.cu -- kernels of the FP32 form (see k32.cuh for the data layout).
+#include "k32.cuh"
+
+namespace swapk32 {
+namespace {
+
+constexpr int TPB = 256;
+constexpr int TPB_PASS = 128;  // particle passes: keeps the shared tiles under 48 KB
+constexpr int KERR_DOMAIN = 3, KERR_MOVE = 7;
+
+inline unsigned nblk(long long n, int tpb = TPB) {
+  const long long b = (n + tpb - 1) / tpb;
+  return (unsigned)(b < 1 ? 1 : b);
+}
+
+#define GSTRIDE(t, n) \
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < (n); t += (long long)gridDim.x * blockDim.x)
+
+__device__ __forceinline__ void set_err(int* err, int code) {
+  if (err) atomicCAS(err, 0, code);
+}
+
+__device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+// 0-based linear index of 1-based node (i,j,k) in the (nx,ny,nz) layout
+__device__ __forceinline__ long long nid(const G32& g, int i, int j, int k) {
+  return (long long)(i - 1) + (long long)g.nx * ((long long)(j - 1) + (long long)g.ny * (long long)(k - 1));
+}
+// node index of physical node (p,q,r), p in [0,ncx): 1-based i = p + 2
+__device__ __forceinline__ long long pid(const G32& g, int p, int q, int r) { return nid(g, p + 2, q + 2, r + 2); }
+// interior image of a 1-based node index (ghost 1 -> n-1, ghost n -> 2)
+__device__ __forceinline__ int img(int i, int n) { return i == 1 ? n - 1 : (i == n ? 2 : i); }
+
+// Store v at interior node (i,j,k) and at every ghost node whose image it
+// is: the periodic fill of boundary.f:9-52 fused into the producer.
+template <class T>
+__device__ __forceinline__ void store_img(const G32& g, T* f, int i, int j, int k, T v) {
+  const int is[2] = {i, i == 2 ? g.nx : (i == g.nx - 1 ? 1 : -1)};
+  const int js[2] = {j, j == 2 ? g.ny : (j == g.ny - 1 ? 1 : -1)};
+  const int ks[2] = {k, k == 2 ? g.nz : (k == g.nz - 1 ? 1 : -1)};
+  for (int a = 0; a < 2; ++a) {
+    if (is[a] < 0) continue;
+    for (int b = 0; b < 2; ++b) {
+      if (js[b] < 0) continue;
+      for (int c = 0; c < 2; ++c) {
+        if (ks[c] < 0) continue;
+        f[nid(g, is[a], js[b], ks[c])] = v;
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void interior_of(const G32& g, long long t, int& i, int& j, int& k) {
+  i = (int)(t % g.ncx) + 2;
+  const long long r = t / g.ncx;
+  j = (int)(r % g.ncy) + 2;
+  k = (int)(r / g.ncy) + 2;
+}
+
+__device__ __forceinline__ long long n_int(const G32& g) { return (long long)g.ncx * g.ncy * g.ncz; }
+
+// Move one axis of a (cell, offset) position by d cells.  upper_closed:
+// offsets in (0,1] (the '>' cell search of x and z, gutsp.f:1396-1412);
+// otherwise [0,1) (the floor of y, gutsp.f:1404).  Periodic in the cell
+// index (gutsp.f:490-510).  Returns false on a move of more than two cells.
+__device__ __forceinline__ bool move_axis(int& c, float& o, float d, int n, bool upper_closed) {
+  if (!(fabsf(d) < 2.0f)) return false;
+  o += d;
+#pragma unroll
+  for (int it = 0; it < 3; ++it) {
+    if (upper_closed) {
+      if (o > 1.0f) { o -= 1.0f; ++c; }
+      else if (o <= 0.0f) { o += 1.0f; --c; }
+    } else {
+      if (o >= 1.0f) { o -= 1.0f; ++c; }
+      else if (o < 0.0f) { o += 1.0f; --c; }
+    }
+  }
+  c = c < 0 ? c + n : (c >= n ? c - n : c);
+  return true;
+}
+
+// Offset of a cell from a brick's first cell along one axis, unwrapped
+// across the periodic boundary into the brick tile's window [-1, 4] when
+// one of the periodic images lies there (n >= 8, so at most one does).
+__device__ __forceinline__ int rel_cell(int c, int c0, int n) {
+  int r = c - c0;
+  if (r < -1) r += n;
+  else if (r > 4) r -= n;
+  return r;
+}
+
+// Step between two cells along one axis, unwrapped into [-1, 1] when one of
+// the periodic images lies there.
+__device__ __forceinline__ int step_cell(int c, int c0, int n) {
+  int r = c - c0;
+  if (r < -1) r += n;
+  else if (r > 1) r -= n;
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// particle passes
+// ---------------------------------------------------------------------------
+
+template <int PASS>
+__global__ void __launch_bounds__(TPB_PASS) k_pass(G32 g, Part p, Species sp, StepParams sprm,
+                                              const int64_t* __restrict__ start, const float4* __restrict__ kit,
+                                              float* __restrict__ partial, int* err) {
+  __shared__ float4 s_kit[PASS == 1 ? 2 : 2 * TNODES];
+  __shared__ float s_dep[4 * TNODES];
+  __shared__ float s_red[TPB_PASS / 32][32][33];  // per-warp transpose of deposit values
+  const long long b = blockIdx.x;
+  const int bi = (int)(b % g.nbx), bj = (int)((b / g.nbx) % g.nby), bk = (int)(b / ((long long)g.nbx * g.nby));
+  const int c0x = 4 * bi, c0y = 4 * bj, c0z = 4 * bk;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (PASS != 1) {
+    for (int t = threadIdx.x; t < TNODES; t += blockDim.x) {
+      const int tx = t % TN, ty = (t / TN) % TN, tz = t / (TN * TN);
+      const int P = wrapi(c0x - 2 + tx, g.ncx), Q = wrapi(c0y - 2 + ty, g.ncy), R = wrapi(c0z - 2 + tz, g.ncz);
+      const long long src = 2 * ((long long)P + (long long)g.ncx * (Q + (long long)g.ncy * R));
+      s_kit[2 * t] = kit[src];
+      s_kit[2 * t + 1] = kit[src + 1];
+    }
+  }
+  for (int t = threadIdx.x; t < 4 * TNODES; t += blockDim.x) s_dep[t] = 0.0f;
+  __syncthreads();
+
+  const float hdt = 0.5f * sprm.dt;
+  const long long first = start[b * BCELLS], last = start[b * BCELLS + BCELLS];
+  // warp-uniform trip count: every lane takes part in the deposit reduction
+  for (long long base = first; base < last; base += blockDim.x) {
+    const long long l = base + threadIdx.x;
+    bool live = l < last;
+    int t0 = -1;
+    float w8[8], qdv[4];
+    if (live) {
+      const int32_t c = p.cell[l];
+      int ci = pk_i(c), cj = pk_j(c), ck = pk_k(c);
+      float ox = p.ox[l], oy = p.oy[l], oz = p.oz[l];
+      float vx = p.vx[l], vy = p.vy[l], vz = p.vz[l];
+      const int s = p.sp ? min((int)p.sp[l], MAX_SPECIES - 1) : 0;
+      const float mr = sp.mrat[s], qw = sp.qw[s];
+      float dvx = 0.f, dvy = 0.f, dvz = 0.f;  // velocity deposited
+      bool moved = false;
+      if (PASS == 1) {
+        const float wx = p.wx[l], wy = p.wy[l], wz = p.wz[l];
+        if (sprm.pending_move) {  // maind.f:479 of the previous step
+          bool ok = move_axis(ci, ox, vx * hdt * g.inv_dx, g.ncx, true);
+          ok &= move_axis(cj, oy, vy * hdt * g.inv_dy, g.ncy, false);
+          ok &= move_axis(ck, oz, vz * hdt * g.inv_dz, g.ncz, true);
+          if (!ok) set_err(err, KERR_MOVE);
+          moved = true;
+        }
+        dvx = 1.5f * vx - 0.5f * wx;  // extrapol_up (gutsp.f:144)
+        dvy = 1.5f * vy - 0.5f * wy;
+        dvz = 1.5f * vz - 0.5f * wz;
+      }
+      int rx = rel_cell(ci, c0x, g.ncx), ry = rel_cell(cj, c0y, g.ncy), rz = rel_cell(ck, c0z, g.ncz);
+      bool inside = !(rx < -1 || rx > 4 || ry < -1 || ry > 4 || rz < -1 || rz > 4);
+      if (PASS != 1 && inside) {
+        // trilinear gather of (ajc-upc, btc) at the 8 corners (gutsp.f:217-251)
+        const float wxl = 1.0f - ox, wxu = ox, wyl = 1.0f - oy, wyu = oy, wzl = 1.0f - oz, wzu = oz;
+        const int tg = (rx + 1) + TN * ((ry + 1) + TN * (rz + 1));
+        float ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;
+#pragma unroll
+        for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+          for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+            for (int cx = 0; cx < 2; ++cx) {
+              const float w = (cx ? wxu : wxl) * (cy ? wyu : wyl) * (cz ? wzu : wzl);
+              const int t = tg + cx + TN * (cy + TN * cz);
+              const float4 f0 = s_kit[2 * t], f1 = s_kit[2 * t + 1];
+              ax = fmaf(w, f0.x, ax); ay = fmaf(w, f0.y, ay); az = fmaf(w, f0.z, az);
+              bx = fmaf(w, f0.w, bx); by = fmaf(w, f1.x, by); bz = fmaf(w, f1.y, bz);
+            }
+        // Ep = ((aj-up) x B) * mrat (gutsp.f:260-270)
+        const float ex = (ay * bz - az * by) * mr, ey = (az * bx - ax * bz) * mr, ez = (ax * by - ay * bx) * mr;
+        // v- and the rotation of get_vplus_vminus (gutsp.f:302-397)
+        const float mx = vx + hdt * ex, my = vy + hdt * ey, mz = vz + hdt * ez;
+        const float Bx = bx * mr, By = by * mr, Bz = bz * mr;
+        const float B2 = Bx * Bx + By * By + Bz * Bz;
+        const float dt2 = sprm.dt * sprm.dt;
+        const float ad = 1.0f / (1.0f + 0.25f * B2 * dt2);
+        const float a1 = (1.0f - 0.25f * B2 * dt2) * ad, a2 = sprm.dt * ad, a3 = 0.5f * dt2 * ad;
+        const float mdb = mx * Bx + my * By + mz * Bz;
+        const float px = a1 * mx + a2 * (my * Bz - mz * By) + a3 * mdb * Bx;
+        const float py = a1 * my + a2 * (mz * Bx - mx * Bz) + a3 * mdb * By;
+        const float pz = a1 * mz + a2 * (mx * By - my * Bx) + a3 * mdb * Bz;
+        if (PASS == 2) {  // improve_up (gutsp.f:422)
+          dvx = 0.5f * (px + mx);
+          dvy = 0.5f * (py + my);
+          dvz = 0.5f * (pz + mz);
+        } else {  // get_vp_final (gutsp.f:444-445) and move_ion_half (gutsp.f:473-510)
+          p.wx[l] = vx; p.wy[l] = vy; p.wz[l] = vz;
+          vx = px + hdt * ex;
+          vy = py + hdt * ey;
+          vz = pz + hdt * ez;
+          p.vx[l] = vx; p.vy[l] = vy; p.vz[l] = vz;
+          bool ok = move_axis(ci, ox, vx * hdt * g.inv_dx, g.ncx, true);
+          ok &= move_axis(cj, oy, vy * hdt * g.inv_dy, g.ncy, false);
+          ok &= move_axis(ck, oz, vz * hdt * g.inv_dz, g.ncz, true);
+          if (!ok) set_err(err, KERR_MOVE);
+          moved = true;
+          dvx = vx; dvy = vy; dvz = vz;
+          rx = rel_cell(ci, c0x, g.ncx); ry = rel_cell(cj, c0y, g.ncy); rz = rel_cell(ck, c0z, g.ncz);
+          inside = !(rx < -1 || rx > 4 || ry < -1 || ry > 4 || rz < -1 || rz > 4);
+        }
+      }
+      if (!inside) {
+        set_err(err, KERR_MOVE);
+        live = false;
+      } else {
+        if (moved) {
+          p.cell[l] = pk(ci, cj, ck);
+          p.ox[l] = ox; p.oy[l] = oy; p.oz[l] = oz;
+        }
+        t0 = (rx + 1) + TN * ((ry + 1) + TN * (rz + 1));
+        const float wxl = 1.0f - ox, wxu = ox, wyl = 1.0f - oy, wyu = oy, wzl = 1.0f - oz, wzu = oz;
+#pragma unroll
+        for (int cc = 0; cc < 8; ++cc)
+          w8[cc] = ((cc & 1) ? wxu : wxl) * (((cc >> 1) & 1) ? wyu : wyl) * ((cc >> 2) ? wzu : wzl);
+        qdv[0] = qw;
+        qdv[1] = qw * dvx;
+        qdv[2] = qw * dvy;
+        qdv[3] = qw * dvz;
+      }
+    }
+    // deposit (gutsp.f:1484-1491, 1704-1756): transpose the 32 values
+    // (4 moments x 8 corners) of the warp's particles, sum them per group of
+    // lanes in the same cell, and add each group's sums to the brick tile
+    // with one shared atomic per value slot.
+    float* row = s_red[warp][lane];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int cc = 0; cc < 8; ++cc) row[q * 8 + cc] = live ? w8[cc] * qdv[q] : 0.0f;
+    __syncwarp();
+    const unsigned grp = __match_any_sync(0xffffffffu, t0);
+    unsigned leaders = __ballot_sync(0xffffffffu, live && lane == __ffs(grp) - 1);
+    const int qv = lane >> 3, cv = lane & 7;
+    const int off = (cv & 1) + TN * (((cv >> 1) & 1) + TN * (cv >> 2));
+    while (leaders) {
+      const int L = __ffs(leaders) - 1;
+      leaders &= leaders - 1;
+      const unsigned gm = __shfl_sync(0xffffffffu, grp, L);
+      const int tL = __shfl_sync(0xffffffffu, t0, L);
+      float acc = 0.0f;
+      for (unsigned m = gm; m; m &= m - 1) acc += s_red[warp][__ffs(m) - 1][lane];
+      if (PASS != 2 || qv != 0) atomicAdd(&s_dep[qv * TNODES + tL + off], acc);
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  float* out = partial + b * (4 * TNODES);
+  for (int t = threadIdx.x; t < 4 * TNODES; t += blockDim.x) out[t] = s_dep[t];
+}
+
+// Sum, at every interior node, the brick tiles that cover it: along each axis
+// node p lies in the tiles of bricks floor((p+2)/4) (offset (p+2)%4) and the
+// one before (offset +4, when <= 6).
+__global__ void k_node_sum(G32 g, const float* __restrict__ partial, int nq, float* __restrict__ np,
+                           float* __restrict__ S) {
+  GSTRIDE(t, n_int(g)) {
+    const int P = (int)(t % g.ncx), Q = (int)((t / g.ncx) % g.ncy), R = (int)(t / ((long long)g.ncx * g.ncy));
+    int bx[2], ox[2], by[2], oy[2], bz[2], oz[2], nxc = 1, nyc = 1, nzc = 1;
+    bx[0] = (P + 2) >> 2; ox[0] = (P + 2) & 3;
+    if (bx[0] >= g.nbx) bx[0] -= g.nbx;
+    if (ox[0] + 4 <= 6) { bx[1] = bx[0] == 0 ? g.nbx - 1 : bx[0] - 1; ox[1] = ox[0] + 4; nxc = 2; }
+    by[0] = (Q + 2) >> 2; oy[0] = (Q + 2) & 3;
+    if (by[0] >= g.nby) by[0] -= g.nby;
+    if (oy[0] + 4 <= 6) { by[1] = by[0] == 0 ? g.nby - 1 : by[0] - 1; oy[1] = oy[0] + 4; nyc = 2; }
+    bz[0] = (R + 2) >> 2; oz[0] = (R + 2) & 3;
+    if (bz[0] >= g.nbz) bz[0] -= g.nbz;
+    if (oz[0] + 4 <= 6) { bz[1] = bz[0] == 0 ? g.nbz - 1 : bz[0] - 1; oz[1] = oz[0] + 4; nzc = 2; }
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int a = 0; a < nxc; ++a)
+      for (int bb = 0; bb < nyc; ++bb)
+        for (int cc = 0; cc < nzc; ++cc) {
+          const long long brick = bx[a] + (long long)g.nbx * (by[bb] + (long long)g.nby * bz[cc]);
+          const int tt = ox[a] + TN * (oy[bb] + TN * oz[cc]);
+          const float* src = partial + brick * (4 * TNODES) + tt;
+          for (int q = 4 - nq; q < 4; ++q) acc[q] += src[q * TNODES];
+        }
+    const long long o = pid(g, P, Q, R);
+    if (nq == 4) np[o] = acc[0];
+    S[o] = acc[1];
+    S[o + g.C] = acc[2];
+    S[o + 2 * g.C] = acc[3];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// fields (interior nodes, ghost images written by the producer)
+// ---------------------------------------------------------------------------
+
+// Generic periodic fill of the ghost shell (boundary.f:9-52).
+__global__ void k_ghost(G32 g, float* f, int ncomp) {
+  GSTRIDE(o, g.C) {
+    const int i = (int)(o % g.nx) + 1, j = (int)((o / g.nx) % g.ny) + 1, k = (int)(o / ((long long)g.nx * g.ny)) + 1;
+    const int wi = img(i, g.nx), wj = img(j, g.ny), wk = img(k, g.nz);
+    if (wi == i && wj == j && wk == k) continue;
+    const long long s = nid(g, wi, wj, wk);
+    for (int m = 0; m < ncomp; ++m) f[o + g.C * m] = f[s + g.C * m];
+  }
+}
+
+// ct = S/np at the interior image; up_m = 0.5*(ct_m(node) + ct_m(node+e_m))
+// (gutsp.f:1825-1836); np and up with ghost images.
+__device__ __forceinline__ float ct_at(const G32& g, const float* np, const float* S, int i, int j, int k, int m) {
+  const long long o = nid(g, img(i, g.nx), img(j, g.ny), img(k, g.nz));
+  const float n = np[o];
+  return n == 0.0f ? 0.0f : S[o + g.C * m] / n;
+}
+
+__global__ void k_ct_up(G32 g, float* __restrict__ np, const float* __restrict__ S, float* __restrict__ up) {
+  GSTRIDE(t, n_int(g)) {
+    int i, j, k;
+    interior_of(g, t, i, j, k);
+    const float ux = 0.5f * (ct_at(g, np, S, i, j, k, 0) + ct_at(g, np, S, i + 1, j, k, 0));
+    const float uy = 0.5f * (ct_at(g, np, S, i, j, k, 1) + ct_at(g, np, S, i, j + 1, k, 1));
+    const float uz = 0.5f * (ct_at(g, np, S, i, j, k, 2) + ct_at(g, np, S, i, j, k + 1, 2));
+    store_img(g, up, i, j, k, ux);
+    store_img(g, up + g.C, i, j, k, uy);
+    store_img(g, up + 2 * g.C, i, j, k, uz);
+  }
+}
+
+// Cell-centre B from the edge field (edge_to_center, grid_interp.f:35-51)
+// with xrat = yrat = zrat = 1/2 (uniform grid), at an interior node.
+__device__ __forceinline__ void e2c(const G32& g, const float* bt, int i, int j, int k, float& c1, float& c2,
+                                    float& c3) {
+  const long long C = g.C;
+  const long long o = nid(g, i, j, k), sx = 1, sy = g.nx, sz = (long long)g.nx * g.ny;
+  float b1, b2;
+  b2 = 0.5f * (bt[o] + bt[o - sy]);
+  b1 = 0.5f * (bt[o - sz] + bt[o - sy - sz]);
+  c1 = 0.5f * (b1 + b2);
+  const float* B = bt + C;
+  b2 = 0.5f * (B[o] + B[o - sx]);
+  b1 = 0.5f * (B[o - sz] + B[o - sx - sz]);
+  c2 = 0.5f * (b1 + b2);
+  B = bt + 2 * C;
+  b2 = 0.5f * (B[o] + B[o - sy]);
+  b1 = 0.5f * (B[o - sx] + B[o - sx - sy]);
+  c3 = 0.5f * (b1 + b2);
+}
+
+// Gather kit per physical node: (ajc - upc, btc) with ajc/upc =
+// face_to_center (grid_interp.f:163-170) and btc = edge_to_center of
+// dB plus the centred b0.
+__global__ void k_kit(G32 g, const float* __restrict__ aj, const float* __restrict__ up,
+                      const float* __restrict__ dbt, const float* __restrict__ b0c, float4* __restrict__ kit) {
+  GSTRIDE(t, n_int(g)) {
+    int i, j, k;
+    interior_of(g, t, i, j, k);
+    const long long C = g.C, o = nid(g, i, j, k), sx = 1, sy = g.nx, sz = (long long)g.nx * g.ny;
+    const float ax = 0.5f * ((aj[o] - up[o]) + (aj[o - sx] - up[o - sx]));
+    const float ay = 0.5f * ((aj[o + C] - up[o + C]) + (aj[o - sy + C] - up[o - sy + C]));
+    const float az = 0.5f * ((aj[o + 2 * C] - up[o + 2 * C]) + (aj[o - sz + 2 * C] - up[o - sz + 2 * C]));
+    float c1, c2, c3;
+    e2c(g, dbt, i, j, k, c1, c2, c3);
+    kit[2 * t] = make_float4(ax, ay, az, c1 + b0c[0]);
+    kit[2 * t + 1] = make_float4(c2 + b0c[1], c3 + b0c[2], 0.0f, 0.0f);
+  }
+}
+
+// curlB (gutsf.f:202-239) on dB with uniform spacing; curl(b0) = 0.
+__global__ void k_curlB(G32 g, const float* __restrict__ b, const float* __restrict__ np, float alpha,
+                        float* __restrict__ aj) {
+  GSTRIDE(t, n_int(g)) {
+    int i, j, k;
+    interior_of(g, t, i, j, k);
+    const long long C = g.C, o = nid(g, i, j, k), sx = 1, sy = g.nx, sz = (long long)g.nx * g.ny;
+    const float n0 = np[o];
+    const float* B1 = b;
+    const float* B2 = b + C;
+    const float* B3 = b + 2 * C;
+    const float c1 = (B3[o] - B3[o - sy]) * g.inv_dy + (B2[o - sz] - B2[o]) * g.inv_dz;
+    const float c2 = (B1[o] - B1[o - sz]) * g.inv_dz + (B3[o - sx] - B3[o]) * g.inv_dx;
+    const float c3 = (B2[o] - B2[o - sx]) * g.inv_dx + (B1[o - sy] - B1[o]) * g.inv_dy;
+    store_img(g, aj, i, j, k, c1 / (0.5f * (n0 + np[o + sx]) * alpha));
+    store_img(g, aj + C, i, j, k, c2 / (0.5f * (n0 + np[o + sy]) * alpha));
+    store_img(g, aj + 2 * C, i, j, k, c3 / (0.5f * (n0 + np[o + sz]) * alpha));
+  }
+}
+
+__global__ void k_half_sum(long long n, const float* __restrict__ a, const float* __restrict__ b,
+                           float* __restrict__ out) {
+  GSTRIDE(t, n) out[t] = 0.5f * (a[t] + b[t]);
+}
+
+// face_to_center of a = aj - up (gutsf.f:1059, grid_interp.f:163-170)
+__device__ __forceinline__ void aa_at(const G32& g, const float* aj, const float* up, long long o, float& x, float& y,
+                                      float& z) {
+  const long long C = g.C, sy = g.nx, sz = (long long)g.nx * g.ny;
+  x = 0.5f * ((aj[o] - up[o]) + (aj[o - 1] - up[o - 1]));
+  y = 0.5f * ((aj[o + C] - up[o + C]) + (aj[o - sy + C] - up[o - sy + C]));
+  z = 0.5f * ((aj[o + 2 * C] - up[o + 2 * C]) + (aj[o - sz + 2 * C] - up[o - sz + 2 * C]));
+}
+
+// Predictor cross product of get_E/crossf2 (gutsf.f:1073-1075, 65-76).
+__global__ void k_ct_pred(G32 g, const float* __restrict__ aj, const float* __restrict__ up,
+                          const float* __restrict__ dbt, const float* __restrict__ b0c, float* __restrict__ ct) {
+  GSTRIDE(t, n_int(g)) {
+    int i, j, k;
+    interior_of(g, t, i, j, k);
+    const long long C = g.C, o = nid(g, i, j, k);
+    float ax, ay, az, bx, by, bz;
+    aa_at(g, aj, up, o, ax, ay, az);
+    e2c(g, dbt, i, j, k, bx, by, bz);
+    bx += b0c[0]; by += b0c[1]; bz += b0c[2];
+    store_img(g, ct, i, j, k, ay * bz - az * by);
+    store_img(g, ct + C, i, j, k, az * bx - ax * bz);
+    store_img(g, ct + 2 * C, i, j, k, ax * by - ay * bx);
+  }
+}
+
+// Corrector: B at m+1/2 via edge_to_face then face_to_center (gutsf.f:1268-
+// 1269): component m is the 1-2-1 average along axis m of edge_to_center.
+__global__ void k_ct_corr(G32 g, const float* __restrict__ aj, const float* __restrict__ up,
+                          const float* __restrict__ dbtp1, const float* __restrict__ b0c, float* __restrict__ ct) {
+  GSTRIDE(t, n_int(g)) {
+    int i, j, k;
+    interior_of(g, t, i, j, k);
+    const long long C = g.C, o = nid(g, i, j, k);
+    float ax, ay, az;
+    aa_at(g, aj, up, o, ax, ay, az);
+    float c1, c2, c3, m1, m2, m3, p1, p2, p3, d1, d2;
+    e2c(g, dbtp1, i, j, k, c1, c2, c3);
+    e2c(g, dbtp1, img(i - 1, g.nx), j, k, m1, d1, d2);
+    e2c(g, dbtp1, img(i + 1, g.nx), j, k, p1, d1, d2);
+    const float bx = 0.25f * (m1 + 2.0f * c1 + p1) + b0c[0];
+    e2c(g, dbtp1, i, img(j - 1, g.ny), k, d1, m2, d2);
+    e2c(g, dbtp1, i, img(j + 1, g.ny), k, d1, p2, d2);
+    const float by = 0.25f * (m2 + 2.0f * c2 + p2) + b0c[1];
+    e2c(g, dbtp1, i, j, img(k - 1, g.nz), d1, d2, m3);
+    e2c(g, dbtp1, i, j, img(k + 1, g.nz), d1, d2, p3);
+    const float bz = 0.25f * (m3 + 2.0f * c3 + p3) + b0c[2];
+    store_img(g, ct, i, j, k, ay * bz - az * by);
+    store_img(g, ct + C, i, j, k, az * bx - ax * bz);
+    store_img(g, ct + 2 * C, i, j, k, ax * by - ay * bx);
+  }
+}
+
+// E = face average of ct + nu*aj (gutsf.f:94-96, 1082).
+__global__ void k_E(G32 g, const float* __restrict__ ct, const float* __restrict__ nu, const float* __restrict__ aj,
+                    float* __restrict__ E) {
+  GSTRIDE(t, n_int(g)) {
+    int i, j, k;
+    interior_of(g, t, i, j, k);
+    const long long C = g.C, o = nid(g, i, j, k), sy = g.nx, sz = (long long)g.nx * g.ny;
+    const float n = nu[o];
+    store_img(g, E, i, j, k, 0.5f * (ct[o] + ct[o + 1]) + n * aj[o]);
+    store_img(g, E + C, i, j, k, 0.5f * (ct[o + C] + ct[o + sy + C]) + n * aj[o + C]);
+    store_img(g, E + 2 * C, i, j, k, 0.5f * (ct[o + 2 * C] + ct[o + sz + 2 * C]) + n * aj[o + 2 * C]);
+  }
+}
+
+// curlE (gutsf.f:288-299) and b1p2 = base - coef*curlE in FP64
+// (gutsf.f:1158-1159, 1349-1350); dB of the result mirrored in FP32.
+__global__ void k_bupd(G32 g, const float* __restrict__ E, const double* __restrict__ base,
+                       const double* __restrict__ b0, double coef, double* __restrict__ b1p2,
+                       float* __restrict__ db1p2) {
+  GSTRIDE(t, n_int(g)) {
+    int i, j, k;
+    interior_of(g, t, i, j, k);
+    const long long C = g.C, o = nid(g, i, j, k), sx = 1, sy = g.nx, sz = (long long)g.nx * g.ny;
+    const float* E1 = E;
+    const float* E2 = E + C;
+    const float* E3 = E + 2 * C;
+    const float ce[3] = {(E3[o + sy] - E3[o]) * g.inv_dy + (E2[o] - E2[o + sz]) * g.inv_dz,
+                         (E3[o] - E3[o + sx]) * g.inv_dx + (E1[o + sz] - E1[o]) * g.inv_dz,
+                         (E1[o] - E1[o + sy]) * g.inv_dy + (E2[o + sx] - E2[o]) * g.inv_dx};
+    for (int m = 0; m < 3; ++m) {
+      const double v = base[o + C * m] - coef * (double)ce[m];
+      store_img(g, b1p2 + C * m, i, j, k, v);
+      store_img(g, db1p2 + C * m, i, j, k, (float)(v - b0[o + C * m]));
+    }
+  }
+}
+
+// Whistler Courant time at every node, ghosts included, as check_time_step
+// loops over them (gutsf.f:1782-1792), plus the smallest value.
+__global__ void k_courant(G32 g, const float* __restrict__ dbt, const float* __restrict__ b0c,
+                          const float* __restrict__ np, float alpha, float dx, float* __restrict__ dtn, unsigned* out) {
+  float mn = 3.0e38f;
+  GSTRIDE(o, g.C) {
+    const float b1 = dbt[o] + b0c[0], b2 = dbt[o + g.C] + b0c[1], b3 = dbt[o + 2 * g.C] + b0c[2];
+    const float btot = sqrtf(b1 * b1 + b2 * b2 + b3 * b3);
+    const float ak = 2.0f / dx;
+    const float a1 = ak * ak * btot / (alpha * np[o]);
+    const float a2 = (ak * btot) * (ak * btot) / (alpha * np[o]);
+    const float womega = 0.5f * (a1 + sqrtf(a1 * a1 + 4.0f * a2));
+    const float d = dx / (womega / ak);
+    dtn[o] = d;
+    mn = fminf(mn, d > 0.0f ? d : 0.0f);
+  }
+  for (int off = 16; off > 0; off >>= 1) mn = fminf(mn, __shfl_down_sync(0xffffffffu, mn, off));
+  if ((threadIdx.x & 31) == 0) atomicMin(out, __float_as_uint(mn));
+}
+
+// ---------------------------------------------------------------------------
+// stable counting sort by cell key for particles that moved at most one cell
+// per axis since the last sort
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ int dir_index(int dx, int dy, int dz) { return (dx + 1) + 3 * (dy + 1) + 9 * (dz + 1); }
+
+// One warp per old key K: direction of every particle of K and its rank
+// among the particles of K with the same direction, in array order.
+__global__ void k_sort_prep(G32 g, const int64_t* __restrict__ start, const int32_t* __restrict__ cell,
+                            uint32_t* __restrict__ dirrank, uint16_t* __restrict__ dep, int* err) {
+  __shared__ unsigned s_cnt[TPB / 32][NDIR];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long K = blockIdx.x * (long long)(blockDim.x >> 5) + w; K < g.nkeys; K += nwarps) {
+    if (lane < NDIR) s_cnt[w][lane] = 0;
+    __syncwarp();
+    int i0, j0, k0;
+    cell_of_key(g, K, i0, j0, k0);
+    const long long a = start[K], e = start[K + 1];
+    for (long long base = a; base < e; base += 32) {
+      const long long l = base + lane;
+      const bool live = l < e;
+      int d = NDIR;  // sentinel for idle lanes
+      if (live) {
+        const int32_t c = cell[l];
+        const int dx = step_cell(pk_i(c), i0, g.ncx), dy = step_cell(pk_j(c), j0, g.ncy),
+                  dz = step_cell(pk_k(c), k0, g.ncz);
+        if (dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1) {
+          set_err(err, KERR_MOVE);
+          d = NDIR + 1;  // not counted; the scatter skips it
+        } else {
+          d = dir_index(dx, dy, dz);
+        }
+      }
+      const unsigned peers = __match_any_sync(0xffffffffu, d);
+      const unsigned lt = peers & ((1u << lane) - 1u);
+      const int leader = __ffs(peers) - 1;
+      const bool counted = live && d < NDIR;
+      unsigned basecnt = 0;
+      if (counted) basecnt = s_cnt[w][d];
+      __syncwarp();
+      if (live && !counted) dirrank[l] = 0xffffffffu;
+      if (counted) {
+        dirrank[l] = ((uint32_t)d << 26) | (basecnt + __popc(lt));
+        if (lane == leader) s_cnt[w][d] = basecnt + __popc(peers);
+      }
+      __syncwarp();
+    }
+    if (lane < NDIR) dep[K * NDIR + lane] = (uint16_t)s_cnt[w][lane];
+    __syncwarp();
+  }
+}
+
+// The old key from which direction d arrives at the cell of key X.
+__device__ __forceinline__ long long src_key(const G32& g, int i, int j, int k, int d) {
+  const int dx = d % 3 - 1, dy = (d / 3) % 3 - 1, dz = d / 9 - 1;
+  return key_of(g, wrapi(i - dx, g.ncx), wrapi(j - dy, g.ncy), wrapi(k - dz, g.ncz));
+}
+
+// Per new key X: the count of arriving particles and, for every direction d,
+// how many of them come from sources earlier in key order than the source of
+// d (the stable order), so the scatter needs one lookup per particle.
+__global__ void k_sort_count(G32 g, const uint16_t* __restrict__ dep, int64_t* __restrict__ count,
+                             uint16_t* __restrict__ pre, int* err) {
+  GSTRIDE(X, g.nkeys) {
+    int i, j, k;
+    cell_of_key(g, X, i, j, k);
+    long long sk[NDIR];
+    unsigned cnt[NDIR];
+    int64_t n = 0;
+    for (int d = 0; d < NDIR; ++d) {
+      sk[d] = src_key(g, i, j, k, d);
+      cnt[d] = dep[sk[d] * NDIR + d];
+      n += cnt[d];
+    }
+    if (n > 65535) set_err(err, KERR_MOVE);
+    for (int d = 0; d < NDIR; ++d) {
+      unsigned p = 0;
+      for (int q = 0; q < NDIR; ++q) p += sk[q] < sk[d] ? cnt[q] : 0u;
+      pre[X * NDIR + d] = (uint16_t)p;
+    }
+    count[X] = n;
+  }
+}
+
+// dest = start_new[X] + (arrivals from sources earlier in key order) + rank.
+__global__ void k_sort_scatter(G32 g, long long N, const int32_t* __restrict__ cell,
+                               const uint32_t* __restrict__ dirrank, const uint16_t* __restrict__ pre,
+                               const int64_t* __restrict__ start_new, Part s, Part d, int* err) {
+  GSTRIDE(l, N) {
+    const int32_t c = cell[l];
+    const uint32_t dr = dirrank[l];
+    const int dd = (int)(dr >> 26);
+    if (dd >= NDIR) {
+      set_err(err, KERR_MOVE);
+      continue;
+    }
+    const long long X = key_of(g, pk_i(c), pk_j(c), pk_k(c));
+    const long long dst = start_new[X] + pre[X * NDIR + dd] + (dr & ((1u << 26) - 1u));
+    if (dst < 0 || dst >= N) {
+      set_err(err, KERR_MOVE);
+      continue;
+    }
+    d.cell[dst] = c;
+    d.ox[dst] = s.ox[l]; d.oy[dst] = s.oy[l]; d.oz[dst] = s.oz[l];
+    d.vx[dst] = s.vx[l]; d.vy[dst] = s.vy[l]; d.vz[dst] = s.vz[l];
+    d.wx[dst] = s.wx[l]; d.wy[dst] = s.wy[l]; d.wz[dst] = s.wz[l];
+    if (s.sp) d.sp[dst] = s.sp[l];
+  }
+}
+
+// three-phase exclusive scan of int64 (block sums, scan of sums, add)
+constexpr int SCAN_ITEMS = 4;
+constexpr int SCAN_TILE = TPB * SCAN_ITEMS;
+
+__device__ __forceinline__ int64_t block_excl_scan(int64_t v, int64_t* sh, int64_t& total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int64_t x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sh[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    int64_t s = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < (int)(blockDim.x >> 5)) sh[lane] = s;
+  }
+  __syncthreads();
+  total = sh[(blockDim.x >> 5) - 1];
+  const int64_t before = w > 0 ? sh[w - 1] : 0;
+  __syncthreads();
+  return before + x - v;
+}
+
+__global__ void k_scan_reduce(const int64_t* __restrict__ in, long long n, int64_t* __restrict__ sums) {
+  __shared__ int64_t sh[32];
+  const long long base = (long long)blockIdx.x * SCAN_TILE;
+  int64_t v = 0;
+  for (int q = 0; q < SCAN_ITEMS; ++q) {
+    const long long idx = base + threadIdx.x * SCAN_ITEMS + q;
+    if (idx < n) v += in[idx];
+  }
+  int64_t tot;
+  block_excl_scan(v, sh, tot);
+  if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+__global__ void k_scan_sums(int64_t* sums, long long nb) {
+  __shared__ int64_t sh[32];
+  int64_t carry = 0;
+  for (long long base = 0; base < nb; base += blockDim.x) {
+    const long long idx = base + threadIdx.x;
+    const int64_t v = idx < nb ? sums[idx] : 0;
+    int64_t tot;
+    const int64_t ex = block_excl_scan(v, sh, tot);
+    if (idx < nb) sums[idx] = carry + ex;
+    carry += tot;
+  }
+}
+
+__global__ void k_scan_apply(const int64_t* __restrict__ in, long long n, const int64_t* __restrict__ sums,
+                             int64_t* __restrict__ out) {
+  __shared__ int64_t sh[32];
+  const long long base = (long long)blockIdx.x * SCAN_TILE;
+  int64_t v[SCAN_ITEMS], s = 0;
+  for (int q = 0; q < SCAN_ITEMS; ++q) {
+    const long long idx = base + threadIdx.x * SCAN_ITEMS + q;
+    v[q] = idx < n ? in[idx] : 0;
+    s += v[q];
+  }
+  int64_t tot;
+  int64_t run = block_excl_scan(s, sh, tot) + sums[blockIdx.x];
+  for (int q = 0; q < SCAN_ITEMS; ++q) {
+    const long long idx = base + threadIdx.x * SCAN_ITEMS + q;
+    if (idx < n) out[idx] = run;
+    run += v[q];
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) out[n] = run;
+}
+
+// ---------------------------------------------------------------------------
+// conversions and diagnostics
+// ---------------------------------------------------------------------------
+
+// FP64 position -> (cell, offset): the reference's cell rules on a uniform
+// grid (x, z: q(i) < x <= q(i+1); y: floor(y/dy)), offsets in cell units.
+__device__ __forceinline__ bool split_axis(double x, double q1, double d, int n, bool upper_closed, int& c, float& o) {
+  const double u = (x - q1) / d;  // position in cells from node 1
+  int i = upper_closed ? (int)ceil(u) - 1 : (int)floor(u);
+  if (i < 0 || i >= n) return false;
+  double f = u - (double)i;
+  if (upper_closed) { if (f <= 0.0) f = 1e-7; if (f > 1.0) f = 1.0; }
+  else { if (f < 0.0) f = 0.0; if (f >= 1.0) f = 0.99999994; }
+  c = i;
+  o = (float)f;
+  if (upper_closed && o <= 0.0f) o = 1e-7f;
+  if (!upper_closed && o >= 1.0f) o = 0.99999994f;
+  return true;
+}
+
+__global__ void k_from_f64(G32 g, long long N, long long NM, const double* __restrict__ xp,
+                           const double* __restrict__ vp, const double* __restrict__ vp1,
+                           const double* __restrict__ mrat, const double* __restrict__ beta_p, Species sp, Part p,
+                           int* err) {
+  GSTRIDE(l, N) {
+    int ci = 0, cj = 0, ck = 0;
+    float ox = 0.5f, oy = 0.5f, oz = 0.5f;
+    const bool ok = split_axis(xp[l], g.qx1, g.dx, g.ncx, true, ci, ox) &&
+                    split_axis(xp[l + NM], g.qy1, g.dy, g.ncy, false, cj, oy) &&
+                    split_axis(xp[l + 2 * NM], g.qz1, g.dz, g.ncz, true, ck, oz);
+    if (!ok) set_err(err, KERR_DOMAIN);
+    p.cell[l] = pk(ci, cj, ck);
+    p.ox[l] = ox; p.oy[l] = oy; p.oz[l] = oz;
+    p.vx[l] = (float)vp[l]; p.vy[l] = (float)vp[l + NM]; p.vz[l] = (float)vp[l + 2 * NM];
+    p.wx[l] = (float)vp1[l]; p.wy[l] = (float)vp1[l + NM]; p.wz[l] = (float)vp1[l + 2 * NM];
+  }
+}
+
+__global__ void k_assign_species(long long N, const double* __restrict__ mrat, const double* __restrict__ beta_p,
+                                 const double* __restrict__ tab_mrat, const double* __restrict__ tab_bp, int n,
+                                 uint8_t* __restrict__ spid, int* miss) {
+  GSTRIDE(l, N) {
+    int s = -1;
+    for (int q = 0; q < n; ++q)
+      if (tab_mrat[q] == mrat[l] && tab_bp[q] == beta_p[l]) { s = q; break; }
+    if (s < 0) {
+      atomicCAS(miss, -1, (int)(l & 0x7fffffff));
+      s = 0;
+    }
+    spid[l] = (uint8_t)s;
+  }
+}
+
+__global__ void k_to_f64(G32 g, long long N, long long NM, Part p, double* __restrict__ xp, double* __restrict__ vp,
+                         double* __restrict__ vp1) {
+  GSTRIDE(l, N) {
+    const int32_t c = p.cell[l];
+    xp[l] = g.qx1 + ((double)pk_i(c) + (double)p.ox[l]) * (double)g.dx;
+    xp[l + NM] = g.qy1 + ((double)pk_j(c) + (double)p.oy[l]) * (double)g.dy;
+    xp[l + 2 * NM] = g.qz1 + ((double)pk_k(c) + (double)p.oz[l]) * (double)g.dz;
+    vp[l] = p.vx[l]; vp[l + NM] = p.vy[l]; vp[l + 2 * NM] = p.vz[l];
+    vp1[l] = p.wx[l]; vp1[l + NM] = p.wy[l]; vp1[l + 2 * NM] = p.wz[l];
+  }
+}
+
+__global__ void k_keys(G32 g, long long N, const int32_t* __restrict__ cell, int32_t* __restrict__ key) {
+  GSTRIDE(l, N) {
+    const int32_t c = cell[l];
+    key[l] = (int32_t)key_of(g, pk_i(c), pk_j(c), pk_k(c));
+  }
+}
+
+// Keys non-decreasing?  Counts per key (for the cell starts).
+__global__ void k_sorted_hist(long long N, const int32_t* __restrict__ key, long long nkeys, int* unsorted,
+                              int64_t* __restrict__ count) {
+  GSTRIDE(l, N) {
+    const int32_t k = key[l];
+    if (l + 1 < N && key[l + 1] < k) atomicExch(unsorted, 1);
+    if (k >= 0 && k < nkeys) atomicAdd(reinterpret_cast<unsigned long long*>(count + k), 1ull);
+    else atomicExch(unsorted, 2);
+  }
+}
+
+__global__ void k_gather_perm(long long N, const int64_t* __restrict__ perm, Part s, Part d) {
+  GSTRIDE(l, N) {
+    const long long q = perm[l];
+    d.cell[l] = s.cell[q];
+    d.ox[l] = s.ox[q]; d.oy[l] = s.oy[q]; d.oz[l] = s.oz[q];
+    d.vx[l] = s.vx[q]; d.vy[l] = s.vy[q]; d.vz[l] = s.vz[q];
+    d.wx[l] = s.wx[q]; d.wy[l] = s.wy[q]; d.wz[l] = s.wz[q];
+    if (s.sp) d.sp[l] = s.sp[q];
+  }
+}
+
+__global__ void k_f64_to_f32(long long n, const double* __restrict__ a, const double* __restrict__ b,
+                             float* __restrict__ out) {
+  GSTRIDE(t, n) out[t] = (float)(b ? a[t] - b[t] : a[t]);
+}
+
+__global__ void k_f32_to_f64(long long n, const float* __restrict__ a, double* __restrict__ out) {
+  GSTRIDE(t, n) out[t] = (double)a[t];
+}
+
+__device__ __forceinline__ double bsum(double v) {
+  __shared__ double sh[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (w == 0) {
+    r = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+  }
+  return r;
+}
+
+__global__ void k_energy_p(long long N, Part p, Species sp, double vol, double* acc) {
+  double s = 0.0;
+  GSTRIDE(l, N) {
+    const int q = p.sp ? min((int)p.sp[l], MAX_SPECIES - 1) : 0;
+    const double v2 = (double)p.vx[l] * p.vx[l] + (double)p.vy[l] * p.vy[l] + (double)p.vz[l] * p.vz[l];
+    // 0.5 m v^2 with m = 1/mrat, times the particle's weight 1/(beta*beta_p) = qw*vol
+    s += 0.5 * (1.0 / (double)sp.mrat[q]) * v2 * (double)sp.qw[q] * vol;
+  }
+  s = bsum(s);
+  if (threadIdx.x == 0) atomicAdd(acc, s);
+}
+
+__global__ void k_energy_f(G32 g, const double* __restrict__ b0, const double* __restrict__ b1,
+                           const float* __restrict__ E, double alpha, double vol, double* acc) {
+  double s1 = 0, s2 = 0, s3 = 0;
+  GSTRIDE(t, n_int(g)) {
+    int i, j, k;
+    interior_of(g, t, i, j, k);
+    const long long o = nid(g, i, j, k);
+    for (int m = 0; m < 3; ++m) {
+      const double bb = b1[o + g.C * m], d = bb - b0[o + g.C * m], e = E[o + g.C * m];
+      s1 += 0.5 * d * d * vol / alpha;
+      s2 += 0.5 * bb * bb * vol / alpha;
+      s3 += 0.5 * e * e * vol;
+    }
+  }
+  s1 = bsum(s1);
+  if (threadIdx.x == 0) atomicAdd(acc + 1, s1);
+  s2 = bsum(s2);
+  if (threadIdx.x == 0) atomicAdd(acc + 2, s2);
+  s3 = bsum(s3);
+  if (threadIdx.x == 0) atomicAdd(acc + 3, s3);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+#define RET(...)                 \
+  do {                           \
+    __VA_ARGS__;                 \
+    return cudaGetLastError();   \
+  } while (0)
+
+cudaError_t pass(int which, const G32& g, const Part& p, const Species& sp, const StepParams& s, const int64_t* start,
+                 const float4* kit, float* partial, int* err, cudaStream_t st) {
+  const unsigned grid = (unsigned)g.nbricks;
+  if (which == 1) RET((k_pass<1><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, partial, err)));
+  if (which == 2) RET((k_pass<2><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, partial, err)));
+  RET((k_pass<3><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, partial, err)));
+}
+cudaError_t node_sum(const G32& g, const float* partial, int nq, float* np, float* S, cudaStream_t st) {
+  RET((k_node_sum<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, partial, nq, np, S)));
+}
+cudaError_t ghost_fill(const G32& g, float* f, int ncomp, cudaStream_t st) {
+  RET((k_ghost<<<nblk(g.C), TPB, 0, st>>>(g, f, ncomp)));
+}
+cudaError_t ct_and_up(const G32& g, const float* np, const float* S, float* up, cudaStream_t st) {
+  RET((k_ct_up<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, const_cast<float*>(np), S, up)));
+}
+cudaError_t build_kit(const G32& g, const float* aj, const float* up, const float* dbt, const float* b0c, float4* kit,
+                      cudaStream_t st) {
+  RET((k_kit<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, aj, up, dbt, b0c, kit)));
+}
+cudaError_t curlB32(const G32& g, const float* dbt, const float* np, float alpha, float* aj, cudaStream_t st) {
+  RET((k_curlB<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, dbt, np, alpha, aj)));
+}
+cudaError_t half_sum32(const G32& g, const float* a, const float* b, float* out, cudaStream_t st) {
+  RET((k_half_sum<<<nblk(3 * g.C), TPB, 0, st>>>(3 * g.C, a, b, out)));
+}
+cudaError_t ct_pred(const G32& g, const float* aj, const float* up, const float* dbt, const float* b0c, float* ct,
+                    cudaStream_t st) {
+  RET((k_ct_pred<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, aj, up, dbt, b0c, ct)));
+}
+cudaError_t ct_corr(const G32& g, const float* aj, const float* up, const float* dbtp1, const float* b0c, float* ct,
+                    cudaStream_t st) {
+  RET((k_ct_corr<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, aj, up, dbtp1, b0c, ct)));
+}
+cudaError_t e_field(const G32& g, const float* ct, const float* nu, const float* aj, const float* np, float gp,
+                    float* E, cudaStream_t st) {
+  (void)np;
+  (void)gp;
+  RET((k_E<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, ct, nu, aj, E)));
+}
+cudaError_t b_update(const G32& g, const float* E, const double* base, const double* b0, double coef, double* b1p2,
+                     float* db1p2, cudaStream_t st) {
+  RET((k_bupd<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, E, base, b0, coef, b1p2, db1p2)));
+}
+cudaError_t courant_min(const G32& g, const float* dbt, const float* b0c, const float* np, float alpha, float dx,
+                        float* dtn, float* d_min, cudaStream_t st) {
+  const unsigned init = 0x7f7fffffu;  // FLT_MAX
+  cudaError_t e = cudaMemcpyAsync(d_min, &init, sizeof(init), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  RET((k_courant<<<nblk(g.C), TPB, 0, st>>>(g, dbt, b0c, np, alpha, dx, dtn, reinterpret_cast<unsigned*>(d_min))));
+}
+cudaError_t sort_prep(const G32& g, const int64_t* start, const int32_t* cell, uint32_t* dirrank, uint16_t* dep,
+                      int* err, cudaStream_t st) {
+  const long long warps = g.nkeys;
+  long long blocks = (warps + (TPB / 32) - 1) / (TPB / 32);
+  if (blocks > 65535LL * 16) blocks = 65535LL * 16;
+  RET((k_sort_prep<<<(unsigned)blocks, TPB, 0, st>>>(g, start, cell, dirrank, dep, err)));
+}
+cudaError_t sort_count(const G32& g, const uint16_t* dep, int64_t* count, uint16_t* pre, int* err, cudaStream_t st) {
+  RET((k_sort_count<<<nblk(g.nkeys), TPB, 0, st>>>(g, dep, count, pre, err)));
+}
+cudaError_t scan_exclusive(const int64_t* in, int64_t* out, long long n, int64_t* sums, cudaStream_t st) {
+  const long long nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+  k_scan_reduce<<<(unsigned)(nb < 1 ? 1 : nb), TPB, 0, st>>>(in, n, sums);
+  k_scan_sums<<<1, 1024, 0, st>>>(sums, nb < 1 ? 1 : nb);
+  RET((k_scan_apply<<<(unsigned)(nb < 1 ? 1 : nb), TPB, 0, st>>>(in, n, sums, out)));
+}
+cudaError_t sort_scatter(const G32& g, long long N, const int32_t* cell, const uint32_t* dirrank, const uint16_t* pre,
+                         const int64_t* start_new, const Part& src, const Part& dst, int* err, cudaStream_t st) {
+  if (N <= 0) return cudaSuccess;
+  RET((k_sort_scatter<<<nblk(N), TPB, 0, st>>>(g, N, cell, dirrank, pre, start_new, src, dst, err)));
+}
+cudaError_t from_f64(const G32& g, long long N, long long NM, const double* xp, const double* vp, const double* vp1,
+                     const double* mrat, const double* beta_p, const Species& sp, Part p, int* err, cudaStream_t st) {
+  if (N <= 0) return cudaSuccess;
+  RET((k_from_f64<<<nblk(N), TPB, 0, st>>>(g, N, NM, xp, vp, vp1, mrat, beta_p, sp, p, err)));
+}
+cudaError_t assign_species(long long N, const double* mrat, const double* beta_p, const double* tab_mrat,
+                           const double* tab_bp, int n, uint8_t* spid, int* miss, cudaStream_t st) {
+  if (N <= 0) return cudaSuccess;
+  RET((k_assign_species<<<nblk(N), TPB, 0, st>>>(N, mrat, beta_p, tab_mrat, tab_bp, n, spid, miss)));
+}
+cudaError_t to_f64(const G32& g, long long N, long long NM, const Part& p, double* xp, double* vp, double* vp1,
+                   cudaStream_t st) {
+  if (N <= 0) return cudaSuccess;
+  RET((k_to_f64<<<nblk(N), TPB, 0, st>>>(g, N, NM, p, xp, vp, vp1)));
+}
+cudaError_t keys_of(const G32& g, long long N, const int32_t* cell, int32_t* key, cudaStream_t st) {
+  if (N <= 0) return cudaSuccess;
+  RET((k_keys<<<nblk(N), TPB, 0, st>>>(g, N, cell, key)));
+}
+cudaError_t sorted_hist(long long N, const int32_t* key, long long nkeys, int* unsorted, int64_t* count,
+                        cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(count, 0, (nkeys + 1) * sizeof(int64_t), st);
+  if (e != cudaSuccess) return e;
+  if (N <= 0) return cudaSuccess;
+  RET((k_sorted_hist<<<nblk(N), TPB, 0, st>>>(N, key, nkeys, unsorted, count)));
+}
+cudaError_t gather_perm(long long N, const int64_t* perm, const Part& src, Part dst, cudaStream_t st) {
+  if (N <= 0) return cudaSuccess;
+  RET((k_gather_perm<<<nblk(N), TPB, 0, st>>>(N, perm, src, dst)));
+}
+cudaError_t grid_f64_to_f32(long long n, const double* a, const double* b, float* out, cudaStream_t st) {
+  RET((k_f64_to_f32<<<nblk(n), TPB, 0, st>>>(n, a, b, out)));
+}
+cudaError_t grid_f32_to_f64(long long n, const float* a, double* out, cudaStream_t st) {
+  RET((k_f32_to_f64<<<nblk(n), TPB, 0, st>>>(n, a, out)));
+}
+cudaError_t energy32(const G32& g, long long N, const Part& p, const Species& sp, double vol, const double* b0,
+                     const double* b1, const float* E, double alpha, double* acc4, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(acc4, 0, 4 * sizeof(double), st);
+  if (e != cudaSuccess) return e;
+  if (N > 0) {
+    k_energy_p<<<nblk(N), TPB, 0, st>>>(N, p, sp, vol, acc4);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  RET((k_energy_f<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, b0, b1, E, alpha, vol, acc4)));
+}
+
+}  // namespace swapk32

@@ -1,0 +1,125 @@
+// k32.cuh -- the FP32 form of the ion step: device structures and launchers.
+//
+// Particles: packed int32 cell (ci | cj<<10 | ck<<20, 0-based physical cells)
+// plus FP32 offsets inside the cell, FP32 v and vp1, a species byte.  They
+// are kept sorted by a brick-major key (bricks of 4x4x4 cells), so one CTA
+// owns one brick's particles as a contiguous range.  Grids keep the
+// reference's (nx,ny,nz[,3]) layout with ghosts; B is accumulated in FP64
+// and its perturbation dB = B - b0 is mirrored in FP32 for the stencils.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace swapk32 {
+
+constexpr int BR = 4;                 // brick edge (cells)
+constexpr int BCELLS = BR * BR * BR;  // 64 cells per brick
+constexpr int TN = BR + 3;            // tile nodes per axis: brick + one-cell mover halo
+constexpr int TNODES = TN * TN * TN;  // 343
+constexpr int NDIR = 27;              // displacements in {-1,0,1}^3
+constexpr int MAX_SPECIES = 16;
+
+struct G32 {
+  int nx, ny, nz;     // nodes incl. ghosts
+  int ncx, ncy, ncz;  // physical cells
+  int nbx, nby, nbz;  // bricks
+  long long C;        // nodes
+  long long nkeys;    // bricks * 64
+  long long nbricks;
+  float dx, dy, dz, inv_dx, inv_dy, inv_dz;
+  double qx1, qy1, qz1;  // q(1) per axis
+};
+
+struct Part {
+  int32_t* cell;
+  float *ox, *oy, *oz;
+  float *vx, *vy, *vz;
+  float *wx, *wy, *wz;  // vp1
+  uint8_t* sp;
+};
+
+struct Species {
+  float mrat[MAX_SPECIES];
+  float qw[MAX_SPECIES];  // 1/(dx*dy*dz*beta*beta_p): density weight of one particle
+  int n;
+};
+
+struct StepParams {
+  float dt;
+  int pending_move;  // P1: apply the previous step's final half move first
+};
+
+__host__ __device__ __forceinline__ int pk_i(int32_t c) { return c & 1023; }
+__host__ __device__ __forceinline__ int pk_j(int32_t c) { return (c >> 10) & 1023; }
+__host__ __device__ __forceinline__ int pk_k(int32_t c) { return (c >> 20) & 1023; }
+__host__ __device__ __forceinline__ int32_t pk(int i, int j, int k) { return i | (j << 10) | (k << 20); }
+
+__host__ __device__ __forceinline__ long long key_of(const G32& g, int i, int j, int k) {
+  const long long b = (long long)(i >> 2) + (long long)g.nbx * ((j >> 2) + (long long)g.nby * (k >> 2));
+  return b * BCELLS + (i & 3) + 4 * (j & 3) + 16 * (k & 3);
+}
+__host__ __device__ __forceinline__ void cell_of_key(const G32& g, long long key, int& i, int& j, int& k) {
+  const long long b = key / BCELLS;
+  const int l = (int)(key % BCELLS);
+  const int bi = (int)(b % g.nbx), bj = (int)((b / g.nbx) % g.nby), bk = (int)(b / ((long long)g.nbx * g.nby));
+  i = bi * 4 + (l & 3);
+  j = bj * 4 + ((l >> 2) & 3);
+  k = bk * 4 + (l >> 4);
+}
+
+// ---- particle passes ----
+// P1: [final half move of the previous step], deposit np and up at
+//     v_n = 1.5 v - 0.5 vp1 (maind.f:479, 385-387, 399).
+// P2: gather, Ep, v-/v+, deposit up at 0.5(v+ + v-) (maind.f:400-402).
+// P3: gather, Ep, v-/v+, vp1 = v, v = v+ + dt/2 Ep, half move, deposit np and
+//     up at v (maind.f:404-413).
+cudaError_t pass(int which, const G32& g, const Part& p, const Species& sp, const StepParams& sprm,
+                 const int64_t* start, const float4* kit, float* partial, int* err, cudaStream_t st);
+// Sum the brick partial tiles into np and S (interior nodes, (nx,ny,nz) layout).
+cudaError_t node_sum(const G32& g, const float* partial, int nq, float* np, float* S, cudaStream_t st);
+
+// ---- fields ----
+cudaError_t ghost_fill(const G32& g, float* f, int ncomp, cudaStream_t st);
+cudaError_t ct_and_up(const G32& g, const float* np, const float* S, float* up, cudaStream_t st);
+cudaError_t build_kit(const G32& g, const float* aj, const float* up, const float* dbt, const float* b0c,
+                      float4* kit, cudaStream_t st);
+cudaError_t curlB32(const G32& g, const float* dbt, const float* np, float alpha, float* aj, cudaStream_t st);
+cudaError_t half_sum32(const G32& g, const float* a, const float* b, float* out, cudaStream_t st);
+cudaError_t ct_pred(const G32& g, const float* aj, const float* up, const float* dbt, const float* b0c,
+                    float* ct, cudaStream_t st);
+cudaError_t ct_corr(const G32& g, const float* aj, const float* up, const float* dbtp1, const float* b0c,
+                    float* ct, cudaStream_t st);
+cudaError_t e_field(const G32& g, const float* ct, const float* nu, const float* aj, const float* np, float gp,
+                    float* E, cudaStream_t st);
+cudaError_t b_update(const G32& g, const float* E, const double* base, const double* b0, double coef, double* b1p2,
+                     float* db1p2, cudaStream_t st);
+cudaError_t courant_min(const G32& g, const float* dbt, const float* b0c, const float* np, float alpha, float dx,
+                        float* dtn, float* d_min, cudaStream_t st);
+
+// ---- sort ----
+cudaError_t sort_prep(const G32& g, const int64_t* start, const int32_t* cell, uint32_t* dirrank, uint16_t* dep,
+                      int* err, cudaStream_t st);
+cudaError_t sort_count(const G32& g, const uint16_t* dep, int64_t* count, uint16_t* pre, int* err, cudaStream_t st);
+cudaError_t scan_exclusive(const int64_t* in, int64_t* out, long long n, int64_t* block_sums, cudaStream_t st);
+cudaError_t sort_scatter(const G32& g, long long N, const int32_t* cell, const uint32_t* dirrank, const uint16_t* pre,
+                         const int64_t* start_new, const Part& src, const Part& dst, int* err, cudaStream_t st);
+
+// ---- conversions ----
+cudaError_t from_f64(const G32& g, long long N, long long NM, const double* xp, const double* vp, const double* vp1,
+                     const double* mrat, const double* beta_p, const Species& sp, Part p, int* err,
+                     cudaStream_t st);
+cudaError_t to_f64(const G32& g, long long N, long long NM, const Part& p, double* xp, double* vp, double* vp1,
+                   cudaStream_t st);
+cudaError_t keys_of(const G32& g, long long N, const int32_t* cell, int32_t* key, cudaStream_t st);
+cudaError_t gather_perm(long long N, const int64_t* perm, const Part& src, Part dst, cudaStream_t st);
+cudaError_t sorted_hist(long long N, const int32_t* key, long long nkeys, int* unsorted, int64_t* count,
+                        cudaStream_t st);
+cudaError_t grid_f64_to_f32(long long n, const double* a, const double* b, float* out, cudaStream_t st);
+cudaError_t grid_f32_to_f64(long long n, const float* a, double* out, cudaStream_t st);
+cudaError_t assign_species(long long N, const double* mrat, const double* beta_p, const double* tab_mrat,
+                           const double* tab_bp, int n, uint8_t* spid, int* miss, cudaStream_t st);
+cudaError_t energy32(const G32& g, long long N, const Part& p, const Species& sp, double vol, const double* b0,
+                     const double* b1, const float* E, double alpha, double* acc4, cudaStream_t st);
+
+}  // namespace swapk32

@@ -10,7 +10,9 @@
 //  * the velocity sampler keeps the reference's form
 //    v = u + vth*sqrt(-ln U)*cos(pi*U') per component (part_init.f:204-206),
 //    i.e. a Gaussian of standard deviation vth/sqrt(2).
-// Particles come out in cell order, x fastest, so the load is cell-sorted.
+// Particles come out cell-sorted: by bricks of 4x4x4 cells (the order of the
+// FP32 form) when every axis has a multiple of 4 physical cells, otherwise
+// by cell with x fastest.
 #include <cmath>
 #include <cstdint>
 
@@ -27,12 +29,22 @@ extern "C" int swap_load_maxwellian_host(const swap_dims* d, const swap_coords* 
   if (first + n > d->ni_max) return SWAP_ECAPACITY;
   const int64_t NM = d->ni_max;
   const double pi = 3.14159265358979323846;
+  const bool bricks = ncx % 4 == 0 && ncy % 4 == 0 && ncz % 4 == 0;
+  const int64_t nbx = ncx / 4, nby = ncy / 4;
 #pragma omp parallel for schedule(static)
   for (int64_t id = 0; id < n; ++id) {
     const int64_t cell = id / s->ppc;
-    const int ci = (int)(cell % ncx);
-    const int cj = (int)((cell / ncx) % ncy);
-    const int ck = (int)(cell / (ncx * ncy));
+    int ci, cj, ck;
+    if (bricks) {
+      const int64_t b = cell / 64, l = cell % 64;
+      ci = (int)(b % nbx) * 4 + (int)(l & 3);
+      cj = (int)((b / nbx) % nby) * 4 + (int)((l >> 2) & 3);
+      ck = (int)(b / (nbx * nby)) * 4 + (int)(l >> 4);
+    } else {
+      ci = (int)(cell % ncx);
+      cj = (int)((cell / ncx) % ncy);
+      ck = (int)(cell / (ncx * ncy));
+    }
     double u[12];
     swapk::particle_uniforms(s->seed, s->stream, (uint64_t)id, 0u, u);
     // cell (i,j,k) spans nodes i..i+1 (1-based), i = ci+1; coords are 0-based

@@ -443,6 +443,7 @@ extern "C" int swap_init(swap_ctx** out, const swap_dims* d, const swap_params* 
 extern "C" int swap_finalize(swap_ctx* c) {
   if (!c) return SWAP_EINVAL;
   if (c->st) cudaStreamSynchronize(c->st);
+  swap_f32_free(c);
   for (auto& kv : c->reg) cudaFree(kv.second.dev);
   for (void* p : c->owned) cudaFree(p);
   if (c->t0) cudaEventDestroy(c->t0);

@@ -66,6 +66,7 @@ struct swap_ctx {
   // particle work arrays of the fused step (maind.f locals Ep, vplus, vminus)
   double *w_Ep = nullptr, *w_vplus = nullptr, *w_vminus = nullptr;
   double last_dtsub = 0, last_ntf = 0;
+  void* f32_state = nullptr;  // the FP32 form (swap_f32.cu)
 
   cudaEvent_t t0 = nullptr, t1 = nullptr;
 
@@ -88,3 +89,5 @@ struct swap_ctx {
   swapk::PartDev part_view();
   void prof_free();
 };
+
+void swap_f32_free(swap_ctx* c);

@@ -1,0 +1,465 @@
+// swap_f32.cu -- the FP32 form of the ion step behind the same context.
+//
+// swap_f32_begin converts the bound FP64 state (device mirrors) into the
+// FP32 form and sorts the particles by brick-major cell key; swap_f32_run
+// advances whole ion steps (maind.f:385-479); swap_f32_end writes the state
+// back into the bound arrays' device mirrors (particles come back in sorted
+// order).  Precision: particle positions as int32 cell + FP32 offset, FP32
+// velocities and moments, FP64 accumulation of B across subcycles.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/swap_gpu.h"
+#include "k32.cuh"
+#include "swap_ctx.h"
+#include "swap_prof.h"
+
+using namespace swapk32;
+
+struct F32State {
+  G32 g{};
+  Species sp{};
+  long long N = 0;
+  Part buf[2]{};
+  int cur = 0;
+  int64_t *start = nullptr, *start_new = nullptr, *count = nullptr, *sums = nullptr;
+  uint32_t* dirrank = nullptr;
+  uint16_t* dep = nullptr;
+  uint16_t* pre = nullptr;
+  float* partial = nullptr;
+  float4* kit = nullptr;
+  float *np = nullptr, *S = nullptr, *up = nullptr, *aj = nullptr, *ct = nullptr, *E = nullptr, *nu = nullptr;
+  float *db1 = nullptr, *db1p2 = nullptr, *dbtp1 = nullptr;
+  double *b0 = nullptr, *b1 = nullptr, *b12 = nullptr, *b1p2 = nullptr;
+  float* b0c = nullptr;  // 3 floats: the uniform b0
+  float* dtn = nullptr;  // per-node Courant time
+  float* d_min = nullptr;
+  double* acc = nullptr;
+  bool pending_move = false;
+  double last_dtsub = 0, last_ntf = 0;
+  std::vector<void*> owned;
+
+  ~F32State() {
+    for (void* p : owned) cudaFree(p);
+  }
+  template <class T>
+  T* alloc(std::size_t n) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, n * sizeof(T) + 64) != cudaSuccess) return nullptr;
+    owned.push_back(p);
+    return static_cast<T*>(p);
+  }
+};
+
+static F32State* f32(swap_ctx* c) { return static_cast<F32State*>(c->f32_state); }
+
+void swap_f32_free(swap_ctx* c) {
+  delete f32(c);
+  c->f32_state = nullptr;
+}
+
+#define TRY(x)             \
+  do {                     \
+    int _r = (x);          \
+    if (_r) return _r;     \
+  } while (0)
+#define KL(name, x)                                           \
+  do {                                                        \
+    ProfScope _ps(c, name, c->st);                            \
+    cudaError_t _e = (x);                                     \
+    if (_e != cudaSuccess) return c->cuda_fail(_e, name);     \
+  } while (0)
+#define CU(x)                                                 \
+  do {                                                        \
+    cudaError_t _e = (x);                                     \
+    if (_e != cudaSuccess) return c->cuda_fail(_e, #x);       \
+  } while (0)
+
+static int check_err(swap_ctx* c) {
+  int herr = 0;
+  CU(cudaMemcpyAsync(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  CU(cudaStreamSynchronize(c->st));
+  if (herr) {
+    cudaMemset(c->d_err, 0, sizeof(int));
+    if (herr == 3) return c->fail(SWAP_EDOMAIN, "a particle lies outside the grid");
+    if (herr == 7)
+      return c->fail(SWAP_EMOVE, "a particle moved more than one cell per axis since the last sort (|v| dt > dx)");
+    return c->fail(SWAP_ECUDA, "device error flag " + std::to_string(herr));
+  }
+  return SWAP_OK;
+}
+
+// ---------------------------------------------------------------------------
+
+extern "C" int swap_f32_begin(swap_ctx* c) {
+  if (!c) return SWAP_EINVAL;
+  TRY(c->begin());
+  if (!c->h_xp || !c->h_b1) return c->fail(SWAP_EINVAL, "swap_bind_particles and swap_bind_fields are required");
+  if (c->prm.grad_pe != 0.0) return c->fail(SWAP_EINVAL, "the FP32 form has no electron-pressure term");
+  const int nx = c->dims.nx, ny = c->dims.ny, nz = c->dims.nz;
+  const int ncx = nx - 2, ncy = ny - 2, ncz = nz - 2;
+  if (ncx % 4 || ncy % 4 || ncz % 4 || ncx < 8 || ncy < 8 || ncz < 8 || ncx > 1024 || ncy > 1024 || ncz > 1024)
+    return c->fail(SWAP_EINVAL, "the FP32 form needs 8..1024 physical cells per axis, multiples of 4");
+  // uniform spacing per axis
+  auto uniform = [](const std::vector<double>& q) {
+    const double d = q[1] - q[0];
+    for (std::size_t i = 1; i < q.size(); ++i)
+      if (std::fabs((q[i] - q[i - 1]) - d) > 1e-9 * std::fabs(d)) return false;
+    return true;
+  };
+  if (!uniform(c->h_qx) || !uniform(c->h_qy) || !uniform(c->h_qz))
+    return c->fail(SWAP_EINVAL, "the FP32 form needs a uniform grid on every axis");
+  swap_f32_free(c);
+  auto* s = new F32State();
+  c->f32_state = s;
+  G32& g = s->g;
+  g.nx = nx; g.ny = ny; g.nz = nz;
+  g.ncx = ncx; g.ncy = ncy; g.ncz = ncz;
+  g.nbx = ncx / 4; g.nby = ncy / 4; g.nbz = ncz / 4;
+  g.C = (long long)nx * ny * nz;
+  g.nbricks = (long long)g.nbx * g.nby * g.nbz;
+  g.nkeys = g.nbricks * BCELLS;
+  const double dx = c->h_qx[1] - c->h_qx[0], dy = c->h_qy[1] - c->h_qy[0], dz = c->h_qz[1] - c->h_qz[0];
+  g.dx = (float)dx; g.dy = (float)dy; g.dz = (float)dz;
+  g.inv_dx = (float)(1.0 / dx); g.inv_dy = (float)(1.0 / dy); g.inv_dz = (float)(1.0 / dz);
+  g.qx1 = c->h_qx[0]; g.qy1 = c->h_qy[0]; g.qz1 = c->h_qz[0];
+
+  // bound FP64 state on the device
+  double *xp, *vp, *vp1, *mrat, *beta_p, *b0, *b1, *b12, *npd, *nud;
+  TRY(c->use(c->h_xp, Access::In, &xp));
+  TRY(c->use(c->h_vp, Access::In, &vp));
+  TRY(c->use(c->h_vp1, Access::In, &vp1));
+  TRY(c->use(c->h_mrat, Access::In, &mrat));
+  TRY(c->use(c->h_beta_p, Access::In, &beta_p));
+  TRY(c->use(c->h_b0, Access::In, &b0));
+  TRY(c->use(c->h_b1, Access::In, &b1));
+  TRY(c->use(c->h_b12, Access::In, &b12));
+  TRY(c->use(c->h_np, Access::In, &npd));
+  TRY(c->use(c->h_nu, Access::In, &nud));
+  const long long N = c->ntot(), NM = c->dims.ni_max;
+  s->N = N;
+
+  // b0 must be uniform for the FP32 stencils (curl b0 = 0); read it back
+  std::vector<double> hb0(3 * (std::size_t)g.C);
+  CU(cudaMemcpy(hb0.data(), b0, hb0.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int m = 0; m < 3; ++m)
+    for (std::size_t o = 0; o < (std::size_t)g.C; ++o)
+      if (hb0[m * g.C + o] != hb0[m * g.C]) return c->fail(SWAP_EINVAL, "the FP32 form needs a uniform b0");
+  const float hb0c[3] = {(float)hb0[0], (float)hb0[g.C], (float)hb0[2 * g.C]};
+
+  // species table from the (mrat, beta_p) pairs present
+  std::vector<double> hm((std::size_t)N), hb((std::size_t)N);
+  if (N > 0) {
+    CU(cudaMemcpy(hm.data(), mrat, N * sizeof(double), cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(hb.data(), beta_p, N * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  std::vector<double> tm, tb;
+  for (long long l = 0; l < N; ++l) {
+    if (!tm.empty() && tm.back() == hm[l] && tb.back() == hb[l]) continue;
+    bool found = false;
+    for (std::size_t q = 0; q < tm.size(); ++q)
+      if (tm[q] == hm[l] && tb[q] == hb[l]) found = true;
+    if (!found) {
+      if (tm.size() == MAX_SPECIES) return c->fail(SWAP_ECAPACITY, "more than 16 (mrat, beta_p) species");
+      tm.push_back(hm[l]);
+      tb.push_back(hb[l]);
+    }
+  }
+  if (tm.empty()) { tm.push_back(1.0); tb.push_back(1.0); }
+  s->sp.n = (int)tm.size();
+  for (int q = 0; q < s->sp.n; ++q) {
+    s->sp.mrat[q] = (float)tm[q];
+    s->sp.qw[q] = (float)(1.0 / (dx * dy * dz * c->prm.beta * tb[q]));
+  }
+
+  // allocations
+  const std::size_t NMs = (std::size_t)std::max<long long>(NM, 1);
+  for (int k = 0; k < 2; ++k) {
+    Part& p = s->buf[k];
+    p.cell = s->alloc<int32_t>(NMs);
+    p.ox = s->alloc<float>(NMs); p.oy = s->alloc<float>(NMs); p.oz = s->alloc<float>(NMs);
+    p.vx = s->alloc<float>(NMs); p.vy = s->alloc<float>(NMs); p.vz = s->alloc<float>(NMs);
+    p.wx = s->alloc<float>(NMs); p.wy = s->alloc<float>(NMs); p.wz = s->alloc<float>(NMs);
+    p.sp = s->alloc<uint8_t>(NMs);
+    if (!p.cell || !p.ox || !p.oy || !p.oz || !p.vx || !p.vy || !p.vz || !p.wx || !p.wy || !p.wz || !p.sp)
+      return c->fail(SWAP_ECUDA, "FP32 particle allocation failed");
+  }
+  const std::size_t C = (std::size_t)g.C, nk = (std::size_t)g.nkeys;
+  s->start = s->alloc<int64_t>(nk + 1);
+  s->start_new = s->alloc<int64_t>(nk + 1);
+  s->count = s->alloc<int64_t>(nk + 1);
+  s->sums = s->alloc<int64_t>(nk / 1024 + 16);
+  s->dirrank = s->alloc<uint32_t>(NMs);
+  s->dep = s->alloc<uint16_t>(nk * NDIR);
+  s->pre = s->alloc<uint16_t>(nk * NDIR);
+  s->partial = s->alloc<float>((std::size_t)g.nbricks * 4 * TNODES);
+  s->kit = s->alloc<float4>(2 * (std::size_t)ncx * ncy * ncz);
+  s->np = s->alloc<float>(C); s->S = s->alloc<float>(3 * C); s->up = s->alloc<float>(3 * C);
+  s->aj = s->alloc<float>(3 * C); s->ct = s->alloc<float>(3 * C); s->E = s->alloc<float>(3 * C);
+  s->nu = s->alloc<float>(C);
+  s->db1 = s->alloc<float>(3 * C); s->db1p2 = s->alloc<float>(3 * C); s->dbtp1 = s->alloc<float>(3 * C);
+  s->b0 = s->alloc<double>(3 * C); s->b1 = s->alloc<double>(3 * C); s->b12 = s->alloc<double>(3 * C);
+  s->b1p2 = s->alloc<double>(3 * C);
+  s->b0c = s->alloc<float>(4);
+  s->d_min = s->alloc<float>(4);
+  s->dtn = s->alloc<float>(C);
+  s->acc = s->alloc<double>(4);
+  if (!s->start || !s->start_new || !s->count || !s->sums || !s->dirrank || !s->dep || !s->pre || !s->partial || !s->kit ||
+      !s->np || !s->S || !s->up || !s->aj || !s->ct || !s->E || !s->nu || !s->db1 || !s->db1p2 || !s->dbtp1 ||
+      !s->b0 || !s->b1 || !s->b12 || !s->b1p2 || !s->b0c || !s->d_min || !s->acc || !s->dtn)
+    return c->fail(SWAP_ECUDA, "FP32 grid allocation failed");
+  CU(cudaMemsetAsync(s->np, 0, C * sizeof(float), c->st));
+  for (void* p : {(void*)s->S, (void*)s->up, (void*)s->aj, (void*)s->ct, (void*)s->E})
+    CU(cudaMemsetAsync(p, 0, 3 * C * sizeof(float), c->st));
+  CU(cudaMemcpyAsync(s->b0c, hb0c, 3 * sizeof(float), cudaMemcpyHostToDevice, c->st));
+
+  // fields: FP64 levels copied, dB = B - b0 in FP32, nu in FP32
+  const std::size_t b3 = 3 * C * sizeof(double);
+  CU(cudaMemcpyAsync(s->b0, b0, b3, cudaMemcpyDeviceToDevice, c->st));
+  CU(cudaMemcpyAsync(s->b1, b1, b3, cudaMemcpyDeviceToDevice, c->st));
+  CU(cudaMemcpyAsync(s->b12, b12, b3, cudaMemcpyDeviceToDevice, c->st));
+  CU(grid_f64_to_f32(3 * g.C, b1, b0, s->db1, c->st));
+  CU(grid_f64_to_f32(g.C, nud, nullptr, s->nu, c->st));
+
+  // particles: convert, assign species, sort by key (host counting sort, once)
+  Part& tmp = s->buf[1];
+  CU(from_f64(g, N, NM, xp, vp, vp1, mrat, beta_p, s->sp, tmp, c->d_err, c->st));
+  {
+    double* tabm = s->alloc<double>(MAX_SPECIES);
+    double* tabb = s->alloc<double>(MAX_SPECIES);
+    int* miss = s->alloc<int>(1);
+    if (!tabm || !tabb || !miss) return c->fail(SWAP_ECUDA, "allocation");
+    CU(cudaMemcpyAsync(tabm, tm.data(), tm.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CU(cudaMemcpyAsync(tabb, tb.data(), tb.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CU(cudaMemsetAsync(miss, 0xff, sizeof(int), c->st));
+    CU(assign_species(N, mrat, beta_p, tabm, tabb, (int)tm.size(), tmp.sp, miss, c->st));
+  }
+  TRY(check_err(c));
+  int32_t* keys = reinterpret_cast<int32_t*>(s->dirrank);
+  CU(keys_of(g, N, tmp.cell, keys, c->st));
+  int* unsorted = s->alloc<int>(1);
+  if (!unsorted) return c->fail(SWAP_ECUDA, "allocation");
+  CU(cudaMemsetAsync(unsorted, 0, sizeof(int), c->st));
+  CU(sorted_hist(N, keys, g.nkeys, unsorted, s->count, c->st));
+  int hun = 0;
+  CU(cudaMemcpyAsync(&hun, unsorted, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  CU(cudaStreamSynchronize(c->st));
+  if (hun == 2) return c->fail(SWAP_EDOMAIN, "a particle lies outside the grid");
+  if (hun == 0) {
+    // already in key order (the product loader and swap_f32_end give that):
+    // starts by scan, particles used as they are
+    CU(scan_exclusive(s->count, s->start, g.nkeys, s->sums, c->st));
+    std::swap(s->buf[0], s->buf[1]);
+  } else {
+    // arbitrary order: one stable counting sort on the host
+    std::vector<int32_t> hk((std::size_t)N);
+    CU(cudaMemcpy(hk.data(), keys, N * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    std::vector<int64_t> cnt(nk + 1, 0), perm((std::size_t)N);
+    for (long long l = 0; l < N; ++l) cnt[(std::size_t)hk[l] + 1]++;
+    for (std::size_t k = 0; k < nk; ++k) cnt[k + 1] += cnt[k];
+    CU(cudaMemcpy(s->start, cnt.data(), (nk + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
+    for (long long l = 0; l < N; ++l) perm[(std::size_t)cnt[(std::size_t)hk[l]]++] = l;
+    void* pbuf = nullptr;
+    CU(cudaMalloc(&pbuf, (std::size_t)std::max<long long>(N, 1) * sizeof(int64_t)));
+    cudaError_t e = cudaMemcpy(pbuf, perm.data(), N * sizeof(int64_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = gather_perm(N, static_cast<int64_t*>(pbuf), tmp, s->buf[0], c->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    cudaFree(pbuf);
+    if (e != cudaSuccess) return c->cuda_fail(e, "initial sort");
+  }
+  s->cur = 0;
+  s->pending_move = false;
+  return check_err(c);
+}
+
+// Deposit finish: node sums -> np (+ghosts) and up (maind.f:386-387 etc.).
+static int finish_deposit(swap_ctx* c, F32State* s, int nq) {
+  KL("f32_node_sum", node_sum(s->g, s->partial, nq, s->np, s->S, c->st));
+  if (nq == 4) KL("f32_ghost_np", ghost_fill(s->g, s->np, 1, c->st));
+  KL("f32_ct_up", ct_and_up(s->g, s->np, s->S, s->up, c->st));
+  return SWAP_OK;
+}
+
+static int subcycles(swap_ctx* c, F32State* s) {
+  const G32& g = s->g;
+  double dtsub = c->prm.dt / (double)c->prm.ntsub;  // maind.f:420-421
+  double ntf = (double)c->prm.ntsub;
+  // check_time_step (gutsf.f:1776-1822): per-node Courant times; when even
+  // the smallest leaves dtsub alone nothing changes, otherwise the
+  // reference's ordered halving (once per violating node, k innermost) is
+  // replayed on the host from the node values.
+  KL("f32_courant", courant_min(g, s->db1, s->b0c, s->np, (float)c->prm.alpha, g.dx, s->dtn, s->d_min, c->st));
+  float mn = 0;
+  CU(cudaMemcpyAsync(&mn, s->d_min, sizeof(float), cudaMemcpyDeviceToHost, c->st));
+  CU(cudaStreamSynchronize(c->st));
+  if ((double)mn <= 2.0 * dtsub) {
+    std::vector<float> h((std::size_t)g.C);
+    CU(cudaMemcpy(h.data(), s->dtn, h.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < g.nx; ++i)
+      for (int j = 0; j < g.ny; ++j)
+        for (int k = 0; k < g.nz; ++k)
+          if ((double)h[(std::size_t)i + (std::size_t)g.nx * (j + (std::size_t)g.ny * k)] <= 2.0 * dtsub) {
+            dtsub /= 2.0;
+            ntf *= 2.0;
+          }
+    if (ntf > 1.0e6) return c->fail(SWAP_ESUBCYCLE, "subcycle count overflow in check_time_step");
+  }
+  s->last_dtsub = dtsub;
+  s->last_ntf = ntf;
+  const int n = (int)ntf;
+  const float alpha = (float)c->prm.alpha;
+  for (int it = 0; it < n; ++it) {
+    KL("f32_curlB", curlB32(g, s->db1, s->np, alpha, s->aj, c->st));                      // maind.f:430
+    KL("f32_ct_pred", ct_pred(g, s->aj, s->up, s->db1, s->b0c, s->ct, c->st));            // get_E
+    KL("f32_E", e_field(g, s->ct, s->nu, s->aj, s->np, 0.f, s->E, c->st));
+    KL("f32_bupd", b_update(g, s->E, s->b12, s->b0, 2.0 * dtsub, s->b1p2, s->db1p2, c->st));  // predict_B
+    KL("f32_half", half_sum32(g, s->db1p2, s->db1, s->dbtp1, c->st));                      // get_Ep1
+    KL("f32_curlB", curlB32(g, s->dbtp1, s->np, alpha, s->aj, c->st));
+    KL("f32_ct_corr", ct_corr(g, s->aj, s->up, s->dbtp1, s->b0c, s->ct, c->st));
+    KL("f32_E", e_field(g, s->ct, s->nu, s->aj, s->np, 0.f, s->E, c->st));
+    KL("f32_bupd", b_update(g, s->E, s->b1, s->b0, dtsub, s->b1p2, s->db1p2, c->st));      // correct_B
+    // f_update_tlev (gutsf.f:10-35): b12 <- b1, b1 <- b1p2 (bt = b1)
+    std::swap(s->b12, s->b1);
+    std::swap(s->b1, s->b1p2);
+    std::swap(s->db1, s->db1p2);
+  }
+  return SWAP_OK;
+}
+
+static int sort_step(swap_ctx* c, F32State* s) {
+  const G32& g = s->g;
+  Part& a = s->buf[s->cur];
+  Part& b = s->buf[1 - s->cur];
+  KL("f32_sort_prep", sort_prep(g, s->start, a.cell, s->dirrank, s->dep, c->d_err, c->st));
+  KL("f32_sort_count", sort_count(g, s->dep, s->count, s->pre, c->d_err, c->st));
+  KL("f32_sort_scan", scan_exclusive(s->count, s->start_new, g.nkeys, s->sums, c->st));
+  KL("f32_sort_scatter", sort_scatter(g, s->N, a.cell, s->dirrank, s->pre, s->start_new, a, b, c->d_err, c->st));
+  std::swap(s->start, s->start_new);
+  s->cur = 1 - s->cur;
+  return SWAP_OK;
+}
+
+static int one_step(swap_ctx* c, F32State* s) {
+  const G32& g = s->g;
+  StepParams sp{(float)c->prm.dt, s->pending_move ? 1 : 0};
+  const Part& p = s->buf[s->cur];
+  KL("f32_P1", pass(1, g, p, s->sp, sp, s->start, s->kit, s->partial, c->d_err, c->st));  // :479,385-387,399
+  TRY(finish_deposit(c, s, 4));
+  KL("f32_curlB", curlB32(g, s->db1, s->np, (float)c->prm.alpha, s->aj, c->st));  // :395
+  KL("f32_kit", build_kit(g, s->aj, s->up, s->db1, s->b0c, s->kit, c->st));       // :398, get_Ep :183-184
+  KL("f32_P2", pass(2, g, p, s->sp, sp, s->start, s->kit, s->partial, c->d_err, c->st));  // :400-402
+  TRY(finish_deposit(c, s, 3));
+  KL("f32_kit", build_kit(g, s->aj, s->up, s->db1, s->b0c, s->kit, c->st));       // :404
+  KL("f32_P3", pass(3, g, p, s->sp, sp, s->start, s->kit, s->partial, c->d_err, c->st));  // :404-413
+  TRY(finish_deposit(c, s, 4));
+  TRY(subcycles(c, s));                                                            // :420-476
+  TRY(sort_step(c, s));
+  s->pending_move = true;                                                          // :479 next P1
+  return SWAP_OK;
+}
+
+extern "C" int swap_f32_run(swap_ctx* c, int32_t nsteps) {
+  if (!c) return SWAP_EINVAL;
+  F32State* s = f32(c);
+  if (!s) return c->fail(SWAP_EINVAL, "swap_f32_begin has not been called");
+  for (int k = 0; k < nsteps; ++k) TRY(one_step(c, s));
+  return check_err(c);
+}
+
+// Apply a pending final half move (maind.f:479) in place.
+static int flush_move(swap_ctx* c, F32State* s) {
+  if (!s->pending_move) return SWAP_OK;
+  StepParams sp{(float)c->prm.dt, 1};
+  KL("f32_P1", pass(1, s->g, s->buf[s->cur], s->sp, sp, s->start, s->kit, s->partial, c->d_err, c->st));
+  s->pending_move = false;
+  return SWAP_OK;
+}
+
+extern "C" int swap_f32_end(swap_ctx* c) {
+  if (!c) return SWAP_EINVAL;
+  F32State* s = f32(c);
+  if (!s) return c->fail(SWAP_EINVAL, "swap_f32_begin has not been called");
+  TRY(c->begin());
+  TRY(flush_move(c, s));
+  double *xp, *vp, *vp1, *b1, *b12, *b1p2, *bt, *npd, *upd, *Ed, *ajd;
+  TRY(c->use(c->h_xp, Access::Out, &xp));
+  TRY(c->use(c->h_vp, Access::Out, &vp));
+  TRY(c->use(c->h_vp1, Access::Out, &vp1));
+  TRY(c->use(c->h_b1, Access::Out, &b1));
+  TRY(c->use(c->h_b12, Access::Out, &b12));
+  TRY(c->use(c->h_b1p2, Access::Out, &b1p2));
+  TRY(c->use(c->h_bt, Access::Out, &bt));
+  TRY(c->use(c->h_np, Access::Out, &npd));
+  TRY(c->use(c->h_up, Access::Out, &upd));
+  TRY(c->use(c->h_E, Access::Out, &Ed));
+  TRY(c->use(c->h_aj, Access::Out, &ajd));
+  const G32& g = s->g;
+  CU(to_f64(g, s->N, c->dims.ni_max, s->buf[s->cur], xp, vp, vp1, c->st));
+  const std::size_t b3 = 3 * (std::size_t)g.C * sizeof(double);
+  CU(cudaMemcpyAsync(b1, s->b1, b3, cudaMemcpyDeviceToDevice, c->st));
+  CU(cudaMemcpyAsync(bt, s->b1, b3, cudaMemcpyDeviceToDevice, c->st));
+  CU(cudaMemcpyAsync(b1p2, s->b1, b3, cudaMemcpyDeviceToDevice, c->st));
+  CU(cudaMemcpyAsync(b12, s->b12, b3, cudaMemcpyDeviceToDevice, c->st));
+  CU(grid_f32_to_f64(g.C, s->np, npd, c->st));
+  CU(grid_f32_to_f64(3 * g.C, s->up, upd, c->st));
+  CU(grid_f32_to_f64(3 * g.C, s->E, Ed, c->st));
+  CU(grid_f32_to_f64(3 * g.C, s->aj, ajd, c->st));
+  int r = c->finish();
+  c->last_dtsub = s->last_dtsub;
+  c->last_ntf = s->last_ntf;
+  return r;
+}
+
+extern "C" int swap_f32_energy(swap_ctx* c, double out[4]) {
+  if (!c || !out) return SWAP_EINVAL;
+  F32State* s = f32(c);
+  if (!s) return c->fail(SWAP_EINVAL, "swap_f32_begin has not been called");
+  const G32& g = s->g;
+  const double vol = (double)g.dx * g.dy * g.dz;
+  CU(energy32(g, s->N, s->buf[s->cur], s->sp, vol, s->b0, s->b1, s->E, c->prm.alpha, s->acc, c->st));
+  CU(cudaMemcpyAsync(out, s->acc, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  CU(cudaStreamSynchronize(c->st));
+  return SWAP_OK;
+}
+
+// Validation entry: displace particles idx[q] (current sorted positions) by
+// the cell steps of dcell[q] (packed like the cell: dx+1 | (dy+1)<<10 |
+// (dz+1)<<20, each step in {-1,0,1}), then run the incremental stable sort
+// that follows every ion step.  Lets a test compare the sort with a stable
+// counting sort of the same keys.
+__global__ void k_displace(G32 g, Part p, long long n, const int64_t* idx, const int32_t* dcell) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+    const long long l = idx[q];
+    const int32_t c = p.cell[l], d = dcell[q];
+    int i = pk_i(c) + pk_i(d) - 1, j = pk_j(c) + pk_j(d) - 1, k = pk_k(c) + pk_k(d) - 1;
+    i = i < 0 ? i + g.ncx : (i >= g.ncx ? i - g.ncx : i);
+    j = j < 0 ? j + g.ncy : (j >= g.ncy ? j - g.ncy : j);
+    k = k < 0 ? k + g.ncz : (k >= g.ncz ? k - g.ncz : k);
+    p.cell[l] = pk(i, j, k);
+  }
+}
+
+extern "C" int swap_f32_displace_resort(swap_ctx* c, int64_t n, const int64_t* idx, const int32_t* dcell) {
+  if (!c || n < 0 || (n > 0 && (!idx || !dcell))) return SWAP_EINVAL;
+  F32State* s = f32(c);
+  if (!s) return c->fail(SWAP_EINVAL, "swap_f32_begin has not been called");
+  for (int64_t q = 0; q < n; ++q) {
+    if (idx[q] < 0 || idx[q] >= s->N) return c->fail(SWAP_EINVAL, "particle index out of range");
+    if (pk_i(dcell[q]) > 2 || pk_j(dcell[q]) > 2 || pk_k(dcell[q]) > 2 || (dcell[q] >> 30))
+      return c->fail(SWAP_EINVAL, "cell steps must be -1, 0 or 1");
+  }
+  if (n > 0) {
+    int64_t* di = s->alloc<int64_t>((std::size_t)n);
+    int32_t* dd = s->alloc<int32_t>((std::size_t)n);
+    if (!di || !dd) return c->fail(SWAP_ECUDA, "allocation");
+    CU(cudaMemcpyAsync(di, idx, n * sizeof(int64_t), cudaMemcpyHostToDevice, c->st));
+    CU(cudaMemcpyAsync(dd, dcell, n * sizeof(int32_t), cudaMemcpyHostToDevice, c->st));
+    k_displace<<<(unsigned)((n + 255) / 256), 256, 0, c->st>>>(s->g, s->buf[s->cur], n, di, dd);
+    CU(cudaGetLastError());
+  }
+  TRY(sort_step(c, s));
+  return check_err(c);
+}

@@ -232,3 +232,26 @@ class Hybrid:
 
     def check_finite(self):
         self._check(self.lib.swap_check_finite(self.ctx))
+
+    # ---- the FP32 form ----
+    def f32_begin(self):
+        """Convert the bound FP64 state into the FP32 form (particles sorted by cell)."""
+        self._check(self.lib.swap_f32_begin(self.ctx))
+
+    def f32_run(self, nsteps: int):
+        self._check(self.lib.swap_f32_run(self.ctx, int(nsteps)))
+
+    def f32_end(self):
+        """Write the FP32 state back into the bound arrays (device copies); then sync_to_host."""
+        self._check(self.lib.swap_f32_end(self.ctx))
+
+    def f32_energy(self):
+        out = np.zeros(4)
+        self._check(self.lib.swap_f32_energy(self.ctx, abi.dptr(out)))
+        return out
+
+    def f32_displace_resort(self, idx, dcell):
+        idx = np.ascontiguousarray(idx, dtype=np.int64)
+        dcell = np.ascontiguousarray(dcell, dtype=np.int32)
+        self._check(self.lib.swap_f32_displace_resort(self.ctx, len(idx), idx.ctypes.data_as(abi.c_int64_p),
+                                                      dcell.ctypes.data_as(abi.c_int32_p)))
