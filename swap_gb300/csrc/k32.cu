@@ -66,15 +66,15 @@ __device__ __forceinline__ long long n_int(const G32& g) { return (long long)g.n
 __device__ __forceinline__ bool move_axis(int& c, float& o, float d, int n, bool upper_closed) {
   if (!(fabsf(d) < 2.0f)) return false;
   o += d;
-#pragma unroll
-  for (int it = 0; it < 3; ++it) {
-    if (upper_closed) {
-      if (o > 1.0f) { o -= 1.0f; ++c; }
-      else if (o <= 0.0f) { o += 1.0f; --c; }
-    } else {
-      if (o >= 1.0f) { o -= 1.0f; ++c; }
-      else if (o < 0.0f) { o += 1.0f; --c; }
-    }
+  // carry whole cells: (0,1] keeps o = 1 in the cell, [0,1) moves it up
+  const float k = upper_closed ? ceilf(o) - 1.0f : floorf(o);
+  o -= k;
+  c += (int)k;
+  if (upper_closed) {  // rounding can leave o at 0 or just above 1
+    if (o <= 0.0f) { o += 1.0f; --c; }
+  } else if (o >= 1.0f) {
+    o -= 1.0f;
+    ++c;
   }
   c = c < 0 ? c + n : (c >= n ? c - n : c);
   return true;
@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(TPB_PASS) k_pass(G32 g, Part p, Species sp, St
                                               float* __restrict__ partial, int* err) {
   __shared__ float4 s_kit[PASS == 1 ? 2 : 2 * TNODES];
   __shared__ float s_dep[4 * TNODES];
-  __shared__ float s_red[TPB_PASS / 32][32][33];  // per-warp transpose of deposit values
+  __shared__ __align__(16) float s_red[TPB_PASS / 32][32][36];  // per-warp transpose of deposit values
   const long long b = blockIdx.x;
   const int bi = (int)(b % g.nbx), bj = (int)((b / g.nbx) % g.nby), bk = (int)(b / ((long long)g.nbx * g.nby));
   const int c0x = 4 * bi, c0y = 4 * bj, c0z = 4 * bk;
@@ -228,27 +228,34 @@ __global__ void __launch_bounds__(TPB_PASS) k_pass(G32 g, Part p, Species sp, St
       }
     }
     // deposit (gutsp.f:1484-1491, 1704-1756): transpose the 32 values
-    // (4 moments x 8 corners) of the warp's particles, sum them per group of
-    // lanes in the same cell, and add each group's sums to the brick tile
-    // with one shared atomic per value slot.
-    float* row = s_red[warp][lane];
+    // (4 moments x 8 corners) of the warp's particles through shared memory;
+    // lane v then runs a segmented sum of value v down the runs of lanes that
+    // share a cell (sorted particles: usually one or two runs) and adds each
+    // run's sum to the brick tile with one shared atomic.
+    float4* row4 = reinterpret_cast<float4*>(s_red[warp][lane]);
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
-#pragma unroll
-      for (int cc = 0; cc < 8; ++cc) row[q * 8 + cc] = live ? w8[cc] * qdv[q] : 0.0f;
+    for (int q = 0; q < 4; ++q) {
+      const float a = live ? qdv[q] : 0.0f;
+      row4[2 * q] = make_float4(w8[0] * a, w8[1] * a, w8[2] * a, w8[3] * a);
+      row4[2 * q + 1] = make_float4(w8[4] * a, w8[5] * a, w8[6] * a, w8[7] * a);
+    }
     __syncwarp();
-    const unsigned grp = __match_any_sync(0xffffffffu, t0);
-    unsigned leaders = __ballot_sync(0xffffffffu, live && lane == __ffs(grp) - 1);
+    const int tprev = __shfl_up_sync(0xffffffffu, t0, 1);
+    const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || t0 != tprev);
+    const unsigned livem = __ballot_sync(0xffffffffu, live);
+    const int nrows = 32 - __clz(livem);
     const int qv = lane >> 3, cv = lane & 7;
     const int off = (cv & 1) + TN * (((cv >> 1) & 1) + TN * (cv >> 2));
-    while (leaders) {
-      const int L = __ffs(leaders) - 1;
-      leaders &= leaders - 1;
-      const unsigned gm = __shfl_sync(0xffffffffu, grp, L);
-      const int tL = __shfl_sync(0xffffffffu, t0, L);
-      float acc = 0.0f;
-      for (unsigned m = gm; m; m &= m - 1) acc += s_red[warp][__ffs(m) - 1][lane];
-      if (PASS != 2 || qv != 0) atomicAdd(&s_dep[qv * TNODES + tL + off], acc);
+    const bool add_here = PASS != 2 || qv != 0;
+    float acc = 0.0f;
+    for (int r = 0; r < nrows; ++r) {
+      acc += s_red[warp][r][lane];
+      // end of a run: the next row starts one, or this is the last live row
+      if (r == nrows - 1 || ((heads >> (r + 1)) & 1u)) {
+        const int tr = __shfl_sync(0xffffffffu, t0, r);
+        if (add_here && tr >= 0) atomicAdd(&s_dep[qv * TNODES + tr + off], acc);
+        acc = 0.0f;
+      }
     }
     __syncwarp();
   }
@@ -459,10 +466,13 @@ __global__ void k_E(G32 g, const float* __restrict__ ct, const float* __restrict
 }
 
 // curlE (gutsf.f:288-299) and b1p2 = base - coef*curlE in FP64
-// (gutsf.f:1158-1159, 1349-1350); dB of the result mirrored in FP32.
+// (gutsf.f:1158-1159, 1349-1350); dB of the result mirrored in FP32.  b0 is
+// uniform in the FP32 form (b0c).  When dbtp1 is given (predictor) the
+// corrector's dB at m+1/2 = (dB(b1p2) + dB(b1))/2 (gutsf.f:1210-1219) is
+// written too.
 __global__ void k_bupd(G32 g, const float* __restrict__ E, const double* __restrict__ base,
-                       const double* __restrict__ b0, double coef, double* __restrict__ b1p2,
-                       float* __restrict__ db1p2) {
+                       const float* __restrict__ b0c, double coef, double* __restrict__ b1p2,
+                       float* __restrict__ db1p2, const float* __restrict__ db1, float* __restrict__ dbtp1) {
   GSTRIDE(t, n_int(g)) {
     int i, j, k;
     interior_of(g, t, i, j, k);
@@ -475,8 +485,10 @@ __global__ void k_bupd(G32 g, const float* __restrict__ E, const double* __restr
                          (E1[o] - E1[o + sy]) * g.inv_dy + (E2[o + sx] - E2[o]) * g.inv_dx};
     for (int m = 0; m < 3; ++m) {
       const double v = base[o + C * m] - coef * (double)ce[m];
+      const float d = (float)(v - (double)b0c[m]);
       store_img(g, b1p2 + C * m, i, j, k, v);
-      store_img(g, db1p2 + C * m, i, j, k, (float)(v - b0[o + C * m]));
+      store_img(g, db1p2 + C * m, i, j, k, d);
+      if (dbtp1) store_img(g, dbtp1 + C * m, i, j, k, 0.5f * (d + db1[o + C * m]));
     }
   }
 }
@@ -890,9 +902,10 @@ cudaError_t e_field(const G32& g, const float* ct, const float* nu, const float*
   (void)gp;
   RET((k_E<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, ct, nu, aj, E)));
 }
-cudaError_t b_update(const G32& g, const float* E, const double* base, const double* b0, double coef, double* b1p2,
-                     float* db1p2, cudaStream_t st) {
-  RET((k_bupd<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, E, base, b0, coef, b1p2, db1p2)));
+cudaError_t b_update(const G32& g, const float* E, const double* base, const float* b0c, double coef, double* b1p2,
+                     float* db1p2, const float* db1, float* dbtp1, cudaStream_t st) {
+  RET((k_bupd<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, E, base, b0c, coef, b1p2, db1p2, db1,
+                                                                       dbtp1)));
 }
 cudaError_t courant_min(const G32& g, const float* dbt, const float* b0c, const float* np, float alpha, float dx,
                         float* dtn, float* d_min, cudaStream_t st) {

@@ -92,8 +92,8 @@ cudaError_t ct_corr(const G32& g, const float* aj, const float* up, const float*
                     float* ct, cudaStream_t st);
 cudaError_t e_field(const G32& g, const float* ct, const float* nu, const float* aj, const float* np, float gp,
                     float* E, cudaStream_t st);
-cudaError_t b_update(const G32& g, const float* E, const double* base, const double* b0, double coef, double* b1p2,
-                     float* db1p2, cudaStream_t st);
+cudaError_t b_update(const G32& g, const float* E, const double* base, const float* b0c, double coef, double* b1p2,
+                     float* db1p2, const float* db1, float* dbtp1, cudaStream_t st);
 cudaError_t courant_min(const G32& g, const float* dbt, const float* b0c, const float* np, float alpha, float dx,
                         float* dtn, float* d_min, cudaStream_t st);
 

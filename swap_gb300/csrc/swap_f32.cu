@@ -315,12 +315,12 @@ static int subcycles(swap_ctx* c, F32State* s) {
     KL("f32_curlB", curlB32(g, s->db1, s->np, alpha, s->aj, c->st));                      // maind.f:430
     KL("f32_ct_pred", ct_pred(g, s->aj, s->up, s->db1, s->b0c, s->ct, c->st));            // get_E
     KL("f32_E", e_field(g, s->ct, s->nu, s->aj, s->np, 0.f, s->E, c->st));
-    KL("f32_bupd", b_update(g, s->E, s->b12, s->b0, 2.0 * dtsub, s->b1p2, s->db1p2, c->st));  // predict_B
+    KL("f32_bupd", b_update(g, s->E, s->b12, s->b0c, 2.0 * dtsub, s->b1p2, s->db1p2, nullptr, nullptr, c->st));  // predict_B
     KL("f32_half", half_sum32(g, s->db1p2, s->db1, s->dbtp1, c->st));                      // get_Ep1
     KL("f32_curlB", curlB32(g, s->dbtp1, s->np, alpha, s->aj, c->st));
     KL("f32_ct_corr", ct_corr(g, s->aj, s->up, s->dbtp1, s->b0c, s->ct, c->st));
     KL("f32_E", e_field(g, s->ct, s->nu, s->aj, s->np, 0.f, s->E, c->st));
-    KL("f32_bupd", b_update(g, s->E, s->b1, s->b0, dtsub, s->b1p2, s->db1p2, c->st));      // correct_B
+    KL("f32_bupd", b_update(g, s->E, s->b1, s->b0c, dtsub, s->b1p2, s->db1p2, nullptr, nullptr, c->st));  // correct_B
     // f_update_tlev (gutsf.f:10-35): b12 <- b1, b1 <- b1p2 (bt = b1)
     std::swap(s->b12, s->b1);
     std::swap(s->b1, s->b1p2);
