@@ -112,6 +112,7 @@ int swap_improve_up(swap_ctx* ctx, double* vp1, const double* vplus, const doubl
                     const double* np);                                                  /* gutsp.f:407  */
 int swap_get_vp_final(swap_ctx* ctx, const double* Ep, double* vp, double* vp1,
                       const double* vplus);                                             /* gutsp.f:433  */
+/* x does not wrap when swap_set_sources opened the x axis (x_open). */
 int swap_move_ion_half(swap_ctx* ctx, double* xp, const double* vp, const double* vp1,
                        double* input_p);                                                /* gutsp.f:454  */
 int swap_curlB(swap_ctx* ctx, double* bt, const double* np, double* aj);                /* gutsf.f:178  */
@@ -138,6 +139,48 @@ int swap_field_subcycles(swap_ctx* ctx);  /* maind.f:420-476 */
 int swap_ion_step_post(swap_ctx* ctx);    /* maind.f:479     */
 int swap_ion_step(swap_ctx* ctx);         /* maind.f:385-479 */
 int swap_run(swap_ctx* ctx, int32_t nsteps);
+
+/* ---- particle sources and sinks (FP64 path) ----
+ * Random draws are Philox4x32-10 keyed by (seed, rule) with counters (ion
+ * step, slot, draw block), replacing the compiler's random_number
+ * (misc.f:24).  Counts are exact functions of the draws.
+ *   ndot > 0       Ionize_sw_mp (chem_rates.f:508-646): pickup ring ions.
+ *   x_open != 0    x axis open: the moves do not wrap x, ions leaving through
+ *                  x <= q(1) or x > q(nx-1) are removed after each move, and
+ *                  a drifting Maxwellian enters from a one-cell ghost slab
+ *                  (inflow_ppc per face cell) at the start of each step.
+ *   nu_ion > 0     ionization of a neutral cloud n_n = N0/(1+(r/r0)^2) per
+ *                  cell, after Ionize_pluto_mp (chem_rates.f:290-503); new
+ *                  heavy ions (mrat_heavy, beta_heavy) at rest.
+ *   cx_a > 0       res_chex (chem_rates.f:805-843): each non-heavy ion turns
+ *                  heavy and at rest with probability
+ *                  dt*n_n*(cx_a - cx_b ln|v|)*|v|.
+ * swap_ion_step / swap_run apply them in this order: ionize, cloud, inflow
+ * at the start of a step; outflow removal after both half moves; res_chex
+ * after the last move (maind.f:484).  step0 is the step counter of the next
+ * fused step; the separate entries take the step number m_tstep. */
+typedef struct swap_sources {
+  uint64_t seed;
+  double ndot, vsw, beta_pu, mrat_pu, delz_ref;   /* Ionize_sw_mp            */
+  int32_t x_open, inflow_ppc;                     /* open x axis, inflow      */
+  double inflow_vth, inflow_ux, inflow_uy, inflow_uz;
+  double cloud_N0, cloud_r0, cloud_x, cloud_y, cloud_z, nu_ion, mrat_heavy, beta_heavy;
+  double cx_a, cx_b;                              /* res_chex cross section  */
+} swap_sources;
+int swap_set_sources(swap_ctx* ctx, const swap_sources* src, int64_t step0);
+/* Ions exchanged by res_chex in the fused steps since swap_set_sources. */
+int swap_chex_count(swap_ctx* ctx, int64_t* count);
+/* Appends the new ions after Ni_tot, then get_interp_weights, update_np,
+ * update_up (chem_rates.f:641-643).  input_p is not updated. */
+int swap_Ionize_sw_mp(swap_ctx* ctx, double* np, double* vp, double* vp1, double* xp, int32_t m_tstep,
+                      double* input_p, double* up);                                     /* chem_rates.f:508 */
+/* Order-preserving removal of ion ion_l (1-based), shifting xp, vp, vp1,
+ * mrat, beta_p and the device ijkp/wght down by one. */
+int swap_remove_ion(swap_ctx* ctx, double* xp, double* vp, double* vp1, int32_t ion_l);   /* gutsp.f:12 */
+int swap_res_chex(swap_ctx* ctx, double* xp, double* vp, int32_t m_tstep, int64_t* count); /* chem_rates.f:805 */
+int swap_inflow_x(swap_ctx* ctx, int32_t m_tstep);
+int swap_ionize_cloud(swap_ctx* ctx, int32_t m_tstep);
+int swap_remove_outflow_x(swap_ctx* ctx);
 
 /* ---- the FP32 form of the fused step ----
  * Particle positions as int32 cell + FP32 offset, FP32 velocities and

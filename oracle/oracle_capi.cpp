@@ -24,6 +24,10 @@ struct OCtx {
   R *b0 = nullptr, *b1 = nullptr, *b12 = nullptr, *b1p2 = nullptr, *bt = nullptr, *btc = nullptr;
   R *np = nullptr, *up = nullptr, *aj = nullptr, *E = nullptr, *nu = nullptr;
   std::vector<R> Ep, vplus, vminus;  // maind.f locals for the fused step
+  swo::Sources src{};
+  bool have_src = false;
+  std::int64_t step = 0;  // ion steps taken by the fused step (RNG counter)
+  std::int64_t chex_count = 0;
   std::string err;
   std::int64_t N() const { return ni_tot ? (std::int64_t)*ni_tot : 0; }
 };
@@ -168,7 +172,7 @@ void copy_out(const std::vector<R>& v1based, int n, R* out) {
   extern "C" int P##move_ion_half(void* h, T* xp, const T* vp, const T* vp1, T* input_p) {                 \
     CTX(T);                                                                                                \
     (void)vp1; (void)input_p;                                                                              \
-    return guard(c, [&] { swo::move_ion_half(c->s, xp, vp, c->N()); });                                    \
+    return guard(c, [&] { swo::move_ion_half(c->s, xp, vp, c->N(), c->have_src && c->src.x_open); });      \
   }                                                                                                        \
   extern "C" int P##curlB(void* h, T* bt, const T* np, T* aj) {                                            \
     CTX(T);                                                                                                \
@@ -234,7 +238,20 @@ void copy_out(const std::vector<R>& v1based, int n, R* out) {
     return guard(c, [&] {                                                                                  \
       auto& s = c->s;                                                                                      \
       T* Ep = c->Ep.data(); T* vpl = c->vplus.data(); T* vmi = c->vminus.data();                           \
-      const std::int64_t N = c->N();                                                                       \
+      if (c->have_src) { /* maind.f:379-383 and the cloud and inflow sources */                                      \
+        const auto& q = c->src;                                                                            \
+        if (q.ndot > 0)                                                                                    \
+          *c->ni_tot += (std::int32_t)swo::ionize_sw(s, q, c->step, c->xp, c->vp, c->vp1, c->mrat,         \
+                                                     c->beta_p, c->N());                                   \
+        if (q.nu_ion > 0)                                                                                  \
+          *c->ni_tot += (std::int32_t)swo::ionize_cloud(s, q, c->step, c->xp, c->vp, c->vp1, c->mrat,      \
+                                                        c->beta_p, c->N());                                \
+        if (q.x_open)                                                                                      \
+          *c->ni_tot += (std::int32_t)swo::inflow_x(s, q, c->step, c->xp, c->vp, c->vp1, c->mrat,          \
+                                                    c->beta_p, c->N());                                    \
+      }                                                                                                    \
+      const bool xo = c->have_src && c->src.x_open;                                                        \
+      std::int64_t N = c->N();                                                                             \
       swo::get_interp_weights(s, c->xp, N);                                /* maind.f:385 */               \
       swo::update_np(s, c->np, c->beta_p, N);                              /* :386 */                      \
       swo::update_up(s, c->vp, c->np, c->up, c->beta_p, N);                /* :387 */                      \
@@ -247,7 +264,11 @@ void copy_out(const std::vector<R>& v1based, int n, R* out) {
       swo::get_Ep(s, Ep, c->aj, c->np, c->up, c->btc, c->nu, c->mrat, N);  /* :404 */                      \
       swo::get_vplus_vminus(s, Ep, c->btc, c->vp, vpl, vmi, c->mrat, N);   /* :405 */                      \
       swo::get_vp_final(s, Ep, c->vp, c->vp1, vpl, N);                     /* :406 */                      \
-      swo::move_ion_half(s, c->xp, c->vp, N);                              /* :408 */                      \
+      swo::move_ion_half(s, c->xp, c->vp, N, xo);                          /* :408 */                      \
+      if (xo) {                                                                                            \
+        *c->ni_tot = (std::int32_t)swo::remove_outflow_x(s, c->xp, c->vp, c->vp1, c->mrat, c->beta_p, N);  \
+        N = c->N();                                                                                        \
+      }                                                                                                    \
       swo::get_interp_weights(s, c->xp, N);                                /* :411 */                      \
       swo::update_np(s, c->np, c->beta_p, N);                              /* :412 */                      \
       swo::update_up(s, c->vp, c->np, c->up, c->beta_p, N);                /* :413 */                      \
@@ -261,8 +282,71 @@ void copy_out(const std::vector<R>& v1based, int n, R* out) {
         swo::correct_B(s, c->b0, c->b1, c->b1p2, c->E, c->aj, c->up, c->np, c->nu);                        \
         swo::f_update_tlev(s.g, c->b1, c->b12, c->b1p2, c->bt);                                            \
       }                                                                                                    \
-      swo::move_ion_half(s, c->xp, c->vp, N);                              /* :479 */                      \
+      swo::move_ion_half(s, c->xp, c->vp, N, xo);                          /* :479 */                      \
+      if (xo) *c->ni_tot = (std::int32_t)swo::remove_outflow_x(s, c->xp, c->vp, c->vp1, c->mrat, c->beta_p, N); \
+      if (c->have_src && c->src.cx_a > 0) /* :484, res_chex */                                             \
+        c->chex_count += swo::res_chex(s, c->src, c->step, c->xp, c->vp, c->vp1, c->mrat, c->N());        \
+      c->step++;                                                                                           \
     });                                                                                                    \
+  }                                                                                                        \
+  extern "C" int P##set_sources(void* h, const swo::Sources* q, std::int64_t step0) {                       \
+    CTX(T);                                                                                                \
+    c->src = *q;                                                                                           \
+    c->have_src = true;                                                                                    \
+    c->step = step0;                                                                                       \
+    return 0;                                                                                              \
+  }                                                                                                        \
+  extern "C" std::int64_t P##chex_count(void* h) {                                                         \
+    CTX(T);                                                                                                \
+    return c->chex_count;                                                                                  \
+  }                                                                                                        \
+  extern "C" int P##Ionize_sw_mp(void* h, T* np, T* vp, T* vp1, T* xp, std::int32_t m, T* input_p, T* up) { \
+    CTX(T);                                                                                                \
+    (void)input_p;                                                                                         \
+    return guard(c, [&] {                                                                                  \
+      *c->ni_tot += (std::int32_t)swo::ionize_sw(c->s, c->src, m, xp, vp, vp1, c->mrat, c->beta_p, c->N()); \
+      swo::get_interp_weights(c->s, xp, c->N());                           /* chem_rates.f:641-643 */      \
+      swo::update_np(c->s, np, c->beta_p, c->N());                                                         \
+      swo::update_up(c->s, vp, np, up, c->beta_p, c->N());                                                 \
+    });                                                                                                    \
+  }                                                                                                        \
+  extern "C" int P##inflow_x(void* h, std::int32_t m) {                                                    \
+    CTX(T);                                                                                                \
+    return guard(c, [&] {                                                                                  \
+      *c->ni_tot += (std::int32_t)swo::inflow_x(c->s, c->src, m, c->xp, c->vp, c->vp1, c->mrat, c->beta_p, \
+                                                c->N());                                                   \
+    });                                                                                                    \
+  }                                                                                                        \
+  extern "C" int P##ionize_cloud(void* h, std::int32_t m) {                                                \
+    CTX(T);                                                                                                \
+    return guard(c, [&] {                                                                                  \
+      *c->ni_tot += (std::int32_t)swo::ionize_cloud(c->s, c->src, m, c->xp, c->vp, c->vp1, c->mrat,        \
+                                                    c->beta_p, c->N());                                    \
+    });                                                                                                    \
+  }                                                                                                        \
+  extern "C" int P##remove_outflow_x(void* h) {                                                            \
+    CTX(T);                                                                                                \
+    return guard(c, [&] {                                                                                  \
+      *c->ni_tot = (std::int32_t)swo::remove_outflow_x(c->s, c->xp, c->vp, c->vp1, c->mrat, c->beta_p,     \
+                                                       c->N());                                            \
+    });                                                                                                    \
+  }                                                                                                        \
+  extern "C" int P##remove_ion(void* h, T* xp, T* vp, T* vp1, std::int32_t ion_l) {                        \
+    CTX(T);                                                                                                \
+    return guard(c, [&] {                                                                                  \
+      std::vector<char> keep((std::size_t)c->N(), 1);                                                      \
+      if (ion_l < 1 || ion_l > c->N()) throw std::runtime_error("remove_ion: index out of range");         \
+      keep[(std::size_t)ion_l - 1] = 0;                                                                    \
+      *c->ni_tot = (std::int32_t)swo::compact(c->s, keep, xp, vp, vp1, c->mrat, c->beta_p, c->N());        \
+    });                                                                                                    \
+  }                                                                                                        \
+  extern "C" int P##res_chex(void* h, T* xp, T* vp, std::int32_t m, std::int64_t* count) {                 \
+    CTX(T);                                                                                                \
+    return guard(c, [&] { *count = swo::res_chex(c->s, c->src, m, xp, vp, c->vp1, c->mrat, c->N()); });    \
+  }                                                                                                        \
+  extern "C" int P##move_ion_half_open(void* h, T* xp, const T* vp) {                                      \
+    CTX(T);                                                                                                \
+    return guard(c, [&] { swo::move_ion_half(c->s, xp, vp, c->N(), true); });                             \
   }                                                                                                        \
   extern "C" int P##sort_perm(void* h, std::int64_t* perm, std::int64_t* counts) {                         \
     CTX(T);                                                                                                \
@@ -302,4 +386,19 @@ extern "C" int oracle_stable_counting_sort(const std::int64_t* keys, std::int64_
   for (std::int64_t k = 0; k < nkeys; ++k) start[(std::size_t)k + 1] += start[(std::size_t)k];
   for (std::int64_t l = 0; l < n; ++l) perm[start[(std::size_t)keys[l]]++] = l;
   return 0;
+}
+
+// The counter-based generator shared by the oracle and the product
+// (swap_gb300/csrc/philox.h), exposed so tests can pin it to the published
+// Philox4x32-10 known-answer vectors.
+extern "C" void oracle_philox4x32_10(const std::uint32_t ctr[4], const std::uint32_t key[2], std::uint32_t out[4]) {
+  swapk::u32x4 c;
+  for (int q = 0; q < 4; ++q) c.v[q] = ctr[q];
+  const swapk::u32x4 r = swapk::philox4x32_10(c, key[0], key[1]);
+  for (int q = 0; q < 4; ++q) out[q] = r.v[q];
+}
+
+extern "C" void oracle_source_uniforms(std::uint64_t seed, std::uint32_t stream, std::int64_t step, std::int64_t a,
+                                       std::uint32_t b, double u[4]) {
+  swapk::source_uniforms(seed, stream, step, a, b, u);
 }

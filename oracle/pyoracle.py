@@ -196,6 +196,45 @@ class Oracle:
             raise RuntimeError("oracle sort_perm failed")
         return perm, counts
 
+    # sources and sinks ----------------------------------------------
+    def set_sources(self, src, step0=0):
+        """src: a swap_gb300.abi.Sources (the same struct layout)."""
+        self._src = src
+        r = self._fn("set_sources")(self.h, C.byref(src), C.c_int64(int(step0)))
+        if r:
+            raise RuntimeError("oracle set_sources failed")
+
+    def chex_count(self):
+        f = self._fn("chex_count")
+        f.restype = C.c_int64
+        return int(f(self.h))
+
+    def Ionize_sw_mp(self, np_, vp, vp1, xp, m_tstep, input_p, up):
+        r = self._fn("Ionize_sw_mp")(self.h, self._ptr(np_), self._ptr(vp), self._ptr(vp1), self._ptr(xp),
+                                     C.c_int32(int(m_tstep)), self._ptr(input_p), self._ptr(up))
+        if r:
+            raise RuntimeError("oracle Ionize_sw_mp: " + self._fn("last_error")(self.h).decode())
+
+    def inflow_x(self, m_tstep):
+        self._call("inflow_x", extra=(C.c_int32(int(m_tstep)),))
+
+    def ionize_cloud(self, m_tstep):
+        self._call("ionize_cloud", extra=(C.c_int32(int(m_tstep)),))
+
+    def remove_outflow_x(self):
+        self._call("remove_outflow_x")
+
+    def remove_ion(self, xp, vp, vp1, ion_l):
+        self._call("remove_ion", xp, vp, vp1, extra=(C.c_int32(int(ion_l)),))
+
+    def res_chex(self, xp, vp, m_tstep):
+        n = C.c_int64()
+        self._call("res_chex", xp, vp, extra=(C.c_int32(int(m_tstep)), C.byref(n)))
+        return n.value
+
+    def move_ion_half_open(self, xp, vp):
+        self._call("move_ion_half_open", xp, vp)
+
     def grd6_setup(self, b0_init, mion, nu_init):
         self._fn("grd6_setup")(self.h, C.c_double(b0_init), C.c_double(mion), C.c_double(nu_init))
 
@@ -216,7 +255,9 @@ def from_hybrid_arrays(h, precision="f64", nthreads=1):
     its own copies of that object's host arrays (bound like the Fortran's)."""
     cfg = h.cfg
     nx, ny, nz = cfg.nodes
-    o = Oracle(nx, ny, nz, h.ni_max, cfg.dt, cfg.ntsub, cfg.alpha, cfg.beta, grad_pe=cfg.grad_pe,
+    co = getattr(h, "coords", None)
+    o = Oracle(nx, ny, nz, h.ni_max, cfg.dt, cfg.ntsub, cfg.alpha, cfg.beta, dx=getattr(co, "dx", 1.0),
+               dy=getattr(co, "dy", 1.0), delz=getattr(co, "delz", 1.0), grad_pe=cfg.grad_pe,
                precision=precision, nthreads=nthreads)
     dt = o.dtype
     cp = lambda a: np.array(a, dtype=dt, order="F", copy=True)

@@ -872,7 +872,7 @@ void get_vp_final(State<R>& s, const R* Ep, R* vp, R* vp1, const R* vplus, std::
 // move_ion_half (gutsp.f:454-570): half-step drift and periodic wrap into
 // (q(1), q(n-1)] on each axis.
 template <class R>
-void move_ion_half(State<R>& s, R* xp, const R* vp, std::int64_t ni_tot) {
+void move_ion_half(State<R>& s, R* xp, const R* vp, std::int64_t ni_tot, bool x_open = false) {
   const Mesh<R>& g = s.g;
   const std::int64_t NM = s.ni_max;
   const R dth = s.dt / R(2.);
@@ -880,8 +880,10 @@ void move_ion_half(State<R>& s, R* xp, const R* vp, std::int64_t ni_tot) {
     R x = xp[l] + dth * vp[l];
     R y = xp[l + NM] + dth * vp[l + NM];
     R z = xp[l + 2 * NM] + dth * vp[l + 2 * NM];
-    if (x > g.qx[g.nx - 1]) x = g.qx[1] + (x - g.qx[g.nx - 1]);
-    else if (x <= g.qx[1]) x = g.qx[g.nx - 1] - (g.qx[1] - x);
+    if (!x_open) {
+      if (x > g.qx[g.nx - 1]) x = g.qx[1] + (x - g.qx[g.nx - 1]);
+      else if (x <= g.qx[1]) x = g.qx[g.nx - 1] - (g.qx[1] - x);
+    }
     if (y > g.qy[g.ny - 1]) y = g.qy[1] + (y - g.qy[g.ny - 1]);
     else if (y <= g.qy[1]) y = g.qy[g.ny - 1] - (g.qy[1] - y);
     if (z > g.qz[g.nz - 1]) z = g.qz[1] + (z - g.qz[g.nz - 1]);
@@ -1009,7 +1011,7 @@ void counting_sort_perm(const Mesh<R>& g, const std::int32_t* ijkp, std::int64_t
 
 // ---------------------------------------------------------------------------
 // Particle sources and sinks (chem_rates.f, gutsp.f:12-46) and the
-// extensions D3-D5 (x inflow/outflow, cloud ionization, charge exchange).
+// extensions: x inflow/outflow, cloud ionization, charge exchange.
 // The compiler's random_number (misc.f:24) is replaced by Philox4x32-10
 // draws keyed by (seed, stream) with counters (step, slot, draw block), so
 // the CPU and GPU paths consume identical uniforms.
@@ -1019,25 +1021,21 @@ namespace swo {
 struct Sources {
   std::uint64_t seed;
   double ndot, vsw, beta_pu, mrat_pu, delz_ref;    // Ionize_sw_mp
-  int x_open, inflow_ppc;                          // D3
+  int x_open, inflow_ppc;                          // open x axis, inflow
   double inflow_vth, inflow_ux, inflow_uy, inflow_uz;
-  double cloud_N0, cloud_r0, cloud_x, cloud_y, cloud_z, nu_ion, mrat_heavy, beta_heavy;  // D4
-  double cx_a, cx_b;                               // D5
+  double cloud_N0, cloud_r0, cloud_x, cloud_y, cloud_z, nu_ion, mrat_heavy, beta_heavy;  // cloud
+  double cx_a, cx_b;                               // res_chex
 };
 
-enum : std::uint32_t { RNG_IONIZE = 1, RNG_INFLOW = 2, RNG_CLOUD = 3, RNG_CHEX = 4 };
+using swapk::RNG_CHEX;
+using swapk::RNG_CLOUD;
+using swapk::RNG_INFLOW;
+using swapk::RNG_IONIZE;
 
-// Four uniforms in (0,1) for (stream, step, a, b).
+// Four uniforms in (0,1) for (stream, step, a, b): the product's draw.
 inline void draw4(const Sources& s, std::uint32_t stream, std::int64_t step, std::int64_t a, std::uint32_t b,
                   double u[4]) {
-  swapk::u32x4 c;
-  c.v[0] = (std::uint32_t)step;
-  c.v[1] = (std::uint32_t)a;
-  c.v[2] = (std::uint32_t)((std::uint64_t)a >> 32);
-  c.v[3] = b;
-  const swapk::u32x4 r = swapk::philox4x32_10(c, (std::uint32_t)s.seed ^ (stream * 0x9E3779B9u),
-                                              (std::uint32_t)(s.seed >> 32));
-  for (int q = 0; q < 4; ++q) u[q] = swapk::u01_open(r.v[q]);
+  swapk::source_uniforms(s.seed, stream, step, a, b, u);
 }
 
 // Ionize_sw_mp (chem_rates.f:508-646): dNi = ndot*dt*beta*beta_pu*dx*dy*delz*nz
@@ -1104,7 +1102,7 @@ std::int64_t compact(const State<R>& s, const std::vector<char>& keep, R* xp, R*
   return w;
 }
 
-// D3 outflow: after a half move with the x axis open, particles with
+// Outflow: after a half move with the x axis open, particles with
 // x > q(nx-1) or x <= q(1) leave the box.
 template <class R>
 std::int64_t remove_outflow_x(const State<R>& s, R* xp, R* vp, R* vp1, R* mrat, R* beta_p, std::int64_t ni_tot) {
@@ -1114,7 +1112,7 @@ std::int64_t remove_outflow_x(const State<R>& s, R* xp, R* vp, R* vp1, R* mrat, 
   return compact(s, keep, xp, vp, vp1, mrat, beta_p, ni_tot);
 }
 
-// D3 inflow: a virtual ghost slab one cell deep before x = q(1).  Each face
+// Inflow: a virtual ghost slab one cell deep before x = q(1).  Each face
 // cell (j,k) holds inflow_ppc particles, stratified like the load, with
 // drifting-Maxwellian velocities of the reference's form; those whose
 // ballistic move over one ion step crosses x = q(1) enter the box at their
@@ -1162,7 +1160,7 @@ inline double cloud_density(const Sources& src, double x, double y, double z) {
   return src.cloud_N0 / (1.0 + r2);
 }
 
-// D4 cloud ionization, after the per-cell rule of Ionize_pluto_mp
+// Cloud ionization, after the per-cell rule of Ionize_pluto_mp
 // (chem_rates.f:346-432): in every physical cell, n_new = vol*beta*beta_h*
 // n_n(centre)*nu_ion*dt; floor plus a Bernoulli trial on the remainder; new
 // heavy ions at rest, uniform in the cell.
@@ -1209,7 +1207,7 @@ std::int64_t ionize_cloud(State<R>& s, const Sources& src, std::int64_t step, R*
   return w - ni_tot;
 }
 
-// D5 charge exchange, after res_chex (chem_rates.f:823-840): each ion with
+// Charge exchange, after res_chex (chem_rates.f:823-840): each ion with
 // mrat != mrat_heavy exchanges with probability dt*n_n*sigma*v_rel,
 // sigma = a - b ln(v_rel); the new ion is heavy and at rest.  Returns the count.
 template <class R>

@@ -70,6 +70,29 @@ class LoadSpec(C.Structure):
     ]
 
 
+class Sources(C.Structure):
+    """swap_sources: particle sources and sinks of the ion step."""
+
+    _fields_ = [
+        ("seed", C.c_uint64),
+        ("ndot", C.c_double), ("vsw", C.c_double), ("beta_pu", C.c_double), ("mrat_pu", C.c_double),
+        ("delz_ref", C.c_double),
+        ("x_open", C.c_int32), ("inflow_ppc", C.c_int32),
+        ("inflow_vth", C.c_double), ("inflow_ux", C.c_double), ("inflow_uy", C.c_double), ("inflow_uz", C.c_double),
+        ("cloud_N0", C.c_double), ("cloud_r0", C.c_double), ("cloud_x", C.c_double), ("cloud_y", C.c_double),
+        ("cloud_z", C.c_double), ("nu_ion", C.c_double), ("mrat_heavy", C.c_double), ("beta_heavy", C.c_double),
+        ("cx_a", C.c_double), ("cx_b", C.c_double),
+    ]
+
+
+def make_sources(**kw) -> Sources:
+    """A Sources with every rule off (all zero) except the fields given."""
+    s = Sources()
+    for k, v in kw.items():
+        setattr(s, k, v)
+    return s
+
+
 # Every exported symbol declared in include/swap_gpu.h, with its argument types.
 P = C.c_void_p
 SIGNATURES: dict[str, tuple] = {
@@ -107,6 +130,14 @@ SIGNATURES: dict[str, tuple] = {
     "swap_ion_step_post": (C.c_int, [P]),
     "swap_ion_step": (C.c_int, [P]),
     "swap_run": (C.c_int, [P, C.c_int32]),
+    "swap_set_sources": (C.c_int, [P, C.POINTER(Sources), C.c_int64]),
+    "swap_chex_count": (C.c_int, [P, c_int64_p]),
+    "swap_Ionize_sw_mp": (C.c_int, [P] + [c_double_p] * 4 + [C.c_int32] + [c_double_p] * 2),
+    "swap_remove_ion": (C.c_int, [P] + [c_double_p] * 3 + [C.c_int32]),
+    "swap_res_chex": (C.c_int, [P, c_double_p, c_double_p, C.c_int32, c_int64_p]),
+    "swap_inflow_x": (C.c_int, [P, C.c_int32]),
+    "swap_ionize_cloud": (C.c_int, [P, C.c_int32]),
+    "swap_remove_outflow_x": (C.c_int, [P]),
     "swap_f32_begin": (C.c_int, [P]),
     "swap_f32_run": (C.c_int, [P, C.c_int32]),
     "swap_f32_end": (C.c_int, [P]),

@@ -32,6 +32,7 @@ UNITS = [
     ("swap_f32.cu", []),
     ("swap_prof.cu", []),
     ("swap_noalloc.cu", ["--fmad=false"]),
+    ("swap_sources.cu", ["--fmad=false", "-Xcompiler", "-ffp-contract=off"]),
     ("loader.cpp", ["-Xcompiler", "-fopenmp,-ffp-contract=off"]),
 ]
 

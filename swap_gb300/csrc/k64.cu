@@ -470,7 +470,7 @@ __global__ void k_vp_final(PartDev p, long long N, double dt, const double* __re
 
 // move_ion_half (gutsp.f:469-510).
 __global__ void k_move_half(Geo g, PartDev p, long long N, double dt, double* __restrict__ xp,
-                            const double* __restrict__ vp) {
+                            const double* __restrict__ vp, bool x_open) {
   const double dth = dt / 2.;
   const long long NM = p.NM;
   GRID_STRIDE(l, N) {
@@ -480,8 +480,10 @@ __global__ void k_move_half(Geo g, PartDev p, long long N, double dt, double* __
     const double qx1 = g.qx[1], qxn = g.qx[g.nx - 1];
     const double qy1 = g.qy[1], qyn = g.qy[g.ny - 1];
     const double qz1 = g.qz[1], qzn = g.qz[g.nz - 1];
-    if (x > qxn) x = qx1 + (x - qxn);
-    else if (x <= qx1) x = qxn - (qx1 - x);
+    if (!x_open) {
+      if (x > qxn) x = qx1 + (x - qxn);
+      else if (x <= qx1) x = qxn - (qx1 - x);
+    }
     if (y > qyn) y = qy1 + (y - qyn);
     else if (y <= qy1) y = qyn - (qy1 - y);
     if (z > qzn) z = qz1 + (z - qzn);
@@ -659,9 +661,9 @@ cudaError_t vp_final(const PartDev& p, long long N, double dt, const double* Ep,
   LAUNCH(k_vp_final, N, p, N, dt, Ep, vp, vp1, vplus);
 }
 cudaError_t move_half(const Geo& g, const PartDev& p, long long N, double dt, double* xp, const double* vp,
-                      cudaStream_t st) {
+                      bool x_open, cudaStream_t st) {
   if (N <= 0) return cudaSuccess;
-  LAUNCH(k_move_half, N, g, p, N, dt, xp, vp);
+  LAUNCH(k_move_half, N, g, p, N, dt, xp, vp, x_open);
 }
 cudaError_t reduce_min(const double* x, long long n, double* d_out, int, cudaStream_t st) {
   const unsigned long long init = (unsigned long long)0x7fefffffffffffffULL;  // DBL_MAX bits

@@ -52,8 +52,10 @@ cudaError_t vplus_vminus(const Geo& g, const PartDev& p, long long N, double dt,
                          cudaStream_t st);
 cudaError_t vp_final(const PartDev& p, long long N, double dt, const double* Ep, double* vp, double* vp1,
                      const double* vplus, cudaStream_t st);
+// x_open: the x axis does not wrap (particles leaving are removed after the
+// move by the caller).
 cudaError_t move_half(const Geo& g, const PartDev& p, long long N, double dt, double* xp, const double* vp,
-                      cudaStream_t st);
+                      bool x_open, cudaStream_t st);
 
 // reductions (FP64)
 cudaError_t reduce_min(const double* x, long long n, double* d_partial, int nblk, cudaStream_t st);

@@ -63,4 +63,19 @@ SWAP_HD void particle_uniforms(uint64_t seed, uint32_t stream, uint64_t id, uint
   }
 }
 
+// Four uniforms for a particle source or sink: stream (which rule), step
+// (ion step number), slot a (new particle / cell / particle index) and draw
+// block b.
+SWAP_HD void source_uniforms(uint64_t seed, uint32_t stream, int64_t step, int64_t a, uint32_t b, double u[4]) {
+  u32x4 c;
+  c.v[0] = (uint32_t)step;
+  c.v[1] = (uint32_t)a;
+  c.v[2] = (uint32_t)((uint64_t)a >> 32);
+  c.v[3] = b;
+  const u32x4 r = philox4x32_10(c, (uint32_t)seed ^ (stream * 0x9E3779B9u), (uint32_t)(seed >> 32));
+  for (int q = 0; q < 4; ++q) u[q] = u01_open(r.v[q]);
+}
+
+enum : uint32_t { RNG_IONIZE = 1, RNG_INFLOW = 2, RNG_CLOUD = 3, RNG_CHEX = 4 };
+
 }  // namespace swapk

@@ -10,6 +10,7 @@
 #include "../../include/swap_gpu.h"
 #include "k64.cuh"
 #include "swap_ctx.h"
+#include "swap_ops.h"
 #include "swap_prof.h"
 
 using namespace swapk;
@@ -358,7 +359,7 @@ int vp_final(swap_ctx* c, const double* Ep, double* vp, double* vp1, const doubl
 }
 
 int move_ion_half(swap_ctx* c, double* xp, const double* vp) {
-  KL("move_half", move_half(c->g, c->part_view(), c->ntot(), c->prm.dt, xp, vp, c->st));
+  KL("move_half", move_half(c->g, c->part_view(), c->ntot(), c->prm.dt, xp, vp, srcops::x_open(c), c->st));
   return 0;
 }
 
@@ -444,6 +445,7 @@ extern "C" int swap_finalize(swap_ctx* c) {
   if (!c) return SWAP_EINVAL;
   if (c->st) cudaStreamSynchronize(c->st);
   swap_f32_free(c);
+  srcops::free_all(c);
   for (auto& kv : c->reg) cudaFree(kv.second.dev);
   for (void* p : c->owned) cudaFree(p);
   if (c->t0) cudaEventDestroy(c->t0);
@@ -840,8 +842,7 @@ int bound_inputs(swap_ctx* c, Bound& b) {
 }
 
 int step_pre(swap_ctx* c, Bound& b) {
-  PartDev p = c->part_view();
-  (void)p;
+  TRY(srcops::step_begin(c, b.xp, b.vp, b.vp1));                            // sources
   TRY(ops::get_interp_weights(c, b.xp));                                     // maind.f:385
   TRY(ops::update_np(c, b.np));                                              // :386
   TRY(ops::update_up_mode(c, 0, b.vp, nullptr, nullptr, b.np, b.up));        // :387
@@ -855,6 +856,7 @@ int step_pre(swap_ctx* c, Bound& b) {
   TRY(ops::vpm(c, c->w_Ep, b.btc, b.vp, c->w_vplus, c->w_vminus));           // :405
   TRY(ops::vp_final(c, c->w_Ep, b.vp, b.vp1, c->w_vplus));                   // :406
   TRY(ops::move_ion_half(c, b.xp, b.vp));                                    // :408
+  TRY(srcops::after_move(c, b.xp, b.vp, b.vp1));                             // outflow
   TRY(ops::get_interp_weights(c, b.xp));                                     // :411
   TRY(ops::update_np(c, b.np));                                              // :412
   TRY(ops::update_up_mode(c, 0, b.vp, nullptr, nullptr, b.np, b.up));        // :413
@@ -874,6 +876,14 @@ int subcycles(swap_ctx* c, Bound& b) {
     TRY(ops::correct_B(c, b.b1, b.b1p2, b.E, b.aj, b.up, b.np, b.nu, dtsub));
     TRY(ops::f_update_tlev(c, b.b1, b.b12, b.b1p2, b.bt));
   }
+  return SWAP_OK;
+}
+
+// maind.f:479 and the sinks after it (res_chex, maind.f:484).
+int step_post(swap_ctx* c, Bound& b) {
+  TRY(ops::move_ion_half(c, b.xp, b.vp));
+  TRY(srcops::after_move(c, b.xp, b.vp, b.vp1));
+  TRY(srcops::step_end(c, b.xp, b.vp, b.vp1));
   return SWAP_OK;
 }
 
@@ -899,7 +909,7 @@ extern "C" int swap_ion_step_post(swap_ctx* c) {
   ENTRY;
   Bound b;
   TRY(bound_inputs(c, b));
-  TRY(ops::move_ion_half(c, b.xp, b.vp));  // maind.f:479
+  TRY(step_post(c, b));  // maind.f:479
   return c->finish();
 }
 
@@ -909,7 +919,7 @@ extern "C" int swap_ion_step(swap_ctx* c) {
   TRY(bound_inputs(c, b));
   TRY(step_pre(c, b));
   TRY(subcycles(c, b));
-  TRY(ops::move_ion_half(c, b.xp, b.vp));
+  TRY(step_post(c, b));
   return c->finish();
 }
 
@@ -920,7 +930,7 @@ extern "C" int swap_run(swap_ctx* c, int32_t nsteps) {
   for (int s = 0; s < nsteps; ++s) {
     TRY(step_pre(c, b));
     TRY(subcycles(c, b));
-    TRY(ops::move_ion_half(c, b.xp, b.vp));
+    TRY(step_post(c, b));
   }
   return c->finish();
 }

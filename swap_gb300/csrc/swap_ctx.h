@@ -68,6 +68,15 @@ struct swap_ctx {
   double last_dtsub = 0, last_ntf = 0;
   void* f32_state = nullptr;  // the FP32 form (swap_f32.cu)
 
+  // particle sources and sinks (swap_sources.cu)
+  swap_sources srcs{};
+  bool have_srcs = false;
+  long long src_step = 0;                    // step counter of the next fused step
+  long long src_cap = 0;                     // capacity of the scan scratch
+  int64_t *src_flag = nullptr, *src_pos = nullptr, *src_sums = nullptr;
+  void* src_tmp = nullptr;                   // ni_max elements of 8 bytes
+  unsigned long long* src_cnt = nullptr;     // [0] last res_chex, [1] fused-step total
+
   cudaEvent_t t0 = nullptr, t1 = nullptr;
 
   // per-kernel profile (CUDA events), filled by the fused paths

@@ -99,6 +99,8 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
   TRY(c->begin());
   if (!c->h_xp || !c->h_b1) return c->fail(SWAP_EINVAL, "swap_bind_particles and swap_bind_fields are required");
   if (c->prm.grad_pe != 0.0) return c->fail(SWAP_EINVAL, "the FP32 form has no electron-pressure term");
+  if (c->have_srcs && (c->srcs.ndot > 0 || c->srcs.x_open || c->srcs.nu_ion > 0 || c->srcs.cx_a > 0))
+    return c->fail(SWAP_EINVAL, "the FP32 form has no particle sources or sinks");
   const int nx = c->dims.nx, ny = c->dims.ny, nz = c->dims.nz;
   const int ncx = nx - 2, ncy = ny - 2, ncz = nz - 2;
   if (ncx % 4 || ncy % 4 || ncz % 4 || ncx < 8 || ncy < 8 || ncz < 8 || ncx > 1024 || ncy > 1024 || ncz > 1024)

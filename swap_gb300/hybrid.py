@@ -213,6 +213,37 @@ class Hybrid:
     def periodic(self, b):
         self._check(self.lib.swap_periodic(self.ctx, abi.dptr(b)))
 
+    # ---- sources and sinks (chem_rates.f, gutsp.f:12-46) ----
+    def set_sources(self, src: "abi.Sources", step0: int = 0):
+        self._sources = src
+        self._check(self.lib.swap_set_sources(self.ctx, C.byref(src), int(step0)))
+
+    def Ionize_sw_mp(self, np_, vp, vp1, xp, m_tstep, input_p, up):
+        self._check(self.lib.swap_Ionize_sw_mp(self.ctx, abi.dptr(np_), abi.dptr(vp), abi.dptr(vp1), abi.dptr(xp),
+                                               int(m_tstep), abi.dptr(input_p), abi.dptr(up)))
+
+    def remove_ion(self, xp, vp, vp1, ion_l):
+        self._check(self.lib.swap_remove_ion(self.ctx, abi.dptr(xp), abi.dptr(vp), abi.dptr(vp1), int(ion_l)))
+
+    def res_chex(self, xp, vp, m_tstep) -> int:
+        n = C.c_int64()
+        self._check(self.lib.swap_res_chex(self.ctx, abi.dptr(xp), abi.dptr(vp), int(m_tstep), C.byref(n)))
+        return n.value
+
+    def inflow_x(self, m_tstep):
+        self._check(self.lib.swap_inflow_x(self.ctx, int(m_tstep)))
+
+    def ionize_cloud(self, m_tstep):
+        self._check(self.lib.swap_ionize_cloud(self.ctx, int(m_tstep)))
+
+    def remove_outflow_x(self):
+        self._check(self.lib.swap_remove_outflow_x(self.ctx))
+
+    def chex_count(self) -> int:
+        n = C.c_int64()
+        self._check(self.lib.swap_chex_count(self.ctx, C.byref(n)))
+        return n.value
+
     # ---- fused step ----
     def ion_step(self):
         self._check(self.lib.swap_ion_step(self.ctx))

@@ -1,60 +1,10 @@
 """Known-answer tests of the CPU oracle (the reference ships none besides
 b0.dat).  Each checks a property the reference algorithm has exactly or to
 roundoff."""
-import ctypes as C
-
 import numpy as np
 import pytest
 
-from swap_gb300 import abi
-from swap_gb300.grid import grd6_setup, grd7
-from swap_gb300.hybrid import RunConfig
-
-
-class Host:
-    """The arrays of maind.f:38-70 for a RunConfig, on the host."""
-
-    def __init__(self, cfg, ni_max=None, load=True):
-        self.cfg = cfg
-        nx, ny, nz = cfg.nodes
-        n = cfg.n_particles if ni_max is None else ni_max
-        self.ni_max = n
-        self.coords = grd7(nx, ny, nz)
-        f3 = lambda: np.zeros((n, 3), order="F")
-        self.xp, self.vp, self.vp1, self.Ep, self.vplus, self.vminus = (f3() for _ in range(6))
-        self.mrat, self.beta_p = np.ones(n), np.ones(n)
-        self.ni_tot = np.array([0], dtype=np.int32)
-        for k, v in grd6_setup(self.coords, cfg.b0, cfg.nu).items():
-            setattr(self, k, v)
-        if load:
-            self.load()
-
-    def load(self, **over):
-        cfg = self.cfg
-        lib = abi.load()
-        nx, ny, nz = cfg.nodes
-        dims = abi.Dims(nx, ny, nz, 0, self.ni_max)
-        co = abi.Coords(*[abi.dptr(getattr(self.coords, a)) for a in self.coords.ARRAYS])
-        spec = abi.LoadSpec(over.get("seed", cfg.seed), 0, over.get("ppc", cfg.ppc), over.get("vth", cfg.vth),
-                            *over.get("u", cfg.u), 1.0, 1.0)
-        cnt = C.c_int64()
-        abi.check(lib, None, lib.swap_load_maxwellian_host(C.byref(dims), C.byref(co), C.byref(spec),
-                                                            abi.dptr(self.xp), abi.dptr(self.vp), abi.dptr(self.vp1),
-                                                            abi.dptr(self.mrat), abi.dptr(self.beta_p), 0,
-                                                            C.byref(cnt)))
-        self.ni_tot[0] = cnt.value
-
-
-def oracle(h, precision="f64"):
-    import pyoracle
-
-    return pyoracle.from_hybrid_arrays(h, precision=precision)
-
-
-def small(**kw):
-    base = dict(name="kat", cells=(8, 6, 6), ppc=4, seed=7)
-    base.update(kw)
-    return RunConfig(**base)
+from helpers import Host, oracle, small
 
 
 def test_rotation_is_exact_cayley():
