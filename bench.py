@@ -157,10 +157,14 @@ def cpu_sample_oracle(cfg_full, steps: int, threads: int):
     from swap_gb300.hybrid import RunConfig
 
     cells = (64, 32, 32)
+    src = dict(cfg_full.sources)
+    if "cloud_x" in src:  # keep the cloud at the centre of the sub-box
+        src.update(cloud_x=cells[0] / 2 + 1.0, cloud_y=cells[1] / 2 + 1.0, cloud_z=cells[2] / 2 + 1.0)
     cfg = RunConfig(name="cpu sample", cells=cells, ppc=cfg_full.ppc, vth=cfg_full.vth, u=cfg_full.u,
-                    dt=cfg_full.dt, ntsub=cfg_full.ntsub, nu=cfg_full.nu, seed=cfg_full.seed)
+                    dt=cfg_full.dt, ntsub=cfg_full.ntsub, nu=cfg_full.nu, seed=cfg_full.seed, sources=src)
     nx, ny, nz = cfg.nodes
-    n = cfg.n_particles
+    n = cfg.ni_max_hint()
+    n_load = cfg.n_particles
 
     class Host:  # arrays in the layout the oracle binds
         pass
@@ -172,7 +176,7 @@ def cpu_sample_oracle(cfg_full, steps: int, threads: int):
     f3 = lambda: np.zeros((n, 3), order="F")
     h.xp, h.vp, h.vp1, h.Ep, h.vplus, h.vminus = (f3() for _ in range(6))
     h.mrat, h.beta_p = np.ones(n), np.ones(n)
-    h.ni_tot = np.array([n], dtype=np.int32)
+    h.ni_tot = np.array([n_load], dtype=np.int32)
     for k, v in grd6_setup(co, cfg.b0, cfg.nu).items():
         setattr(h, k, v)
     # the same stratified Maxwellian load as the GPU run, made by the product loader
@@ -188,13 +192,16 @@ def cpu_sample_oracle(cfg_full, steps: int, threads: int):
                                                         abi.dptr(h.vp), abi.dptr(h.vp1), abi.dptr(h.mrat),
                                                         abi.dptr(h.beta_p), 0, C.byref(cnt)))
     o = pyoracle.from_hybrid_arrays(h, precision="f64", nthreads=threads)
+    if cfg.sources:
+        o.set_sources(cfg.make_sources(), 0)
     t0 = time.perf_counter()
     o.run(steps)
     dt = time.perf_counter() - t0
     info = {"sample": f"{cells[0]}x{cells[1]}x{cells[2]}-cell sub-box of the workload at {cfg.ppc} ppc "
-                      f"({n:,} ions), {steps} FP64 ion steps of the oracle",
+                      f"({n_load:,} ions), {steps} FP64 ion steps of the oracle"
+                      + (" with the workload's sources and sinks" if cfg.sources else ""),
             "seconds": dt}
-    return n * steps / dt, info
+    return n_load * steps / dt, info
 
 
 # ---------------------------------------------------------------------------
@@ -259,22 +266,26 @@ def run_ours(args):
         cfg = config(args.config, **over)
     # Each rank runs its own replica of the workload: the particle-decomposed
     # exchange (an allreduce of the moments after each deposit) is not built.
-    h = Hybrid(cfg, pinned=True)
+    h = Hybrid(cfg, ni_max=cfg.ni_max_hint(), pinned=True)
     t_load = time.perf_counter()
     h.load_maxwellian(seed=cfg.seed + 1000 * rank)
     t_load = time.perf_counter() - t_load
-    N = int(h.ni_tot[0])
+    src = cfg.make_sources()
+    if src is not None:
+        src.seed += 1000 * rank
+        h.set_sources(src, 0)
     h.sync_to_device()
 
     f32 = args.precision == "f32"
     if f32:
         h.f32_begin()
-        run = h.f32_run
+        run, count = h.f32_run, h.f32_count
     else:
-        run = h.run
+        run, count = h.run, (lambda: int(h.ni_tot[0]))
     for _ in range(args.warmup):
         run(1)
     lib, ctx = h.lib, h.ctx
+    n_before = count()
 
     # ---- timed region: K steps, device-resident, CUDA events on the library stream
     lib.swap_profile_reset(ctx)
@@ -289,6 +300,8 @@ def run_ours(args):
     run(args.steps)
     h._check(lib.swap_timer_stop(ctx, C.byref(ms)))
     clk = clocks.stop()
+    # with inflow and outflow the count drifts a little: use the mean
+    N = (n_before + count()) // 2
     lib.swap_profile_enable(ctx, 0)
     t_ms = barrier_max(ms.value, ws)
 
@@ -349,6 +362,7 @@ def run_ours(args):
         "dtype": "f32" if f32 else "f64", "data": "synthetic (seeded stratified Maxwellian load, normalized units)",
         "config": {"workload": cfg.name, "cells": list(cfg.cells), "ppc": cfg.ppc, "ions": N,
                    "subcycles": cfg.ntsub,
+                   "boundary": "x inflow/outflow, periodic y,z" if cfg.sources.get("x_open") else "periodic",
                    "precision_form": "FP32 form (int32 cell + FP32 offset, FP32 moments, FP64 B)" if f32
                    else "FP64 drop-in",
                    "l2": "inputs larger than L2 (particle state %.1f GB)" % (N * (41 if f32 else 72) / 1e9),

@@ -193,6 +193,8 @@ int swap_f32_begin(swap_ctx* ctx);
 int swap_f32_run(swap_ctx* ctx, int32_t nsteps);
 int swap_f32_end(swap_ctx* ctx);
 int swap_f32_energy(swap_ctx* ctx, double out[4]);
+/* Ions in the FP32 state (sources and sinks change it step by step). */
+int swap_f32_count(swap_ctx* ctx, int64_t* n);
 /* Validation: move particles idx[q] of the current (sorted) order by one
  * cell step per axis (dcell[q] = (dx+1) | (dy+1)<<10 | (dz+1)<<20) and run
  * the stable incremental sort that follows each ion step. */

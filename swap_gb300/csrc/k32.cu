@@ -1,12 +1,13 @@
 // k32.cu -- kernels of the FP32 form (see k32.cuh for the data layout).
 #include "k32.cuh"
+#include "philox.h"
 
 namespace swapk32 {
 namespace {
 
 constexpr int TPB = 256;
 constexpr int TPB_PASS = 128;  // particle passes: keeps the shared tiles under 48 KB
-constexpr int KERR_DOMAIN = 3, KERR_MOVE = 7;
+constexpr int KERR_DOMAIN = 3, KERR_CAPACITY = 4, KERR_MOVE = 7;
 
 inline unsigned nblk(long long n, int tpb = TPB) {
   const long long b = (n + tpb - 1) / tpb;
@@ -19,6 +20,8 @@ inline unsigned nblk(long long n, int tpb = TPB) {
 __device__ __forceinline__ void set_err(int* err, int code) {
   if (err) atomicCAS(err, 0, code);
 }
+
+constexpr uint32_t DR_BAD = 0xffffffffu, DR_DEAD = 0xfffffffeu;  // dirrank of unsorted ions
 
 __device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
@@ -62,8 +65,9 @@ __device__ __forceinline__ long long n_int(const G32& g) { return (long long)g.n
 // Move one axis of a (cell, offset) position by d cells.  upper_closed:
 // offsets in (0,1] (the '>' cell search of x and z, gutsp.f:1396-1412);
 // otherwise [0,1) (the floor of y, gutsp.f:1404).  Periodic in the cell
-// index (gutsp.f:490-510).  Returns false on a move of more than two cells.
-__device__ __forceinline__ bool move_axis(int& c, float& o, float d, int n, bool upper_closed) {
+// index (gutsp.f:490-510) when wrap; otherwise the cell may leave [0, n).
+// Returns false on a move of more than two cells.
+__device__ __forceinline__ bool move_axis(int& c, float& o, float d, int n, bool upper_closed, bool wrap = true) {
   if (!(fabsf(d) < 2.0f)) return false;
   o += d;
   // carry whole cells: (0,1] keeps o = 1 in the cell, [0,1) moves it up
@@ -76,7 +80,7 @@ __device__ __forceinline__ bool move_axis(int& c, float& o, float d, int n, bool
     o -= 1.0f;
     ++c;
   }
-  c = c < 0 ? c + n : (c >= n ? c - n : c);
+  if (wrap) c = c < 0 ? c + n : (c >= n ? c - n : c);
   return true;
 }
 
@@ -103,7 +107,7 @@ __device__ __forceinline__ int step_cell(int c, int c0, int n) {
 // particle passes
 // ---------------------------------------------------------------------------
 
-template <int PASS>
+template <int PASS, bool CHEX = false>
 __global__ void __launch_bounds__(TPB_PASS) k_pass(G32 g, Part p, Species sp, StepParams sprm,
                                               const int64_t* __restrict__ start, const float4* __restrict__ kit,
                                               float* __restrict__ partial, int* err) {
@@ -128,29 +132,58 @@ __global__ void __launch_bounds__(TPB_PASS) k_pass(G32 g, Part p, Species sp, St
 
   const float hdt = 0.5f * sprm.dt;
   const long long first = start[b * BCELLS], last = start[b * BCELLS + BCELLS];
+  unsigned n_chex = 0;
   // warp-uniform trip count: every lane takes part in the deposit reduction
   for (long long base = first; base < last; base += blockDim.x) {
     const long long l = base + threadIdx.x;
-    bool live = l < last;
+    const int32_t c = l < last ? p.cell[l] : CELL_DEAD;
+    bool live = c >= 0;  // past the range, or removed by outflow
     int t0 = -1;
     float w8[8], qdv[4];
     if (live) {
-      const int32_t c = p.cell[l];
+      const bool fresh = (c & CELL_FRESH) != 0;
       int ci = pk_i(c), cj = pk_j(c), ck = pk_k(c);
       float ox = p.ox[l], oy = p.oy[l], oz = p.oz[l];
       float vx = p.vx[l], vy = p.vy[l], vz = p.vz[l];
-      const int s = p.sp ? min((int)p.sp[l], MAX_SPECIES - 1) : 0;
-      const float mr = sp.mrat[s], qw = sp.qw[s];
+      int s = p.sp ? min((int)p.sp[l], MAX_SPECIES - 1) : 0;
+      float mr = sp.mrat[s], qw = sp.qw[s];
       float dvx = 0.f, dvy = 0.f, dvz = 0.f;  // velocity deposited
-      bool moved = false;
+      bool moved = fresh;                     // a fresh ion's cell word loses its flag
       if (PASS == 1) {
-        const float wx = p.wx[l], wy = p.wy[l], wz = p.wz[l];
-        if (sprm.pending_move) {  // maind.f:479 of the previous step
-          bool ok = move_axis(ci, ox, vx * hdt * g.inv_dx, g.ncx, true);
+        float wx = p.wx[l], wy = p.wy[l], wz = p.wz[l];
+        if (fresh && sprm.drop_fresh) {
+          live = false;  // created for a step that is not taken
+        } else if (sprm.pending_move && !fresh) {  // maind.f:479 of the previous step
+          bool ok = move_axis(ci, ox, vx * hdt * g.inv_dx, g.ncx, true, !sprm.x_open);
           ok &= move_axis(cj, oy, vy * hdt * g.inv_dy, g.ncy, false);
           ok &= move_axis(ck, oz, vz * hdt * g.inv_dz, g.ncz, true);
           if (!ok) set_err(err, KERR_MOVE);
           moved = true;
+          if (ci < 0 || ci >= g.ncx) {
+            live = false;  // outflow through an open x face
+          } else if (CHEX && sprm.heavy_of[s] != s) {
+            // res_chex of the completed step (chem_rates.f:823-840), FP32
+            const float x = (float)g.qx1 + ((float)ci + ox) * g.dx - sprm.cloud_x;
+            const float y = (float)g.qy1 + ((float)cj + oy) * g.dy - sprm.cloud_y;
+            const float z = (float)g.qz1 + ((float)ck + oz) * g.dz - sprm.cloud_z;
+            const float vrel = sqrtf(vx * vx + vy * vy + vz * vz);
+            const float sigma = vrel > 0.f ? sprm.cx_a - sprm.cx_b * logf(vrel) : 0.f;
+            if (sigma > 0.f) {
+              const float dens = sprm.cloud_N0 / (1.0f + (x * x + y * y + z * z) * sprm.inv_r0sq);
+              const float prob = sprm.dt * dens * sigma * vrel;
+              if (swapk::source_uniform_f32(sprm.seed, swapk::RNG_CHEX, sprm.chex_step, l) < prob) {
+                vx = vy = vz = 0.f;
+                wx = wy = wz = 0.f;
+                p.vx[l] = 0.f; p.vy[l] = 0.f; p.vz[l] = 0.f;
+                p.wx[l] = 0.f; p.wy[l] = 0.f; p.wz[l] = 0.f;
+                s = sprm.heavy_of[s];
+                p.sp[l] = (uint8_t)s;
+                mr = sp.mrat[s];
+                qw = sp.qw[s];
+                ++n_chex;
+              }
+            }
+          }
         }
         dvx = 1.5f * vx - 0.5f * wx;  // extrapol_up (gutsp.f:144)
         dvy = 1.5f * vy - 0.5f * wy;
@@ -198,17 +231,20 @@ __global__ void __launch_bounds__(TPB_PASS) k_pass(G32 g, Part p, Species sp, St
           vy = py + hdt * ey;
           vz = pz + hdt * ez;
           p.vx[l] = vx; p.vy[l] = vy; p.vz[l] = vz;
-          bool ok = move_axis(ci, ox, vx * hdt * g.inv_dx, g.ncx, true);
+          bool ok = move_axis(ci, ox, vx * hdt * g.inv_dx, g.ncx, true, !sprm.x_open);
           ok &= move_axis(cj, oy, vy * hdt * g.inv_dy, g.ncy, false);
           ok &= move_axis(ck, oz, vz * hdt * g.inv_dz, g.ncz, true);
           if (!ok) set_err(err, KERR_MOVE);
           moved = true;
+          if (ci < 0 || ci >= g.ncx) live = false;  // outflow through an open x face
           dvx = vx; dvy = vy; dvz = vz;
           rx = rel_cell(ci, c0x, g.ncx); ry = rel_cell(cj, c0y, g.ncy); rz = rel_cell(ck, c0z, g.ncz);
           inside = !(rx < -1 || rx > 4 || ry < -1 || ry > 4 || rz < -1 || rz > 4);
         }
       }
-      if (!inside) {
+      if (!live) {
+        p.cell[l] = CELL_DEAD;
+      } else if (!inside) {
         set_err(err, KERR_MOVE);
         live = false;
       } else {
@@ -258,6 +294,10 @@ __global__ void __launch_bounds__(TPB_PASS) k_pass(G32 g, Part p, Species sp, St
       }
     }
     __syncwarp();
+  }
+  if (CHEX) {
+    for (int o = 16; o > 0; o >>= 1) n_chex += __shfl_down_sync(0xffffffffu, n_chex, o);
+    if (lane == 0 && n_chex) atomicAdd(sprm.chex_count, (unsigned long long)n_chex);
   }
   __syncthreads();
   float* out = partial + b * (4 * TNODES);
@@ -537,7 +577,9 @@ __global__ void k_sort_prep(G32 g, const int64_t* __restrict__ start, const int3
       const long long l = base + lane;
       const bool live = l < e;
       int d = NDIR;  // sentinel for idle lanes
-      if (live) {
+      if (live && cell[l] < 0) {
+        d = NDIR + 2;  // removed (outflow): not counted, skipped by the scatter
+      } else if (live) {
         const int32_t c = cell[l];
         const int dx = step_cell(pk_i(c), i0, g.ncx), dy = step_cell(pk_j(c), j0, g.ncy),
                   dz = step_cell(pk_k(c), k0, g.ncz);
@@ -555,7 +597,7 @@ __global__ void k_sort_prep(G32 g, const int64_t* __restrict__ start, const int3
       unsigned basecnt = 0;
       if (counted) basecnt = s_cnt[w][d];
       __syncwarp();
-      if (live && !counted) dirrank[l] = 0xffffffffu;
+      if (live && !counted) dirrank[l] = d == NDIR + 2 ? DR_DEAD : DR_BAD;
       if (counted) {
         dirrank[l] = ((uint32_t)d << 26) | (basecnt + __popc(lt));
         if (lane == leader) s_cnt[w][d] = basecnt + __popc(peers);
@@ -576,8 +618,8 @@ __device__ __forceinline__ long long src_key(const G32& g, int i, int j, int k, 
 // Per new key X: the count of arriving particles and, for every direction d,
 // how many of them come from sources earlier in key order than the source of
 // d (the stable order), so the scatter needs one lookup per particle.
-__global__ void k_sort_count(G32 g, const uint16_t* __restrict__ dep, int64_t* __restrict__ count,
-                             uint16_t* __restrict__ pre, int* err) {
+__global__ void k_sort_count(G32 g, const uint16_t* __restrict__ dep, const int32_t* __restrict__ ncount,
+                             int64_t* __restrict__ count, uint16_t* __restrict__ pre, int* err) {
   GSTRIDE(X, g.nkeys) {
     int i, j, k;
     cell_of_key(g, X, i, j, k);
@@ -590,6 +632,7 @@ __global__ void k_sort_count(G32 g, const uint16_t* __restrict__ dep, int64_t* _
       n += cnt[d];
     }
     if (n > 65535) set_err(err, KERR_MOVE);
+    if (ncount) n += ncount[X];
     for (int d = 0; d < NDIR; ++d) {
       unsigned p = 0;
       for (int q = 0; q < NDIR; ++q) p += sk[q] < sk[d] ? cnt[q] : 0u;
@@ -600,12 +643,13 @@ __global__ void k_sort_count(G32 g, const uint16_t* __restrict__ dep, int64_t* _
 }
 
 // dest = start_new[X] + (arrivals from sources earlier in key order) + rank.
-__global__ void k_sort_scatter(G32 g, long long N, const int32_t* __restrict__ cell,
+__global__ void k_sort_scatter(G32 g, long long N, long long cap, const int32_t* __restrict__ cell,
                                const uint32_t* __restrict__ dirrank, const uint16_t* __restrict__ pre,
                                const int64_t* __restrict__ start_new, Part s, Part d, int* err) {
   GSTRIDE(l, N) {
     const int32_t c = cell[l];
     const uint32_t dr = dirrank[l];
+    if (dr == DR_DEAD) continue;
     const int dd = (int)(dr >> 26);
     if (dd >= NDIR) {
       set_err(err, KERR_MOVE);
@@ -613,8 +657,8 @@ __global__ void k_sort_scatter(G32 g, long long N, const int32_t* __restrict__ c
     }
     const long long X = key_of(g, pk_i(c), pk_j(c), pk_k(c));
     const long long dst = start_new[X] + pre[X * NDIR + dd] + (dr & ((1u << 26) - 1u));
-    if (dst < 0 || dst >= N) {
-      set_err(err, KERR_MOVE);
+    if (dst < 0 || dst >= cap) {
+      set_err(err, KERR_CAPACITY);
       continue;
     }
     d.cell[dst] = c;
@@ -622,6 +666,27 @@ __global__ void k_sort_scatter(G32 g, long long N, const int32_t* __restrict__ c
     d.vx[dst] = s.vx[l]; d.vy[dst] = s.vy[l]; d.vz[dst] = s.vz[l];
     d.wx[dst] = s.wx[l]; d.wy[dst] = s.wy[l]; d.wz[dst] = s.wz[l];
     if (s.sp) d.sp[dst] = s.sp[l];
+  }
+}
+
+// Staged new ions: after the arrivals of their key, in staging order.
+__global__ void k_new_scatter(G32 g, long long n_host, const int64_t* __restrict__ n_dev, long long n_max, Part s,
+                              const int32_t* __restrict__ key, const int32_t* __restrict__ rank,
+                              const int32_t* __restrict__ ncount, const int64_t* __restrict__ start_new, Part d,
+                              long long cap, int* err) {
+  const long long n = n_host + (n_dev ? *n_dev : 0);
+  GSTRIDE(q, n < n_max ? n : n_max) {
+    const long long X = key[q];
+    const long long dst = start_new[X + 1] - ncount[X] + rank[q];
+    if (dst < 0 || dst >= cap) {
+      set_err(err, KERR_CAPACITY);
+      continue;
+    }
+    d.cell[dst] = s.cell[q] | CELL_FRESH;
+    d.ox[dst] = s.ox[q]; d.oy[dst] = s.oy[q]; d.oz[dst] = s.oz[q];
+    d.vx[dst] = s.vx[q]; d.vy[dst] = s.vy[q]; d.vz[dst] = s.vz[q];
+    d.wx[dst] = s.wx[q]; d.wy[dst] = s.wy[q]; d.wz[dst] = s.wz[q];
+    d.sp[dst] = s.sp[q];
   }
 }
 
@@ -703,22 +768,6 @@ __global__ void k_scan_apply(const int64_t* __restrict__ in, long long n, const 
 // conversions and diagnostics
 // ---------------------------------------------------------------------------
 
-// FP64 position -> (cell, offset): the reference's cell rules on a uniform
-// grid (x, z: q(i) < x <= q(i+1); y: floor(y/dy)), offsets in cell units.
-__device__ __forceinline__ bool split_axis(double x, double q1, double d, int n, bool upper_closed, int& c, float& o) {
-  const double u = (x - q1) / d;  // position in cells from node 1
-  int i = upper_closed ? (int)ceil(u) - 1 : (int)floor(u);
-  if (i < 0 || i >= n) return false;
-  double f = u - (double)i;
-  if (upper_closed) { if (f <= 0.0) f = 1e-7; if (f > 1.0) f = 1.0; }
-  else { if (f < 0.0) f = 0.0; if (f >= 1.0) f = 0.99999994; }
-  c = i;
-  o = (float)f;
-  if (upper_closed && o <= 0.0f) o = 1e-7f;
-  if (!upper_closed && o >= 1.0f) o = 0.99999994f;
-  return true;
-}
-
 __global__ void k_from_f64(G32 g, long long N, long long NM, const double* __restrict__ xp,
                            const double* __restrict__ vp, const double* __restrict__ vp1,
                            const double* __restrict__ mrat, const double* __restrict__ beta_p, Species sp, Part p,
@@ -761,6 +810,15 @@ __global__ void k_to_f64(G32 g, long long N, long long NM, Part p, double* __res
     xp[l + 2 * NM] = g.qz1 + ((double)pk_k(c) + (double)p.oz[l]) * (double)g.dz;
     vp[l] = p.vx[l]; vp[l + NM] = p.vy[l]; vp[l + 2 * NM] = p.vz[l];
     vp1[l] = p.wx[l]; vp1[l + NM] = p.wy[l]; vp1[l + 2 * NM] = p.wz[l];
+  }
+}
+
+__global__ void k_species_to_f64(long long N, const uint8_t* __restrict__ spid, const double* __restrict__ tm,
+                                 const double* __restrict__ tb, double* __restrict__ mrat, double* __restrict__ beta_p) {
+  GSTRIDE(l, N) {
+    const int q = min((int)spid[l], MAX_SPECIES - 1);
+    mrat[l] = tm[q];
+    beta_p[l] = tb[q];
   }
 }
 
@@ -820,6 +878,8 @@ __device__ __forceinline__ double bsum(double v) {
 __global__ void k_energy_p(long long N, Part p, Species sp, double vol, double* acc) {
   double s = 0.0;
   GSTRIDE(l, N) {
+    const int32_t c = p.cell[l];
+    if (c < 0 || (c & CELL_FRESH)) continue;  // removed, or created for the coming step
     const int q = p.sp ? min((int)p.sp[l], MAX_SPECIES - 1) : 0;
     const double v2 = (double)p.vx[l] * p.vx[l] + (double)p.vy[l] * p.vy[l] + (double)p.vz[l] * p.vz[l];
     // 0.5 m v^2 with m = 1/mrat, times the particle's weight 1/(beta*beta_p) = qw*vol
@@ -865,6 +925,8 @@ __global__ void k_energy_f(G32 g, const double* __restrict__ b0, const double* _
 cudaError_t pass(int which, const G32& g, const Part& p, const Species& sp, const StepParams& s, const int64_t* start,
                  const float4* kit, float* partial, int* err, cudaStream_t st) {
   const unsigned grid = (unsigned)g.nbricks;
+  if (which == 1 && s.chex)
+    RET((k_pass<1, true><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, partial, err)));
   if (which == 1) RET((k_pass<1><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, partial, err)));
   if (which == 2) RET((k_pass<2><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, partial, err)));
   RET((k_pass<3><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, partial, err)));
@@ -921,8 +983,16 @@ cudaError_t sort_prep(const G32& g, const int64_t* start, const int32_t* cell, u
   if (blocks > 65535LL * 16) blocks = 65535LL * 16;
   RET((k_sort_prep<<<(unsigned)blocks, TPB, 0, st>>>(g, start, cell, dirrank, dep, err)));
 }
-cudaError_t sort_count(const G32& g, const uint16_t* dep, int64_t* count, uint16_t* pre, int* err, cudaStream_t st) {
-  RET((k_sort_count<<<nblk(g.nkeys), TPB, 0, st>>>(g, dep, count, pre, err)));
+cudaError_t sort_count(const G32& g, const uint16_t* dep, const int32_t* ncount, int64_t* count, uint16_t* pre,
+                       int* err, cudaStream_t st) {
+  RET((k_sort_count<<<nblk(g.nkeys), TPB, 0, st>>>(g, dep, ncount, count, pre, err)));
+}
+cudaError_t new_scatter(const G32& g, long long n_host, const int64_t* n_dev, long long n_max, const Part& stage,
+                        const int32_t* key, const int32_t* rank, const int32_t* ncount, const int64_t* start_new,
+                        const Part& dst, long long cap, int* err, cudaStream_t st) {
+  if (n_max <= 0) return cudaSuccess;
+  RET((k_new_scatter<<<nblk(n_max), TPB, 0, st>>>(g, n_host, n_dev, n_max, stage, key, rank, ncount, start_new, dst,
+                                                  cap, err)));
 }
 cudaError_t scan_exclusive(const int64_t* in, int64_t* out, long long n, int64_t* sums, cudaStream_t st) {
   const long long nb = (n + SCAN_TILE - 1) / SCAN_TILE;
@@ -930,10 +1000,11 @@ cudaError_t scan_exclusive(const int64_t* in, int64_t* out, long long n, int64_t
   k_scan_sums<<<1, 1024, 0, st>>>(sums, nb < 1 ? 1 : nb);
   RET((k_scan_apply<<<(unsigned)(nb < 1 ? 1 : nb), TPB, 0, st>>>(in, n, sums, out)));
 }
-cudaError_t sort_scatter(const G32& g, long long N, const int32_t* cell, const uint32_t* dirrank, const uint16_t* pre,
-                         const int64_t* start_new, const Part& src, const Part& dst, int* err, cudaStream_t st) {
+cudaError_t sort_scatter(const G32& g, long long N, long long cap, const int32_t* cell, const uint32_t* dirrank,
+                         const uint16_t* pre, const int64_t* start_new, const Part& src, const Part& dst, int* err,
+                         cudaStream_t st) {
   if (N <= 0) return cudaSuccess;
-  RET((k_sort_scatter<<<nblk(N), TPB, 0, st>>>(g, N, cell, dirrank, pre, start_new, src, dst, err)));
+  RET((k_sort_scatter<<<nblk(N), TPB, 0, st>>>(g, N, cap, cell, dirrank, pre, start_new, src, dst, err)));
 }
 cudaError_t from_f64(const G32& g, long long N, long long NM, const double* xp, const double* vp, const double* vp1,
                      const double* mrat, const double* beta_p, const Species& sp, Part p, int* err, cudaStream_t st) {
@@ -949,6 +1020,11 @@ cudaError_t to_f64(const G32& g, long long N, long long NM, const Part& p, doubl
                    cudaStream_t st) {
   if (N <= 0) return cudaSuccess;
   RET((k_to_f64<<<nblk(N), TPB, 0, st>>>(g, N, NM, p, xp, vp, vp1)));
+}
+cudaError_t species_to_f64(long long N, const uint8_t* spid, const double* tab_mrat, const double* tab_bp,
+                           double* mrat, double* beta_p, cudaStream_t st) {
+  if (N <= 0) return cudaSuccess;
+  RET((k_species_to_f64<<<nblk(N), TPB, 0, st>>>(N, spid, tab_mrat, tab_bp, mrat, beta_p)));
 }
 cudaError_t keys_of(const G32& g, long long N, const int32_t* cell, int32_t* key, cudaStream_t st) {
   if (N <= 0) return cudaSuccess;

@@ -8,6 +8,7 @@
 // and its perturbation dB = B - b0 is mirrored in FP32 for the stencils.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -45,9 +46,23 @@ struct Species {
   int n;
 };
 
+// Flags in the packed cell word.  A dead ion (outflow) is skipped by every
+// pass and dropped by the next sort; a fresh ion was created by a source for
+// the coming step, so P1 does not apply the previous step's final move to it.
+constexpr int32_t CELL_DEAD = -1;
+constexpr int32_t CELL_FRESH = 1 << 30;
+
 struct StepParams {
   float dt;
   int pending_move;  // P1: apply the previous step's final half move first
+  int x_open;        // x does not wrap; ions leaving in x are marked dead
+  int drop_fresh;    // P1 at the end of a run: fresh ions are marked dead
+  int chex;          // P1: res_chex of the step the pending move completes
+  long long chex_step;
+  uint64_t seed;
+  float cx_a, cx_b, cloud_N0, inv_r0sq, cloud_x, cloud_y, cloud_z;
+  uint8_t heavy_of[MAX_SPECIES];     // species after charge exchange
+  unsigned long long* chex_count;    // exchanges, accumulated
 };
 
 __host__ __device__ __forceinline__ int pk_i(int32_t c) { return c & 1023; }
@@ -66,6 +81,36 @@ __host__ __device__ __forceinline__ void cell_of_key(const G32& g, long long key
   i = bi * 4 + (l & 3);
   j = bj * 4 + ((l >> 2) & 3);
   k = bk * 4 + (l >> 4);
+}
+
+// FP64 position -> (cell, offset): the reference's cell rules on a uniform
+// grid (x, z: q(i) < x <= q(i+1); y: floor(y/dy)), offsets in cell units.
+__device__ __forceinline__ bool split_axis(double x, double q1, double d, int n, bool upper_closed, int& c, float& o) {
+  const double u = (x - q1) / d;  // position in cells from node 1
+  int i = upper_closed ? (int)ceil(u) - 1 : (int)floor(u);
+  if (i < 0 || i >= n) return false;
+  double f = u - (double)i;
+  if (upper_closed) { if (f <= 0.0) f = 1e-7; if (f > 1.0) f = 1.0; }
+  else { if (f < 0.0) f = 0.0; if (f >= 1.0) f = 0.99999994; }
+  c = i;
+  o = (float)f;
+  if (upper_closed && o <= 0.0f) o = 1e-7f;
+  if (!upper_closed && o >= 1.0f) o = 0.99999994f;
+  return true;
+}
+
+// Offset of x inside a known cell c, clamped to (0,1] or [0,1).
+__device__ __forceinline__ float offset_in_cell(double x, double q1, double d, int c, bool upper_closed) {
+  double f = (x - q1) / d - (double)c;
+  float o;
+  if (upper_closed) {
+    o = (float)(f > 1.0 ? 1.0 : f);
+    if (!(o > 0.0f)) o = 1e-7f;
+  } else {
+    o = (float)(f < 0.0 ? 0.0 : f);
+    if (!(o < 1.0f)) o = 0.99999994f;
+  }
+  return o;
 }
 
 // ---- particle passes ----
@@ -100,10 +145,19 @@ cudaError_t courant_min(const G32& g, const float* dbt, const float* b0c, const 
 // ---- sort ----
 cudaError_t sort_prep(const G32& g, const int64_t* start, const int32_t* cell, uint32_t* dirrank, uint16_t* dep,
                       int* err, cudaStream_t st);
-cudaError_t sort_count(const G32& g, const uint16_t* dep, int64_t* count, uint16_t* pre, int* err, cudaStream_t st);
+// ncount (may be null): new ions per key, placed after the arrivals.
+cudaError_t sort_count(const G32& g, const uint16_t* dep, const int32_t* ncount, int64_t* count, uint16_t* pre,
+                       int* err, cudaStream_t st);
 cudaError_t scan_exclusive(const int64_t* in, int64_t* out, long long n, int64_t* block_sums, cudaStream_t st);
-cudaError_t sort_scatter(const G32& g, long long N, const int32_t* cell, const uint32_t* dirrank, const uint16_t* pre,
-                         const int64_t* start_new, const Part& src, const Part& dst, int* err, cudaStream_t st);
+// Survivors to start_new[X] + pre + rank; removed ions are skipped; cap = ni_max.
+cudaError_t sort_scatter(const G32& g, long long N, long long cap, const int32_t* cell, const uint32_t* dirrank,
+                         const uint16_t* pre, const int64_t* start_new, const Part& src, const Part& dst, int* err,
+                         cudaStream_t st);
+// Staged new ions q < n_host + *n_dev (n_dev may be null) to
+// start_new[X+1] - ncount[X] + rank[q], flagged fresh; cap = ni_max.
+cudaError_t new_scatter(const G32& g, long long n_host, const int64_t* n_dev, long long n_max, const Part& stage,
+                        const int32_t* key, const int32_t* rank, const int32_t* ncount, const int64_t* start_new,
+                        const Part& dst, long long cap, int* err, cudaStream_t st);
 
 // ---- conversions ----
 cudaError_t from_f64(const G32& g, long long N, long long NM, const double* xp, const double* vp, const double* vp1,
@@ -111,6 +165,9 @@ cudaError_t from_f64(const G32& g, long long N, long long NM, const double* xp, 
                      cudaStream_t st);
 cudaError_t to_f64(const G32& g, long long N, long long NM, const Part& p, double* xp, double* vp, double* vp1,
                    cudaStream_t st);
+// mrat, beta_p from the species ids through the FP64 tables.
+cudaError_t species_to_f64(long long N, const uint8_t* spid, const double* tab_mrat, const double* tab_bp,
+                           double* mrat, double* beta_p, cudaStream_t st);
 cudaError_t keys_of(const G32& g, long long N, const int32_t* cell, int32_t* key, cudaStream_t st);
 cudaError_t gather_perm(long long N, const int64_t* perm, const Part& src, Part dst, cudaStream_t st);
 cudaError_t sorted_hist(long long N, const int32_t* key, long long nkeys, int* unsorted, int64_t* count,

@@ -76,6 +76,18 @@ SWAP_HD void source_uniforms(uint64_t seed, uint32_t stream, int64_t step, int64
   for (int q = 0; q < 4; ++q) u[q] = u01_open(r.v[q]);
 }
 
+// One uniform in (0,1) as a float, from the first word of the same block
+// (draw block 0): 24 bits, centred in its interval.
+SWAP_HD float source_uniform_f32(uint64_t seed, uint32_t stream, int64_t step, int64_t a) {
+  u32x4 c;
+  c.v[0] = (uint32_t)step;
+  c.v[1] = (uint32_t)a;
+  c.v[2] = (uint32_t)((uint64_t)a >> 32);
+  c.v[3] = 0u;
+  const u32x4 r = philox4x32_10(c, (uint32_t)seed ^ (stream * 0x9E3779B9u), (uint32_t)(seed >> 32));
+  return ((float)(r.v[0] >> 8) + 0.5f) * (1.0f / 16777216.0f);
+}
+
 enum : uint32_t { RNG_IONIZE = 1, RNG_INFLOW = 2, RNG_CLOUD = 3, RNG_CHEX = 4 };
 
 }  // namespace swapk

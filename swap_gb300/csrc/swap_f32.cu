@@ -15,6 +15,7 @@
 #include "../../include/swap_gpu.h"
 #include "k32.cuh"
 #include "swap_ctx.h"
+#include "swap_ops.h"
 #include "swap_prof.h"
 
 using namespace swapk32;
@@ -41,8 +42,14 @@ struct F32State {
   bool pending_move = false;
   double last_dtsub = 0, last_ntf = 0;
   std::vector<void*> owned;
+  // species tables (FP64, device) and the particle sources and sinks
+  double *tabm = nullptr, *tabb = nullptr;
+  srcops::F32Stage stage;
+  bool src_on = false, x_open = false, ended = false;
+  uint8_t heavy_of[MAX_SPECIES]{};
 
   ~F32State() {
+    srcops::stage_free(stage);
     for (void* p : owned) cudaFree(p);
   }
   template <class T>
@@ -85,12 +92,15 @@ static int check_err(swap_ctx* c) {
   if (herr) {
     cudaMemset(c->d_err, 0, sizeof(int));
     if (herr == 3) return c->fail(SWAP_EDOMAIN, "a particle lies outside the grid");
+    if (herr == 4) return c->fail(SWAP_ECAPACITY, "Ni_max exceeded by new ions");
     if (herr == 7)
       return c->fail(SWAP_EMOVE, "a particle moved more than one cell per axis since the last sort (|v| dt > dx)");
     return c->fail(SWAP_ECUDA, "device error flag " + std::to_string(herr));
   }
   return SWAP_OK;
 }
+
+static int sort_step(swap_ctx* c, F32State* s, long long src_step);
 
 // ---------------------------------------------------------------------------
 
@@ -99,8 +109,6 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
   TRY(c->begin());
   if (!c->h_xp || !c->h_b1) return c->fail(SWAP_EINVAL, "swap_bind_particles and swap_bind_fields are required");
   if (c->prm.grad_pe != 0.0) return c->fail(SWAP_EINVAL, "the FP32 form has no electron-pressure term");
-  if (c->have_srcs && (c->srcs.ndot > 0 || c->srcs.x_open || c->srcs.nu_ion > 0 || c->srcs.cx_a > 0))
-    return c->fail(SWAP_EINVAL, "the FP32 form has no particle sources or sinks");
   const int nx = c->dims.nx, ny = c->dims.ny, nz = c->dims.nz;
   const int ncx = nx - 2, ncy = ny - 2, ncz = nz - 2;
   if (ncx % 4 || ncy % 4 || ncz % 4 || ncx < 8 || ncy < 8 || ncz < 8 || ncx > 1024 || ncy > 1024 || ncz > 1024)
@@ -171,6 +179,27 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
     }
   }
   if (tm.empty()) { tm.push_back(1.0); tb.push_back(1.0); }
+  // species the sources create: ring ions, inflow, cloud ions, and the heavy
+  // twin (mrat_heavy, same beta_p) of every species for charge exchange
+  s->src_on = srcops::any_rule(c);
+  s->x_open = srcops::x_open(c);
+  auto species = [&](double m, double bp) -> int {
+    for (std::size_t q = 0; q < tm.size(); ++q)
+      if (tm[q] == m && tb[q] == bp) return (int)q;
+    tm.push_back(m);
+    tb.push_back(bp);
+    return (int)tm.size() - 1;
+  };
+  if (s->src_on) {
+    const swap_sources& q = c->srcs;
+    if (q.ndot > 0) s->stage.sp_ion = (uint8_t)species(q.mrat_pu, q.beta_pu);
+    if (q.x_open) s->stage.sp_inflow = (uint8_t)species(1.0, 1.0);
+    if (q.nu_ion > 0) s->stage.sp_cloud = (uint8_t)species(q.mrat_heavy, q.beta_heavy);
+  }
+  for (int q = 0; q < MAX_SPECIES; ++q) s->heavy_of[q] = (uint8_t)q;
+  if (s->src_on && c->srcs.cx_a > 0)
+    for (std::size_t q = 0, n0 = tm.size(); q < n0; ++q) s->heavy_of[q] = (uint8_t)species(c->srcs.mrat_heavy, tb[q]);
+  if (tm.size() > (std::size_t)MAX_SPECIES) return c->fail(SWAP_ECAPACITY, "more than 16 (mrat, beta_p) species");
   s->sp.n = (int)tm.size();
   for (int q = 0; q < s->sp.n; ++q) {
     s->sp.mrat[q] = (float)tm[q];
@@ -230,8 +259,8 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
   Part& tmp = s->buf[1];
   CU(from_f64(g, N, NM, xp, vp, vp1, mrat, beta_p, s->sp, tmp, c->d_err, c->st));
   {
-    double* tabm = s->alloc<double>(MAX_SPECIES);
-    double* tabb = s->alloc<double>(MAX_SPECIES);
+    double* tabm = s->tabm = s->alloc<double>(MAX_SPECIES);
+    double* tabb = s->tabb = s->alloc<double>(MAX_SPECIES);
     int* miss = s->alloc<int>(1);
     if (!tabm || !tabb || !miss) return c->fail(SWAP_ECUDA, "allocation");
     CU(cudaMemcpyAsync(tabm, tm.data(), tm.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
@@ -274,6 +303,8 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
   }
   s->cur = 0;
   s->pending_move = false;
+  TRY(check_err(c));
+  if (s->src_on) TRY(sort_step(c, s, c->src_step));  // the sources of the first step
   return check_err(c);
 }
 
@@ -331,22 +362,65 @@ static int subcycles(swap_ctx* c, F32State* s) {
   return SWAP_OK;
 }
 
-static int sort_step(swap_ctx* c, F32State* s) {
+// The stable incremental counting sort after each step (particles moved at
+// most one cell per axis since the last sort).  Removed ions are dropped;
+// with src_step >= 0 the new ions of that step's sources are placed after the
+// arrivals of their cell, flagged fresh.
+static int sort_step(swap_ctx* c, F32State* s, long long src_step) {
   const G32& g = s->g;
   Part& a = s->buf[s->cur];
   Part& b = s->buf[1 - s->cur];
+  long long n_host = 0, n_max = 0;
+  const int64_t* n_dev = nullptr;
+  if (src_step >= 0 && s->src_on) TRY(srcops::f32_stage(c, g, s->stage, src_step, &n_host, &n_dev, &n_max));
+  const bool staged = n_max > 0;
+  const long long cap = c->dims.ni_max;
   KL("f32_sort_prep", sort_prep(g, s->start, a.cell, s->dirrank, s->dep, c->d_err, c->st));
-  KL("f32_sort_count", sort_count(g, s->dep, s->count, s->pre, c->d_err, c->st));
+  KL("f32_sort_count", sort_count(g, s->dep, staged ? s->stage.ncount : nullptr, s->count, s->pre, c->d_err, c->st));
   KL("f32_sort_scan", scan_exclusive(s->count, s->start_new, g.nkeys, s->sums, c->st));
-  KL("f32_sort_scatter", sort_scatter(g, s->N, a.cell, s->dirrank, s->pre, s->start_new, a, b, c->d_err, c->st));
+  KL("f32_sort_scatter", sort_scatter(g, s->N, cap, a.cell, s->dirrank, s->pre, s->start_new, a, b, c->d_err, c->st));
+  if (staged)
+    KL("f32_new_scatter", new_scatter(g, n_host, n_dev, n_max, s->stage.part, s->stage.key, s->stage.rank,
+                                      s->stage.ncount, s->start_new, b, cap, c->d_err, c->st));
   std::swap(s->start, s->start_new);
   s->cur = 1 - s->cur;
+  if (s->src_on) {  // the count changed: the host needs it for the next launches
+    int64_t n = 0;
+    CU(cudaMemcpyAsync(&n, s->start + g.nkeys, sizeof(int64_t), cudaMemcpyDeviceToHost, c->st));
+    CU(cudaStreamSynchronize(c->st));
+    if (n > cap) return c->fail(SWAP_ECAPACITY, "Ni_max exceeded by new ions");
+    s->N = n;
+  }
   return SWAP_OK;
+}
+
+// Step parameters of the particle passes, with the sources and sinks that
+// act inside them (open-x outflow, res_chex of the completed step).
+static StepParams step_params(swap_ctx* c, F32State* s, bool pending, bool drop_fresh) {
+  StepParams p{};
+  p.dt = (float)c->prm.dt;
+  p.pending_move = pending ? 1 : 0;
+  p.x_open = s->x_open ? 1 : 0;
+  p.drop_fresh = drop_fresh ? 1 : 0;
+  const swap_sources& q = c->srcs;
+  p.chex = (s->src_on && q.cx_a > 0 && pending) ? 1 : 0;
+  p.chex_step = c->src_step - 1;  // the step the pending move completes
+  p.seed = q.seed;
+  p.cx_a = (float)q.cx_a;
+  p.cx_b = (float)q.cx_b;
+  p.cloud_N0 = (float)q.cloud_N0;
+  p.inv_r0sq = q.cloud_r0 > 0 ? (float)(1.0 / (q.cloud_r0 * q.cloud_r0)) : 0.f;
+  p.cloud_x = (float)q.cloud_x;
+  p.cloud_y = (float)q.cloud_y;
+  p.cloud_z = (float)q.cloud_z;
+  for (int k = 0; k < MAX_SPECIES; ++k) p.heavy_of[k] = s->heavy_of[k];
+  p.chex_count = p.chex ? srcops::counters(c) + 1 : nullptr;
+  return p;
 }
 
 static int one_step(swap_ctx* c, F32State* s) {
   const G32& g = s->g;
-  StepParams sp{(float)c->prm.dt, s->pending_move ? 1 : 0};
+  const StepParams sp = step_params(c, s, s->pending_move, false);
   const Part& p = s->buf[s->cur];
   KL("f32_P1", pass(1, g, p, s->sp, sp, s->start, s->kit, s->partial, c->d_err, c->st));  // :479,385-387,399
   TRY(finish_deposit(c, s, 4));
@@ -358,8 +432,9 @@ static int one_step(swap_ctx* c, F32State* s) {
   KL("f32_P3", pass(3, g, p, s->sp, sp, s->start, s->kit, s->partial, c->d_err, c->st));  // :404-413
   TRY(finish_deposit(c, s, 4));
   TRY(subcycles(c, s));                                                            // :420-476
-  TRY(sort_step(c, s));
+  TRY(sort_step(c, s, c->src_step + 1));  // with the sources of the next step
   s->pending_move = true;                                                          // :479 next P1
+  if (c->have_srcs) c->src_step++;
   return SWAP_OK;
 }
 
@@ -367,16 +442,19 @@ extern "C" int swap_f32_run(swap_ctx* c, int32_t nsteps) {
   if (!c) return SWAP_EINVAL;
   F32State* s = f32(c);
   if (!s) return c->fail(SWAP_EINVAL, "swap_f32_begin has not been called");
+  if (s->ended && s->src_on) return c->fail(SWAP_EINVAL, "call swap_f32_begin again after swap_f32_end");
   for (int k = 0; k < nsteps; ++k) TRY(one_step(c, s));
   return check_err(c);
 }
 
-// Apply a pending final half move (maind.f:479) in place.
+// Apply a pending final half move (maind.f:479) in place, with the outflow
+// and res_chex that follow it; ions created for a step not taken are dropped.
 static int flush_move(swap_ctx* c, F32State* s) {
-  if (!s->pending_move) return SWAP_OK;
-  StepParams sp{(float)c->prm.dt, 1};
+  if (!s->pending_move && !s->src_on) return SWAP_OK;
+  const StepParams sp = step_params(c, s, s->pending_move, true);
   KL("f32_P1", pass(1, s->g, s->buf[s->cur], s->sp, sp, s->start, s->kit, s->partial, c->d_err, c->st));
   s->pending_move = false;
+  if (s->src_on) TRY(sort_step(c, s, -1));
   return SWAP_OK;
 }
 
@@ -398,8 +476,14 @@ extern "C" int swap_f32_end(swap_ctx* c) {
   TRY(c->use(c->h_up, Access::Out, &upd));
   TRY(c->use(c->h_E, Access::Out, &Ed));
   TRY(c->use(c->h_aj, Access::Out, &ajd));
+  double *mratd, *bpd;
+  TRY(c->use(c->h_mrat, Access::Out, &mratd));
+  TRY(c->use(c->h_beta_p, Access::Out, &bpd));
   const G32& g = s->g;
   CU(to_f64(g, s->N, c->dims.ni_max, s->buf[s->cur], xp, vp, vp1, c->st));
+  CU(species_to_f64(s->N, s->buf[s->cur].sp, s->tabm, s->tabb, mratd, bpd, c->st));
+  *c->ni_tot_ptr = (int32_t)s->N;
+  s->ended = true;
   const std::size_t b3 = 3 * (std::size_t)g.C * sizeof(double);
   CU(cudaMemcpyAsync(b1, s->b1, b3, cudaMemcpyDeviceToDevice, c->st));
   CU(cudaMemcpyAsync(bt, s->b1, b3, cudaMemcpyDeviceToDevice, c->st));
@@ -413,6 +497,14 @@ extern "C" int swap_f32_end(swap_ctx* c) {
   c->last_dtsub = s->last_dtsub;
   c->last_ntf = s->last_ntf;
   return r;
+}
+
+extern "C" int swap_f32_count(swap_ctx* c, int64_t* n) {
+  if (!c || !n) return SWAP_EINVAL;
+  F32State* s = f32(c);
+  if (!s) return c->fail(SWAP_EINVAL, "swap_f32_begin has not been called");
+  *n = s->N;
+  return SWAP_OK;
 }
 
 extern "C" int swap_f32_energy(swap_ctx* c, double out[4]) {
@@ -462,6 +554,6 @@ extern "C" int swap_f32_displace_resort(swap_ctx* c, int64_t n, const int64_t* i
     k_displace<<<(unsigned)((n + 255) / 256), 256, 0, c->st>>>(s->g, s->buf[s->cur], n, di, dd);
     CU(cudaGetLastError());
   }
-  TRY(sort_step(c, s));
+  TRY(sort_step(c, s, -1));
   return check_err(c);
 }

@@ -2,6 +2,7 @@
 // of the FP64 drop-in; every pointer argument is a device pointer.
 #pragma once
 
+#include "k32.cuh"
 #include "swap_ctx.h"
 
 namespace ops {
@@ -22,4 +23,22 @@ int after_move(swap_ctx* c, double* xp, double* vp, double* vp1);
 // End of a fused step: res_chex, then the step counter advances.
 int step_end(swap_ctx* c, double* xp, double* vp, double* vp1);
 void free_all(swap_ctx* c);
+// [0] last res_chex, [1] total exchanges (allocated on first use).
+unsigned long long* counters(swap_ctx* c);
+
+// New ions of one step staged for the FP32 form's sort: their state, the
+// key of their cell, their rank among the new ions of that key, and the
+// count per key.  Grown on demand; freed by stage_free.
+struct F32Stage {
+  swapk32::Part part{};
+  int32_t *key = nullptr, *rank = nullptr, *ncount = nullptr;
+  long long cap = 0, nkeys = 0;
+  uint8_t sp_ion = 0, sp_cloud = 0, sp_inflow = 0;
+};
+bool any_rule(const swap_ctx* c);
+// Stage the new ions of step m: n_host + *n_dev ions (n_dev may be null), at
+// most n_max, in staging order ionize, cloud, inflow.
+int f32_stage(swap_ctx* c, const swapk32::G32& g, F32Stage& st, long long m, long long* n_host,
+              const int64_t** n_dev, long long* n_max);
+void stage_free(F32Stage& st);
 }  // namespace srcops

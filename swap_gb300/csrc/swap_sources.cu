@@ -13,7 +13,9 @@
 #include "../../include/swap_gpu.h"
 #include "k32.cuh"
 #include "k64.cuh"
+#include "swap_dev.cuh"
 #include "philox.h"
+#include "sources_dev.cuh"
 #include "swap_ctx.h"
 #include "swap_ops.h"
 #include "swap_prof.h"
@@ -30,47 +32,20 @@ struct PView {
   long long NM;
 };
 
-// Ionize_sw_mp's new ions (chem_rates.f:567-620): ring velocity, uniform
-// position in the box, pickup mrat and beta_pu.
+// Ionize_sw_mp's new ions (chem_rates.f:567-620), appended after N.
 __global__ void k_ionize(Geo g, PView p, long long N, long long n, swap_sources s, long long step) {
-  const double twopi = 2.0 * 3.14159265358979323846;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-    double u[4];
-    source_uniforms(s.seed, RNG_IONIZE, step, q, 1u, u);
+    double st[6];
+    swapsrc::ionize_state(g, s, step, q, st);
     const long long l = N + q, NM = p.NM;
-    const double th = u[0] * twopi;
-    p.vp[l] = s.vsw + s.vsw * cos(th);
-    p.vp[l + NM] = s.vsw * sin(th);
-    p.vp[l + 2 * NM] = 0.0;
-    p.xp[l] = g.qx[1] + (1.0 - u[1]) * (g.qx[g.nx - 1] - g.qx[1]);
-    p.xp[l + NM] = g.qy[1] + (1.0 - u[2]) * (g.qy[g.ny - 1] - g.qy[1]);
-    p.xp[l + 2 * NM] = g.qz[1] + (1.0 - u[3]) * (g.qz[g.nz - 1] - g.qz[1]);
-    for (int m = 0; m < 3; ++m) p.vp1[l + m * NM] = p.vp[l + m * NM];
+    for (int m = 0; m < 3; ++m) {
+      p.xp[l + m * NM] = st[m];
+      p.vp[l + m * NM] = st[3 + m];
+      p.vp1[l + m * NM] = st[3 + m];
+    }
     p.mrat[l] = s.mrat_pu;
     p.beta_p[l] = s.beta_pu;
   }
-}
-
-// Inflow: the ghost-slab candidate of slot (ck, cj, pp); returns whether
-// its ballistic move over dt crosses x = q(1) into the box, and the state.
-__device__ __forceinline__ bool inflow_candidate(const Geo& g, const swap_sources& s, long long step, long long slot,
-                                                 int cj, int ck, double dt, double st[6]) {
-  const double pi = 3.14159265358979323846;
-  double u[4], v[4], e[4];
-  source_uniforms(s.seed, RNG_INFLOW, step, slot, 0u, u);
-  source_uniforms(s.seed, RNG_INFLOW, step, slot, 1u, v);
-  source_uniforms(s.seed, RNG_INFLOW, step, slot, 2u, e);
-  const double vx = s.inflow_ux + s.inflow_vth * sqrt(-log(u[3])) * cos(pi * v[0]);
-  const double vy = s.inflow_uy + s.inflow_vth * sqrt(-log(v[1])) * cos(pi * v[2]);
-  const double vz = s.inflow_uz + s.inflow_vth * sqrt(-log(v[3])) * cos(pi * e[0]);
-  const double x0 = g.qx[1], dxg = g.dxg[1];
-  const double xg = x0 - dxg + u[0] * dxg;
-  const double xn = xg + dt * vx;
-  st[0] = xn;
-  st[1] = g.qy[cj + 1] + u[1] * (g.qy[cj + 2] - g.qy[cj + 1]);
-  st[2] = g.qz[ck + 1] + u[2] * (g.qz[ck + 2] - g.qz[ck + 1]);
-  st[3] = vx; st[4] = vy; st[5] = vz;
-  return xn > x0 && !(xn > g.qx[g.nx - 1]);
 }
 
 __global__ void k_inflow_flags(Geo g, swap_sources s, long long step, double dt, int64_t* flag) {
@@ -79,7 +54,7 @@ __global__ void k_inflow_flags(Geo g, swap_sources s, long long step, double dt,
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nslot; t += (long long)gridDim.x * blockDim.x) {
     const int cj = (int)((t / ppc) % ncy), ck = (int)(t / ((long long)ppc * ncy));
     double st[6];
-    flag[t] = inflow_candidate(g, s, step, t, cj, ck, dt, st) ? 1 : 0;
+    flag[t] = swapsrc::inflow_candidate(g, s, step, t, cj, ck, dt, st) ? 1 : 0;
   }
 }
 
@@ -91,40 +66,29 @@ __global__ void k_inflow_write(Geo g, PView p, swap_sources s, long long step, d
     if (!flag[t]) continue;
     const int cj = (int)((t / ppc) % ncy), ck = (int)(t / ((long long)ppc * ncy));
     double st[6];
-    inflow_candidate(g, s, step, t, cj, ck, dt, st);
+    swapsrc::inflow_candidate(g, s, step, t, cj, ck, dt, st);
     const long long l = N + pos[t];
-    p.xp[l] = st[0]; p.xp[l + NM] = st[1]; p.xp[l + 2 * NM] = st[2];
-    for (int m = 0; m < 3; ++m) { p.vp[l + m * NM] = st[3 + m]; p.vp1[l + m * NM] = st[3 + m]; }
+    for (int m = 0; m < 3; ++m) {
+      p.xp[l + m * NM] = st[m];
+      p.vp[l + m * NM] = st[3 + m];
+      p.vp1[l + m * NM] = st[3 + m];
+    }
     p.mrat[l] = 1.0;
     p.beta_p[l] = 1.0;
   }
 }
 
-__device__ __forceinline__ double cloud_density(const swap_sources& s, double x, double y, double z) {
-  const double dx = x - s.cloud_x, dy = y - s.cloud_y, dz = z - s.cloud_z;
-  const double r2 = (dx * dx + dy * dy + dz * dz) / (s.cloud_r0 * s.cloud_r0);
-  return s.cloud_N0 / (1.0 + r2);
-}
-
-// Cloud ionization: new heavy ions of one cell: floor(lambda) + Bernoulli(remainder).
+// Cloud ionization: per-cell counts (the oracle's cell order, x fastest).
 __global__ void k_cloud_count(Geo g, swap_sources s, long long step, double dt, double beta, int64_t* cnt) {
   const int ncx = g.nx - 2, ncy = g.ny - 2, ncz = g.nz - 2;
   const long long ncell = (long long)ncx * ncy * ncz;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncell; c += (long long)gridDim.x * blockDim.x) {
     const int ci = (int)(c % ncx), cj = (int)((c / ncx) % ncy), ck = (int)(c / ((long long)ncx * ncy));
-    const double xc = 0.5 * (g.qx[ci + 1] + g.qx[ci + 2]);
-    const double yc = 0.5 * (g.qy[cj + 1] + g.qy[cj + 2]);
-    const double zc = 0.5 * (g.qz[ck + 1] + g.qz[ck + 2]);
-    const double vol = g.dxg[ci + 1] * g.dyg[cj + 1] * g.dzg[ck + 1];
-    const double lam = vol * beta * s.beta_heavy * cloud_density(s, xc, yc, zc) * s.nu_ion * dt;
-    long long n = (long long)floor(lam);
-    double u[4];
-    source_uniforms(s.seed, RNG_CLOUD, step, c, 0u, u);
-    if (u[0] < lam - (double)n) ++n;
-    cnt[c] = n;
+    cnt[c] = swapsrc::cloud_count(g, s, step, dt, beta, ci, cj, ck, c);
   }
 }
 
+// New heavy ions at rest, uniform in their cell (mrat_heavy, beta_heavy).
 __global__ void k_cloud_write(Geo g, PView p, swap_sources s, long long step, const int64_t* cnt, const int64_t* pos,
                               long long N) {
   const int ncx = g.nx - 2, ncy = g.ny - 2, ncz = g.nz - 2;
@@ -132,34 +96,29 @@ __global__ void k_cloud_write(Geo g, PView p, swap_sources s, long long step, co
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncell; c += (long long)gridDim.x * blockDim.x) {
     const int ci = (int)(c % ncx), cj = (int)((c / ncx) % ncy), ck = (int)(c / ((long long)ncx * ncy));
     for (long long q = 0; q < cnt[c]; ++q) {
-      double u[4];
-      source_uniforms(s.seed, RNG_CLOUD, step, c, (uint32_t)(1 + q), u);
+      double x[3];
+      swapsrc::cloud_position(g, s, step, ci, cj, ck, c, q, x);
       const long long l = N + pos[c] + q;
-      p.xp[l] = g.qx[ci + 1] + u[0] * (g.qx[ci + 2] - g.qx[ci + 1]);
-      p.xp[l + NM] = g.qy[cj + 1] + u[1] * (g.qy[cj + 2] - g.qy[cj + 1]);
-      p.xp[l + 2 * NM] = g.qz[ck + 1] + u[2] * (g.qz[ck + 2] - g.qz[ck + 1]);
-      for (int m = 0; m < 3; ++m) { p.vp[l + m * NM] = 0.0; p.vp1[l + m * NM] = 0.0; }
+      for (int m = 0; m < 3; ++m) {
+        p.xp[l + m * NM] = x[m];
+        p.vp[l + m * NM] = 0.0;
+        p.vp1[l + m * NM] = 0.0;
+      }
       p.mrat[l] = s.mrat_heavy;
       p.beta_p[l] = s.beta_heavy;
     }
   }
 }
 
-// Charge exchange after res_chex (chem_rates.f:823-840).
+// Charge exchange after res_chex (chem_rates.f:823-840): the new ion is heavy
+// and at rest; ions already heavy are skipped.
 __global__ void k_chex(PView p, long long N, swap_sources s, long long step, double dt, unsigned long long* count) {
   const long long NM = p.NM;
   unsigned long long mine = 0;
   for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x) {
     if (p.mrat[l] == s.mrat_heavy) continue;
-    const double vx = p.vp[l], vy = p.vp[l + NM], vz = p.vp[l + 2 * NM];
-    const double vrel = sqrt(vx * vx + vy * vy + vz * vz);
-    if (!(vrel > 0.0)) continue;
-    const double sigma = s.cx_a - s.cx_b * log(vrel);
-    if (!(sigma > 0.0)) continue;
-    const double prob = dt * cloud_density(s, p.xp[l], p.xp[l + NM], p.xp[l + 2 * NM]) * sigma * vrel;
-    double u[4];
-    source_uniforms(s.seed, RNG_CHEX, step, l, 0u, u);
-    if (u[0] < prob) {
+    if (swapsrc::chex_trial(s, step, l, dt, p.xp[l], p.xp[l + NM], p.xp[l + 2 * NM], p.vp[l], p.vp[l + NM],
+                            p.vp[l + 2 * NM])) {
       for (int m = 0; m < 3; ++m) { p.vp[l + m * NM] = 0.0; p.vp1[l + m * NM] = 0.0; }
       p.mrat[l] = s.mrat_heavy;
       ++mine;
@@ -184,6 +143,97 @@ __global__ void k_compact(const T* __restrict__ src, T* __restrict__ dst, long l
                           const int64_t* __restrict__ pos) {
   for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x)
     if (keep[l]) dst[pos[l]] = src[l];
+}
+
+// ---- the FP32 form: new ions staged for the sort ----
+
+using swapk32::G32;
+using swapk32::key_of;
+using swapk32::offset_in_cell;
+using swapk32::pk;
+
+__device__ __forceinline__ void stage_one(swapk32::Part& st, long long q, int ci, int cj, int ck, float ox, float oy,
+                                          float oz, const double v[3], uint8_t sp) {
+  st.cell[q] = pk(ci, cj, ck);
+  st.ox[q] = ox; st.oy[q] = oy; st.oz[q] = oz;
+  st.vx[q] = (float)v[0]; st.vy[q] = (float)v[1]; st.vz[q] = (float)v[2];
+  st.wx[q] = (float)v[0]; st.wy[q] = (float)v[1]; st.wz[q] = (float)v[2];
+  st.sp[q] = sp;
+}
+
+// Ring ions anywhere in the box: state and key; ranks follow sequentially.
+__global__ void k32_stage_ionize(Geo g64, G32 g, swap_sources s, long long step, long long n, swapk32::Part st,
+                                 int32_t* key, uint8_t sp, int* err) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+    double x[6];
+    swapsrc::ionize_state(g64, s, step, q, x);
+    int ci = 0, cj = 0, ck = 0;
+    float ox = 0.5f, oy = 0.5f, oz = 0.5f;
+    const bool ok = swapk32::split_axis(x[0], g.qx1, g.dx, g.ncx, true, ci, ox) &&
+                    swapk32::split_axis(x[1], g.qy1, g.dy, g.ncy, false, cj, oy) &&
+                    swapk32::split_axis(x[2], g.qz1, g.dz, g.ncz, true, ck, oz);
+    if (!ok) atomicCAS(err, 0, KERR_DOMAIN);
+    stage_one(st, q, ci, cj, ck, ox, oy, oz, x + 3, sp);
+    key[q] = (int32_t)key_of(g, ci, cj, ck);
+  }
+}
+
+// Ranks of n staged ions among the new ions of their key, in staging order.
+__global__ void k32_rank_seq(long long n, const int32_t* key, int32_t* rank, int32_t* ncount) {
+  for (long long q = 0; q < n; ++q) rank[q] = ncount[key[q]]++;
+}
+
+// Cloud ions of cell c (the restatement's cell order), staged at base+pos[c].
+__global__ void k32_stage_cloud(Geo g64, G32 g, swap_sources s, long long step, const int64_t* cnt,
+                                const int64_t* pos, long long base, swapk32::Part st, int32_t* key, int32_t* rank,
+                                int32_t* ncount, uint8_t sp) {
+  const long long ncell = (long long)g.ncx * g.ncy * g.ncz;
+  const double zero[3] = {0.0, 0.0, 0.0};
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncell; c += (long long)gridDim.x * blockDim.x) {
+    const long long n = cnt[c];
+    if (n == 0) continue;
+    const int ci = (int)(c % g.ncx), cj = (int)((c / g.ncx) % g.ncy), ck = (int)(c / ((long long)g.ncx * g.ncy));
+    const int32_t X = (int32_t)key_of(g, ci, cj, ck);
+    const int32_t r0 = ncount[X];
+    for (long long q = 0; q < n; ++q) {
+      double x[3];
+      swapsrc::cloud_position(g64, s, step, ci, cj, ck, c, q, x);
+      const long long o = base + pos[c] + q;
+      stage_one(st, o, ci, cj, ck, offset_in_cell(x[0], g.qx1, g.dx, ci, true),
+                offset_in_cell(x[1], g.qy1, g.dy, cj, false), offset_in_cell(x[2], g.qz1, g.dz, ck, true), zero, sp);
+      key[o] = X;
+      rank[o] = r0 + (int32_t)q;
+    }
+    ncount[X] = r0 + (int32_t)n;
+  }
+}
+
+// Inflow ions of face cell (cj, ck): all enter physical cell (0, cj, ck);
+// staged at base+pos[slot] in slot order.
+__global__ void k32_stage_inflow(Geo g64, G32 g, swap_sources s, long long step, double dt, const int64_t* flag,
+                                 const int64_t* pos, long long base, swapk32::Part st, int32_t* key, int32_t* rank,
+                                 int32_t* ncount, uint8_t sp, int* err) {
+  const long long nface = (long long)g.ncy * g.ncz;
+  const int ppc = s.inflow_ppc;
+  for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < nface; f += (long long)gridDim.x * blockDim.x) {
+    const int cj = (int)(f % g.ncy), ck = (int)(f / g.ncy);
+    const int32_t X = (int32_t)key_of(g, 0, cj, ck);
+    const int32_t r0 = ncount[X];
+    int32_t k = 0;
+    for (int p = 0; p < ppc; ++p) {
+      const long long slot = f * ppc + p;
+      if (!flag[slot]) continue;
+      double x[6];
+      swapsrc::inflow_candidate(g64, s, step, slot, cj, ck, dt, x);
+      if ((x[0] - g.qx1) / g.dx > 1.0) atomicCAS(err, 0, KERR_MOVE);  // entered past the first cell
+      const long long o = base + pos[slot];
+      stage_one(st, o, 0, cj, ck, offset_in_cell(x[0], g.qx1, g.dx, 0, true),
+                offset_in_cell(x[1], g.qy1, g.dy, cj, false), offset_in_cell(x[2], g.qz1, g.dz, ck, true), x + 3, sp);
+      key[o] = X;
+      rank[o] = r0 + k++;
+    }
+    ncount[X] = r0 + k;
+  }
 }
 
 }  // namespace
@@ -438,6 +488,106 @@ int step_end(swap_ctx* c, double* xp, double* vp, double* vp1) {
     CU(cudaGetLastError());
   }
   c->src_step++;
+  return SWAP_OK;
+}
+
+unsigned long long* counters(swap_ctx* c) {
+  return src_scratch(c, 0) == SWAP_OK ? c->src_cnt : nullptr;
+}
+
+bool any_rule(const swap_ctx* c) {
+  const swap_sources& s = c->srcs;
+  return c->have_srcs && (s.ndot > 0 || s.x_open || s.nu_ion > 0 || s.cx_a > 0);
+}
+
+void stage_free(F32Stage& st) {
+  swapk32::Part& p = st.part;
+  for (void* q : {(void*)p.cell, (void*)p.ox, (void*)p.oy, (void*)p.oz, (void*)p.vx, (void*)p.vy, (void*)p.vz,
+                  (void*)p.wx, (void*)p.wy, (void*)p.wz, (void*)p.sp, (void*)st.key, (void*)st.rank, (void*)st.ncount})
+    if (q) cudaFree(q);
+  st.part = swapk32::Part{};
+  st.key = st.rank = st.ncount = nullptr;
+  st.cap = st.nkeys = 0;
+}
+
+static int stage_reserve(swap_ctx* c, F32Stage& st, long long need, long long nkeys) {
+  if (!st.ncount || st.nkeys != nkeys) {
+    if (st.ncount) cudaFree(st.ncount);
+    st.ncount = nullptr;
+    if (cudaMalloc(&st.ncount, (std::size_t)nkeys * sizeof(int32_t)) != cudaSuccess)
+      return c->fail(SWAP_ECUDA, "allocation of the new-ion counts failed");
+    st.nkeys = nkeys;
+  }
+  if (need <= st.cap) return SWAP_OK;
+  CU(cudaStreamSynchronize(c->st));
+  int32_t* nc = st.ncount;
+  const long long nk = st.nkeys;
+  st.ncount = nullptr;
+  stage_free(st);
+  st.ncount = nc;
+  st.nkeys = nk;
+  const long long cap = need + need / 4 + 1024;
+  swapk32::Part& p = st.part;
+  void** f4[] = {(void**)&p.ox, (void**)&p.oy, (void**)&p.oz, (void**)&p.vx, (void**)&p.vy, (void**)&p.vz,
+                 (void**)&p.wx, (void**)&p.wy, (void**)&p.wz, (void**)&p.cell, (void**)&st.key, (void**)&st.rank};
+  for (void** a : f4)
+    if (cudaMalloc(a, (std::size_t)cap * 4) != cudaSuccess) return c->fail(SWAP_ECUDA, "staging allocation failed");
+  if (cudaMalloc((void**)&p.sp, (std::size_t)cap) != cudaSuccess) return c->fail(SWAP_ECUDA, "staging allocation failed");
+  st.cap = cap;
+  return SWAP_OK;
+}
+
+int f32_stage(swap_ctx* c, const swapk32::G32& g, F32Stage& st, long long m, long long* n_host,
+              const int64_t** n_dev, long long* n_max) {
+  *n_host = 0;
+  *n_dev = nullptr;
+  *n_max = 0;
+  const swap_sources& s = c->srcs;
+  if (!any_rule(c)) return SWAP_OK;
+  const long long n_ion = s.ndot > 0 ? ionize_count(c, m) : 0;
+  const long long ncell = (long long)g.ncx * g.ncy * g.ncz;
+  const long long nslot = s.x_open ? (long long)g.ncy * g.ncz * s.inflow_ppc : 0;
+  long long n_cloud = 0;
+  if (s.nu_ion > 0) {
+    TRY(src_scratch(c, ncell));
+    {
+      ProfScope ps(c, "f32_src_cloud_count", c->st);
+      k_cloud_count<<<nb(ncell), TPB, 0, c->st>>>(c->g, s, m, c->prm.dt, c->prm.beta, c->src_flag);
+    }
+    CU(cudaGetLastError());
+    TRY(scan_count(c, ncell, &n_cloud));
+  }
+  TRY(stage_reserve(c, st, n_ion + n_cloud + nslot, g.nkeys));
+  CU(cudaMemsetAsync(st.ncount, 0, (std::size_t)g.nkeys * sizeof(int32_t), c->st));
+  if (n_ion > 0) {
+    ProfScope ps(c, "f32_src_ionize", c->st);
+    k32_stage_ionize<<<nb(n_ion), TPB, 0, c->st>>>(c->g, g, s, m, n_ion, st.part, st.key, st.sp_ion, c->d_err);
+    k32_rank_seq<<<1, 1, 0, c->st>>>(n_ion, st.key, st.rank, st.ncount);
+  }
+  CU(cudaGetLastError());
+  if (n_cloud > 0) {
+    ProfScope ps(c, "f32_src_cloud", c->st);
+    k32_stage_cloud<<<nb(ncell), TPB, 0, c->st>>>(c->g, g, s, m, c->src_flag, c->src_pos, n_ion, st.part, st.key,
+                                                  st.rank, st.ncount, st.sp_cloud);
+  }
+  CU(cudaGetLastError());
+  if (nslot > 0) {
+    TRY(src_scratch(c, nslot));
+    {
+      ProfScope ps(c, "f32_src_inflow", c->st);
+      k_inflow_flags<<<nb(nslot), TPB, 0, c->st>>>(c->g, s, m, c->prm.dt, c->src_flag);
+      CU(cudaGetLastError());
+      CU(swapk32::scan_exclusive(c->src_flag, c->src_pos, nslot, c->src_sums, c->st));
+      const long long nface = (long long)g.ncy * g.ncz;
+      k32_stage_inflow<<<nb(nface), TPB, 0, c->st>>>(c->g, g, s, m, c->prm.dt, c->src_flag, c->src_pos,
+                                                     n_ion + n_cloud, st.part, st.key, st.rank, st.ncount,
+                                                     st.sp_inflow, c->d_err);
+    }
+    CU(cudaGetLastError());
+    *n_dev = c->src_pos + nslot;
+  }
+  *n_host = n_ion + n_cloud;
+  *n_max = n_ion + n_cloud + nslot;
   return SWAP_OK;
 }
 

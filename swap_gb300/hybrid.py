@@ -35,6 +35,7 @@ class RunConfig:
     steps: int = 100
     seed: int = 1
     grad_pe: float = 0.0
+    sources: dict = field(default_factory=dict)  # swap_sources fields; empty = periodic box, no sources
     extra: dict = field(default_factory=dict)
 
     @property
@@ -54,16 +55,48 @@ class RunConfig:
         # one macro-particle per cell of volume 1 carries n0/ppc
         return self.ppc / self.n0
 
+    def make_sources(self):
+        """The workload's sources and sinks as an abi.Sources (None when it has none)."""
+        return abi.make_sources(**self.sources) if self.sources else None
+
+    def ni_max_hint(self) -> int:
+        """Particle capacity with headroom for a workload whose count varies."""
+        n = self.n_particles
+        return n if not self.sources else int(n * 1.05) + 4096
+
 
 def config(n: int, **over) -> RunConfig:
-    """The named workloads: 0 = 64x32x32 cells, 16 ppc (1,048,576 ions; the
-    stated 524,288 is 8 ppc); 1 = 256x128x128 cells, 32 ppc (134,217,728 ions)."""
+    """The named workloads.
+
+    0: periodic box of 64x32x32 cells, 16 ppc (1,048,576 ions; the stated
+       524,288 is 8 ppc), u = (2,0,0), 100 steps, seed 1.
+    1: 256x128x128 cells, 32 ppc (134,217,728 ions), 200 steps, seed 2, with
+       the x axis open: a drifting Maxwellian (u = (2,0,0), vth 0.5) enters
+       through x = q(1) from a one-cell slab of 32 ions per face cell and ions
+       leaving in x are removed; periodic in y and z.
+    2: 256x128x128 cells, 16 ppc solar-wind H+ at u = (4,0,0) through an open
+       x axis, a neutral cloud N0/(1+(r/5)^2) at the box centre (N0 = 1000)
+       ionized at 1e-3 Omega_i into mass-16 ions at rest, charge exchange
+       sigma = 1 - 0.1 ln v_rel; 300 steps, seed 3.
+    """
     base = {
         0: dict(name="uniform H+ 64x32x32, 16 ppc", cells=(64, 32, 32), ppc=16, steps=100, seed=1),
-        1: dict(name="uniform H+ 256x128x128, 32 ppc", cells=(256, 128, 128), ppc=32, steps=200, seed=2),
+        1: dict(name="H+ 256x128x128, 32 ppc, x inflow/outflow", cells=(256, 128, 128), ppc=32, steps=200,
+                seed=2),
+        2: dict(name="pickup ions 256x128x128, 16 ppc, cloud + charge exchange", cells=(256, 128, 128), ppc=16,
+                u=(4.0, 0.0, 0.0), steps=300, seed=3),
     }[n]
     base.update(over)
-    return RunConfig(**base)
+    cfg = RunConfig(**base)
+    if n in (1, 2) and "sources" not in over:
+        src = dict(seed=cfg.seed, x_open=1, inflow_ppc=cfg.ppc, inflow_vth=cfg.vth, inflow_ux=cfg.u[0],
+                   inflow_uy=cfg.u[1], inflow_uz=cfg.u[2])
+        if n == 2:
+            cx, cy, cz = (c / 2.0 + 1.0 for c in cfg.cells)  # box centre (q(1) = 1 with unit spacing)
+            src.update(cloud_N0=1000.0, cloud_r0=5.0, cloud_x=cx, cloud_y=cy, cloud_z=cz, nu_ion=1e-3,
+                       mrat_heavy=1.0 / 16.0, beta_heavy=1.0, cx_a=1.0, cx_b=0.1)
+        cfg.sources = src
+    return cfg
 
 
 class Hybrid:
@@ -275,6 +308,12 @@ class Hybrid:
     def f32_end(self):
         """Write the FP32 state back into the bound arrays (device copies); then sync_to_host."""
         self._check(self.lib.swap_f32_end(self.ctx))
+
+    def f32_count(self) -> int:
+        """Ions in the FP32 form's state (the count changes with sources and sinks)."""
+        n = C.c_int64()
+        self._check(self.lib.swap_f32_count(self.ctx, C.byref(n)))
+        return n.value
 
     def f32_energy(self):
         out = np.zeros(4)
