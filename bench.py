@@ -134,14 +134,13 @@ KERNEL_BYTES_F32 = {
     "f32_sort_scatter": 41 + 4 + 41,
     "f32_sort_prep": 4 + 4,
 }
-# per interior node (FP32 fields, FP64 B levels)
+# per interior node (FP32 fields, double-float B levels of 8 B per component)
 NODE_BYTES_F32 = {
     "f32_curlB": 12 + 4 + 12,
-    "f32_ct_pred": 36 + 12,
-    "f32_ct_corr": 36 + 12,
-    "f32_E": 28 + 12,
-    "f32_bupd": 12 + 48 + 36,
-    "f32_half": 24 + 12,
+    "f32_aj_ct_pred": 12 + 4 + 12 + 12 + 12,        # read dB, np, up; write aj, ct
+    "f32_aj_ct_corr": 12 + 4 + 12 + 12 + 12,
+    "f32_bstep_pred": 12 + 12 + 4 + 24 + 12 + 24 + 12 + 12,  # read ct, aj, nu, B, dB1; write B, dB, dB(m+1/2)
+    "f32_bstep_corr": 12 + 12 + 4 + 24 + 24 + 12,    # read ct, aj, nu, B; write B, dB
     "f32_kit": 36 + 32,
     "f32_node_sum": 16 * 2 + 16,
     "f32_ct_up": 16 + 12,
@@ -363,7 +362,7 @@ def run_ours(args):
         "config": {"workload": cfg.name, "cells": list(cfg.cells), "ppc": cfg.ppc, "ions": N,
                    "subcycles": cfg.ntsub,
                    "boundary": "x inflow/outflow, periodic y,z" if cfg.sources.get("x_open") else "periodic",
-                   "precision_form": "FP32 form (int32 cell + FP32 offset, FP32 moments, FP64 B)" if f32
+                   "precision_form": "FP32 form (int32 cell + FP32 offset, FP32 moments, double-float B)" if f32
                    else "FP64 drop-in",
                    "l2": "inputs larger than L2 (particle state %.1f GB)" % (N * (41 if f32 else 72) / 1e9),
                    "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU"},

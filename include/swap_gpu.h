@@ -132,6 +132,13 @@ int swap_check_time_step(swap_ctx* ctx, const double* bt, const double* np, doub
                          double* ntf);                                                  /* gutsf.f:1776 */
 int swap_periodic(swap_ctx* ctx, double* b);                                            /* boundary.f:9 */
 int swap_periodic_scalar(swap_ctx* ctx, double* b);                                     /* boundary.f:167 */
+/* Diagnostics moments of the output block (maind.f:515-517), from the
+ * ijkp/wght of the last get_interp_weights, as the reference.  mion is the
+ * ion mass (swap_set_mion; 1 in normalized units). */
+int swap_update_rho(swap_ctx* ctx, double* mnp);                                        /* gutsp.f:1517 */
+int swap_get_temperature(swap_ctx* ctx, const double* xp, const double* vp, const double* np,
+                         double* temp_p);                                               /* gutsp.f:2257 */
+int swap_set_mion(swap_ctx* ctx, double mion);
 
 /* ---- fused, device-resident ion step on the bound arrays ---- */
 int swap_ion_step_pre(swap_ctx* ctx);     /* maind.f:385-413 */
@@ -184,7 +191,10 @@ int swap_remove_outflow_x(swap_ctx* ctx);
 
 /* ---- the FP32 form of the fused step ----
  * Particle positions as int32 cell + FP32 offset, FP32 velocities and
- * moments, B accumulated in FP64 across subcycles.  Needs a uniform grid with
+ * moments, B accumulated across subcycles in double-float (pairs of floats,
+ * 48 significant bits: GB300's FP64 rate is a small fraction of its FP32
+ * rate).  The sources and sinks of swap_set_sources apply, with new ions
+ * drawn as in the FP64 path and charge exchange drawn per sorted ion.  Needs a uniform grid with
  * 8..1024 physical cells per axis in multiples of 4, a uniform b0, at most 16
  * (mrat, beta_p) species, and |v|*dt < dx per axis (SWAP_EMOVE otherwise).
  * begin converts the bound FP64 state; end writes it back into the bound

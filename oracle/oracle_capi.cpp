@@ -289,6 +289,15 @@ void copy_out(const std::vector<R>& v1based, int n, R* out) {
       c->step++;                                                                                           \
     });                                                                                                    \
   }                                                                                                        \
+  extern "C" int P##update_rho(void* h, T* mnp, double mion) {                                            \
+    CTX(T);                                                                                                \
+    return guard(c, [&] { swo::update_rho(c->s, mnp, c->mrat, c->beta_p, c->N(), (T)mion); });             \
+  }                                                                                                        \
+  extern "C" int P##get_temperature(void* h, const T* xp, const T* vp, const T* np, T* temp_p, double mion) { \
+    CTX(T);                                                                                                \
+    (void)xp;                                                                                              \
+    return guard(c, [&] { swo::get_temperature(c->s, vp, np, temp_p, c->mrat, c->beta_p, c->N(), (T)mion); }); \
+  }                                                                                                        \
   extern "C" int P##set_sources(void* h, const swo::Sources* q, std::int64_t step0) {                       \
     CTX(T);                                                                                                \
     c->src = *q;                                                                                           \

@@ -196,6 +196,12 @@ class Oracle:
             raise RuntimeError("oracle sort_perm failed")
         return perm, counts
 
+    def update_rho(self, mnp, mion=1.0):
+        self._call("update_rho", mnp, extra=(C.c_double(mion),))
+
+    def get_temperature(self, xp, vp, np_, temp_p, mion=1.0):
+        self._call("get_temperature", xp, vp, np_, temp_p, extra=(C.c_double(mion),))
+
     # sources and sinks ----------------------------------------------
     def set_sources(self, src, step0=0):
         """src: a swap_gb300.abi.Sources (the same struct layout)."""

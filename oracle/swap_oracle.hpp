@@ -739,6 +739,81 @@ void update_up(State<R>& s, const R* vp, const R* np, R* up, const R* beta_p, st
   periodic(g, up);
 }
 
+// update_rho (gutsp.f:1517-1590): mass density mnp(node) += (w/mrat)/volb,
+// times mion, fold, periodic_scalar.
+template <class R>
+void update_rho(State<R>& s, R* mnp, const R* mrat, const R* beta_p, std::int64_t ni_tot, R mion) {
+  const Mesh<R>& g = s.g;
+  const std::int64_t NM = s.ni_max;
+  std::fill(mnp, mnp + g.C, R(0.0));
+  deposit_loop(s, ni_tot, g.C, mnp, [&](std::int64_t l, R* acc) {
+    const int i = s.ijkp[l], j = s.ijkp[l + NM], k = s.ijkp[l + 2 * NM];
+    const R volb = (g.qx[i + 1] - g.qx[i]) * (g.qy[j + 1] - g.qy[j]) * (g.qz[k + 1] - g.qz[k]) * s.beta *
+                   beta_p[l];  // gutsp.f:1557-1558
+    std::size_t nd[8];
+    corner_nodes(g, i, j, k, nd);
+    for (int c = 0; c < 8; ++c) acc[nd[c]] = acc[nd[c]] + (s.wght[l + c * NM] / mrat[l]) / volb;
+  });
+  for (std::size_t o = 0; o < g.C; ++o) mnp[o] = mion * mnp[o];  // gutsp.f:1571
+  fold_scalar(g, mnp);                                            // gutsp.f:1574-1576
+  periodic_scalar(g, mnp);
+}
+
+// get_temperature (gutsp.f:2257-2541): with mvp = v/sqrt(mrat), deposit
+// <mvp^2> and <mvp> per node (skipping nodes with np = 0), fold, periodic,
+// face-average each, then temp_p = (1/3)*1e6*mion*|<mvp^2> - <mvp>^2|.
+template <class R>
+void get_temperature(State<R>& s, const R* vp, const R* np, R* temp_p, const R* mrat, const R* beta_p,
+                     std::int64_t ni_tot, R mion) {
+  const Mesh<R>& g = s.g;
+  const std::int64_t NM = s.ni_max;
+  const std::size_t C = g.C;
+  std::vector<R> up2(3 * C, R(0)), upa(3 * C, R(0));
+  for (int pass = 0; pass < 2; ++pass) {
+    std::vector<R>& out = pass == 0 ? up2 : upa;
+    R* ct = s.ct.data();
+    std::fill(ct, ct + 3 * C, R(0.0));
+    deposit_loop(s, ni_tot, 3 * C, ct, [&](std::int64_t l, R* acc) {
+      const int i = s.ijkp[l], j = s.ijkp[l + NM], k = s.ijkp[l + 2 * NM];
+      const R volb = (g.qx[i + 1] - g.qx[i]) * (g.qy[j + 1] - g.qy[j]) * (g.qz[k + 1] - g.qz[k]) * s.beta *
+                     beta_p[l];  // gutsp.f:2310-2311
+      const R sq = std::sqrt(mrat[l]);
+      R mv[3];
+      for (int m = 0; m < 3; ++m) {
+        mv[m] = vp[l + m * NM] / sq;  // gutsp.f:2291
+        if (pass == 0) mv[m] = mv[m] * mv[m];
+      }
+      std::size_t nd[8];
+      corner_nodes(g, i, j, k, nd);
+      for (int c = 0; c < 8; ++c) {
+        if (!(np[nd[c]] > R(0.0))) continue;  // gutsp.f:2313, 2425 etc.
+        const R nvolb = np[nd[c]] * volb;
+        const R w = s.wght[l + c * NM];
+        for (int m = 0; m < 3; ++m) acc[nd[c] + C * m] = acc[nd[c] + C * m] + mv[m] * w / nvolb;
+      }
+    });
+    for (int m = 0; m < 3; ++m) fold_scalar(g, ct + C * m);  // gutsp.f:2373-2375, 2485-2487
+    periodic(g, ct);
+    for (int i = 1; i <= g.nx - 1; ++i)  // gutsp.f:2395-2403, 2507-2515
+      for (int j = 1; j <= g.ny - 1; ++j)
+        for (int k = 1; k <= g.nz - 1; ++k) {
+          const std::size_t o = g.n(i, j, k);
+          out[o] = R(0.5) * (ct[o] + ct[g.n(i + 1, j, k)]);
+          out[o + C] = R(0.5) * (ct[o + C] + ct[g.n(i, j + 1, k) + C]);
+          out[o + 2 * C] = R(0.5) * (ct[o + 2 * C] + ct[g.n(i, j, k + 1) + 2 * C]);
+        }
+    periodic(g, out.data());
+  }
+  for (std::size_t o = 0; o < C; ++o) {  // gutsp.f:2521-2529
+    R a[3];
+    for (int m = 0; m < 3; ++m) {
+      const R d = up2[o + C * m] - upa[o + C * m] * upa[o + C * m];
+      a[m] = d * d;
+    }
+    temp_p[o] = (R(1.0) / R(3.0)) * R(1e6) * mion * std::sqrt(a[0] + a[1] + a[2]);
+  }
+}
+
 // extrapol_up (gutsp.f:127-150): deposit v at time level n = 1.5 vp - 0.5 vp1.
 template <class R>
 void extrapol_up(State<R>& s, R* up, const R* vp, const R* vp1, const R* np, const R* beta_p,

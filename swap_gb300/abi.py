@@ -125,6 +125,9 @@ SIGNATURES: dict[str, tuple] = {
     "swap_check_time_step": (C.c_int, [P] + [c_double_p] * 4),
     "swap_periodic": (C.c_int, [P, c_double_p]),
     "swap_periodic_scalar": (C.c_int, [P, c_double_p]),
+    "swap_update_rho": (C.c_int, [P, c_double_p]),
+    "swap_get_temperature": (C.c_int, [P] + [c_double_p] * 4),
+    "swap_set_mion": (C.c_int, [P, C.c_double]),
     "swap_ion_step_pre": (C.c_int, [P]),
     "swap_field_subcycles": (C.c_int, [P]),
     "swap_ion_step_post": (C.c_int, [P]),

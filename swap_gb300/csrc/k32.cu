@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(TPB_PASS) k_pass(G32 g, Part p, Species sp, St
                                               float* __restrict__ partial, int* err) {
   __shared__ float4 s_kit[PASS == 1 ? 2 : 2 * TNODES];
   __shared__ float s_dep[4 * TNODES];
-  __shared__ __align__(16) float s_red[TPB_PASS / 32][32][36];  // per-warp transpose of deposit values
+  __shared__ __align__(16) float s_red[TPB_PASS / 32][32][36];  // per warp: [value][particle], padded
   const long long b = blockIdx.x;
   const int bi = (int)(b % g.nbx), bj = (int)((b / g.nbx) % g.nby), bk = (int)(b / ((long long)g.nbx * g.nby));
   const int c0x = 4 * bi, c0y = 4 * bj, c0z = 4 * bk;
@@ -263,34 +263,43 @@ __global__ void __launch_bounds__(TPB_PASS) k_pass(G32 g, Part p, Species sp, St
         qdv[3] = qw * dvz;
       }
     }
-    // deposit (gutsp.f:1484-1491, 1704-1756): transpose the 32 values
-    // (4 moments x 8 corners) of the warp's particles through shared memory;
-    // lane v then runs a segmented sum of value v down the runs of lanes that
-    // share a cell (sorted particles: usually one or two runs) and adds each
-    // run's sum to the brick tile with one shared atomic.
-    float4* row4 = reinterpret_cast<float4*>(s_red[warp][lane]);
+    // deposit (gutsp.f:1484-1491, 1704-1756): the warp's 32 particles x 32
+    // values (4 moments x 8 corners) go to shared memory as value-major
+    // rows; lane v then sums value v down the runs of particles that share
+    // a cell (sorted particles: usually one or two runs), with the run ends
+    // known to the whole warp, and adds each run's sum to the brick tile
+    // with one shared atomic.
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const float a = live ? qdv[q] : 0.0f;
-      row4[2 * q] = make_float4(w8[0] * a, w8[1] * a, w8[2] * a, w8[3] * a);
-      row4[2 * q + 1] = make_float4(w8[4] * a, w8[5] * a, w8[6] * a, w8[7] * a);
+#pragma unroll
+      for (int c8 = 0; c8 < 8; ++c8) s_red[warp][8 * q + c8][lane] = w8[c8] * a;
     }
     __syncwarp();
     const int tprev = __shfl_up_sync(0xffffffffu, t0, 1);
     const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || t0 != tprev);
-    const unsigned livem = __ballot_sync(0xffffffffu, live);
-    const int nrows = 32 - __clz(livem);
+    const unsigned ends = (heads >> 1) | 0x80000000u;  // the row before each head, and row 31
     const int qv = lane >> 3, cv = lane & 7;
     const int off = (cv & 1) + TN * (((cv >> 1) & 1) + TN * (cv >> 2));
     const bool add_here = PASS != 2 || qv != 0;
+    const float4* row = reinterpret_cast<const float4*>(s_red[warp][lane]);
     float acc = 0.0f;
-    for (int r = 0; r < nrows; ++r) {
-      acc += s_red[warp][r][lane];
-      // end of a run: the next row starts one, or this is the last live row
-      if (r == nrows - 1 || ((heads >> (r + 1)) & 1u)) {
-        const int tr = __shfl_sync(0xffffffffu, t0, r);
-        if (add_here && tr >= 0) atomicAdd(&s_dep[qv * TNODES + tr + off], acc);
-        acc = 0.0f;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {  // two halves of 16 rows, to bound the registers
+      float x[16];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float4 v = row[4 * h + q];
+        x[4 * q] = v.x; x[4 * q + 1] = v.y; x[4 * q + 2] = v.z; x[4 * q + 3] = v.w;
+      }
+#pragma unroll
+      for (int r = 0; r < 16; ++r) {
+        acc += x[r];
+        if ((ends >> (16 * h + r)) & 1u) {
+          const int tr = __shfl_sync(0xffffffffu, t0, 16 * h + r);
+          if (add_here && tr >= 0) atomicAdd(&s_dep[qv * TNODES + tr + off], acc);
+          acc = 0.0f;
+        }
       }
     }
     __syncwarp();
@@ -433,104 +442,182 @@ __global__ void k_curlB(G32 g, const float* __restrict__ b, const float* __restr
   }
 }
 
-__global__ void k_half_sum(long long n, const float* __restrict__ a, const float* __restrict__ b,
-                           float* __restrict__ out) {
-  GSTRIDE(t, n) out[t] = 0.5f * (a[t] + b[t]);
-}
+// ---- the field subcycle: two fused kernels per half step ----
+//
+// Launched over the interior nodes as a 3D grid (no index division).  Every
+// field keeps its periodic ghost images (written by store_img), so a value at
+// a ghost coordinate is computed at the interior image.
 
-// face_to_center of a = aj - up (gutsf.f:1059, grid_interp.f:163-170)
-__device__ __forceinline__ void aa_at(const G32& g, const float* aj, const float* up, long long o, float& x, float& y,
-                                      float& z) {
-  const long long C = g.C, sy = g.nx, sz = (long long)g.nx * g.ny;
-  x = 0.5f * ((aj[o] - up[o]) + (aj[o - 1] - up[o - 1]));
-  y = 0.5f * ((aj[o + C] - up[o + C]) + (aj[o - sy + C] - up[o - sy + C]));
-  z = 0.5f * ((aj[o + 2 * C] - up[o + 2 * C]) + (aj[o - sz + 2 * C] - up[o - sz + 2 * C]));
-}
+constexpr int FBX = 32, FBY = 4;
 
-// Predictor cross product of get_E/crossf2 (gutsf.f:1073-1075, 65-76).
-__global__ void k_ct_pred(G32 g, const float* __restrict__ aj, const float* __restrict__ up,
-                          const float* __restrict__ dbt, const float* __restrict__ b0c, float* __restrict__ ct) {
-  GSTRIDE(t, n_int(g)) {
-    int i, j, k;
-    interior_of(g, t, i, j, k);
-    const long long C = g.C, o = nid(g, i, j, k);
-    float ax, ay, az, bx, by, bz;
-    aa_at(g, aj, up, o, ax, ay, az);
-    e2c(g, dbt, i, j, k, bx, by, bz);
-    bx += b0c[0]; by += b0c[1]; bz += b0c[2];
-    store_img(g, ct, i, j, k, ay * bz - az * by);
-    store_img(g, ct + C, i, j, k, az * bx - ax * bz);
-    store_img(g, ct + 2 * C, i, j, k, ax * by - ay * bx);
+#define FIELD_NODE(i, j, k)                                   \
+  const int i = blockIdx.x * FBX + threadIdx.x + 2;          \
+  const int j = blockIdx.y * FBY + threadIdx.y + 2;          \
+  const int k = blockIdx.z + 2;                              \
+  if (i > g.ncx + 1 || j > g.ncy + 1) return
+
+// Component m of aj = curl(dB)/(alpha * face-averaged np) at node (i,j,k)
+// (curlB, gutsf.f:202-239; curl b0 = 0 for the uniform b0).
+template <int m>
+__device__ __forceinline__ float aj_comp(const G32& g, const float* __restrict__ b, const float* __restrict__ np,
+                                         float alpha, int i, int j, int k) {
+  i = img(i, g.nx);
+  j = img(j, g.ny);
+  k = img(k, g.nz);
+  const long long C = g.C, o = nid(g, i, j, k), sx = 1, sy = g.nx, sz = (long long)g.nx * g.ny;
+  const float* B1 = b;
+  const float* B2 = b + C;
+  const float* B3 = b + 2 * C;
+  float c;
+  long long s;
+  if (m == 0) {
+    c = (B3[o] - B3[o - sy]) * g.inv_dy + (B2[o - sz] - B2[o]) * g.inv_dz;
+    s = sx;
+  } else if (m == 1) {
+    c = (B1[o] - B1[o - sz]) * g.inv_dz + (B3[o - sx] - B3[o]) * g.inv_dx;
+    s = sy;
+  } else {
+    c = (B2[o] - B2[o - sx]) * g.inv_dx + (B1[o - sy] - B1[o]) * g.inv_dy;
+    s = sz;
   }
+  return c / (0.5f * (np[o] + np[o + s]) * alpha);
 }
 
-// Corrector: B at m+1/2 via edge_to_face then face_to_center (gutsf.f:1268-
-// 1269): component m is the 1-2-1 average along axis m of edge_to_center.
-__global__ void k_ct_corr(G32 g, const float* __restrict__ aj, const float* __restrict__ up,
-                          const float* __restrict__ dbtp1, const float* __restrict__ b0c, float* __restrict__ ct) {
-  GSTRIDE(t, n_int(g)) {
-    int i, j, k;
-    interior_of(g, t, i, j, k);
-    const long long C = g.C, o = nid(g, i, j, k);
-    float ax, ay, az;
-    aa_at(g, aj, up, o, ax, ay, az);
+// curlB, face_to_center(aj - up) and the cross product of get_E (gutsf.f:
+// 1059-1075, crossf2 gutsf.f:65-76): writes aj and ct.  Predictor: B at
+// cell centres from edge_to_center of dB (grid_interp.f:35-51).  Corrector:
+// B at m+1/2 through edge_to_face then face_to_center (gutsf.f:1268-1269),
+// i.e. component m is the 1-2-1 average along axis m of edge_to_center.
+template <bool CORR>
+__global__ void __launch_bounds__(FBX * FBY) k_aj_ct(G32 g, const float* __restrict__ db,
+                                                     const float* __restrict__ np, const float* __restrict__ up,
+                                                     const float* __restrict__ b0c, float alpha,
+                                                     float* __restrict__ aj, float* __restrict__ ct) {
+  FIELD_NODE(i, j, k);
+  const long long C = g.C, o = nid(g, i, j, k), sx = 1, sy = g.nx, sz = (long long)g.nx * g.ny;
+  const float a1 = aj_comp<0>(g, db, np, alpha, i, j, k);
+  const float a2 = aj_comp<1>(g, db, np, alpha, i, j, k);
+  const float a3 = aj_comp<2>(g, db, np, alpha, i, j, k);
+  const float a1m = aj_comp<0>(g, db, np, alpha, i - 1, j, k);
+  const float a2m = aj_comp<1>(g, db, np, alpha, i, j - 1, k);
+  const float a3m = aj_comp<2>(g, db, np, alpha, i, j, k - 1);
+  store_img(g, aj, i, j, k, a1);
+  store_img(g, aj + C, i, j, k, a2);
+  store_img(g, aj + 2 * C, i, j, k, a3);
+  const float ax = 0.5f * ((a1 - up[o]) + (a1m - up[o - sx]));
+  const float ay = 0.5f * ((a2 - up[o + C]) + (a2m - up[o - sy + C]));
+  const float az = 0.5f * ((a3 - up[o + 2 * C]) + (a3m - up[o - sz + 2 * C]));
+  float bx, by, bz;
+  if (!CORR) {
+    e2c(g, db, i, j, k, bx, by, bz);
+  } else {
     float c1, c2, c3, m1, m2, m3, p1, p2, p3, d1, d2;
-    e2c(g, dbtp1, i, j, k, c1, c2, c3);
-    e2c(g, dbtp1, img(i - 1, g.nx), j, k, m1, d1, d2);
-    e2c(g, dbtp1, img(i + 1, g.nx), j, k, p1, d1, d2);
-    const float bx = 0.25f * (m1 + 2.0f * c1 + p1) + b0c[0];
-    e2c(g, dbtp1, i, img(j - 1, g.ny), k, d1, m2, d2);
-    e2c(g, dbtp1, i, img(j + 1, g.ny), k, d1, p2, d2);
-    const float by = 0.25f * (m2 + 2.0f * c2 + p2) + b0c[1];
-    e2c(g, dbtp1, i, j, img(k - 1, g.nz), d1, d2, m3);
-    e2c(g, dbtp1, i, j, img(k + 1, g.nz), d1, d2, p3);
-    const float bz = 0.25f * (m3 + 2.0f * c3 + p3) + b0c[2];
-    store_img(g, ct, i, j, k, ay * bz - az * by);
-    store_img(g, ct + C, i, j, k, az * bx - ax * bz);
-    store_img(g, ct + 2 * C, i, j, k, ax * by - ay * bx);
+    e2c(g, db, i, j, k, c1, c2, c3);
+    e2c(g, db, img(i - 1, g.nx), j, k, m1, d1, d2);
+    e2c(g, db, img(i + 1, g.nx), j, k, p1, d1, d2);
+    e2c(g, db, i, img(j - 1, g.ny), k, d1, m2, d2);
+    e2c(g, db, i, img(j + 1, g.ny), k, d1, p2, d2);
+    e2c(g, db, i, j, img(k - 1, g.nz), d1, d2, m3);
+    e2c(g, db, i, j, img(k + 1, g.nz), d1, d2, p3);
+    bx = 0.25f * (m1 + 2.0f * c1 + p1);
+    by = 0.25f * (m2 + 2.0f * c2 + p2);
+    bz = 0.25f * (m3 + 2.0f * c3 + p3);
+  }
+  bx += b0c[0];
+  by += b0c[1];
+  bz += b0c[2];
+  store_img(g, ct, i, j, k, ay * bz - az * by);
+  store_img(g, ct + C, i, j, k, az * bx - ax * bz);
+  store_img(g, ct + 2 * C, i, j, k, ax * by - ay * bx);
+}
+
+// Component m of E = face average of ct + nu*aj at node (i,j,k) (gutsf.f:
+// 94-96, 1082).
+template <int m>
+__device__ __forceinline__ float e_comp(const G32& g, const float* __restrict__ ct, const float* __restrict__ nu,
+                                        const float* __restrict__ aj, int i, int j, int k) {
+  i = img(i, g.nx);
+  j = img(j, g.ny);
+  k = img(k, g.nz);
+  const long long C = g.C, o = nid(g, i, j, k);
+  const long long s = m == 0 ? 1 : (m == 1 ? (long long)g.nx : (long long)g.nx * g.ny);
+  return 0.5f * (ct[o + C * m] + ct[o + s + C * m]) + nu[o] * aj[o + C * m];
+}
+
+// Double-float arithmetic (a pair of floats carrying 48 significant bits):
+// the FP32 form accumulates B across subcycles in it, because GB300's FP64
+// pipe runs at a small fraction of its FP32 rate.  Dekker/Knuth error-free
+// transformations with explicitly rounded operations (never contracted).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// (bh + bl) - (ch + cl) * x
+__device__ __forceinline__ void df_sub_mul(float bh, float bl, float ch, float cl, float x, float& rh, float& rl) {
+  const float p = __fmul_rn(ch, x);
+  const float q = __fmaf_rn(cl, x, __fmaf_rn(ch, x, -p));  // low part of the product
+  float s, e;
+  two_sum(bh, -p, s, e);
+  e = __fadd_rn(e, __fsub_rn(bl, q));
+  rh = __fadd_rn(s, e);
+  rl = __fsub_rn(e, __fsub_rn(rh, s));
+}
+
+// E on the fly, curlE (gutsf.f:288-299) and B_new = base - coef*curlE
+// (predict_B gutsf.f:1158-1159 with coef = 2 dtsub on b12; correct_B
+// gutsf.f:1349-1350 with coef = dtsub on b1) in double-float; dB of the
+// result in FP32.  Predictor: also dB at m+1/2 = (dB_new + dB1)/2
+// (gutsf.f:1210-1219).  WRITE_E: store E (the step's last corrector).
+template <bool PRED, bool WRITE_E>
+__global__ void __launch_bounds__(FBX * FBY) k_bstep(G32 g, const float* __restrict__ ct,
+                                                     const float* __restrict__ nu, const float* __restrict__ aj,
+                                                     const float* __restrict__ bh, const float* __restrict__ bl,
+                                                     float ch, float cl, const float* __restrict__ b0c,
+                                                     float* __restrict__ oh, float* __restrict__ ol,
+                                                     float* __restrict__ dbo, const float* __restrict__ db1,
+                                                     float* __restrict__ dbtp1, float* __restrict__ E) {
+  FIELD_NODE(i, j, k);
+  const long long C = g.C, o = nid(g, i, j, k);
+  const float e1 = e_comp<0>(g, ct, nu, aj, i, j, k);
+  const float e2 = e_comp<1>(g, ct, nu, aj, i, j, k);
+  const float e3 = e_comp<2>(g, ct, nu, aj, i, j, k);
+  const float e1y = e_comp<0>(g, ct, nu, aj, i, j + 1, k), e1z = e_comp<0>(g, ct, nu, aj, i, j, k + 1);
+  const float e2x = e_comp<1>(g, ct, nu, aj, i + 1, j, k), e2z = e_comp<1>(g, ct, nu, aj, i, j, k + 1);
+  const float e3x = e_comp<2>(g, ct, nu, aj, i + 1, j, k), e3y = e_comp<2>(g, ct, nu, aj, i, j + 1, k);
+  const float ce[3] = {(e3y - e3) * g.inv_dy + (e2 - e2z) * g.inv_dz,
+                       (e3 - e3x) * g.inv_dx + (e1z - e1) * g.inv_dz,
+                       (e1 - e1y) * g.inv_dy + (e2x - e2) * g.inv_dx};
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    float rh, rl;
+    df_sub_mul(bh[o + C * m], bl[o + C * m], ch, cl, ce[m], rh, rl);
+    const float d = __fadd_rn(__fsub_rn(rh, b0c[m]), rl);
+    store_img(g, oh + C * m, i, j, k, rh);
+    store_img(g, ol + C * m, i, j, k, rl);
+    store_img(g, dbo + C * m, i, j, k, d);
+    if (PRED) store_img(g, dbtp1 + C * m, i, j, k, 0.5f * (d + db1[o + C * m]));
+  }
+  if (WRITE_E) {
+    store_img(g, E, i, j, k, e1);
+    store_img(g, E + C, i, j, k, e2);
+    store_img(g, E + 2 * C, i, j, k, e3);
   }
 }
 
-// E = face average of ct + nu*aj (gutsf.f:94-96, 1082).
-__global__ void k_E(G32 g, const float* __restrict__ ct, const float* __restrict__ nu, const float* __restrict__ aj,
-                    float* __restrict__ E) {
-  GSTRIDE(t, n_int(g)) {
-    int i, j, k;
-    interior_of(g, t, i, j, k);
-    const long long C = g.C, o = nid(g, i, j, k), sy = g.nx, sz = (long long)g.nx * g.ny;
-    const float n = nu[o];
-    store_img(g, E, i, j, k, 0.5f * (ct[o] + ct[o + 1]) + n * aj[o]);
-    store_img(g, E + C, i, j, k, 0.5f * (ct[o + C] + ct[o + sy + C]) + n * aj[o + C]);
-    store_img(g, E + 2 * C, i, j, k, 0.5f * (ct[o + 2 * C] + ct[o + sz + 2 * C]) + n * aj[o + 2 * C]);
+// FP64 <-> double-float.
+__global__ void k_split_df(long long n, const double* __restrict__ a, float* __restrict__ h, float* __restrict__ l) {
+  GSTRIDE(t, n) {
+    const double v = a[t];
+    const float vh = (float)v;
+    h[t] = vh;
+    l[t] = (float)(v - (double)vh);
   }
 }
-
-// curlE (gutsf.f:288-299) and b1p2 = base - coef*curlE in FP64
-// (gutsf.f:1158-1159, 1349-1350); dB of the result mirrored in FP32.  b0 is
-// uniform in the FP32 form (b0c).  When dbtp1 is given (predictor) the
-// corrector's dB at m+1/2 = (dB(b1p2) + dB(b1))/2 (gutsf.f:1210-1219) is
-// written too.
-__global__ void k_bupd(G32 g, const float* __restrict__ E, const double* __restrict__ base,
-                       const float* __restrict__ b0c, double coef, double* __restrict__ b1p2,
-                       float* __restrict__ db1p2, const float* __restrict__ db1, float* __restrict__ dbtp1) {
-  GSTRIDE(t, n_int(g)) {
-    int i, j, k;
-    interior_of(g, t, i, j, k);
-    const long long C = g.C, o = nid(g, i, j, k), sx = 1, sy = g.nx, sz = (long long)g.nx * g.ny;
-    const float* E1 = E;
-    const float* E2 = E + C;
-    const float* E3 = E + 2 * C;
-    const float ce[3] = {(E3[o + sy] - E3[o]) * g.inv_dy + (E2[o] - E2[o + sz]) * g.inv_dz,
-                         (E3[o] - E3[o + sx]) * g.inv_dx + (E1[o + sz] - E1[o]) * g.inv_dz,
-                         (E1[o] - E1[o + sy]) * g.inv_dy + (E2[o + sx] - E2[o]) * g.inv_dx};
-    for (int m = 0; m < 3; ++m) {
-      const double v = base[o + C * m] - coef * (double)ce[m];
-      const float d = (float)(v - (double)b0c[m]);
-      store_img(g, b1p2 + C * m, i, j, k, v);
-      store_img(g, db1p2 + C * m, i, j, k, d);
-      if (dbtp1) store_img(g, dbtp1 + C * m, i, j, k, 0.5f * (d + db1[o + C * m]));
-    }
-  }
+__global__ void k_join_df(long long n, const float* __restrict__ h, const float* __restrict__ l,
+                          double* __restrict__ a) {
+  GSTRIDE(t, n) a[t] = (double)h[t] + (double)l[t];
 }
 
 // Whistler Courant time at every node, ghosts included, as check_time_step
@@ -618,25 +705,51 @@ __device__ __forceinline__ long long src_key(const G32& g, int i, int j, int k, 
 // Per new key X: the count of arriving particles and, for every direction d,
 // how many of them come from sources earlier in key order than the source of
 // d (the stable order), so the scatter needs one lookup per particle.
-__global__ void k_sort_count(G32 g, const uint16_t* __restrict__ dep, const int32_t* __restrict__ ncount,
-                             int64_t* __restrict__ count, uint16_t* __restrict__ pre, int* err) {
+// For a cell whose 27 source cells need no periodic wrap, the key order of
+// the sources depends only on the cell's place in its brick (when there are
+// at least 3 bricks along x and y): `order` lists, per place, the directions
+// by increasing source key.  Other cells compare the 27 keys directly.
+__global__ void __launch_bounds__(TPB) k_sort_count(G32 g, const uint16_t* __restrict__ dep,
+                                                    const int32_t* __restrict__ ncount,
+                                                    const uint8_t* __restrict__ order, int64_t* __restrict__ count,
+                                                    uint16_t* __restrict__ pre, int* err) {
+  __shared__ uint8_t s_ord[BCELLS * NDIR];
+  __shared__ unsigned s_cnt[NDIR][TPB];  // per thread, indexed by direction
+  for (int t = threadIdx.x; t < BCELLS * NDIR; t += blockDim.x) s_ord[t] = order[t];
+  __syncthreads();
+  const bool bricks_ok = g.nbx >= 3 && g.nby >= 3;
   GSTRIDE(X, g.nkeys) {
     int i, j, k;
     cell_of_key(g, X, i, j, k);
-    long long sk[NDIR];
-    unsigned cnt[NDIR];
     int64_t n = 0;
+#pragma unroll
     for (int d = 0; d < NDIR; ++d) {
-      sk[d] = src_key(g, i, j, k, d);
-      cnt[d] = dep[sk[d] * NDIR + d];
-      n += cnt[d];
+      const unsigned c = dep[src_key(g, i, j, k, d) * NDIR + d];
+      s_cnt[d][threadIdx.x] = c;
+      n += c;
     }
     if (n > 65535) set_err(err, KERR_MOVE);
     if (ncount) n += ncount[X];
-    for (int d = 0; d < NDIR; ++d) {
-      unsigned p = 0;
-      for (int q = 0; q < NDIR; ++q) p += sk[q] < sk[d] ? cnt[q] : 0u;
-      pre[X * NDIR + d] = (uint16_t)p;
+    const bool fast = bricks_ok && i > 0 && i < g.ncx - 1 && j > 0 && j < g.ncy - 1 && k > 0 && k < g.ncz - 1;
+    if (fast) {
+      const uint8_t* ord = s_ord + (X % BCELLS) * NDIR;
+      unsigned run = 0;
+      for (int r = 0; r < NDIR; ++r) {
+        const int d = ord[r];
+        pre[X * NDIR + d] = (uint16_t)run;
+        run += s_cnt[d][threadIdx.x];
+      }
+    } else {
+      int sk[NDIR];  // keys fit in 31 bits (at most 1024^3 cells)
+#pragma unroll
+      for (int d = 0; d < NDIR; ++d) sk[d] = (int)src_key(g, i, j, k, d);
+#pragma unroll
+      for (int d = 0; d < NDIR; ++d) {
+        unsigned p = 0;
+#pragma unroll
+        for (int q = 0; q < NDIR; ++q) p += sk[q] < sk[d] ? s_cnt[q][threadIdx.x] : 0u;
+        pre[X * NDIR + d] = (uint16_t)p;
+      }
     }
     count[X] = n;
   }
@@ -889,15 +1002,17 @@ __global__ void k_energy_p(long long N, Part p, Species sp, double vol, double* 
   if (threadIdx.x == 0) atomicAdd(acc, s);
 }
 
-__global__ void k_energy_f(G32 g, const double* __restrict__ b0, const double* __restrict__ b1,
-                           const float* __restrict__ E, double alpha, double vol, double* acc) {
+__global__ void k_energy_f(G32 g, const double* __restrict__ b0, const float* __restrict__ b1h,
+                           const float* __restrict__ b1l, const float* __restrict__ E, double alpha, double vol,
+                           double* acc) {
   double s1 = 0, s2 = 0, s3 = 0;
   GSTRIDE(t, n_int(g)) {
     int i, j, k;
     interior_of(g, t, i, j, k);
     const long long o = nid(g, i, j, k);
     for (int m = 0; m < 3; ++m) {
-      const double bb = b1[o + g.C * m], d = bb - b0[o + g.C * m], e = E[o + g.C * m];
+      const double bb = (double)b1h[o + g.C * m] + (double)b1l[o + g.C * m];
+      const double d = bb - b0[o + g.C * m], e = E[o + g.C * m];
       s1 += 0.5 * d * d * vol / alpha;
       s2 += 0.5 * bb * bb * vol / alpha;
       s3 += 0.5 * e * e * vol;
@@ -947,27 +1062,30 @@ cudaError_t build_kit(const G32& g, const float* aj, const float* up, const floa
 cudaError_t curlB32(const G32& g, const float* dbt, const float* np, float alpha, float* aj, cudaStream_t st) {
   RET((k_curlB<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, dbt, np, alpha, aj)));
 }
-cudaError_t half_sum32(const G32& g, const float* a, const float* b, float* out, cudaStream_t st) {
-  RET((k_half_sum<<<nblk(3 * g.C), TPB, 0, st>>>(3 * g.C, a, b, out)));
+cudaError_t aj_ct(const G32& g, bool corr, const float* db, const float* np, const float* up, const float* b0c,
+                  float alpha, float* aj, float* ct, cudaStream_t st) {
+  const dim3 grid((g.ncx + FBX - 1) / FBX, (g.ncy + FBY - 1) / FBY, g.ncz), blk(FBX, FBY);
+  if (corr) RET((k_aj_ct<true><<<grid, blk, 0, st>>>(g, db, np, up, b0c, alpha, aj, ct)));
+  RET((k_aj_ct<false><<<grid, blk, 0, st>>>(g, db, np, up, b0c, alpha, aj, ct)));
 }
-cudaError_t ct_pred(const G32& g, const float* aj, const float* up, const float* dbt, const float* b0c, float* ct,
-                    cudaStream_t st) {
-  RET((k_ct_pred<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, aj, up, dbt, b0c, ct)));
+cudaError_t b_step(const G32& g, bool pred, bool write_e, const float* ct, const float* nu, const float* aj,
+                   const float* bh, const float* bl, double coef, const float* b0c, float* oh, float* ol, float* dbo,
+                   const float* db1, float* dbtp1, float* E, cudaStream_t st) {
+  const dim3 grid((g.ncx + FBX - 1) / FBX, (g.ncy + FBY - 1) / FBY, g.ncz), blk(FBX, FBY);
+  const float ch = (float)coef, cl = (float)(coef - (double)ch);
+  if (pred && write_e)
+    RET((k_bstep<true, true><<<grid, blk, 0, st>>>(g, ct, nu, aj, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E)));
+  if (pred)
+    RET((k_bstep<true, false><<<grid, blk, 0, st>>>(g, ct, nu, aj, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E)));
+  if (write_e)
+    RET((k_bstep<false, true><<<grid, blk, 0, st>>>(g, ct, nu, aj, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E)));
+  RET((k_bstep<false, false><<<grid, blk, 0, st>>>(g, ct, nu, aj, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E)));
 }
-cudaError_t ct_corr(const G32& g, const float* aj, const float* up, const float* dbtp1, const float* b0c, float* ct,
-                    cudaStream_t st) {
-  RET((k_ct_corr<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, aj, up, dbtp1, b0c, ct)));
+cudaError_t split_df(long long n, const double* a, float* h, float* l, cudaStream_t st) {
+  RET((k_split_df<<<nblk(n), TPB, 0, st>>>(n, a, h, l)));
 }
-cudaError_t e_field(const G32& g, const float* ct, const float* nu, const float* aj, const float* np, float gp,
-                    float* E, cudaStream_t st) {
-  (void)np;
-  (void)gp;
-  RET((k_E<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, ct, nu, aj, E)));
-}
-cudaError_t b_update(const G32& g, const float* E, const double* base, const float* b0c, double coef, double* b1p2,
-                     float* db1p2, const float* db1, float* dbtp1, cudaStream_t st) {
-  RET((k_bupd<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, E, base, b0c, coef, b1p2, db1p2, db1,
-                                                                       dbtp1)));
+cudaError_t join_df(long long n, const float* h, const float* l, double* a, cudaStream_t st) {
+  RET((k_join_df<<<nblk(n), TPB, 0, st>>>(n, h, l, a)));
 }
 cudaError_t courant_min(const G32& g, const float* dbt, const float* b0c, const float* np, float alpha, float dx,
                         float* dtn, float* d_min, cudaStream_t st) {
@@ -983,9 +1101,31 @@ cudaError_t sort_prep(const G32& g, const int64_t* start, const int32_t* cell, u
   if (blocks > 65535LL * 16) blocks = 65535LL * 16;
   RET((k_sort_prep<<<(unsigned)blocks, TPB, 0, st>>>(g, start, cell, dirrank, dep, err)));
 }
-cudaError_t sort_count(const G32& g, const uint16_t* dep, const int32_t* ncount, int64_t* count, uint16_t* pre,
-                       int* err, cudaStream_t st) {
-  RET((k_sort_count<<<nblk(g.nkeys), TPB, 0, st>>>(g, dep, ncount, count, pre, err)));
+cudaError_t sort_count(const G32& g, const uint16_t* dep, const int32_t* ncount, const uint8_t* order,
+                       int64_t* count, uint16_t* pre, int* err, cudaStream_t st) {
+  RET((k_sort_count<<<nblk(g.nkeys), TPB, 0, st>>>(g, dep, ncount, order, count, pre, err)));
+}
+void sort_order_table(uint8_t* out) {
+  for (int l = 0; l < BCELLS; ++l) {
+    const int li = l & 3, lj = (l >> 2) & 3, lk = l >> 4;
+    int rank[NDIR], dirs[NDIR];
+    for (int d = 0; d < NDIR; ++d) {
+      const int dx = d % 3 - 1, dy = (d / 3) % 3 - 1, dz = d / 9 - 1;
+      const int si = li - dx, sj = lj - dy, sk = lk - dz;  // the source cell, relative to this brick
+      const int bx = si < 0 ? -1 : (si > 3 ? 1 : 0), by = sj < 0 ? -1 : (sj > 3 ? 1 : 0),
+                bz = sk < 0 ? -1 : (sk > 3 ? 1 : 0);
+      const int local = (si - 4 * bx) + 4 * (sj - 4 * by) + 16 * (sk - 4 * bz);
+      rank[d] = ((bz + 1) * 9 + (by + 1) * 3 + (bx + 1)) * BCELLS + local;
+      dirs[d] = d;
+    }
+    for (int a = 1; a < NDIR; ++a)  // insertion sort by source key
+      for (int b = a; b > 0 && rank[dirs[b]] < rank[dirs[b - 1]]; --b) {
+        const int t = dirs[b];
+        dirs[b] = dirs[b - 1];
+        dirs[b - 1] = t;
+      }
+    for (int r = 0; r < NDIR; ++r) out[l * NDIR + r] = (uint8_t)dirs[r];
+  }
 }
 cudaError_t new_scatter(const G32& g, long long n_host, const int64_t* n_dev, long long n_max, const Part& stage,
                         const int32_t* key, const int32_t* rank, const int32_t* ncount, const int64_t* start_new,
@@ -1048,14 +1188,15 @@ cudaError_t grid_f32_to_f64(long long n, const float* a, double* out, cudaStream
   RET((k_f32_to_f64<<<nblk(n), TPB, 0, st>>>(n, a, out)));
 }
 cudaError_t energy32(const G32& g, long long N, const Part& p, const Species& sp, double vol, const double* b0,
-                     const double* b1, const float* E, double alpha, double* acc4, cudaStream_t st) {
+                     const float* b1h, const float* b1l, const float* E, double alpha, double* acc4,
+                     cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(acc4, 0, 4 * sizeof(double), st);
   if (e != cudaSuccess) return e;
   if (N > 0) {
     k_energy_p<<<nblk(N), TPB, 0, st>>>(N, p, sp, vol, acc4);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
-  RET((k_energy_f<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, b0, b1, E, alpha, vol, acc4)));
+  RET((k_energy_f<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, b0, b1h, b1l, E, alpha, vol, acc4)));
 }
 
 }  // namespace swapk32

@@ -130,24 +130,30 @@ cudaError_t ct_and_up(const G32& g, const float* np, const float* S, float* up, 
 cudaError_t build_kit(const G32& g, const float* aj, const float* up, const float* dbt, const float* b0c,
                       float4* kit, cudaStream_t st);
 cudaError_t curlB32(const G32& g, const float* dbt, const float* np, float alpha, float* aj, cudaStream_t st);
-cudaError_t half_sum32(const G32& g, const float* a, const float* b, float* out, cudaStream_t st);
-cudaError_t ct_pred(const G32& g, const float* aj, const float* up, const float* dbt, const float* b0c,
-                    float* ct, cudaStream_t st);
-cudaError_t ct_corr(const G32& g, const float* aj, const float* up, const float* dbtp1, const float* b0c,
-                    float* ct, cudaStream_t st);
-cudaError_t e_field(const G32& g, const float* ct, const float* nu, const float* aj, const float* np, float gp,
-                    float* E, cudaStream_t st);
-cudaError_t b_update(const G32& g, const float* E, const double* base, const float* b0c, double coef, double* b1p2,
-                     float* db1p2, const float* db1, float* dbtp1, cudaStream_t st);
+// One half of a field subcycle in two fused kernels: aj and the cross
+// product ct (predictor: B from dB; corrector: B at m+1/2), then E on the
+// fly, curlE and B_new = base - coef*curlE in double-float (hi, lo float
+// pairs) with its FP32 dB (and, predictor, dB at m+1/2 = (dB_new + dB1)/2).
+cudaError_t aj_ct(const G32& g, bool corr, const float* db, const float* np, const float* up, const float* b0c,
+                  float alpha, float* aj, float* ct, cudaStream_t st);
+cudaError_t b_step(const G32& g, bool pred, bool write_e, const float* ct, const float* nu, const float* aj,
+                   const float* bh, const float* bl, double coef, const float* b0c, float* oh, float* ol, float* dbo,
+                   const float* db1, float* dbtp1, float* E, cudaStream_t st);
+// FP64 <-> double-float (hi + lo).
+cudaError_t split_df(long long n, const double* a, float* h, float* l, cudaStream_t st);
+cudaError_t join_df(long long n, const float* h, const float* l, double* a, cudaStream_t st);
 cudaError_t courant_min(const G32& g, const float* dbt, const float* b0c, const float* np, float alpha, float dx,
                         float* dtn, float* d_min, cudaStream_t st);
 
 // ---- sort ----
 cudaError_t sort_prep(const G32& g, const int64_t* start, const int32_t* cell, uint32_t* dirrank, uint16_t* dep,
                       int* err, cudaStream_t st);
-// ncount (may be null): new ions per key, placed after the arrivals.
-cudaError_t sort_count(const G32& g, const uint16_t* dep, const int32_t* ncount, int64_t* count, uint16_t* pre,
-                       int* err, cudaStream_t st);
+// ncount (may be null): new ions per key, placed after the arrivals.  order:
+// the BCELLS x NDIR table of sort_order_table on the device.
+cudaError_t sort_count(const G32& g, const uint16_t* dep, const int32_t* ncount, const uint8_t* order,
+                       int64_t* count, uint16_t* pre, int* err, cudaStream_t st);
+// Directions by increasing source key for every place in a brick (host).
+void sort_order_table(uint8_t* out);
 cudaError_t scan_exclusive(const int64_t* in, int64_t* out, long long n, int64_t* block_sums, cudaStream_t st);
 // Survivors to start_new[X] + pre + rank; removed ions are skipped; cap = ni_max.
 cudaError_t sort_scatter(const G32& g, long long N, long long cap, const int32_t* cell, const uint32_t* dirrank,
@@ -177,6 +183,7 @@ cudaError_t grid_f32_to_f64(long long n, const float* a, double* out, cudaStream
 cudaError_t assign_species(long long N, const double* mrat, const double* beta_p, const double* tab_mrat,
                            const double* tab_bp, int n, uint8_t* spid, int* miss, cudaStream_t st);
 cudaError_t energy32(const G32& g, long long N, const Part& p, const Species& sp, double vol, const double* b0,
-                     const double* b1, const float* E, double alpha, double* acc4, cudaStream_t st);
+                     const float* b1h, const float* b1l, const float* E, double alpha, double* acc4,
+                     cudaStream_t st);
 
 }  // namespace swapk32

@@ -327,13 +327,17 @@ __global__ void k_deposit_u(Geo g, PartDev p, long long N, double beta, int mode
   const long long C = g.C;
   GRID_STRIDE(l, N) {
     double v[3];
+    const double sq = mode >= 3 ? sqrt(p.mrat[l]) : 1.0;
     for (int m = 0; m < 3; ++m) {
       const double a = va[l + m * p.NM];
       if (mode == 0) v[m] = a;
       else if (mode == 1) v[m] = 1.5 * a - 0.5 * vb[l + m * p.NM];  // gutsp.f:144
-      else {
+      else if (mode == 2) {
         v[m] = 0.5 * (a + vb[l + m * p.NM]);  // gutsp.f:422
         out_v1[l + m * p.NM] = v[m];
+      } else {
+        const double mv = a / sq;  // get_temperature's mvp (gutsp.f:2291)
+        v[m] = mode == 3 ? mv * mv : mv;
       }
     }
     const int i = p.ijk[l], j = p.ijk[l + p.NM], k = p.ijk[l + 2 * p.NM];
@@ -353,6 +357,47 @@ __global__ void k_deposit_u(Geo g, PartDev p, long long N, double beta, int mode
       atomicAdd(S + tg[c] + C, v[1] * w);
       atomicAdd(S + tg[c] + 2 * C, v[2] * w);
     }
+  }
+}
+
+// update_rho deposit (gutsp.f:1543-1567): (w/mrat)/volb.
+__global__ void k_deposit_rho(Geo g, PartDev p, long long N, double beta, double* __restrict__ mnp, int* err) {
+  GRID_STRIDE(l, N) {
+    const int i = p.ijk[l], j = p.ijk[l + p.NM], k = p.ijk[l + 2 * p.NM];
+    if (!cell_ok(g, i, j, k)) {
+      set_err(err, KERR_DOMAIN);
+      continue;
+    }
+    const double volb =
+        (g.qx[i + 1] - g.qx[i]) * (g.qy[j + 1] - g.qy[j]) * (g.qz[k + 1] - g.qz[k]) * beta * p.beta_p[l];
+    long long tg[8];
+    corner_targets(g, i, j, k, tg);
+    for (int c = 0; c < 8; ++c)
+      if (tg[c] >= 0) atomicAdd(mnp + tg[c], (p.wght[l + c * p.NM] / p.mrat[l]) / volb);
+  }
+}
+
+// f *= a on interior nodes.
+__global__ void k_scale_int(Geo g, double* __restrict__ f, double a) {
+  GRID_STRIDE(t, n_interior(g)) {
+    int i, j, k;
+    interior_ijk(g, t, i, j, k);
+    const long long o = nidx(g, i, j, k);
+    f[o] = a * f[o];
+  }
+}
+
+// temp_p = (1/3)*1e6*mion*|<mvp^2> - <mvp>^2| at every node (gutsp.f:2521-2527).
+__global__ void k_temperature(Geo g, const double* __restrict__ up2, const double* __restrict__ upa, double mion,
+                              double* __restrict__ temp) {
+  const long long C = g.C;
+  GRID_STRIDE(o, C) {
+    double a = 0.0;
+    for (int m = 0; m < 3; ++m) {
+      const double d = up2[o + C * m] - upa[o + C * m] * upa[o + C * m];
+      a = a + d * d;
+    }
+    temp[o] = (1.0 / 3.0) * 1e6 * mion * sqrt(a);
   }
 }
 
@@ -535,7 +580,7 @@ __global__ void k_energy_fields(Geo g, double alpha, const double* __restrict__ 
                                 const double* __restrict__ E, double* acc) {
   const long long N = n_interior(g);
   const long long C = g.C;
-  double s1 = 0, s2 = 0, s3 = 0;
+  double s1 = 0, s2 = 0, s3 = 0, sc[3] = {0, 0, 0};
   GRID_STRIDE(t, N) {
     int i, j, k;
     interior_ijk(g, t, i, j, k);
@@ -543,10 +588,16 @@ __global__ void k_energy_fields(Geo g, double alpha, const double* __restrict__ 
     const double vol = g.dxc[i] * g.dyc[j] * g.dzc[k];
     for (int m = 0; m < 3; ++m) {
       const double b = b1[o + C * m], d = b1[o + C * m] - b0[o + C * m], e = E[o + C * m];
-      s1 += 0.5 * d * d * vol / alpha;
+      const double eb = 0.5 * d * d * vol / alpha;
+      s1 += eb;
+      sc[m] += eb;
       s2 += 0.5 * b * b * vol / alpha;
       s3 += 0.5 * e * e * vol;
     }
+  }
+  for (int m = 0; m < 3; ++m) {  // per component of |b1-b0|^2 (EB1x, EB1y, EB1z)
+    sc[m] = block_sum(sc[m]);
+    if (threadIdx.x == 0) atomicAdd(acc + 4 + m, sc[m]);
   }
   s1 = block_sum(s1);
   if (threadIdx.x == 0) atomicAdd(acc + 1, s1);
@@ -641,6 +692,18 @@ cudaError_t deposit_u(const Geo& g, const PartDev& p, long long N, double beta, 
   if (N <= 0) return cudaSuccess;
   LAUNCH(k_deposit_u, N, g, p, N, beta, mode, va, vb, out_v1, S, err);
 }
+cudaError_t deposit_rho(const Geo& g, const PartDev& p, long long N, double beta, double* mnp, int* err,
+                        cudaStream_t st) {
+  if (N <= 0) return cudaSuccess;
+  LAUNCH(k_deposit_rho, N, g, p, N, beta, mnp, err);
+}
+cudaError_t scale_interior(const Geo& g, double* f, double a, cudaStream_t st) {
+  LAUNCH(k_scale_int, n_interior(g), g, f, a);
+}
+cudaError_t temperature(const Geo& g, const double* up2, const double* upa, double mion, double* temp,
+                        cudaStream_t st) {
+  LAUNCH(k_temperature, g.C, g, up2, upa, mion, temp);
+}
 cudaError_t ct_from_sums(const Geo& g, const double* S, const double* np, double* ct, cudaStream_t st) {
   LAUNCH(k_ct_from_sums, n_interior(g), g, S, np, ct);
 }
@@ -673,7 +736,7 @@ cudaError_t reduce_min(const double* x, long long n, double* d_out, int, cudaStr
 }
 cudaError_t energy_parts(const Geo& g, const PartDev& p, long long N, double beta, double alpha, const double* vp,
                          const double* b0, const double* b1, const double* E, double* d_acc4, cudaStream_t st) {
-  cudaError_t e = cudaMemsetAsync(d_acc4, 0, 4 * sizeof(double), st);
+  cudaError_t e = cudaMemsetAsync(d_acc4, 0, 7 * sizeof(double), st);
   if (e != cudaSuccess) return e;
   if (N > 0) {
     k_energy_particles<<<nblocks(N), TPB, 0, st>>>(p, N, beta, vp, d_acc4);

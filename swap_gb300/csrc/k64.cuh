@@ -41,10 +41,18 @@ cudaError_t grad_pe_face_int(const Geo& g, const double* np, double grad_pe, dou
 cudaError_t interp_weights(const Geo& g, const PartDev& p, long long N, int* err, cudaStream_t st);
 cudaError_t deposit_np(const Geo& g, const PartDev& p, long long N, double beta, double* np, int* err,
                        cudaStream_t st);
-// mode: 0 = v, 1 = 1.5 v - 0.5 v1 (extrapol_up), 2 = 0.5 (a + b) (improve_up, also stores into out_v1)
+// mode: 0 = v, 1 = 1.5 v - 0.5 v1 (extrapol_up), 2 = 0.5 (a + b) (improve_up, also stores into out_v1),
+// 3 = (v/sqrt(mrat))^2 and 4 = v/sqrt(mrat) per component (get_temperature)
 cudaError_t deposit_u(const Geo& g, const PartDev& p, long long N, double beta, int mode, const double* va,
                       const double* vb, double* out_v1, double* S, int* err, cudaStream_t st);
 cudaError_t ct_from_sums(const Geo& g, const double* S, const double* np, double* ct, cudaStream_t st);
+// update_rho deposit (folded into the interior), interior scaling, and the
+// temperature of get_temperature from the two face moments.
+cudaError_t deposit_rho(const Geo& g, const PartDev& p, long long N, double beta, double* mnp, int* err,
+                        cudaStream_t st);
+cudaError_t scale_interior(const Geo& g, double* f, double a, cudaStream_t st);
+cudaError_t temperature(const Geo& g, const double* up2, const double* upa, double mion, double* temp,
+                        cudaStream_t st);
 cudaError_t get_Ep(const Geo& g, const PartDev& p, long long N, const double* ajc, const double* upc,
                    const double* btc, const double* gpc, double* Ep, int* err, cudaStream_t st);
 cudaError_t vplus_vminus(const Geo& g, const PartDev& p, long long N, double dt, const double* Ep,

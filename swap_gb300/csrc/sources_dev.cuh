@@ -54,6 +54,21 @@ __device__ __forceinline__ bool inflow_candidate(const Geo& g, const swap_source
   return xn > x0 && !(xn > g.qx[g.nx - 1]);
 }
 
+// Whether inflow candidate `slot` enters the box: the draws and operations
+// of inflow_candidate that decide it, and nothing else.
+__device__ __forceinline__ bool inflow_enters(const Geo& g, const swap_sources& s, long long step, long long slot,
+                                              double dt) {
+  const double pi = 3.14159265358979323846;
+  double u[4], v[4];
+  swapk::source_uniforms(s.seed, swapk::RNG_INFLOW, step, slot, 0u, u);
+  swapk::source_uniforms(s.seed, swapk::RNG_INFLOW, step, slot, 1u, v);
+  const double vx = s.inflow_ux + s.inflow_vth * sqrt(-log(u[3])) * cos(pi * v[0]);
+  const double x0 = g.qx[1], dxg = g.dxg[1];
+  const double xg = x0 - dxg + u[0] * dxg;
+  const double xn = xg + dt * vx;
+  return xn > x0 && !(xn > g.qx[g.nx - 1]);
+}
+
 // Neutral cloud density n_n(r) = N0/(1+(r/r0)^2).
 __device__ __forceinline__ double cloud_density(const swap_sources& s, double x, double y, double z) {
   const double dx = x - s.cloud_x, dy = y - s.cloud_y, dz = z - s.cloud_z;

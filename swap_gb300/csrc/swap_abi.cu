@@ -358,6 +358,25 @@ int vp_final(swap_ctx* c, const double* Ep, double* vp, double* vp1, const doubl
   return 0;
 }
 
+// update_rho (gutsp.f:1517-1590): mion * sum (w/mrat)/volb, folded, periodic.
+int update_rho(swap_ctx* c, double* mnp) {
+  TRY(need_weights(c));
+  KL("cudaMemsetAsync", cudaMemsetAsync(mnp, 0, (std::size_t)c->g.C * sizeof(double), c->st));
+  KL("deposit_rho", deposit_rho(c->g, c->part_view(), c->ntot(), c->prm.beta, mnp, c->d_err, c->st));
+  KL("scale_interior", scale_interior(c->g, mnp, c->mion, c->st));
+  KL("periodic", periodic1(c->g, mnp, c->st));
+  return 0;
+}
+
+// get_temperature (gutsp.f:2257-2541): the face moments of (v/sqrt(mrat))^2
+// and v/sqrt(mrat) through update_up's path, then the temperature per node.
+int get_temperature(swap_ctx* c, const double* vp, const double* np, double* temp_p) {
+  TRY(update_up_mode(c, 3, vp, nullptr, nullptr, np, c->s_btc2));
+  TRY(update_up_mode(c, 4, vp, nullptr, nullptr, np, c->s_btmf));
+  KL("temperature", temperature(c->g, c->s_btc2, c->s_btmf, c->mion, temp_p, c->st));
+  return 0;
+}
+
 int move_ion_half(swap_ctx* c, double* xp, const double* vp) {
   KL("move_half", move_half(c->g, c->part_view(), c->ntot(), c->prm.dt, xp, vp, srcops::x_open(c), c->st));
   return 0;
@@ -802,6 +821,34 @@ extern "C" int swap_periodic_scalar(swap_ctx* c, double* b) {
   TRY(c->use(b, Access::InOut, &db));
   CU(periodic1(c->g, db, c->st));
   return c->finish();
+}
+
+extern "C" int swap_update_rho(swap_ctx* c, double* mnp) {
+  ENTRY;
+  double* d;
+  TRY(need_particle_scalars(c));
+  TRY(c->use(mnp, Access::Out, &d));
+  TRY(ops::update_rho(c, d));
+  return c->finish();
+}
+
+extern "C" int swap_get_temperature(swap_ctx* c, const double* xp, const double* vp, const double* np,
+                                    double* temp_p) {
+  ENTRY;
+  (void)xp;  // the reference reads positions through ijkp/wght only
+  double *dvp, *dnp, *dt;
+  TRY(need_particle_scalars(c));
+  TRY(c->use(vp, Access::In, &dvp));
+  TRY(c->use(np, Access::In, &dnp));
+  TRY(c->use(temp_p, Access::Out, &dt));
+  TRY(ops::get_temperature(c, dvp, dnp, dt));
+  return c->finish();
+}
+
+extern "C" int swap_set_mion(swap_ctx* c, double mion) {
+  if (!c || !(mion > 0)) return SWAP_EINVAL;
+  c->mion = mion;
+  return SWAP_OK;
 }
 
 // ---------------------------------------------------------------------------

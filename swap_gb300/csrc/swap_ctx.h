@@ -66,6 +66,7 @@ struct swap_ctx {
   // particle work arrays of the fused step (maind.f locals Ep, vplus, vminus)
   double *w_Ep = nullptr, *w_vplus = nullptr, *w_vminus = nullptr;
   double last_dtsub = 0, last_ntf = 0;
+  double mion = 1.0;  // ion mass of update_rho / get_temperature (normalized units: 1)
   void* f32_state = nullptr;  // the FP32 form (swap_f32.cu)
 
   // particle sources and sinks (swap_sources.cu)

@@ -5,7 +5,8 @@
 // advances whole ion steps (maind.f:385-479); swap_f32_end writes the state
 // back into the bound arrays' device mirrors (particles come back in sorted
 // order).  Precision: particle positions as int32 cell + FP32 offset, FP32
-// velocities and moments, FP64 accumulation of B across subcycles.
+// velocities and moments, B accumulated across subcycles in double-float
+// (float hi + lo pairs, 48 significant bits).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -34,8 +35,13 @@ struct F32State {
   float4* kit = nullptr;
   float *np = nullptr, *S = nullptr, *up = nullptr, *aj = nullptr, *ct = nullptr, *E = nullptr, *nu = nullptr;
   float *db1 = nullptr, *db1p2 = nullptr, *dbtp1 = nullptr;
-  double *b0 = nullptr, *b1 = nullptr, *b12 = nullptr, *b1p2 = nullptr;
+  double* b0 = nullptr;  // FP64 b0, for the diagnostics
+  // B levels in double-float: hi + lo float pairs (48 significant bits)
+  struct DF {
+    float *h = nullptr, *l = nullptr;
+  } b1, b12, b1p2;
   float* b0c = nullptr;  // 3 floats: the uniform b0
+  uint8_t* order = nullptr;  // source-key order table of the incremental sort
   float* dtn = nullptr;  // per-node Courant time
   float* d_min = nullptr;
   double* acc = nullptr;
@@ -226,21 +232,31 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
   s->dirrank = s->alloc<uint32_t>(NMs);
   s->dep = s->alloc<uint16_t>(nk * NDIR);
   s->pre = s->alloc<uint16_t>(nk * NDIR);
+  s->order = s->alloc<uint8_t>(BCELLS * NDIR);
+  {
+    uint8_t ord[BCELLS * NDIR];
+    sort_order_table(ord);
+    if (!s->order || cudaMemcpy(s->order, ord, sizeof(ord), cudaMemcpyHostToDevice) != cudaSuccess)
+      return c->fail(SWAP_ECUDA, "sort order table");
+  }
   s->partial = s->alloc<float>((std::size_t)g.nbricks * 4 * TNODES);
   s->kit = s->alloc<float4>(2 * (std::size_t)ncx * ncy * ncz);
   s->np = s->alloc<float>(C); s->S = s->alloc<float>(3 * C); s->up = s->alloc<float>(3 * C);
   s->aj = s->alloc<float>(3 * C); s->ct = s->alloc<float>(3 * C); s->E = s->alloc<float>(3 * C);
   s->nu = s->alloc<float>(C);
   s->db1 = s->alloc<float>(3 * C); s->db1p2 = s->alloc<float>(3 * C); s->dbtp1 = s->alloc<float>(3 * C);
-  s->b0 = s->alloc<double>(3 * C); s->b1 = s->alloc<double>(3 * C); s->b12 = s->alloc<double>(3 * C);
-  s->b1p2 = s->alloc<double>(3 * C);
+  s->b0 = s->alloc<double>(3 * C);
+  for (F32State::DF* d : {&s->b1, &s->b12, &s->b1p2}) {
+    d->h = s->alloc<float>(3 * C);
+    d->l = s->alloc<float>(3 * C);
+  }
   s->b0c = s->alloc<float>(4);
   s->d_min = s->alloc<float>(4);
   s->dtn = s->alloc<float>(C);
   s->acc = s->alloc<double>(4);
   if (!s->start || !s->start_new || !s->count || !s->sums || !s->dirrank || !s->dep || !s->pre || !s->partial || !s->kit ||
       !s->np || !s->S || !s->up || !s->aj || !s->ct || !s->E || !s->nu || !s->db1 || !s->db1p2 || !s->dbtp1 ||
-      !s->b0 || !s->b1 || !s->b12 || !s->b1p2 || !s->b0c || !s->d_min || !s->acc || !s->dtn)
+      !s->b0 || !s->b1.l || !s->b12.l || !s->b1p2.l || !s->b0c || !s->d_min || !s->acc || !s->dtn)
     return c->fail(SWAP_ECUDA, "FP32 grid allocation failed");
   CU(cudaMemsetAsync(s->np, 0, C * sizeof(float), c->st));
   for (void* p : {(void*)s->S, (void*)s->up, (void*)s->aj, (void*)s->ct, (void*)s->E})
@@ -250,8 +266,8 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
   // fields: FP64 levels copied, dB = B - b0 in FP32, nu in FP32
   const std::size_t b3 = 3 * C * sizeof(double);
   CU(cudaMemcpyAsync(s->b0, b0, b3, cudaMemcpyDeviceToDevice, c->st));
-  CU(cudaMemcpyAsync(s->b1, b1, b3, cudaMemcpyDeviceToDevice, c->st));
-  CU(cudaMemcpyAsync(s->b12, b12, b3, cudaMemcpyDeviceToDevice, c->st));
+  CU(split_df(3 * g.C, b1, s->b1.h, s->b1.l, c->st));
+  CU(split_df(3 * g.C, b12, s->b12.h, s->b12.l, c->st));
   CU(grid_f64_to_f32(3 * g.C, b1, b0, s->db1, c->st));
   CU(grid_f64_to_f32(g.C, nud, nullptr, s->nu, c->st));
 
@@ -345,15 +361,15 @@ static int subcycles(swap_ctx* c, F32State* s) {
   const int n = (int)ntf;
   const float alpha = (float)c->prm.alpha;
   for (int it = 0; it < n; ++it) {
-    KL("f32_curlB", curlB32(g, s->db1, s->np, alpha, s->aj, c->st));                      // maind.f:430
-    KL("f32_ct_pred", ct_pred(g, s->aj, s->up, s->db1, s->b0c, s->ct, c->st));            // get_E
-    KL("f32_E", e_field(g, s->ct, s->nu, s->aj, s->np, 0.f, s->E, c->st));
-    KL("f32_bupd", b_update(g, s->E, s->b12, s->b0c, 2.0 * dtsub, s->b1p2, s->db1p2, nullptr, nullptr, c->st));  // predict_B
-    KL("f32_half", half_sum32(g, s->db1p2, s->db1, s->dbtp1, c->st));                      // get_Ep1
-    KL("f32_curlB", curlB32(g, s->dbtp1, s->np, alpha, s->aj, c->st));
-    KL("f32_ct_corr", ct_corr(g, s->aj, s->up, s->dbtp1, s->b0c, s->ct, c->st));
-    KL("f32_E", e_field(g, s->ct, s->nu, s->aj, s->np, 0.f, s->E, c->st));
-    KL("f32_bupd", b_update(g, s->E, s->b1, s->b0c, dtsub, s->b1p2, s->db1p2, nullptr, nullptr, c->st));  // correct_B
+    const bool last = it == n - 1;
+    // predictor: curlB (maind.f:430) and predict_B with its get_E (maind.f:457), plus dB at m+1/2
+    KL("f32_aj_ct_pred", aj_ct(g, false, s->db1, s->np, s->up, s->b0c, alpha, s->aj, s->ct, c->st));
+    KL("f32_bstep_pred", b_step(g, true, false, s->ct, s->nu, s->aj, s->b12.h, s->b12.l, 2.0 * dtsub, s->b0c,
+                                s->b1p2.h, s->b1p2.l, s->db1p2, s->db1, s->dbtp1, s->E, c->st));
+    // corrector: correct_B (maind.f:462) with its curlB and get_Ep1 at m+1/2
+    KL("f32_aj_ct_corr", aj_ct(g, true, s->dbtp1, s->np, s->up, s->b0c, alpha, s->aj, s->ct, c->st));
+    KL("f32_bstep_corr", b_step(g, false, last, s->ct, s->nu, s->aj, s->b1.h, s->b1.l, dtsub, s->b0c, s->b1p2.h,
+                                s->b1p2.l, s->db1p2, nullptr, nullptr, s->E, c->st));
     // f_update_tlev (gutsf.f:10-35): b12 <- b1, b1 <- b1p2 (bt = b1)
     std::swap(s->b12, s->b1);
     std::swap(s->b1, s->b1p2);
@@ -376,7 +392,8 @@ static int sort_step(swap_ctx* c, F32State* s, long long src_step) {
   const bool staged = n_max > 0;
   const long long cap = c->dims.ni_max;
   KL("f32_sort_prep", sort_prep(g, s->start, a.cell, s->dirrank, s->dep, c->d_err, c->st));
-  KL("f32_sort_count", sort_count(g, s->dep, staged ? s->stage.ncount : nullptr, s->count, s->pre, c->d_err, c->st));
+  KL("f32_sort_count", sort_count(g, s->dep, staged ? s->stage.ncount : nullptr, s->order, s->count, s->pre,
+                                  c->d_err, c->st));
   KL("f32_sort_scan", scan_exclusive(s->count, s->start_new, g.nkeys, s->sums, c->st));
   KL("f32_sort_scatter", sort_scatter(g, s->N, cap, a.cell, s->dirrank, s->pre, s->start_new, a, b, c->d_err, c->st));
   if (staged)
@@ -485,10 +502,10 @@ extern "C" int swap_f32_end(swap_ctx* c) {
   *c->ni_tot_ptr = (int32_t)s->N;
   s->ended = true;
   const std::size_t b3 = 3 * (std::size_t)g.C * sizeof(double);
-  CU(cudaMemcpyAsync(b1, s->b1, b3, cudaMemcpyDeviceToDevice, c->st));
-  CU(cudaMemcpyAsync(bt, s->b1, b3, cudaMemcpyDeviceToDevice, c->st));
-  CU(cudaMemcpyAsync(b1p2, s->b1, b3, cudaMemcpyDeviceToDevice, c->st));
-  CU(cudaMemcpyAsync(b12, s->b12, b3, cudaMemcpyDeviceToDevice, c->st));
+  CU(join_df(3 * g.C, s->b1.h, s->b1.l, b1, c->st));
+  CU(cudaMemcpyAsync(bt, b1, b3, cudaMemcpyDeviceToDevice, c->st));
+  CU(cudaMemcpyAsync(b1p2, b1, b3, cudaMemcpyDeviceToDevice, c->st));
+  CU(join_df(3 * g.C, s->b12.h, s->b12.l, b12, c->st));
   CU(grid_f32_to_f64(g.C, s->np, npd, c->st));
   CU(grid_f32_to_f64(3 * g.C, s->up, upd, c->st));
   CU(grid_f32_to_f64(3 * g.C, s->E, Ed, c->st));
@@ -513,7 +530,7 @@ extern "C" int swap_f32_energy(swap_ctx* c, double out[4]) {
   if (!s) return c->fail(SWAP_EINVAL, "swap_f32_begin has not been called");
   const G32& g = s->g;
   const double vol = (double)g.dx * g.dy * g.dz;
-  CU(energy32(g, s->N, s->buf[s->cur], s->sp, vol, s->b0, s->b1, s->E, c->prm.alpha, s->acc, c->st));
+  CU(energy32(g, s->N, s->buf[s->cur], s->sp, vol, s->b0, s->b1.h, s->b1.l, s->E, c->prm.alpha, s->acc, c->st));
   CU(cudaMemcpyAsync(out, s->acc, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->st));
   CU(cudaStreamSynchronize(c->st));
   return SWAP_OK;

@@ -11,6 +11,8 @@ int update_np(swap_ctx* c, double* np);
 // update_up with the velocity chosen by mode (0 v, 1 1.5v-0.5v1, 2 0.5(v+ + v-)).
 int update_up_mode(swap_ctx* c, int mode, const double* va, const double* vb, double* out_v1, const double* np,
                    double* up);
+int update_rho(swap_ctx* c, double* mnp);
+int get_temperature(swap_ctx* c, const double* vp, const double* np, double* temp_p);
 }  // namespace ops
 
 // Particle sources and sinks (swap_sources.cu).  Each updates *ni_tot.

@@ -49,12 +49,10 @@ __global__ void k_ionize(Geo g, PView p, long long N, long long n, swap_sources 
 }
 
 __global__ void k_inflow_flags(Geo g, swap_sources s, long long step, double dt, int64_t* flag) {
-  const int ncy = g.ny - 2, ncz = g.nz - 2, ppc = s.inflow_ppc;
+  const long long ncy = g.ny - 2, ncz = g.nz - 2, ppc = s.inflow_ppc;
   const long long nslot = (long long)ncy * ncz * ppc;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nslot; t += (long long)gridDim.x * blockDim.x) {
-    const int cj = (int)((t / ppc) % ncy), ck = (int)(t / ((long long)ppc * ncy));
-    double st[6];
-    flag[t] = swapsrc::inflow_candidate(g, s, step, t, cj, ck, dt, st) ? 1 : 0;
+    flag[t] = swapsrc::inflow_enters(g, s, step, t, dt) ? 1 : 0;
   }
 }
 
@@ -208,31 +206,37 @@ __global__ void k32_stage_cloud(Geo g64, G32 g, swap_sources s, long long step, 
   }
 }
 
-// Inflow ions of face cell (cj, ck): all enter physical cell (0, cj, ck);
-// staged at base+pos[slot] in slot order.
+// Inflow ions: slot t of face cell f = t / ppc enters physical cell
+// (0, cj, ck); staged at base+pos[t]; its rank among the key's new ions
+// follows the ones staged before (ncount) and the earlier slots of its face.
 __global__ void k32_stage_inflow(Geo g64, G32 g, swap_sources s, long long step, double dt, const int64_t* flag,
                                  const int64_t* pos, long long base, swapk32::Part st, int32_t* key, int32_t* rank,
-                                 int32_t* ncount, uint8_t sp, int* err) {
-  const long long nface = (long long)g.ncy * g.ncz;
+                                 const int32_t* ncount, uint8_t sp, int* err) {
   const int ppc = s.inflow_ppc;
-  for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < nface; f += (long long)gridDim.x * blockDim.x) {
+  const long long nslot = (long long)g.ncy * g.ncz * ppc;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nslot; t += (long long)gridDim.x * blockDim.x) {
+    if (!flag[t]) continue;
+    const long long f = t / ppc;
     const int cj = (int)(f % g.ncy), ck = (int)(f / g.ncy);
     const int32_t X = (int32_t)key_of(g, 0, cj, ck);
-    const int32_t r0 = ncount[X];
-    int32_t k = 0;
-    for (int p = 0; p < ppc; ++p) {
-      const long long slot = f * ppc + p;
-      if (!flag[slot]) continue;
-      double x[6];
-      swapsrc::inflow_candidate(g64, s, step, slot, cj, ck, dt, x);
-      if ((x[0] - g.qx1) / g.dx > 1.0) atomicCAS(err, 0, KERR_MOVE);  // entered past the first cell
-      const long long o = base + pos[slot];
-      stage_one(st, o, 0, cj, ck, offset_in_cell(x[0], g.qx1, g.dx, 0, true),
-                offset_in_cell(x[1], g.qy1, g.dy, cj, false), offset_in_cell(x[2], g.qz1, g.dz, ck, true), x + 3, sp);
-      key[o] = X;
-      rank[o] = r0 + k++;
-    }
-    ncount[X] = r0 + k;
+    double x[6];
+    swapsrc::inflow_candidate(g64, s, step, t, cj, ck, dt, x);
+    if ((x[0] - g.qx1) / g.dx > 1.0) atomicCAS(err, 0, KERR_MOVE);  // entered past the first cell
+    const long long o = base + pos[t];
+    stage_one(st, o, 0, cj, ck, offset_in_cell(x[0], g.qx1, g.dx, 0, true),
+              offset_in_cell(x[1], g.qy1, g.dy, cj, false), offset_in_cell(x[2], g.qz1, g.dz, ck, true), x + 3, sp);
+    key[o] = X;
+    rank[o] = ncount[X] + (int32_t)(pos[t] - pos[f * ppc]);
+  }
+}
+
+// After k32_stage_inflow: the inflow ions of each face cell join the count
+// of its key.
+__global__ void k32_count_inflow(G32 g, int ppc, const int64_t* pos, int32_t* ncount) {
+  const long long nface = (long long)g.ncy * g.ncz;
+  for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < nface; f += (long long)gridDim.x * blockDim.x) {
+    const int cj = (int)(f % g.ncy), ck = (int)(f / g.ncy);
+    ncount[key_of(g, 0, cj, ck)] += (int32_t)(pos[(f + 1) * ppc] - pos[f * ppc]);
   }
 }
 
@@ -578,10 +582,12 @@ int f32_stage(swap_ctx* c, const swapk32::G32& g, F32Stage& st, long long m, lon
       k_inflow_flags<<<nb(nslot), TPB, 0, c->st>>>(c->g, s, m, c->prm.dt, c->src_flag);
       CU(cudaGetLastError());
       CU(swapk32::scan_exclusive(c->src_flag, c->src_pos, nslot, c->src_sums, c->st));
-      const long long nface = (long long)g.ncy * g.ncz;
-      k32_stage_inflow<<<nb(nface), TPB, 0, c->st>>>(c->g, g, s, m, c->prm.dt, c->src_flag, c->src_pos,
+      k32_stage_inflow<<<nb(nslot), TPB, 0, c->st>>>(c->g, g, s, m, c->prm.dt, c->src_flag, c->src_pos,
                                                      n_ion + n_cloud, st.part, st.key, st.rank, st.ncount,
                                                      st.sp_inflow, c->d_err);
+      CU(cudaGetLastError());
+      const long long nface = (long long)g.ncy * g.ncz;
+      k32_count_inflow<<<nb(nface), TPB, 0, c->st>>>(g, s.inflow_ppc, c->src_pos, st.ncount);
     }
     CU(cudaGetLastError());
     *n_dev = c->src_pos + nslot;

@@ -243,6 +243,15 @@ class Hybrid:
         self._check(self.lib.swap_check_time_step(self.ctx, abi.dptr(bt), abi.dptr(np_), C.byref(d), C.byref(n)))
         return d.value, n.value
 
+    def update_rho(self, mnp):
+        self._check(self.lib.swap_update_rho(self.ctx, abi.dptr(mnp)))
+
+    def get_temperature(self, xp, vp, np_, temp_p):
+        self._check(self.lib.swap_get_temperature(self.ctx, *map(abi.dptr, (xp, vp, np_, temp_p))))
+
+    def set_mion(self, mion: float):
+        self._check(self.lib.swap_set_mion(self.ctx, float(mion)))
+
     def periodic(self, b):
         self._check(self.lib.swap_periodic(self.ctx, abi.dptr(b)))
 

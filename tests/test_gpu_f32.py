@@ -1,5 +1,5 @@
-"""The FP32 form (int32 cell + FP32 offset particles, FP32 moments, FP64 B
-accumulation) through the C-ABI, against the FP64 oracle and against the
+"""The FP32 form (int32 cell + FP32 offset particles, FP32 moments, B
+accumulated in double-float) through the C-ABI, against the FP64 oracle and against the
 stable counting sort it must reproduce.
 
 Bars:
@@ -79,8 +79,9 @@ def test_f32_conversion_and_initial_sort():
     assert np.array_equal(np.bincount(k2, minlength=nkeys), counts)
 
 
-def test_f32_incremental_sort_is_the_stable_counting_sort():
-    h, n = tagged_hybrid(cells=(12, 8, 8), ppc=5, seed=9)
+@pytest.mark.parametrize("cells", [(12, 8, 8), (16, 12, 12)])  # second: most keys take the order-table path
+def test_f32_incremental_sort_is_the_stable_counting_sort(cells):
+    h, n = tagged_hybrid(cells=cells, ppc=5, seed=9)
     h.f32_begin()
     h.f32_end()
     h.sync_to_host()
