@@ -128,9 +128,9 @@ KERNEL_BYTES_F64 = {
 # Algorithmic bytes per unit for the FP32 form (particles: cell 4 + offsets 12
 # + v 12 + vp1 12 + species 1 = 41 B of state).
 KERNEL_BYTES_F32 = {
-    "f32_P1": 41 + 16,           # read state; write cell + offsets
+    "f32_P1": 41,                # read state (deposit only)
     "f32_P2": 29,                # read cell, offsets, v, species
-    "f32_P3": 29 + 40,           # + write v, vp1, cell, offsets
+    "f32_P3": 29 + 40 + 4,       # + write v, vp1, cell, offsets and the sort's direction/rank
     "f32_sort_scatter": 41 + 4 + 41,
     "f32_sort_prep": 4 + 4,
 }

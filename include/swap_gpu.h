@@ -189,6 +189,39 @@ int swap_inflow_x(swap_ctx* ctx, int32_t m_tstep);
 int swap_ionize_cloud(swap_ctx* ctx, int32_t m_tstep);
 int swap_remove_outflow_x(swap_ctx* ctx);
 
+/* ---- diagnostic output (maind.f:237-358, 498-573) ----
+ * Fortran sequential unformatted files in out_dir (which must end with a
+ * path separator, as the reference's out_dir): para.dat at open; every
+ * swap_diag_step writes c.energy.dat and c.momentum.dat; every nout-th step
+ * also c.np, c.b1 (bt), c.aj (aj*alpha*face-averaged np), c.E, c.up,
+ * c.temp_p (get_temperature/1.6e-19), c.mnp (update_rho), the particle
+ * files c.xp_0, c.vp_0, c.mrat_0, c.beta_p_0 (rank > 0: c.xp_<rank> ...),
+ * and zero-filled c.np_b, c.mixed, c.up_t, c.up_b, whose producers the
+ * reference does not call.  The energy record holds (input_E, input_EeP,
+ * Evp, Euf, EB1, EB1x, EB1y, EB1z, EE, EeP, input_chex, input_bill) with
+ * the full-3D normalized energies of swap_energy and 0 for fluid terms.
+ * Reads the FP64 state: with the FP32 form call swap_f32_end first. */
+typedef struct swap_diag_spec {
+  int32_t nt;          /* steps of the run (para.dat)                        */
+  int32_t nout;        /* dump every nout steps (inputs.dat nout)            */
+  int32_t real_bytes;  /* 4 (the reference's -real-size 32) or 8             */
+  int32_t rank;        /* 0 writes every file; k > 0 only its particles      */
+  double dtsub_init, vtop, vbottom, mion, m_pu, m_heavy, np_top, np_bottom, b0_top, b0_bottom, vth_top,
+      vth_bottom;      /* para.dat scalars; mion also sets swap_set_mion      */
+} swap_diag_spec;
+int swap_diag_open(swap_ctx* ctx, const char* out_dir, const swap_diag_spec* spec);
+int swap_diag_step(swap_ctx* ctx, int32_t m);
+int swap_diag_close(swap_ctx* ctx);
+
+/* ---- checkpoint / restart (the role of restart.vars, maind.f:208-226,
+ * 586-607, in this library's own binary layout) ----
+ * write: the bound arrays (synced to the host first), Ni_tot, the sources and
+ * their step counter and, when the FP32 form is running, its whole state.
+ * read: into a context with the same grid and arrays bound; restores the
+ * host arrays and, for an FP32 checkpoint, the FP32 state bit for bit. */
+int swap_checkpoint_write(swap_ctx* ctx, const char* path);
+int swap_checkpoint_read(swap_ctx* ctx, const char* path);
+
 /* ---- the FP32 form of the fused step ----
  * Particle positions as int32 cell + FP32 offset, FP32 velocities and
  * moments, B accumulated across subcycles in double-float (pairs of floats,

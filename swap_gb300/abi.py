@@ -85,6 +85,14 @@ class Sources(C.Structure):
     ]
 
 
+class DiagSpec(C.Structure):
+    """swap_diag_spec: diagnostic output settings and para.dat scalars."""
+
+    _fields_ = [("nt", C.c_int32), ("nout", C.c_int32), ("real_bytes", C.c_int32), ("rank", C.c_int32)] + [
+        (n, C.c_double) for n in ("dtsub_init", "vtop", "vbottom", "mion", "m_pu", "m_heavy", "np_top",
+                                  "np_bottom", "b0_top", "b0_bottom", "vth_top", "vth_bottom")]
+
+
 def make_sources(**kw) -> Sources:
     """A Sources with every rule off (all zero) except the fields given."""
     s = Sources()
@@ -141,6 +149,11 @@ SIGNATURES: dict[str, tuple] = {
     "swap_inflow_x": (C.c_int, [P, C.c_int32]),
     "swap_ionize_cloud": (C.c_int, [P, C.c_int32]),
     "swap_remove_outflow_x": (C.c_int, [P]),
+    "swap_diag_open": (C.c_int, [P, C.c_char_p, C.POINTER(DiagSpec)]),
+    "swap_diag_step": (C.c_int, [P, C.c_int32]),
+    "swap_diag_close": (C.c_int, [P]),
+    "swap_checkpoint_write": (C.c_int, [P, C.c_char_p]),
+    "swap_checkpoint_read": (C.c_int, [P, C.c_char_p]),
     "swap_f32_begin": (C.c_int, [P]),
     "swap_f32_run": (C.c_int, [P, C.c_int32]),
     "swap_f32_end": (C.c_int, [P]),

@@ -34,6 +34,7 @@ UNITS = [
     ("swap_noalloc.cu", ["--fmad=false"]),
     ("swap_sources.cu", ["--fmad=false", "-Xcompiler", "-ffp-contract=off"]),
     ("loader.cpp", ["-Xcompiler", "-fopenmp,-ffp-contract=off"]),
+    ("swap_diag.cu", []),
 ]
 
 

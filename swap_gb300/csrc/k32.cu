@@ -107,13 +107,29 @@ __device__ __forceinline__ int step_cell(int c, int c0, int n) {
 // particle passes
 // ---------------------------------------------------------------------------
 
+__device__ __forceinline__ int dir_index(int dx, int dy, int dz) { return (dx + 1) + 3 * (dy + 1) + 9 * (dz + 1); }
+
+// One CTA per brick; its particles are the contiguous range of the brick's
+// keys and lie in their key's cell (every move happens in pass 3, after
+// which the sort restores that).
+//   P1: deposit np and up at v_n = 1.5 v - 0.5 vp1 (maind.f:385-387, 399).
+//   P2: gather, Ep, v-/v+, deposit up at 0.5 (v+ + v-) (maind.f:400-402).
+//   P3: gather, Ep, v-/v+, vp1 = v, v = v+ + dt/2 Ep (maind.f:404-406), the
+//       half move of maind.f:408 and the deposit of np and up at it
+//       (:411-413), then the half move of maind.f:479 (v is unchanged by the
+//       field subcycles in between), open-x outflow after each move and
+//       res_chex after the second (maind.f:484).  It also prepares the sort:
+//       the direction of every particle's new cell from its key's cell and
+//       its rank among the particles of that key and direction, in order.
 template <int PASS, bool CHEX = false>
 __global__ void __launch_bounds__(TPB_PASS) k_pass(G32 g, Part p, Species sp, StepParams sprm,
                                               const int64_t* __restrict__ start, const float4* __restrict__ kit,
-                                              float* __restrict__ partial, int* err) {
+                                              float* __restrict__ partial, uint32_t* __restrict__ dirrank,
+                                              uint16_t* __restrict__ dep, int* err) {
   __shared__ float4 s_kit[PASS == 1 ? 2 : 2 * TNODES];
   __shared__ float s_dep[4 * TNODES];
   __shared__ __align__(16) float s_red[TPB_PASS / 32][32][36];  // per warp: [value][particle], padded
+  __shared__ unsigned s_rank[PASS == 3 ? BCELLS * NDIR : 1];   // running count per (local key, direction)
   const long long b = blockIdx.x;
   const int bi = (int)(b % g.nbx), bj = (int)((b / g.nbx) % g.nby), bk = (int)(b / ((long long)g.nbx * g.nby));
   const int c0x = 4 * bi, c0y = 4 * bj, c0z = 4 * bk;
@@ -128,6 +144,8 @@ __global__ void __launch_bounds__(TPB_PASS) k_pass(G32 g, Part p, Species sp, St
     }
   }
   for (int t = threadIdx.x; t < 4 * TNODES; t += blockDim.x) s_dep[t] = 0.0f;
+  if (PASS == 3)
+    for (int t = threadIdx.x; t < BCELLS * NDIR; t += blockDim.x) s_rank[t] = 0u;
   __syncthreads();
 
   const float hdt = 0.5f * sprm.dt;
@@ -137,61 +155,34 @@ __global__ void __launch_bounds__(TPB_PASS) k_pass(G32 g, Part p, Species sp, St
   for (long long base = first; base < last; base += blockDim.x) {
     const long long l = base + threadIdx.x;
     const int32_t c = l < last ? p.cell[l] : CELL_DEAD;
-    bool live = c >= 0;  // past the range, or removed by outflow
+    bool live = c >= 0;  // past the range, or removed
+    if (PASS == 3 && dirrank && !live && l < last) dirrank[l] = DR_DEAD;
     int t0 = -1;
+    int grp = -1;  // P3: local key * NDIR + direction for the sort, -1 when not sorted
     float w8[8], qdv[4];
     if (live) {
       const bool fresh = (c & CELL_FRESH) != 0;
       int ci = pk_i(c), cj = pk_j(c), ck = pk_k(c);
+      const int kl = (ci & 3) + 4 * (cj & 3) + 16 * (ck & 3);  // local key: the particle is in its key's cell
       float ox = p.ox[l], oy = p.oy[l], oz = p.oz[l];
       float vx = p.vx[l], vy = p.vy[l], vz = p.vz[l];
       int s = p.sp ? min((int)p.sp[l], MAX_SPECIES - 1) : 0;
       float mr = sp.mrat[s], qw = sp.qw[s];
       float dvx = 0.f, dvy = 0.f, dvz = 0.f;  // velocity deposited
-      bool moved = fresh;                     // a fresh ion's cell word loses its flag
+      int rx = ci - c0x, ry = cj - c0y, rz = ck - c0z;
       if (PASS == 1) {
-        float wx = p.wx[l], wy = p.wy[l], wz = p.wz[l];
-        if (fresh && sprm.drop_fresh) {
-          live = false;  // created for a step that is not taken
-        } else if (sprm.pending_move && !fresh) {  // maind.f:479 of the previous step
-          bool ok = move_axis(ci, ox, vx * hdt * g.inv_dx, g.ncx, true, !sprm.x_open);
-          ok &= move_axis(cj, oy, vy * hdt * g.inv_dy, g.ncy, false);
-          ok &= move_axis(ck, oz, vz * hdt * g.inv_dz, g.ncz, true);
-          if (!ok) set_err(err, KERR_MOVE);
-          moved = true;
-          if (ci < 0 || ci >= g.ncx) {
-            live = false;  // outflow through an open x face
-          } else if (CHEX && sprm.heavy_of[s] != s) {
-            // res_chex of the completed step (chem_rates.f:823-840), FP32
-            const float x = (float)g.qx1 + ((float)ci + ox) * g.dx - sprm.cloud_x;
-            const float y = (float)g.qy1 + ((float)cj + oy) * g.dy - sprm.cloud_y;
-            const float z = (float)g.qz1 + ((float)ck + oz) * g.dz - sprm.cloud_z;
-            const float vrel = sqrtf(vx * vx + vy * vy + vz * vz);
-            const float sigma = vrel > 0.f ? sprm.cx_a - sprm.cx_b * logf(vrel) : 0.f;
-            if (sigma > 0.f) {
-              const float dens = sprm.cloud_N0 / (1.0f + (x * x + y * y + z * z) * sprm.inv_r0sq);
-              const float prob = sprm.dt * dens * sigma * vrel;
-              if (swapk::source_uniform_f32(sprm.seed, swapk::RNG_CHEX, sprm.chex_step, l) < prob) {
-                vx = vy = vz = 0.f;
-                wx = wy = wz = 0.f;
-                p.vx[l] = 0.f; p.vy[l] = 0.f; p.vz[l] = 0.f;
-                p.wx[l] = 0.f; p.wy[l] = 0.f; p.wz[l] = 0.f;
-                s = sprm.heavy_of[s];
-                p.sp[l] = (uint8_t)s;
-                mr = sp.mrat[s];
-                qw = sp.qw[s];
-                ++n_chex;
-              }
-            }
+        if (fresh) {
+          if (sprm.drop_fresh) {  // created for a step that is not taken
+            live = false;
+            p.cell[l] = CELL_DEAD;
+          } else {
+            p.cell[l] = c & ~CELL_FRESH;
           }
         }
-        dvx = 1.5f * vx - 0.5f * wx;  // extrapol_up (gutsp.f:144)
-        dvy = 1.5f * vy - 0.5f * wy;
-        dvz = 1.5f * vz - 0.5f * wz;
-      }
-      int rx = rel_cell(ci, c0x, g.ncx), ry = rel_cell(cj, c0y, g.ncy), rz = rel_cell(ck, c0z, g.ncz);
-      bool inside = !(rx < -1 || rx > 4 || ry < -1 || ry > 4 || rz < -1 || rz > 4);
-      if (PASS != 1 && inside) {
+        dvx = 1.5f * vx - 0.5f * p.wx[l];  // extrapol_up (gutsp.f:144)
+        dvy = 1.5f * vy - 0.5f * p.wy[l];
+        dvz = 1.5f * vz - 0.5f * p.wz[l];
+      } else {
         // trilinear gather of (ajc-upc, btc) at the 8 corners (gutsp.f:217-251)
         const float wxl = 1.0f - ox, wxu = ox, wyl = 1.0f - oy, wyu = oy, wzl = 1.0f - oz, wzu = oz;
         const int tg = (rx + 1) + TN * ((ry + 1) + TN * (rz + 1));
@@ -225,33 +216,76 @@ __global__ void __launch_bounds__(TPB_PASS) k_pass(G32 g, Part p, Species sp, St
           dvx = 0.5f * (px + mx);
           dvy = 0.5f * (py + my);
           dvz = 0.5f * (pz + mz);
-        } else {  // get_vp_final (gutsp.f:444-445) and move_ion_half (gutsp.f:473-510)
-          p.wx[l] = vx; p.wy[l] = vy; p.wz[l] = vz;
+        } else {
+          // get_vp_final (gutsp.f:444-445)
+          float wx = vx, wy = vy, wz = vz;
           vx = px + hdt * ex;
           vy = py + hdt * ey;
           vz = pz + hdt * ez;
-          p.vx[l] = vx; p.vy[l] = vy; p.vz[l] = vz;
-          bool ok = move_axis(ci, ox, vx * hdt * g.inv_dx, g.ncx, true, !sprm.x_open);
-          ok &= move_axis(cj, oy, vy * hdt * g.inv_dy, g.ncy, false);
-          ok &= move_axis(ck, oz, vz * hdt * g.inv_dz, g.ncz, true);
-          if (!ok) set_err(err, KERR_MOVE);
-          moved = true;
-          if (ci < 0 || ci >= g.ncx) live = false;  // outflow through an open x face
           dvx = vx; dvy = vy; dvz = vz;
+          // move_ion_half of maind.f:408 (gutsp.f:473-510): the deposit position
+          const float mvx = vx * hdt * g.inv_dx, mvy = vy * hdt * g.inv_dy, mvz = vz * hdt * g.inv_dz;
+          bool ok = move_axis(ci, ox, mvx, g.ncx, true, !sprm.x_open);
+          ok &= move_axis(cj, oy, mvy, g.ncy, false);
+          ok &= move_axis(ck, oz, mvz, g.ncz, true);
+          const bool out1 = ci < 0 || ci >= g.ncx;  // outflow through an open x face
           rx = rel_cell(ci, c0x, g.ncx); ry = rel_cell(cj, c0y, g.ncy); rz = rel_cell(ck, c0z, g.ncz);
-          inside = !(rx < -1 || rx > 4 || ry < -1 || ry > 4 || rz < -1 || rz > 4);
+          float dox = ox, doy = oy, doz = oz;
+          // move_ion_half of maind.f:479: the stored position
+          int ci2 = ci, cj2 = cj, ck2 = ck;
+          bool out2 = out1;
+          if (!out1) {
+            ok &= move_axis(ci2, ox, mvx, g.ncx, true, !sprm.x_open);
+            ok &= move_axis(cj2, oy, mvy, g.ncy, false);
+            ok &= move_axis(ck2, oz, mvz, g.ncz, true);
+            out2 = ci2 < 0 || ci2 >= g.ncx;
+          }
+          if (!ok) set_err(err, KERR_MOVE);
+          if (CHEX && !out2 && sprm.heavy_of[s] != s) {
+            // res_chex (chem_rates.f:823-840) at the end of the step, FP32
+            const float x = (float)g.qx1 + ((float)ci2 + ox) * g.dx - sprm.cloud_x;
+            const float y = (float)g.qy1 + ((float)cj2 + oy) * g.dy - sprm.cloud_y;
+            const float z = (float)g.qz1 + ((float)ck2 + oz) * g.dz - sprm.cloud_z;
+            const float vrel = sqrtf(vx * vx + vy * vy + vz * vz);
+            const float sigma = vrel > 0.f ? sprm.cx_a - sprm.cx_b * logf(vrel) : 0.f;
+            if (sigma > 0.f) {
+              const float dens = sprm.cloud_N0 / (1.0f + (x * x + y * y + z * z) * sprm.inv_r0sq);
+              const float prob = sprm.dt * dens * sigma * vrel;
+              if (swapk::source_uniform_f32(sprm.seed, swapk::RNG_CHEX, sprm.chex_step, l) < prob) {
+                vx = vy = vz = 0.f;
+                wx = wy = wz = 0.f;
+                p.sp[l] = (uint8_t)sprm.heavy_of[s];
+                ++n_chex;
+              }
+            }
+          }
+          p.wx[l] = wx; p.wy[l] = wy; p.wz[l] = wz;
+          p.vx[l] = vx; p.vy[l] = vy; p.vz[l] = vz;
+          if (out2) {
+            p.cell[l] = CELL_DEAD;
+            if (dirrank) dirrank[l] = DR_DEAD;
+          } else {
+            p.cell[l] = pk(ci2, cj2, ck2);
+            p.ox[l] = ox; p.oy[l] = oy; p.oz[l] = oz;
+            const int sx = step_cell(ci2, c0x + (kl & 3), g.ncx), sy = step_cell(cj2, c0y + ((kl >> 2) & 3), g.ncy),
+                      sz = step_cell(ck2, c0z + (kl >> 4), g.ncz);
+            if (sx < -1 || sx > 1 || sy < -1 || sy > 1 || sz < -1 || sz > 1) {
+              set_err(err, KERR_MOVE);
+              if (dirrank) dirrank[l] = DR_BAD;
+            } else {
+              grp = kl * NDIR + dir_index(sx, sy, sz);
+            }
+          }
+          ox = dox; oy = doy; oz = doz;  // the deposit uses the maind.f:408 position
+          if (out1) live = false;
         }
       }
-      if (!live) {
-        p.cell[l] = CELL_DEAD;
-      } else if (!inside) {
+      const bool inside = !(rx < -1 || rx > 4 || ry < -1 || ry > 4 || rz < -1 || rz > 4);
+      if (live && !inside) {
         set_err(err, KERR_MOVE);
         live = false;
-      } else {
-        if (moved) {
-          p.cell[l] = pk(ci, cj, ck);
-          p.ox[l] = ox; p.oy[l] = oy; p.oz[l] = oz;
-        }
+      }
+      if (live) {
         t0 = (rx + 1) + TN * ((ry + 1) + TN * (rz + 1));
         const float wxl = 1.0f - ox, wxu = ox, wyl = 1.0f - oy, wyu = oy, wzl = 1.0f - oz, wzu = oz;
 #pragma unroll
@@ -273,7 +307,7 @@ __global__ void __launch_bounds__(TPB_PASS) k_pass(G32 g, Part p, Species sp, St
     for (int q = 0; q < 4; ++q) {
       const float a = live ? qdv[q] : 0.0f;
 #pragma unroll
-      for (int c8 = 0; c8 < 8; ++c8) s_red[warp][8 * q + c8][lane] = w8[c8] * a;
+      for (int c8 = 0; c8 < 8; ++c8) s_red[warp][8 * q + c8][lane] = live ? w8[c8] * a : 0.0f;
     }
     __syncwarp();
     const int tprev = __shfl_up_sync(0xffffffffu, t0, 1);
@@ -303,6 +337,23 @@ __global__ void __launch_bounds__(TPB_PASS) k_pass(G32 g, Part p, Species sp, St
       }
     }
     __syncwarp();
+    if (PASS == 3 && dirrank) {
+      // stable ranks per (key, direction): the warps of the CTA take their
+      // turn in order, each adding its particles after the earlier ones
+      const unsigned peers = __match_any_sync(0xffffffffu, grp >= 0 ? grp : -1 - lane);
+      const unsigned lt = peers & ((1u << lane) - 1u);
+      for (int w = 0; w < TPB_PASS / 32; ++w) {
+        if (warp == w) {
+          const unsigned before = grp >= 0 ? s_rank[grp] : 0u;
+          __syncwarp();
+          if (grp >= 0) {
+            dirrank[l] = ((uint32_t)(grp % NDIR) << 26) | (before + __popc(lt));
+            if (lt == 0) s_rank[grp] = before + __popc(peers);
+          }
+        }
+        __syncthreads();
+      }
+    }
   }
   if (CHEX) {
     for (int o = 16; o > 0; o >>= 1) n_chex += __shfl_down_sync(0xffffffffu, n_chex, o);
@@ -311,6 +362,8 @@ __global__ void __launch_bounds__(TPB_PASS) k_pass(G32 g, Part p, Species sp, St
   __syncthreads();
   float* out = partial + b * (4 * TNODES);
   for (int t = threadIdx.x; t < 4 * TNODES; t += blockDim.x) out[t] = s_dep[t];
+  if (PASS == 3 && dep)
+    for (int t = threadIdx.x; t < BCELLS * NDIR; t += blockDim.x) dep[b * (BCELLS * NDIR) + t] = (uint16_t)s_rank[t];
 }
 
 // Sum, at every interior node, the brick tiles that cover it: along each axis
@@ -644,8 +697,6 @@ __global__ void k_courant(G32 g, const float* __restrict__ dbt, const float* __r
 // stable counting sort by cell key for particles that moved at most one cell
 // per axis since the last sort
 // ---------------------------------------------------------------------------
-
-__device__ __forceinline__ int dir_index(int dx, int dy, int dz) { return (dx + 1) + 3 * (dy + 1) + 9 * (dz + 1); }
 
 // One warp per old key K: direction of every particle of K and its rank
 // among the particles of K with the same direction, in array order.
@@ -1038,13 +1089,13 @@ __global__ void k_energy_f(G32 g, const double* __restrict__ b0, const float* __
   } while (0)
 
 cudaError_t pass(int which, const G32& g, const Part& p, const Species& sp, const StepParams& s, const int64_t* start,
-                 const float4* kit, float* partial, int* err, cudaStream_t st) {
+                 const float4* kit, float* partial, uint32_t* dirrank, uint16_t* dep, int* err, cudaStream_t st) {
   const unsigned grid = (unsigned)g.nbricks;
-  if (which == 1 && s.chex)
-    RET((k_pass<1, true><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, partial, err)));
-  if (which == 1) RET((k_pass<1><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, partial, err)));
-  if (which == 2) RET((k_pass<2><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, partial, err)));
-  RET((k_pass<3><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, partial, err)));
+  if (which == 1) RET((k_pass<1><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, partial, dirrank, dep, err)));
+  if (which == 2) RET((k_pass<2><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, partial, dirrank, dep, err)));
+  if (s.chex)
+    RET((k_pass<3, true><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, partial, dirrank, dep, err)));
+  RET((k_pass<3><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, partial, dirrank, dep, err)));
 }
 cudaError_t node_sum(const G32& g, const float* partial, int nq, float* np, float* S, cudaStream_t st) {
   RET((k_node_sum<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, partial, nq, np, S)));

@@ -48,16 +48,15 @@ struct Species {
 
 // Flags in the packed cell word.  A dead ion (outflow) is skipped by every
 // pass and dropped by the next sort; a fresh ion was created by a source for
-// the coming step, so P1 does not apply the previous step's final move to it.
+// the coming step (P1 clears the flag, or drops the ion at the end of a run).
 constexpr int32_t CELL_DEAD = -1;
 constexpr int32_t CELL_FRESH = 1 << 30;
 
 struct StepParams {
   float dt;
-  int pending_move;  // P1: apply the previous step's final half move first
   int x_open;        // x does not wrap; ions leaving in x are marked dead
   int drop_fresh;    // P1 at the end of a run: fresh ions are marked dead
-  int chex;          // P1: res_chex of the step the pending move completes
+  int chex;          // P3: res_chex after the step's last move
   long long chex_step;
   uint64_t seed;
   float cx_a, cx_b, cloud_N0, inv_r0sq, cloud_x, cloud_y, cloud_z;
@@ -114,13 +113,17 @@ __device__ __forceinline__ float offset_in_cell(double x, double q1, double d, i
 }
 
 // ---- particle passes ----
-// P1: [final half move of the previous step], deposit np and up at
-//     v_n = 1.5 v - 0.5 vp1 (maind.f:479, 385-387, 399).
+// Particles lie in their sorted key's cell at P1 and P2; every move happens
+// in P3, and the sort that follows restores the order.
+// P1: deposit np and up at v_n = 1.5 v - 0.5 vp1 (maind.f:385-387, 399).
 // P2: gather, Ep, v-/v+, deposit up at 0.5(v+ + v-) (maind.f:400-402).
 // P3: gather, Ep, v-/v+, vp1 = v, v = v+ + dt/2 Ep, half move, deposit np and
-//     up at v (maind.f:404-413).
+//     up there (maind.f:404-413), the second half move (maind.f:479),
+//     outflow and res_chex; writes each particle's sort direction and rank
+//     (dirrank) and the per-key direction counts (dep) when those are given.
 cudaError_t pass(int which, const G32& g, const Part& p, const Species& sp, const StepParams& sprm,
-                 const int64_t* start, const float4* kit, float* partial, int* err, cudaStream_t st);
+                 const int64_t* start, const float4* kit, float* partial, uint32_t* dirrank, uint16_t* dep, int* err,
+                 cudaStream_t st);
 // Sum the brick partial tiles into np and S (interior nodes, (nx,ny,nz) layout).
 cudaError_t node_sum(const G32& g, const float* partial, int nq, float* np, float* S, cudaStream_t st);
 

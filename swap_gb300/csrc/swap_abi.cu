@@ -464,6 +464,7 @@ extern "C" int swap_finalize(swap_ctx* c) {
   if (!c) return SWAP_EINVAL;
   if (c->st) cudaStreamSynchronize(c->st);
   swap_f32_free(c);
+  swap_diag_free(c);
   srcops::free_all(c);
   for (auto& kv : c->reg) cudaFree(kv.second.dev);
   for (void* p : c->owned) cudaFree(p);
@@ -985,6 +986,16 @@ extern "C" int swap_run(swap_ctx* c, int32_t nsteps) {
 // ---------------------------------------------------------------------------
 // diagnostics
 // ---------------------------------------------------------------------------
+
+int ops::energy7(swap_ctx* c, double out[7]) {
+  TRY(c->begin());
+  Bound b;
+  TRY(bound_inputs(c, b));
+  CU(energy_parts(c->g, c->part_view(), c->ntot(), c->prm.beta, c->prm.alpha, b.vp, b.b0, b.b1, b.E, c->s_red,
+                  c->st));
+  CU(cudaMemcpyAsync(out, c->s_red, 7 * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  return c->finish();
+}
 
 extern "C" int swap_energy(swap_ctx* c, double out[4]) {
   ENTRY;

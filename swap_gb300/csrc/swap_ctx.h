@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstddef>
+#include <cstdio>
 #include <cstdint>
 #include <string>
 #include <unordered_map>
@@ -68,6 +69,7 @@ struct swap_ctx {
   double last_dtsub = 0, last_ntf = 0;
   double mion = 1.0;  // ion mass of update_rho / get_temperature (normalized units: 1)
   void* f32_state = nullptr;  // the FP32 form (swap_f32.cu)
+  void* diag_state = nullptr; // diagnostic output files (swap_diag.cu)
 
   // particle sources and sinks (swap_sources.cu)
   swap_sources srcs{};
@@ -101,3 +103,7 @@ struct swap_ctx {
 };
 
 void swap_f32_free(swap_ctx* c);
+bool swap_f32_ended(swap_ctx* c);  // the FP32 state was written back by swap_f32_end
+void swap_diag_free(swap_ctx* c);
+// The FP32 state to or from an open checkpoint file (swap_f32.cu).
+int swap_f32_checkpoint(swap_ctx* c, std::FILE* f, bool write);

@@ -9,6 +9,7 @@
 // (float hi + lo pairs, 48 significant bits).
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -45,7 +46,6 @@ struct F32State {
   float* dtn = nullptr;  // per-node Courant time
   float* d_min = nullptr;
   double* acc = nullptr;
-  bool pending_move = false;
   double last_dtsub = 0, last_ntf = 0;
   std::vector<void*> owned;
   // species tables (FP64, device) and the particle sources and sinks
@@ -68,6 +68,8 @@ struct F32State {
 };
 
 static F32State* f32(swap_ctx* c) { return static_cast<F32State*>(c->f32_state); }
+
+bool swap_f32_ended(swap_ctx* c) { return !f32(c) || f32(c)->ended; }
 
 void swap_f32_free(swap_ctx* c) {
   delete f32(c);
@@ -106,7 +108,7 @@ static int check_err(swap_ctx* c) {
   return SWAP_OK;
 }
 
-static int sort_step(swap_ctx* c, F32State* s, long long src_step);
+static int sort_step(swap_ctx* c, F32State* s, long long src_step, bool prepared = false);
 
 // ---------------------------------------------------------------------------
 
@@ -318,7 +320,6 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
     if (e != cudaSuccess) return c->cuda_fail(e, "initial sort");
   }
   s->cur = 0;
-  s->pending_move = false;
   TRY(check_err(c));
   if (s->src_on) TRY(sort_step(c, s, c->src_step));  // the sources of the first step
   return check_err(c);
@@ -381,8 +382,9 @@ static int subcycles(swap_ctx* c, F32State* s) {
 // The stable incremental counting sort after each step (particles moved at
 // most one cell per axis since the last sort).  Removed ions are dropped;
 // with src_step >= 0 the new ions of that step's sources are placed after the
-// arrivals of their cell, flagged fresh.
-static int sort_step(swap_ctx* c, F32State* s, long long src_step) {
+// arrivals of their cell, flagged fresh.  prepared: pass 3 already wrote the
+// directions, ranks and per-key counts.
+static int sort_step(swap_ctx* c, F32State* s, long long src_step, bool prepared) {
   const G32& g = s->g;
   Part& a = s->buf[s->cur];
   Part& b = s->buf[1 - s->cur];
@@ -391,7 +393,7 @@ static int sort_step(swap_ctx* c, F32State* s, long long src_step) {
   if (src_step >= 0 && s->src_on) TRY(srcops::f32_stage(c, g, s->stage, src_step, &n_host, &n_dev, &n_max));
   const bool staged = n_max > 0;
   const long long cap = c->dims.ni_max;
-  KL("f32_sort_prep", sort_prep(g, s->start, a.cell, s->dirrank, s->dep, c->d_err, c->st));
+  if (!prepared) KL("f32_sort_prep", sort_prep(g, s->start, a.cell, s->dirrank, s->dep, c->d_err, c->st));
   KL("f32_sort_count", sort_count(g, s->dep, staged ? s->stage.ncount : nullptr, s->order, s->count, s->pre,
                                   c->d_err, c->st));
   KL("f32_sort_scan", scan_exclusive(s->count, s->start_new, g.nkeys, s->sums, c->st));
@@ -412,16 +414,15 @@ static int sort_step(swap_ctx* c, F32State* s, long long src_step) {
 }
 
 // Step parameters of the particle passes, with the sources and sinks that
-// act inside them (open-x outflow, res_chex of the completed step).
-static StepParams step_params(swap_ctx* c, F32State* s, bool pending, bool drop_fresh) {
+// act inside them (open-x outflow, res_chex at the end of the step).
+static StepParams step_params(swap_ctx* c, F32State* s, bool drop_fresh) {
   StepParams p{};
   p.dt = (float)c->prm.dt;
-  p.pending_move = pending ? 1 : 0;
   p.x_open = s->x_open ? 1 : 0;
   p.drop_fresh = drop_fresh ? 1 : 0;
   const swap_sources& q = c->srcs;
-  p.chex = (s->src_on && q.cx_a > 0 && pending) ? 1 : 0;
-  p.chex_step = c->src_step - 1;  // the step the pending move completes
+  p.chex = (s->src_on && q.cx_a > 0) ? 1 : 0;
+  p.chex_step = c->src_step;  // the ion step being taken
   p.seed = q.seed;
   p.cx_a = (float)q.cx_a;
   p.cx_b = (float)q.cx_b;
@@ -437,20 +438,20 @@ static StepParams step_params(swap_ctx* c, F32State* s, bool pending, bool drop_
 
 static int one_step(swap_ctx* c, F32State* s) {
   const G32& g = s->g;
-  const StepParams sp = step_params(c, s, s->pending_move, false);
+  const StepParams sp = step_params(c, s, false);
   const Part& p = s->buf[s->cur];
-  KL("f32_P1", pass(1, g, p, s->sp, sp, s->start, s->kit, s->partial, c->d_err, c->st));  // :479,385-387,399
+  KL("f32_P1", pass(1, g, p, s->sp, sp, s->start, s->kit, s->partial, nullptr, nullptr, c->d_err, c->st));  // :385-387,399
   TRY(finish_deposit(c, s, 4));
   KL("f32_curlB", curlB32(g, s->db1, s->np, (float)c->prm.alpha, s->aj, c->st));  // :395
   KL("f32_kit", build_kit(g, s->aj, s->up, s->db1, s->b0c, s->kit, c->st));       // :398, get_Ep :183-184
-  KL("f32_P2", pass(2, g, p, s->sp, sp, s->start, s->kit, s->partial, c->d_err, c->st));  // :400-402
+  KL("f32_P2", pass(2, g, p, s->sp, sp, s->start, s->kit, s->partial, nullptr, nullptr, c->d_err, c->st));  // :400-402
   TRY(finish_deposit(c, s, 3));
   KL("f32_kit", build_kit(g, s->aj, s->up, s->db1, s->b0c, s->kit, c->st));       // :404
-  KL("f32_P3", pass(3, g, p, s->sp, sp, s->start, s->kit, s->partial, c->d_err, c->st));  // :404-413
+  // :404-413, the final half move of :479 and res_chex; prepares the sort
+  KL("f32_P3", pass(3, g, p, s->sp, sp, s->start, s->kit, s->partial, s->dirrank, s->dep, c->d_err, c->st));
   TRY(finish_deposit(c, s, 4));
   TRY(subcycles(c, s));                                                            // :420-476
-  TRY(sort_step(c, s, c->src_step + 1));  // with the sources of the next step
-  s->pending_move = true;                                                          // :479 next P1
+  TRY(sort_step(c, s, c->src_step + 1, true));  // with the sources of the next step
   if (c->have_srcs) c->src_step++;
   return SWAP_OK;
 }
@@ -464,15 +465,14 @@ extern "C" int swap_f32_run(swap_ctx* c, int32_t nsteps) {
   return check_err(c);
 }
 
-// Apply a pending final half move (maind.f:479) in place, with the outflow
-// and res_chex that follow it; ions created for a step not taken are dropped.
-static int flush_move(swap_ctx* c, F32State* s) {
-  if (!s->pending_move && !s->src_on) return SWAP_OK;
-  const StepParams sp = step_params(c, s, s->pending_move, true);
-  KL("f32_P1", pass(1, s->g, s->buf[s->cur], s->sp, sp, s->start, s->kit, s->partial, c->d_err, c->st));
-  s->pending_move = false;
-  if (s->src_on) TRY(sort_step(c, s, -1));
-  return SWAP_OK;
+// Drop the ions created for a step that is not taken (the sources of the
+// next step, inserted by the last sort).
+static int drop_fresh(swap_ctx* c, F32State* s) {
+  if (!s->src_on) return SWAP_OK;
+  const StepParams sp = step_params(c, s, true);
+  KL("f32_P1", pass(1, s->g, s->buf[s->cur], s->sp, sp, s->start, s->kit, s->partial, nullptr, nullptr, c->d_err,
+                    c->st));
+  return sort_step(c, s, -1);
 }
 
 extern "C" int swap_f32_end(swap_ctx* c) {
@@ -480,7 +480,7 @@ extern "C" int swap_f32_end(swap_ctx* c) {
   F32State* s = f32(c);
   if (!s) return c->fail(SWAP_EINVAL, "swap_f32_begin has not been called");
   TRY(c->begin());
-  TRY(flush_move(c, s));
+  TRY(drop_fresh(c, s));
   double *xp, *vp, *vp1, *b1, *b12, *b1p2, *bt, *npd, *upd, *Ed, *ajd;
   TRY(c->use(c->h_xp, Access::Out, &xp));
   TRY(c->use(c->h_vp, Access::Out, &vp));
@@ -573,4 +573,76 @@ extern "C" int swap_f32_displace_resort(swap_ctx* c, int64_t n, const int64_t* i
   }
   TRY(sort_step(c, s, -1));
   return check_err(c);
+}
+
+// ---------------------------------------------------------------------------
+// checkpoint of the FP32 state: everything a step reads from the previous one
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct DevBlock {
+  const char* name;
+  void* dev;
+  std::size_t bytes;
+};
+
+std::vector<DevBlock> f32_blocks(F32State* s) {
+  const std::size_t N = (std::size_t)s->N, C = (std::size_t)s->g.C, nk = (std::size_t)s->g.nkeys;
+  Part& p = s->buf[s->cur];
+  return {{"cell", p.cell, N * 4},          {"ox", p.ox, N * 4},         {"oy", p.oy, N * 4},
+          {"oz", p.oz, N * 4},              {"vx", p.vx, N * 4},         {"vy", p.vy, N * 4},
+          {"vz", p.vz, N * 4},              {"wx", p.wx, N * 4},         {"wy", p.wy, N * 4},
+          {"wz", p.wz, N * 4},              {"sp", p.sp, N},             {"start", s->start, (nk + 1) * 8},
+          {"b1h", s->b1.h, 3 * C * 4},      {"b1l", s->b1.l, 3 * C * 4}, {"b12h", s->b12.h, 3 * C * 4},
+          {"b12l", s->b12.l, 3 * C * 4},    {"db1", s->db1, 3 * C * 4},  {"np", s->np, C * 4},
+          {"up", s->up, 3 * C * 4},         {"aj", s->aj, 3 * C * 4},    {"E", s->E, 3 * C * 4},
+          {"tabm", s->tabm, MAX_SPECIES * 8}, {"tabb", s->tabb, MAX_SPECIES * 8}};
+}
+
+}  // namespace
+
+int swap_f32_checkpoint(swap_ctx* c, std::FILE* f, bool write) {
+  F32State* s = f32(c);
+  if (!s) return c->fail(SWAP_EINVAL, "no FP32 state");
+  struct Meta {
+    int64_t N;
+    Species sp;
+    uint8_t heavy_of[MAX_SPECIES];
+    uint8_t sp_ion, sp_cloud, sp_inflow, pad;
+  } m{};
+  if (write) {
+    m.N = s->N;
+    m.sp = s->sp;
+    std::memcpy(m.heavy_of, s->heavy_of, sizeof(m.heavy_of));
+    m.sp_ion = s->stage.sp_ion;
+    m.sp_cloud = s->stage.sp_cloud;
+    m.sp_inflow = s->stage.sp_inflow;
+    if (std::fwrite(&m, sizeof(m), 1, f) != 1) return c->fail(SWAP_EINVAL, "checkpoint write failed");
+  } else {
+    if (std::fread(&m, sizeof(m), 1, f) != 1) return c->fail(SWAP_EINVAL, "checkpoint read failed");
+    if (m.N < 0 || m.N > c->dims.ni_max) return c->fail(SWAP_ECAPACITY, "checkpoint holds more ions than Ni_max");
+    s->N = m.N;
+    s->sp = m.sp;
+    std::memcpy(s->heavy_of, m.heavy_of, sizeof(m.heavy_of));
+    s->stage.sp_ion = m.sp_ion;
+    s->stage.sp_cloud = m.sp_cloud;
+    s->stage.sp_inflow = m.sp_inflow;
+  }
+  CU(cudaStreamSynchronize(c->st));
+  std::vector<char> buf;
+  for (const DevBlock& bl : f32_blocks(s)) {
+    buf.resize(bl.bytes);
+    if (write) {
+      if (bl.bytes) CU(cudaMemcpy(buf.data(), bl.dev, bl.bytes, cudaMemcpyDeviceToHost));
+      if (bl.bytes && std::fwrite(buf.data(), 1, bl.bytes, f) != bl.bytes)
+        return c->fail(SWAP_EINVAL, std::string("checkpoint write failed at ") + bl.name);
+    } else {
+      if (bl.bytes && std::fread(buf.data(), 1, bl.bytes, f) != bl.bytes)
+        return c->fail(SWAP_EINVAL, std::string("checkpoint read failed at ") + bl.name);
+      if (bl.bytes) CU(cudaMemcpy(bl.dev, buf.data(), bl.bytes, cudaMemcpyHostToDevice));
+    }
+  }
+  if (!write) s->ended = false;
+  return SWAP_OK;
 }

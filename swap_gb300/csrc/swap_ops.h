@@ -12,6 +12,9 @@ int update_np(swap_ctx* c, double* np);
 int update_up_mode(swap_ctx* c, int mode, const double* va, const double* vb, double* out_v1, const double* np,
                    double* up);
 int update_rho(swap_ctx* c, double* mnp);
+// Energies of the bound FP64 state: kinetic, |b1-b0|^2, |b1|^2, |E|^2 and
+// the x, y, z parts of |b1-b0|^2 (normalized units, full 3D).
+int energy7(swap_ctx* c, double out[7]);
 int get_temperature(swap_ctx* c, const double* vp, const double* np, double* temp_p);
 }  // namespace ops
 

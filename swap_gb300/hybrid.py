@@ -306,6 +306,29 @@ class Hybrid:
     def check_finite(self):
         self._check(self.lib.swap_check_finite(self.ctx))
 
+    # ---- diagnostic output and checkpoints ----
+    def diag_open(self, out_dir: str, nt: int, nout: int, real_bytes: int = 4, rank: int = 0, **scalars):
+        """Open the reference's output files in out_dir (para.dat written now)."""
+        spec = abi.DiagSpec(nt, nout, real_bytes, rank)
+        spec.dtsub_init = self.cfg.dt / self.cfg.ntsub
+        spec.mion = 1.0
+        for k, v in scalars.items():
+            setattr(spec, k, v)
+        d = out_dir if out_dir.endswith("/") else out_dir + "/"
+        self._check(self.lib.swap_diag_open(self.ctx, d.encode(), C.byref(spec)))
+
+    def diag_step(self, m: int):
+        self._check(self.lib.swap_diag_step(self.ctx, int(m)))
+
+    def diag_close(self):
+        self._check(self.lib.swap_diag_close(self.ctx))
+
+    def checkpoint_write(self, path: str):
+        self._check(self.lib.swap_checkpoint_write(self.ctx, str(path).encode()))
+
+    def checkpoint_read(self, path: str):
+        self._check(self.lib.swap_checkpoint_read(self.ctx, str(path).encode()))
+
     # ---- the FP32 form ----
     def f32_begin(self):
         """Convert the bound FP64 state into the FP32 form (particles sorted by cell)."""

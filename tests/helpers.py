@@ -102,3 +102,21 @@ def small(**kw):
     base = dict(name="kat", cells=(8, 6, 6), ppc=4, seed=7)
     base.update(kw)
     return RunConfig(**base)
+
+
+def fortran_records(path):
+    """The records of a Fortran sequential unformatted file (4-byte markers)."""
+    import struct
+
+    out = []
+    with open(path, "rb") as f:
+        data = f.read()
+    o = 0
+    while o < len(data):
+        (n,) = struct.unpack_from("<i", data, o)
+        rec = data[o + 4:o + 4 + n]
+        (n2,) = struct.unpack_from("<i", data, o + 4 + n)
+        assert n == n2, (path, o, n, n2)
+        out.append(rec)
+        o += 8 + n
+    return out
