@@ -295,6 +295,14 @@ int swap_update_up_noalloc(const swap_dims* dims, const swap_params* params, con
                            const double* xp, const double* vp, const double* beta_p, int64_t ni_tot,
                            const double* np, double* up, void* stream);
 
+/* ---- tensor-core check (no counterpart in the reference) ----
+ * D = A * B^T on the 5th-generation tensor cores (tcgen05, BF16 in, FP32
+ * accumulate) for device arrays A (128 x K bf16, row-major), B (32 x K bf16,
+ * row-major) and D (128 x 32 FP32); K a multiple of 16 up to 256.  The GEMM
+ * core of the surrogate's convolutions, exposed so its operand layout can be
+ * checked against a CPU product. */
+int swap_tc_gemm_check(const void* A, const void* B, float* D, int32_t K);
+
 /* ---- timing (CUDA events on the context's stream) ---- */
 int swap_timer_start(swap_ctx* ctx);
 int swap_timer_stop(swap_ctx* ctx, double* ms);

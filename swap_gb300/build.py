@@ -35,6 +35,7 @@ UNITS = [
     ("swap_sources.cu", ["--fmad=false", "-Xcompiler", "-ffp-contract=off"]),
     ("loader.cpp", ["-Xcompiler", "-fopenmp,-ffp-contract=off"]),
     ("swap_diag.cu", []),
+    ("surrogate.cu", []),
 ]
 
 

@@ -32,7 +32,19 @@ module swap_gpu_iface
      type(c_ptr) :: dx_cell, dy_cell, dz_cell, xrat, yrat, zrat
   end type swap_coords_t
 
+  type, bind(C) :: swap_sources_t
+     integer(c_int64_t) :: seed
+     real(c_double) :: ndot, vsw, beta_pu, mrat_pu, delz_ref
+     integer(c_int32_t) :: x_open, inflow_ppc
+     real(c_double) :: inflow_vth, inflow_ux, inflow_uy, inflow_uz
+     real(c_double) :: cloud_N0, cloud_r0, cloud_x, cloud_y, cloud_z, nu_ion, mrat_heavy, beta_heavy
+     real(c_double) :: cx_a, cx_b
+  end type swap_sources_t
+
   type(c_ptr), save :: swap_gpu_ctx = c_null_ptr
+  ! The ion step number for the random draws of res_chex, whose reference
+  ! argument list has none: set it to the main loop's m before the call.
+  integer(c_int32_t), save :: swap_step = 0
 
   interface
      integer(c_int) function swap_init(ctx, dims, params, coords) bind(C, name="swap_init")
@@ -176,6 +188,52 @@ module swap_gpu_iface
        type(c_ptr), value :: ctx
        real(c_double) :: b(*)
      end function c_periodic_scalar
+     integer(c_int) function swap_set_sources(ctx, src, step0) bind(C, name="swap_set_sources")
+       import :: c_int, c_ptr, c_int64_t, swap_sources_t
+       type(c_ptr), value :: ctx
+       type(swap_sources_t) :: src
+       integer(c_int64_t), value :: step0
+     end function swap_set_sources
+     integer(c_int) function c_Ionize_sw_mp(ctx, np, vp, vp1, xp, m_tstep, input_p, up) &
+          bind(C, name="swap_Ionize_sw_mp")
+       import :: c_int, c_ptr, c_double, c_int32_t
+       type(c_ptr), value :: ctx
+       real(c_double) :: np(*), vp(*), vp1(*), xp(*), input_p(*), up(*)
+       integer(c_int32_t), value :: m_tstep
+     end function c_Ionize_sw_mp
+     integer(c_int) function c_remove_ion(ctx, xp, vp, vp1, ion_l) bind(C, name="swap_remove_ion")
+       import :: c_int, c_ptr, c_double, c_int32_t
+       type(c_ptr), value :: ctx
+       real(c_double) :: xp(*), vp(*), vp1(*)
+       integer(c_int32_t), value :: ion_l
+     end function c_remove_ion
+     integer(c_int) function c_res_chex(ctx, xp, vp, m_tstep, count) bind(C, name="swap_res_chex")
+       import :: c_int, c_ptr, c_double, c_int32_t, c_int64_t
+       type(c_ptr), value :: ctx
+       real(c_double) :: xp(*), vp(*)
+       integer(c_int32_t), value :: m_tstep
+       integer(c_int64_t) :: count
+     end function c_res_chex
+     integer(c_int) function c_update_rho(ctx, mnp) bind(C, name="swap_update_rho")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: mnp(*)
+     end function c_update_rho
+     integer(c_int) function c_get_temperature(ctx, xp, vp, np, temp_p) bind(C, name="swap_get_temperature")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: xp(*), vp(*), np(*), temp_p(*)
+     end function c_get_temperature
+     integer(c_int) function swap_checkpoint_write(ctx, path) bind(C, name="swap_checkpoint_write")
+       import :: c_int, c_ptr, c_char
+       type(c_ptr), value :: ctx
+       character(kind=c_char) :: path(*)
+     end function swap_checkpoint_write
+     integer(c_int) function swap_checkpoint_read(ctx, path) bind(C, name="swap_checkpoint_read")
+       import :: c_int, c_ptr, c_char
+       type(c_ptr), value :: ctx
+       character(kind=c_char) :: path(*)
+     end function swap_checkpoint_read
   end interface
 
 contains
@@ -203,8 +261,8 @@ end module swap_gpu_iface
 
 ! Wrappers with the reference names.  The makefile links this module's
 ! object in place of the bodies of the same subroutines in gutsp.f,
-! gutsf.f, grid_interp.f and boundary.f (INTEGRATION.md); maind.f is
-! unchanged.  Implicit state (dt, dtsub, ijkp, wght) is held by the context.
+! gutsf.f, grid_interp.f, boundary.f and, for the sources, chem_rates.f;
+! maind.f is unchanged.  Implicit state (dt, dtsub, ijkp, wght) is held by the context.
 module swap_gpu_calls
   use iso_c_binding
   use swap_gpu_iface
@@ -287,4 +345,28 @@ contains
     real(c_double) :: b(*)
     call swap_check(c_periodic_scalar(swap_gpu_ctx, b), 'periodic_scalar')
   end subroutine periodic_scalar
+  subroutine Ionize_sw_mp(np, vp, vp1, xp, m_tstep, input_p, up)
+    real(c_double) :: np(*), vp(*), vp1(*), xp(*), input_p(*), up(*)
+    integer :: m_tstep
+    call swap_check(c_Ionize_sw_mp(swap_gpu_ctx, np, vp, vp1, xp, int(m_tstep, c_int32_t), input_p, up), &
+                    'Ionize_sw_mp')
+  end subroutine Ionize_sw_mp
+  subroutine remove_ion(xp, vp, vp1, ion_l)
+    real(c_double) :: xp(*), vp(*), vp1(*)
+    integer :: ion_l
+    call swap_check(c_remove_ion(swap_gpu_ctx, xp, vp, vp1, int(ion_l, c_int32_t)), 'remove_ion')
+  end subroutine remove_ion
+  subroutine res_chex(xp, vp)
+    real(c_double) :: xp(*), vp(*)
+    integer(c_int64_t) :: n
+    call swap_check(c_res_chex(swap_gpu_ctx, xp, vp, swap_step, n), 'res_chex')
+  end subroutine res_chex
+  subroutine update_rho(mnp)
+    real(c_double) :: mnp(*)
+    call swap_check(c_update_rho(swap_gpu_ctx, mnp), 'update_rho')
+  end subroutine update_rho
+  subroutine get_temperature(xp, vp, np, temp_p)
+    real(c_double) :: xp(*), vp(*), np(*), temp_p(*)
+    call swap_check(c_get_temperature(swap_gpu_ctx, xp, vp, np, temp_p), 'get_temperature')
+  end subroutine get_temperature
 end module swap_gpu_calls
