@@ -302,6 +302,14 @@ int swap_update_up_noalloc(const swap_dims* dims, const swap_params* params, con
  * core of the surrogate's convolutions, exposed so its operand layout can be
  * checked against a CPU product. */
 int swap_tc_gemm_check(const void* A, const void* B, float* D, int32_t K);
+/* One periodic 3x3x3 convolution layer of the surrogate on the tensor cores:
+ * device arrays X [V][cin] bf16 (V = nx*ny*nz voxels, x fastest, a multiple
+ * of 128), W [27][cout][cin] bf16 with tap = (dz+1)*9 + (dy+1)*3 + (dx+1),
+ * bias [cout] FP32 or NULL; writes Y [V][cout] bf16 (GELU applied when gelu
+ * is nonzero) and/or Yf [V][cout] FP32 (before the activation).
+ * (cin, cout) in {(16,32), (32,32), (32,16), (16,16)}. */
+int swap_conv3_check(int32_t nx, int32_t ny, int32_t nz, int32_t cin, int32_t cout, const void* X, const void* W,
+                     const float* bias, void* Y, float* Yf, int32_t gelu);
 
 /* ---- timing (CUDA events on the context's stream) ---- */
 int swap_timer_start(swap_ctx* ctx);

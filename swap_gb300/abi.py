@@ -168,6 +168,7 @@ SIGNATURES: dict[str, tuple] = {
     "swap_update_up_noalloc": (C.c_int, [C.POINTER(Dims), C.POINTER(Params), C.POINTER(Coords)]
                                + [P] * 3 + [C.c_int64, P, P, P]),
     "swap_tc_gemm_check": (C.c_int, [P, P, P, C.c_int32]),
+    "swap_conv3_check": (C.c_int, [C.c_int32] * 5 + [P, P, P, P, P, C.c_int32]),
     "swap_timer_start": (C.c_int, [P]),
     "swap_timer_stop": (C.c_int, [P, c_double_p]),
     "swap_profile_enable": (C.c_int, [P, C.c_int]),
