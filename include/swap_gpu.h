@@ -311,6 +311,44 @@ int swap_tc_gemm_check(const void* A, const void* B, float* D, int32_t K);
 int swap_conv3_check(int32_t nx, int32_t ny, int32_t nz, int32_t cin, int32_t cout, const void* X, const void* W,
                      const float* bias, void* Y, float* Yf, int32_t gelu);
 
+/* ---- the learned field-subcycle surrogate (FP32 form) ----
+ * A 3D convolutional network (4 periodic 3x3x3 layers, 8 -> 32 -> 32 -> 32
+ * -> 3 channels, GELU; BF16 weights and activations, FP32 accumulation on
+ * the tensor cores) maps the state at the start of the field subcycles (B,
+ * u_p, n_p, p_e = n_p per node) to the step's mean corrector E; B then
+ * advances as B - dt curl E, so div B stays where it was.  It is trained on
+ * pairs the plain subcycles of swap_surrogate_collect produce, with Adam.
+ * Attached to a context, it replaces the subcycles; every judge_every-th
+ * step both run, the plain result is kept, and a B rel-L2 difference above
+ * bound switches the network off until a judged step passes. */
+typedef struct swap_surrogate swap_surrogate;
+int swap_surrogate_create(swap_surrogate** net, uint64_t seed, int32_t max_samples);
+int swap_surrogate_destroy(swap_surrogate* net);
+const char* swap_surrogate_last_error(const swap_surrogate* net);
+/* nsteps FP32 steps of ctx (after swap_f32_begin) with the plain subcycles,
+ * each adding one training pair. */
+int swap_surrogate_collect(swap_surrogate* net, swap_ctx* ctx, int32_t nsteps);
+int swap_surrogate_samples(swap_surrogate* net, int32_t* n);
+/* epochs of Adam over the pairs; loss = mean squared normalised E error of
+ * the last epoch. */
+int swap_surrogate_train(swap_surrogate* net, int32_t epochs, double lr, double* loss);
+int swap_surrogate_loss(swap_surrogate* net, double* loss);
+int swap_surrogate_attach(swap_ctx* ctx, swap_surrogate* net, int32_t judge_every, double bound);
+/* [0] steps by the network, [1] judged steps, [2] fallbacks, [3] last judged
+ * B rel-L2, [4] last judged (B - b0) rel-L2. */
+int swap_surrogate_stats(swap_ctx* ctx, double out[5]);
+/* Test access: normalisation (8 input means and stds, output scale) and
+ * FP32 master weights of a layer ([27][cout][cin] with (cin, cout) = (16,32),
+ * (32,32), (32,32), (32,16): padded channels zero) with its bias; get or set. */
+int swap_surrogate_norm(swap_surrogate* net, float* mean, float* stdv, float* out_mean, float* out_std,
+                        int32_t set);
+int swap_surrogate_weights(swap_surrogate* net, int32_t layer, float* w, float* b, int32_t set);
+/* One forward and backward pass on device inputs [V][8] and targets [V][3]
+ * of an nx*ny*nz box: loss = 0.5 mean((out - (tgt - out_mean)/out_std)^2), gradients of
+ * every layer into grads as (gW0, gb0, gW1, gb1, gW2, gb2, gW3, gb3). */
+int swap_surrogate_grads(swap_surrogate* net, int32_t nx, int32_t ny, int32_t nz, const float* vin, const float* tgt,
+                         double* loss, float* grads);
+
 /* ---- timing (CUDA events on the context's stream) ---- */
 int swap_timer_start(swap_ctx* ctx);
 int swap_timer_stop(swap_ctx* ctx, double* ms);

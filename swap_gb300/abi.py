@@ -169,6 +169,18 @@ SIGNATURES: dict[str, tuple] = {
                                + [P] * 3 + [C.c_int64, P, P, P]),
     "swap_tc_gemm_check": (C.c_int, [P, P, P, C.c_int32]),
     "swap_conv3_check": (C.c_int, [C.c_int32] * 5 + [P, P, P, P, P, C.c_int32]),
+    "swap_surrogate_create": (C.c_int, [C.POINTER(P), C.c_uint64, C.c_int32]),
+    "swap_surrogate_destroy": (C.c_int, [P]),
+    "swap_surrogate_last_error": (C.c_char_p, [P]),
+    "swap_surrogate_collect": (C.c_int, [P, P, C.c_int32]),
+    "swap_surrogate_samples": (C.c_int, [P, C.POINTER(C.c_int32)]),
+    "swap_surrogate_train": (C.c_int, [P, C.c_int32, C.c_double, c_double_p]),
+    "swap_surrogate_loss": (C.c_int, [P, c_double_p]),
+    "swap_surrogate_attach": (C.c_int, [P, P, C.c_int32, C.c_double]),
+    "swap_surrogate_stats": (C.c_int, [P, c_double_p]),
+    "swap_surrogate_norm": (C.c_int, [P, P, P, P, P, C.c_int32]),
+    "swap_surrogate_weights": (C.c_int, [P, C.c_int32, P, P, C.c_int32]),
+    "swap_surrogate_grads": (C.c_int, [P] + [C.c_int32] * 3 + [P, P, c_double_p, P]),
     "swap_timer_start": (C.c_int, [P]),
     "swap_timer_stop": (C.c_int, [P, c_double_p]),
     "swap_profile_enable": (C.c_int, [P, C.c_int]),

@@ -60,7 +60,7 @@ __device__ __forceinline__ void interior_of(const G32& g, long long t, int& i, i
   k = (int)(r / g.ncy) + 2;
 }
 
-__device__ __forceinline__ long long n_int(const G32& g) { return (long long)g.ncx * g.ncy * g.ncz; }
+__host__ __device__ __forceinline__ long long n_int(const G32& g) { return (long long)g.ncx * g.ncy * g.ncz; }
 
 // Move one axis of a (cell, offset) position by d cells.  upper_closed:
 // offsets in (0,1] (the '>' cell search of x and z, gutsp.f:1396-1412);
@@ -630,7 +630,8 @@ __global__ void __launch_bounds__(FBX * FBY) k_bstep(G32 g, const float* __restr
                                                      float ch, float cl, const float* __restrict__ b0c,
                                                      float* __restrict__ oh, float* __restrict__ ol,
                                                      float* __restrict__ dbo, const float* __restrict__ db1,
-                                                     float* __restrict__ dbtp1, float* __restrict__ E) {
+                                                     float* __restrict__ dbtp1, float* __restrict__ E,
+                                                     float* __restrict__ e_acc) {
   FIELD_NODE(i, j, k);
   const long long C = g.C, o = nid(g, i, j, k);
   const float e1 = e_comp<0>(g, ct, nu, aj, i, j, k);
@@ -656,6 +657,127 @@ __global__ void __launch_bounds__(FBX * FBY) k_bstep(G32 g, const float* __restr
     store_img(g, E, i, j, k, e1);
     store_img(g, E + C, i, j, k, e2);
     store_img(g, E + 2 * C, i, j, k, e3);
+  }
+  if (e_acc) {  // the sum of the correctors' E over a step: the surrogate's target
+    e_acc[o] += e1;
+    e_acc[o + C] += e2;
+    e_acc[o + 2 * C] += e3;
+  }
+}
+
+// B_new = base - coef * curl E for a given E (with ghost images), in
+// double-float, with its FP32 dB: the field advance of the surrogate, whose
+// discrete curl keeps div B where it was.
+__global__ void __launch_bounds__(FBX * FBY) k_bstep_given_e(G32 g, const float* __restrict__ E,
+                                                             const float* __restrict__ bh,
+                                                             const float* __restrict__ bl, float ch, float cl,
+                                                             const float* __restrict__ b0c, float* __restrict__ oh,
+                                                             float* __restrict__ ol, float* __restrict__ dbo) {
+  FIELD_NODE(i, j, k);
+  const long long C = g.C, o = nid(g, i, j, k), sx = 1, sy = g.nx, sz = (long long)g.nx * g.ny;
+  const float* E1 = E;
+  const float* E2 = E + C;
+  const float* E3 = E + 2 * C;
+  const float ce[3] = {(E3[o + sy] - E3[o]) * g.inv_dy + (E2[o] - E2[o + sz]) * g.inv_dz,
+                       (E3[o] - E3[o + sx]) * g.inv_dx + (E1[o + sz] - E1[o]) * g.inv_dz,
+                       (E1[o] - E1[o + sy]) * g.inv_dy + (E2[o + sx] - E2[o]) * g.inv_dx};
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    float rh, rl;
+    df_sub_mul(bh[o + C * m], bl[o + C * m], ch, cl, ce[m], rh, rl);
+    store_img(g, oh + C * m, i, j, k, rh);
+    store_img(g, ol + C * m, i, j, k, rl);
+    store_img(g, dbo + C * m, i, j, k, __fadd_rn(__fsub_rn(rh, b0c[m]), rl));
+  }
+}
+
+// b_out = b_new + f * (b_old - b_new) on hi parts, lo of b_new kept: the B
+// one subcycle before the end of a surrogate step (the predictor's leapfrog
+// base of the next plain subcycle).
+__global__ void __launch_bounds__(FBX * FBY) k_df_lerp(G32 g, const float* __restrict__ nh,
+                                                       const float* __restrict__ nl, const float* __restrict__ oh,
+                                                       float f, float* __restrict__ rh, float* __restrict__ rl) {
+  FIELD_NODE(i, j, k);
+  const long long C = g.C, o = nid(g, i, j, k);
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    const float d = f * (oh[o + C * m] - nh[o + C * m]);
+    float s, e;
+    two_sum(nh[o + C * m], d, s, e);
+    e = __fadd_rn(e, nl[o + C * m]);
+    const float h = __fadd_rn(s, e);
+    store_img(g, rh + C * m, i, j, k, h);
+    store_img(g, rl + C * m, i, j, k, __fsub_rn(e, __fsub_rn(h, s)));
+  }
+}
+
+// The judge's sums over the interior: |B_a - B_b|^2, |B_b|^2, |B_b - b0|^2
+// (double-float levels a and b).
+__global__ void k_judge(G32 g, const float* __restrict__ ah, const float* __restrict__ al,
+                        const float* __restrict__ bh, const float* __restrict__ bl, const float* __restrict__ b0c,
+                        double* acc) {
+  double s0 = 0, s1 = 0, s2 = 0;
+  GSTRIDE(t, n_int(g)) {
+    int i, j, k;
+    interior_of(g, t, i, j, k);
+    const long long o = nid(g, i, j, k);
+    for (int m = 0; m < 3; ++m) {
+      const double a = (double)ah[o + g.C * m] + (double)al[o + g.C * m];
+      const double b = (double)bh[o + g.C * m] + (double)bl[o + g.C * m];
+      s0 += (a - b) * (a - b);
+      s1 += b * b;
+      s2 += (b - (double)b0c[m]) * (b - (double)b0c[m]);
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    s0 += __shfl_down_sync(0xffffffffu, s0, off);
+    s1 += __shfl_down_sync(0xffffffffu, s1, off);
+    s2 += __shfl_down_sync(0xffffffffu, s2, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(acc, s0);
+    atomicAdd(acc + 1, s1);
+    atomicAdd(acc + 2, s2);
+  }
+}
+
+// The surrogate's inputs at every interior node (voxel v = x + ncx*(y +
+// ncy*z)): B = dB + b0, u_p, n_p and p_e = te * n_p, FP32 [V][8].
+__global__ void k_grid_to_voxels(G32 g, const float* __restrict__ db, const float* __restrict__ b0c,
+                                 const float* __restrict__ up, const float* __restrict__ np, float te,
+                                 float* __restrict__ out) {
+  GSTRIDE(v, n_int(g)) {
+    int i, j, k;
+    interior_of(g, v, i, j, k);
+    const long long C = g.C, o = nid(g, i, j, k);
+    float* r = out + v * 8;
+    r[0] = db[o] + b0c[0];
+    r[1] = db[o + C] + b0c[1];
+    r[2] = db[o + 2 * C] + b0c[2];
+    r[3] = up[o];
+    r[4] = up[o + C];
+    r[5] = up[o + 2 * C];
+    r[6] = np[o];
+    r[7] = te * np[o];
+  }
+}
+
+// An E predicted per voxel ([V][3]) into the field layout with ghost images.
+__global__ void k_voxels_to_grid(G32 g, const float* __restrict__ ev, float* __restrict__ E) {
+  GSTRIDE(v, n_int(g)) {
+    int i, j, k;
+    interior_of(g, v, i, j, k);
+    for (int m = 0; m < 3; ++m) store_img(g, E + g.C * m, i, j, k, ev[v * 3 + m]);
+  }
+}
+
+// Grid E (interior) into [V][3] per voxel, times a factor.
+__global__ void k_grid_e_to_voxels(G32 g, const float* __restrict__ E, float f, float* __restrict__ ev) {
+  GSTRIDE(v, n_int(g)) {
+    int i, j, k;
+    interior_of(g, v, i, j, k);
+    const long long o = nid(g, i, j, k);
+    for (int m = 0; m < 3; ++m) ev[v * 3 + m] = f * E[o + g.C * m];
   }
 }
 
@@ -1121,16 +1243,47 @@ cudaError_t aj_ct(const G32& g, bool corr, const float* db, const float* np, con
 }
 cudaError_t b_step(const G32& g, bool pred, bool write_e, const float* ct, const float* nu, const float* aj,
                    const float* bh, const float* bl, double coef, const float* b0c, float* oh, float* ol, float* dbo,
-                   const float* db1, float* dbtp1, float* E, cudaStream_t st) {
+                   const float* db1, float* dbtp1, float* E, float* e_acc, cudaStream_t st) {
   const dim3 grid((g.ncx + FBX - 1) / FBX, (g.ncy + FBY - 1) / FBY, g.ncz), blk(FBX, FBY);
   const float ch = (float)coef, cl = (float)(coef - (double)ch);
   if (pred && write_e)
-    RET((k_bstep<true, true><<<grid, blk, 0, st>>>(g, ct, nu, aj, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E)));
+    RET((k_bstep<true, true><<<grid, blk, 0, st>>>(g, ct, nu, aj, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E,
+                                                   e_acc)));
   if (pred)
-    RET((k_bstep<true, false><<<grid, blk, 0, st>>>(g, ct, nu, aj, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E)));
+    RET((k_bstep<true, false><<<grid, blk, 0, st>>>(g, ct, nu, aj, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E,
+                                                    e_acc)));
   if (write_e)
-    RET((k_bstep<false, true><<<grid, blk, 0, st>>>(g, ct, nu, aj, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E)));
-  RET((k_bstep<false, false><<<grid, blk, 0, st>>>(g, ct, nu, aj, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E)));
+    RET((k_bstep<false, true><<<grid, blk, 0, st>>>(g, ct, nu, aj, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E,
+                                                    e_acc)));
+  RET((k_bstep<false, false><<<grid, blk, 0, st>>>(g, ct, nu, aj, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E,
+                                                   e_acc)));
+}
+cudaError_t b_step_given_e(const G32& g, const float* E, const float* bh, const float* bl, double coef,
+                           const float* b0c, float* oh, float* ol, float* dbo, cudaStream_t st) {
+  const dim3 grid((g.ncx + FBX - 1) / FBX, (g.ncy + FBY - 1) / FBY, g.ncz), blk(FBX, FBY);
+  const float ch = (float)coef, cl = (float)(coef - (double)ch);
+  RET((k_bstep_given_e<<<grid, blk, 0, st>>>(g, E, bh, bl, ch, cl, b0c, oh, ol, dbo)));
+}
+cudaError_t df_lerp(const G32& g, const float* nh, const float* nl, const float* oh, float f, float* rh, float* rl,
+                    cudaStream_t st) {
+  const dim3 grid((g.ncx + FBX - 1) / FBX, (g.ncy + FBY - 1) / FBY, g.ncz), blk(FBX, FBY);
+  RET((k_df_lerp<<<grid, blk, 0, st>>>(g, nh, nl, oh, f, rh, rl)));
+}
+cudaError_t grid_to_voxels(const G32& g, const float* db, const float* b0c, const float* up, const float* np,
+                           float te, float* out, cudaStream_t st) {
+  RET((k_grid_to_voxels<<<nblk(n_int(g)), TPB, 0, st>>>(g, db, b0c, up, np, te, out)));
+}
+cudaError_t judge_sums(const G32& g, const float* ah, const float* al, const float* bh, const float* bl,
+                       const float* b0c, double* acc3, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(acc3, 0, 3 * sizeof(double), st);
+  if (e != cudaSuccess) return e;
+  RET((k_judge<<<nblk(n_int(g)), TPB, 0, st>>>(g, ah, al, bh, bl, b0c, acc3)));
+}
+cudaError_t voxels_to_grid(const G32& g, const float* ev, float* E, cudaStream_t st) {
+  RET((k_voxels_to_grid<<<nblk(n_int(g)), TPB, 0, st>>>(g, ev, E)));
+}
+cudaError_t grid_e_to_voxels(const G32& g, const float* E, float f, float* ev, cudaStream_t st) {
+  RET((k_grid_e_to_voxels<<<nblk(n_int(g)), TPB, 0, st>>>(g, E, f, ev)));
 }
 cudaError_t split_df(long long n, const double* a, float* h, float* l, cudaStream_t st) {
   RET((k_split_df<<<nblk(n), TPB, 0, st>>>(n, a, h, l)));

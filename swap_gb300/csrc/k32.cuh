@@ -139,9 +139,25 @@ cudaError_t curlB32(const G32& g, const float* dbt, const float* np, float alpha
 // pairs) with its FP32 dB (and, predictor, dB at m+1/2 = (dB_new + dB1)/2).
 cudaError_t aj_ct(const G32& g, bool corr, const float* db, const float* np, const float* up, const float* b0c,
                   float alpha, float* aj, float* ct, cudaStream_t st);
+// e_acc (may be null): the step's E summed over the correctors.
 cudaError_t b_step(const G32& g, bool pred, bool write_e, const float* ct, const float* nu, const float* aj,
                    const float* bh, const float* bl, double coef, const float* b0c, float* oh, float* ol, float* dbo,
-                   const float* db1, float* dbtp1, float* E, cudaStream_t st);
+                   const float* db1, float* dbtp1, float* E, float* e_acc, cudaStream_t st);
+// The surrogate's field advance: B_new = base - coef * curl E for a given E.
+cudaError_t b_step_given_e(const G32& g, const float* E, const float* bh, const float* bl, double coef,
+                           const float* b0c, float* oh, float* ol, float* dbo, cudaStream_t st);
+// r = b_new + f*(b_old - b_new) (double-float, hi parts of b_old).
+cudaError_t df_lerp(const G32& g, const float* nh, const float* nl, const float* oh, float f, float* rh, float* rl,
+                    cudaStream_t st);
+// Surrogate inputs per interior node, FP32 [V][8]: B, u_p, n_p, te*n_p.
+cudaError_t grid_to_voxels(const G32& g, const float* db, const float* b0c, const float* up, const float* np,
+                           float te, float* out, cudaStream_t st);
+// Sums over the interior of |B_a - B_b|^2, |B_b|^2 and |B_b - b0|^2.
+cudaError_t judge_sums(const G32& g, const float* ah, const float* al, const float* bh, const float* bl,
+                       const float* b0c, double* acc3, cudaStream_t st);
+// [V][3] <-> the field layout (ghost images written).
+cudaError_t voxels_to_grid(const G32& g, const float* ev, float* E, cudaStream_t st);
+cudaError_t grid_e_to_voxels(const G32& g, const float* E, float f, float* ev, cudaStream_t st);
 // FP64 <-> double-float (hi + lo).
 cudaError_t split_df(long long n, const double* a, float* h, float* l, cudaStream_t st);
 cudaError_t join_df(long long n, const float* h, const float* l, double* a, cudaStream_t st);

@@ -5,8 +5,11 @@
 // This unit starts with the GEMM core that the convolutions are built on and
 // an entry that runs it on caller data, so its operand layouts can be checked
 // against a CPU product.
+#include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <string>
+#include <vector>
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -92,7 +95,17 @@ struct ConvArgs {
   int* err;
 };
 
-__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+// GELU in its tanh form (Hendrycks and Gimpel, 2016) on the hardware tanh:
+// 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))).
+__device__ __forceinline__ float tanh_hw(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+constexpr float GELU_K0 = 0.7978845608028654f, GELU_K1 = 0.044715f;
+__device__ __forceinline__ float gelu(float x) {
+  return 0.5f * x * (1.0f + tanh_hw(GELU_K0 * fmaf(GELU_K1 * x, x * x, x)));
+}
 
 template <int CIN, int COUT>
 __global__ void __launch_bounds__(128) k_conv3(ConvArgs a) {
@@ -177,7 +190,7 @@ __global__ void __launch_bounds__(128) k_conv3(ConvArgs a) {
     if (a.Z) {
 #pragma unroll
       for (int c = 0; c < COUT; c += 8) {
-        __nv_bfloat16 h[8];
+        alignas(16) __nv_bfloat16 h[8];
 #pragma unroll
         for (int e = 0; e < 8; ++e) h[e] = __float2bfloat16(acc[c + e]);
         *reinterpret_cast<uint4*>(a.Z + vo * COUT + c) = *reinterpret_cast<const uint4*>(h);
@@ -186,7 +199,7 @@ __global__ void __launch_bounds__(128) k_conv3(ConvArgs a) {
     if (a.Y) {
 #pragma unroll
       for (int c = 0; c < COUT; c += 8) {
-        __nv_bfloat16 h[8];
+        alignas(16) __nv_bfloat16 h[8];
 #pragma unroll
         for (int e = 0; e < 8; ++e) h[e] = __float2bfloat16(a.gelu ? gelu(acc[c + e]) : acc[c + e]);
         *reinterpret_cast<uint4*>(a.Y + vo * COUT + c) = *reinterpret_cast<const uint4*>(h);
@@ -207,8 +220,202 @@ __global__ void __launch_bounds__(128) k_conv3(ConvArgs a) {
   if (warp == 0) tc05::tmem_free(tmem, 32);
 }
 
+// The line-ring form, for rows of x that hold whole tiles (nx a multiple of
+// 128).  A tile is 128 consecutive voxels of one x row.  A work unit is a
+// column of tiles (x segment, z) over a range of y; walking it in y, every
+// tile needs the rows y-1, y, y+1 of the planes z-1, z, z+1, each 130 voxels
+// long (one periodic neighbour on either side).  A ring of 4 y positions x 3
+// z lines stays in shared memory as channel-group planes [group of 8
+// channels][row][8 values], so a tile loads only the 3 lines of one new y.
+// With rows 16 bytes apart in a plane, the A operand of tap (dx, dy, dz) is
+// the plane of ring slot y+dy, line dz, started dx + 1 rows in: a
+// descriptor offset, no copy per tap.  Two accumulators (64 tensor-memory
+// columns) let the copies for tile y+1 and the epilogue of tile y-1 run while
+// the tensor core works on tile y.  256 threads: all copy; thread 0 issues
+// the MMAs; warp w reads accumulator lanes 32*(w%4).. and half (w/4) of the
+// columns.
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(256) k_conv3r(ConvArgs a, int ychunk) {
+  static_assert(CIN % 16 == 0 && (COUT == 16 || COUT == 32), "operand shapes");
+  constexpr int KG = CIN / 8;                // channel groups (16 bytes each)
+  constexpr int RP = KG == 2 ? 132 : 130;    // rows per plane; the padding spreads the copies over the banks
+  constexpr int PLANE = RP * 16, LINE = KG * PLANE, SLOT = 3 * LINE, NSLOT = 4;
+  constexpr int WBYTES = 27 * COUT * CIN * 2;
+  constexpr int RPT = 256 / KG, NPASS = (130 + RPT - 1) / RPT;  // rows per pass of the block, passes per line
+  constexpr int HC = COUT / 2;               // accumulator columns per warp
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t* sW = smem;
+  uint8_t* sR = smem + WBYTES;
+  __shared__ uint64_t mbar[2];
+  __shared__ uint32_t tslot;
+  __shared__ float sbias[COUT];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int i = tid; i < 27 * COUT * CIN; i += 256) {
+    const int t = i / (COUT * CIN), r = i % (COUT * CIN), n = r / CIN, k = r % CIN;
+    *reinterpret_cast<__nv_bfloat16*>(sW + t * (COUT * CIN * 2) + tc05::core_offset(n, k, COUT)) = a.W[i];
+  }
+  if (tid < COUT) sbias[tid] = a.bias ? a.bias[tid] : 0.0f;
+  if (warp == 0) tc05::tmem_alloc(&tslot, 64);
+  if (tid == 0) {
+    tc05::mbar_init(&mbar[0], 1);
+    tc05::mbar_init(&mbar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc05::fence_before_sync();
+  __syncthreads();
+  tc05::fence_after_sync();
+  const int nx = a.nx, ny = a.ny, nz = a.nz, segs = nx / 128;
+  const int ychunks = (ny + ychunk - 1) / ychunk;
+  const long long nunits = (long long)segs * nz * ychunks;
+  const int kg = tid % KG, r0 = tid / KG;
+  int xs[NPASS];       // source x of this thread's rows in the current unit
+  long long zb[3];     // nx*ny*z' of the unit's three planes
+  auto load_y = [&](int yv) {  // the three lines of y position yv (ny > yv >= -1 before wrapping)
+    const int yy = yv < 0 ? yv + ny : (yv >= ny ? yv - ny : yv);
+    uint8_t* dst = sR + ((yv + NSLOT) & (NSLOT - 1)) * SLOT + kg * PLANE;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const __nv_bfloat16* src = a.X + (zb[d] + (long long)nx * yy) * CIN + kg * 8;
+#pragma unroll
+      for (int p = 0; p < NPASS; ++p) {
+        const int r = r0 + p * RPT;
+        if (r < 130) tc05::cp_async16(dst + d * LINE + r * 16, src + (long long)xs[p] * CIN);
+      }
+    }
+  };
+  auto epilogue = [&](long long v0, int b) {
+    const int q = warp & 3, c0 = (warp >> 2) * HC;
+    const uint32_t taddr = tslot + (uint32_t)(b * 32 + c0) + ((uint32_t)(q * 32) << 16);
+    float acc[HC];
+    if constexpr (HC == 16) tc05::tmem_ld16(taddr, acc);
+    else tc05::tmem_ld8(taddr, acc);
+    const long long vo = v0 + q * 32 + lane;
+#pragma unroll
+    for (int c = 0; c < HC; ++c) acc[c] += sbias[c0 + c];
+    if (a.Z) {
+#pragma unroll
+      for (int c = 0; c < HC; c += 8) {
+        alignas(16) __nv_bfloat16 h[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) h[e] = __float2bfloat16(acc[c + e]);
+        *reinterpret_cast<uint4*>(a.Z + vo * COUT + c0 + c) = *reinterpret_cast<const uint4*>(h);
+      }
+    }
+    if (a.Y) {
+#pragma unroll
+      for (int c = 0; c < HC; c += 8) {
+        alignas(16) __nv_bfloat16 h[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) h[e] = __float2bfloat16(a.gelu ? gelu(acc[c + e]) : acc[c + e]);
+        *reinterpret_cast<uint4*>(a.Y + vo * COUT + c0 + c) = *reinterpret_cast<const uint4*>(h);
+      }
+    }
+    if (a.Yf) {
+#pragma unroll
+      for (int c = 0; c < HC; ++c)
+        if (c0 + c < a.nstore) a.Yf[vo * a.ldf + c0 + c] = acc[c];
+    }
+  };
+  constexpr uint32_t idesc = tc05::idesc_bf16_f32(128, COUT);
+  const uint64_t adesc0 = tc05::desc_noswizzle(tc05::smem_u32(sR), PLANE, 128);
+  const uint64_t bdesc0 = tc05::desc_noswizzle(tc05::smem_u32(sW), (COUT / 8) * 128, 128);
+  uint32_t parity = 0;  // bit b: the phase of mbar[b] to wait for next
+  long long step = 0;   // tiles issued by this block: accumulator and barrier step & 1
+  bool ok = true;
+  for (long long u = blockIdx.x; u < nunits; u += gridDim.x) {
+    const int seg = (int)(u % segs);
+    const long long rest = u / segs;
+    const int yc = (int)(rest % ychunks), z = (int)(rest / ychunks);
+    const int x0 = seg * 128, y0 = yc * ychunk, y1 = y0 + ychunk < ny ? y0 + ychunk : ny;
+#pragma unroll
+    for (int p = 0; p < NPASS; ++p) {
+      int x = x0 - 1 + r0 + p * RPT;
+      xs[p] = x < 0 ? x + nx : (x >= nx ? x - nx : x);
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      int zz = z + d - 1;
+      zz = zz < 0 ? zz + nz : (zz >= nz ? zz - nz : zz);
+      zb[d] = (long long)nx * ny * zz;
+    }
+    load_y(y0 - 1);
+    load_y(y0);
+    load_y(y0 + 1);
+    tc05::cp_async_commit();
+    long long prev = -1;  // first voxel of the tile whose epilogue is pending
+    for (int y = y0; y < y1; ++y, ++step) {
+      const int b = (int)(step & 1);
+      tc05::cp_async_wait_all();  // this thread's copies are in shared memory
+      tc05::fence_async_smem();   // and visible to the tensor core
+      tc05::fence_before_sync();
+      __syncthreads();
+      tc05::fence_after_sync();
+      if (tid == 0) {
+        uint32_t so[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) so[d] = (uint32_t)(((y + d - 1 + NSLOT) & (NSLOT - 1)) * SLOT);
+#pragma unroll
+        for (int t = 0; t < 27; ++t) {
+#pragma unroll
+          for (int kk = 0; kk < KG / 2; ++kk) {
+            const uint32_t aoff = so[(t / 3) % 3] + (t / 9) * LINE + 2 * kk * PLANE + (t % 3) * 16;
+            const uint32_t boff = t * (COUT * CIN * 2) + kk * 2 * ((COUT / 8) * 128);
+            tc05::mma_bf16(tslot + b * 32, adesc0 + (aoff >> 4), bdesc0 + (boff >> 4), idesc, t > 0 || kk > 0);
+          }
+        }
+        tc05::mma_commit(&mbar[b]);
+      }
+      if (prev >= 0) {  // tile y-1 is multiplied: its accumulator and ring slot y-2 are free
+        ok &= tc05::mbar_wait(&mbar[b ^ 1], (parity >> (b ^ 1)) & 1u, WAIT_LIMIT);
+        parity ^= 1u << (b ^ 1);
+        tc05::fence_after_sync();
+      }
+      if (y + 2 <= y1) {  // the new lines of tile y+1
+        load_y(y + 2);
+        tc05::cp_async_commit();
+      }
+      if (prev >= 0) epilogue(prev, b ^ 1);
+      tc05::fence_before_sync();
+      prev = ((long long)z * ny + y) * nx + x0;
+    }
+    // drain the unit's last tile
+    const int b = (int)((step - 1) & 1);
+    ok &= tc05::mbar_wait(&mbar[b], (parity >> b) & 1u, WAIT_LIMIT);
+    parity ^= 1u << b;
+    tc05::fence_after_sync();
+    epilogue(prev, b);
+    tc05::fence_before_sync();
+  }
+  tc05::cp_async_wait_all();
+  if (!ok) atomicCAS(a.err, 0, SWAP_EWAIT);
+  tc05::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc05::tmem_free(tslot, 64);
+}
+
+template <int CIN, int COUT>
+cudaError_t launch_conv3r(const ConvArgs& a, int nsm, cudaStream_t st) {
+  constexpr int KG = CIN / 8, RP = KG == 2 ? 132 : 130;
+  const int smem = 27 * COUT * CIN * 2 + 4 * 3 * KG * RP * 16;
+  cudaError_t e = cudaFuncSetAttribute(k_conv3r<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  int per_sm = 1;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3r<CIN, COUT>, 256, smem);
+  if (e != cudaSuccess) return e;
+  per_sm = per_sm < 1 ? 1 : (per_sm > 4 ? 4 : per_sm);  // 64 tensor-memory columns each
+  const long long blocks = (long long)per_sm * nsm, cols = (long long)(a.nx / 128) * a.nz;
+  // y chunks: enough work units to balance the blocks, at least 8 tiles each
+  int ychunk = a.ny;
+  while (ychunk > 8 && cols * ((a.ny + ychunk - 1) / ychunk) < 4 * blocks) ychunk = (ychunk + 1) / 2;
+  const long long units = cols * ((a.ny + ychunk - 1) / ychunk);
+  const int grid = (int)(units < blocks ? units : blocks);
+  k_conv3r<CIN, COUT><<<grid, 256, smem, st>>>(a, ychunk);
+  return cudaGetLastError();
+}
+
 template <int CIN, int COUT>
 cudaError_t launch_conv3(const ConvArgs& a, int nsm, cudaStream_t st) {
+  if (a.nx % 128 == 0) return launch_conv3r<CIN, COUT>(a, nsm, st);
   const int smem = 27 * COUT * CIN * 2 + 2 * 128 * CIN * 2;
   cudaError_t e = cudaFuncSetAttribute(k_conv3<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
@@ -280,4 +487,665 @@ extern "C" int swap_conv3_check(int32_t nx, int32_t ny, int32_t nz, int32_t cin,
   if (e == cudaErrorInvalidValue) return SWAP_EINVAL;
   if (e != cudaSuccess) return SWAP_ECUDA;
   return h ? SWAP_EWAIT : SWAP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// the network: 4 periodic 3x3x3 conv layers, 8 -> 32 -> 32 -> 32 -> 3
+// channels, GELU between them; BF16 weights and activations, FP32
+// accumulation, FP32 master weights trained with Adam
+// ---------------------------------------------------------------------------
+
+namespace {
+
+constexpr int NL = 4;
+constexpr int LCIN[NL] = {16, 32, 32, 32};   // layer 0: 8 input channels padded to 16
+constexpr int LCOUT[NL] = {32, 32, 32, 16};  // layer 3: 3 output channels padded to 16
+constexpr int NIN = 8, NOUT = 3;
+
+__device__ __forceinline__ float gelu_grad(float x) {
+  const float t = tanh_hw(GELU_K0 * fmaf(GELU_K1 * x, x * x, x));
+  return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * GELU_K0 * fmaf(3.0f * GELU_K1, x * x, 1.0f);
+}
+
+// Normalised BF16 inputs [V][16] from FP32 [V][8].
+__global__ void k_norm_inputs(long long V, const float* __restrict__ in, const float* __restrict__ mean,
+                              const float* __restrict__ inv_std, __nv_bfloat16* __restrict__ x) {
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
+    alignas(16) __nv_bfloat16 h[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) h[c] = __float2bfloat16(c < NIN ? (in[v * NIN + c] - mean[c]) * inv_std[c] : 0.0f);
+    uint4* dst = reinterpret_cast<uint4*>(x + v * 16);
+    dst[0] = reinterpret_cast<const uint4*>(h)[0];
+    dst[1] = reinterpret_cast<const uint4*>(h)[1];
+  }
+}
+
+// Output normalisation: the network predicts (E - mean) / std per component.
+struct OutNorm {
+  float mean[3], std[3];
+};
+
+// Loss 0.5*mean (out - (tgt - mean)/std)^2 over V*3 values, its gradient as
+// BF16 [V][16] (channels 3..15 zero); the sum of squares goes to *acc.
+__global__ void k_loss(long long V, const float* __restrict__ out, const float* __restrict__ tgt, OutNorm on,
+                       float gscale, __nv_bfloat16* __restrict__ d16, float* acc) {
+  float s = 0.0f;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
+    alignas(16) __nv_bfloat16 h[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) h[c] = __float2bfloat16(0.0f);
+#pragma unroll
+    for (int c = 0; c < NOUT; ++c) {
+      const float d = out[v * NOUT + c] - (tgt[v * NOUT + c] - on.mean[c]) / on.std[c];
+      s += d * d;
+      h[c] = __float2bfloat16(d * gscale);
+    }
+    uint4* dst = reinterpret_cast<uint4*>(d16 + v * 16);
+    dst[0] = reinterpret_cast<const uint4*>(h)[0];
+    dst[1] = reinterpret_cast<const uint4*>(h)[1];
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(acc, s);
+}
+
+// dZ = dY * GELU'(Z) as BF16 [V][C].
+__global__ void k_gelu_back(long long n, const float* __restrict__ dy, const __nv_bfloat16* __restrict__ z,
+                            __nv_bfloat16* __restrict__ dz) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+    dz[t] = __float2bfloat16(dy[t] * gelu_grad(__bfloat162float(z[t])));
+}
+
+// Weight gradient of a periodic conv layer on the CUDA cores:
+// gW[tap][co][ci] += sum_v dZ[v][co] * X[v + tap][ci], gb[co] += sum_v dZ[v][co].
+// Block (chunk, tap); each thread owns a 2x2 (co, ci) block.
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(256) k_conv3_dw(int nx, int ny, int nz, long long V,
+                                                  const __nv_bfloat16* __restrict__ X,
+                                                  const __nv_bfloat16* __restrict__ dZ, float* __restrict__ gW,
+                                                  float* __restrict__ gb, int vchunk) {
+  constexpr int SUB = 64, NPAIR = (COUT / 2) * (CIN / 2);
+  __shared__ float sdz[SUB][COUT + 1];
+  __shared__ float sx[SUB][CIN + 1];
+  const int t = blockIdx.y, dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
+  const int p = threadIdx.x, co = 2 * (p / (CIN / 2)), ci = 2 * (p % (CIN / 2));
+  float a00 = 0, a01 = 0, a10 = 0, a11 = 0, s0 = 0, s1 = 0;
+  const long long v0 = (long long)blockIdx.x * vchunk;
+  const long long v1 = v0 + vchunk < V ? v0 + vchunk : V;
+  for (long long vb = v0; vb < v1; vb += SUB) {
+    for (int i = threadIdx.x; i < SUB * COUT; i += blockDim.x) {
+      const long long v = vb + i / COUT;
+      sdz[i / COUT][i % COUT] = v < v1 ? __bfloat162float(dZ[v * COUT + i % COUT]) : 0.0f;
+    }
+    for (int i = threadIdx.x; i < SUB * CIN; i += blockDim.x) {
+      const long long v = vb + i / CIN;
+      float val = 0.0f;
+      if (v < v1) {
+        const int x = (int)(v % nx), y = (int)((v / nx) % ny), z = (int)(v / ((long long)nx * ny));
+        int xn = x + dx, yn = y + dy, zn = z + dz;
+        xn = xn < 0 ? xn + nx : (xn >= nx ? xn - nx : xn);
+        yn = yn < 0 ? yn + ny : (yn >= ny ? yn - ny : yn);
+        zn = zn < 0 ? zn + nz : (zn >= nz ? zn - nz : zn);
+        val = __bfloat162float(X[(xn + (long long)nx * (yn + (long long)ny * zn)) * CIN + i % CIN]);
+      }
+      sx[i / CIN][i % CIN] = val;
+    }
+    __syncthreads();
+    if (p < NPAIR) {
+#pragma unroll 8
+      for (int v = 0; v < SUB; ++v) {
+        const float d0 = sdz[v][co], d1 = sdz[v][co + 1], x0 = sx[v][ci], x1 = sx[v][ci + 1];
+        a00 = fmaf(d0, x0, a00); a01 = fmaf(d0, x1, a01);
+        a10 = fmaf(d1, x0, a10); a11 = fmaf(d1, x1, a11);
+        s0 += d0; s1 += d1;
+      }
+    }
+    __syncthreads();
+  }
+  if (p < NPAIR) {
+    float* w = gW + (long long)t * COUT * CIN;
+    atomicAdd(w + co * CIN + ci, a00);
+    atomicAdd(w + co * CIN + ci + 1, a01);
+    atomicAdd(w + (co + 1) * CIN + ci, a10);
+    atomicAdd(w + (co + 1) * CIN + ci + 1, a11);
+    if (t == 13 && ci == 0) {
+      atomicAdd(gb + co, s0);
+      atomicAdd(gb + co + 1, s1);
+    }
+  }
+}
+
+// Adam on n parameters; BF16 copy refreshed.
+__global__ void k_adam(long long n, float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ vv, float lr, float b1, float b2, float c1, float c2, float eps,
+                       __nv_bfloat16* __restrict__ wh) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * vv[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    vv[i] = vi;
+    const float wi = w[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+    w[i] = wi;
+    if (wh) wh[i] = __float2bfloat16(wi);
+  }
+}
+
+// The data-gradient weights of a layer: Wt[tap][ci][co] = W[26 - tap][co][ci].
+__global__ void k_flip_t(int cin, int cout, const __nv_bfloat16* __restrict__ W, __nv_bfloat16* __restrict__ Wt) {
+  const int n = 27 * cin * cout;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int t = i / (cin * cout), r = i % (cin * cout), ci = r / cout, co = r % cout;
+    Wt[i] = W[(26 - t) * cout * cin + co * cin + ci];
+  }
+}
+
+// E [V][3] from the network's normalised output.
+__global__ void k_denorm(long long V, const float* __restrict__ out, OutNorm on, float* __restrict__ ve) {
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x)
+#pragma unroll
+    for (int c = 0; c < NOUT; ++c) ve[v * NOUT + c] = fmaf(out[v * NOUT + c], on.std[c], on.mean[c]);
+}
+
+inline unsigned nblk(long long n, int tpb = 256) {
+  const long long b = (n + tpb - 1) / tpb;
+  return (unsigned)(b < 1 ? 1 : (b > 65535LL * 8 ? 65535LL * 8 : b));
+}
+
+template <int CIN, int COUT>
+cudaError_t conv3_dw(int nx, int ny, int nz, long long V, const __nv_bfloat16* X, const __nv_bfloat16* dZ, float* gW,
+                     float* gb, cudaStream_t st) {
+  // at most 64 voxel chunks per tap: few enough atomic adds per weight
+  const long long nchunk = std::min<long long>((V + 2047) / 2048, 64);
+  const int vchunk = (int)(((V + nchunk - 1) / nchunk + 63) / 64 * 64);
+  const dim3 grid((unsigned)((V + vchunk - 1) / vchunk), 27);
+  k_conv3_dw<CIN, COUT><<<grid, 256, 0, st>>>(nx, ny, nz, V, X, dZ, gW, gb, vchunk);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host side of the network
+// ---------------------------------------------------------------------------
+
+struct swap_surrogate {
+  uint64_t seed = 1;
+  float* w[NL] = {};        // FP32 master weights [27][cout][cin]
+  float* b[NL] = {};        // biases [cout]
+  __nv_bfloat16* wh[NL] = {};  // BF16 copies
+  __nv_bfloat16* wt[NL] = {};  // data-gradient weights [27][cin][cout]
+  float *gw[NL] = {}, *gb[NL] = {}, *mw[NL] = {}, *vw[NL] = {}, *mb[NL] = {}, *vb[NL] = {};
+  long long adam_t = 0;
+  // normalisation: inputs (x - mean) / std, outputs (E - mean) / std
+  float in_mean[NIN] = {}, in_std[NIN] = {1, 1, 1, 1, 1, 1, 1, 1};
+  OutNorm on{{0, 0, 0}, {1, 1, 1}};
+  bool normed = false;
+  float *d_mean = nullptr, *d_istd = nullptr;
+  // dataset of one grid shape
+  int nx = 0, ny = 0, nz = 0;
+  long long V = 0;
+  int max_samples = 0;
+  std::vector<float*> ds_in, ds_tgt;  // [V][8], [V][3]
+  // work buffers for V voxels
+  __nv_bfloat16* x0 = nullptr;             // [V][16]
+  __nv_bfloat16 *Z[NL - 1] = {}, *Y[NL - 1] = {};  // [V][32]
+  float* out = nullptr;                    // [V][3]
+  __nv_bfloat16* d16 = nullptr;            // [V][16]
+  float* dy = nullptr;                     // [V][32]
+  __nv_bfloat16 *dzA = nullptr, *dzB = nullptr;  // [V][32]
+  float* acc = nullptr;
+  int* err = nullptr;
+  std::vector<void*> owned;
+  std::string msg;
+
+  template <class T>
+  T* alloc(std::size_t n) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, n * sizeof(T) + 16) != cudaSuccess) return nullptr;
+    owned.push_back(p);
+    return static_cast<T*>(p);
+  }
+  ~swap_surrogate() {
+    for (void* p : owned) cudaFree(p);
+  }
+};
+
+namespace {
+
+int fail(swap_surrogate* n, int code, const std::string& m) {
+  n->msg = m;
+  return code;
+}
+
+#define SCU(x)                                                            \
+  do {                                                                    \
+    cudaError_t _e = (x);                                                 \
+    if (_e != cudaSuccess) return fail(net, SWAP_ECUDA, std::string(#x) + ": " + cudaGetErrorString(_e)); \
+  } while (0)
+
+// Work buffers for a grid of nx*ny*nz voxels (the first call fixes it).
+int ensure_shape(swap_surrogate* net, int nx, int ny, int nz) {
+  const long long V = (long long)nx * ny * nz;
+  if (net->V == V && net->nx == nx && net->ny == ny && net->nz == nz) return SWAP_OK;
+  if (net->V != 0) return fail(net, SWAP_EINVAL, "the surrogate is bound to another grid shape");
+  if (V % 128) return fail(net, SWAP_EINVAL, "the surrogate needs a voxel count that is a multiple of 128");
+  net->nx = nx; net->ny = ny; net->nz = nz; net->V = V;
+  net->x0 = net->alloc<__nv_bfloat16>(V * 16);
+  for (int l = 0; l < NL - 1; ++l) {
+    net->Z[l] = net->alloc<__nv_bfloat16>(V * 32);
+    net->Y[l] = net->alloc<__nv_bfloat16>(V * 32);
+  }
+  net->out = net->alloc<float>(V * NOUT);
+  net->d16 = net->alloc<__nv_bfloat16>(V * 16);
+  net->dy = net->alloc<float>(V * 32);
+  net->dzA = net->alloc<__nv_bfloat16>(V * 32);
+  net->dzB = net->alloc<__nv_bfloat16>(V * 32);
+  if (!net->x0 || !net->Z[2] || !net->out || !net->d16 || !net->dy || !net->dzB)
+    return fail(net, SWAP_ECUDA, "surrogate work buffers");
+  return SWAP_OK;
+}
+
+ConvArgs conv_args(swap_surrogate* net) {
+  ConvArgs a{};
+  a.nx = net->nx; a.ny = net->ny; a.nz = net->nz; a.V = net->V;
+  a.err = net->err;
+  return a;
+}
+
+int upload_norm(swap_surrogate* net, cudaStream_t st) {
+  float istd[NIN];
+  for (int c = 0; c < NIN; ++c) istd[c] = 1.0f / net->in_std[c];
+  SCU(cudaMemcpyAsync(net->d_mean, net->in_mean, sizeof(net->in_mean), cudaMemcpyHostToDevice, st));
+  SCU(cudaMemcpyAsync(net->d_istd, istd, sizeof(istd), cudaMemcpyHostToDevice, st));
+  return SWAP_OK;
+}
+
+// Forward pass on net->x0; training keeps the pre-activations.
+int forward(swap_surrogate* net, bool train, cudaStream_t st) {
+  ConvArgs a = conv_args(net);
+  for (int l = 0; l < NL; ++l) {
+    a.X = l == 0 ? net->x0 : net->Y[l - 1];
+    a.W = net->wh[l];
+    a.bias = net->b[l];
+    if (l < NL - 1) {
+      a.Y = net->Y[l];
+      a.Z = train ? net->Z[l] : nullptr;
+      a.Yf = nullptr;
+      a.gelu = 1;
+    } else {
+      a.Y = nullptr;
+      a.Z = nullptr;
+      a.Yf = net->out;
+      a.ldf = NOUT;
+      a.nstore = NOUT;
+      a.gelu = 0;
+    }
+    SCU(conv3(LCIN[l], LCOUT[l], a, st));
+  }
+  return SWAP_OK;
+}
+
+// Backward from net->d16 (the output gradient): gradients into gw/gb.
+int backward(swap_surrogate* net, cudaStream_t st) {
+  const int nx = net->nx, ny = net->ny, nz = net->nz;
+  const long long V = net->V;
+  SCU((conv3_dw<32, 16>(nx, ny, nz, V, net->Y[2], net->d16, net->gw[3], net->gb[3], st)));
+  ConvArgs a = conv_args(net);
+  a.Y = nullptr; a.Z = nullptr; a.bias = nullptr; a.gelu = 0; a.ldf = 32; a.nstore = 32; a.Yf = net->dy;
+  // layer 3 -> 2
+  a.X = net->d16; a.W = net->wt[3];
+  SCU(conv3(16, 32, a, st));
+  k_gelu_back<<<nblk(V * 32), 256, 0, st>>>(V * 32, net->dy, net->Z[2], net->dzA);
+  SCU((conv3_dw<32, 32>(nx, ny, nz, V, net->Y[1], net->dzA, net->gw[2], net->gb[2], st)));
+  // layer 2 -> 1
+  a.X = net->dzA; a.W = net->wt[2];
+  SCU(conv3(32, 32, a, st));
+  k_gelu_back<<<nblk(V * 32), 256, 0, st>>>(V * 32, net->dy, net->Z[1], net->dzB);
+  SCU((conv3_dw<32, 32>(nx, ny, nz, V, net->Y[0], net->dzB, net->gw[1], net->gb[1], st)));
+  // layer 1 -> 0
+  a.X = net->dzB; a.W = net->wt[1];
+  SCU(conv3(32, 32, a, st));
+  k_gelu_back<<<nblk(V * 32), 256, 0, st>>>(V * 32, net->dy, net->Z[0], net->dzA);
+  SCU((conv3_dw<16, 32>(nx, ny, nz, V, net->x0, net->dzA, net->gw[0], net->gb[0], st)));
+  return SWAP_OK;
+}
+
+int zero_grads(swap_surrogate* net, cudaStream_t st) {
+  for (int l = 0; l < NL; ++l) {
+    SCU(cudaMemsetAsync(net->gw[l], 0, 27 * LCIN[l] * LCOUT[l] * sizeof(float), st));
+    SCU(cudaMemsetAsync(net->gb[l], 0, LCOUT[l] * sizeof(float), st));
+  }
+  return SWAP_OK;
+}
+
+int refresh_flips(swap_surrogate* net, cudaStream_t st) {
+  for (int l = 1; l < NL; ++l) k_flip_t<<<nblk(27 * LCIN[l] * LCOUT[l]), 256, 0, st>>>(LCIN[l], LCOUT[l], net->wh[l],
+                                                                                    net->wt[l]);
+  SCU(cudaGetLastError());
+  return SWAP_OK;
+}
+
+int adam_step(swap_surrogate* net, float lr, cudaStream_t st) {
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  ++net->adam_t;
+  const float c1 = 1.0f / (1.0f - powf(b1, (float)net->adam_t)), c2 = 1.0f / (1.0f - powf(b2, (float)net->adam_t));
+  for (int l = 0; l < NL; ++l) {
+    const long long nw = 27LL * LCIN[l] * LCOUT[l];
+    k_adam<<<nblk(nw), 256, 0, st>>>(nw, net->w[l], net->gw[l], net->mw[l], net->vw[l], lr, b1, b2, c1, c2, eps,
+                                     net->wh[l]);
+    k_adam<<<1, 64, 0, st>>>(LCOUT[l], net->b[l], net->gb[l], net->mb[l], net->vb[l], lr, b1, b2, c1, c2, eps,
+                             nullptr);
+  }
+  SCU(cudaGetLastError());
+  return refresh_flips(net, st);
+}
+
+// Loss of the current x0 against target tgt ([V][3], unnormalised); the
+// output gradient goes to d16.  Returns the sum of squares in *sq.
+int loss_grad(swap_surrogate* net, const float* tgt, float gnorm, double* sq, cudaStream_t st) {
+  SCU(cudaMemsetAsync(net->acc, 0, sizeof(float), st));
+  k_loss<<<nblk(net->V), 256, 0, st>>>(net->V, net->out, tgt, net->on, gnorm, net->d16, net->acc);
+  float h = 0;
+  SCU(cudaMemcpyAsync(&h, net->acc, sizeof(float), cudaMemcpyDeviceToHost, st));
+  SCU(cudaStreamSynchronize(st));
+  *sq = h;
+  return SWAP_OK;
+}
+
+int check_err(swap_surrogate* net) {
+  int h = 0;
+  SCU(cudaMemcpy(&h, net->err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h) {
+    cudaMemset(net->err, 0, sizeof(int));
+    return fail(net, SWAP_EWAIT, "a tensor-core wait reached its limit");
+  }
+  return SWAP_OK;
+}
+
+}  // namespace
+
+namespace surr {
+
+// E predicted for FP32 inputs [V][8] (device) into ve [V][3] (device).
+int predict_e(swap_surrogate* net, int nx, int ny, int nz, const float* vin, float* ve, cudaStream_t st) {
+  if (!net->normed) return fail(net, SWAP_EINVAL, "the surrogate has not been trained");
+  int r = ensure_shape(net, nx, ny, nz);
+  if (r) return r;
+  k_norm_inputs<<<nblk(net->V), 256, 0, st>>>(net->V, vin, net->d_mean, net->d_istd, net->x0);
+  r = forward(net, false, st);
+  if (r) return r;
+  k_denorm<<<nblk(net->V), 256, 0, st>>>(net->V, net->out, net->on, ve);
+  SCU(cudaGetLastError());
+  return SWAP_OK;
+}
+
+// Append a training pair: inputs [V][8] and the target E [V][3] (device).
+int add_sample(swap_surrogate* net, int nx, int ny, int nz, const float* vin, const float* ve, cudaStream_t st) {
+  int r = ensure_shape(net, nx, ny, nz);
+  if (r) return r;
+  if ((int)net->ds_in.size() >= net->max_samples) return SWAP_OK;  // the dataset is full
+  float* a = net->alloc<float>(net->V * NIN);
+  float* t = net->alloc<float>(net->V * NOUT);
+  if (!a || !t) return fail(net, SWAP_ECUDA, "surrogate dataset allocation");
+  SCU(cudaMemcpyAsync(a, vin, net->V * NIN * sizeof(float), cudaMemcpyDeviceToDevice, st));
+  SCU(cudaMemcpyAsync(t, ve, net->V * NOUT * sizeof(float), cudaMemcpyDeviceToDevice, st));
+  net->ds_in.push_back(a);
+  net->ds_tgt.push_back(t);
+  return SWAP_OK;
+}
+
+const char* last_error(swap_surrogate* net) { return net->msg.c_str(); }
+
+}  // namespace surr
+
+// ---------------------------------------------------------------------------
+// C-ABI of the network
+// ---------------------------------------------------------------------------
+
+#include <algorithm>
+#include <random>
+
+extern "C" int swap_surrogate_create(swap_surrogate** out, uint64_t seed, int32_t max_samples) {
+  if (!out || max_samples < 1) return SWAP_EINVAL;
+  *out = nullptr;
+  auto* net = new swap_surrogate();
+  net->seed = seed;
+  net->max_samples = max_samples;
+  std::mt19937_64 rng(seed);
+  for (int l = 0; l < NL; ++l) {
+    const int ci = LCIN[l], co = LCOUT[l];
+    const std::size_t nw = 27 * (std::size_t)ci * co;
+    net->w[l] = net->alloc<float>(nw);
+    net->b[l] = net->alloc<float>(co);
+    net->wh[l] = net->alloc<__nv_bfloat16>(nw);
+    net->wt[l] = net->alloc<__nv_bfloat16>(nw);
+    net->gw[l] = net->alloc<float>(nw);
+    net->gb[l] = net->alloc<float>(co);
+    net->mw[l] = net->alloc<float>(nw);
+    net->vw[l] = net->alloc<float>(nw);
+    net->mb[l] = net->alloc<float>(co);
+    net->vb[l] = net->alloc<float>(co);
+    if (!net->w[l] || !net->vb[l]) {
+      delete net;
+      return SWAP_ECUDA;
+    }
+    // He initialisation over the real fan-in; padded channels stay zero; the
+    // output layer starts small
+    const int ci_real = l == 0 ? NIN : ci, co_real = l == NL - 1 ? NOUT : co;
+    const double sd = (l == NL - 1 ? 0.1 : 1.0) * std::sqrt(2.0 / (27.0 * ci_real));
+    std::normal_distribution<double> nd(0.0, sd);
+    std::vector<float> hw(nw, 0.0f);
+    std::vector<__nv_bfloat16> hh(nw);
+    for (int t = 0; t < 27; ++t)
+      for (int o = 0; o < co_real; ++o)
+        for (int i = 0; i < ci_real; ++i) hw[((std::size_t)t * co + o) * ci + i] = (float)nd(rng);
+    for (std::size_t i = 0; i < nw; ++i) hh[i] = __float2bfloat16(hw[i]);
+    cudaMemcpy(net->w[l], hw.data(), nw * sizeof(float), cudaMemcpyHostToDevice);
+    cudaMemcpy(net->wh[l], hh.data(), nw * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice);
+    cudaMemset(net->b[l], 0, co * sizeof(float));
+    for (float* p : {net->mw[l], net->vw[l]}) cudaMemset(p, 0, nw * sizeof(float));
+    for (float* p : {net->mb[l], net->vb[l]}) cudaMemset(p, 0, co * sizeof(float));
+  }
+  net->d_mean = net->alloc<float>(NIN);
+  net->d_istd = net->alloc<float>(NIN);
+  net->acc = net->alloc<float>(4);
+  net->err = net->alloc<int>(1);
+  if (!net->d_mean || !net->d_istd || !net->acc || !net->err) {
+    delete net;
+    return SWAP_ECUDA;
+  }
+  cudaMemset(net->err, 0, sizeof(int));
+  if (upload_norm(net, nullptr) || refresh_flips(net, nullptr) || cudaDeviceSynchronize() != cudaSuccess) {
+    delete net;
+    return SWAP_ECUDA;
+  }
+  *out = net;
+  return SWAP_OK;
+}
+
+extern "C" int swap_surrogate_destroy(swap_surrogate* net) {
+  if (!net) return SWAP_EINVAL;
+  cudaDeviceSynchronize();
+  delete net;
+  return SWAP_OK;
+}
+
+extern "C" const char* swap_surrogate_last_error(const swap_surrogate* net) {
+  return net ? net->msg.c_str() : "null surrogate";
+}
+
+extern "C" int swap_surrogate_samples(swap_surrogate* net, int32_t* n) {
+  if (!net || !n) return SWAP_EINVAL;
+  *n = (int32_t)net->ds_in.size();
+  return SWAP_OK;
+}
+
+// Normalisation (mean and std of the 8 inputs and of the 3 outputs): get or
+// set.
+extern "C" int swap_surrogate_norm(swap_surrogate* net, float* mean, float* stdv, float* out_mean, float* out_std,
+                                   int32_t set) {
+  if (!net || !mean || !stdv || !out_mean || !out_std) return SWAP_EINVAL;
+  if (set) {
+    for (int c = 0; c < NIN; ++c)
+      if (!(stdv[c] > 0)) return fail(net, SWAP_EINVAL, "standard deviations must be positive");
+    for (int c = 0; c < NOUT; ++c)
+      if (!(out_std[c] > 0)) return fail(net, SWAP_EINVAL, "standard deviations must be positive");
+    for (int c = 0; c < NIN; ++c) {
+      net->in_mean[c] = mean[c];
+      net->in_std[c] = stdv[c];
+    }
+    for (int c = 0; c < NOUT; ++c) {
+      net->on.mean[c] = out_mean[c];
+      net->on.std[c] = out_std[c];
+    }
+    net->normed = true;
+    return upload_norm(net, nullptr);
+  }
+  for (int c = 0; c < NIN; ++c) {
+    mean[c] = net->in_mean[c];
+    stdv[c] = net->in_std[c];
+  }
+  for (int c = 0; c < NOUT; ++c) {
+    out_mean[c] = net->on.mean[c];
+    out_std[c] = net->on.std[c];
+  }
+  return SWAP_OK;
+}
+
+// FP32 master weights of a layer ([27][cout][cin], cin/cout padded as the
+// layer's shapes 16/32) and bias [cout]: get or set.
+extern "C" int swap_surrogate_weights(swap_surrogate* net, int32_t layer, float* w, float* b, int32_t set) {
+  if (!net || layer < 0 || layer >= NL || !w || !b) return SWAP_EINVAL;
+  const std::size_t nw = 27 * (std::size_t)LCIN[layer] * LCOUT[layer];
+  if (set) {
+    std::vector<__nv_bfloat16> hh(nw);
+    for (std::size_t i = 0; i < nw; ++i) hh[i] = __float2bfloat16(w[i]);
+    SCU(cudaMemcpy(net->w[layer], w, nw * sizeof(float), cudaMemcpyHostToDevice));
+    SCU(cudaMemcpy(net->wh[layer], hh.data(), nw * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice));
+    SCU(cudaMemcpy(net->b[layer], b, LCOUT[layer] * sizeof(float), cudaMemcpyHostToDevice));
+    if (refresh_flips(net, nullptr)) return SWAP_ECUDA;
+    SCU(cudaDeviceSynchronize());
+    return SWAP_OK;
+  }
+  SCU(cudaMemcpy(w, net->w[layer], nw * sizeof(float), cudaMemcpyDeviceToHost));
+  SCU(cudaMemcpy(b, net->b[layer], LCOUT[layer] * sizeof(float), cudaMemcpyDeviceToHost));
+  return SWAP_OK;
+}
+
+// One forward and backward pass on device inputs vin [V][8] and targets tgt
+// [V][3] (unnormalised) of an nx*ny*nz box: the loss 0.5*mean((out -
+// (tgt - out_mean)/out_std)^2) and the gradients of every layer, written to grads as
+// (gW[0], gb[0], gW[1], gb[1], ...).
+extern "C" int swap_surrogate_grads(swap_surrogate* net, int32_t nx, int32_t ny, int32_t nz, const float* vin,
+                                    const float* tgt, double* loss, float* grads) {
+  if (!net || !vin || !tgt || !loss || !grads) return SWAP_EINVAL;
+  int r = ensure_shape(net, nx, ny, nz);
+  if (r) return r;
+  cudaStream_t st = nullptr;
+  k_norm_inputs<<<nblk(net->V), 256, 0, st>>>(net->V, vin, net->d_mean, net->d_istd, net->x0);
+  if ((r = forward(net, true, st))) return r;
+  double sq = 0;
+  if ((r = loss_grad(net, tgt, 1.0f / (3.0f * (float)net->V), &sq, st))) return r;
+  if ((r = zero_grads(net, st)) || (r = backward(net, st))) return r;
+  SCU(cudaDeviceSynchronize());
+  if ((r = check_err(net))) return r;
+  *loss = 0.5 * sq / (3.0 * (double)net->V);
+  float* o = grads;
+  for (int l = 0; l < NL; ++l) {
+    const std::size_t nw = 27 * (std::size_t)LCIN[l] * LCOUT[l];
+    SCU(cudaMemcpy(o, net->gw[l], nw * sizeof(float), cudaMemcpyDeviceToHost));
+    o += nw;
+    SCU(cudaMemcpy(o, net->gb[l], LCOUT[l] * sizeof(float), cudaMemcpyDeviceToHost));
+    o += LCOUT[l];
+  }
+  return SWAP_OK;
+}
+
+// Normalisation from the dataset: per-channel mean and std of the inputs and
+// of the target E (the uniform part of E has no curl, so the network spends
+// its precision on the varying part).
+static int fit_norm(swap_surrogate* net) {
+  const std::size_t n = net->ds_in.size();
+  if (!n) return fail(net, SWAP_EINVAL, "the surrogate has no training samples");
+  const std::size_t take = std::min<std::size_t>(n, 16), V = (std::size_t)net->V;
+  std::vector<float> hi(V * NIN), ht(V * NOUT);
+  double s[NIN] = {}, s2[NIN] = {}, e1[NOUT] = {}, e2[NOUT] = {};
+  for (std::size_t q = 0; q < take; ++q) {
+    const std::size_t k = q * n / take;
+    SCU(cudaMemcpy(hi.data(), net->ds_in[k], hi.size() * 4, cudaMemcpyDeviceToHost));
+    SCU(cudaMemcpy(ht.data(), net->ds_tgt[k], ht.size() * 4, cudaMemcpyDeviceToHost));
+    for (std::size_t v = 0; v < V; ++v) {
+      for (int c = 0; c < NIN; ++c) {
+        s[c] += hi[v * NIN + c];
+        s2[c] += (double)hi[v * NIN + c] * hi[v * NIN + c];
+      }
+      for (int c = 0; c < NOUT; ++c) {
+        e1[c] += ht[v * NOUT + c];
+        e2[c] += (double)ht[v * NOUT + c] * ht[v * NOUT + c];
+      }
+    }
+  }
+  const double cnt = (double)take * V;
+  for (int c = 0; c < NIN; ++c) {
+    const double m = s[c] / cnt, var = std::max(s2[c] / cnt - m * m, 0.0);
+    net->in_mean[c] = (float)m;
+    net->in_std[c] = (float)std::max(std::sqrt(var), 1e-6 * std::max(1.0, std::fabs(m)));
+  }
+  for (int c = 0; c < NOUT; ++c) {
+    const double m = e1[c] / cnt, var = std::max(e2[c] / cnt - m * m, 0.0);
+    net->on.mean[c] = (float)m;
+    net->on.std[c] = (float)std::max(std::sqrt(var), 1e-6 * std::max(1.0, std::fabs(m)));
+  }
+  net->normed = true;
+  return upload_norm(net, nullptr);
+}
+
+// Adam over the collected pairs for `epochs` passes in shuffled order; the
+// mean squared normalised error of the last pass goes to *loss.
+extern "C" int swap_surrogate_train(swap_surrogate* net, int32_t epochs, double lr, double* loss) {
+  if (!net || epochs < 0 || !(lr > 0)) return SWAP_EINVAL;
+  int r;
+  if (!net->normed && (r = fit_norm(net))) return r;
+  const std::size_t n = net->ds_in.size();
+  if (!n) return fail(net, SWAP_EINVAL, "the surrogate has no training samples");
+  cudaStream_t st = nullptr;
+  std::mt19937_64 rng(net->seed + 17 + (uint64_t)net->adam_t);
+  std::vector<std::size_t> order(n);
+  double last = 0;
+  for (int e = 0; e < epochs; ++e) {
+    for (std::size_t i = 0; i < n; ++i) order[i] = i;
+    std::shuffle(order.begin(), order.end(), rng);
+    double tot = 0;
+    for (std::size_t k : order) {
+      k_norm_inputs<<<nblk(net->V), 256, 0, st>>>(net->V, net->ds_in[k], net->d_mean, net->d_istd, net->x0);
+      if ((r = forward(net, true, st))) return r;
+      double sq = 0;
+      if ((r = loss_grad(net, net->ds_tgt[k], 1.0f / (3.0f * (float)net->V), &sq, st))) return r;
+      tot += sq / (3.0 * (double)net->V);
+      if ((r = zero_grads(net, st)) || (r = backward(net, st)) || (r = adam_step(net, (float)lr, st))) return r;
+    }
+    last = tot / (double)n;
+  }
+  SCU(cudaDeviceSynchronize());
+  if ((r = check_err(net))) return r;
+  if (loss) *loss = last;
+  return SWAP_OK;
+}
+
+// Mean squared normalised error over the collected pairs (no update).
+extern "C" int swap_surrogate_loss(swap_surrogate* net, double* loss) {
+  if (!net || !loss) return SWAP_EINVAL;
+  int r;
+  if (!net->normed && (r = fit_norm(net))) return r;
+  double tot = 0;
+  for (std::size_t k = 0; k < net->ds_in.size(); ++k) {
+    k_norm_inputs<<<nblk(net->V), 256, 0, nullptr>>>(net->V, net->ds_in[k], net->d_mean, net->d_istd, net->x0);
+    if ((r = forward(net, false, nullptr))) return r;
+    double sq = 0;
+    if ((r = loss_grad(net, net->ds_tgt[k], 0.0f, &sq, nullptr))) return r;
+    tot += sq / (3.0 * (double)net->V);
+  }
+  if ((r = check_err(net))) return r;
+  *loss = net->ds_in.empty() ? 0.0 : tot / (double)net->ds_in.size();
+  return SWAP_OK;
 }

@@ -19,6 +19,7 @@
 #include "swap_ctx.h"
 #include "swap_ops.h"
 #include "swap_prof.h"
+#include "surrogate.h"
 
 using namespace swapk32;
 
@@ -53,6 +54,16 @@ struct F32State {
   srcops::F32Stage stage;
   bool src_on = false, x_open = false, ended = false;
   uint8_t heavy_of[MAX_SPECIES]{};
+  // the learned subcycle surrogate
+  swap_surrogate* sur = nullptr;      // attached network
+  swap_surrogate* collect = nullptr;  // network collecting training pairs
+  int sur_every = 8;
+  double sur_bound = 1e-3;
+  bool sur_off = false;               // the last judge failed: plain until one passes
+  long long sur_step = 0, sur_used = 0, sur_judged = 0, sur_fallbacks = 0;
+  double sur_err_b = 0, sur_err_db = 0;
+  float *e_sum = nullptr, *vin = nullptr, *ve = nullptr, *jh = nullptr, *jl = nullptr, *jdb = nullptr;
+  double* jacc = nullptr;
 
   ~F32State() {
     srcops::stage_free(stage);
@@ -333,7 +344,7 @@ static int finish_deposit(swap_ctx* c, F32State* s, int nq) {
   return SWAP_OK;
 }
 
-static int subcycles(swap_ctx* c, F32State* s) {
+static int subcycles(swap_ctx* c, F32State* s, float* e_acc = nullptr) {
   const G32& g = s->g;
   double dtsub = c->prm.dt / (double)c->prm.ntsub;  // maind.f:420-421
   double ntf = (double)c->prm.ntsub;
@@ -366,11 +377,11 @@ static int subcycles(swap_ctx* c, F32State* s) {
     // predictor: curlB (maind.f:430) and predict_B with its get_E (maind.f:457), plus dB at m+1/2
     KL("f32_aj_ct_pred", aj_ct(g, false, s->db1, s->np, s->up, s->b0c, alpha, s->aj, s->ct, c->st));
     KL("f32_bstep_pred", b_step(g, true, false, s->ct, s->nu, s->aj, s->b12.h, s->b12.l, 2.0 * dtsub, s->b0c,
-                                s->b1p2.h, s->b1p2.l, s->db1p2, s->db1, s->dbtp1, s->E, c->st));
+                                s->b1p2.h, s->b1p2.l, s->db1p2, s->db1, s->dbtp1, s->E, nullptr, c->st));
     // corrector: correct_B (maind.f:462) with its curlB and get_Ep1 at m+1/2
     KL("f32_aj_ct_corr", aj_ct(g, true, s->dbtp1, s->np, s->up, s->b0c, alpha, s->aj, s->ct, c->st));
     KL("f32_bstep_corr", b_step(g, false, last, s->ct, s->nu, s->aj, s->b1.h, s->b1.l, dtsub, s->b0c, s->b1p2.h,
-                                s->b1p2.l, s->db1p2, nullptr, nullptr, s->E, c->st));
+                                s->b1p2.l, s->db1p2, nullptr, nullptr, s->E, e_acc, c->st));
     // f_update_tlev (gutsf.f:10-35): b12 <- b1, b1 <- b1p2 (bt = b1)
     std::swap(s->b12, s->b1);
     std::swap(s->b1, s->b1p2);
@@ -436,6 +447,84 @@ static StepParams step_params(swap_ctx* c, F32State* s, bool drop_fresh) {
   return p;
 }
 
+// Buffers of the surrogate's field step (allocated on first use).
+static int sur_buffers(swap_ctx* c, F32State* s) {
+  if (s->e_sum) return SWAP_OK;
+  const std::size_t C = (std::size_t)s->g.C, V = (std::size_t)s->g.ncx * s->g.ncy * s->g.ncz;
+  s->e_sum = s->alloc<float>(3 * C);
+  s->vin = s->alloc<float>(8 * V);
+  s->ve = s->alloc<float>(3 * V);
+  s->jh = s->alloc<float>(3 * C);
+  s->jl = s->alloc<float>(3 * C);
+  s->jdb = s->alloc<float>(3 * C);
+  s->jacc = s->alloc<double>(4);
+  if (!s->e_sum || !s->vin || !s->ve || !s->jh || !s->jl || !s->jdb || !s->jacc)
+    return c->fail(SWAP_ECUDA, "surrogate buffers");
+  return SWAP_OK;
+}
+
+// The network's field advance from the state at the start of the subcycles:
+// E predicted per node, B into (oh, ol) and its dB into odb as B - dt curl E.
+static int sur_predict(swap_ctx* c, F32State* s, float* oh, float* ol, float* odb) {
+  const G32& g = s->g;
+  KL("f32_sur_inputs", grid_to_voxels(g, s->db1, s->b0c, s->up, s->np, 1.0f, s->vin, c->st));
+  {
+    ProfScope ps(c, "f32_sur_net", c->st);  // the network's own launches (normalise, 4 convs, scale)
+    if (surr::predict_e(s->sur, g.ncx, g.ncy, g.ncz, s->vin, s->ve, c->st))
+      return c->fail(SWAP_EINVAL, std::string("surrogate: ") + surr::last_error(s->sur));
+  }
+  KL("f32_sur_E", voxels_to_grid(g, s->ve, s->E, c->st));
+  KL("f32_sur_B", b_step_given_e(g, s->E, s->b1.h, s->b1.l, c->prm.dt, s->b0c, oh, ol, odb, c->st));
+  return SWAP_OK;
+}
+
+// maind.f:420-476: the plain subcycles, or the network in their place.  With
+// a network attached every sur_every-th step is judged: both run, the plain
+// result is kept, and a B error above the bound switches the network off
+// until a judged step passes.  Collecting: plain subcycles, and the pair
+// (inputs, mean corrector E) joins the network's training set.
+static int field_step(swap_ctx* c, F32State* s) {
+  const G32& g = s->g;
+  const bool judge = s->sur && s->sur_step % s->sur_every == 0;
+  const bool use_net = s->sur && !judge && !s->sur_off;
+  if (s->sur) ++s->sur_step;
+  if (use_net) {
+    TRY(sur_predict(c, s, s->b1p2.h, s->b1p2.l, s->db1p2));
+    // b12: B one subcycle before the end of the step, the leapfrog base of the next predictor
+    KL("f32_sur_B", df_lerp(g, s->b1p2.h, s->b1p2.l, s->b1.h, 1.0f / (float)c->prm.ntsub, s->b12.h, s->b12.l,
+                            c->st));
+    std::swap(s->b1, s->b1p2);
+    std::swap(s->db1, s->db1p2);
+    ++s->sur_used;
+    return SWAP_OK;
+  }
+  const bool collect = s->collect != nullptr;
+  if (collect || judge) {
+    TRY(sur_buffers(c, s));
+    CU(cudaMemsetAsync(s->e_sum, 0, 3 * (std::size_t)g.C * sizeof(float), c->st));
+  }
+  if (judge) TRY(sur_predict(c, s, s->jh, s->jl, s->jdb));
+  if (collect) KL("f32_sur_inputs", grid_to_voxels(g, s->db1, s->b0c, s->up, s->np, 1.0f, s->vin, c->st));
+  TRY(subcycles(c, s, (collect || judge) ? s->e_sum : nullptr));
+  if (collect) {
+    KL("f32_sur_target", grid_e_to_voxels(g, s->e_sum, (float)(1.0 / s->last_ntf), s->ve, c->st));
+    if (surr::add_sample(s->collect, g.ncx, g.ncy, g.ncz, s->vin, s->ve, c->st))
+      return c->fail(SWAP_EINVAL, std::string("surrogate: ") + surr::last_error(s->collect));
+  }
+  if (judge) {
+    double h[3];
+    KL("f32_sur_judge", judge_sums(g, s->jh, s->jl, s->b1.h, s->b1.l, s->b0c, s->jacc, c->st));
+    CU(cudaMemcpyAsync(h, s->jacc, sizeof(h), cudaMemcpyDeviceToHost, c->st));
+    CU(cudaStreamSynchronize(c->st));
+    s->sur_err_b = std::sqrt(h[0] / std::max(h[1], 1e-300));
+    s->sur_err_db = std::sqrt(h[0] / std::max(h[2], 1e-300));
+    ++s->sur_judged;
+    s->sur_off = s->sur_err_b > s->sur_bound;
+    if (s->sur_off) ++s->sur_fallbacks;
+  }
+  return SWAP_OK;
+}
+
 static int one_step(swap_ctx* c, F32State* s) {
   const G32& g = s->g;
   const StepParams sp = step_params(c, s, false);
@@ -450,7 +539,7 @@ static int one_step(swap_ctx* c, F32State* s) {
   // :404-413, the final half move of :479 and res_chex; prepares the sort
   KL("f32_P3", pass(3, g, p, s->sp, sp, s->start, s->kit, s->partial, s->dirrank, s->dep, c->d_err, c->st));
   TRY(finish_deposit(c, s, 4));
-  TRY(subcycles(c, s));                                                            // :420-476
+  TRY(field_step(c, s));                                                          // :420-476
   TRY(sort_step(c, s, c->src_step + 1, true));  // with the sources of the next step
   if (c->have_srcs) c->src_step++;
   return SWAP_OK;
@@ -644,5 +733,46 @@ int swap_f32_checkpoint(swap_ctx* c, std::FILE* f, bool write) {
     }
   }
   if (!write) s->ended = false;
+  return SWAP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// the surrogate on the FP32 form
+// ---------------------------------------------------------------------------
+
+extern "C" int swap_surrogate_collect(swap_surrogate* net, swap_ctx* c, int32_t nsteps) {
+  if (!net || !c || nsteps < 0) return SWAP_EINVAL;
+  F32State* s = f32(c);
+  if (!s || s->ended) return c->fail(SWAP_EINVAL, "swap_f32_begin has not been called");
+  s->collect = net;
+  int r = SWAP_OK;
+  for (int k = 0; k < nsteps && !r; ++k) r = one_step(c, s);
+  s->collect = nullptr;
+  return r ? r : check_err(c);
+}
+
+extern "C" int swap_surrogate_attach(swap_ctx* c, swap_surrogate* net, int32_t judge_every, double bound) {
+  if (!c) return SWAP_EINVAL;
+  F32State* s = f32(c);
+  if (!s) return c->fail(SWAP_EINVAL, "swap_f32_begin has not been called");
+  if (net && (judge_every < 1 || !(bound > 0))) return c->fail(SWAP_EINVAL, "judge_every >= 1 and bound > 0");
+  s->sur = net;
+  s->sur_every = judge_every;
+  s->sur_bound = bound;
+  s->sur_off = false;
+  s->sur_step = 0;
+  if (net) TRY(sur_buffers(c, s));
+  return SWAP_OK;
+}
+
+extern "C" int swap_surrogate_stats(swap_ctx* c, double out[5]) {
+  if (!c || !out) return SWAP_EINVAL;
+  F32State* s = f32(c);
+  if (!s) return c->fail(SWAP_EINVAL, "swap_f32_begin has not been called");
+  out[0] = (double)s->sur_used;
+  out[1] = (double)s->sur_judged;
+  out[2] = (double)s->sur_fallbacks;
+  out[3] = s->sur_err_b;
+  out[4] = s->sur_err_db;
   return SWAP_OK;
 }

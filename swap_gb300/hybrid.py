@@ -357,3 +357,101 @@ class Hybrid:
         dcell = np.ascontiguousarray(dcell, dtype=np.int32)
         self._check(self.lib.swap_f32_displace_resort(self.ctx, len(idx), idx.ctypes.data_as(abi.c_int64_p),
                                                       dcell.ctypes.data_as(abi.c_int32_p)))
+
+
+class Surrogate:
+    """The learned field-subcycle surrogate (a handle of the C-ABI)."""
+
+    LAYERS = ((16, 32), (32, 32), (32, 32), (32, 16))  # (cin, cout) of the 4 conv layers, padded
+
+    def __init__(self, seed: int = 1, max_samples: int = 4096):
+        self.lib = abi.load()
+        h = C.c_void_p()
+        abi.check(self.lib, None, self.lib.swap_surrogate_create(C.byref(h), int(seed), int(max_samples)))
+        self.h = h
+
+    def _check(self, code):
+        if code:
+            raise abi.SwapError(code, self.lib.swap_surrogate_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.swap_surrogate_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def collect(self, hybrid: "Hybrid", nsteps: int):
+        """nsteps plain FP32 steps of `hybrid` (after f32_begin), each a training pair."""
+        r = self.lib.swap_surrogate_collect(self.h, hybrid.ctx, int(nsteps))
+        if r:
+            raise abi.SwapError(r, self.lib.swap_last_error(hybrid.ctx).decode())
+
+    def samples(self) -> int:
+        n = C.c_int32()
+        self._check(self.lib.swap_surrogate_samples(self.h, C.byref(n)))
+        return n.value
+
+    def train(self, epochs: int, lr: float = 1e-3) -> float:
+        loss = C.c_double()
+        self._check(self.lib.swap_surrogate_train(self.h, int(epochs), float(lr), C.byref(loss)))
+        return loss.value
+
+    def loss(self) -> float:
+        loss = C.c_double()
+        self._check(self.lib.swap_surrogate_loss(self.h, C.byref(loss)))
+        return loss.value
+
+    def norm(self, mean=None, std=None, out_mean=None, out_std=None):
+        """Get (mean, std, out_mean, out_std) or set them: inputs are fed as
+        (x - mean)/std, the network predicts (E - out_mean)/out_std."""
+        a = [np.zeros(8, np.float32), np.ones(8, np.float32), np.zeros(3, np.float32), np.ones(3, np.float32)]
+        if mean is None:
+            self._check(self.lib.swap_surrogate_norm(self.h, *(x.ctypes.data for x in a), 0))
+            return tuple(a)
+        for x, v in zip(a, (mean, std, out_mean, out_std)):
+            x[:] = v
+        self._check(self.lib.swap_surrogate_norm(self.h, *(x.ctypes.data for x in a), 1))
+        return None
+
+    def weights(self, layer: int, w=None, b=None):
+        cin, cout = self.LAYERS[layer]
+        if w is None:
+            w = np.zeros((27, cout, cin), dtype=np.float32)
+            b = np.zeros(cout, dtype=np.float32)
+            self._check(self.lib.swap_surrogate_weights(self.h, layer, w.ctypes.data, b.ctypes.data, 0))
+            return w, b
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        b = np.ascontiguousarray(b, dtype=np.float32)
+        self._check(self.lib.swap_surrogate_weights(self.h, layer, w.ctypes.data, b.ctypes.data, 1))
+        return None
+
+    def grads(self, dims, vin_dev_ptr: int, tgt_dev_ptr: int):
+        """Loss and per-layer (gW, gb) for device inputs [V][8] and targets [V][3]."""
+        n = sum(27 * ci * co + co for ci, co in self.LAYERS)
+        g = np.zeros(n, dtype=np.float32)
+        loss = C.c_double()
+        self._check(self.lib.swap_surrogate_grads(self.h, *dims, vin_dev_ptr, tgt_dev_ptr, C.byref(loss), g.ctypes.data))
+        out, o = [], 0
+        for ci, co in self.LAYERS:
+            gw = g[o:o + 27 * ci * co].reshape(27, co, ci)
+            o += 27 * ci * co
+            out.append((gw, g[o:o + co].copy()))
+            o += co
+        return loss.value, out
+
+
+def attach_surrogate(h: "Hybrid", net, judge_every: int = 8, bound: float = 1e-3):
+    """Use `net` for the field subcycles of h's FP32 steps (None detaches)."""
+    h._check(h.lib.swap_surrogate_attach(h.ctx, None if net is None else net.h, int(judge_every), float(bound)))
+
+
+def surrogate_stats(h: "Hybrid") -> dict:
+    out = np.zeros(5)
+    h._check(h.lib.swap_surrogate_stats(h.ctx, abi.dptr(out)))
+    return {"net_steps": int(out[0]), "judged": int(out[1]), "fallbacks": int(out[2]), "err_b": out[3],
+            "err_db": out[4]}

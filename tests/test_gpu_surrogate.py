@@ -1,6 +1,9 @@
 """The surrogate's tensor-core kernels (tcgen05, BF16 in, FP32 accumulate)
-against CPU products of the same BF16 values.  Bar: rel 1e-5 of the product
-scale (FP32 accumulation of exact BF16 products)."""
+against CPU products of the same BF16 values, and its training gradients
+against float64 autograd on the CPU.  Bars: rel 1e-5 of the product scale for
+the kernels (FP32 accumulation of exact BF16 products); loss within 2e-3 and
+every layer's gradient within rel-L2 3e-2 (the GPU keeps BF16 activation and
+output gradients, the CPU reference rounds only the forward values)."""
 import numpy as np
 import pytest
 
@@ -42,8 +45,10 @@ def conv3_ref(X, W, bias, dims):
     return y + (bias.double() if bias is not None else 0.0)
 
 
+# rows shorter than a tile take the gather form; nx a multiple of 128 the halo form
 @pytest.mark.parametrize("cin,cout,dims", [(16, 32, (8, 8, 4)), (32, 32, (16, 8, 8)), (32, 16, (8, 4, 8)),
-                                           (16, 16, (32, 4, 2))])
+                                           (16, 16, (32, 4, 2)), (16, 32, (128, 4, 2)), (32, 32, (256, 3, 2)),
+                                           (32, 16, (128, 2, 3)), (16, 16, (384, 2, 2)), (32, 32, (128, 1, 1))])
 def test_conv3_matches_cpu(cin, cout, dims):
     import torch
 
@@ -62,5 +67,129 @@ def test_conv3_matches_cpu(cin, cout, dims):
     assert r == 0
     got = Yf.cpu().double()
     assert (got - want).abs().max().item() / want.abs().max().item() < 1e-5
-    gelu = torch.nn.functional.gelu(want)  # exact (erf) GELU, then bf16
+    gelu = torch.nn.functional.gelu(want, approximate="tanh")  # tanh-form GELU, then bf16
     assert (Y.cpu().double() - gelu).abs().max().item() <= 1e-2 * gelu.abs().max().item()
+
+
+def _ref_forward_backward(vin, tgt, layers, mean, std, out_mean, out_std, dims):
+    """The network in float64 on the CPU with the GPU's BF16 roundings of the
+    inputs, weights and hidden activations; loss and weight gradients."""
+    import torch
+    import torch.nn.functional as F
+
+    nx, ny, nz = dims
+    x = ((vin - mean) / std).float().to(torch.bfloat16).double()
+    x = torch.cat([x, torch.zeros(x.shape[0], 8, dtype=x.dtype)], 1)
+    params = []
+    h = x
+    for l, (w, b) in enumerate(layers):
+        W = torch.tensor(w).to(torch.bfloat16).double().requires_grad_(True)
+        B = torch.tensor(b).double().requires_grad_(True)
+        params.append((W, B))
+        cin, cout = W.shape[2], W.shape[1]
+        xi = h.T.reshape(1, cin, nz, ny, nx)
+        wk = W.reshape(3, 3, 3, cout, cin).permute(3, 4, 0, 1, 2)
+        z = F.conv3d(F.pad(xi, (1, 1, 1, 1, 1, 1), mode="circular"), wk).reshape(cout, -1).T + B
+        if l < len(layers) - 1:
+            y = F.gelu(z, approximate="tanh")
+            h = y + (y.detach().to(torch.bfloat16).double() - y.detach())  # BF16 value, exact gradient
+        else:
+            h = z
+    out = h[:, :3]
+    loss = 0.5 * ((out - (tgt - out_mean) / out_std) ** 2).mean()
+    loss.backward()
+    return loss.item(), [(W.grad.numpy(), B.grad.numpy()) for W, B in params]
+
+
+@pytest.mark.parametrize("dims", [(8, 8, 4), (128, 2, 2)])
+def test_surrogate_gradients_match_cpu(dims):
+    import torch
+
+    from swap_gb300.hybrid import Surrogate
+
+    V = dims[0] * dims[1] * dims[2]
+    net = Surrogate(seed=5)
+    g = torch.Generator().manual_seed(3)
+    vin = torch.randn(V, 8, generator=g, dtype=torch.float64)
+    tgt = torch.randn(V, 3, generator=g, dtype=torch.float64)
+    mean, std = np.full(8, 0.1), np.full(8, 1.5)
+    out_mean, out_std = np.array([0.5, -0.25, 0.0]), np.array([0.75, 0.5, 2.0])
+    net.norm(mean, std, out_mean, out_std)
+    layers = [net.weights(l) for l in range(4)]
+    T = torch.tensor
+    loss_ref, g_ref = _ref_forward_backward(vin, tgt, layers, T(mean), T(std), T(out_mean), T(out_std), dims)
+    dvin = vin.float().cuda()
+    dtgt = tgt.float().cuda()
+    loss, g_gpu = net.grads(dims, dvin.data_ptr(), dtgt.data_ptr())
+    assert abs(loss - loss_ref) <= 2e-3 * loss_ref
+    for l in range(4):
+        for a, b in zip(g_gpu[l], g_ref[l]):
+            err = np.linalg.norm(a - b) / np.linalg.norm(b)
+            assert err < 3e-2, (l, err)  # BF16 activations and gradients against float64
+
+
+def _trained(cells, ppc, collect, epochs, seed=3):
+    from helpers import make_hybrid
+    from swap_gb300.hybrid import Surrogate
+
+    h = make_hybrid(cells=cells, ppc=ppc, seed=seed, db=0.0)
+    h.f32_begin()
+    net = Surrogate(seed=2, max_samples=64)
+    net.collect(h, collect)
+    assert net.samples() == collect
+    l0 = net.loss()
+    l1 = net.train(epochs, lr=2e-3)
+    return h, net, l0, l1
+
+
+def test_surrogate_in_the_step_is_judged_and_falls_back():
+    """Collect -> train -> attach: judged steps stay within the bound and keep
+    div B; an impossible bound switches the network off at every judge."""
+    from swap_gb300.hybrid import attach_surrogate, surrogate_stats
+
+    h, net, l0, l1 = _trained((128, 16, 16), 8, collect=16, epochs=20)
+    assert l1 < 0.1 * l0, (l0, l1)
+    attach_surrogate(h, net, judge_every=4, bound=1e-2)
+    h.f32_run(12)
+    st = surrogate_stats(h)
+    assert (st["net_steps"], st["judged"], st["fallbacks"]) == (9, 3, 0), st
+    assert st["err_b"] < 1e-2
+    attach_surrogate(h, net, judge_every=2, bound=1e-12)
+    h.f32_run(6)
+    st = surrogate_stats(h)
+    # judged at steps 0, 2, 4, each above the bound: the network never runs
+    assert (st["net_steps"], st["judged"], st["fallbacks"]) == (9, 6, 3), st
+    attach_surrogate(h, None)
+    h.f32_end()
+    h.sync_to_host()
+    assert np.all(np.isfinite(h.b1))
+    assert h.max_abs_divB(h.b1) < 1e-5  # -dt curl E keeps div B where it was
+
+
+def test_surrogate_step_is_faster_than_the_subcycles():
+    """The gain: the same FP32 step with the network in place of the ten
+    field subcycles takes less time."""
+    import time
+
+    import torch
+
+    from swap_gb300.hybrid import attach_surrogate, surrogate_stats
+
+    h, net, _, _ = _trained((256, 32, 32), 4, collect=8, epochs=4)
+
+    def ms_per_step(n=10):
+        h.f32_run(2)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        h.f32_run(n)
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t) / n * 1e3
+
+    plain = ms_per_step()
+    attach_surrogate(h, net, judge_every=1000, bound=1.0)
+    h.f32_run(1)  # the judged first step
+    fast = ms_per_step()
+    assert surrogate_stats(h)["net_steps"] >= 12
+    attach_surrogate(h, None)
+    h.f32_end()
+    assert fast < 0.85 * plain, (fast, plain)
