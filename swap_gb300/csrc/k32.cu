@@ -1,13 +1,14 @@
 // k32.cu -- kernels of the FP32 form (see k32.cuh for the data layout).
 #include "k32.cuh"
 #include "philox.h"
+#include "tc05.cuh"
 
 namespace swapk32 {
 namespace {
 
 constexpr int TPB = 256;
 constexpr int TPB_PASS = 128;  // particle passes: keeps the shared tiles under 48 KB
-constexpr int KERR_DOMAIN = 3, KERR_CAPACITY = 4, KERR_MOVE = 7;
+constexpr int KERR_DOMAIN = 3, KERR_CAPACITY = 4, KERR_MOVE = 7, KERR_STAGE = 8;
 
 inline unsigned nblk(long long n, int tpb = TPB) {
   const long long b = (n + tpb - 1) / tpb;
@@ -122,14 +123,21 @@ __device__ __forceinline__ int dir_index(int dx, int dy, int dz) { return (dx + 
 //       the direction of every particle's new cell from its key's cell and
 //       its rank among the particles of that key and direction, in order.
 template <int PASS, bool CHEX = false>
-__global__ void __launch_bounds__(TPB_PASS) k_pass(G32 g, Part p, Species sp, StepParams sprm,
+__global__ void __launch_bounds__(TPB_PASS, PASS == 1 ? 8 : 6) k_pass(G32 g, Part p, Species sp, StepParams sprm,
                                               const int64_t* __restrict__ start, const float4* __restrict__ kit,
                                               float* __restrict__ partial, uint32_t* __restrict__ dirrank,
                                               uint16_t* __restrict__ dep, int* err) {
+  // the chunk's particles, copied in by the bulk-copy engine (double-buffered):
+  // offsets and v, plus vp1 in P1; cell words; species bytes
+  constexpr int NF = PASS == 1 ? 9 : 6;
+  __shared__ __align__(128) float s_f[2][NF][TPB_PASS];
+  __shared__ __align__(128) int32_t s_c[2][TPB_PASS];
+  __shared__ __align__(128) uint8_t s_s[2][TPB_PASS];
+  __shared__ uint64_t s_full[2];
   __shared__ float4 s_kit[PASS == 1 ? 2 : 2 * TNODES];
   __shared__ float s_dep[4 * TNODES];
-  __shared__ __align__(16) float s_red[TPB_PASS / 32][32][36];  // per warp: [value][particle], padded
-  __shared__ unsigned s_rank[PASS == 3 ? BCELLS * NDIR : 1];   // running count per (local key, direction)
+  __shared__ __align__(16) float s_red[TPB_PASS / 32][12][36];  // per warp: [8 weights, 4 moments][particle]
+  __shared__ uint16_t s_rank[PASS == 3 ? BCELLS * NDIR : 2];   // running count per (local key, direction)
   const long long b = blockIdx.x;
   const int bi = (int)(b % g.nbx), bj = (int)((b / g.nbx) % g.nby), bk = (int)(b / ((long long)g.nbx * g.nby));
   const int c0x = 4 * bi, c0y = 4 * bj, c0z = 4 * bk;
@@ -145,18 +153,51 @@ __global__ void __launch_bounds__(TPB_PASS) k_pass(G32 g, Part p, Species sp, St
   }
   for (int t = threadIdx.x; t < 4 * TNODES; t += blockDim.x) s_dep[t] = 0.0f;
   if (PASS == 3)
-    for (int t = threadIdx.x; t < BCELLS * NDIR; t += blockDim.x) s_rank[t] = 0u;
+    for (int t = threadIdx.x; t < BCELLS * NDIR; t += blockDim.x) s_rank[t] = 0;
+  if (threadIdx.x == 0) {
+    tc05::mbar_init(&s_full[0], 1);
+    tc05::mbar_init(&s_full[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
   __syncthreads();
 
   const float hdt = 0.5f * sprm.dt;
   const long long first = start[b * BCELLS], last = start[b * BCELLS + BCELLS];
+  // chunks of 128 particles from a 16-aligned start (every copy then starts
+  // on a 16-byte boundary); lanes outside [first, last) are masked
+  const long long a0 = first & ~15LL;
+  const int nchunk = last > first ? (int)((last - a0 + TPB_PASS - 1) / TPB_PASS) : 0;
+  // one thread copies chunk k's particle arrays into buffer k & 1
+  auto issue = [&](int k) {
+    const int u = k & 1;
+    const long long i0 = a0 + (long long)TPB_PASS * k;
+    constexpr uint32_t FB = TPB_PASS * 4;
+    tc05::mbar_expect_tx(&s_full[u], (NF + 1) * FB + (p.sp ? TPB_PASS : 0));
+    tc05::bulk_g2s(s_c[u], p.cell + i0, FB, &s_full[u]);
+    const float* src[9] = {p.ox, p.oy, p.oz, p.vx, p.vy, p.vz, p.wx, p.wy, p.wz};
+#pragma unroll
+    for (int f = 0; f < NF; ++f) tc05::bulk_g2s(s_f[u][f], src[f] + i0, FB, &s_full[u]);
+    if (p.sp) tc05::bulk_g2s(s_s[u], p.sp + i0, TPB_PASS, &s_full[u]);
+  };
+  if (threadIdx.x == 0 && nchunk > 0) issue(0);
   unsigned n_chex = 0;
   // warp-uniform trip count: every lane takes part in the deposit reduction
-  for (long long base = first; base < last; base += blockDim.x) {
-    const long long l = base + threadIdx.x;
-    const int32_t c = l < last ? p.cell[l] : CELL_DEAD;
-    bool live = c >= 0;  // past the range, or removed
-    if (PASS == 3 && dirrank && !live && l < last) dirrank[l] = DR_DEAD;
+  for (int kc = 0; kc < nchunk; ++kc) {
+    const int u = kc & 1;
+    bool got = true;
+    if (threadIdx.x == 0) got = tc05::mbar_wait(&s_full[u], (kc >> 1) & 1, 1u << 22);
+    // the barrier publishes the chunk to every thread and frees the other
+    // buffer (chunk kc-1 is done): the next copy goes there
+    if (__syncthreads_or(!got)) {
+      set_err(err, KERR_STAGE);
+      break;
+    }
+    if (threadIdx.x == 0 && kc + 1 < nchunk) issue(kc + 1);
+    const long long l = a0 + (long long)TPB_PASS * kc + threadIdx.x;
+    const bool mine = l >= first && l < last;
+    const int32_t c = mine ? s_c[u][threadIdx.x] : CELL_DEAD;
+    bool live = c >= 0;  // outside the range, or removed
+    if (PASS == 3 && dirrank && !live && mine) dirrank[l] = DR_DEAD;
     int t0 = -1;
     int grp = -1;  // P3: local key * NDIR + direction for the sort, -1 when not sorted
     float w8[8], qdv[4];
@@ -164,9 +205,9 @@ __global__ void __launch_bounds__(TPB_PASS) k_pass(G32 g, Part p, Species sp, St
       const bool fresh = (c & CELL_FRESH) != 0;
       int ci = pk_i(c), cj = pk_j(c), ck = pk_k(c);
       const int kl = (ci & 3) + 4 * (cj & 3) + 16 * (ck & 3);  // local key: the particle is in its key's cell
-      float ox = p.ox[l], oy = p.oy[l], oz = p.oz[l];
-      float vx = p.vx[l], vy = p.vy[l], vz = p.vz[l];
-      int s = p.sp ? min((int)p.sp[l], MAX_SPECIES - 1) : 0;
+      float ox = s_f[u][0][threadIdx.x], oy = s_f[u][1][threadIdx.x], oz = s_f[u][2][threadIdx.x];
+      float vx = s_f[u][3][threadIdx.x], vy = s_f[u][4][threadIdx.x], vz = s_f[u][5][threadIdx.x];
+      int s = p.sp ? min((int)s_s[u][threadIdx.x], MAX_SPECIES - 1) : 0;
       float mr = sp.mrat[s], qw = sp.qw[s];
       float dvx = 0.f, dvy = 0.f, dvz = 0.f;  // velocity deposited
       int rx = ci - c0x, ry = cj - c0y, rz = ck - c0z;
@@ -179,9 +220,10 @@ __global__ void __launch_bounds__(TPB_PASS) k_pass(G32 g, Part p, Species sp, St
             p.cell[l] = c & ~CELL_FRESH;
           }
         }
-        dvx = 1.5f * vx - 0.5f * p.wx[l];  // extrapol_up (gutsp.f:144)
-        dvy = 1.5f * vy - 0.5f * p.wy[l];
-        dvz = 1.5f * vz - 0.5f * p.wz[l];
+        // extrapol_up (gutsp.f:144)
+        dvx = 1.5f * vx - 0.5f * s_f[u][PASS == 1 ? 6 : 0][threadIdx.x];
+        dvy = 1.5f * vy - 0.5f * s_f[u][PASS == 1 ? 7 : 0][threadIdx.x];
+        dvz = 1.5f * vz - 0.5f * s_f[u][PASS == 1 ? 8 : 0][threadIdx.x];
       } else {
         // trilinear gather of (ajc-upc, btc) at the 8 corners (gutsp.f:217-251)
         const float wxl = 1.0f - ox, wxu = ox, wyl = 1.0f - oy, wyu = oy, wzl = 1.0f - oz, wzu = oz;
@@ -297,18 +339,16 @@ __global__ void __launch_bounds__(TPB_PASS) k_pass(G32 g, Part p, Species sp, St
         qdv[3] = qw * dvz;
       }
     }
-    // deposit (gutsp.f:1484-1491, 1704-1756): the warp's 32 particles x 32
-    // values (4 moments x 8 corners) go to shared memory as value-major
-    // rows; lane v then sums value v down the runs of particles that share
-    // a cell (sorted particles: usually one or two runs), with the run ends
-    // known to the whole warp, and adds each run's sum to the brick tile
-    // with one shared atomic.
+    // deposit (gutsp.f:1484-1491, 1704-1756): the warp's 32 particles' 8
+    // corner weights and 4 moments go to shared memory as value-major rows;
+    // lane v = (moment q, corner c) then sums w_c * m_q down the runs of
+    // particles that share a cell (sorted particles: usually one or two
+    // runs), with the run ends known to the whole warp, and adds each run's
+    // sum to the brick tile with one shared atomic.
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const float a = live ? qdv[q] : 0.0f;
+    for (int c8 = 0; c8 < 8; ++c8) s_red[warp][c8][lane] = live ? w8[c8] : 0.0f;
 #pragma unroll
-      for (int c8 = 0; c8 < 8; ++c8) s_red[warp][8 * q + c8][lane] = live ? w8[c8] * a : 0.0f;
-    }
+    for (int q = 0; q < 4; ++q) s_red[warp][8 + q][lane] = live ? qdv[q] : 0.0f;
     __syncwarp();
     const int tprev = __shfl_up_sync(0xffffffffu, t0, 1);
     const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || t0 != tprev);
@@ -316,19 +356,21 @@ __global__ void __launch_bounds__(TPB_PASS) k_pass(G32 g, Part p, Species sp, St
     const int qv = lane >> 3, cv = lane & 7;
     const int off = (cv & 1) + TN * (((cv >> 1) & 1) + TN * (cv >> 2));
     const bool add_here = PASS != 2 || qv != 0;
-    const float4* row = reinterpret_cast<const float4*>(s_red[warp][lane]);
+    const float4* wrow = reinterpret_cast<const float4*>(s_red[warp][cv]);
+    const float4* mrow = reinterpret_cast<const float4*>(s_red[warp][8 + qv]);
     float acc = 0.0f;
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {  // two halves of 16 rows, to bound the registers
-      float x[16];
+    for (int h = 0; h < 2; ++h) {  // two halves of 16 particles, to bound the registers
+      float x[16], m[16];
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        const float4 v = row[4 * h + q];
+        const float4 v = wrow[4 * h + q], w = mrow[4 * h + q];
         x[4 * q] = v.x; x[4 * q + 1] = v.y; x[4 * q + 2] = v.z; x[4 * q + 3] = v.w;
+        m[4 * q] = w.x; m[4 * q + 1] = w.y; m[4 * q + 2] = w.z; m[4 * q + 3] = w.w;
       }
 #pragma unroll
       for (int r = 0; r < 16; ++r) {
-        acc += x[r];
+        acc = fmaf(x[r], m[r], acc);
         if ((ends >> (16 * h + r)) & 1u) {
           const int tr = __shfl_sync(0xffffffffu, t0, 16 * h + r);
           if (add_here && tr >= 0) atomicAdd(&s_dep[qv * TNODES + tr + off], acc);
@@ -348,7 +390,7 @@ __global__ void __launch_bounds__(TPB_PASS) k_pass(G32 g, Part p, Species sp, St
           __syncwarp();
           if (grp >= 0) {
             dirrank[l] = ((uint32_t)(grp % NDIR) << 26) | (before + __popc(lt));
-            if (lt == 0) s_rank[grp] = before + __popc(peers);
+            if (lt == 0) s_rank[grp] = (uint16_t)(before + __popc(peers));
           }
         }
         __syncthreads();
@@ -936,6 +978,13 @@ __global__ void k_sort_scatter(G32 g, long long N, long long cap, const int32_t*
     const int32_t c = cell[l];
     const uint32_t dr = dirrank[l];
     if (dr == DR_DEAD) continue;
+    // every source field is read before the first store: the source and
+    // destination buffers are distinct, and loading them together keeps the
+    // ion's reads in flight at once instead of one per store
+    const float ox = s.ox[l], oy = s.oy[l], oz = s.oz[l];
+    const float vx = s.vx[l], vy = s.vy[l], vz = s.vz[l];
+    const float wx = s.wx[l], wy = s.wy[l], wz = s.wz[l];
+    const uint8_t spc = s.sp ? s.sp[l] : 0;
     const int dd = (int)(dr >> 26);
     if (dd >= NDIR) {
       set_err(err, KERR_MOVE);
@@ -948,10 +997,10 @@ __global__ void k_sort_scatter(G32 g, long long N, long long cap, const int32_t*
       continue;
     }
     d.cell[dst] = c;
-    d.ox[dst] = s.ox[l]; d.oy[dst] = s.oy[l]; d.oz[dst] = s.oz[l];
-    d.vx[dst] = s.vx[l]; d.vy[dst] = s.vy[l]; d.vz[dst] = s.vz[l];
-    d.wx[dst] = s.wx[l]; d.wy[dst] = s.wy[l]; d.wz[dst] = s.wz[l];
-    if (s.sp) d.sp[dst] = s.sp[l];
+    d.ox[dst] = ox; d.oy[dst] = oy; d.oz[dst] = oz;
+    d.vx[dst] = vx; d.vy[dst] = vy; d.vz[dst] = vz;
+    d.wx[dst] = wx; d.wy[dst] = wy; d.wz[dst] = wz;
+    if (s.sp) d.sp[dst] = spc;
   }
 }
 
@@ -963,16 +1012,21 @@ __global__ void k_new_scatter(G32 g, long long n_host, const int64_t* __restrict
   const long long n = n_host + (n_dev ? *n_dev : 0);
   GSTRIDE(q, n < n_max ? n : n_max) {
     const long long X = key[q];
+    const int32_t c = s.cell[q];  // all reads before the first store (see k_sort_scatter)
+    const float ox = s.ox[q], oy = s.oy[q], oz = s.oz[q];
+    const float vx = s.vx[q], vy = s.vy[q], vz = s.vz[q];
+    const float wx = s.wx[q], wy = s.wy[q], wz = s.wz[q];
+    const uint8_t spc = s.sp[q];
     const long long dst = start_new[X + 1] - ncount[X] + rank[q];
     if (dst < 0 || dst >= cap) {
       set_err(err, KERR_CAPACITY);
       continue;
     }
-    d.cell[dst] = s.cell[q] | CELL_FRESH;
-    d.ox[dst] = s.ox[q]; d.oy[dst] = s.oy[q]; d.oz[dst] = s.oz[q];
-    d.vx[dst] = s.vx[q]; d.vy[dst] = s.vy[q]; d.vz[dst] = s.vz[q];
-    d.wx[dst] = s.wx[q]; d.wy[dst] = s.wy[q]; d.wz[dst] = s.wz[q];
-    d.sp[dst] = s.sp[q];
+    d.cell[dst] = c | CELL_FRESH;
+    d.ox[dst] = ox; d.oy[dst] = oy; d.oz[dst] = oz;
+    d.vx[dst] = vx; d.vy[dst] = vy; d.vz[dst] = vz;
+    d.wx[dst] = wx; d.wy[dst] = wy; d.wz[dst] = wz;
+    d.sp[dst] = spc;
   }
 }
 
@@ -1129,11 +1183,16 @@ __global__ void k_sorted_hist(long long N, const int32_t* __restrict__ key, long
 __global__ void k_gather_perm(long long N, const int64_t* __restrict__ perm, Part s, Part d) {
   GSTRIDE(l, N) {
     const long long q = perm[l];
-    d.cell[l] = s.cell[q];
-    d.ox[l] = s.ox[q]; d.oy[l] = s.oy[q]; d.oz[l] = s.oz[q];
-    d.vx[l] = s.vx[q]; d.vy[l] = s.vy[q]; d.vz[l] = s.vz[q];
-    d.wx[l] = s.wx[q]; d.wy[l] = s.wy[q]; d.wz[l] = s.wz[q];
-    if (s.sp) d.sp[l] = s.sp[q];
+    const int32_t c = s.cell[q];  // all reads before the first store (see k_sort_scatter)
+    const float ox = s.ox[q], oy = s.oy[q], oz = s.oz[q];
+    const float vx = s.vx[q], vy = s.vy[q], vz = s.vz[q];
+    const float wx = s.wx[q], wy = s.wy[q], wz = s.wz[q];
+    const uint8_t spc = s.sp ? s.sp[q] : 0;
+    d.cell[l] = c;
+    d.ox[l] = ox; d.oy[l] = oy; d.oz[l] = oz;
+    d.vx[l] = vx; d.vy[l] = vy; d.vz[l] = vz;
+    d.wx[l] = wx; d.wy[l] = wy; d.wz[l] = wz;
+    if (s.sp) d.sp[l] = spc;
   }
 }
 

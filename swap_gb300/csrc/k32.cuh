@@ -32,6 +32,10 @@ struct G32 {
   double qx1, qy1, qz1;  // q(1) per axis
 };
 
+// Elements past the capacity that every particle array is allocated with:
+// the passes copy 128-ion chunks from 16-aligned starts.
+constexpr int PASS_PAD = 256;
+
 struct Part {
   int32_t* cell;
   float *ox, *oy, *oz;

@@ -114,6 +114,7 @@ static int check_err(swap_ctx* c) {
     if (herr == 4) return c->fail(SWAP_ECAPACITY, "Ni_max exceeded by new ions");
     if (herr == 7)
       return c->fail(SWAP_EMOVE, "a particle moved more than one cell per axis since the last sort (|v| dt > dx)");
+    if (herr == 8) return c->fail(SWAP_EWAIT, "a particle chunk copy did not complete within its wait limit");
     return c->fail(SWAP_ECUDA, "device error flag " + std::to_string(herr));
   }
   return SWAP_OK;
@@ -227,13 +228,15 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
 
   // allocations
   const std::size_t NMs = (std::size_t)std::max<long long>(NM, 1);
+  // the passes copy whole 128-ion chunks from 16-aligned starts: pad the arrays
+  const std::size_t NMp = NMs + PASS_PAD;
   for (int k = 0; k < 2; ++k) {
     Part& p = s->buf[k];
-    p.cell = s->alloc<int32_t>(NMs);
-    p.ox = s->alloc<float>(NMs); p.oy = s->alloc<float>(NMs); p.oz = s->alloc<float>(NMs);
-    p.vx = s->alloc<float>(NMs); p.vy = s->alloc<float>(NMs); p.vz = s->alloc<float>(NMs);
-    p.wx = s->alloc<float>(NMs); p.wy = s->alloc<float>(NMs); p.wz = s->alloc<float>(NMs);
-    p.sp = s->alloc<uint8_t>(NMs);
+    p.cell = s->alloc<int32_t>(NMp);
+    p.ox = s->alloc<float>(NMp); p.oy = s->alloc<float>(NMp); p.oz = s->alloc<float>(NMp);
+    p.vx = s->alloc<float>(NMp); p.vy = s->alloc<float>(NMp); p.vz = s->alloc<float>(NMp);
+    p.wx = s->alloc<float>(NMp); p.wy = s->alloc<float>(NMp); p.wz = s->alloc<float>(NMp);
+    p.sp = s->alloc<uint8_t>(NMp);
     if (!p.cell || !p.ox || !p.oy || !p.oz || !p.vx || !p.vy || !p.vz || !p.wx || !p.wy || !p.wz || !p.sp)
       return c->fail(SWAP_ECUDA, "FP32 particle allocation failed");
   }
