@@ -139,6 +139,12 @@ KERNEL_BYTES_F32 = {
     "f32_sort_scatter": 41 + 4 + 41,
     "f32_sort_prep": 4 + 4,
 }
+# DRAM bytes per particle that ncu measured for these kernels
+# (dram__bytes_read.sum + dram__bytes_write.sum over one launch at 128x64x64
+# cells, 16 ppc, 8.4M particles; profiles/k_pass_fp32_128x64x64_16ppc.md and
+# profiles/k_sort_scatter_fp32_128x64x64_16ppc.md); the roofline's traffic is
+# this figure times the particles of a launch.
+KERNEL_TRAFFIC_F32 = {"f32_P1": 45.3, "f32_P2": 35.1, "f32_P3": 77.1, "f32_sort_scatter": 86.0}
 # per interior node (FP32 fields, double-float B levels of 8 B per component)
 NODE_BYTES_F32 = {
     "f32_curlB": 12 + 4 + 12,
@@ -424,7 +430,11 @@ def run_ours(args):
         "gpu_launches": launches,
         "clocks": clk,
         "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "frac": (achieved / peak) if achieved else None,
+                     "traffic": (KERNEL_TRAFFIC_F32[top_name] * units if f32 and top_name in KERNEL_TRAFFIC_F32
+                                 else None),
+                     "traffic_source": "ncu DRAM bytes per particle at 128x64x64 cells x 16 ppc, times the "
+                                       "particles of one launch" if f32 and top_name in KERNEL_TRAFFIC_F32 else None,
                      "peak_source": "measured" if peaks else "fallback",
                      "bytes_per_unit": per_unit, "units_per_launch": units,
                      "note": None if f32 else "FP64 kernels on GB300 are bound by the FP64 pipe, not HBM"},
