@@ -480,10 +480,8 @@ __global__ void k_ct_up(G32 g, float* __restrict__ np, const float* __restrict__
 
 // Cell-centre B from the edge field (edge_to_center, grid_interp.f:35-51)
 // with xrat = yrat = zrat = 1/2 (uniform grid), at an interior node.
-__device__ __forceinline__ void e2c(const G32& g, const float* bt, int i, int j, int k, float& c1, float& c2,
-                                    float& c3) {
-  const long long C = g.C;
-  const long long o = nid(g, i, j, k), sx = 1, sy = g.nx, sz = (long long)g.nx * g.ny;
+__device__ __forceinline__ void e2c_o(const G32& g, const float* bt, long long o, float& c1, float& c2, float& c3) {
+  const long long C = g.C, sx = 1, sy = g.nx, sz = (long long)g.nx * g.ny;
   float b1, b2;
   b2 = 0.5f * (bt[o] + bt[o - sy]);
   b1 = 0.5f * (bt[o - sz] + bt[o - sy - sz]);
@@ -496,6 +494,10 @@ __device__ __forceinline__ void e2c(const G32& g, const float* bt, int i, int j,
   b2 = 0.5f * (B[o] + B[o - sy]);
   b1 = 0.5f * (B[o - sx] + B[o - sx - sy]);
   c3 = 0.5f * (b1 + b2);
+}
+__device__ __forceinline__ void e2c(const G32& g, const float* bt, int i, int j, int k, float& c1, float& c2,
+                                    float& c3) {
+  e2c_o(g, bt, nid(g, i, j, k), c1, c2, c3);
 }
 
 // Gather kit per physical node: (ajc - upc, btc) with ajc/upc =
@@ -554,12 +556,9 @@ constexpr int FBX = 32, FBY = 4;
 // Component m of aj = curl(dB)/(alpha * face-averaged np) at node (i,j,k)
 // (curlB, gutsf.f:202-239; curl b0 = 0 for the uniform b0).
 template <int m>
-__device__ __forceinline__ float aj_comp(const G32& g, const float* __restrict__ b, const float* __restrict__ np,
-                                         float alpha, int i, int j, int k) {
-  i = img(i, g.nx);
-  j = img(j, g.ny);
-  k = img(k, g.nz);
-  const long long C = g.C, o = nid(g, i, j, k), sx = 1, sy = g.nx, sz = (long long)g.nx * g.ny;
+__device__ __forceinline__ float aj_o(const G32& g, const float* __restrict__ b, const float* __restrict__ np,
+                                      float alpha, long long o) {
+  const long long C = g.C, sx = 1, sy = g.nx, sz = (long long)g.nx * g.ny;
   const float* B1 = b;
   const float* B2 = b + C;
   const float* B3 = b + 2 * C;
@@ -578,11 +577,35 @@ __device__ __forceinline__ float aj_comp(const G32& g, const float* __restrict__
   return c / (0.5f * (np[o] + np[o + s]) * alpha);
 }
 
+// Linear index of node (i+di, j+dj, k+dk) for |d| <= 1: by strides for a node
+// whose neighbours are all interior (INNER), else at the interior image.
+template <bool INNER>
+__device__ __forceinline__ long long nbr(const G32& g, long long o, int i, int j, int k, int di, int dj, int dk) {
+  if (INNER) return o + di + (long long)g.nx * (dj + (long long)g.ny * dk);
+  return nid(g, img(i + di, g.nx), img(j + dj, g.ny), img(k + dk, g.nz));
+}
+// a node at least one node away from every ghost plane
+__device__ __forceinline__ bool inner_node(const G32& g, int i, int j, int k) {
+  return i > 2 && i < g.nx - 1 && j > 2 && j < g.ny - 1 && k > 2 && k < g.nz - 1;
+}
+// store at an interior node, with its ghost images unless INNER
+template <bool INNER, class T>
+__device__ __forceinline__ void put(const G32& g, T* f, long long o, int i, int j, int k, T v) {
+  if (INNER) f[o] = v;
+  else store_img(g, f, i, j, k, v);
+}
+
 // curlB, face_to_center(aj - up) and the cross product of get_E (gutsf.f:
 // 1059-1075, crossf2 gutsf.f:65-76): writes aj and ct.  Predictor: B at
 // cell centres from edge_to_center of dB (grid_interp.f:35-51).  Corrector:
 // B at m+1/2 through edge_to_face then face_to_center (gutsf.f:1268-1269),
 // i.e. component m is the 1-2-1 average along axis m of edge_to_center.
+template <int m>
+__device__ __forceinline__ float aj_comp(const G32& g, const float* __restrict__ b, const float* __restrict__ np,
+                                         float alpha, int i, int j, int k) {
+  return aj_o<m>(g, b, np, alpha, nid(g, img(i, g.nx), img(j, g.ny), img(k, g.nz)));
+}
+
 template <bool CORR>
 __global__ void __launch_bounds__(FBX * FBY) k_aj_ct(G32 g, const float* __restrict__ db,
                                                      const float* __restrict__ np, const float* __restrict__ up,
@@ -629,12 +652,9 @@ __global__ void __launch_bounds__(FBX * FBY) k_aj_ct(G32 g, const float* __restr
 // Component m of E = face average of ct + nu*aj at node (i,j,k) (gutsf.f:
 // 94-96, 1082).
 template <int m>
-__device__ __forceinline__ float e_comp(const G32& g, const float* __restrict__ ct, const float* __restrict__ nu,
-                                        const float* __restrict__ aj, int i, int j, int k) {
-  i = img(i, g.nx);
-  j = img(j, g.ny);
-  k = img(k, g.nz);
-  const long long C = g.C, o = nid(g, i, j, k);
+__device__ __forceinline__ float e_o(const G32& g, const float* __restrict__ ct, const float* __restrict__ nu,
+                                     const float* __restrict__ aj, long long o) {
+  const long long C = g.C;
   const long long s = m == 0 ? 1 : (m == 1 ? (long long)g.nx : (long long)g.nx * g.ny);
   return 0.5f * (ct[o + C * m] + ct[o + s + C * m]) + nu[o] * aj[o + C * m];
 }
@@ -665,6 +685,48 @@ __device__ __forceinline__ void df_sub_mul(float bh, float bl, float ch, float c
 // gutsf.f:1349-1350 with coef = dtsub on b1) in double-float; dB of the
 // result in FP32.  Predictor: also dB at m+1/2 = (dB_new + dB1)/2
 // (gutsf.f:1210-1219).  WRITE_E: store E (the step's last corrector).
+template <bool PRED, bool WRITE_E, bool INNER>
+__device__ __forceinline__ void bstep_node(const G32& g, const float* __restrict__ ct, const float* __restrict__ nu,
+                                           const float* __restrict__ aj, const float* __restrict__ bh,
+                                           const float* __restrict__ bl, float ch, float cl,
+                                           const float* __restrict__ b0c, float* __restrict__ oh,
+                                           float* __restrict__ ol, float* __restrict__ dbo,
+                                           const float* __restrict__ db1, float* __restrict__ dbtp1,
+                                           float* __restrict__ E, float* __restrict__ e_acc, int i, int j, int k) {
+  const long long C = g.C, o = nid(g, i, j, k);
+  const long long ox = nbr<INNER>(g, o, i, j, k, 1, 0, 0), oy = nbr<INNER>(g, o, i, j, k, 0, 1, 0),
+                  oz = nbr<INNER>(g, o, i, j, k, 0, 0, 1);
+  const float e1 = e_o<0>(g, ct, nu, aj, o);
+  const float e2 = e_o<1>(g, ct, nu, aj, o);
+  const float e3 = e_o<2>(g, ct, nu, aj, o);
+  const float e1y = e_o<0>(g, ct, nu, aj, oy), e1z = e_o<0>(g, ct, nu, aj, oz);
+  const float e2x = e_o<1>(g, ct, nu, aj, ox), e2z = e_o<1>(g, ct, nu, aj, oz);
+  const float e3x = e_o<2>(g, ct, nu, aj, ox), e3y = e_o<2>(g, ct, nu, aj, oy);
+  const float ce[3] = {(e3y - e3) * g.inv_dy + (e2 - e2z) * g.inv_dz,
+                       (e3 - e3x) * g.inv_dx + (e1z - e1) * g.inv_dz,
+                       (e1 - e1y) * g.inv_dy + (e2x - e2) * g.inv_dx};
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    float rh, rl;
+    df_sub_mul(bh[o + C * m], bl[o + C * m], ch, cl, ce[m], rh, rl);
+    const float d = __fadd_rn(__fsub_rn(rh, b0c[m]), rl);
+    put<INNER>(g, oh + C * m, o, i, j, k, rh);
+    put<INNER>(g, ol + C * m, o, i, j, k, rl);
+    put<INNER>(g, dbo + C * m, o, i, j, k, d);
+    if (PRED) put<INNER>(g, dbtp1 + C * m, o, i, j, k, 0.5f * (d + db1[o + C * m]));
+  }
+  if (WRITE_E) {
+    put<INNER>(g, E, o, i, j, k, e1);
+    put<INNER>(g, E + C, o, i, j, k, e2);
+    put<INNER>(g, E + 2 * C, o, i, j, k, e3);
+  }
+  if (e_acc) {  // the sum of the correctors' E over a step: the surrogate's target
+    e_acc[o] += e1;
+    e_acc[o + C] += e2;
+    e_acc[o + 2 * C] += e3;
+  }
+}
+
 template <bool PRED, bool WRITE_E>
 __global__ void __launch_bounds__(FBX * FBY) k_bstep(G32 g, const float* __restrict__ ct,
                                                      const float* __restrict__ nu, const float* __restrict__ aj,
@@ -675,36 +737,11 @@ __global__ void __launch_bounds__(FBX * FBY) k_bstep(G32 g, const float* __restr
                                                      float* __restrict__ dbtp1, float* __restrict__ E,
                                                      float* __restrict__ e_acc) {
   FIELD_NODE(i, j, k);
-  const long long C = g.C, o = nid(g, i, j, k);
-  const float e1 = e_comp<0>(g, ct, nu, aj, i, j, k);
-  const float e2 = e_comp<1>(g, ct, nu, aj, i, j, k);
-  const float e3 = e_comp<2>(g, ct, nu, aj, i, j, k);
-  const float e1y = e_comp<0>(g, ct, nu, aj, i, j + 1, k), e1z = e_comp<0>(g, ct, nu, aj, i, j, k + 1);
-  const float e2x = e_comp<1>(g, ct, nu, aj, i + 1, j, k), e2z = e_comp<1>(g, ct, nu, aj, i, j, k + 1);
-  const float e3x = e_comp<2>(g, ct, nu, aj, i + 1, j, k), e3y = e_comp<2>(g, ct, nu, aj, i, j + 1, k);
-  const float ce[3] = {(e3y - e3) * g.inv_dy + (e2 - e2z) * g.inv_dz,
-                       (e3 - e3x) * g.inv_dx + (e1z - e1) * g.inv_dz,
-                       (e1 - e1y) * g.inv_dy + (e2x - e2) * g.inv_dx};
-#pragma unroll
-  for (int m = 0; m < 3; ++m) {
-    float rh, rl;
-    df_sub_mul(bh[o + C * m], bl[o + C * m], ch, cl, ce[m], rh, rl);
-    const float d = __fadd_rn(__fsub_rn(rh, b0c[m]), rl);
-    store_img(g, oh + C * m, i, j, k, rh);
-    store_img(g, ol + C * m, i, j, k, rl);
-    store_img(g, dbo + C * m, i, j, k, d);
-    if (PRED) store_img(g, dbtp1 + C * m, i, j, k, 0.5f * (d + db1[o + C * m]));
-  }
-  if (WRITE_E) {
-    store_img(g, E, i, j, k, e1);
-    store_img(g, E + C, i, j, k, e2);
-    store_img(g, E + 2 * C, i, j, k, e3);
-  }
-  if (e_acc) {  // the sum of the correctors' E over a step: the surrogate's target
-    e_acc[o] += e1;
-    e_acc[o + C] += e2;
-    e_acc[o + 2 * C] += e3;
-  }
+  if (inner_node(g, i, j, k))
+    bstep_node<PRED, WRITE_E, true>(g, ct, nu, aj, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E, e_acc, i, j, k);
+  else
+    bstep_node<PRED, WRITE_E, false>(g, ct, nu, aj, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E, e_acc, i, j,
+                                     k);
 }
 
 // B_new = base - coef * curl E for a given E (with ghost images), in
