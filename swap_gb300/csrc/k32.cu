@@ -369,14 +369,27 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 1 ? 8 : 6) k_pass(G32 g, Par
         m[4 * q] = w.x; m[4 * q + 1] = w.y; m[4 * q + 2] = w.z; m[4 * q + 3] = w.w;
       }
 #pragma unroll
-      for (int r = 0; r < 16; ++r) {
-        acc = fmaf(x[r], m[r], acc);
-        if ((ends >> (16 * h + r)) & 1u) {
-          const int tr = __shfl_sync(0xffffffffu, t0, 16 * h + r);
-          if (add_here && tr >= 0) atomicAdd(&s_dep[qv * TNODES + tr + off], acc);
-          acc = 0.0f;
+      for (int g4 = 0; g4 < 4; ++g4) {  // run ends are rare: test them per group of 4 particles
+        const unsigned e4 = ((ends & 0x7fffffffu) >> (16 * h + 4 * g4)) & 0xfu;
+        if (e4 == 0u) {
+#pragma unroll
+          for (int r = 4 * g4; r < 4 * g4 + 4; ++r) acc = fmaf(x[r], m[r], acc);
+        } else {
+#pragma unroll
+          for (int r = 4 * g4; r < 4 * g4 + 4; ++r) {
+            acc = fmaf(x[r], m[r], acc);
+            if ((e4 >> (r - 4 * g4)) & 1u) {
+              const int tr = __shfl_sync(0xffffffffu, t0, 16 * h + r);
+              if (add_here && tr >= 0) atomicAdd(&s_dep[qv * TNODES + tr + off], acc);
+              acc = 0.0f;
+            }
+          }
         }
       }
+    }
+    {  // the run that ends at the warp's last particle
+      const int tr = __shfl_sync(0xffffffffu, t0, 31);
+      if (add_here && tr >= 0) atomicAdd(&s_dep[qv * TNODES + tr + off], acc);
     }
     __syncwarp();
     if (PASS == 3 && dirrank) {
@@ -405,7 +418,9 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 1 ? 8 : 6) k_pass(G32 g, Par
   float* out = partial + b * (4 * TNODES);
   for (int t = threadIdx.x; t < 4 * TNODES; t += blockDim.x) out[t] = s_dep[t];
   if (PASS == 3 && dep)
-    for (int t = threadIdx.x; t < BCELLS * NDIR; t += blockDim.x) dep[b * (BCELLS * NDIR) + t] = (uint16_t)s_rank[t];
+    for (int t = threadIdx.x; t < BCELLS * NDIR; t += blockDim.x)  // direction-major: dep[dir][key]
+      dep[(long long)(t / BCELLS) * g.nkeys + b * BCELLS + t % BCELLS] =
+          (uint16_t)s_rank[(t % BCELLS) * NDIR + t / BCELLS];
 }
 
 // Sum, at every interior node, the brick tiles that cover it: along each axis
@@ -943,7 +958,7 @@ __global__ void k_sort_prep(G32 g, const int64_t* __restrict__ start, const int3
       }
       __syncwarp();
     }
-    if (lane < NDIR) dep[K * NDIR + lane] = (uint16_t)s_cnt[w][lane];
+    if (lane < NDIR) dep[(long long)lane * g.nkeys + K] = (uint16_t)s_cnt[w][lane];
     __syncwarp();
   }
 }
@@ -976,7 +991,7 @@ __global__ void __launch_bounds__(TPB) k_sort_count(G32 g, const uint16_t* __res
     int64_t n = 0;
 #pragma unroll
     for (int d = 0; d < NDIR; ++d) {
-      const unsigned c = dep[src_key(g, i, j, k, d) * NDIR + d];
+      const unsigned c = dep[(long long)d * g.nkeys + src_key(g, i, j, k, d)];
       s_cnt[d][threadIdx.x] = c;
       n += c;
     }

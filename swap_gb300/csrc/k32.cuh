@@ -124,7 +124,8 @@ __device__ __forceinline__ float offset_in_cell(double x, double q1, double d, i
 // P3: gather, Ep, v-/v+, vp1 = v, v = v+ + dt/2 Ep, half move, deposit np and
 //     up there (maind.f:404-413), the second half move (maind.f:479),
 //     outflow and res_chex; writes each particle's sort direction and rank
-//     (dirrank) and the per-key direction counts (dep) when those are given.
+//     (dirrank) and the per-key direction counts (dep, direction-major:
+//     dep[dir * nkeys + key]) when those are given.
 cudaError_t pass(int which, const G32& g, const Part& p, const Species& sp, const StepParams& sprm,
                  const int64_t* start, const float4* kit, float* partial, uint32_t* dirrank, uint16_t* dep, int* err,
                  cudaStream_t st);
@@ -169,6 +170,7 @@ cudaError_t courant_min(const G32& g, const float* dbt, const float* b0c, const 
                         float* dtn, float* d_min, cudaStream_t st);
 
 // ---- sort ----
+// Sort words and the direction-major counts dep[dir * nkeys + key] without pass 3.
 cudaError_t sort_prep(const G32& g, const int64_t* start, const int32_t* cell, uint32_t* dirrank, uint16_t* dep,
                       int* err, cudaStream_t st);
 // ncount (may be null): new ions per key, placed after the arrivals.  order:
