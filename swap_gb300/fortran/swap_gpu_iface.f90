@@ -41,6 +41,12 @@ module swap_gpu_iface
      real(c_double) :: cx_a, cx_b
   end type swap_sources_t
 
+  type, bind(C) :: swap_diag_spec_t
+     integer(c_int32_t) :: nt, nout, real_bytes, rank
+     real(c_double) :: dtsub_init, vtop, vbottom, mion, m_pu, m_heavy, np_top, np_bottom, b0_top, b0_bottom, &
+                       vth_top, vth_bottom
+  end type swap_diag_spec_t
+
   type(c_ptr), save :: swap_gpu_ctx = c_null_ptr
   ! The ion step number for the random draws of res_chex, whose reference
   ! argument list has none: set it to the main loop's m before the call.
@@ -224,6 +230,145 @@ module swap_gpu_iface
        type(c_ptr), value :: ctx
        real(c_double) :: xp(*), vp(*), np(*), temp_p(*)
      end function c_get_temperature
+     ! ---- whole steps (maind.f:379-484), the fused FP64 path
+     integer(c_int) function swap_ion_step(ctx) bind(C, name="swap_ion_step")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function swap_ion_step
+     integer(c_int) function swap_ion_step_pre(ctx) bind(C, name="swap_ion_step_pre")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function swap_ion_step_pre
+     integer(c_int) function swap_field_subcycles(ctx) bind(C, name="swap_field_subcycles")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function swap_field_subcycles
+     integer(c_int) function swap_ion_step_post(ctx) bind(C, name="swap_ion_step_post")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function swap_ion_step_post
+     integer(c_int) function swap_run(ctx, nsteps) bind(C, name="swap_run")
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), value :: nsteps
+     end function swap_run
+     integer(c_int) function swap_energy(ctx, out) bind(C, name="swap_energy")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: out(4)
+     end function swap_energy
+     integer(c_int) function swap_sync_to_device(ctx, a) bind(C, name="swap_sync_to_device")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx, a
+     end function swap_sync_to_device
+     integer(c_int) function swap_max_abs_divB(ctx, b, out) bind(C, name="swap_max_abs_divB")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: b(*), out
+     end function swap_max_abs_divB
+     integer(c_int) function swap_check_finite(ctx) bind(C, name="swap_check_finite")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function swap_check_finite
+     ! ---- the FP32 form: n whole steps on the device
+     integer(c_int) function swap_f32_begin(ctx) bind(C, name="swap_f32_begin")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function swap_f32_begin
+     integer(c_int) function swap_f32_run(ctx, nsteps) bind(C, name="swap_f32_run")
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), value :: nsteps
+     end function swap_f32_run
+     integer(c_int) function swap_f32_end(ctx) bind(C, name="swap_f32_end")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function swap_f32_end
+     integer(c_int) function swap_f32_energy(ctx, out) bind(C, name="swap_f32_energy")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: out(4)
+     end function swap_f32_energy
+     integer(c_int) function swap_f32_count(ctx, n) bind(C, name="swap_f32_count")
+       import :: c_int, c_ptr, c_int64_t
+       type(c_ptr), value :: ctx
+       integer(c_int64_t) :: n
+     end function swap_f32_count
+     ! ---- sources and sinks without a reference argument list of their own
+     integer(c_int) function swap_inflow_x(ctx, m_tstep) bind(C, name="swap_inflow_x")
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), value :: m_tstep
+     end function swap_inflow_x
+     integer(c_int) function swap_ionize_cloud(ctx, m_tstep) bind(C, name="swap_ionize_cloud")
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), value :: m_tstep
+     end function swap_ionize_cloud
+     integer(c_int) function swap_remove_outflow_x(ctx) bind(C, name="swap_remove_outflow_x")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function swap_remove_outflow_x
+     integer(c_int) function swap_chex_count(ctx, n) bind(C, name="swap_chex_count")
+       import :: c_int, c_ptr, c_int64_t
+       type(c_ptr), value :: ctx
+       integer(c_int64_t) :: n
+     end function swap_chex_count
+     integer(c_int) function swap_set_mion(ctx, mion) bind(C, name="swap_set_mion")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), value :: mion
+     end function swap_set_mion
+     ! ---- diagnostics writer (maind.f:237-358, 498-573)
+     integer(c_int) function swap_diag_open(ctx, out_dir, spec) bind(C, name="swap_diag_open")
+       import :: c_int, c_ptr, c_char, swap_diag_spec_t
+       type(c_ptr), value :: ctx
+       character(kind=c_char) :: out_dir(*)
+       type(swap_diag_spec_t) :: spec
+     end function swap_diag_open
+     integer(c_int) function swap_diag_step(ctx, m) bind(C, name="swap_diag_step")
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), value :: m
+     end function swap_diag_step
+     integer(c_int) function swap_diag_close(ctx) bind(C, name="swap_diag_close")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function swap_diag_close
+     ! ---- the learned field-subcycle surrogate of the FP32 form
+     integer(c_int) function swap_surrogate_create(net, seed, max_samples) bind(C, name="swap_surrogate_create")
+       import :: c_int, c_ptr, c_int64_t, c_int32_t
+       type(c_ptr) :: net
+       integer(c_int64_t), value :: seed
+       integer(c_int32_t), value :: max_samples
+     end function swap_surrogate_create
+     integer(c_int) function swap_surrogate_destroy(net) bind(C, name="swap_surrogate_destroy")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: net
+     end function swap_surrogate_destroy
+     integer(c_int) function swap_surrogate_collect(net, ctx, nsteps) bind(C, name="swap_surrogate_collect")
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: net, ctx
+       integer(c_int32_t), value :: nsteps
+     end function swap_surrogate_collect
+     integer(c_int) function swap_surrogate_train(net, epochs, lr, loss) bind(C, name="swap_surrogate_train")
+       import :: c_int, c_ptr, c_int32_t, c_double
+       type(c_ptr), value :: net
+       integer(c_int32_t), value :: epochs
+       real(c_double), value :: lr
+       real(c_double) :: loss
+     end function swap_surrogate_train
+     integer(c_int) function swap_surrogate_attach(ctx, net, judge_every, bound) bind(C, name="swap_surrogate_attach")
+       import :: c_int, c_ptr, c_int32_t, c_double
+       type(c_ptr), value :: ctx, net
+       integer(c_int32_t), value :: judge_every
+       real(c_double), value :: bound
+     end function swap_surrogate_attach
+     integer(c_int) function swap_surrogate_stats(ctx, out) bind(C, name="swap_surrogate_stats")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double) :: out(5)
+     end function swap_surrogate_stats
      integer(c_int) function swap_checkpoint_write(ctx, path) bind(C, name="swap_checkpoint_write")
        import :: c_int, c_ptr, c_char
        type(c_ptr), value :: ctx
