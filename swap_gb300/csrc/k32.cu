@@ -1003,7 +1003,7 @@ __global__ void __launch_bounds__(TPB) k_sort_count(G32 g, const uint16_t* __res
       unsigned run = 0;
       for (int r = 0; r < NDIR; ++r) {
         const int d = ord[r];
-        pre[X * NDIR + d] = (uint16_t)run;
+        pre[(long long)d * g.nkeys + X] = (uint16_t)run;  // direction-major: coalesced
         run += s_cnt[d][threadIdx.x];
       }
     } else {
@@ -1015,7 +1015,7 @@ __global__ void __launch_bounds__(TPB) k_sort_count(G32 g, const uint16_t* __res
         unsigned p = 0;
 #pragma unroll
         for (int q = 0; q < NDIR; ++q) p += sk[q] < sk[d] ? s_cnt[q][threadIdx.x] : 0u;
-        pre[X * NDIR + d] = (uint16_t)p;
+        pre[(long long)d * g.nkeys + X] = (uint16_t)p;
       }
     }
     count[X] = n;
@@ -1043,7 +1043,7 @@ __global__ void k_sort_scatter(G32 g, long long N, long long cap, const int32_t*
       continue;
     }
     const long long X = key_of(g, pk_i(c), pk_j(c), pk_k(c));
-    const long long dst = start_new[X] + pre[X * NDIR + dd] + (dr & ((1u << 26) - 1u));
+    const long long dst = start_new[X] + pre[(long long)dd * g.nkeys + X] + (dr & ((1u << 26) - 1u));
     if (dst < 0 || dst >= cap) {
       set_err(err, KERR_CAPACITY);
       continue;

@@ -174,7 +174,8 @@ cudaError_t courant_min(const G32& g, const float* dbt, const float* b0c, const 
 cudaError_t sort_prep(const G32& g, const int64_t* start, const int32_t* cell, uint32_t* dirrank, uint16_t* dep,
                       int* err, cudaStream_t st);
 // ncount (may be null): new ions per key, placed after the arrivals.  order:
-// the BCELLS x NDIR table of sort_order_table on the device.
+// the BCELLS x NDIR table of sort_order_table on the device.  pre is
+// direction-major: pre[dir * nkeys + key].
 cudaError_t sort_count(const G32& g, const uint16_t* dep, const int32_t* ncount, const uint8_t* order,
                        int64_t* count, uint16_t* pre, int* err, cudaStream_t st);
 // Directions by increasing source key for every place in a brick (host).
