@@ -110,6 +110,64 @@ __device__ __forceinline__ int step_cell(int c, int c0, int n) {
 
 __device__ __forceinline__ int dir_index(int dx, int dy, int dz) { return (dx + 1) + 3 * (dy + 1) + 9 * (dz + 1); }
 
+// The warp's deposit (gutsp.f:1484-1491, 1704-1756): the 32 particles' 8
+// corner weights and 4 moments go to shared memory as value-major rows; lane
+// v = (moment q, corner c) then sums w_c * m_q down the runs of particles
+// that share a cell (sorted particles: usually one or two runs), with the run
+// ends known to the whole warp (tested per group of four particles), and adds
+// each run's sum to the brick tile with one shared atomic.  t0: the tile index
+// of the particle's lower corner node, -1 when it deposits nothing.  ALL_Q:
+// every moment (otherwise the density, q = 0, is skipped).
+template <bool ALL_Q>
+__device__ __forceinline__ void warp_deposit(float (*red)[36], bool live, int t0, const float (&w8)[8],
+                                             const float (&qdv)[4], float* tile, int lane) {
+#pragma unroll
+  for (int c8 = 0; c8 < 8; ++c8) red[c8][lane] = live ? w8[c8] : 0.0f;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) red[8 + q][lane] = live ? qdv[q] : 0.0f;
+  __syncwarp();
+  const int tprev = __shfl_up_sync(0xffffffffu, t0, 1);
+  const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || t0 != tprev);
+  const unsigned ends = heads >> 1;  // the particle before each head (and, below, the last one)
+  const int qv = lane >> 3, cv = lane & 7;
+  const int off = (cv & 1) + TN * (((cv >> 1) & 1) + TN * (cv >> 2));
+  const bool add_here = ALL_Q || qv != 0;
+  const float4* wrow = reinterpret_cast<const float4*>(red[cv]);
+  const float4* mrow = reinterpret_cast<const float4*>(red[8 + qv]);
+  float acc = 0.0f;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {  // two halves of 16 particles, to bound the registers
+    float x[16], m[16];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float4 v = wrow[4 * h + q], w = mrow[4 * h + q];
+      x[4 * q] = v.x; x[4 * q + 1] = v.y; x[4 * q + 2] = v.z; x[4 * q + 3] = v.w;
+      m[4 * q] = w.x; m[4 * q + 1] = w.y; m[4 * q + 2] = w.z; m[4 * q + 3] = w.w;
+    }
+#pragma unroll
+    for (int g4 = 0; g4 < 4; ++g4) {
+      const unsigned e4 = (ends >> (16 * h + 4 * g4)) & 0xfu;
+      if (e4 == 0u) {
+#pragma unroll
+        for (int r = 4 * g4; r < 4 * g4 + 4; ++r) acc = fmaf(x[r], m[r], acc);
+      } else {
+#pragma unroll
+        for (int r = 4 * g4; r < 4 * g4 + 4; ++r) {
+          acc = fmaf(x[r], m[r], acc);
+          if ((e4 >> (r - 4 * g4)) & 1u) {
+            const int tr = __shfl_sync(0xffffffffu, t0, 16 * h + r);
+            if (add_here && tr >= 0) atomicAdd(&tile[qv * TNODES + tr + off], acc);
+            acc = 0.0f;
+          }
+        }
+      }
+    }
+  }
+  const int tr = __shfl_sync(0xffffffffu, t0, 31);  // the run that ends at the last particle
+  if (add_here && tr >= 0) atomicAdd(&tile[qv * TNODES + tr + off], acc);
+  __syncwarp();
+}
+
 // One CTA per brick; its particles are the contiguous range of the brick's
 // keys and lie in their key's cell (every move happens in pass 3, after
 // which the sort restores that).
@@ -134,9 +192,13 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 1 ? 8 : 6) k_pass(G32 g, Par
   __shared__ __align__(128) int32_t s_c[2][TPB_PASS];
   __shared__ __align__(128) uint8_t s_s[2][TPB_PASS];
   __shared__ uint64_t s_full[2];
-  __shared__ float4 s_kit[PASS == 1 ? 2 : 2 * TNODES];
+  // the field-gather tile: (aj-up, B_x) and (B_y, B_z) per node
+  __shared__ float4 s_kitA[PASS == 1 ? 1 : TNODES];
+  __shared__ float2 s_kitB[PASS == 1 ? 1 : TNODES];
   __shared__ float s_dep[4 * TNODES];
-  __shared__ __align__(16) float s_red[TPB_PASS / 32][12][36];  // per warp: [8 weights, 4 moments][particle]
+  // per warp: [8 weights, 4 moments][particle]; rows padded to 36 floats so
+  // that the 8 rows a reducing lane group reads start on different banks
+  __shared__ __align__(16) float s_red[TPB_PASS / 32][12][36];
   __shared__ uint16_t s_rank[PASS == 3 ? BCELLS * NDIR : 2];   // running count per (local key, direction)
   const long long b = blockIdx.x;
   const int bi = (int)(b % g.nbx), bj = (int)((b / g.nbx) % g.nby), bk = (int)(b / ((long long)g.nbx * g.nby));
@@ -147,8 +209,9 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 1 ? 8 : 6) k_pass(G32 g, Par
       const int tx = t % TN, ty = (t / TN) % TN, tz = t / (TN * TN);
       const int P = wrapi(c0x - 2 + tx, g.ncx), Q = wrapi(c0y - 2 + ty, g.ncy), R = wrapi(c0z - 2 + tz, g.ncz);
       const long long src = 2 * ((long long)P + (long long)g.ncx * (Q + (long long)g.ncy * R));
-      s_kit[2 * t] = kit[src];
-      s_kit[2 * t + 1] = kit[src + 1];
+      s_kitA[t] = kit[src];
+      const float4 hi = kit[src + 1];
+      s_kitB[t] = make_float2(hi.x, hi.y);
     }
   }
   for (int t = threadIdx.x; t < 4 * TNODES; t += blockDim.x) s_dep[t] = 0.0f;
@@ -237,7 +300,8 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 1 ? 8 : 6) k_pass(G32 g, Par
             for (int cx = 0; cx < 2; ++cx) {
               const float w = (cx ? wxu : wxl) * (cy ? wyu : wyl) * (cz ? wzu : wzl);
               const int t = tg + cx + TN * (cy + TN * cz);
-              const float4 f0 = s_kit[2 * t], f1 = s_kit[2 * t + 1];
+              const float4 f0 = s_kitA[t];
+              const float2 f1 = s_kitB[t];
               ax = fmaf(w, f0.x, ax); ay = fmaf(w, f0.y, ay); az = fmaf(w, f0.z, az);
               bx = fmaf(w, f0.w, bx); by = fmaf(w, f1.x, by); bz = fmaf(w, f1.y, bz);
             }
@@ -339,59 +403,7 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 1 ? 8 : 6) k_pass(G32 g, Par
         qdv[3] = qw * dvz;
       }
     }
-    // deposit (gutsp.f:1484-1491, 1704-1756): the warp's 32 particles' 8
-    // corner weights and 4 moments go to shared memory as value-major rows;
-    // lane v = (moment q, corner c) then sums w_c * m_q down the runs of
-    // particles that share a cell (sorted particles: usually one or two
-    // runs), with the run ends known to the whole warp, and adds each run's
-    // sum to the brick tile with one shared atomic.
-#pragma unroll
-    for (int c8 = 0; c8 < 8; ++c8) s_red[warp][c8][lane] = live ? w8[c8] : 0.0f;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) s_red[warp][8 + q][lane] = live ? qdv[q] : 0.0f;
-    __syncwarp();
-    const int tprev = __shfl_up_sync(0xffffffffu, t0, 1);
-    const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || t0 != tprev);
-    const unsigned ends = (heads >> 1) | 0x80000000u;  // the row before each head, and row 31
-    const int qv = lane >> 3, cv = lane & 7;
-    const int off = (cv & 1) + TN * (((cv >> 1) & 1) + TN * (cv >> 2));
-    const bool add_here = PASS != 2 || qv != 0;
-    const float4* wrow = reinterpret_cast<const float4*>(s_red[warp][cv]);
-    const float4* mrow = reinterpret_cast<const float4*>(s_red[warp][8 + qv]);
-    float acc = 0.0f;
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {  // two halves of 16 particles, to bound the registers
-      float x[16], m[16];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const float4 v = wrow[4 * h + q], w = mrow[4 * h + q];
-        x[4 * q] = v.x; x[4 * q + 1] = v.y; x[4 * q + 2] = v.z; x[4 * q + 3] = v.w;
-        m[4 * q] = w.x; m[4 * q + 1] = w.y; m[4 * q + 2] = w.z; m[4 * q + 3] = w.w;
-      }
-#pragma unroll
-      for (int g4 = 0; g4 < 4; ++g4) {  // run ends are rare: test them per group of 4 particles
-        const unsigned e4 = ((ends & 0x7fffffffu) >> (16 * h + 4 * g4)) & 0xfu;
-        if (e4 == 0u) {
-#pragma unroll
-          for (int r = 4 * g4; r < 4 * g4 + 4; ++r) acc = fmaf(x[r], m[r], acc);
-        } else {
-#pragma unroll
-          for (int r = 4 * g4; r < 4 * g4 + 4; ++r) {
-            acc = fmaf(x[r], m[r], acc);
-            if ((e4 >> (r - 4 * g4)) & 1u) {
-              const int tr = __shfl_sync(0xffffffffu, t0, 16 * h + r);
-              if (add_here && tr >= 0) atomicAdd(&s_dep[qv * TNODES + tr + off], acc);
-              acc = 0.0f;
-            }
-          }
-        }
-      }
-    }
-    {  // the run that ends at the warp's last particle
-      const int tr = __shfl_sync(0xffffffffu, t0, 31);
-      if (add_here && tr >= 0) atomicAdd(&s_dep[qv * TNODES + tr + off], acc);
-    }
-    __syncwarp();
+    warp_deposit<PASS != 2>(s_red[warp], live, t0, w8, qdv, s_dep, lane);
     if (PASS == 3 && dirrank) {
       // stable ranks per (key, direction): the warps of the CTA take their
       // turn in order, each adding its particles after the earlier ones
@@ -417,6 +429,7 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 1 ? 8 : 6) k_pass(G32 g, Par
   __syncthreads();
   float* out = partial + b * (4 * TNODES);
   for (int t = threadIdx.x; t < 4 * TNODES; t += blockDim.x) out[t] = s_dep[t];
+
   if (PASS == 3 && dep)
     for (int t = threadIdx.x; t < BCELLS * NDIR; t += blockDim.x)  // direction-major: dep[dir][key]
       dep[(long long)(t / BCELLS) * g.nkeys + b * BCELLS + t % BCELLS] =
@@ -1324,11 +1337,12 @@ __global__ void k_energy_f(G32 g, const double* __restrict__ b0, const float* __
 cudaError_t pass(int which, const G32& g, const Part& p, const Species& sp, const StepParams& s, const int64_t* start,
                  const float4* kit, float* partial, uint32_t* dirrank, uint16_t* dep, int* err, cudaStream_t st) {
   const unsigned grid = (unsigned)g.nbricks;
-  if (which == 1) RET((k_pass<1><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, partial, dirrank, dep, err)));
-  if (which == 2) RET((k_pass<2><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, partial, dirrank, dep, err)));
-  if (s.chex)
-    RET((k_pass<3, true><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, partial, dirrank, dep, err)));
-  RET((k_pass<3><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, partial, dirrank, dep, err)));
+#define PASS_ARGS g, p, sp, s, start, kit, partial, dirrank, dep, err
+  if (which == 1) RET((k_pass<1><<<grid, TPB_PASS, 0, st>>>(PASS_ARGS)));
+  if (which == 2) RET((k_pass<2><<<grid, TPB_PASS, 0, st>>>(PASS_ARGS)));
+  if (s.chex) RET((k_pass<3, true><<<grid, TPB_PASS, 0, st>>>(PASS_ARGS)));
+  RET((k_pass<3><<<grid, TPB_PASS, 0, st>>>(PASS_ARGS)));
+#undef PASS_ARGS
 }
 cudaError_t node_sum(const G32& g, const float* partial, int nq, float* np, float* S, cudaStream_t st) {
   RET((k_node_sum<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, partial, nq, np, S)));
@@ -1449,6 +1463,7 @@ cudaError_t new_scatter(const G32& g, long long n_host, const int64_t* n_dev, lo
   RET((k_new_scatter<<<nblk(n_max), TPB, 0, st>>>(g, n_host, n_dev, n_max, stage, key, rank, ncount, start_new, dst,
                                                   cap, err)));
 }
+
 cudaError_t scan_exclusive(const int64_t* in, int64_t* out, long long n, int64_t* sums, cudaStream_t st) {
   const long long nb = (n + SCAN_TILE - 1) / SCAN_TILE;
   k_scan_reduce<<<(unsigned)(nb < 1 ? 1 : nb), TPB, 0, st>>>(in, n, sums);
