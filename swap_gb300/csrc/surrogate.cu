@@ -224,13 +224,14 @@ __global__ void __launch_bounds__(128) k_conv3(ConvArgs a) {
 // 128).  A tile is 128 consecutive voxels of one x row.  A work unit is a
 // column of tiles (x segment, z) over a range of y; walking it in y, every
 // tile needs the rows y-1, y, y+1 of the planes z-1, z, z+1, each 130 voxels
-// long (one periodic neighbour on either side).  A ring of 4 y positions x 3
+// long (one periodic neighbour on either side).  A ring of 6 y positions x 3
 // z lines stays in shared memory as channel-group planes [group of 8
-// channels][row][8 values], so a tile loads only the 3 lines of one new y.
+// channels][row][8 values], so a tile loads only the 3 lines of one new y,
+// and the copies run three tiles ahead of the tensor core.
 // With rows 16 bytes apart in a plane, the A operand of tap (dx, dy, dz) is
 // the plane of ring slot y+dy, line dz, started dx + 1 rows in: a
 // descriptor offset, no copy per tap.  Two accumulators (64 tensor-memory
-// columns) let the copies for tile y+1 and the epilogue of tile y-1 run while
+// columns) let the epilogue of tile y-1 and the copies for tile y+3 run while
 // the tensor core works on tile y.  256 threads: all copy; thread 0 issues
 // the MMAs; warp w reads accumulator lanes 32*(w%4).. and half (w/4) of the
 // columns.
@@ -239,7 +240,7 @@ __global__ void __launch_bounds__(256) k_conv3r(ConvArgs a, int ychunk) {
   static_assert(CIN % 16 == 0 && (COUT == 16 || COUT == 32), "operand shapes");
   constexpr int KG = CIN / 8;                // channel groups (16 bytes each)
   constexpr int RP = KG == 2 ? 132 : 130;    // rows per plane; the padding spreads the copies over the banks
-  constexpr int PLANE = RP * 16, LINE = KG * PLANE, SLOT = 3 * LINE, NSLOT = 4;
+  constexpr int PLANE = RP * 16, LINE = KG * PLANE, SLOT = 3 * LINE, NSLOT = 6, AHEAD = 3;
   constexpr int WBYTES = 27 * COUT * CIN * 2;
   constexpr int RPT = 256 / KG, NPASS = (130 + RPT - 1) / RPT;  // rows per pass of the block, passes per line
   constexpr int HC = COUT / 2;               // accumulator columns per warp
@@ -272,7 +273,7 @@ __global__ void __launch_bounds__(256) k_conv3r(ConvArgs a, int ychunk) {
   long long zb[3];     // nx*ny*z' of the unit's three planes
   auto load_y = [&](int yv) {  // the three lines of y position yv (ny > yv >= -1 before wrapping)
     const int yy = yv < 0 ? yv + ny : (yv >= ny ? yv - ny : yv);
-    uint8_t* dst = sR + ((yv + NSLOT) & (NSLOT - 1)) * SLOT + kg * PLANE;
+    uint8_t* dst = sR + ((yv + NSLOT) % NSLOT) * SLOT + kg * PLANE;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       const __nv_bfloat16* src = a.X + (zb[d] + (long long)nx * yy) * CIN + kg * 8;
@@ -338,14 +339,20 @@ __global__ void __launch_bounds__(256) k_conv3r(ConvArgs a, int ychunk) {
       zz = zz < 0 ? zz + nz : (zz >= nz ? zz - nz : zz);
       zb[d] = (long long)nx * ny * zz;
     }
+    // lines y0-1 .. y0+1 for the first tile, then one group per later line
+    // up to AHEAD tiles ahead; every step commits one group (maybe empty)
     load_y(y0 - 1);
     load_y(y0);
     load_y(y0 + 1);
     tc05::cp_async_commit();
+    for (int a = 2; a <= AHEAD; ++a) {
+      if (y0 + a <= y1) load_y(y0 + a);
+      tc05::cp_async_commit();
+    }
     long long prev = -1;  // first voxel of the tile whose epilogue is pending
     for (int y = y0; y < y1; ++y, ++step) {
       const int b = (int)(step & 1);
-      tc05::cp_async_wait_all();  // this thread's copies are in shared memory
+      tc05::cp_async_wait<AHEAD - 1>();  // this thread's copies of tile y's lines are in shared memory
       tc05::fence_async_smem();   // and visible to the tensor core
       tc05::fence_before_sync();
       __syncthreads();
@@ -353,7 +360,7 @@ __global__ void __launch_bounds__(256) k_conv3r(ConvArgs a, int ychunk) {
       if (tid == 0) {
         uint32_t so[3];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) so[d] = (uint32_t)(((y + d - 1 + NSLOT) & (NSLOT - 1)) * SLOT);
+        for (int d = 0; d < 3; ++d) so[d] = (uint32_t)(((y + d - 1 + NSLOT) % NSLOT) * SLOT);
 #pragma unroll
         for (int t = 0; t < 27; ++t) {
 #pragma unroll
@@ -370,10 +377,9 @@ __global__ void __launch_bounds__(256) k_conv3r(ConvArgs a, int ychunk) {
         parity ^= 1u << (b ^ 1);
         tc05::fence_after_sync();
       }
-      if (y + 2 <= y1) {  // the new lines of tile y+1
-        load_y(y + 2);
-        tc05::cp_async_commit();
-      }
+      // the new line of tile y+AHEAD, into the slot of line y-2 (NSLOT = AHEAD + 3)
+      if (y + 1 + AHEAD <= y1) load_y(y + 1 + AHEAD);
+      tc05::cp_async_commit();
       if (prev >= 0) epilogue(prev, b ^ 1);
       tc05::fence_before_sync();
       prev = ((long long)z * ny + y) * nx + x0;
@@ -396,7 +402,7 @@ __global__ void __launch_bounds__(256) k_conv3r(ConvArgs a, int ychunk) {
 template <int CIN, int COUT>
 cudaError_t launch_conv3r(const ConvArgs& a, int nsm, cudaStream_t st) {
   constexpr int KG = CIN / 8, RP = KG == 2 ? 132 : 130;
-  const int smem = 27 * COUT * CIN * 2 + 4 * 3 * KG * RP * 16;
+  const int smem = 27 * COUT * CIN * 2 + 6 * 3 * KG * RP * 16;
   cudaError_t e = cudaFuncSetAttribute(k_conv3r<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   int per_sm = 1;
