@@ -1199,7 +1199,7 @@ __global__ void k_assign_species(long long N, const double* __restrict__ mrat, c
     for (int q = 0; q < n; ++q)
       if (tab_mrat[q] == mrat[l] && tab_bp[q] == beta_p[l]) { s = q; break; }
     if (s < 0) {
-      atomicCAS(miss, -1, (int)(l & 0x7fffffff));
+      atomicMin(miss, (int)(l & 0x7fffffff));  // the first particle of a pair not in the table
       s = 0;
     }
     spid[l] = (uint8_t)s;
@@ -1285,17 +1285,22 @@ __device__ __forceinline__ double bsum(double v) {
   return r;
 }
 
-__global__ void k_energy_p(long long N, Part p, Species sp, double vol, double* acc) {
-  double s = 0.0;
+// kf[q] = 0.5 m_q w_q for species q (m = 1/mrat, w = qw*vol the particle's
+// weight 1/(beta*beta_p)): kinetic energy kf * v^2, summed in FP32 per thread
+// (a thread sees a few hundred particles) and in FP64 across threads.
+struct KinFactor {
+  float k[MAX_SPECIES];
+};
+__global__ void k_energy_p(long long N, Part p, KinFactor kf, double* acc) {
+  float sf = 0.0f;
   GSTRIDE(l, N) {
     const int32_t c = p.cell[l];
     if (c < 0 || (c & CELL_FRESH)) continue;  // removed, or created for the coming step
     const int q = p.sp ? min((int)p.sp[l], MAX_SPECIES - 1) : 0;
-    const double v2 = (double)p.vx[l] * p.vx[l] + (double)p.vy[l] * p.vy[l] + (double)p.vz[l] * p.vz[l];
-    // 0.5 m v^2 with m = 1/mrat, times the particle's weight 1/(beta*beta_p) = qw*vol
-    s += 0.5 * (1.0 / (double)sp.mrat[q]) * v2 * (double)sp.qw[q] * vol;
+    const float vx = p.vx[l], vy = p.vy[l], vz = p.vz[l];
+    sf = fmaf(kf.k[q], fmaf(vx, vx, fmaf(vy, vy, vz * vz)), sf);
   }
-  s = bsum(s);
+  const double s = bsum((double)sf);
   if (threadIdx.x == 0) atomicAdd(acc, s);
 }
 
@@ -1486,6 +1491,14 @@ cudaError_t assign_species(long long N, const double* mrat, const double* beta_p
   if (N <= 0) return cudaSuccess;
   RET((k_assign_species<<<nblk(N), TPB, 0, st>>>(N, mrat, beta_p, tab_mrat, tab_bp, n, spid, miss)));
 }
+__global__ void k_not_uniform(long long C, const double* __restrict__ b, int* flag) {
+  GSTRIDE(t, 3 * C) {
+    if (b[t] != b[(t / C) * C]) atomicExch(flag, 1);
+  }
+}
+cudaError_t not_uniform(long long C, const double* b, int* flag, cudaStream_t st) {
+  RET((k_not_uniform<<<nblk(3 * C), TPB, 0, st>>>(C, b, flag)));
+}
 cudaError_t to_f64(const G32& g, long long N, long long NM, const Part& p, double* xp, double* vp, double* vp1,
                    cudaStream_t st) {
   if (N <= 0) return cudaSuccess;
@@ -1522,11 +1535,17 @@ cudaError_t energy32(const G32& g, long long N, const Part& p, const Species& sp
                      cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(acc4, 0, 4 * sizeof(double), st);
   if (e != cudaSuccess) return e;
+  const unsigned cap = 152 * 8;  // a few particles' worth of work per thread, few atomics
   if (N > 0) {
-    k_energy_p<<<nblk(N), TPB, 0, st>>>(N, p, sp, vol, acc4);
+    KinFactor kf{};
+    for (int q = 0; q < MAX_SPECIES && q < sp.n; ++q)
+      kf.k[q] = (float)(0.5 * (1.0 / (double)sp.mrat[q]) * (double)sp.qw[q] * vol);
+    const unsigned nb = nblk(N) < cap ? nblk(N) : cap;
+    k_energy_p<<<nb, TPB, 0, st>>>(N, p, kf, acc4);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
-  RET((k_energy_f<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, b0, b1h, b1l, E, alpha, vol, acc4)));
+  const long long nn = (long long)g.ncx * g.ncy * g.ncz;
+  RET((k_energy_f<<<nblk(nn) < cap ? nblk(nn) : cap, TPB, 0, st>>>(g, b0, b1h, b1l, E, alpha, vol, acc4)));
 }
 
 }  // namespace swapk32

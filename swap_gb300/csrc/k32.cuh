@@ -208,6 +208,9 @@ cudaError_t grid_f64_to_f32(long long n, const double* a, const double* b, float
 cudaError_t grid_f32_to_f64(long long n, const float* a, double* out, cudaStream_t st);
 cudaError_t assign_species(long long N, const double* mrat, const double* beta_p, const double* tab_mrat,
                            const double* tab_bp, int n, uint8_t* spid, int* miss, cudaStream_t st);
+// flag = 1 when a 3-component grid of C nodes per component is not uniform
+// (every node equal to node 0 of its component)
+cudaError_t not_uniform(long long C, const double* b, int* flag, cudaStream_t st);
 cudaError_t energy32(const G32& g, long long N, const Part& p, const Species& sp, double vol, const double* b0,
                      const float* b1h, const float* b1l, const float* E, double alpha, double* acc4,
                      cudaStream_t st);

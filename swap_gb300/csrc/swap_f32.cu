@@ -68,13 +68,32 @@ struct F32State {
   ~F32State() {
     srcops::stage_free(stage);
     for (void* p : owned) cudaFree(p);
+    release_pool();
   }
+  // device blocks of a previous state of the same context, handed back in
+  // allocation order while their sizes match (swap_f32_begin again on the
+  // same grid allocates nothing); the rest are freed by release_pool
+  std::vector<std::pair<void*, std::size_t>> pool;
+  std::size_t pool_next = 0;
+  std::vector<std::size_t> owned_bytes;
   template <class T>
   T* alloc(std::size_t n) {
+    const std::size_t bytes = n * sizeof(T) + 64;
     void* p = nullptr;
-    if (cudaMalloc(&p, n * sizeof(T) + 64) != cudaSuccess) return nullptr;
+    if (pool_next < pool.size() && pool[pool_next].second == bytes) {
+      p = pool[pool_next++].first;
+    } else {
+      release_pool();
+      if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+    }
     owned.push_back(p);
+    owned_bytes.push_back(bytes);
     return static_cast<T*>(p);
+  }
+  void release_pool() {
+    for (std::size_t q = pool_next; q < pool.size(); ++q) cudaFree(pool[q].first);
+    pool.clear();
+    pool_next = 0;
   }
 };
 
@@ -142,8 +161,14 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
   };
   if (!uniform(c->h_qx) || !uniform(c->h_qy) || !uniform(c->h_qz))
     return c->fail(SWAP_EINVAL, "the FP32 form needs a uniform grid on every axis");
-  swap_f32_free(c);
   auto* s = new F32State();
+  if (F32State* old = f32(c)) {  // reuse its device blocks (same grid: same sizes, same order)
+    for (std::size_t q = 0; q < old->owned.size(); ++q) s->pool.emplace_back(old->owned[q], old->owned_bytes[q]);
+    for (std::size_t q = old->pool_next; q < old->pool.size(); ++q) s->pool.push_back(old->pool[q]);
+    old->owned.clear();
+    old->pool.clear();
+    swap_f32_free(c);
+  }
   c->f32_state = s;
   G32& g = s->g;
   g.nx = nx; g.ny = ny; g.nz = nz;
@@ -172,31 +197,47 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
   const long long N = c->ntot(), NM = c->dims.ni_max;
   s->N = N;
 
-  // b0 must be uniform for the FP32 stencils (curl b0 = 0); read it back
-  std::vector<double> hb0(3 * (std::size_t)g.C);
-  CU(cudaMemcpy(hb0.data(), b0, hb0.size() * sizeof(double), cudaMemcpyDeviceToHost));
-  for (int m = 0; m < 3; ++m)
-    for (std::size_t o = 0; o < (std::size_t)g.C; ++o)
-      if (hb0[m * g.C + o] != hb0[m * g.C]) return c->fail(SWAP_EINVAL, "the FP32 form needs a uniform b0");
-  const float hb0c[3] = {(float)hb0[0], (float)hb0[g.C], (float)hb0[2 * g.C]};
-
-  // species table from the (mrat, beta_p) pairs present
-  std::vector<double> hm((std::size_t)N), hb((std::size_t)N);
-  if (N > 0) {
-    CU(cudaMemcpy(hm.data(), mrat, N * sizeof(double), cudaMemcpyDeviceToHost));
-    CU(cudaMemcpy(hb.data(), beta_p, N * sizeof(double), cudaMemcpyDeviceToHost));
+  // b0 must be uniform for the FP32 stencils (curl b0 = 0): checked on the device
+  double hb0v[3];
+  {
+    int* flag = s->alloc<int>(1);
+    if (!flag) return c->fail(SWAP_ECUDA, "allocation");
+    CU(cudaMemsetAsync(flag, 0, sizeof(int), c->st));
+    CU(not_uniform(g.C, b0, flag, c->st));
+    int hf = 0;
+    CU(cudaMemcpyAsync(&hf, flag, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    for (int m = 0; m < 3; ++m)
+      CU(cudaMemcpyAsync(&hb0v[m], b0 + m * g.C, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CU(cudaStreamSynchronize(c->st));
+    if (hf) return c->fail(SWAP_EINVAL, "the FP32 form needs a uniform b0");
   }
+  const float hb0c[3] = {(float)hb0v[0], (float)hb0v[1], (float)hb0v[2]};
+
+  // species table from the (mrat, beta_p) pairs present, in order of first
+  // appearance: found on the device, one pass per species (the first
+  // particle whose pair is not yet in the table adds it)
   std::vector<double> tm, tb;
-  for (long long l = 0; l < N; ++l) {
-    if (!tm.empty() && tm.back() == hm[l] && tb.back() == hb[l]) continue;
-    bool found = false;
-    for (std::size_t q = 0; q < tm.size(); ++q)
-      if (tm[q] == hm[l] && tb[q] == hb[l]) found = true;
-    if (!found) {
-      if (tm.size() == MAX_SPECIES) return c->fail(SWAP_ECAPACITY, "more than 16 (mrat, beta_p) species");
-      tm.push_back(hm[l]);
-      tb.push_back(hb[l]);
-    }
+  uint8_t* spid = s->alloc<uint8_t>((std::size_t)std::max<long long>(N, 1));
+  double* tabm = s->tabm = s->alloc<double>(MAX_SPECIES);
+  double* tabb = s->tabb = s->alloc<double>(MAX_SPECIES);
+  int* miss = s->alloc<int>(1);
+  if (!spid || !tabm || !tabb || !miss) return c->fail(SWAP_ECUDA, "allocation");
+  for (long long first = 0; N > 0 && first >= 0;) {
+    double pr[2];
+    CU(cudaMemcpyAsync(&pr[0], mrat + first, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CU(cudaMemcpyAsync(&pr[1], beta_p + first, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CU(cudaStreamSynchronize(c->st));
+    if (tm.size() == MAX_SPECIES) return c->fail(SWAP_ECAPACITY, "more than 16 (mrat, beta_p) species");
+    tm.push_back(pr[0]);
+    tb.push_back(pr[1]);
+    CU(cudaMemcpyAsync(tabm, tm.data(), tm.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CU(cudaMemcpyAsync(tabb, tb.data(), tb.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CU(cudaMemsetAsync(miss, 0x7f, sizeof(int), c->st));  // INT_MAX-like: no miss
+    CU(assign_species(N, mrat, beta_p, tabm, tabb, (int)tm.size(), spid, miss, c->st));
+    int hm = 0;
+    CU(cudaMemcpyAsync(&hm, miss, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CU(cudaStreamSynchronize(c->st));
+    first = hm == 0x7f7f7f7f ? -1 : hm;
   }
   if (tm.empty()) { tm.push_back(1.0); tb.push_back(1.0); }
   // species the sources create: ring ions, inflow, cloud ions, and the heavy
@@ -290,16 +331,10 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
   // particles: convert, assign species, sort by key (host counting sort, once)
   Part& tmp = s->buf[1];
   CU(from_f64(g, N, NM, xp, vp, vp1, mrat, beta_p, s->sp, tmp, c->d_err, c->st));
-  {
-    double* tabm = s->tabm = s->alloc<double>(MAX_SPECIES);
-    double* tabb = s->tabb = s->alloc<double>(MAX_SPECIES);
-    int* miss = s->alloc<int>(1);
-    if (!tabm || !tabb || !miss) return c->fail(SWAP_ECUDA, "allocation");
-    CU(cudaMemcpyAsync(tabm, tm.data(), tm.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
-    CU(cudaMemcpyAsync(tabb, tb.data(), tb.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
-    CU(cudaMemsetAsync(miss, 0xff, sizeof(int), c->st));
-    CU(assign_species(N, mrat, beta_p, tabm, tabb, (int)tm.size(), tmp.sp, miss, c->st));
-  }
+  if (N > 0) CU(cudaMemcpyAsync(tmp.sp, spid, (std::size_t)N, cudaMemcpyDeviceToDevice, c->st));
+  // the full table (with the sources' species) for the conversion back
+  CU(cudaMemcpyAsync(tabm, tm.data(), tm.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
+  CU(cudaMemcpyAsync(tabb, tb.data(), tb.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
   TRY(check_err(c));
   int32_t* keys = reinterpret_cast<int32_t*>(s->dirrank);
   CU(keys_of(g, N, tmp.cell, keys, c->st));

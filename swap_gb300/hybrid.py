@@ -118,13 +118,19 @@ class Hybrid:
         f = (lambda: self._pinned((NM, 3))) if pinned else (lambda: np.zeros((NM, 3), dtype=np.float64, order="F"))
         self.xp, self.vp, self.vp1 = f(), f(), f()
         self.Ep, self.vplus, self.vminus = f(), f(), f()
-        self.mrat = np.ones(NM, dtype=np.float64)
-        self.beta_p = np.ones(NM, dtype=np.float64)
+        self.mrat = self._pinned((NM,)) if pinned else np.zeros(NM, dtype=np.float64)
+        self.beta_p = self._pinned((NM,)) if pinned else np.zeros(NM, dtype=np.float64)
+        self.mrat[:] = 1.0
+        self.beta_p[:] = 1.0
         self.ijkp = np.zeros((NM, 3), dtype=np.int32, order="F")
         self.ni_tot = np.zeros(1, dtype=np.int32)
         # fields (maind.f:38-70)
         flds = grd6_setup(self.coords, cfg.b0, cfg.nu)
         for k, v in flds.items():
+            if pinned:
+                pv = self._pinned(v.shape)
+                pv[...] = v
+                v = pv
             setattr(self, k, v)
         self.input_p = np.zeros(3)
         ctx = C.c_void_p()
