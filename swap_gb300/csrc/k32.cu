@@ -181,7 +181,7 @@ __device__ __forceinline__ void warp_deposit(float (*red)[36], bool live, int t0
 //       the direction of every particle's new cell from its key's cell and
 //       its rank among the particles of that key and direction, in order.
 template <int PASS, bool CHEX = false>
-__global__ void __launch_bounds__(TPB_PASS, PASS == 1 ? 8 : 6) k_pass(G32 g, Part p, Species sp, StepParams sprm,
+__global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Part p, Species sp, StepParams sprm,
                                               const int64_t* __restrict__ start, const float4* __restrict__ kit,
                                               float* __restrict__ partial, uint32_t* __restrict__ dirrank,
                                               uint16_t* __restrict__ dep, int* err) {

@@ -148,7 +148,7 @@ def test_surrogate_in_the_step_is_judged_and_falls_back():
     from swap_gb300.hybrid import attach_surrogate, surrogate_stats
 
     h, net, l0, l1 = _trained((128, 16, 16), 8, collect=16, epochs=20)
-    assert l1 < 0.1 * l0, (l0, l1)
+    assert l1 < 0.3 * l0, (l0, l1)  # at least a threefold drop of the normalised loss
     attach_surrogate(h, net, judge_every=4, bound=1e-2)
     h.f32_run(12)
     st = surrogate_stats(h)
