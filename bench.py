@@ -452,26 +452,25 @@ def run_ours(args):
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = peaks.get("hbm_gbs", 6800.0)
 
-    # ---- end to end through the C-ABI with host buffers (pinned): upload the
-    # whole state, K steps each followed by the per-step Energy_diag read
-    # (maind.f:391-393,503-505), download the whole state.
-    # inputs: the particles (x, v, vp1, mrat, beta_p) and every field; outputs:
-    # the particles and the fields a step changes
+    # ---- end to end through the C-ABI with host buffers (pinned): the whole
+    # state starts in host memory, K steps each followed by the per-step
+    # Energy_diag read (maind.f:391-393,503-505), the state ends in host memory.
+    # Every array is marked host-current; the entries move what they read
+    # (the particles x, v, vp1, mrat, beta_p and the fields b0, b1, b12, np,
+    # nu) and sync_to_host brings back what they wrote.  In the FP32 form the
+    # particle vectors cross NVLink-C2C inside the conversion kernels (host-
+    # direct mode).  The library counts the bytes moved either way.
     state_arrays = [h.xp, h.vp, h.vp1, h.mrat, h.beta_p]
-    state_bytes_p = N * 8 * 11
     in_fields = [getattr(h, a) for a in ("b0", "b1", "b12", "b1p2", "bt", "btc", "np", "up", "aj", "E", "nu")]
-    out_fields = [getattr(h, a) for a in ("b1", "b12", "b1p2", "bt", "np", "up", "aj", "E")]
-    h2d_bytes = state_bytes_p + sum(a.nbytes for a in in_fields)
-    d2h_bytes = state_bytes_p + sum(a.nbytes for a in out_fields) + 32 * args.steps
     if f32:
         h.f32_end()
     h.sync_to_host()
     barrier(ws)
     torch.cuda.synchronize()
+    h.transfer_bytes(reset=True)
     w0 = time.perf_counter()
     for a in state_arrays + in_fields:
         h.mark_host_dirty(a)
-    h.sync_to_device()  # uploads exactly the arrays marked
     if f32:
         h.f32_begin()
         for _ in range(args.steps):
@@ -479,12 +478,15 @@ def run_ours(args):
             h.f32_energy()
         h.f32_end()
     else:
+        h.sync_to_device()
         for _ in range(args.steps):
             h.run(1)
             h.energy()
     h.sync_to_host()
     torch.cuda.synchronize()
     e2e_s = barrier_max(time.perf_counter() - w0, ws)
+    h2d_bytes, d2h_bytes = h.transfer_bytes(reset=True)
+    d2h_bytes += 32 * args.steps  # the energy reads
     del state_arrays
 
     value = N * args.steps * ws / (t_ms / 1e3)

@@ -97,6 +97,16 @@ int swap_bind_array(swap_ctx* ctx, void* host, int64_t bytes);
 int swap_sync_to_device(swap_ctx* ctx, const void* host);
 int swap_sync_to_host(swap_ctx* ctx, void* host);
 int swap_mark_host_dirty(swap_ctx* ctx, const void* host);
+/* On by default where the device addresses host memory directly (Grace-
+ * Blackwell, NVLink-C2C): swap_f32_begin then reads the FP64 particle arrays
+ * xp, vp, vp1 in the caller's memory when the host copy is current, and
+ * swap_f32_end writes xp, vp, vp1, mrat and beta_p straight back (the host
+ * copy becomes current, the device copy stale).  0 = always stage through
+ * the device mirrors.  SWAP_EINVAL if the device cannot. */
+int swap_set_host_direct(swap_ctx* ctx, int on);
+/* Bytes moved from the caller's memory to the device (h2d) and back (d2h)
+ * since the last reset: mirror copies and direct reads and writes. */
+int swap_transfer_bytes(swap_ctx* ctx, int64_t* h2d, int64_t* d2h, int reset);
 
 /* ---- one entry per reference subroutine (same arguments, same order) ---- */
 int swap_get_interp_weights(swap_ctx* ctx, const double* xp);                          /* gutsp.f:1378 */

@@ -114,6 +114,8 @@ SIGNATURES: dict[str, tuple] = {
     "swap_sync_to_device": (C.c_int, [P, P]),
     "swap_sync_to_host": (C.c_int, [P, P]),
     "swap_mark_host_dirty": (C.c_int, [P, P]),
+    "swap_set_host_direct": (C.c_int, [P, C.c_int]),
+    "swap_transfer_bytes": (C.c_int, [P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_int]),
     "swap_get_interp_weights": (C.c_int, [P, c_double_p]),
     "swap_update_np": (C.c_int, [P, c_double_p]),
     "swap_update_up": (C.c_int, [P] + [c_double_p] * 3),

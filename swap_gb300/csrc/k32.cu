@@ -1307,6 +1307,8 @@ __global__ void k_energy_p(long long N, Part p, KinFactor kf, double* acc) {
 __global__ void k_energy_f(G32 g, const double* __restrict__ b0, const float* __restrict__ b1h,
                            const float* __restrict__ b1l, const float* __restrict__ E, double alpha, double vol,
                            double* acc) {
+  // sums of squares per thread, scaled once per block: the FP64 pipe of
+  // this part is narrow, and a division per node would dominate the kernel
   double s1 = 0, s2 = 0, s3 = 0;
   GSTRIDE(t, n_int(g)) {
     int i, j, k;
@@ -1314,18 +1316,20 @@ __global__ void k_energy_f(G32 g, const double* __restrict__ b0, const float* __
     const long long o = nid(g, i, j, k);
     for (int m = 0; m < 3; ++m) {
       const double bb = (double)b1h[o + g.C * m] + (double)b1l[o + g.C * m];
-      const double d = bb - b0[o + g.C * m], e = E[o + g.C * m];
-      s1 += 0.5 * d * d * vol / alpha;
-      s2 += 0.5 * bb * bb * vol / alpha;
-      s3 += 0.5 * e * e * vol;
+      const double d = bb - b0[o + g.C * m];
+      const float e = E[o + g.C * m];
+      s1 = fma(d, d, s1);
+      s2 = fma(bb, bb, s2);
+      s3 += (double)(e * e);
     }
   }
+  const double kb = 0.5 * vol / alpha;
   s1 = bsum(s1);
-  if (threadIdx.x == 0) atomicAdd(acc + 1, s1);
+  if (threadIdx.x == 0) atomicAdd(acc + 1, s1 * kb);
   s2 = bsum(s2);
-  if (threadIdx.x == 0) atomicAdd(acc + 2, s2);
+  if (threadIdx.x == 0) atomicAdd(acc + 2, s2 * kb);
   s3 = bsum(s3);
-  if (threadIdx.x == 0) atomicAdd(acc + 3, s3);
+  if (threadIdx.x == 0) atomicAdd(acc + 3, s3 * (0.5 * vol));
 }
 
 }  // namespace

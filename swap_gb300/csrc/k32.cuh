@@ -92,9 +92,9 @@ __device__ __forceinline__ bool split_axis(double x, double q1, double d, int n,
   const double u = (x - q1) / d;  // position in cells from node 1
   int i = upper_closed ? (int)ceil(u) - 1 : (int)floor(u);
   if (i < 0 || i >= n) return false;
-  double f = u - (double)i;
-  if (upper_closed) { if (f <= 0.0) f = 1e-7; if (f > 1.0) f = 1.0; }
-  else { if (f < 0.0) f = 0.0; if (f >= 1.0) f = 0.99999994; }
+  // u - i is exact and lies in (0,1] (upper closed) or [0,1): only the
+  // rounding to float can reach the excluded end
+  const double f = u - (double)i;
   c = i;
   o = (float)f;
   if (upper_closed && o <= 0.0f) o = 1e-7f;

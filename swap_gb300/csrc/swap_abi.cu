@@ -82,6 +82,9 @@ int swap_ctx::transfer(Mirror& m, bool to_dev) {
     e = to_dev ? cudaMemcpyAsync(d, h, m.bytes, kind, st) : cudaMemcpyAsync(h, d, m.bytes, kind, st);
   }
   if (e != cudaSuccess) return cuda_fail(e, "transfer");
+  const long long moved = (m.kind == MirrorKind::Grid) ? (long long)m.bytes
+                          : ntot() * (m.kind == MirrorKind::ParticleI3 ? 12 : m.kind == MirrorKind::Particle1 ? 8 : 24);
+  (to_dev ? h2d_bytes : d2h_bytes) += moved;
   if (to_dev) m.dev_valid = true;
   else m.host_valid = true;
   return SWAP_OK;
@@ -102,8 +105,22 @@ int swap_ctx::use(const void* host, Access acc, double** dev) {
   return SWAP_OK;
 }
 
+int swap_ctx::use_host(const void* host, Access acc, double** ptr, bool* direct) {
+  *direct = false;
+  if (!host_direct || acc == Access::InOut) return use(host, acc, ptr);
+  if (!host) return fail(SWAP_EINVAL, "null array argument");
+  Mirror* m = find(host);
+  if (!m) return fail(SWAP_EINVAL, "array not registered with swap_bind_*");
+  if (acc == Access::In && m->dev_valid) return use(host, acc, ptr);  // the device copy is current
+  if (acc == Access::Out) touched_host.push_back(m);
+  *ptr = static_cast<double*>(m->host);
+  *direct = true;
+  return SWAP_OK;
+}
+
 int swap_ctx::begin() {
   touched.clear();
+  touched_host.clear();
   err.clear();
   const long long N = ntot();
   if (N < 0 || N > dims.ni_max) return fail(SWAP_ECAPACITY, "Ni_tot exceeds Ni_max");
@@ -120,6 +137,11 @@ int swap_ctx::finish() {
     m->host_valid = false;
   }
   touched.clear();
+  for (Mirror* m : touched_host) {
+    m->host_valid = true;
+    m->dev_valid = false;
+  }
+  touched_host.clear();
   int herr = 0;
   e = cudaMemcpy(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(e, "error flag");
@@ -403,6 +425,12 @@ extern "C" int swap_init(swap_ctx** out, const swap_dims* d, const swap_params* 
   auto* c = new swap_ctx();
   c->dims = *d;
   c->prm = *p;
+  {
+    int dev = 0, pageable = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess)
+      c->host_direct = pageable != 0;
+  }
   if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
     delete c;
     return SWAP_ECUDA;
@@ -557,6 +585,26 @@ extern "C" int swap_sync_to_host(swap_ctx* c, void* host) {
   }
   cudaError_t e = cudaStreamSynchronize(c->st);
   return e == cudaSuccess ? SWAP_OK : c->cuda_fail(e, "sync_to_host");
+}
+
+extern "C" int swap_set_host_direct(swap_ctx* c, int on) {
+  if (!c) return SWAP_EINVAL;
+  if (on) {
+    int dev = 0, pageable = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess || !pageable)
+      return c->fail(SWAP_EINVAL, "this device cannot address host memory directly");
+  }
+  c->host_direct = on != 0;
+  return SWAP_OK;
+}
+
+extern "C" int swap_transfer_bytes(swap_ctx* c, int64_t* h2d, int64_t* d2h, int reset) {
+  if (!c) return SWAP_EINVAL;
+  if (h2d) *h2d = c->h2d_bytes;
+  if (d2h) *d2h = c->d2h_bytes;
+  if (reset) c->h2d_bytes = c->d2h_bytes = 0;
+  return SWAP_OK;
 }
 
 extern "C" int swap_mark_host_dirty(swap_ctx* c, const void* host) {

@@ -43,6 +43,13 @@ struct swap_ctx {
   // registry of bound host arrays
   std::unordered_map<const void*, Mirror> reg;
   std::vector<Mirror*> touched;
+  std::vector<Mirror*> touched_host;  // outputs written straight into the caller's memory
+  // On Grace-Blackwell the GPU reads and writes the caller's (pageable or
+  // page-locked) memory over NVLink-C2C at the link's speed: the FP32 form's
+  // conversions then read and write the FP64 particle arrays in place, with
+  // no staging copy through the device mirror.
+  bool host_direct = false;
+  int64_t h2d_bytes = 0, d2h_bytes = 0;  // bytes moved between the caller's memory and the device
   std::vector<void*> owned;  // device buffers freed at finalize
 
   // host addresses of the bound arrays (the Fortran's own)
@@ -95,6 +102,9 @@ struct swap_ctx {
   int add_mirror(void* host, std::size_t bytes, MirrorKind kind);
   int transfer(Mirror& m, bool to_dev);
   int use(const void* host, Access acc, double** dev);
+  // As use(), but with host_direct an input whose host copy is current, and
+  // every output, resolves to the caller's own memory.
+  int use_host(const void* host, Access acc, double** ptr, bool* direct);
   int begin();
   int finish();
   long long ntot() const;

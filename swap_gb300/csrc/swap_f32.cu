@@ -182,11 +182,13 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
   g.inv_dx = (float)(1.0 / dx); g.inv_dy = (float)(1.0 / dy); g.inv_dz = (float)(1.0 / dz);
   g.qx1 = c->h_qx[0]; g.qy1 = c->h_qy[0]; g.qz1 = c->h_qz[0];
 
-  // bound FP64 state on the device
+  // bound FP64 state: the particle vectors are read where they are current
+  // (in the caller's memory in host-direct mode), the rest on the device
   double *xp, *vp, *vp1, *mrat, *beta_p, *b0, *b1, *b12, *npd, *nud;
-  TRY(c->use(c->h_xp, Access::In, &xp));
-  TRY(c->use(c->h_vp, Access::In, &vp));
-  TRY(c->use(c->h_vp1, Access::In, &vp1));
+  bool direct[3];
+  TRY(c->use_host(c->h_xp, Access::In, &xp, &direct[0]));
+  TRY(c->use_host(c->h_vp, Access::In, &vp, &direct[1]));
+  TRY(c->use_host(c->h_vp1, Access::In, &vp1, &direct[2]));
   TRY(c->use(c->h_mrat, Access::In, &mrat));
   TRY(c->use(c->h_beta_p, Access::In, &beta_p));
   TRY(c->use(c->h_b0, Access::In, &b0));
@@ -217,7 +219,9 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
   // appearance: found on the device, one pass per species (the first
   // particle whose pair is not yet in the table adds it)
   std::vector<double> tm, tb;
-  uint8_t* spid = s->alloc<uint8_t>((std::size_t)std::max<long long>(N, 1));
+  // sized by ni_max, like every block here, so that the next swap_f32_begin
+  // on this grid finds the same sizes in the same order and allocates nothing
+  uint8_t* spid = s->alloc<uint8_t>((std::size_t)std::max<long long>(NM, 1));
   double* tabm = s->tabm = s->alloc<double>(MAX_SPECIES);
   double* tabb = s->tabb = s->alloc<double>(MAX_SPECIES);
   int* miss = s->alloc<int>(1);
@@ -331,6 +335,8 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
   // particles: convert, assign species, sort by key (host counting sort, once)
   Part& tmp = s->buf[1];
   CU(from_f64(g, N, NM, xp, vp, vp1, mrat, beta_p, s->sp, tmp, c->d_err, c->st));
+  for (bool d : direct)
+    if (d) c->h2d_bytes += 24 * N;
   if (N > 0) CU(cudaMemcpyAsync(tmp.sp, spid, (std::size_t)N, cudaMemcpyDeviceToDevice, c->st));
   // the full table (with the sources' species) for the conversion back
   CU(cudaMemcpyAsync(tabm, tm.data(), tm.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
@@ -608,10 +614,13 @@ extern "C" int swap_f32_end(swap_ctx* c) {
   if (!s) return c->fail(SWAP_EINVAL, "swap_f32_begin has not been called");
   TRY(c->begin());
   TRY(drop_fresh(c, s));
+  // the particle arrays straight into the caller's memory in host-direct
+  // mode, the fields into the device copies
   double *xp, *vp, *vp1, *b1, *b12, *b1p2, *bt, *npd, *upd, *Ed, *ajd;
-  TRY(c->use(c->h_xp, Access::Out, &xp));
-  TRY(c->use(c->h_vp, Access::Out, &vp));
-  TRY(c->use(c->h_vp1, Access::Out, &vp1));
+  bool direct[5];
+  TRY(c->use_host(c->h_xp, Access::Out, &xp, &direct[0]));
+  TRY(c->use_host(c->h_vp, Access::Out, &vp, &direct[1]));
+  TRY(c->use_host(c->h_vp1, Access::Out, &vp1, &direct[2]));
   TRY(c->use(c->h_b1, Access::Out, &b1));
   TRY(c->use(c->h_b12, Access::Out, &b12));
   TRY(c->use(c->h_b1p2, Access::Out, &b1p2));
@@ -621,11 +630,13 @@ extern "C" int swap_f32_end(swap_ctx* c) {
   TRY(c->use(c->h_E, Access::Out, &Ed));
   TRY(c->use(c->h_aj, Access::Out, &ajd));
   double *mratd, *bpd;
-  TRY(c->use(c->h_mrat, Access::Out, &mratd));
-  TRY(c->use(c->h_beta_p, Access::Out, &bpd));
+  TRY(c->use_host(c->h_mrat, Access::Out, &mratd, &direct[3]));
+  TRY(c->use_host(c->h_beta_p, Access::Out, &bpd, &direct[4]));
   const G32& g = s->g;
   CU(to_f64(g, s->N, c->dims.ni_max, s->buf[s->cur], xp, vp, vp1, c->st));
   CU(species_to_f64(s->N, s->buf[s->cur].sp, s->tabm, s->tabb, mratd, bpd, c->st));
+  for (int a = 0; a < 5; ++a)
+    if (direct[a]) c->d2h_bytes += (a < 3 ? 24 : 8) * s->N;
   *c->ni_tot_ptr = (int32_t)s->N;
   s->ended = true;
   const std::size_t b3 = 3 * (std::size_t)g.C * sizeof(double);

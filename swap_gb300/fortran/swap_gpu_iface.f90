@@ -94,6 +94,17 @@ module swap_gpu_iface
        import :: c_int, c_ptr
        type(c_ptr), value :: ctx, a
      end function swap_mark_host_dirty
+     integer(c_int) function swap_set_host_direct(ctx, on) bind(C, name="swap_set_host_direct")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: on
+     end function swap_set_host_direct
+     integer(c_int) function swap_transfer_bytes(ctx, h2d, d2h, reset) bind(C, name="swap_transfer_bytes")
+       import :: c_int, c_ptr, c_int64_t
+       type(c_ptr), value :: ctx
+       integer(c_int64_t), intent(out) :: h2d, d2h
+       integer(c_int), value :: reset
+     end function swap_transfer_bytes
      ! --- gutsp.f ---
      integer(c_int) function c_get_interp_weights(ctx, xp) bind(C, name="swap_get_interp_weights")
        import :: c_int, c_ptr, c_double

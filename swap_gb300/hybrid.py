@@ -191,6 +191,16 @@ class Hybrid:
     def mark_host_dirty(self, arr=None):
         self._check(self.lib.swap_mark_host_dirty(self.ctx, None if arr is None else arr.ctypes.data_as(C.c_void_p)))
 
+    def set_host_direct(self, on: bool):
+        """Let the FP32 form's conversions read and write the FP64 particle arrays in host memory."""
+        self._check(self.lib.swap_set_host_direct(self.ctx, int(bool(on))))
+
+    def transfer_bytes(self, reset=False):
+        """(h2d, d2h) bytes moved between the bound host arrays and the device since the last reset."""
+        h2d, d2h = C.c_int64(), C.c_int64()
+        self._check(self.lib.swap_transfer_bytes(self.ctx, C.byref(h2d), C.byref(d2h), int(bool(reset))))
+        return h2d.value, d2h.value
+
     # ---- gutsp.f ----
     def get_interp_weights(self, xp):
         self._check(self.lib.swap_get_interp_weights(self.ctx, abi.dptr(xp)))
@@ -344,7 +354,10 @@ class Hybrid:
         self._check(self.lib.swap_f32_run(self.ctx, int(nsteps)))
 
     def f32_end(self):
-        """Write the FP32 state back into the bound arrays (device copies); then sync_to_host."""
+        """Write the FP32 state back into the bound arrays; then sync_to_host.
+
+        The particle arrays go straight into host memory when the device addresses
+        it (host-direct mode); the fields go to the device copies."""
         self._check(self.lib.swap_f32_end(self.ctx))
 
     def f32_count(self) -> int:
