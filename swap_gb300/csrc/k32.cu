@@ -508,8 +508,10 @@ __global__ void k_ct_up(G32 g, float* __restrict__ np, const float* __restrict__
 
 // Cell-centre B from the edge field (edge_to_center, grid_interp.f:35-51)
 // with xrat = yrat = zrat = 1/2 (uniform grid), at an interior node.
-__device__ __forceinline__ void e2c_o(const G32& g, const float* bt, long long o, float& c1, float& c2, float& c3) {
-  const long long C = g.C, sx = 1, sy = g.nx, sz = (long long)g.nx * g.ny;
+// I: the offset type, 32-bit unsigned where every offset of the call fits
+template <class I = long long>
+__device__ __forceinline__ void e2c_o(const G32& g, const float* bt, I o, float& c1, float& c2, float& c3) {
+  const I C = (I)g.C, sx = 1, sy = (I)g.nx, sz = (I)g.nx * (I)g.ny;
   float b1, b2;
   b2 = 0.5f * (bt[o] + bt[o - sy]);
   b1 = 0.5f * (bt[o - sz] + bt[o - sy - sz]);
@@ -583,15 +585,15 @@ constexpr int FBX = 32, FBY = 4;
 
 // Component m of aj = curl(dB)/(alpha * face-averaged np) at node (i,j,k)
 // (curlB, gutsf.f:202-239; curl b0 = 0 for the uniform b0).
-template <int m>
+template <int m, class I = long long>
 __device__ __forceinline__ float aj_o(const G32& g, const float* __restrict__ b, const float* __restrict__ np,
-                                      float alpha, long long o) {
-  const long long C = g.C, sx = 1, sy = g.nx, sz = (long long)g.nx * g.ny;
+                                      float alpha, I o) {
+  const I C = (I)g.C, sx = 1, sy = (I)g.nx, sz = (I)g.nx * (I)g.ny;
   const float* B1 = b;
   const float* B2 = b + C;
   const float* B3 = b + 2 * C;
   float c;
-  long long s;
+  I s;
   if (m == 0) {
     c = (B3[o] - B3[o - sy]) * g.inv_dy + (B2[o - sz] - B2[o]) * g.inv_dz;
     s = sx;
@@ -602,7 +604,9 @@ __device__ __forceinline__ float aj_o(const G32& g, const float* __restrict__ b,
     c = (B2[o] - B2[o - sx]) * g.inv_dx + (B1[o - sy] - B1[o]) * g.inv_dy;
     s = sz;
   }
-  return c / (0.5f * (np[o] + np[o + s]) * alpha);
+  // the fast divide (two ulps): the denominator, a density times alpha, is
+  // far from the range where it loses accuracy
+  return __fdividef(c, 0.5f * (np[o] + np[o + s]) * alpha);
 }
 
 // Linear index of node (i+di, j+dj, k+dk) for |d| <= 1: by strides for a node
@@ -640,6 +644,47 @@ __global__ void __launch_bounds__(FBX * FBY) k_aj_ct(G32 g, const float* __restr
                                                      const float* __restrict__ b0c, float alpha,
                                                      float* __restrict__ aj, float* __restrict__ ct) {
   FIELD_NODE(i, j, k);
+  if (inner_node(g, i, j, k)) {
+    // every neighbour interior and no ghost image to store: strides, 32-bit
+    // offsets (3 C < 2^32), the same arithmetic as below
+    using U = unsigned;
+    const U C = (U)g.C, o = (U)nid(g, i, j, k), sy = (U)g.nx, sz = (U)g.nx * (U)g.ny;
+    const float a1 = aj_o<0, U>(g, db, np, alpha, o);
+    const float a2 = aj_o<1, U>(g, db, np, alpha, o);
+    const float a3 = aj_o<2, U>(g, db, np, alpha, o);
+    const float a1m = aj_o<0, U>(g, db, np, alpha, o - 1);
+    const float a2m = aj_o<1, U>(g, db, np, alpha, o - sy);
+    const float a3m = aj_o<2, U>(g, db, np, alpha, o - sz);
+    aj[o] = a1;
+    aj[o + C] = a2;
+    aj[o + 2 * C] = a3;
+    const float ax = 0.5f * ((a1 - up[o]) + (a1m - up[o - 1]));
+    const float ay = 0.5f * ((a2 - up[o + C]) + (a2m - up[o - sy + C]));
+    const float az = 0.5f * ((a3 - up[o + 2 * C]) + (a3m - up[o - sz + 2 * C]));
+    float bx, by, bz;
+    if (!CORR) {
+      e2c_o<U>(g, db, o, bx, by, bz);
+    } else {
+      float c1, c2, c3, m1, m2, m3, p1, p2, p3, d1, d2;
+      e2c_o<U>(g, db, o, c1, c2, c3);
+      e2c_o<U>(g, db, o - 1, m1, d1, d2);
+      e2c_o<U>(g, db, o + 1, p1, d1, d2);
+      e2c_o<U>(g, db, o - sy, d1, m2, d2);
+      e2c_o<U>(g, db, o + sy, d1, p2, d2);
+      e2c_o<U>(g, db, o - sz, d1, d2, m3);
+      e2c_o<U>(g, db, o + sz, d1, d2, p3);
+      bx = 0.25f * (m1 + 2.0f * c1 + p1);
+      by = 0.25f * (m2 + 2.0f * c2 + p2);
+      bz = 0.25f * (m3 + 2.0f * c3 + p3);
+    }
+    bx += b0c[0];
+    by += b0c[1];
+    bz += b0c[2];
+    ct[o] = ay * bz - az * by;
+    ct[o + C] = az * bx - ax * bz;
+    ct[o + 2 * C] = ax * by - ay * bx;
+    return;
+  }
   const long long C = g.C, o = nid(g, i, j, k), sx = 1, sy = g.nx, sz = (long long)g.nx * g.ny;
   const float a1 = aj_comp<0>(g, db, np, alpha, i, j, k);
   const float a2 = aj_comp<1>(g, db, np, alpha, i, j, k);
