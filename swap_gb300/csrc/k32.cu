@@ -118,16 +118,23 @@ __device__ __forceinline__ int dir_index(int dx, int dy, int dz) { return (dx + 
 // each run's sum to the brick tile with one shared atomic.  t0: the tile index
 // of the particle's lower corner node, -1 when it deposits nothing.  ALL_Q:
 // every moment (otherwise the density, q = 0, is skipped).
-template <bool ALL_Q>
+// MOVERS (pass 3, which deposits after a half move): the runs follow trun,
+// the particle's cell before the move (sorted, so runs stay long), and the
+// few particles that changed cell (mover) take no part in them; each of
+// those then adds its 32 values to the tile directly, one per lane.
+template <bool ALL_Q, bool MOVERS = false>
 __device__ __forceinline__ void warp_deposit(float (*red)[36], bool live, int t0, const float (&w8)[8],
-                                             const float (&qdv)[4], float* tile, int lane) {
+                                             const float (&qdv)[4], float* tile, int lane, int trun = -1,
+                                             bool mover = false) {
+  const bool in_runs = live && !(MOVERS && mover);
 #pragma unroll
   for (int c8 = 0; c8 < 8; ++c8) red[c8][lane] = live ? w8[c8] : 0.0f;
 #pragma unroll
-  for (int q = 0; q < 4; ++q) red[8 + q][lane] = live ? qdv[q] : 0.0f;
+  for (int q = 0; q < 4; ++q) red[8 + q][lane] = in_runs ? qdv[q] : 0.0f;
   __syncwarp();
-  const int tprev = __shfl_up_sync(0xffffffffu, t0, 1);
-  const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || t0 != tprev);
+  const int key = MOVERS ? trun : t0;
+  const int tprev = __shfl_up_sync(0xffffffffu, key, 1);
+  const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || key != tprev);
   const unsigned ends = heads >> 1;  // the particle before each head (and, below, the last one)
   const int qv = lane >> 3, cv = lane & 7;
   const int off = (cv & 1) + TN * (((cv >> 1) & 1) + TN * (cv >> 2));
@@ -155,7 +162,7 @@ __device__ __forceinline__ void warp_deposit(float (*red)[36], bool live, int t0
         for (int r = 4 * g4; r < 4 * g4 + 4; ++r) {
           acc = fmaf(x[r], m[r], acc);
           if ((e4 >> (r - 4 * g4)) & 1u) {
-            const int tr = __shfl_sync(0xffffffffu, t0, 16 * h + r);
+            const int tr = __shfl_sync(0xffffffffu, key, 16 * h + r);
             if (add_here && tr >= 0) atomicAdd(&tile[qv * TNODES + tr + off], acc);
             acc = 0.0f;
           }
@@ -163,8 +170,25 @@ __device__ __forceinline__ void warp_deposit(float (*red)[36], bool live, int t0
       }
     }
   }
-  const int tr = __shfl_sync(0xffffffffu, t0, 31);  // the run that ends at the last particle
+  const int tr = __shfl_sync(0xffffffffu, key, 31);  // the run that ends at the last particle
   if (add_here && tr >= 0) atomicAdd(&tile[qv * TNODES + tr + off], acc);
+  if (MOVERS) {
+    unsigned mv = __ballot_sync(0xffffffffu, live && mover);
+    if (mv) {
+      __syncwarp();
+      if (live && mover) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) red[8 + q][lane] = qdv[q];
+      }
+      __syncwarp();
+      while (mv) {
+        const int m = __ffs(mv) - 1;
+        mv &= mv - 1;
+        const int tm = __shfl_sync(0xffffffffu, t0, m);
+        if (add_here) atomicAdd(&tile[qv * TNODES + tm + off], red[cv][m] * red[8 + qv][m]);
+      }
+    }
+  }
   __syncwarp();
 }
 
@@ -262,6 +286,8 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
     bool live = c >= 0;  // outside the range, or removed
     if (PASS == 3 && dirrank && !live && mine) dirrank[l] = DR_DEAD;
     int t0 = -1;
+    int t0o = -1;       // P3: tile index of the cell before the move
+    bool mover = false;  // P3: deposits in another cell than its own
     int grp = -1;  // P3: local key * NDIR + direction for the sort, -1 when not sorted
     float w8[8], qdv[4];
     if (live) {
@@ -274,6 +300,7 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
       float mr = sp.mrat[s], qw = sp.qw[s];
       float dvx = 0.f, dvy = 0.f, dvz = 0.f;  // velocity deposited
       int rx = ci - c0x, ry = cj - c0y, rz = ck - c0z;
+      if (PASS == 3) t0o = (rx + 1) + TN * ((ry + 1) + TN * (rz + 1));
       if (PASS == 1) {
         if (fresh) {
           if (sprm.drop_fresh) {  // created for a step that is not taken
@@ -393,6 +420,7 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
       }
       if (live) {
         t0 = (rx + 1) + TN * ((ry + 1) + TN * (rz + 1));
+        mover = PASS == 3 && t0 != t0o;
         const float wxl = 1.0f - ox, wxu = ox, wyl = 1.0f - oy, wyu = oy, wzl = 1.0f - oz, wzu = oz;
 #pragma unroll
         for (int cc = 0; cc < 8; ++cc)
@@ -403,7 +431,7 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
         qdv[3] = qw * dvz;
       }
     }
-    warp_deposit<PASS != 2>(s_red[warp], live, t0, w8, qdv, s_dep, lane);
+    warp_deposit<PASS != 2, PASS == 3>(s_red[warp], live, t0, w8, qdv, s_dep, lane, t0o, mover);
     if (PASS == 3 && dirrank) {
       // stable ranks per (key, direction): the warps of the CTA take their
       // turn in order, each adding its particles after the earlier ones
