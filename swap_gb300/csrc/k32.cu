@@ -302,14 +302,7 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
       int rx = ci - c0x, ry = cj - c0y, rz = ck - c0z;
       if (PASS == 3) t0o = (rx + 1) + TN * ((ry + 1) + TN * (rz + 1));
       if (PASS == 1) {
-        if (fresh) {
-          if (sprm.drop_fresh) {  // created for a step that is not taken
-            live = false;
-            p.cell[l] = CELL_DEAD;
-          } else {
-            p.cell[l] = c & ~CELL_FRESH;
-          }
-        }
+        if (fresh) p.cell[l] = c & ~CELL_FRESH;
         // extrapol_up (gutsp.f:144)
         dvx = 1.5f * vx - 0.5f * s_f[u][PASS == 1 ? 6 : 0][threadIdx.x];
         dvy = 1.5f * vy - 0.5f * s_f[u][PASS == 1 ? 7 : 0][threadIdx.x];
@@ -1300,6 +1293,13 @@ __global__ void k_species_to_f64(long long N, const uint8_t* __restrict__ spid, 
   }
 }
 
+__global__ void k_drop_fresh(long long N, int32_t* __restrict__ cell) {
+  GSTRIDE(l, N) {
+    const int32_t c = cell[l];
+    if (c >= 0 && (c & CELL_FRESH)) cell[l] = CELL_DEAD;
+  }
+}
+
 __global__ void k_keys(G32 g, long long N, const int32_t* __restrict__ cell, int32_t* __restrict__ key) {
   GSTRIDE(l, N) {
     const int32_t c = cell[l];
@@ -1585,6 +1585,10 @@ cudaError_t species_to_f64(long long N, const uint8_t* spid, const double* tab_m
                            double* mrat, double* beta_p, cudaStream_t st) {
   if (N <= 0) return cudaSuccess;
   RET((k_species_to_f64<<<nblk(N), TPB, 0, st>>>(N, spid, tab_mrat, tab_bp, mrat, beta_p)));
+}
+cudaError_t drop_fresh_cells(long long N, int32_t* cell, cudaStream_t st) {
+  if (N <= 0) return cudaSuccess;
+  RET((k_drop_fresh<<<nblk(N), TPB, 0, st>>>(N, cell)));
 }
 cudaError_t keys_of(const G32& g, long long N, const int32_t* cell, int32_t* key, cudaStream_t st) {
   if (N <= 0) return cudaSuccess;

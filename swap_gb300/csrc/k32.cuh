@@ -59,7 +59,6 @@ constexpr int32_t CELL_FRESH = 1 << 30;
 struct StepParams {
   float dt;
   int x_open;        // x does not wrap; ions leaving in x are marked dead
-  int drop_fresh;    // P1 at the end of a run: fresh ions are marked dead
   int chex;          // P3: res_chex after the step's last move
   long long chex_step;
   uint64_t seed;
@@ -201,6 +200,8 @@ cudaError_t to_f64(const G32& g, long long N, long long NM, const Part& p, doubl
 cudaError_t species_to_f64(long long N, const uint8_t* spid, const double* tab_mrat, const double* tab_bp,
                            double* mrat, double* beta_p, cudaStream_t st);
 cudaError_t keys_of(const G32& g, long long N, const int32_t* cell, int32_t* key, cudaStream_t st);
+// Remove the ions created for a step that is not taken (CELL_FRESH -> dead).
+cudaError_t drop_fresh_cells(long long N, int32_t* cell, cudaStream_t st);
 cudaError_t gather_perm(long long N, const int64_t* perm, const Part& src, Part dst, cudaStream_t st);
 cudaError_t sorted_hist(long long N, const int32_t* key, long long nkeys, int* unsorted, int64_t* count,
                         cudaStream_t st);

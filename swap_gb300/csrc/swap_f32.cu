@@ -470,11 +470,10 @@ static int sort_step(swap_ctx* c, F32State* s, long long src_step, bool prepared
 
 // Step parameters of the particle passes, with the sources and sinks that
 // act inside them (open-x outflow, res_chex at the end of the step).
-static StepParams step_params(swap_ctx* c, F32State* s, bool drop_fresh) {
+static StepParams step_params(swap_ctx* c, F32State* s) {
   StepParams p{};
   p.dt = (float)c->prm.dt;
   p.x_open = s->x_open ? 1 : 0;
-  p.drop_fresh = drop_fresh ? 1 : 0;
   const swap_sources& q = c->srcs;
   p.chex = (s->src_on && q.cx_a > 0) ? 1 : 0;
   p.chex_step = c->src_step;  // the ion step being taken
@@ -571,7 +570,7 @@ static int field_step(swap_ctx* c, F32State* s) {
 
 static int one_step(swap_ctx* c, F32State* s) {
   const G32& g = s->g;
-  const StepParams sp = step_params(c, s, false);
+  const StepParams sp = step_params(c, s);
   const Part& p = s->buf[s->cur];
   KL("f32_P1", pass(1, g, p, s->sp, sp, s->start, s->kit, s->partial, nullptr, nullptr, c->d_err, c->st));  // :385-387,399
   TRY(finish_deposit(c, s, 4));
@@ -602,9 +601,7 @@ extern "C" int swap_f32_run(swap_ctx* c, int32_t nsteps) {
 // next step, inserted by the last sort).
 static int drop_fresh(swap_ctx* c, F32State* s) {
   if (!s->src_on) return SWAP_OK;
-  const StepParams sp = step_params(c, s, true);
-  KL("f32_P1", pass(1, s->g, s->buf[s->cur], s->sp, sp, s->start, s->kit, s->partial, nullptr, nullptr, c->d_err,
-                    c->st));
+  KL("f32_drop_fresh", drop_fresh_cells(s->N, s->buf[s->cur].cell, c->st));
   return sort_step(c, s, -1);
 }
 
