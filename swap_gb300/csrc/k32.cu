@@ -54,11 +54,14 @@ __device__ __forceinline__ void store_img(const G32& g, T* f, int i, int j, int 
   }
 }
 
+// 32-bit division: t < ncx*ncy*ncz <= 2^30 (64-bit division is a long
+// emulated sequence)
 __device__ __forceinline__ void interior_of(const G32& g, long long t, int& i, int& j, int& k) {
-  i = (int)(t % g.ncx) + 2;
-  const long long r = t / g.ncx;
-  j = (int)(r % g.ncy) + 2;
-  k = (int)(r / g.ncy) + 2;
+  const unsigned u = (unsigned)t, nx = (unsigned)g.ncx, ny = (unsigned)g.ncy;
+  const unsigned r = u / nx, r2 = r / ny;
+  i = (int)(u - r * nx) + 2;
+  j = (int)(r - r2 * ny) + 2;
+  k = (int)r2 + 2;
 }
 
 __host__ __device__ __forceinline__ long long n_int(const G32& g) { return (long long)g.ncx * g.ncy * g.ncz; }
@@ -463,7 +466,11 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
 __global__ void k_node_sum(G32 g, const float* __restrict__ partial, int nq, float* __restrict__ np,
                            float* __restrict__ S) {
   GSTRIDE(t, n_int(g)) {
-    const int P = (int)(t % g.ncx), Q = (int)((t / g.ncx) % g.ncy), R = (int)(t / ((long long)g.ncx * g.ncy));
+    int P, Q, R;
+    interior_of(g, t, P, Q, R);
+    P -= 2;
+    Q -= 2;
+    R -= 2;
     int bx[2], ox[2], by[2], oy[2], bz[2], oz[2], nxc = 1, nyc = 1, nzc = 1;
     bx[0] = (P + 2) >> 2; ox[0] = (P + 2) & 3;
     if (bx[0] >= g.nbx) bx[0] -= g.nbx;
@@ -498,7 +505,9 @@ __global__ void k_node_sum(G32 g, const float* __restrict__ partial, int nq, flo
 // Generic periodic fill of the ghost shell (boundary.f:9-52).
 __global__ void k_ghost(G32 g, float* f, int ncomp) {
   GSTRIDE(o, g.C) {
-    const int i = (int)(o % g.nx) + 1, j = (int)((o / g.nx) % g.ny) + 1, k = (int)(o / ((long long)g.nx * g.ny)) + 1;
+    // 32-bit division: o < C < 2^32
+    const unsigned u = (unsigned)o, nx = (unsigned)g.nx, ny = (unsigned)g.ny, r = u / nx, r2 = r / ny;
+    const int i = (int)(u - r * nx) + 1, j = (int)(r - r2 * ny) + 1, k = (int)r2 + 1;
     const int wi = img(i, g.nx), wj = img(j, g.ny), wk = img(k, g.nz);
     if (wi == i && wj == j && wk == k) continue;
     const long long s = nid(g, wi, wj, wk);
@@ -508,16 +517,27 @@ __global__ void k_ghost(G32 g, float* f, int ncomp) {
 
 // ct = S/np at the interior image; up_m = 0.5*(ct_m(node) + ct_m(node+e_m))
 // (gutsp.f:1825-1836); np and up with ghost images.
-__device__ __forceinline__ float ct_at(const G32& g, const float* np, const float* S, int i, int j, int k, int m) {
-  const long long o = nid(g, img(i, g.nx), img(j, g.ny), img(k, g.nz));
+// (The fast divide, two ulps: n is a density, far from where it loses accuracy.)
+__device__ __forceinline__ float ct_o(const float* np, const float* S, long long o, long long cm) {
   const float n = np[o];
-  return n == 0.0f ? 0.0f : S[o + g.C * m] / n;
+  return n == 0.0f ? 0.0f : __fdividef(S[o + cm], n);
+}
+__device__ __forceinline__ float ct_at(const G32& g, const float* np, const float* S, int i, int j, int k, int m) {
+  return ct_o(np, S, nid(g, img(i, g.nx), img(j, g.ny), img(k, g.nz)), g.C * m);
 }
 
 __global__ void k_ct_up(G32 g, float* __restrict__ np, const float* __restrict__ S, float* __restrict__ up) {
   GSTRIDE(t, n_int(g)) {
     int i, j, k;
     interior_of(g, t, i, j, k);
+    if (i > 2 && j > 2 && k > 2 && i < g.nx - 1 && j < g.ny - 1 && k < g.nz - 1) {
+      // the +1 neighbours interior and no ghost image to store: strides
+      const long long C = g.C, o = nid(g, i, j, k), sy = g.nx, sz = (long long)g.nx * g.ny;
+      up[o] = 0.5f * (ct_o(np, S, o, 0) + ct_o(np, S, o + 1, 0));
+      up[o + C] = 0.5f * (ct_o(np, S, o, C) + ct_o(np, S, o + sy, C));
+      up[o + 2 * C] = 0.5f * (ct_o(np, S, o, 2 * C) + ct_o(np, S, o + sz, 2 * C));
+      continue;
+    }
     const float ux = 0.5f * (ct_at(g, np, S, i, j, k, 0) + ct_at(g, np, S, i + 1, j, k, 0));
     const float uy = 0.5f * (ct_at(g, np, S, i, j, k, 1) + ct_at(g, np, S, i, j + 1, k, 1));
     const float uz = 0.5f * (ct_at(g, np, S, i, j, k, 2) + ct_at(g, np, S, i, j, k + 1, 2));

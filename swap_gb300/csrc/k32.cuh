@@ -77,9 +77,11 @@ __host__ __device__ __forceinline__ long long key_of(const G32& g, int i, int j,
   return b * BCELLS + (i & 3) + 4 * (j & 3) + 16 * (k & 3);
 }
 __host__ __device__ __forceinline__ void cell_of_key(const G32& g, long long key, int& i, int& j, int& k) {
-  const long long b = key / BCELLS;
+  // 32-bit division: keys < 2^30
+  const unsigned b = (unsigned)(key / BCELLS), nbx = (unsigned)g.nbx, nby = (unsigned)g.nby;
   const int l = (int)(key % BCELLS);
-  const int bi = (int)(b % g.nbx), bj = (int)((b / g.nbx) % g.nby), bk = (int)(b / ((long long)g.nbx * g.nby));
+  const unsigned r = b / nbx, r2 = r / nby;
+  const int bi = (int)(b - r * nbx), bj = (int)(r - r2 * nby), bk = (int)r2;
   i = bi * 4 + (l & 3);
   j = bj * 4 + ((l >> 2) & 3);
   k = bk * 4 + (l >> 4);
