@@ -65,7 +65,15 @@ struct F32State {
   float *e_sum = nullptr, *vin = nullptr, *ve = nullptr, *jh = nullptr, *jl = nullptr, *jdb = nullptr;
   double* jacc = nullptr;
 
+  // the next step's new ions are staged on a second stream while this step's
+  // fields advance (the staging draws in FP64, the field kernels stream HBM)
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_main = nullptr, ev_side = nullptr;
   ~F32State() {
+    if (side) cudaStreamSynchronize(side);
+    if (ev_main) cudaEventDestroy(ev_main);
+    if (ev_side) cudaEventDestroy(ev_side);
+    if (side) cudaStreamDestroy(side);
     srcops::stage_free(stage);
     for (void* p : owned) cudaFree(p);
     release_pool();
@@ -139,7 +147,14 @@ static int check_err(swap_ctx* c) {
   return SWAP_OK;
 }
 
-static int sort_step(swap_ctx* c, F32State* s, long long src_step, bool prepared = false);
+// New ions staged ahead on the second stream (valid: the counts below hold).
+struct PreStaged {
+  bool valid = false;
+  long long n_host = 0, n_max = 0;
+  const int64_t* n_dev = nullptr;
+};
+static int sort_step(swap_ctx* c, F32State* s, long long src_step, bool prepared = false,
+                     const PreStaged* pre = nullptr);
 
 // ---------------------------------------------------------------------------
 
@@ -439,13 +454,20 @@ static int subcycles(swap_ctx* c, F32State* s, float* e_acc = nullptr) {
 // with src_step >= 0 the new ions of that step's sources are placed after the
 // arrivals of their cell, flagged fresh.  prepared: pass 3 already wrote the
 // directions, ranks and per-key counts.
-static int sort_step(swap_ctx* c, F32State* s, long long src_step, bool prepared) {
+static int sort_step(swap_ctx* c, F32State* s, long long src_step, bool prepared, const PreStaged* pre) {
   const G32& g = s->g;
   Part& a = s->buf[s->cur];
   Part& b = s->buf[1 - s->cur];
   long long n_host = 0, n_max = 0;
   const int64_t* n_dev = nullptr;
-  if (src_step >= 0 && s->src_on) TRY(srcops::f32_stage(c, g, s->stage, src_step, &n_host, &n_dev, &n_max));
+  if (pre && pre->valid) {
+    CU(cudaStreamWaitEvent(c->st, s->ev_side, 0));
+    n_host = pre->n_host;
+    n_max = pre->n_max;
+    n_dev = pre->n_dev;
+  } else if (src_step >= 0 && s->src_on) {
+    TRY(srcops::f32_stage(c, g, s->stage, src_step, &n_host, &n_dev, &n_max));
+  }
   const bool staged = n_max > 0;
   const long long cap = c->dims.ni_max;
   if (!prepared) KL("f32_sort_prep", sort_prep(g, s->start, a.cell, s->dirrank, s->dep, c->d_err, c->st));
@@ -568,6 +590,26 @@ static int field_step(swap_ctx* c, F32State* s) {
   return SWAP_OK;
 }
 
+// Stage the new ions of step m on the second stream, after the main stream's
+// work so far (the last sort read the previous staging's buffers).
+static int stage_ahead(swap_ctx* c, F32State* s, long long m, PreStaged* pre) {
+  if (!s->side) {
+    CU(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+    CU(cudaEventCreateWithFlags(&s->ev_main, cudaEventDisableTiming));
+    CU(cudaEventCreateWithFlags(&s->ev_side, cudaEventDisableTiming));
+  }
+  CU(cudaEventRecord(s->ev_main, c->st));
+  CU(cudaStreamWaitEvent(s->side, s->ev_main, 0));
+  cudaStream_t main = c->st;
+  c->st = s->side;  // the staging's launches and profile scopes go to the second stream
+  const int r = srcops::f32_stage(c, s->g, s->stage, m, &pre->n_host, &pre->n_dev, &pre->n_max);
+  c->st = main;
+  if (r) return r;
+  CU(cudaEventRecord(s->ev_side, s->side));
+  pre->valid = true;
+  return SWAP_OK;
+}
+
 static int one_step(swap_ctx* c, F32State* s) {
   const G32& g = s->g;
   const StepParams sp = step_params(c, s);
@@ -581,9 +623,11 @@ static int one_step(swap_ctx* c, F32State* s) {
   KL("f32_kit", build_kit(g, s->aj, s->up, s->db1, s->b0c, s->kit, c->st));       // :404
   // :404-413, the final half move of :479 and res_chex; prepares the sort
   KL("f32_P3", pass(3, g, p, s->sp, sp, s->start, s->kit, s->partial, s->dirrank, s->dep, c->d_err, c->st));
+  PreStaged pre;
+  if (s->src_on) TRY(stage_ahead(c, s, c->src_step + 1, &pre));  // the sources of the next step
   TRY(finish_deposit(c, s, 4));
   TRY(field_step(c, s));                                                          // :420-476
-  TRY(sort_step(c, s, c->src_step + 1, true));  // with the sources of the next step
+  TRY(sort_step(c, s, c->src_step + 1, true, &pre));
   if (c->have_srcs) c->src_step++;
   return SWAP_OK;
 }
