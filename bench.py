@@ -161,7 +161,7 @@ NODE_BYTES_F32 = {
     "f32_curlB": 12 + 4 + 12,
     "f32_aj_ct_pred": 12 + 4 + 12 + 12 + 12,        # read dB, np, up; write aj, ct
     "f32_aj_ct_corr": 12 + 4 + 12 + 12 + 12,
-    "f32_bstep_pred": 12 + 12 + 4 + 24 + 12 + 24 + 12 + 12,  # read ct, aj, nu, B, dB1; write B, dB, dB(m+1/2)
+    "f32_bstep_pred": 12 + 12 + 4 + 24 + 12 + 12,  # read ct, aj, nu, B, dB1; write dB(m+1/2)
     "f32_bstep_corr": 12 + 12 + 4 + 24 + 24 + 12,    # read ct, aj, nu, B; write B, dB
     "f32_kit": 36 + 32,
     "f32_node_sum": 16 * 2 + 16,

@@ -797,8 +797,9 @@ __device__ __forceinline__ void df_sub_mul(float bh, float bl, float ch, float c
 // E on the fly, curlE (gutsf.f:288-299) and B_new = base - coef*curlE
 // (predict_B gutsf.f:1158-1159 with coef = 2 dtsub on b12; correct_B
 // gutsf.f:1349-1350 with coef = dtsub on b1) in double-float; dB of the
-// result in FP32.  Predictor: also dB at m+1/2 = (dB_new + dB1)/2
-// (gutsf.f:1210-1219).  WRITE_E: store E (the step's last corrector).
+// result in FP32.  Predictor: only dB at m+1/2 = (dB_new + dB1)/2
+// (gutsf.f:1210-1219), the one use of the predicted B.  WRITE_E: store E
+// (the step's last corrector).
 template <bool PRED, bool WRITE_E, bool INNER>
 __device__ __forceinline__ void bstep_node(const G32& g, const float* __restrict__ ct, const float* __restrict__ nu,
                                            const float* __restrict__ aj, const float* __restrict__ bh,
@@ -824,10 +825,15 @@ __device__ __forceinline__ void bstep_node(const G32& g, const float* __restrict
     float rh, rl;
     df_sub_mul(bh[o + C * m], bl[o + C * m], ch, cl, ce[m], rh, rl);
     const float d = __fadd_rn(__fsub_rn(rh, b0c[m]), rl);
-    put<INNER>(g, oh + C * m, o, i, j, k, rh);
-    put<INNER>(g, ol + C * m, o, i, j, k, rl);
-    put<INNER>(g, dbo + C * m, o, i, j, k, d);
-    if (PRED) put<INNER>(g, dbtp1 + C * m, o, i, j, k, 0.5f * (d + db1[o + C * m]));
+    if (PRED) {
+      // the predicted B enters the corrector only through dB at m+1/2:
+      // the corrector rewrites B and dB from b1
+      put<INNER>(g, dbtp1 + C * m, o, i, j, k, 0.5f * (d + db1[o + C * m]));
+    } else {
+      put<INNER>(g, oh + C * m, o, i, j, k, rh);
+      put<INNER>(g, ol + C * m, o, i, j, k, rl);
+      put<INNER>(g, dbo + C * m, o, i, j, k, d);
+    }
   }
   if (WRITE_E) {
     put<INNER>(g, E, o, i, j, k, e1);
