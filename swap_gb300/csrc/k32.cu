@@ -1319,10 +1319,48 @@ __global__ void k_species_to_f64(long long N, const uint8_t* __restrict__ spid, 
   }
 }
 
-__global__ void k_drop_fresh(long long N, int32_t* __restrict__ cell) {
-  GSTRIDE(l, N) {
-    const int32_t c = cell[l];
-    if (c >= 0 && (c & CELL_FRESH)) cell[l] = CELL_DEAD;
+// The write-back without the ions staged for a step not taken: tiles of
+// KEEP_TILE ions, each block's count of kept ions, then (after a scan of the
+// counts) the order-preserving conversion of the kept ones.
+constexpr int KEEP_TILE = TPB * 8;
+__device__ __forceinline__ bool kept(int32_t c) { return c >= 0 && !(c & CELL_FRESH); }
+
+__global__ void k_keep_count(long long N, const int32_t* __restrict__ cell, int64_t* __restrict__ bcount) {
+  __shared__ int64_t sh[32];
+  const long long base = (long long)blockIdx.x * KEEP_TILE;
+  int64_t n = 0;
+  for (int q = 0; q < KEEP_TILE / TPB; ++q) {
+    const long long l = base + q * TPB + threadIdx.x;
+    n += (l < N && kept(cell[l])) ? 1 : 0;
+  }
+  int64_t tot;
+  block_excl_scan(n, sh, tot);
+  if (threadIdx.x == 0) bcount[blockIdx.x] = tot;
+}
+
+__global__ void k_to_f64_kept(G32 g, long long N, long long NM, Part p, const int64_t* __restrict__ bstart,
+                              const double* __restrict__ tm, const double* __restrict__ tb, double* __restrict__ xp,
+                              double* __restrict__ vp, double* __restrict__ vp1, double* __restrict__ mrat,
+                              double* __restrict__ beta_p) {
+  __shared__ int64_t sh[32];
+  const long long base = (long long)blockIdx.x * KEEP_TILE;
+  int64_t run = bstart[blockIdx.x];
+  for (int q = 0; q < KEEP_TILE / TPB; ++q) {
+    const long long l = base + q * TPB + threadIdx.x;
+    const int32_t c = l < N ? p.cell[l] : CELL_DEAD;
+    const bool k = kept(c);
+    int64_t tot;
+    const long long d = run + block_excl_scan(k ? 1 : 0, sh, tot);
+    run += tot;
+    if (!k) continue;
+    xp[d] = g.qx1 + ((double)pk_i(c) + (double)p.ox[l]) * (double)g.dx;
+    xp[d + NM] = g.qy1 + ((double)pk_j(c) + (double)p.oy[l]) * (double)g.dy;
+    xp[d + 2 * NM] = g.qz1 + ((double)pk_k(c) + (double)p.oz[l]) * (double)g.dz;
+    vp[d] = p.vx[l]; vp[d + NM] = p.vy[l]; vp[d + 2 * NM] = p.vz[l];
+    vp1[d] = p.wx[l]; vp1[d + NM] = p.wy[l]; vp1[d + 2 * NM] = p.wz[l];
+    const int s = p.sp ? min((int)p.sp[l], MAX_SPECIES - 1) : 0;
+    mrat[d] = tm[s];
+    beta_p[d] = tb[s];
   }
 }
 
@@ -1393,11 +1431,13 @@ struct KinFactor {
 __global__ void k_energy_p(long long N, Part p, KinFactor kf, double* acc) {
   float sf = 0.0f;
   GSTRIDE(l, N) {
+    // every load issued before the test, so that an ion's loads are in
+    // flight together (the kernel streams 17 B per ion)
     const int32_t c = p.cell[l];
-    if (c < 0 || (c & CELL_FRESH)) continue;  // removed, or created for the coming step
     const int q = p.sp ? min((int)p.sp[l], MAX_SPECIES - 1) : 0;
     const float vx = p.vx[l], vy = p.vy[l], vz = p.vz[l];
-    sf = fmaf(kf.k[q], fmaf(vx, vx, fmaf(vy, vy, vz * vz)), sf);
+    const float e = kf.k[q] * fmaf(vx, vx, fmaf(vy, vy, vz * vz));
+    if (c >= 0 && !(c & CELL_FRESH)) sf += e;  // not removed, not created for the coming step
   }
   const double s = bsum((double)sf);
   if (threadIdx.x == 0) atomicAdd(acc, s);
@@ -1612,9 +1652,23 @@ cudaError_t species_to_f64(long long N, const uint8_t* spid, const double* tab_m
   if (N <= 0) return cudaSuccess;
   RET((k_species_to_f64<<<nblk(N), TPB, 0, st>>>(N, spid, tab_mrat, tab_bp, mrat, beta_p)));
 }
-cudaError_t drop_fresh_cells(long long N, int32_t* cell, cudaStream_t st) {
+cudaError_t to_f64_kept(const G32& g, long long N, long long NM, const Part& p, const double* tab_mrat,
+                        const double* tab_bp, double* xp, double* vp, double* vp1, double* mrat, double* beta_p,
+                        int64_t* bcount, int64_t* bstart, int64_t* sums, long long* kept_out, cudaStream_t st) {
+  *kept_out = 0;
   if (N <= 0) return cudaSuccess;
-  RET((k_drop_fresh<<<nblk(N), TPB, 0, st>>>(N, cell)));
+  const long long nb = (N + KEEP_TILE - 1) / KEEP_TILE;
+  cudaError_t e;
+  k_keep_count<<<(unsigned)nb, TPB, 0, st>>>(N, p.cell, bcount);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = scan_exclusive(bcount, bstart, nb, sums, st)) != cudaSuccess) return e;
+  k_to_f64_kept<<<(unsigned)nb, TPB, 0, st>>>(g, N, NM, p, bstart, tab_mrat, tab_bp, xp, vp, vp1, mrat, beta_p);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  int64_t n = 0;
+  if ((e = cudaMemcpyAsync(&n, bstart + nb, sizeof(int64_t), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+  *kept_out = n;
+  return cudaSuccess;
 }
 cudaError_t keys_of(const G32& g, long long N, const int32_t* cell, int32_t* key, cudaStream_t st) {
   if (N <= 0) return cudaSuccess;
@@ -1642,7 +1696,7 @@ cudaError_t energy32(const G32& g, long long N, const Part& p, const Species& sp
                      cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(acc4, 0, 4 * sizeof(double), st);
   if (e != cudaSuccess) return e;
-  const unsigned cap = 152 * 8;  // a few particles' worth of work per thread, few atomics
+  const unsigned cap = 152 * 16;  // many particles per thread, few atomics, the SMs full
   if (N > 0) {
     KinFactor kf{};
     for (int q = 0; q < MAX_SPECIES && q < sp.n; ++q)

@@ -202,8 +202,12 @@ cudaError_t to_f64(const G32& g, long long N, long long NM, const Part& p, doubl
 cudaError_t species_to_f64(long long N, const uint8_t* spid, const double* tab_mrat, const double* tab_bp,
                            double* mrat, double* beta_p, cudaStream_t st);
 cudaError_t keys_of(const G32& g, long long N, const int32_t* cell, int32_t* key, cudaStream_t st);
-// Remove the ions created for a step that is not taken (CELL_FRESH -> dead).
-cudaError_t drop_fresh_cells(long long N, int32_t* cell, cudaStream_t st);
+// The state's ions in FP64 without those created for a step that is not
+// taken (CELL_FRESH) or removed, in their order; kept_out: how many.
+// bcount, bstart (N / (8 TPB) + 2 each) and sums are scratch.
+cudaError_t to_f64_kept(const G32& g, long long N, long long NM, const Part& p, const double* tab_mrat,
+                        const double* tab_bp, double* xp, double* vp, double* vp1, double* mrat, double* beta_p,
+                        int64_t* bcount, int64_t* bstart, int64_t* sums, long long* kept_out, cudaStream_t st);
 cudaError_t gather_perm(long long N, const int64_t* perm, const Part& src, Part dst, cudaStream_t st);
 cudaError_t sorted_hist(long long N, const int32_t* key, long long nkeys, int* unsorted, int64_t* count,
                         cudaStream_t st);

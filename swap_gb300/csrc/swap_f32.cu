@@ -53,6 +53,7 @@ struct F32State {
   double *tabm = nullptr, *tabb = nullptr;
   srcops::F32Stage stage;
   bool src_on = false, x_open = false, ended = false;
+  long long n_out = 0;  // ions written back by swap_f32_end
   uint8_t heavy_of[MAX_SPECIES]{};
   // the learned subcycle surrogate
   swap_surrogate* sur = nullptr;      // attached network
@@ -641,20 +642,11 @@ extern "C" int swap_f32_run(swap_ctx* c, int32_t nsteps) {
   return check_err(c);
 }
 
-// Drop the ions created for a step that is not taken (the sources of the
-// next step, inserted by the last sort).
-static int drop_fresh(swap_ctx* c, F32State* s) {
-  if (!s->src_on) return SWAP_OK;
-  KL("f32_drop_fresh", drop_fresh_cells(s->N, s->buf[s->cur].cell, c->st));
-  return sort_step(c, s, -1);
-}
-
 extern "C" int swap_f32_end(swap_ctx* c) {
   if (!c) return SWAP_EINVAL;
   F32State* s = f32(c);
   if (!s) return c->fail(SWAP_EINVAL, "swap_f32_begin has not been called");
   TRY(c->begin());
-  TRY(drop_fresh(c, s));
   // the particle arrays straight into the caller's memory in host-direct
   // mode, the fields into the device copies
   double *xp, *vp, *vp1, *b1, *b12, *b1p2, *bt, *npd, *upd, *Ed, *ajd;
@@ -674,11 +666,20 @@ extern "C" int swap_f32_end(swap_ctx* c) {
   TRY(c->use_host(c->h_mrat, Access::Out, &mratd, &direct[3]));
   TRY(c->use_host(c->h_beta_p, Access::Out, &bpd, &direct[4]));
   const G32& g = s->g;
-  CU(to_f64(g, s->N, c->dims.ni_max, s->buf[s->cur], xp, vp, vp1, c->st));
-  CU(species_to_f64(s->N, s->buf[s->cur].sp, s->tabm, s->tabb, mratd, bpd, c->st));
+  long long n_out = s->N;
+  if (s->src_on) {
+    // without the ions the last sort staged for the next step (not taken),
+    // compacted as they are written; the sort's count arrays are scratch now
+    CU(to_f64_kept(g, s->N, c->dims.ni_max, s->buf[s->cur], s->tabm, s->tabb, xp, vp, vp1, mratd, bpd, s->count,
+                   s->start_new, s->sums, &n_out, c->st));
+  } else {
+    CU(to_f64(g, s->N, c->dims.ni_max, s->buf[s->cur], xp, vp, vp1, c->st));
+    CU(species_to_f64(s->N, s->buf[s->cur].sp, s->tabm, s->tabb, mratd, bpd, c->st));
+  }
   for (int a = 0; a < 5; ++a)
-    if (direct[a]) c->d2h_bytes += (a < 3 ? 24 : 8) * s->N;
-  *c->ni_tot_ptr = (int32_t)s->N;
+    if (direct[a]) c->d2h_bytes += (a < 3 ? 24 : 8) * n_out;
+  *c->ni_tot_ptr = (int32_t)n_out;
+  s->n_out = n_out;
   s->ended = true;
   const std::size_t b3 = 3 * (std::size_t)g.C * sizeof(double);
   CU(join_df(3 * g.C, s->b1.h, s->b1.l, b1, c->st));
@@ -699,7 +700,9 @@ extern "C" int swap_f32_count(swap_ctx* c, int64_t* n) {
   if (!c || !n) return SWAP_EINVAL;
   F32State* s = f32(c);
   if (!s) return c->fail(SWAP_EINVAL, "swap_f32_begin has not been called");
-  *n = s->N;
+  // after swap_f32_end the state's ions are those written back (the buffer
+  // still holds the next step's staged ions)
+  *n = s->ended ? s->n_out : s->N;
   return SWAP_OK;
 }
 
