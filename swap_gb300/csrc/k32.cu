@@ -346,8 +346,9 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
           dvy = 0.5f * (py + my);
           dvz = 0.5f * (pz + mz);
         } else {
-          // get_vp_final (gutsp.f:444-445)
-          float wx = vx, wy = vy, wz = vz;
+          // get_vp_final (gutsp.f:444-445).  vp1 = the old v stays where it
+          // is: the new v goes into the vp1 arrays, and the host swaps the
+          // two after the pass (12 bytes per ion not written)
           vx = px + hdt * ex;
           vy = py + hdt * ey;
           vz = pz + hdt * ez;
@@ -382,14 +383,15 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
               const float prob = sprm.dt * dens * sigma * vrel;
               if (swapk::source_uniform_f32(sprm.seed, swapk::RNG_CHEX, sprm.chex_step, l) < prob) {
                 vx = vy = vz = 0.f;
-                wx = wy = wz = 0.f;
+                p.vx[l] = 0.f;  // vp1 too
+                p.vy[l] = 0.f;
+                p.vz[l] = 0.f;
                 p.sp[l] = (uint8_t)sprm.heavy_of[s];
                 ++n_chex;
               }
             }
           }
-          p.wx[l] = wx; p.wy[l] = wy; p.wz[l] = wz;
-          p.vx[l] = vx; p.vy[l] = vy; p.vz[l] = vz;
+          p.wx[l] = vx; p.wy[l] = vy; p.wz[l] = vz;
           if (out2) {
             p.cell[l] = CELL_DEAD;
             if (dirrank) dirrank[l] = DR_DEAD;

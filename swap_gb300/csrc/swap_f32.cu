@@ -624,6 +624,12 @@ static int one_step(swap_ctx* c, F32State* s) {
   KL("f32_kit", build_kit(g, s->aj, s->up, s->db1, s->b0c, s->kit, c->st));       // :404
   // :404-413, the final half move of :479 and res_chex; prepares the sort
   KL("f32_P3", pass(3, g, p, s->sp, sp, s->start, s->kit, s->partial, s->dirrank, s->dep, c->d_err, c->st));
+  {  // pass 3 wrote the new v into the vp1 arrays and left the old v (the new vp1) in place
+    Part& q = s->buf[s->cur];
+    std::swap(q.vx, q.wx);
+    std::swap(q.vy, q.wy);
+    std::swap(q.vz, q.wz);
+  }
   PreStaged pre;
   if (s->src_on) TRY(stage_ahead(c, s, c->src_step + 1, &pre));  // the sources of the next step
   TRY(finish_deposit(c, s, 4));
