@@ -92,7 +92,11 @@ struct swap_ctx {
   // per-kernel profile (CUDA events), filled by the fused paths
   bool prof_on = false;
   std::vector<ProfEntry> prof;
-  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_pending;
+  struct ProfPending {
+    int idx, kernels;
+    cudaEvent_t a, b;
+  };
+  std::vector<ProfPending> prof_pending;
   std::vector<cudaEvent_t> prof_pool;
 
   int fail(int code, const std::string& msg);

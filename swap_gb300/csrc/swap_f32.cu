@@ -126,6 +126,13 @@ void swap_f32_free(swap_ctx* c) {
     cudaError_t _e = (x);                                     \
     if (_e != cudaSuccess) return c->cuda_fail(_e, name);     \
   } while (0)
+// a launcher call that launches n kernels
+#define KLN(name, n, x)                                       \
+  do {                                                        \
+    ProfScope _ps(c, name, c->st, n);                         \
+    cudaError_t _e = (x);                                     \
+    if (_e != cudaSuccess) return c->cuda_fail(_e, name);     \
+  } while (0)
 #define CU(x)                                                 \
   do {                                                        \
     cudaError_t _e = (x);                                     \
@@ -474,7 +481,7 @@ static int sort_step(swap_ctx* c, F32State* s, long long src_step, bool prepared
   if (!prepared) KL("f32_sort_prep", sort_prep(g, s->start, a.cell, s->dirrank, s->dep, c->d_err, c->st));
   KL("f32_sort_count", sort_count(g, s->dep, staged ? s->stage.ncount : nullptr, s->order, s->count, s->pre,
                                   c->d_err, c->st));
-  KL("f32_sort_scan", scan_exclusive(s->count, s->start_new, g.nkeys, s->sums, c->st));
+  KLN("f32_sort_scan", 3, scan_exclusive(s->count, s->start_new, g.nkeys, s->sums, c->st));
   KL("f32_sort_scatter", sort_scatter(g, s->N, cap, a.cell, s->dirrank, s->pre, s->start_new, a, b, c->d_err, c->st));
   if (staged)
     KL("f32_new_scatter", new_scatter(g, n_host, n_dev, n_max, s->stage.part, s->stage.key, s->stage.rank,
@@ -535,7 +542,7 @@ static int sur_predict(swap_ctx* c, F32State* s, float* oh, float* ol, float* od
   const G32& g = s->g;
   KL("f32_sur_inputs", grid_to_voxels(g, s->db1, s->b0c, s->up, s->np, 1.0f, s->vin, c->st));
   {
-    ProfScope ps(c, "f32_sur_net", c->st);  // the network's own launches (normalise, 4 convs, scale)
+    ProfScope ps(c, "f32_sur_net", c->st, 6);  // the network's own launches (normalise, 4 convs, scale)
     if (surr::predict_e(s->sur, g.ncx, g.ncy, g.ncz, s->vin, s->ve, c->st))
       return c->fail(SWAP_EINVAL, std::string("surrogate: ") + surr::last_error(s->sur));
   }

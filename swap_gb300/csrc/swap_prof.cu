@@ -4,8 +4,8 @@
 
 void swap_ctx::prof_free() {
   for (auto& p : prof_pending) {
-    cudaEventDestroy(p.second.first);
-    cudaEventDestroy(p.second.second);
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
   }
   prof_pending.clear();
   for (cudaEvent_t e : prof_pool) cudaEventDestroy(e);
@@ -23,7 +23,8 @@ static cudaEvent_t take_event(swap_ctx* c) {
   return e;
 }
 
-ProfScope::ProfScope(swap_ctx* c, const char* name, cudaStream_t st) : c_(c), st_(st) {
+ProfScope::ProfScope(swap_ctx* c, const char* name, cudaStream_t st, int kernels)
+    : c_(c), st_(st), kernels_(kernels) {
   if (!c_ || !c_->prof_on) {
     c_ = nullptr;
     return;
@@ -43,19 +44,19 @@ ProfScope::ProfScope(swap_ctx* c, const char* name, cudaStream_t st) : c_(c), st
 ProfScope::~ProfScope() {
   if (!c_) return;
   cudaEventRecord(b_, st_);
-  c_->prof_pending.push_back({idx_, {a_, b_}});
+  c_->prof_pending.push_back({idx_, kernels_, a_, b_});
   if (c_->prof_pending.size() > 4096) swap_prof_collect(c_);
 }
 
 void swap_prof_collect(swap_ctx* c) {
   for (auto& p : c->prof_pending) {
-    cudaEventSynchronize(p.second.second);
+    cudaEventSynchronize(p.b);
     float ms = 0;
-    cudaEventElapsedTime(&ms, p.second.first, p.second.second);
-    c->prof[(std::size_t)p.first].ms += ms;
-    c->prof[(std::size_t)p.first].launches += 1;
-    c->prof_pool.push_back(p.second.first);
-    c->prof_pool.push_back(p.second.second);
+    cudaEventElapsedTime(&ms, p.a, p.b);
+    c->prof[(std::size_t)p.idx].ms += ms;
+    c->prof[(std::size_t)p.idx].launches += p.kernels;
+    c->prof_pool.push_back(p.a);
+    c->prof_pool.push_back(p.b);
   }
   c->prof_pending.clear();
 }

@@ -559,12 +559,15 @@ int f32_stage(swap_ctx* c, const swapk32::G32& g, F32Stage& st, long long m, lon
       k_cloud_count<<<nb(ncell), TPB, 0, c->st>>>(c->g, s, m, c->prm.dt, c->prm.beta, c->src_flag);
     }
     CU(cudaGetLastError());
-    TRY(scan_count(c, ncell, &n_cloud));
+    {
+      ProfScope ps(c, "f32_src_cloud_scan", c->st, 3);
+      TRY(scan_count(c, ncell, &n_cloud));
+    }
   }
   TRY(stage_reserve(c, st, n_ion + n_cloud + nslot, g.nkeys));
   CU(cudaMemsetAsync(st.ncount, 0, (std::size_t)g.nkeys * sizeof(int32_t), c->st));
   if (n_ion > 0) {
-    ProfScope ps(c, "f32_src_ionize", c->st);
+    ProfScope ps(c, "f32_src_ionize", c->st, 2);
     k32_stage_ionize<<<nb(n_ion), TPB, 0, c->st>>>(c->g, g, s, m, n_ion, st.part, st.key, st.sp_ion, c->d_err);
     k32_rank_seq<<<1, 1, 0, c->st>>>(n_ion, st.key, st.rank, st.ncount);
   }
@@ -578,7 +581,7 @@ int f32_stage(swap_ctx* c, const swapk32::G32& g, F32Stage& st, long long m, lon
   if (nslot > 0) {
     TRY(src_scratch(c, nslot));
     {
-      ProfScope ps(c, "f32_src_inflow", c->st);
+      ProfScope ps(c, "f32_src_inflow", c->st, 6);  // flags, the scan's 3, stage, count
       k_inflow_flags<<<nb(nslot), TPB, 0, c->st>>>(c->g, s, m, c->prm.dt, c->src_flag);
       CU(cudaGetLastError());
       CU(swapk32::scan_exclusive(c->src_flag, c->src_pos, nslot, c->src_sums, c->st));
