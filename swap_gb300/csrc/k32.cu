@@ -912,6 +912,22 @@ __global__ void __launch_bounds__(FBX * FBY) k_df_lerp(G32 g, const float* __res
   }
 }
 
+// Block sum (thread 0 holds the result; every thread of the block calls it).
+__device__ __forceinline__ double bsum(double v) {
+  __shared__ double sh[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (w == 0) {
+    r = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+  }
+  return r;
+}
+
 // The judge's sums over the interior: |B_a - B_b|^2, |B_b|^2, |B_b - b0|^2
 // (double-float levels a and b).
 __global__ void k_judge(G32 g, const float* __restrict__ ah, const float* __restrict__ al,
@@ -930,16 +946,13 @@ __global__ void k_judge(G32 g, const float* __restrict__ ah, const float* __rest
       s2 += (b - (double)b0c[m]) * (b - (double)b0c[m]);
     }
   }
-  for (int off = 16; off > 0; off >>= 1) {
-    s0 += __shfl_down_sync(0xffffffffu, s0, off);
-    s1 += __shfl_down_sync(0xffffffffu, s1, off);
-    s2 += __shfl_down_sync(0xffffffffu, s2, off);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    atomicAdd(acc, s0);
-    atomicAdd(acc + 1, s1);
-    atomicAdd(acc + 2, s2);
-  }
+  // one atomic per block and sum (a grid of a few blocks per SM)
+  s0 = bsum(s0);
+  if (threadIdx.x == 0) atomicAdd(acc, s0);
+  s1 = bsum(s1);
+  if (threadIdx.x == 0) atomicAdd(acc + 1, s1);
+  s2 = bsum(s2);
+  if (threadIdx.x == 0) atomicAdd(acc + 2, s2);
 }
 
 // The surrogate's inputs at every interior node (voxel v = x + ncx*(y +
@@ -1012,8 +1025,16 @@ __global__ void k_courant(G32 g, const float* __restrict__ dbt, const float* __r
     dtn[o] = d;
     mn = fminf(mn, d > 0.0f ? d : 0.0f);
   }
+  // one atomic per block (a grid of a few per SM): atomics from every warp to
+  // the one address serialise in L2
+  __shared__ float s_mn[TPB / 32];
   for (int off = 16; off > 0; off >>= 1) mn = fminf(mn, __shfl_down_sync(0xffffffffu, mn, off));
-  if ((threadIdx.x & 31) == 0) atomicMin(out, __float_as_uint(mn));
+  if ((threadIdx.x & 31) == 0) s_mn[threadIdx.x >> 5] = mn;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) mn = fminf(mn, s_mn[w]);
+    atomicMin(out, __float_as_uint(mn));
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1409,21 +1430,6 @@ __global__ void k_f32_to_f64(long long n, const float* __restrict__ a, double* _
   GSTRIDE(t, n) out[t] = (double)a[t];
 }
 
-__device__ __forceinline__ double bsum(double v) {
-  __shared__ double sh[32];
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  __syncthreads();
-  if (lane == 0) sh[w] = v;
-  __syncthreads();
-  double r = 0.0;
-  if (w == 0) {
-    r = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
-    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
-  }
-  return r;
-}
-
 // kf[q] = 0.5 m_q w_q for species q (m = 1/mrat, w = qw*vol the particle's
 // weight 1/(beta*beta_p)): kinetic energy kf * v^2, summed in FP32 per thread
 // (a thread sees a few hundred particles) and in FP64 across threads.
@@ -1552,7 +1558,8 @@ cudaError_t judge_sums(const G32& g, const float* ah, const float* al, const flo
                        const float* b0c, double* acc3, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(acc3, 0, 3 * sizeof(double), st);
   if (e != cudaSuccess) return e;
-  RET((k_judge<<<nblk(n_int(g)), TPB, 0, st>>>(g, ah, al, bh, bl, b0c, acc3)));
+  const unsigned nb = nblk(n_int(g)) < 152u * 8u ? nblk(n_int(g)) : 152u * 8u;
+  RET((k_judge<<<nb, TPB, 0, st>>>(g, ah, al, bh, bl, b0c, acc3)));
 }
 cudaError_t voxels_to_grid(const G32& g, const float* ev, float* E, cudaStream_t st) {
   RET((k_voxels_to_grid<<<nblk(n_int(g)), TPB, 0, st>>>(g, ev, E)));
@@ -1571,7 +1578,8 @@ cudaError_t courant_min(const G32& g, const float* dbt, const float* b0c, const 
   const unsigned init = 0x7f7fffffu;  // FLT_MAX
   cudaError_t e = cudaMemcpyAsync(d_min, &init, sizeof(init), cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return e;
-  RET((k_courant<<<nblk(g.C), TPB, 0, st>>>(g, dbt, b0c, np, alpha, dx, dtn, reinterpret_cast<unsigned*>(d_min))));
+  const unsigned nb = nblk(g.C) < 152u * 8u ? nblk(g.C) : 152u * 8u;
+  RET((k_courant<<<nb, TPB, 0, st>>>(g, dbt, b0c, np, alpha, dx, dtn, reinterpret_cast<unsigned*>(d_min))));
 }
 cudaError_t sort_prep(const G32& g, const int64_t* start, const int32_t* cell, uint32_t* dirrank, uint16_t* dep,
                       int* err, cudaStream_t st) {
