@@ -1400,8 +1400,13 @@ __global__ void k_sorted_hist(long long N, const int32_t* __restrict__ key, long
   GSTRIDE(l, N) {
     const int32_t k = key[l];
     if (l + 1 < N && key[l + 1] < k) atomicExch(unsorted, 1);
-    if (k >= 0 && k < nkeys) atomicAdd(reinterpret_cast<unsigned long long*>(count + k), 1ull);
-    else atomicExch(unsorted, 2);
+    const bool ok = k >= 0 && k < nkeys;
+    if (!ok) atomicExch(unsorted, 2);
+    // one atomic per group of the warp's lanes with the same key (sorted
+    // keys: one or two groups), not one per particle on the same address
+    const unsigned peers = __match_any_sync(__activemask(), ok ? k : -1);
+    if (ok && (int)(threadIdx.x & 31) == __ffs(peers) - 1)
+      atomicAdd(reinterpret_cast<unsigned long long*>(count + k), (unsigned long long)__popc(peers));
   }
 }
 
