@@ -61,12 +61,12 @@ def copy_state(dst_h, src_o):
 class Host:
     """The arrays of maind.f:38-70 for a RunConfig, on the host."""
 
-    def __init__(self, cfg, ni_max=None, load=True):
+    def __init__(self, cfg, ni_max=None, load=True, coords=None):
         self.cfg = cfg
         nx, ny, nz = cfg.nodes
         n = cfg.n_particles if ni_max is None else ni_max
         self.ni_max = n
-        self.coords = grd7(nx, ny, nz)
+        self.coords = coords if coords is not None else grd7(nx, ny, nz)
         f3 = lambda: np.zeros((n, 3), order="F")
         self.xp, self.vp, self.vp1, self.Ep, self.vplus, self.vminus = (f3() for _ in range(6))
         self.mrat, self.beta_p = np.ones(n), np.ones(n)

@@ -16,29 +16,36 @@ to rounding, tests/test_gpu_parity.py):
   - ions held still (mrat = 0): the whistler rate equals -k_eff^2 to 1e-8;
   - mobile ions: the product of the two roots equals -k_eff^2 to 0.3%, and
     the roots themselves lie within 2.5% of the fluid values at 32 cells per
-    wavelength.  Their sum (the Hall splitting) comes out at 0.81 of -k^2 for
-    every wavelength, time step and subcycle count tried, and depends on where
-    the ions sit inside their cells (0.75 with one ion per cell at the centre,
-    0.82 with three per axis): a property of the scheme's particle-grid
-    coupling, which the test keeps from drifting.
+    wavelength;
+  - their sum (the Hall splitting) falls short of the fluid -k^2 by an amount
+    first order in dz/d_i, independent of k, the time step and the subcycle
+    count: the ions' velocity reaches the grid (deposit) and comes back
+    (gather) smoothed over a cell, a correction of the same order k^2 as the
+    Hall term when dz ~ d_i.  With one ion per cell: 0.75, 0.87, 0.94 of -k^2
+    at dz = 1, 1/2, 1/4 d_i.
 """
 import numpy as np
 
 from helpers import Host, oracle, small
+from swap_gb300.grid import grd7
 
 NZ_CELLS = 32
 
 
-def _wave(steps, every, eps=0.02, frozen=False):
-    """B-only circularly polarized start on a quiet 2x2x2-per-cell lattice;
+def _wave(steps, every, eps=0.02, frozen=False, nz_cells=NZ_CELLS, delz=1.0, q=(0.25, 0.75)):
+    """B-only circularly polarized start on a quiet lattice (q: the ions'
+    places inside a cell, per axis; the box is nz_cells * delz = 32 d_i long);
     the spatial Fourier coefficient of dBx + i dBy at k, sampled every
-    `every` steps."""
-    cfg = small(cells=(4, 4, NZ_CELLS), ppc=8, vth=0.0, u=(0.0, 0.0, 0.0), nu=0.0 if frozen else 0.002)
-    h = Host(cfg, load=False)
+    `every` steps.  beta = ppc for a cell of volume delz makes the density
+    n = 1/delz, and then d_i v_A = 1/n and v_A^2 = 1/n."""
+    q = np.asarray(q)
+    cfg = small(cells=(4, 4, nz_cells), ppc=len(q) ** 3, vth=0.0, u=(0.0, 0.0, 0.0),
+                nu=0.0 if frozen else 0.002)
+    nx, ny, nz = cfg.nodes
+    h = Host(cfg, load=False, coords=grd7(nx, ny, nz, delz=delz))
     co = h.coords
-    k = 2.0 * np.pi / (NZ_CELLS * co.delz)
+    k = 2.0 * np.pi / (nz_cells * co.delz)
     ncx, ncy, ncz = cfg.cells
-    q = np.array([0.25, 0.75])
     px, py, pz = np.meshgrid(np.arange(ncx), np.arange(ncy), np.arange(ncz), indexing="ij")
     x = np.concatenate([np.stack([co.qx[px.ravel()] + a * co.dx, co.qy[py.ravel()] + b * co.dy,
                                   co.qz[pz.ravel()] + c * co.delz], axis=1) for a in q for b in q for c in q])
@@ -86,5 +93,26 @@ def test_ion_cyclotron_and_whistler_branches():
     assert abs(om_r - ex_r) < 0.03 * abs(ex_r), (om_r, ex_r)
     k_eff2 = (2.0 * np.sin(k / 2.0)) ** 2
     assert abs(om_l * om_r + k_eff2) < 0.005 * k_eff2  # the Alfven part: -k_eff^2
-    assert 0.78 < (om_l + om_r) / (-k * k) < 0.84  # the scheme's Hall splitting (see above)
+    assert 0.78 < (om_l + om_r) / (-k * k) < 0.84  # the scheme's Hall splitting at dz = d_i (see above)
     assert np.all(np.abs(roots) <= 1.0 + 1e-9)  # no growth
+
+
+def _roots(a, dt):
+    lhs = np.stack([a[1:-1], a[:-2]], axis=1)
+    c, *_ = np.linalg.lstsq(lhs, a[2:], rcond=None)
+    return sorted(-np.angle(np.roots([1.0, -c[0], -c[1]])) / dt)
+
+
+def test_hall_splitting_converges_at_first_order_in_dz():
+    """One ion per cell at the centre; the same 32 d_i wavelength on 32 and
+    64 cells: the shortfall of the splitting from the fluid value halves."""
+    short = []
+    for nz_cells, delz in ((32, 1.0), (64, 0.5)):
+        a, dt, k = _wave(steps=2000, every=10, nz_cells=nz_cells, delz=delz, q=(0.5,))
+        om_r, om_l = _roots(a, dt)
+        n = 1.0 / delz
+        k_eff2 = (2.0 * np.sin(k * delz / 2.0) / delz) ** 2
+        assert abs(-om_l * om_r / (k_eff2 / n) - 1.0) < 0.005  # the Alfven part
+        short.append(1.0 - (om_l + om_r) / (-k * k / n))
+    assert 0.2 < short[0] < 0.3
+    assert 0.45 < short[1] / short[0] < 0.55
