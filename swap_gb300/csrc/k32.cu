@@ -125,7 +125,7 @@ __device__ __forceinline__ int dir_index(int dx, int dy, int dz) { return (dx + 
 // the particle's cell before the move (sorted, so runs stay long), and the
 // few particles that changed cell (mover) take no part in them; each of
 // those then adds its 32 values to the tile directly, one per lane.
-template <bool ALL_Q, bool MOVERS = false>
+template <bool ALL_Q, int T, bool MOVERS = false>
 __device__ __forceinline__ void warp_deposit(float (*red)[36], bool live, int t0, const float (&w8)[8],
                                              const float (&qdv)[4], float* tile, int lane, int trun = -1,
                                              bool mover = false) {
@@ -140,7 +140,7 @@ __device__ __forceinline__ void warp_deposit(float (*red)[36], bool live, int t0
   const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || key != tprev);
   const unsigned ends = heads >> 1;  // the particle before each head (and, below, the last one)
   const int qv = lane >> 3, cv = lane & 7;
-  const int off = (cv & 1) + TN * (((cv >> 1) & 1) + TN * (cv >> 2));
+  const int off = (cv & 1) + T * (((cv >> 1) & 1) + T * (cv >> 2));
   const bool add_here = ALL_Q || qv != 0;
   const float4* wrow = reinterpret_cast<const float4*>(red[cv]);
   const float4* mrow = reinterpret_cast<const float4*>(red[8 + qv]);
@@ -166,7 +166,7 @@ __device__ __forceinline__ void warp_deposit(float (*red)[36], bool live, int t0
           acc = fmaf(x[r], m[r], acc);
           if ((e4 >> (r - 4 * g4)) & 1u) {
             const int tr = __shfl_sync(0xffffffffu, key, 16 * h + r);
-            if (add_here && tr >= 0) atomicAdd(&tile[qv * TNODES + tr + off], acc);
+            if (add_here && tr >= 0) atomicAdd(&tile[qv * T * T * T + tr + off], acc);
             acc = 0.0f;
           }
         }
@@ -174,7 +174,7 @@ __device__ __forceinline__ void warp_deposit(float (*red)[36], bool live, int t0
     }
   }
   const int tr = __shfl_sync(0xffffffffu, key, 31);  // the run that ends at the last particle
-  if (add_here && tr >= 0) atomicAdd(&tile[qv * TNODES + tr + off], acc);
+  if (add_here && tr >= 0) atomicAdd(&tile[qv * T * T * T + tr + off], acc);
   if (MOVERS) {
     unsigned mv = __ballot_sync(0xffffffffu, live && mover);
     if (mv) {
@@ -188,7 +188,7 @@ __device__ __forceinline__ void warp_deposit(float (*red)[36], bool live, int t0
         const int m = __ffs(mv) - 1;
         mv &= mv - 1;
         const int tm = __shfl_sync(0xffffffffu, t0, m);
-        if (add_here) atomicAdd(&tile[qv * TNODES + tm + off], red[cv][m] * red[8 + qv][m]);
+        if (add_here) atomicAdd(&tile[qv * T * T * T + tm + off], red[cv][m] * red[8 + qv][m]);
       }
     }
   }
@@ -220,9 +220,12 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
   __shared__ __align__(128) uint8_t s_s[2][TPB_PASS];
   __shared__ uint64_t s_full[2];
   // the field-gather tile: (aj-up, B_x) and (B_y, B_z) per node
-  __shared__ float4 s_kitA[PASS == 1 ? 1 : TNODES];
-  __shared__ float2 s_kitB[PASS == 1 ? 1 : TNODES];
-  __shared__ float s_dep[4 * TNODES];
+  // tile geometry: T nodes per axis; a cell rx of the brick (rx in [-1,4] for
+  // pass 3's movers, [0,3] otherwise) has its lower corner at offset rx + O
+  constexpr int T = pass_tile(PASS), TNOD = T * T * T, O = PASS == 3 ? 1 : 0;
+  __shared__ float4 s_kitA[PASS == 1 ? 1 : TNOD];
+  __shared__ float2 s_kitB[PASS == 1 ? 1 : TNOD];
+  __shared__ float s_dep[4 * TNOD];
   // per warp: [8 weights, 4 moments][particle]; rows padded to 36 floats so
   // that the 8 rows a reducing lane group reads start on different banks
   __shared__ __align__(16) float s_red[TPB_PASS / 32][12][36];
@@ -232,16 +235,17 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
   const int c0x = 4 * bi, c0y = 4 * bj, c0z = 4 * bk;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (PASS != 1) {
-    for (int t = threadIdx.x; t < TNODES; t += blockDim.x) {
-      const int tx = t % TN, ty = (t / TN) % TN, tz = t / (TN * TN);
-      const int P = wrapi(c0x - 2 + tx, g.ncx), Q = wrapi(c0y - 2 + ty, g.ncy), R = wrapi(c0z - 2 + tz, g.ncz);
+    for (int t = threadIdx.x; t < TNOD; t += blockDim.x) {
+      const int tx = t % T, ty = (t / T) % T, tz = t / (T * T);
+      const int P = wrapi(c0x - 1 - O + tx, g.ncx), Q = wrapi(c0y - 1 - O + ty, g.ncy),
+                R = wrapi(c0z - 1 - O + tz, g.ncz);
       const long long src = 2 * ((long long)P + (long long)g.ncx * (Q + (long long)g.ncy * R));
       s_kitA[t] = kit[src];
       const float4 hi = kit[src + 1];
       s_kitB[t] = make_float2(hi.x, hi.y);
     }
   }
-  for (int t = threadIdx.x; t < 4 * TNODES; t += blockDim.x) s_dep[t] = 0.0f;
+  for (int t = threadIdx.x; t < 4 * TNOD; t += blockDim.x) s_dep[t] = 0.0f;
   if (PASS == 3)
     for (int t = threadIdx.x; t < BCELLS * NDIR; t += blockDim.x) s_rank[t] = 0;
   if (threadIdx.x == 0) {
@@ -313,7 +317,11 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
       } else {
         // trilinear gather of (ajc-upc, btc) at the 8 corners (gutsp.f:217-251)
         const float wxl = 1.0f - ox, wxu = ox, wyl = 1.0f - oy, wyu = oy, wzl = 1.0f - oz, wzu = oz;
-        const int tg = (rx + 1) + TN * ((ry + 1) + TN * (rz + 1));
+        // (the ion lies in its key's cell; clamped so that a broken sort
+        // cannot index outside the tile: the check below reports it)
+        const int gx = PASS == 3 ? rx : min(max(rx, 0), 3), gy = PASS == 3 ? ry : min(max(ry, 0), 3),
+                  gz = PASS == 3 ? rz : min(max(rz, 0), 3);
+        const int tg = (gx + O) + T * ((gy + O) + T * (gz + O));
         float ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;
 #pragma unroll
         for (int cz = 0; cz < 2; ++cz)
@@ -322,7 +330,7 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
 #pragma unroll
             for (int cx = 0; cx < 2; ++cx) {
               const float w = (cx ? wxu : wxl) * (cy ? wyu : wyl) * (cz ? wzu : wzl);
-              const int t = tg + cx + TN * (cy + TN * cz);
+              const int t = tg + cx + T * (cy + T * cz);
               const float4 f0 = s_kitA[t];
               const float2 f1 = s_kitB[t];
               ax = fmaf(w, f0.x, ax); ay = fmaf(w, f0.y, ay); az = fmaf(w, f0.z, az);
@@ -411,13 +419,14 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
           if (out1) live = false;
         }
       }
-      const bool inside = !(rx < -1 || rx > 4 || ry < -1 || ry > 4 || rz < -1 || rz > 4);
+      const bool inside = PASS == 3 ? !(rx < -1 || rx > 4 || ry < -1 || ry > 4 || rz < -1 || rz > 4)
+                                    : !(rx < 0 || rx > 3 || ry < 0 || ry > 3 || rz < 0 || rz > 3);
       if (live && !inside) {
         set_err(err, KERR_MOVE);
         live = false;
       }
       if (live) {
-        t0 = (rx + 1) + TN * ((ry + 1) + TN * (rz + 1));
+        t0 = (rx + O) + T * ((ry + O) + T * (rz + O));
         mover = PASS == 3 && t0 != t0o;
         const float wxl = 1.0f - ox, wxu = ox, wyl = 1.0f - oy, wyu = oy, wzl = 1.0f - oz, wzu = oz;
 #pragma unroll
@@ -429,7 +438,7 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
         qdv[3] = qw * dvz;
       }
     }
-    warp_deposit<PASS != 2, PASS == 3>(s_red[warp], live, t0, w8, qdv, s_dep, lane, t0o, mover);
+    warp_deposit<PASS != 2, T, PASS == 3>(s_red[warp], live, t0, w8, qdv, s_dep, lane, t0o, mover);
     if (PASS == 3 && dirrank) {
       // stable ranks per (key, direction): the warps of the CTA take their
       // turn in order, each adding its particles after the earlier ones
@@ -453,8 +462,8 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
     if (lane == 0 && n_chex) atomicAdd(sprm.chex_count, (unsigned long long)n_chex);
   }
   __syncthreads();
-  float* out = partial + b * (4 * TNODES);
-  for (int t = threadIdx.x; t < 4 * TNODES; t += blockDim.x) out[t] = s_dep[t];
+  float* out = partial + b * (4 * TNOD);
+  for (int t = threadIdx.x; t < 4 * TNOD; t += blockDim.x) out[t] = s_dep[t];
 
   if (PASS == 3 && dep)
     for (int t = threadIdx.x; t < BCELLS * NDIR; t += blockDim.x)  // direction-major: dep[dir][key]
@@ -462,11 +471,14 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
           (uint16_t)s_rank[(t % BCELLS) * NDIR + t / BCELLS];
 }
 
-// Sum, at every interior node, the brick tiles that cover it: along each axis
-// node p lies in the tiles of bricks floor((p+2)/4) (offset (p+2)%4) and the
-// one before (offset +4, when <= 6).
+// Sum, at every interior node, the brick tiles (T nodes per axis) that cover
+// it: along each axis node p lies in the tile of brick floor((p+1+O)/4) at
+// offset (p+1+O)%4 and in the one before at offset +4 when that is < T
+// (O = 1 for the 7-node tiles, whose origin is one node lower).
+template <int T>
 __global__ void k_node_sum(G32 g, const float* __restrict__ partial, int nq, float* __restrict__ np,
                            float* __restrict__ S) {
+  constexpr int O = T == TN ? 1 : 0, TNOD = T * T * T;
   GSTRIDE(t, n_int(g)) {
     int P, Q, R;
     interior_of(g, t, P, Q, R);
@@ -474,23 +486,23 @@ __global__ void k_node_sum(G32 g, const float* __restrict__ partial, int nq, flo
     Q -= 2;
     R -= 2;
     int bx[2], ox[2], by[2], oy[2], bz[2], oz[2], nxc = 1, nyc = 1, nzc = 1;
-    bx[0] = (P + 2) >> 2; ox[0] = (P + 2) & 3;
+    bx[0] = (P + 1 + O) >> 2; ox[0] = (P + 1 + O) & 3;
     if (bx[0] >= g.nbx) bx[0] -= g.nbx;
-    if (ox[0] + 4 <= 6) { bx[1] = bx[0] == 0 ? g.nbx - 1 : bx[0] - 1; ox[1] = ox[0] + 4; nxc = 2; }
-    by[0] = (Q + 2) >> 2; oy[0] = (Q + 2) & 3;
+    if (ox[0] + 4 < T) { bx[1] = bx[0] == 0 ? g.nbx - 1 : bx[0] - 1; ox[1] = ox[0] + 4; nxc = 2; }
+    by[0] = (Q + 1 + O) >> 2; oy[0] = (Q + 1 + O) & 3;
     if (by[0] >= g.nby) by[0] -= g.nby;
-    if (oy[0] + 4 <= 6) { by[1] = by[0] == 0 ? g.nby - 1 : by[0] - 1; oy[1] = oy[0] + 4; nyc = 2; }
-    bz[0] = (R + 2) >> 2; oz[0] = (R + 2) & 3;
+    if (oy[0] + 4 < T) { by[1] = by[0] == 0 ? g.nby - 1 : by[0] - 1; oy[1] = oy[0] + 4; nyc = 2; }
+    bz[0] = (R + 1 + O) >> 2; oz[0] = (R + 1 + O) & 3;
     if (bz[0] >= g.nbz) bz[0] -= g.nbz;
-    if (oz[0] + 4 <= 6) { bz[1] = bz[0] == 0 ? g.nbz - 1 : bz[0] - 1; oz[1] = oz[0] + 4; nzc = 2; }
+    if (oz[0] + 4 < T) { bz[1] = bz[0] == 0 ? g.nbz - 1 : bz[0] - 1; oz[1] = oz[0] + 4; nzc = 2; }
     float acc[4] = {0.f, 0.f, 0.f, 0.f};
     for (int a = 0; a < nxc; ++a)
       for (int bb = 0; bb < nyc; ++bb)
         for (int cc = 0; cc < nzc; ++cc) {
           const long long brick = bx[a] + (long long)g.nbx * (by[bb] + (long long)g.nby * bz[cc]);
-          const int tt = ox[a] + TN * (oy[bb] + TN * oz[cc]);
-          const float* src = partial + brick * (4 * TNODES) + tt;
-          for (int q = 4 - nq; q < 4; ++q) acc[q] += src[q * TNODES];
+          const int tt = ox[a] + T * (oy[bb] + T * oz[cc]);
+          const float* src = partial + brick * (4 * TNOD) + tt;
+          for (int q = 4 - nq; q < 4; ++q) acc[q] += src[q * TNOD];
         }
     const long long o = pid(g, P, Q, R);
     if (nq == 4) np[o] = acc[0];
@@ -1505,8 +1517,10 @@ cudaError_t pass(int which, const G32& g, const Part& p, const Species& sp, cons
   RET((k_pass<3><<<grid, TPB_PASS, 0, st>>>(PASS_ARGS)));
 #undef PASS_ARGS
 }
-cudaError_t node_sum(const G32& g, const float* partial, int nq, float* np, float* S, cudaStream_t st) {
-  RET((k_node_sum<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, partial, nq, np, S)));
+cudaError_t node_sum(const G32& g, int pass, const float* partial, int nq, float* np, float* S, cudaStream_t st) {
+  const unsigned nb = nblk((long long)g.ncx * g.ncy * g.ncz);
+  if (pass_tile(pass) == TN) RET((k_node_sum<TN><<<nb, TPB, 0, st>>>(g, partial, nq, np, S)));
+  RET((k_node_sum<TN_IN><<<nb, TPB, 0, st>>>(g, partial, nq, np, S)));
 }
 cudaError_t ghost_fill(const G32& g, float* f, int ncomp, cudaStream_t st) {
   RET((k_ghost<<<nblk(g.C), TPB, 0, st>>>(g, f, ncomp)));

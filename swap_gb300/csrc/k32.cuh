@@ -18,6 +18,12 @@ constexpr int BR = 4;                 // brick edge (cells)
 constexpr int BCELLS = BR * BR * BR;  // 64 cells per brick
 constexpr int TN = BR + 3;            // tile nodes per axis: brick + one-cell mover halo
 constexpr int TNODES = TN * TN * TN;  // 343
+// Passes 1 and 2 deposit and gather only in their ions' own cells (no move
+// before them): a tile of brick + 1 node per axis, origin one node lower.
+constexpr int TN_IN = BR + 1;
+constexpr int TNODES_IN = TN_IN * TN_IN * TN_IN;  // 125
+// Tile nodes per axis of the passes' deposit tiles (and of k_node_sum).
+__host__ __device__ constexpr int pass_tile(int pass) { return pass == 3 ? TN : TN_IN; }
 constexpr int NDIR = 27;              // displacements in {-1,0,1}^3
 constexpr int MAX_SPECIES = 16;
 
@@ -131,7 +137,8 @@ cudaError_t pass(int which, const G32& g, const Part& p, const Species& sp, cons
                  const int64_t* start, const float4* kit, float* partial, uint32_t* dirrank, uint16_t* dep, int* err,
                  cudaStream_t st);
 // Sum the brick partial tiles into np and S (interior nodes, (nx,ny,nz) layout).
-cudaError_t node_sum(const G32& g, const float* partial, int nq, float* np, float* S, cudaStream_t st);
+// pass: the pass (1-3) whose tiles `partial` holds
+cudaError_t node_sum(const G32& g, int pass, const float* partial, int nq, float* np, float* S, cudaStream_t st);
 
 // ---- fields ----
 cudaError_t ghost_fill(const G32& g, float* f, int ncomp, cudaStream_t st);

@@ -404,8 +404,8 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
 }
 
 // Deposit finish: node sums -> np (+ghosts) and up (maind.f:386-387 etc.).
-static int finish_deposit(swap_ctx* c, F32State* s, int nq) {
-  KL("f32_node_sum", node_sum(s->g, s->partial, nq, s->np, s->S, c->st));
+static int finish_deposit(swap_ctx* c, F32State* s, int pass, int nq) {
+  KL("f32_node_sum", node_sum(s->g, pass, s->partial, nq, s->np, s->S, c->st));
   if (nq == 4) KL("f32_ghost_np", ghost_fill(s->g, s->np, 1, c->st));
   KL("f32_ct_up", ct_and_up(s->g, s->np, s->S, s->up, c->st));
   return SWAP_OK;
@@ -623,11 +623,11 @@ static int one_step(swap_ctx* c, F32State* s) {
   const StepParams sp = step_params(c, s);
   const Part& p = s->buf[s->cur];
   KL("f32_P1", pass(1, g, p, s->sp, sp, s->start, s->kit, s->partial, nullptr, nullptr, c->d_err, c->st));  // :385-387,399
-  TRY(finish_deposit(c, s, 4));
+  TRY(finish_deposit(c, s, 1, 4));
   KL("f32_curlB", curlB32(g, s->db1, s->np, (float)c->prm.alpha, s->aj, c->st));  // :395
   KL("f32_kit", build_kit(g, s->aj, s->up, s->db1, s->b0c, s->kit, c->st));       // :398, get_Ep :183-184
   KL("f32_P2", pass(2, g, p, s->sp, sp, s->start, s->kit, s->partial, nullptr, nullptr, c->d_err, c->st));  // :400-402
-  TRY(finish_deposit(c, s, 3));
+  TRY(finish_deposit(c, s, 2, 3));
   KL("f32_kit", build_kit(g, s->aj, s->up, s->db1, s->b0c, s->kit, c->st));       // :404
   // :404-413, the final half move of :479 and res_chex; prepares the sort
   KL("f32_P3", pass(3, g, p, s->sp, sp, s->start, s->kit, s->partial, s->dirrank, s->dep, c->d_err, c->st));
@@ -639,7 +639,7 @@ static int one_step(swap_ctx* c, F32State* s) {
   }
   PreStaged pre;
   if (s->src_on) TRY(stage_ahead(c, s, c->src_step + 1, &pre));  // the sources of the next step
-  TRY(finish_deposit(c, s, 4));
+  TRY(finish_deposit(c, s, 3, 4));
   TRY(field_step(c, s));                                                          // :420-476
   TRY(sort_step(c, s, c->src_step + 1, true, &pre));
   if (c->have_srcs) c->src_step++;
