@@ -220,11 +220,12 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
   __shared__ __align__(128) uint8_t s_s[2][TPB_PASS];
   __shared__ uint64_t s_full[2];
   // the field-gather tile: (aj-up, B_x) and (B_y, B_z) per node
-  // tile geometry: T nodes per axis; a cell rx of the brick (rx in [-1,4] for
-  // pass 3's movers, [0,3] otherwise) has its lower corner at offset rx + O
+  // deposit tile: T nodes per axis; a cell rx of the brick (rx in [-1,4] for
+  // pass 3's movers, [0,3] otherwise) has its lower corner at offset rx + O.
+  // The gather happens before any move: its tile is TN_IN wide, origin 0.
   constexpr int T = pass_tile(PASS), TNOD = T * T * T, O = PASS == 3 ? 1 : 0;
-  __shared__ float4 s_kitA[PASS == 1 ? 1 : TNOD];
-  __shared__ float2 s_kitB[PASS == 1 ? 1 : TNOD];
+  __shared__ float4 s_kitA[PASS == 1 ? 1 : TNODES_IN];
+  __shared__ float2 s_kitB[PASS == 1 ? 1 : TNODES_IN];
   __shared__ float s_dep[4 * TNOD];
   // per warp: [8 weights, 4 moments][particle]; rows padded to 36 floats so
   // that the 8 rows a reducing lane group reads start on different banks
@@ -235,10 +236,9 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
   const int c0x = 4 * bi, c0y = 4 * bj, c0z = 4 * bk;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (PASS != 1) {
-    for (int t = threadIdx.x; t < TNOD; t += blockDim.x) {
-      const int tx = t % T, ty = (t / T) % T, tz = t / (T * T);
-      const int P = wrapi(c0x - 1 - O + tx, g.ncx), Q = wrapi(c0y - 1 - O + ty, g.ncy),
-                R = wrapi(c0z - 1 - O + tz, g.ncz);
+    for (int t = threadIdx.x; t < TNODES_IN; t += blockDim.x) {
+      const int tx = t % TN_IN, ty = (t / TN_IN) % TN_IN, tz = t / (TN_IN * TN_IN);
+      const int P = wrapi(c0x - 1 + tx, g.ncx), Q = wrapi(c0y - 1 + ty, g.ncy), R = wrapi(c0z - 1 + tz, g.ncz);
       const long long src = 2 * ((long long)P + (long long)g.ncx * (Q + (long long)g.ncy * R));
       s_kitA[t] = kit[src];
       const float4 hi = kit[src + 1];
@@ -318,10 +318,9 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
         // trilinear gather of (ajc-upc, btc) at the 8 corners (gutsp.f:217-251)
         const float wxl = 1.0f - ox, wxu = ox, wyl = 1.0f - oy, wyu = oy, wzl = 1.0f - oz, wzu = oz;
         // (the ion lies in its key's cell; clamped so that a broken sort
-        // cannot index outside the tile: the check below reports it)
-        const int gx = PASS == 3 ? rx : min(max(rx, 0), 3), gy = PASS == 3 ? ry : min(max(ry, 0), 3),
-                  gz = PASS == 3 ? rz : min(max(rz, 0), 3);
-        const int tg = (gx + O) + T * ((gy + O) + T * (gz + O));
+        // cannot index outside the tile: the checks below report it)
+        const int gx = min(max(rx, 0), 3), gy = min(max(ry, 0), 3), gz = min(max(rz, 0), 3);
+        const int tg = gx + TN_IN * (gy + TN_IN * gz);
         float ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;
 #pragma unroll
         for (int cz = 0; cz < 2; ++cz)
@@ -330,7 +329,7 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
 #pragma unroll
             for (int cx = 0; cx < 2; ++cx) {
               const float w = (cx ? wxu : wxl) * (cy ? wyu : wyl) * (cz ? wzu : wzl);
-              const int t = tg + cx + T * (cy + T * cz);
+              const int t = tg + cx + TN_IN * (cy + TN_IN * cz);
               const float4 f0 = s_kitA[t];
               const float2 f1 = s_kitB[t];
               ax = fmaf(w, f0.x, ax); ay = fmaf(w, f0.y, ay); az = fmaf(w, f0.z, az);
