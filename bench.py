@@ -155,7 +155,7 @@ KERNEL_BYTES_F32 = {
 # cells, 16 ppc, 8.4M particles; profiles/k_pass_fp32_128x64x64_16ppc.md and
 # profiles/k_sort_scatter_fp32_128x64x64_16ppc.md); the roofline's traffic is
 # this figure times the particles of a launch.
-KERNEL_TRAFFIC_F32 = {"f32_P1": 45.3, "f32_P2": 34.6, "f32_P3": 65.0, "f32_sort_scatter": 86.0}
+KERNEL_TRAFFIC_F32 = {"f32_P1": 42.8, "f32_P2": 32.4, "f32_P3": 64.8, "f32_sort_scatter": 86.0}
 # per interior node (FP32 fields, double-float B levels of 8 B per component)
 NODE_BYTES_F32 = {
     "f32_curlB": 12 + 4 + 12,
