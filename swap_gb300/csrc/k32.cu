@@ -473,7 +473,8 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
 // Sum, at every interior node, the brick tiles (T nodes per axis) that cover
 // it: along each axis node p lies in the tile of brick floor((p+1+O)/4) at
 // offset (p+1+O)%4 and in the one before at offset +4 when that is < T
-// (O = 1 for the 7-node tiles, whose origin is one node lower).
+// (O = 1 for the 7-node tiles, whose origin is one node lower).  The density
+// is stored with its ghost images (boundary.f:167-206 fused in).
 template <int T>
 __global__ void k_node_sum(G32 g, const float* __restrict__ partial, int nq, float* __restrict__ np,
                            float* __restrict__ S) {
@@ -504,7 +505,7 @@ __global__ void k_node_sum(G32 g, const float* __restrict__ partial, int nq, flo
           for (int q = 4 - nq; q < 4; ++q) acc[q] += src[q * TNOD];
         }
     const long long o = pid(g, P, Q, R);
-    if (nq == 4) np[o] = acc[0];
+    if (nq == 4) store_img(g, np, P + 2, Q + 2, R + 2, acc[0]);  // np with its ghost images
     S[o] = acc[1];
     S[o + g.C] = acc[2];
     S[o + 2 * g.C] = acc[3];
@@ -514,19 +515,6 @@ __global__ void k_node_sum(G32 g, const float* __restrict__ partial, int nq, flo
 // ---------------------------------------------------------------------------
 // fields (interior nodes, ghost images written by the producer)
 // ---------------------------------------------------------------------------
-
-// Generic periodic fill of the ghost shell (boundary.f:9-52).
-__global__ void k_ghost(G32 g, float* f, int ncomp) {
-  GSTRIDE(o, g.C) {
-    // 32-bit division: o < C < 2^32
-    const unsigned u = (unsigned)o, nx = (unsigned)g.nx, ny = (unsigned)g.ny, r = u / nx, r2 = r / ny;
-    const int i = (int)(u - r * nx) + 1, j = (int)(r - r2 * ny) + 1, k = (int)r2 + 1;
-    const int wi = img(i, g.nx), wj = img(j, g.ny), wk = img(k, g.nz);
-    if (wi == i && wj == j && wk == k) continue;
-    const long long s = nid(g, wi, wj, wk);
-    for (int m = 0; m < ncomp; ++m) f[o + g.C * m] = f[s + g.C * m];
-  }
-}
 
 // ct = S/np at the interior image; up_m = 0.5*(ct_m(node) + ct_m(node+e_m))
 // (gutsp.f:1825-1836); np and up with ghost images.
@@ -1520,9 +1508,6 @@ cudaError_t node_sum(const G32& g, int pass, const float* partial, int nq, float
   const unsigned nb = nblk((long long)g.ncx * g.ncy * g.ncz);
   if (pass_tile(pass) == TN) RET((k_node_sum<TN><<<nb, TPB, 0, st>>>(g, partial, nq, np, S)));
   RET((k_node_sum<TN_IN><<<nb, TPB, 0, st>>>(g, partial, nq, np, S)));
-}
-cudaError_t ghost_fill(const G32& g, float* f, int ncomp, cudaStream_t st) {
-  RET((k_ghost<<<nblk(g.C), TPB, 0, st>>>(g, f, ncomp)));
 }
 cudaError_t ct_and_up(const G32& g, const float* np, const float* S, float* up, cudaStream_t st) {
   RET((k_ct_up<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, const_cast<float*>(np), S, up)));

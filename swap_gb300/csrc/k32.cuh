@@ -141,7 +141,6 @@ cudaError_t pass(int which, const G32& g, const Part& p, const Species& sp, cons
 cudaError_t node_sum(const G32& g, int pass, const float* partial, int nq, float* np, float* S, cudaStream_t st);
 
 // ---- fields ----
-cudaError_t ghost_fill(const G32& g, float* f, int ncomp, cudaStream_t st);
 cudaError_t ct_and_up(const G32& g, const float* np, const float* S, float* up, cudaStream_t st);
 cudaError_t build_kit(const G32& g, const float* aj, const float* up, const float* dbt, const float* b0c,
                       float4* kit, cudaStream_t st);

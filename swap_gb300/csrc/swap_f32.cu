@@ -406,7 +406,6 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
 // Deposit finish: node sums -> np (+ghosts) and up (maind.f:386-387 etc.).
 static int finish_deposit(swap_ctx* c, F32State* s, int pass, int nq) {
   KL("f32_node_sum", node_sum(s->g, pass, s->partial, nq, s->np, s->S, c->st));
-  if (nq == 4) KL("f32_ghost_np", ghost_fill(s->g, s->np, 1, c->st));
   KL("f32_ct_up", ct_and_up(s->g, s->np, s->S, s->up, c->st));
   return SWAP_OK;
 }
