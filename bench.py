@@ -1,23 +1,31 @@
 """Throughput of SWAP's hybrid PIC ion step on GB300: ion particle-steps/s.
 
-A step is one full ion step of maind.f:385-479 (three particle passes with
-four moment deposits, the field predictor-corrector with its subcycles and
-the final half move) over every particle of the workload.
+A step is one full ion step of maind.f:379-484 (the sources, three particle
+passes with four moment deposits, the field predictor-corrector with its
+subcycles, the final half move and the sinks) over every ion of the workload.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--precision f64] [--config 1]
 
-With the FP32 form the line also carries "accuracy": the FP32 form and the
-FP32 form with the surrogate against the FP64 drop-in after --acc-steps ion
-steps of the periodic 64x32x32 box (B and n_p rel-L2, energy drift), and
-"surrogate": the same step timed
-with the learned field surrogate (trained on pairs collected from plain
-steps of the same run) in place of the field subcycles, judged against them
-every few steps.  --surrogate off skips it.
+The headline times the FP32 form on the 256x128x128-cell, 32-ppc workload
+(134M ions, x inflow/outflow).  The line also carries
+  "e2e":       the same steps through the C-ABI with host buffers;
+  "surrogate": the step with the learned field surrogate in place of the
+               subcycles, judged against them every few steps;
+  "fp64":      the FP64 GPU drop-in (swap_run) on the same workload;
+  "accuracy":  the FP32 form and the FP32 form with the surrogate against the
+               FP64 drop-in after --acc-steps ion steps of the periodic
+               64x32x32 box;
+  "accuracy_configs": the pickup-ion workloads (256x128x128 and 512x256x256
+               cells at 16 ppc, neutral cloud and charge exchange) at their
+               stated sizes, FP32 form against FP64 drop-in, with the FP32
+               form's ions per brick;
+  "cpu_baseline": one full-size ion step of the oracle on the host cores.
 
-Rank 0 prints one JSON line.  --impl reference times the reference's CPU
-path (the C++ restatement in oracle/, the reference itself has no Fortran
-compiler here) on the host cores.
+--impl reference times the reference's CPU path on the host cores: the C++
+restatement in oracle/ at the reference's own precision (FP32), on the whole
+workload, one full ion step per timed step, with the FP64 oracle beside it.
+Rank 0 prints one JSON line.
 """
 from __future__ import annotations
 
@@ -152,9 +160,8 @@ KERNEL_BYTES_F32 = {
 }
 # DRAM bytes per particle that ncu measured for these kernels
 # (dram__bytes_read.sum + dram__bytes_write.sum over one launch at 128x64x64
-# cells, 16 ppc, 8.4M particles; profiles/k_pass_fp32_128x64x64_16ppc.md and
-# profiles/k_sort_scatter_fp32_128x64x64_16ppc.md); the roofline's traffic is
-# this figure times the particles of a launch.
+# cells, 16 ppc, 8.4M particles); the roofline's traffic is this figure times
+# the particles of a launch.
 KERNEL_TRAFFIC_F32 = {"f32_P1": 42.8, "f32_P2": 32.4, "f32_P3": 64.8, "f32_sort_scatter": 86.0}
 # per interior node (FP32 fields, double-float B levels of 8 B per component)
 NODE_BYTES_F32 = {
@@ -169,60 +176,45 @@ NODE_BYTES_F32 = {
 }
 
 
-def cpu_sample_oracle(cfg_full, steps: int, threads: int):
-    """Time the oracle's FP64 ion step on a sub-box of the workload (same ppc,
-    same physics), on `threads` host threads.  Returns (particle-steps/s, info)."""
-    sys.path.insert(0, str(ROOT / "oracle"))
+def config_line(cfg, ions, f32=True):
+    """The workload's description in a bench line."""
+    return {"workload": cfg.name, "cells": list(cfg.cells), "ppc": cfg.ppc, "ions": int(ions),
+            "subcycles": cfg.ntsub,
+            "boundary": "x inflow/outflow, periodic y,z" if cfg.sources.get("x_open") else "periodic",
+            "precision_form": ("FP32 form (int32 cell + FP32 offset, FP32 moments, double-float B)" if f32
+                               else "FP64 drop-in"),
+            "l2": "inputs larger than L2 (particle state %.1f GB)" % (ions * (41 if f32 else 72) / 1e9)}
+
+
+def oracle_run(cfg, precision: str, warmup: int, steps: int, threads: int) -> dict:
+    """The reference's CPU path (the oracle's restatement) on the whole
+    workload: the oracle's own seeded load, `warmup` untimed ion steps, then
+    `steps` ion steps each timed by the wall clock.  Nothing of the product
+    is loaded.  Particle-steps are the mean of each step's ion count before
+    and after it (inflow and outflow change the count a little)."""
+    if str(ROOT / "oracle") not in sys.path:
+        sys.path.insert(0, str(ROOT / "oracle"))
     import pyoracle
-    from swap_gb300.grid import grd6_setup, grd7
-    from swap_gb300.hybrid import RunConfig
 
-    cells = (64, 32, 32)
-    src = dict(cfg_full.sources)
-    if "cloud_x" in src:  # keep the cloud at the centre of the sub-box
-        src.update(cloud_x=cells[0] / 2 + 1.0, cloud_y=cells[1] / 2 + 1.0, cloud_z=cells[2] / 2 + 1.0)
-    cfg = RunConfig(name="cpu sample", cells=cells, ppc=cfg_full.ppc, vth=cfg_full.vth, u=cfg_full.u,
-                    dt=cfg_full.dt, ntsub=cfg_full.ntsub, nu=cfg_full.nu, seed=cfg_full.seed, sources=src)
-    nx, ny, nz = cfg.nodes
-    n = cfg.ni_max_hint()
-    n_load = cfg.n_particles
-
-    class Host:  # arrays in the layout the oracle binds
-        pass
-
-    h = Host()
-    h.cfg = cfg
-    h.ni_max = n
-    co = grd7(nx, ny, nz)
-    f3 = lambda: np.zeros((n, 3), order="F")
-    h.xp, h.vp, h.vp1, h.Ep, h.vplus, h.vminus = (f3() for _ in range(6))
-    h.mrat, h.beta_p = np.ones(n), np.ones(n)
-    h.ni_tot = np.array([n_load], dtype=np.int32)
-    for k, v in grd6_setup(co, cfg.b0, cfg.nu).items():
-        setattr(h, k, v)
-    # the same stratified Maxwellian load as the GPU run, made by the product loader
-    from swap_gb300 import abi
-    import ctypes as C
-
-    lib = abi.load()
-    dims = abi.Dims(nx, ny, nz, 0, n)
-    cc = abi.Coords(*[abi.dptr(getattr(co, a)) for a in co.ARRAYS])
-    spec = abi.LoadSpec(cfg.seed, 0, cfg.ppc, cfg.vth, *cfg.u, 1.0, 1.0)
-    cnt = C.c_int64()
-    abi.check(lib, None, lib.swap_load_maxwellian_host(C.byref(dims), C.byref(cc), C.byref(spec), abi.dptr(h.xp),
-                                                        abi.dptr(h.vp), abi.dptr(h.vp1), abi.dptr(h.mrat),
-                                                        abi.dptr(h.beta_p), 0, C.byref(cnt)))
-    o = pyoracle.from_hybrid_arrays(h, precision="f64", nthreads=threads)
-    if cfg.sources:
-        o.set_sources(cfg.make_sources(), 0)
     t0 = time.perf_counter()
-    o.run(steps)
-    dt = time.perf_counter() - t0
-    info = {"sample": f"{cells[0]}x{cells[1]}x{cells[2]}-cell sub-box of the workload at {cfg.ppc} ppc "
-                      f"({n_load:,} ions), {steps} FP64 ion steps of the oracle"
-                      + (" with the workload's sources and sinks" if cfg.sources else ""),
-            "seconds": dt}
-    return n_load * steps / dt, info
+    o = pyoracle.standalone(cfg, precision=precision, nthreads=threads)
+    t_load = time.perf_counter() - t0
+    for _ in range(warmup):
+        o.ion_step()
+    units, secs, per_step = 0.0, 0.0, []
+    for _ in range(steps):
+        n0 = int(o.ni_tot[0])
+        t = time.perf_counter()
+        o.ion_step()
+        dt = time.perf_counter() - t
+        units += 0.5 * (n0 + int(o.ni_tot[0]))
+        secs += dt
+        per_step.append(round(dt, 3))
+    o.close()
+    del o
+    return {"value": units / secs, "unit": UNIT, "ms_per_step": secs / steps * 1e3, "ions": units / steps,
+            "steps": steps, "warmup": warmup, "load_s": t_load, "step_s": per_step, "threads": threads,
+            "precision": precision}
 
 
 # ---------------------------------------------------------------------------
@@ -230,6 +222,10 @@ def cpu_sample_oracle(cfg_full, steps: int, threads: int):
 # ---------------------------------------------------------------------------
 
 def run_reference(args):
+    """The oracle at the reference's own precision (FP32: makefile:1 builds
+    SWAP with -real-size 32) on the whole workload, every timed step a full
+    ion step over all of its ions; the FP64 oracle beside it on the same
+    workload for a few steps."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
@@ -237,24 +233,22 @@ def run_reference(args):
 
     cfg = config(args.config)
     threads = os.cpu_count() or 1
-    for _ in range(args.warmup):
-        cpu_sample_oracle(cfg, 1, threads)
-    vals = []
-    info = None
-    for _ in range(args.steps):
-        v, info = cpu_sample_oracle(cfg, 1, threads)
-        vals.append(v)
-    value = statistics.median(vals)
+    r = oracle_run(cfg, "f32", args.warmup, args.steps, threads)
+    sample = (f"the whole workload ({r['ions']:,.0f} ions), one full FP32 ion step of the oracle per timed step "
+              f"after {args.warmup} warm-up steps, OpenMP over {threads} host threads")
     line = {
         "impl": "reference",
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": cfg.n_particles / value * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": cfg.name, "cells": list(cfg.cells), "ppc": cfg.ppc, "ions": cfg.n_particles,
-                   "subcycles": cfg.ntsub},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": info["sample"]},
-        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded stratified Maxwellian load, normalized units)",
+        "config": dict(config_line(cfg, r["ions"]), precision_form="the oracle at the reference's precision (FP32)",
+                       parallelism=f"{threads} host threads"),
+        "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "step_s": r["step_s"], "load_s": r["load_s"],
     }
+    if args.ref_fp64_steps > 0:
+        line["fp64"] = oracle_run(cfg, "f64", 1, args.ref_fp64_steps, threads)
     print(json.dumps(line), flush=True)
     return 0
 
@@ -377,6 +371,111 @@ def run_accuracy(args):
     return out
 
 
+def brick_load(starts: np.ndarray) -> dict:
+    """Ions per 4x4x4-cell brick (one CTA of the particle passes each) and
+    per cell, from the FP32 state's key starts (key = brick * 64 + cell)."""
+    per_cell = np.diff(starts)
+    per_brick = starts[64::64] - starts[:-1:64]
+    return {"brick_mean": float(per_brick.mean()), "brick_max": int(per_brick.max()),
+            "brick_min": int(per_brick.min()), "brick_max_over_mean": float(per_brick.max() / per_brick.mean()),
+            "cell_min": int(per_cell.min()), "cell_max": int(per_cell.max()),
+            "cell_p99": float(np.percentile(per_cell, 99))}
+
+
+def run_compare(n: int, steps: int, cx: bool = True) -> dict:
+    """A named workload at its stated size, run `steps` ion steps from the
+    same seeded load by the FP64 GPU drop-in and by the FP32 form: B, B - b0
+    and n_p rel-L2 of the FP32 form against the FP64 run, each run's energy
+    drift, the ion counts, both step times, and the FP32 form's load per
+    brick.  With cx=False charge exchange is off: the FP32 form draws it per
+    sorted ion and the FP64 path per array index, so with it on the two runs
+    are different draws of the same process and their difference holds that
+    sampling noise as well as the FP32 rounding."""
+    import ctypes as C
+
+    from swap_gb300.hybrid import Hybrid, config
+
+    cfg = config(n)
+    if not cx:
+        src = dict(cfg.sources)
+        src.update(cx_a=0.0, cx_b=0.0)
+        cfg = config(n, sources=src)
+    NM = cfg.ni_max_hint(steps + 4)
+
+    def fresh():
+        h = Hybrid(cfg, ni_max=NM, work_arrays=False)
+        h.load_maxwellian(seed=cfg.seed)
+        h.set_sources(cfg.make_sources(), 0)
+        h.sync_to_device()
+        return h
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+    def timed(h, fn):
+        ms = C.c_double()
+        h._check(h.lib.swap_timer_start(h.ctx))
+        fn()
+        h._check(h.lib.swap_timer_stop(h.ctx, C.byref(ms)))
+        return ms.value
+
+    def total(e):
+        return float(e[0] + e[1])
+
+    t0 = time.perf_counter()
+    h = fresh()
+    n0 = int(h.ni_tot[0])
+    e0 = h.energy()
+    ms64 = timed(h, lambda: h.run(steps))
+    e64 = h.energy()
+    h.sync_to_host()
+    ref = {"b1": h.b1.copy(), "b0": h.b0.copy(), "np": h.np.copy()}
+    n64 = int(h.ni_tot[0])
+    h.close()
+    del h
+    h = fresh()
+    h.f32_begin()
+    ea = h.f32_energy()
+    ms32 = timed(h, lambda: h.f32_run(steps))
+    eb = h.f32_energy()
+    load = brick_load(h.f32_key_starts())
+    n32 = h.f32_count()
+    h.f32_end()
+    h.sync_to_host()
+    out = {"workload": cfg.name + ("" if cx else " (charge exchange off)"), "steps": steps, "ions_start": n0,
+           "ions_fp64": n64, "ions_fp32": n32,
+           "fp64_ms_per_step": ms64 / steps, "fp32_ms_per_step": ms32 / steps,
+           "fp32_over_fp64_speed": ms64 / ms32,
+           "b_rel_l2": rel(h.b1, ref["b1"]), "db_rel_l2": rel(h.b1 - h.b0, ref["b1"] - ref["b0"]),
+           "np_rel_l2": rel(h.np, ref["np"]),
+           "fp64_energy_drift": (total(e64) - total(e0)) / total(e0),
+           "fp32_energy_drift": (total(eb) - total(ea)) / total(ea),
+           "energy_vs_fp64": (total(eb) - total(e64)) / total(e64),
+           "fp32_load_per_brick": load}
+    h.close()
+    del h
+    out["seconds"] = time.perf_counter() - t0
+    return out
+
+
+def run_fp64_leg(h, steps: int, warmup: int) -> dict:
+    """The FP64 GPU drop-in (swap_run) on the same workload and state:
+    `warmup` untimed steps, then `steps` timed by CUDA events."""
+    import ctypes as C
+
+    h.sync_to_device()
+    for _ in range(warmup):
+        h.run(1)
+    n0 = int(h.ni_tot[0])
+    ms = C.c_double()
+    h._check(h.lib.swap_timer_start(h.ctx))
+    h.run(steps)
+    h._check(h.lib.swap_timer_stop(h.ctx, C.byref(ms)))
+    N = 0.5 * (n0 + int(h.ni_tot[0]))
+    return {"ms_per_step": ms.value / steps, "value": N * steps / (ms.value / 1e3), "unit": UNIT, "steps": steps,
+            "warmup": warmup, "ions": N, "dtype": "f64"}
+
+
 def run_ours(args):
     ws, rank, local = dist_env()
     import torch
@@ -495,20 +594,13 @@ def run_ours(args):
     e2e_s = barrier_max(time.perf_counter() - w0, ws)
     h2d_bytes, d2h_bytes = h.transfer_bytes(reset=True)
     d2h_bytes += 32 * args.steps  # the energy reads
-    del state_arrays
 
     value = N * args.steps * ws / (t_ms / 1e3)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if f32 else "f64", "data": "synthetic (seeded stratified Maxwellian load, normalized units)",
-        "config": {"workload": cfg.name, "cells": list(cfg.cells), "ppc": cfg.ppc, "ions": N,
-                   "subcycles": cfg.ntsub,
-                   "boundary": "x inflow/outflow, periodic y,z" if cfg.sources.get("x_open") else "periodic",
-                   "precision_form": "FP32 form (int32 cell + FP32 offset, FP32 moments, double-float B)" if f32
-                   else "FP64 drop-in",
-                   "l2": "inputs larger than L2 (particle state %.1f GB)" % (N * (41 if f32 else 72) / 1e9),
-                   "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU"},
+        "config": dict(config_line(cfg, N, f32), parallelism=f"replicas x{ws}" if ws > 1 else "1 GPU"),
         "gpu_launches": launches,
         "clocks": clk,
         "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -531,23 +623,85 @@ def run_ours(args):
             line["surrogate"] = run_surrogate(h, args, N, ws)
         except Exception as e:  # the headline stands without it
             line["surrogate"] = {"error": f"{type(e).__name__}: {e}"}
-    if rank == 0 and f32 and args.acc_steps > 0:
+    if f32 and args.fp64_steps > 0:
+        # the plain FP64 GPU drop-in on the same workload: the other side of
+        # the metric's FP32-versus-FP64 comparison
         try:
-            line["accuracy"] = run_accuracy(args)
-        except Exception as e:  # the headline stands without it
-            line["accuracy"] = {"error": f"{type(e).__name__}: {e}"}
+            line["fp64"] = run_fp64_leg(h, args.fp64_steps, 2)
+            line["fp64"]["fp32_over_fp64_speed"] = line["fp64"]["ms_per_step"] / line["ms_per_step"]
+        except Exception as e:
+            line["fp64"] = {"error": f"{type(e).__name__}: {e}"}
+    h.close()
+    del h, state_arrays, in_fields
+    import gc
+
+    gc.collect()
+    if rank == 0:
+        run_accuracy_legs(args, line)
     if rank == 0 and not args.no_cpu_baseline:
-        v, info = cpu_sample_oracle(cfg, 1, os.cpu_count() or 1)
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
-                                "sample": info["sample"]}
+        r = oracle_run(cfg, "f32", 1, 1, os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": r["value"], "unit": UNIT, "cores": r["threads"], "kind": "port",
+                                "sample": f"one full FP32 ion step of the oracle over the whole workload "
+                                          f"({r['ions']:,.0f} ions) after one warm-up step"}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    h.close()
     if ws > 1:
         import torch.distributed as dist
 
         dist.destroy_process_group()
     return 0
+
+
+def run_conv_only(spec) -> int:
+    """The surrogate's tensor-core convolution alone on random BF16 data, for
+    profiling one launch in isolation: spec = CIN COUT NX NY NZ [REPEATS].
+    CIN, COUT are 16 or 32 (the network's layer shapes); NX*NY*NZ must be a
+    multiple of 128, and NX a multiple of 128 selects the line-ring form."""
+    import torch
+
+    from swap_gb300 import abi
+
+    if len(spec) not in (5, 6):
+        print(run_conv_only.__doc__)
+        return 2
+    cin, cout, nx, ny, nz = spec[:5]
+    reps = spec[5] if len(spec) == 6 else 2
+    lib = abi.load()
+    V = nx * ny * nz
+    X = torch.randn(V, cin, device="cuda").to(torch.bfloat16)
+    W = (0.1 * torch.randn(27, cout, cin, device="cuda")).to(torch.bfloat16)
+    b = torch.zeros(cout, device="cuda")
+    Y = torch.empty(V, cout, dtype=torch.bfloat16, device="cuda")
+    for _ in range(reps):
+        r = lib.swap_conv3_check(nx, ny, nz, cin, cout, X.data_ptr(), W.data_ptr(), b.data_ptr(), Y.data_ptr(), None,
+                                 1)
+        if r:
+            print(f"swap_conv3_check returned {r}")
+            return 1
+    torch.cuda.synchronize()
+    print("ok")
+    return 0
+
+
+def run_accuracy_legs(args, line):
+    """The error legs of the line: the 64x32x32 box (FP64, FP32, FP32 with
+    the surrogate), then the configs --acc-configs at their stated sizes."""
+    if args.precision == "f32" and args.acc_steps > 0:
+        try:
+            line["accuracy"] = run_accuracy(args)
+        except Exception as e:  # the headline stands without it
+            line["accuracy"] = {"error": f"{type(e).__name__}: {e}"}
+    steps = {2: args.acc2_steps, 3: args.acc3_steps}
+    for n in [int(x) for x in args.acc_configs.split(",") if x.strip()]:
+        for cx in ([True, False] if args.acc_cx_off else [True]):
+            key = f"config{n}" + ("" if cx else "_no_cx")
+            try:
+                line.setdefault("accuracy_configs", {})[key] = run_compare(n, steps.get(n, 20), cx=cx)
+            except Exception as e:
+                line.setdefault("accuracy_configs", {})[key] = {"error": f"{type(e).__name__}: {e}"}
+            import gc
+
+            gc.collect()
 
 
 def main():
@@ -567,6 +721,18 @@ def main():
     ap.add_argument("--sur-bound", type=float, default=1e-3, help="judge bound on the relative B error")
     ap.add_argument("--acc-steps", type=int, default=1000,
                     help="ion steps of the accuracy comparison against the FP64 drop-in (0 skips it)")
+    ap.add_argument("--acc-configs", default="2,3",
+                    help="workloads run at their stated size by both the FP64 drop-in and the FP32 form")
+    ap.add_argument("--acc2-steps", type=int, default=100, help="ion steps of the 256x128x128 pickup-ion comparison")
+    ap.add_argument("--acc3-steps", type=int, default=20, help="ion steps of the 512x256x256 pickup-ion comparison")
+    ap.add_argument("--acc-cx-off", action="store_true",
+                    help="also run each comparison with charge exchange off (no sampling difference)")
+    ap.add_argument("--only-accuracy", action="store_true", help="run the accuracy legs alone")
+    ap.add_argument("--conv-only", type=int, nargs="+", default=None, metavar="N",
+                    help="CIN COUT NX NY NZ [REPEATS]: the surrogate's convolution alone (profiling)")
+    ap.add_argument("--fp64-steps", type=int, default=5, help="timed steps of the FP64 GPU drop-in leg (0 skips)")
+    ap.add_argument("--ref-fp64-steps", type=int, default=2,
+                    help="reference arm: timed full-size steps of the FP64 oracle beside the FP32 one (0 skips)")
     ap.add_argument("--cells", type=int, nargs=3, default=None, help="override the workload's cells (profiling)")
     ap.add_argument("--ppc", type=int, default=None, help="override particles per cell (profiling)")
     args = ap.parse_args()
@@ -574,6 +740,16 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.conv_only:
+        return run_conv_only(args.conv_only)
+    if args.only_accuracy:
+        import torch
+
+        torch.cuda.set_device(0)
+        line = {"accuracy_only": True}
+        run_accuracy_legs(args, line)
+        print(json.dumps(line), flush=True)
+        return 0
     return run_ours(args)
 
 

@@ -248,6 +248,11 @@ int swap_f32_end(swap_ctx* ctx);
 int swap_f32_energy(swap_ctx* ctx, double out[4]);
 /* Ions in the FP32 state (sources and sinks change it step by step). */
 int swap_f32_count(swap_ctx* ctx, int64_t* n);
+/* Where each sort key's ions start in the FP32 state's sorted order:
+ * starts[0..nkeys], nkeys = (cells/4 per axis, multiplied) * 64, key =
+ * brick * 64 + cell in the brick (x fastest, bricks x fastest), so key q
+ * holds starts[q+1] - starts[q] ions.  n = entries of starts (>= nkeys+1). */
+int swap_f32_key_starts(swap_ctx* ctx, int64_t* starts, int64_t n);
 /* Validation: move particles idx[q] of the current (sorted) order by one
  * cell step per axis (dcell[q] = (dx+1) | (dy+1)<<10 | (dz+1)<<20) and run
  * the stable incremental sort that follows each ion step. */
@@ -286,13 +291,16 @@ int swap_load_maxwellian_host(const swap_dims* dims, const swap_coords* coords, 
  * swap_get_interp_weights + swap_update_up (gutsp.f:1378-1435, 1649-1842)
  * from the caller's DEVICE arrays xp, vp (ni_max,3), beta_p (ni_max), np
  * (nx,ny,nz) into the caller's device array up (nx,ny,nz,3), on `stream`
- * (a cudaStream_t; NULL = default stream), and returns after the stream
- * finishes.  coords are host arrays, as for swap_init.
+ * (a cudaStream_t; NULL = default stream), and returns after that stream
+ * finishes (it waits on that one stream, not on the device).  coords are
+ * host arrays, as for swap_init.
  *   - It allocates nothing.  Its scratch is one file-scope device array of
  *     SWAP_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds
  *     until the process exits.
  *   - The first call on a device resolves that array's address
- *     (cudaGetSymbolAddress); make the first call before any stream capture.
+ *     (cudaGetSymbolAddress) and keeps it; make the first call before any
+ *     stream capture, and make no call on a device after cudaDeviceReset
+ *     there.  After an error the entry waits for its stream before returning.
  *   - All calls share the array and each call clears the part it uses first;
  *     calls that overlap on the GPU race, so serialize them.
  *   - More than SWAP_NOALLOC_MAX_NODES nodes, or more than

@@ -60,6 +60,7 @@ struct Api {
     c->s.beta = (R)beta;
     c->s.grad_pe = (R)grad_pe;
     c->s.nthreads = nthreads < 1 ? 1 : nthreads;
+    c->s.g.nt = c->s.nthreads;
     swo::state_alloc(c->s, ni_max);
     const std::size_t n3 = (std::size_t)ni_max * 3;
     c->Ep.assign(n3, R(0));
@@ -68,6 +69,66 @@ struct Api {
     return c;
   }
 };
+
+// The initial ion load of the workloads: ppc ions in every physical cell,
+// positions uniform in the cell, each velocity component
+// u + vth*sqrt(-ln U)*cos(pi*U') (the form of part_init.f:204-206), vp1 = vp
+// (part_init.f:220).  It replaces load_Maxwellian (part_init.f:146-232),
+// which draws positions over the whole box from the compiler's
+// random_number; here the twelve uniforms of ion `id` are the Philox4x32-10
+// block keyed by (seed, stream) with the ion's id as counter (the generator of
+// ../swap_gb300/csrc/philox.h).  Ions come out by bricks of 4x4x4 cells, each
+// brick's cells x fastest, when every axis has a multiple of 4 physical
+// cells, else by cell with x fastest.  Arithmetic is in double, then rounded
+// to R.
+template <class R>
+std::int64_t load_maxwellian(const swo::State<R>& s, std::uint64_t seed, std::uint32_t stream, int ppc, double vth,
+                             double ux, double uy, double uz, double mrat, double beta_p, std::int64_t first, R* xp,
+                             R* vp, R* vp1, R* mr, R* bp) {
+  const auto& g = s.g;
+  const std::int64_t ncx = g.nx - 2, ncy = g.ny - 2, ncz = g.nz - 2;
+  const std::int64_t n = ncx * ncy * ncz * (std::int64_t)ppc;
+  const std::int64_t NM = s.ni_max;
+  if (ppc < 0 || first < 0) throw std::runtime_error("load_maxwellian: bad arguments");
+  if (first + n > NM) throw std::runtime_error("load_maxwellian: Ni_max exceeded");
+  const double pi = 3.14159265358979323846;
+  const bool bricks = ncx % 4 == 0 && ncy % 4 == 0 && ncz % 4 == 0;
+  SWO_OMP_FOR(g.nt)
+  for (std::int64_t id = 0; id < n; ++id) {
+    const std::int64_t cell = id / ppc;
+    std::int64_t ci, cj, ck;
+    if (bricks) {
+      const std::int64_t b = cell / 64, q = cell % 64, bx = ncx / 4, by = ncy / 4;
+      ci = (b % bx) * 4 + (q % 4);
+      cj = ((b / bx) % by) * 4 + (q / 4) % 4;
+      ck = (b / (bx * by)) * 4 + q / 16;
+    } else {
+      ci = cell % ncx;
+      cj = (cell / ncx) % ncy;
+      ck = cell / (ncx * ncy);
+    }
+    double u[12];
+    swapk::particle_uniforms(seed, stream, (std::uint64_t)id, 0u, u);
+    // physical cell (ci,cj,ck) spans nodes ci+1..ci+2 of the 1-based mesh
+    const double x0 = g.qx[ci + 1], x1 = g.qx[ci + 2];
+    const double y0 = g.qy[cj + 1], y1 = g.qy[cj + 2];
+    const double z0 = g.qz[ck + 1], z1 = g.qz[ck + 2];
+    const std::int64_t l = first + id;
+    const double v[3] = {ux + vth * std::sqrt(-std::log(u[3])) * std::cos(pi * u[4]),
+                         uy + vth * std::sqrt(-std::log(u[5])) * std::cos(pi * u[6]),
+                         uz + vth * std::sqrt(-std::log(u[7])) * std::cos(pi * u[8])};
+    xp[l] = (R)(x0 + u[0] * (x1 - x0));
+    xp[l + NM] = (R)(y0 + u[1] * (y1 - y0));
+    xp[l + 2 * NM] = (R)(z0 + u[2] * (z1 - z0));
+    for (int m = 0; m < 3; ++m) {
+      vp[l + m * NM] = (R)v[m];
+      vp1[l + m * NM] = (R)v[m];
+    }
+    mr[l] = (R)mrat;
+    bp[l] = (R)beta_p;
+  }
+  return n;
+}
 
 template <class R>
 void copy_out(const std::vector<R>& v1based, int n, R* out) {
@@ -131,6 +192,18 @@ void copy_out(const std::vector<R>& v1based, int n, R* out) {
   extern "C" void P##set_nthreads(void* h, int n) {                                                        \
     CTX(T);                                                                                                \
     c->s.nthreads = n < 1 ? 1 : n;                                                                         \
+    c->s.g.nt = c->s.nthreads;                                                                             \
+  }                                                                                                        \
+  /* The stratified Maxwellian load into the bound arrays (see load_maxwellian). */                        \
+  extern "C" int P##load_maxwellian(void* h, std::uint64_t seed, std::uint32_t stream, int ppc, double vth,  \
+                                    double ux, double uy, double uz, double mrat, double beta_p,           \
+                                    std::int64_t first, std::int64_t* count) {                             \
+    CTX(T);                                                                                                \
+    return guard(c, [&] {                                                                                  \
+      *count = load_maxwellian<T>(c->s, seed, stream, ppc, vth, ux, uy, uz, mrat, beta_p, first, c->xp,    \
+                                  c->vp, c->vp1, c->mrat, c->beta_p);                                      \
+      if (c->ni_tot) *c->ni_tot = (std::int32_t)(first + *count);                                          \
+    });                                                                                                    \
   }                                                                                                        \
   extern "C" int P##get_interp_weights(void* h, const T* xp) {                                             \
     CTX(T);                                                                                                \

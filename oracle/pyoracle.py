@@ -115,6 +115,16 @@ class Oracle:
     def set_nthreads(self, n):
         self._fn("set_nthreads")(self.h, int(n))
 
+    def load_maxwellian(self, seed, ppc, vth, u, stream=0, mrat=1.0, beta_p=1.0, first=0):
+        """The workloads' stratified Maxwellian load into the bound particle
+        arrays (oracle_capi.cpp load_maxwellian); sets Ni_tot = first + count."""
+        cnt = C.c_int64()
+        self._call("load_maxwellian", extra=(C.c_uint64(int(seed)), C.c_uint32(int(stream)), C.c_int(int(ppc)),
+                                             C.c_double(vth), C.c_double(u[0]), C.c_double(u[1]),
+                                             C.c_double(u[2]), C.c_double(mrat), C.c_double(beta_p),
+                                             C.c_int64(int(first)), C.byref(cnt)))
+        return cnt.value
+
     # gutsp.f ----------------------------------------------------------
     def get_interp_weights(self, xp):
         self._call("get_interp_weights", xp)
@@ -254,6 +264,43 @@ def initparameters(b0_init, ion_amu, nf_init, dt_frac, dx_frac, nu_init_frac, nt
        C.c_double(nu_init_frac), int(ntsub), out)
     keys = ("mion", "omega_p", "lambda_i", "dx", "dy", "delz", "dt", "dtsub_init", "nu_init", "alpha")
     return dict(zip(keys, list(out)))
+
+
+def standalone(cfg, ni_max=None, precision="f64", nthreads=1):
+    """An Oracle for a workload (a swap_gb300.hybrid.RunConfig) with its own
+    arrays of maind.f:38-70: the uniform grid of grd7, b0 = (0,0,cfg.b0) and
+    the time levels equal to it, nu = cfg.nu (grd6_setup, initial.f:54-85),
+    particles loaded by the oracle's own load_maxwellian with cfg's seed and
+    the workload's sources set.  Nothing of the product is loaded."""
+    nx, ny, nz = cfg.nodes
+    NM = int(ni_max if ni_max is not None else cfg.ni_max_hint())
+    o = Oracle(nx, ny, nz, NM, cfg.dt, cfg.ntsub, cfg.alpha, cfg.beta, grad_pe=cfg.grad_pe, precision=precision,
+               nthreads=nthreads)
+    dt = o.dtype
+    f3 = lambda: np.zeros((NM, 3), dtype=dt, order="F")
+    o.xp, o.vp, o.vp1 = f3(), f3(), f3()
+    o.mrat, o.beta_p = np.ones(NM, dtype=dt), np.ones(NM, dtype=dt)
+    o.ijkp_arr = np.zeros((1, 3), dtype=np.int32, order="F")
+    o.ni_tot = np.zeros(1, dtype=np.int32)
+    grid = lambda *c: np.zeros((nx, ny, nz) + c, dtype=dt, order="F")
+    o.b0 = grid(3)
+    o.b0[..., 2] = cfg.b0
+    for n in ("b1", "b12", "b1p2", "bt"):
+        setattr(o, n, o.b0.copy(order="F"))
+    for n in ("btc", "up", "aj", "E"):
+        setattr(o, n, grid(3))
+    o.np = grid()
+    o.nu = grid()
+    o.nu[...] = cfg.nu
+    o.input_p = np.zeros(3, dtype=dt)
+    o.bind_particles(o.xp, o.vp, o.vp1, o.mrat, o.beta_p, o.ijkp_arr, o.ni_tot)
+    o.bind_fields(o.b0, o.b1, o.b12, o.b1p2, o.bt, o.btc, o.np, o.up, o.aj, o.E, o.nu)
+    o.load_maxwellian(cfg.seed, cfg.ppc, cfg.vth, cfg.u)
+    src = cfg.make_sources()
+    if src is not None:
+        o.set_sources(src, 0)
+    o.cfg = cfg
+    return o
 
 
 def from_hybrid_arrays(h, precision="f64", nthreads=1):

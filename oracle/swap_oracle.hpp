@@ -35,6 +35,12 @@
 #include <omp.h>
 #endif
 
+// Loops over nodes or particles in which every iteration writes only its own
+// outputs run on `nt` host threads when the CPU baseline is timed; their
+// results do not depend on the thread count.  Parity runs use one thread.
+#define SWO_PRAGMA(x) _Pragma(#x)
+#define SWO_OMP_FOR(nt) SWO_PRAGMA(omp parallel for schedule(static) num_threads(nt) if ((nt) > 1))
+
 namespace swo {
 
 // ---------------------------------------------------------------------------
@@ -45,6 +51,7 @@ namespace swo {
 template <class R>
 struct Mesh {
   int nx = 0, ny = 0, nz = 0;
+  int nt = 1;         // host threads of the node and particle loops (see SWO_OMP_FOR)
   std::size_t C = 0;  // nodes, ghosts included
   R dx = 0, dy = 0, delz = 0;
   std::vector<R> qx, qy, qz;
@@ -220,44 +227,33 @@ void state_alloc(State<R>& s, std::int64_t ni_max) {
 // ---------------------------------------------------------------------------
 
 // periodic (boundary.f:9-52): ghost planes 1 and n copy nodes n-1 and 2, x
-// then y then z, for all three components.
+// then y then z, for each of the three components in turn -- the scalar fill
+// below applied to each component.
+template <class R>
+void periodic_scalar(const Mesh<R>& g, R* f);
+
 template <class R>
 void periodic(const Mesh<R>& g, R* b) {
-  const int nx = g.nx, ny = g.ny, nz = g.nz;
-  for (int m = 0; m < 3; ++m) {
-    R* f = b + g.C * m;
-    for (int k = 1; k <= nz; ++k)
-      for (int j = 1; j <= ny; ++j) {
-        f[g.n(1, j, k)] = f[g.n(nx - 1, j, k)];
-        f[g.n(nx, j, k)] = f[g.n(2, j, k)];
-      }
-    for (int k = 1; k <= nz; ++k)
-      for (int i = 1; i <= nx; ++i) {
-        f[g.n(i, 1, k)] = f[g.n(i, ny - 1, k)];
-        f[g.n(i, ny, k)] = f[g.n(i, 2, k)];
-      }
-    for (int j = 1; j <= ny; ++j)
-      for (int i = 1; i <= nx; ++i) {
-        f[g.n(i, j, 1)] = f[g.n(i, j, nz - 1)];
-        f[g.n(i, j, nz)] = f[g.n(i, j, 2)];
-      }
-  }
+  for (int m = 0; m < 3; ++m) periodic_scalar(g, b + g.C * m);
 }
 
 // periodic_scalar (boundary.f:167-206)
 template <class R>
 void periodic_scalar(const Mesh<R>& g, R* f) {
   const int nx = g.nx, ny = g.ny, nz = g.nz;
+  SWO_OMP_FOR(g.nt)
   for (int k = 1; k <= nz; ++k)
     for (int j = 1; j <= ny; ++j) {
       f[g.n(1, j, k)] = f[g.n(nx - 1, j, k)];
       f[g.n(nx, j, k)] = f[g.n(2, j, k)];
     }
+  SWO_OMP_FOR(g.nt)
   for (int k = 1; k <= nz; ++k)
     for (int i = 1; i <= nx; ++i) {
       f[g.n(i, 1, k)] = f[g.n(i, ny - 1, k)];
       f[g.n(i, ny, k)] = f[g.n(i, 2, k)];
     }
+  SWO_OMP_FOR(g.nt)
   for (int j = 1; j <= ny; ++j)
     for (int i = 1; i <= nx; ++i) {
       f[g.n(i, j, 1)] = f[g.n(i, j, nz - 1)];
@@ -275,9 +271,10 @@ template <class R>
 void face_to_center(const Mesh<R>& g, R* v, R* vc) {
   periodic(g, v);
   const std::size_t C = g.C;
-  for (int i = 2; i <= g.nx; ++i)
+  SWO_OMP_FOR(g.nt)
+  for (int k = 2; k <= g.nz; ++k)
     for (int j = 2; j <= g.ny; ++j)
-      for (int k = 2; k <= g.nz; ++k) {
+      for (int i = 2; i <= g.nx; ++i) {
         const std::size_t o = g.n(i, j, k);
         vc[o] = g.xrat[i] * (v[o] - v[g.n(i - 1, j, k)]) + v[g.n(i - 1, j, k)];
         vc[o + C] = g.yrat[j] * (v[o + C] - v[g.n(i, j - 1, k) + C]) + v[g.n(i, j - 1, k) + C];
@@ -312,6 +309,7 @@ inline void edge_center_at(const Mesh<R>& g, const R* bt, int i, int j, int k, R
 template <class R>
 void edge_to_center(const Mesh<R>& g, R* bt, R* btc) {
   periodic(g, bt);
+  SWO_OMP_FOR(g.nt)
   for (int k = 2; k <= g.nz - 1; ++k)
     for (int j = 2; j <= g.ny - 1; ++j)
       for (int i = 2; i <= g.nx - 1; ++i) edge_center_at(g, bt, i, j, k, btc);
@@ -325,11 +323,13 @@ void edge_to_center(const Mesh<R>& g, R* bt, R* btc) {
 template <class R>
 void edge_to_face(const Mesh<R>& g, R* bt, R* btmf, R* btc_local) {
   periodic(g, bt);
+  SWO_OMP_FOR(g.nt)
   for (int k = 2; k <= g.nz; ++k)
     for (int j = 2; j <= g.ny; ++j)
       for (int i = 2; i <= g.nx; ++i) edge_center_at(g, bt, i, j, k, btc_local);
   periodic(g, btc_local);
   const std::size_t C = g.C;
+  SWO_OMP_FOR(g.nt)
   for (int k = 2; k <= g.nz - 1; ++k)
     for (int j = 2; j <= g.ny - 1; ++j)
       for (int i = 2; i <= g.nx - 1; ++i) {
@@ -353,6 +353,7 @@ void crossf2(State<R>& s, R* aa, R* btc, R* cc) {
   R* ct = s.ct.data();
   periodic(g, aa);
   periodic(g, btc);
+  SWO_OMP_FOR(g.nt)
   for (int k = 2; k <= g.nz - 1; ++k)
     for (int j = 2; j <= g.ny - 1; ++j)
       for (int i = 2; i <= g.nx - 1; ++i) {
@@ -364,6 +365,7 @@ void crossf2(State<R>& s, R* aa, R* btc, R* cc) {
         ct[o + 2 * C] = ax * by - ay * bx;
       }
   periodic(g, ct);
+  SWO_OMP_FOR(g.nt)
   for (int k = 2; k <= g.nz - 1; ++k)
     for (int j = 2; j <= g.ny - 1; ++j)
       for (int i = 2; i <= g.nx - 1; ++i) {
@@ -383,6 +385,7 @@ void curlB(State<R>& s, R* b1, const R* np, R* aj) {
   const Mesh<R>& g = s.g;
   const std::size_t C = g.C;
   periodic(g, b1);
+  SWO_OMP_FOR(g.nt)
   for (int k = 2; k <= g.nz - 1; ++k)
     for (int j = 2; j <= g.ny - 1; ++j)
       for (int i = 2; i <= g.nx - 1; ++i) {
@@ -405,9 +408,10 @@ void curlB(State<R>& s, R* b1, const R* np, R* aj) {
 template <class R>
 void curlE(const Mesh<R>& g, const R* E, R* curl_E) {
   const std::size_t C = g.C;
-  for (int i = 2; i <= g.nx - 1; ++i)
+  SWO_OMP_FOR(g.nt)
+  for (int k = 2; k <= g.nz - 1; ++k)
     for (int j = 2; j <= g.ny - 1; ++j)
-      for (int k = 2; k <= g.nz - 1; ++k) {
+      for (int i = 2; i <= g.nx - 1; ++i) {
         const std::size_t o = g.n(i, j, k);
         curl_E[o] = (E[g.n(i, j + 1, k) + 2 * C] - E[o + 2 * C]) / g.dy_grid[j] +
                     (E[o + C] - E[g.n(i, j, k + 1) + C]) / g.dz_grid[k];
@@ -442,6 +446,7 @@ void get_E(State<R>& s, R* E, R* bt, R* aj, const R* up, const R* np, const R* n
   const Mesh<R>& g = s.g;
   const std::size_t C = g.C;
   R* a = s.a.data();
+  SWO_OMP_FOR(g.nt)
   for (int k = 2; k <= g.nz - 1; ++k)
     for (int j = 2; j <= g.ny - 1; ++j)
       for (int i = 2; i <= g.nx - 1; ++i)
@@ -453,6 +458,7 @@ void get_E(State<R>& s, R* E, R* bt, R* aj, const R* up, const R* np, const R* n
   edge_to_center(g, bt, s.btcl.data());   // gutsf.f:1074
   crossf2(s, s.aa.data(), s.btcl.data(), s.c.data());  // gutsf.f:1075
   const R* c = s.c.data();
+  SWO_OMP_FOR(g.nt)
   for (int k = 2; k <= g.nz - 1; ++k)
     for (int j = 2; j <= g.ny - 1; ++j)
       for (int i = 2; i <= g.nx - 1; ++i)
@@ -473,6 +479,7 @@ void predict_B(State<R>& s, R* b0, R* b1, R* b12, R* b1p2, R* bt, R* E, R* aj, R
   get_E(s, E, bt, aj, up, np, nu);
   curlE(g, E, s.curl_E.data());
   const R* ce = s.curl_E.data();
+  SWO_OMP_FOR(g.nt)
   for (int k = 2; k <= g.nz - 1; ++k)
     for (int j = 2; j <= g.ny - 1; ++j)
       for (int i = 2; i <= g.nx - 1; ++i)
@@ -491,9 +498,11 @@ void get_Ep1(State<R>& s, R* E, R* b1, R* b1p2, R* aj, const R* up, const R* np,
   const Mesh<R>& g = s.g;
   const std::size_t C = g.C;
   R* btp1 = s.btp1.data();
+  SWO_OMP_FOR(g.nt)
   for (std::size_t o = 0; o < 3 * C; ++o) btp1[o] = R(0.5) * (b1p2[o] + b1[o]);  // :1210-1219
   curlB(s, btp1, np, aj);  // gutsf.f:1221
   R* a = s.a.data();
+  SWO_OMP_FOR(g.nt)
   for (int k = 2; k <= g.nz - 1; ++k)
     for (int j = 2; j <= g.ny - 1; ++j)
       for (int i = 2; i <= g.nx - 1; ++i)
@@ -506,6 +515,7 @@ void get_Ep1(State<R>& s, R* E, R* b1, R* b1p2, R* aj, const R* up, const R* np,
   face_to_center(g, s.btp1mf.data(), s.btcl.data());     // :1269
   crossf2(s, s.aa.data(), s.btcl.data(), s.c.data());    // :1276
   const R* c = s.c.data();
+  SWO_OMP_FOR(g.nt)
   for (int k = 2; k <= g.nz - 1; ++k)
     for (int j = 2; j <= g.ny - 1; ++j)
       for (int i = 2; i <= g.nx - 1; ++i)
@@ -526,6 +536,7 @@ void correct_B(State<R>& s, R* b0, R* b1, R* b1p2, R* E, R* aj, R* up, R* np, R*
   get_Ep1(s, E, b1, b1p2, aj, up, np, nu);
   curlE(g, E, s.curl_E.data());
   const R* ce = s.curl_E.data();
+  SWO_OMP_FOR(g.nt)
   for (int k = 2; k <= g.nz - 1; ++k)
     for (int j = 2; j <= g.ny - 1; ++j)
       for (int i = 2; i <= g.nx - 1; ++i)
@@ -539,6 +550,7 @@ void correct_B(State<R>& s, R* b0, R* b1, R* b1p2, R* E, R* aj, R* up, R* np, R*
 // f_update_tlev (gutsf.f:10-35): bt <- b1p2, b12 <- b1, b1 <- b1p2.
 template <class R>
 void f_update_tlev(const Mesh<R>& g, R* b1, R* b12, R* b1p2, R* bt) {
+  SWO_OMP_FOR(g.nt)
   for (std::size_t o = 0; o < 3 * g.C; ++o) {
     bt[o] = b1p2[o];
     b12[o] = b1[o];
@@ -642,10 +654,13 @@ inline void corner_nodes(const Mesh<R>& g, int i, int j, int k, std::size_t nd[8
 template <class R>
 void fold_scalar(const Mesh<R>& g, R* f) {
   const int nx = g.nx, ny = g.ny, nz = g.nz;
+  SWO_OMP_FOR(g.nt)
   for (int k = 1; k <= nz; ++k)
     for (int j = 1; j <= ny; ++j) f[g.n(nx - 1, j, k)] = f[g.n(nx - 1, j, k)] + f[g.n(1, j, k)];
+  SWO_OMP_FOR(g.nt)
   for (int k = 1; k <= nz; ++k)
     for (int i = 1; i <= nx; ++i) f[g.n(i, ny - 1, k)] = f[g.n(i, ny - 1, k)] + f[g.n(i, 1, k)];
+  SWO_OMP_FOR(g.nt)
   for (int j = 1; j <= ny; ++j)
     for (int i = 1; i <= nx; ++i) f[g.n(i, j, nz - 1)] = f[g.n(i, j, nz - 1)] + f[g.n(i, j, 1)];
 }
@@ -728,9 +743,10 @@ void update_up(State<R>& s, const R* vp, const R* np, R* up, const R* beta_p, st
   });
   for (int m = 0; m < 3; ++m) fold_scalar(g, ct + C * m);  // gutsp.f:1803-1805
   periodic(g, ct);                                          // gutsp.f:1808
-  for (int i = 1; i <= g.nx - 1; ++i)                       // gutsp.f:1825-1836
+  SWO_OMP_FOR(g.nt)
+  for (int k = 1; k <= g.nz - 1; ++k)                       // gutsp.f:1825-1836
     for (int j = 1; j <= g.ny - 1; ++j)
-      for (int k = 1; k <= g.nz - 1; ++k) {
+      for (int i = 1; i <= g.nx - 1; ++i) {
         const std::size_t o = g.n(i, j, k);
         up[o] = R(0.5) * (ct[o] + ct[g.n(i + 1, j, k)]);
         up[o + C] = R(0.5) * (ct[o + C] + ct[g.n(i, j + 1, k) + C]);
@@ -794,9 +810,10 @@ void get_temperature(State<R>& s, const R* vp, const R* np, R* temp_p, const R* 
     });
     for (int m = 0; m < 3; ++m) fold_scalar(g, ct + C * m);  // gutsp.f:2373-2375, 2485-2487
     periodic(g, ct);
-    for (int i = 1; i <= g.nx - 1; ++i)  // gutsp.f:2395-2403, 2507-2515
+    SWO_OMP_FOR(g.nt)
+    for (int k = 1; k <= g.nz - 1; ++k)  // gutsp.f:2395-2403, 2507-2515
       for (int j = 1; j <= g.ny - 1; ++j)
-        for (int k = 1; k <= g.nz - 1; ++k) {
+        for (int i = 1; i <= g.nx - 1; ++i) {
           const std::size_t o = g.n(i, j, k);
           out[o] = R(0.5) * (ct[o] + ct[g.n(i + 1, j, k)]);
           out[o + C] = R(0.5) * (ct[o + C] + ct[g.n(i, j + 1, k) + C]);
@@ -821,6 +838,7 @@ void extrapol_up(State<R>& s, R* up, const R* vp, const R* vp1, const R* np, con
   const std::int64_t NM = s.ni_max;
   R* vn = s.v_tmp.data();
   for (int m = 0; m < 3; ++m)
+    SWO_OMP_FOR(s.g.nt)
     for (std::int64_t l = 0; l < ni_tot; ++l)
       vn[l + m * NM] = R(1.5) * vp[l + m * NM] - R(0.5) * vp1[l + m * NM];
   update_up(s, vn, np, up, beta_p, ni_tot);
@@ -893,6 +911,7 @@ void get_vplus_vminus(State<R>& s, const R* Ep, const R* btc, const R* vp, R* vp
   const std::size_t C = g.C;
   const R dt = s.dt;
   for (int m = 0; m < 3; ++m)
+    SWO_OMP_FOR(g.nt)
     for (std::int64_t l = 0; l < ni_tot; ++l)
       vminus[l + m * NM] = vp[l + m * NM] + R(0.5) * dt * Ep[l + m * NM];  // gutsp.f:302-305
 #pragma omp parallel for schedule(static) num_threads(s.nthreads) if (s.nthreads > 1)
@@ -928,6 +947,7 @@ void improve_up(State<R>& s, R* vp1, const R* vplus, const R* vminus, R* up, con
                 std::int64_t ni_tot) {
   const std::int64_t NM = s.ni_max;
   for (int m = 0; m < 3; ++m)
+    SWO_OMP_FOR(s.g.nt)
     for (std::int64_t l = 0; l < ni_tot; ++l)
       vp1[l + m * NM] = R(0.5) * (vplus[l + m * NM] + vminus[l + m * NM]);
   update_up(s, vp1, np, up, beta_p, ni_tot);
@@ -938,6 +958,7 @@ template <class R>
 void get_vp_final(State<R>& s, const R* Ep, R* vp, R* vp1, const R* vplus, std::int64_t ni_tot) {
   const std::int64_t NM = s.ni_max;
   for (int m = 0; m < 3; ++m)
+    SWO_OMP_FOR(s.g.nt)
     for (std::int64_t l = 0; l < ni_tot; ++l) {
       vp1[l + m * NM] = vp[l + m * NM];
       vp[l + m * NM] = vplus[l + m * NM] + R(0.5) * s.dt * Ep[l + m * NM];
@@ -951,6 +972,7 @@ void move_ion_half(State<R>& s, R* xp, const R* vp, std::int64_t ni_tot, bool x_
   const Mesh<R>& g = s.g;
   const std::int64_t NM = s.ni_max;
   const R dth = s.dt / R(2.);
+  SWO_OMP_FOR(g.nt)
   for (std::int64_t l = 0; l < ni_tot; ++l) {
     R x = xp[l] + dth * vp[l];
     R y = xp[l + NM] + dth * vp[l + NM];
@@ -1157,32 +1179,68 @@ std::int64_t ionize_sw(State<R>& s, const Sources& src, std::int64_t step, R* xp
 
 // Stable removal of every particle with keep[l] == 0: the bulk form of
 // remove_ion's order-preserving shift (gutsp.f:29-41).  Returns the new count.
+// On more than one host thread the kept ions' destinations come from a
+// blocked prefix count and each array moves through the scratch v_tmp, which
+// gives the same arrays as the sequential shift.
 template <class R>
-std::int64_t compact(const State<R>& s, const std::vector<char>& keep, R* xp, R* vp, R* vp1, R* mrat, R* beta_p,
+std::int64_t compact(State<R>& s, const std::vector<char>& keep, R* xp, R* vp, R* vp1, R* mrat, R* beta_p,
                      std::int64_t ni_tot) {
   const std::int64_t NM = s.ni_max;
-  std::int64_t w = 0;
-  for (std::int64_t l = 0; l < ni_tot; ++l) {
-    if (!keep[(std::size_t)l]) continue;
-    if (w != l)
-      for (int m = 0; m < 3; ++m) {
-        xp[w + m * NM] = xp[l + m * NM];
-        vp[w + m * NM] = vp[l + m * NM];
-        vp1[w + m * NM] = vp1[l + m * NM];
-      }
-    mrat[w] = mrat[l];
-    beta_p[w] = beta_p[l];
-    ++w;
+  const int T = std::max(1, s.g.nt);
+  if (T == 1 || ni_tot < 4096) {
+    std::int64_t w = 0;
+    for (std::int64_t l = 0; l < ni_tot; ++l) {
+      if (!keep[(std::size_t)l]) continue;
+      if (w != l)
+        for (int m = 0; m < 3; ++m) {
+          xp[w + m * NM] = xp[l + m * NM];
+          vp[w + m * NM] = vp[l + m * NM];
+          vp1[w + m * NM] = vp1[l + m * NM];
+        }
+      mrat[w] = mrat[l];
+      beta_p[w] = beta_p[l];
+      ++w;
+    }
+    return w;
   }
+  const std::int64_t B = (ni_tot + T - 1) / T;
+  std::vector<std::int64_t> off((std::size_t)T + 1, 0);
+  SWO_OMP_FOR(T)
+  for (int t = 0; t < T; ++t) {
+    std::int64_t c = 0;
+    for (std::int64_t l = t * B; l < std::min(ni_tot, (t + 1) * B); ++l) c += keep[(std::size_t)l] ? 1 : 0;
+    off[(std::size_t)t + 1] = c;
+  }
+  for (int t = 0; t < T; ++t) off[(std::size_t)t + 1] += off[(std::size_t)t];
+  const std::int64_t w = off[(std::size_t)T];
+  R* tmp = s.v_tmp.data();
+  auto move = [&](R* a) {
+    SWO_OMP_FOR(T)
+    for (int t = 0; t < T; ++t) {
+      std::int64_t d = off[(std::size_t)t];
+      for (std::int64_t l = t * B; l < std::min(ni_tot, (t + 1) * B); ++l)
+        if (keep[(std::size_t)l]) tmp[d++] = a[l];
+    }
+    SWO_OMP_FOR(T)
+    for (std::int64_t l = 0; l < w; ++l) a[l] = tmp[l];
+  };
+  for (int m = 0; m < 3; ++m) {
+    move(xp + m * NM);
+    move(vp + m * NM);
+    move(vp1 + m * NM);
+  }
+  move(mrat);
+  move(beta_p);
   return w;
 }
 
 // Outflow: after a half move with the x axis open, particles with
 // x > q(nx-1) or x <= q(1) leave the box.
 template <class R>
-std::int64_t remove_outflow_x(const State<R>& s, R* xp, R* vp, R* vp1, R* mrat, R* beta_p, std::int64_t ni_tot) {
+std::int64_t remove_outflow_x(State<R>& s, R* xp, R* vp, R* vp1, R* mrat, R* beta_p, std::int64_t ni_tot) {
   const Mesh<R>& g = s.g;
   std::vector<char> keep((std::size_t)ni_tot);
+  SWO_OMP_FOR(g.nt)
   for (std::int64_t l = 0; l < ni_tot; ++l) keep[(std::size_t)l] = xp[l] > g.qx[1] && xp[l] <= g.qx[g.nx - 1];
   return compact(s, keep, xp, vp, vp1, mrat, beta_p, ni_tot);
 }

@@ -254,20 +254,9 @@ __global__ void k_weights(Geo g, PartDev p, long long N, int* err) {
       p.ijk[l] = 1; p.ijk[l + p.NM] = 1; p.ijk[l + 2 * p.NM] = 1;
       continue;
     }
-    const double vol = 1.0 / ((g.qx[i + 1] - g.qx[i]) * (g.qy[j + 1] - g.qy[j]) * (g.qz[k + 1] - g.qz[k]));
-    const double x1 = fabs(x - g.qx[i]), x2 = fabs(x - g.qx[i + 1]);
-    const double y1 = fabs(y - g.qy[j]), y2 = fabs(y - g.qy[j + 1]);
-    const double z1 = fabs(z - g.qz[k]), z2 = fabs(z - g.qz[k + 1]);
-    double* w = p.wght;
-    const long long NM = p.NM;
-    w[l] = x2 * y2 * z2 * vol;
-    w[l + NM] = x1 * y2 * z2 * vol;
-    w[l + 2 * NM] = x2 * y2 * z1 * vol;
-    w[l + 3 * NM] = x1 * y2 * z1 * vol;
-    w[l + 4 * NM] = x2 * y1 * z2 * vol;
-    w[l + 5 * NM] = x1 * y1 * z2 * vol;
-    w[l + 6 * NM] = x2 * y1 * z1 * vol;
-    w[l + 7 * NM] = x1 * y1 * z1 * vol;
+    double w[8];
+    weights8(g, i, j, k, x, y, z, w);
+    for (int c = 0; c < 8; ++c) p.wght[l + c * p.NM] = w[c];
   }
 }
 
@@ -282,25 +271,6 @@ __device__ __forceinline__ void corners(const Geo& g, int i, int j, int k, long 
   const long long o = nidx(g, i, j, k), sy = g.nx, sz = (long long)g.nx * g.ny;
   nd[0] = o; nd[1] = o + 1; nd[2] = o + sz; nd[3] = o + 1 + sz;
   nd[4] = o + sy; nd[5] = o + 1 + sy; nd[6] = o + sy + sz; nd[7] = o + 1 + sy + sz;
-}
-
-// Deposit target of a raw corner after the periodic fold (gutsp.f:1496-1498,
-// 1803-1805) and the ghost overwrite of periodic_scalar/periodic: plane 1 goes
-// to plane n-1, plane n is discarded.  Returns -1 for a discarded corner.
-__device__ __forceinline__ long long fold_target(const Geo& g, int i, int j, int k) {
-  if (i == g.nx || j == g.ny || k == g.nz) return -1;
-  return nidx(g, i == 1 ? g.nx - 1 : i, j == 1 ? g.ny - 1 : j, k == 1 ? g.nz - 1 : k);
-}
-
-__device__ __forceinline__ void corner_targets(const Geo& g, int i, int j, int k, long long tg[8]) {
-  tg[0] = fold_target(g, i, j, k);
-  tg[1] = fold_target(g, i + 1, j, k);
-  tg[2] = fold_target(g, i, j, k + 1);
-  tg[3] = fold_target(g, i + 1, j, k + 1);
-  tg[4] = fold_target(g, i, j + 1, k);
-  tg[5] = fold_target(g, i + 1, j + 1, k);
-  tg[6] = fold_target(g, i, j + 1, k + 1);
-  tg[7] = fold_target(g, i + 1, j + 1, k + 1);
 }
 
 // update_np deposit (gutsp.f:1461-1493) into the folded node.

@@ -92,4 +92,44 @@ __device__ __forceinline__ int cell_search(const double* __restrict__ q, int n, 
   return i;
 }
 
+// The eight interpolation weights of a particle at (x,y,z) in cell (i,j,k),
+// in the reference's order (000,100,001,101,010,110,011,111 over x,z,y;
+// gutsp.f:1414-1429).  Units compiled with --fmad=false round every product
+// like the Fortran.
+__device__ __forceinline__ void weights8(const Geo& g, int i, int j, int k, double x, double y, double z,
+                                         double w[8]) {
+  const double vol = 1.0 / ((g.qx[i + 1] - g.qx[i]) * (g.qy[j + 1] - g.qy[j]) * (g.qz[k + 1] - g.qz[k]));
+  const double x1 = fabs(x - g.qx[i]), x2 = fabs(x - g.qx[i + 1]);
+  const double y1 = fabs(y - g.qy[j]), y2 = fabs(y - g.qy[j + 1]);
+  const double z1 = fabs(z - g.qz[k]), z2 = fabs(z - g.qz[k + 1]);
+  w[0] = x2 * y2 * z2 * vol;
+  w[1] = x1 * y2 * z2 * vol;
+  w[2] = x2 * y2 * z1 * vol;
+  w[3] = x1 * y2 * z1 * vol;
+  w[4] = x2 * y1 * z2 * vol;
+  w[5] = x1 * y1 * z2 * vol;
+  w[6] = x2 * y1 * z1 * vol;
+  w[7] = x1 * y1 * z1 * vol;
+}
+
+// Deposit target of a raw corner after the periodic fold (gutsp.f:1496-1498,
+// 1803-1805) and the ghost overwrite of periodic_scalar/periodic: plane 1 goes
+// to plane n-1, plane n is discarded.  Returns -1 for a discarded corner.
+__device__ __forceinline__ long long fold_target(const Geo& g, int i, int j, int k) {
+  if (i == g.nx || j == g.ny || k == g.nz) return -1;
+  return nidx(g, i == 1 ? g.nx - 1 : i, j == 1 ? g.ny - 1 : j, k == 1 ? g.nz - 1 : k);
+}
+
+// The folded targets of the eight corners, in the weights' order.
+__device__ __forceinline__ void corner_targets(const Geo& g, int i, int j, int k, long long tg[8]) {
+  tg[0] = fold_target(g, i, j, k);
+  tg[1] = fold_target(g, i + 1, j, k);
+  tg[2] = fold_target(g, i, j, k + 1);
+  tg[3] = fold_target(g, i + 1, j, k + 1);
+  tg[4] = fold_target(g, i, j + 1, k);
+  tg[5] = fold_target(g, i + 1, j + 1, k);
+  tg[6] = fold_target(g, i, j + 1, k + 1);
+  tg[7] = fold_target(g, i + 1, j + 1, k + 1);
+}
+
 }  // namespace swapk

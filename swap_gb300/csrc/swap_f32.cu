@@ -718,6 +718,17 @@ extern "C" int swap_f32_count(swap_ctx* c, int64_t* n) {
   return SWAP_OK;
 }
 
+extern "C" int swap_f32_key_starts(swap_ctx* c, int64_t* starts, int64_t n) {
+  if (!c || !starts) return SWAP_EINVAL;
+  F32State* s = f32(c);
+  if (!s || s->ended) return c->fail(SWAP_EINVAL, "no running FP32 state (swap_f32_begin first)");
+  if (n < s->g.nkeys + 1) return c->fail(SWAP_EINVAL, "starts holds fewer than nkeys + 1 entries");
+  CU(cudaMemcpyAsync(starts, s->start, (std::size_t)(s->g.nkeys + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost,
+                     c->st));
+  CU(cudaStreamSynchronize(c->st));
+  return SWAP_OK;
+}
+
 extern "C" int swap_f32_energy(swap_ctx* c, double out[4]) {
   if (!c || !out) return SWAP_EINVAL;
   F32State* s = f32(c);

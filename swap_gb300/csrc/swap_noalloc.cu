@@ -5,32 +5,41 @@
 // device memory belongs to another allocator -- for example a process in
 // which a framework's caching allocator has already reserved the GPU's
 // memory, so a direct cudaMalloc fails or fragments that pool.  Another is a
-// caller driving its own asynchronous pipeline: cudaMalloc and cudaFree can
-// synchronize the device, which such a caller cannot afford inside its time
-// step.  Neither can create a swap_ctx, because swap_init allocates the
-// device mirrors and scratch.  This entry takes the caller's own device
-// arrays for every input and output and keeps its one scratch array -- the
-// per-node velocity sums -- in a file-scope __device__ array instead.
+// caller driving its own asynchronous pipeline on several streams: cudaMalloc
+// and cudaFree can synchronize the whole device, every stream of it, which
+// such a caller cannot afford inside its time step.  (This entry waits only
+// for the one stream it is given: it returns after that stream has finished
+// its work, to read the out-of-grid flag.)  Neither caller can create a
+// swap_ctx, because swap_init allocates the device mirrors and scratch.  This
+// entry takes the caller's own device arrays for every input and output and
+// keeps its one scratch array -- the grid coordinates and the per-node
+// velocity sums -- in a file-scope __device__ array instead.
 //
 // Properties:
 //  * scratch is static: every GPU that loads this library holds it
 //    (SWAP_NOALLOC_SCRATCH_BYTES) until the process exits;
 //  * the first call on a device looks up the scratch address with
-//    cudaGetSymbolAddress (no allocation); make that first call before any
-//    stream capture;
+//    cudaGetSymbolAddress (no allocation) and keeps it for the process; make
+//    that first call before any stream capture, and do not call the entry
+//    again on a device after cudaDeviceReset on it (the module is loaded
+//    anew and the kept address is stale);
 //  * all calls share the scratch, so calls that overlap on the GPU (two
-//    streams, two threads) race; serialize them;
+//    streams, two threads) race; serialize them.  After an error the entry
+//    waits for its stream before it returns, so no work of the failed call
+//    is still running when the caller tries again;
 //  * sizes beyond SWAP_NOALLOC_MAX_NODES nodes or SWAP_NOALLOC_MAX_AXIS
 //    nodes on an axis are rejected with SWAP_ECAPACITY.
 //
-// Compiled with --fmad=false like the FP64 drop-in, so the result equals
-// swap_update_up up to the order of the atomic sums.
+// The cell search, weights and fold are the FP64 drop-in's own
+// (swap_dev.cuh), and the unit is compiled with --fmad=false like it, so the
+// result equals swap_update_up up to the order of the atomic sums.
 #include <cstdint>
 #include <mutex>
 
 #include <cuda_runtime.h>
 
 #include "../../include/swap_gpu.h"
+#include "swap_dev.cuh"
 
 namespace {
 
@@ -69,65 +78,26 @@ int setup(double** scratch, int** flag) {
   return SWAP_OK;
 }
 
-struct NaGeo {
-  int nx, ny, nz;
-  long long C;
-  const double *qx, *qy, *qz;  // 1-based, in the scratch
-  double dy, inv_dx, inv_dz;
-};
-
-__device__ __forceinline__ long long na_idx(const NaGeo& g, int i, int j, int k) {
-  return (long long)(i - 1) + (long long)g.nx * ((long long)(j - 1) + (long long)g.ny * (long long)(k - 1));
-}
-
-// q(i) < x <= q(i+1): the linear search of gutsp.f:1396-1401.
-__device__ __forceinline__ int na_search(const double* q, int n, double x, double inv_d) {
-  if (!(x > q[1]) || x > q[n]) return 0;
-  int i = (int)((x - q[1]) * inv_d) + 1;
-  i = i < 1 ? 1 : (i > n - 1 ? n - 1 : i);
-  while (i > 1 && !(x > q[i])) --i;
-  while (i < n - 1 && x > q[i + 1]) ++i;
-  return i;
-}
-
-// Folded deposit target (gutsp.f:1803-1805 + periodic): plane 1 -> n-1,
-// plane n dropped.
-__device__ __forceinline__ long long na_fold(const NaGeo& g, int i, int j, int k) {
-  if (i == g.nx || j == g.ny || k == g.nz) return -1;
-  return na_idx(g, i == 1 ? g.nx - 1 : i, j == 1 ? g.ny - 1 : j, k == 1 ? g.nz - 1 : k);
-}
+using swapk::Geo;
 
 // Weights (gutsp.f:1414-1429) and the update_up deposit (gutsp.f:1676-1800)
 // of one particle into S = sum v*w/volb at folded nodes.
-__global__ void k_na_deposit(NaGeo g, const double* __restrict__ xp, const double* __restrict__ vp,
+__global__ void k_na_deposit(Geo g, const double* __restrict__ xp, const double* __restrict__ vp,
                              const double* __restrict__ beta_p, long long N, long long NM, double beta,
                              double* __restrict__ S, int* flag) {
   for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x) {
     const double x = xp[l], y = xp[l + NM], z = xp[l + 2 * NM];
-    const int i = na_search(g.qx, g.nx, x, g.inv_dx);
+    const int i = swapk::cell_search(g.qx, g.nx, x, g.inv_dx);
     const int j = (int)floor(y / g.dy);
-    const int k = na_search(g.qz, g.nz, z, g.inv_dz);
+    const int k = swapk::cell_search(g.qz, g.nz, z, g.inv_dz);
     if (i < 1 || j < 1 || j >= g.ny || k < 1) {
       atomicCAS(flag, 0, SWAP_EDOMAIN);
       continue;
     }
-    const double vol = 1.0 / ((g.qx[i + 1] - g.qx[i]) * (g.qy[j + 1] - g.qy[j]) * (g.qz[k + 1] - g.qz[k]));
-    const double x1 = fabs(x - g.qx[i]), x2 = fabs(x - g.qx[i + 1]);
-    const double y1 = fabs(y - g.qy[j]), y2 = fabs(y - g.qy[j + 1]);
-    const double z1 = fabs(z - g.qz[k]), z2 = fabs(z - g.qz[k + 1]);
     double w[8];
-    w[0] = x2 * y2 * z2 * vol;
-    w[1] = x1 * y2 * z2 * vol;
-    w[2] = x2 * y2 * z1 * vol;
-    w[3] = x1 * y2 * z1 * vol;
-    w[4] = x2 * y1 * z2 * vol;
-    w[5] = x1 * y1 * z2 * vol;
-    w[6] = x2 * y1 * z1 * vol;
-    w[7] = x1 * y1 * z1 * vol;
-    const long long tg[8] = {na_fold(g, i, j, k),         na_fold(g, i + 1, j, k),
-                             na_fold(g, i, j, k + 1),     na_fold(g, i + 1, j, k + 1),
-                             na_fold(g, i, j + 1, k),     na_fold(g, i + 1, j + 1, k),
-                             na_fold(g, i, j + 1, k + 1), na_fold(g, i + 1, j + 1, k + 1)};
+    swapk::weights8(g, i, j, k, x, y, z, w);
+    long long tg[8];
+    swapk::corner_targets(g, i, j, k, tg);
     const double volb =
         (g.qx[i + 1] - g.qx[i]) * (g.qy[j + 1] - g.qy[j]) * (g.qz[k + 1] - g.qz[k]) * beta * beta_p[l];
     const double ivolb = 1.0 / volb;
@@ -142,28 +112,24 @@ __global__ void k_na_deposit(NaGeo g, const double* __restrict__ xp, const doubl
   }
 }
 
-__device__ __forceinline__ int na_wrap(int i, int n) { return i == 1 ? n - 1 : (i == n ? 2 : i); }
-
 // ct(node) = S/np at the node's interior image (zero where np = 0), then the
 // face average up_m = 0.5*(ct_m(node) + ct_m(node+e_m)) (gutsp.f:1825-1836)
 // on the interior.
-__device__ __forceinline__ double na_ct(const NaGeo& g, const double* S, const double* np, int i, int j, int k,
+__device__ __forceinline__ double na_ct(const Geo& g, const double* S, const double* np, int i, int j, int k,
                                         int m) {
-  const long long o = na_idx(g, na_wrap(i, g.nx), na_wrap(j, g.ny), na_wrap(k, g.nz));
+  const long long o = swapk::nidx(g, swapk::wrapn(i, g.nx), swapk::wrapn(j, g.ny), swapk::wrapn(k, g.nz));
   const double n = np[o];
   return n == 0.0 ? 0.0 : S[o + g.C * m] / n;
 }
 
-__global__ void k_na_up(NaGeo g, const double* __restrict__ S, const double* __restrict__ np,
+__global__ void k_na_up(Geo g, const double* __restrict__ S, const double* __restrict__ np,
                         double* __restrict__ up) {
-  const long long ix = g.nx - 2, iy = g.ny - 2;
-  const long long n_int = ix * iy * (g.nz - 2);
+  const long long n_int = swapk::n_interior(g);
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n_int;
        t += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(t % ix) + 2;
-    const int j = (int)((t / ix) % iy) + 2;
-    const int k = (int)(t / (ix * iy)) + 2;
-    const long long o = na_idx(g, i, j, k);
+    int i, j, k;
+    swapk::interior_ijk(g, t, i, j, k);
+    const long long o = swapk::nidx(g, i, j, k);
     up[o] = 0.5 * (na_ct(g, S, np, i, j, k, 0) + na_ct(g, S, np, i + 1, j, k, 0));
     up[o + g.C] = 0.5 * (na_ct(g, S, np, i, j, k, 1) + na_ct(g, S, np, i, j + 1, k, 1));
     up[o + 2 * g.C] = 0.5 * (na_ct(g, S, np, i, j, k, 2) + na_ct(g, S, np, i, j, k + 1, 2));
@@ -172,14 +138,14 @@ __global__ void k_na_up(NaGeo g, const double* __restrict__ S, const double* __r
 
 // periodic(up) (gutsp.f:1839, boundary.f:9-52): each ghost node copies its
 // interior image.
-__global__ void k_na_periodic(NaGeo g, double* __restrict__ b) {
+__global__ void k_na_periodic(Geo g, double* __restrict__ b) {
   for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < g.C; o += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(o % g.nx) + 1;
     const int j = (int)((o / g.nx) % g.ny) + 1;
     const int k = (int)(o / ((long long)g.nx * g.ny)) + 1;
-    const int wi = na_wrap(i, g.nx), wj = na_wrap(j, g.ny), wk = na_wrap(k, g.nz);
+    const int wi = swapk::wrapn(i, g.nx), wj = swapk::wrapn(j, g.ny), wk = swapk::wrapn(k, g.nz);
     if (wi == i && wj == j && wk == k) continue;
-    const long long s = na_idx(g, wi, wj, wk);
+    const long long s = swapk::nidx(g, wi, wj, wk);
     for (int m = 0; m < 3; ++m) b[o + g.C * m] = b[s + g.C * m];
   }
 }
@@ -209,14 +175,19 @@ extern "C" int swap_update_up_noalloc(const swap_dims* dims, const swap_params* 
   double* qz = scratch + 2 * kGeoLen;
   double* S = scratch + 3 * kGeoLen;
   // The scratch keeps the previous call's contents: load this call's
-  // geometry and clear the sums and the flag.
+  // geometry and clear the sums and the flag.  Once anything is queued, an
+  // error waits for the stream before returning (see the file's notes).
+  auto fail_after_enqueue = [st]() {
+    cudaStreamSynchronize(st);
+    return SWAP_ECUDA;
+  };
   if (cudaMemcpyAsync(qx + 1, coords->qx, dims->nx * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemcpyAsync(qy + 1, coords->qy, dims->ny * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemcpyAsync(qz + 1, coords->qz, dims->nz * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemsetAsync(S, 0, 3 * C * sizeof(double), st) != cudaSuccess ||
       cudaMemsetAsync(flag, 0, sizeof(int), st) != cudaSuccess)
-    return SWAP_ECUDA;
-  NaGeo g;
+    return fail_after_enqueue();
+  Geo g{};
   g.nx = dims->nx; g.ny = dims->ny; g.nz = dims->nz;
   g.C = C;
   g.qx = qx; g.qy = qy; g.qz = qz;
@@ -225,11 +196,12 @@ extern "C" int swap_update_up_noalloc(const swap_dims* dims, const swap_params* 
   g.inv_dz = 1.0 / (coords->qz[1] - coords->qz[0]);
   if (ni_tot > 0) k_na_deposit<<<na_blocks(ni_tot), 256, 0, st>>>(g, xp, vp, beta_p, ni_tot, dims->ni_max,
                                                                     params->beta, S, flag);
-  k_na_up<<<na_blocks((long long)(g.nx - 2) * (g.ny - 2) * (g.nz - 2)), 256, 0, st>>>(g, S, np, up);
+  k_na_up<<<na_blocks(swapk::n_interior(g)), 256, 0, st>>>(g, S, np, up);
   k_na_periodic<<<na_blocks(C), 256, 0, st>>>(g, up);
-  if (cudaGetLastError() != cudaSuccess) return SWAP_ECUDA;
+  if (cudaGetLastError() != cudaSuccess) return fail_after_enqueue();
   int hflag = 0;
-  if (cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return SWAP_ECUDA;
+  if (cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    return fail_after_enqueue();
   if (cudaStreamSynchronize(st) != cudaSuccess) return SWAP_ECUDA;
   return hflag ? SWAP_EDOMAIN : SWAP_OK;
 }

@@ -59,10 +59,27 @@ class RunConfig:
         """The workload's sources and sinks as an abi.Sources (None when it has none)."""
         return abi.make_sources(**self.sources) if self.sources else None
 
-    def ni_max_hint(self) -> int:
-        """Particle capacity with headroom for a workload whose count varies."""
+    def cloud_ions_per_step(self) -> float:
+        """Expected ions the cloud ionization creates per step: the sum over
+        cell centres of beta*beta_heavy*n_n*nu_ion*dt (unit cells)."""
+        q = self.sources
+        if not q.get("nu_ion"):
+            return 0.0
+        cx, cy, cz = (np.arange(c) + 1.5 for c in self.cells)
+        r2 = ((cx[:, None, None] - q["cloud_x"]) ** 2 + (cy[None, :, None] - q["cloud_y"]) ** 2
+              + (cz[None, None, :] - q["cloud_z"]) ** 2) / q["cloud_r0"] ** 2
+        dens = float(np.sum(q["cloud_N0"] / (1.0 + r2)))
+        return self.beta * q.get("beta_heavy", 1.0) * dens * q["nu_ion"] * self.dt
+
+    def ni_max_hint(self, steps: int | None = None) -> int:
+        """Particle capacity with headroom for a workload whose count varies:
+        5% for inflow and outflow, plus the cloud's new ions over `steps`
+        (default: the workload's step count)."""
         n = self.n_particles
-        return n if not self.sources else int(n * 1.05) + 4096
+        if not self.sources:
+            return n
+        cloud = self.cloud_ions_per_step() * (self.steps if steps is None else steps)
+        return int(n * 1.05 + 1.1 * cloud) + 4096
 
 
 def config(n: int, **over) -> RunConfig:
@@ -78,6 +95,10 @@ def config(n: int, **over) -> RunConfig:
        x axis, a neutral cloud N0/(1+(r/5)^2) at the box centre (N0 = 1000)
        ionized at 1e-3 Omega_i into mass-16 ions at rest, charge exchange
        sigma = 1 - 0.1 ln v_rel; 300 steps, seed 3.
+    3: the physics of 2 on 512x256x256 cells at 16 ppc (536,870,912 ions),
+       1000 steps, seed 4 (the FP32 form against an FP64 run).
+    4: 3 with a stronger B0 (2, so Omega_i dt = 0.1) and 20 field subcycles
+       per ion step, seed 5 (the learned field surrogate's workload).
     """
     base = {
         0: dict(name="uniform H+ 64x32x32, 16 ppc", cells=(64, 32, 32), ppc=16, steps=100, seed=1),
@@ -85,13 +106,17 @@ def config(n: int, **over) -> RunConfig:
                 seed=2),
         2: dict(name="pickup ions 256x128x128, 16 ppc, cloud + charge exchange", cells=(256, 128, 128), ppc=16,
                 u=(4.0, 0.0, 0.0), steps=300, seed=3),
+        3: dict(name="pickup ions 512x256x256, 16 ppc, cloud + charge exchange", cells=(512, 256, 256), ppc=16,
+                u=(4.0, 0.0, 0.0), steps=1000, seed=4),
+        4: dict(name="pickup ions 512x256x256, 16 ppc, strong B0, 20 subcycles", cells=(512, 256, 256), ppc=16,
+                u=(4.0, 0.0, 0.0), b0=2.0, ntsub=20, steps=1000, seed=5),
     }[n]
     base.update(over)
     cfg = RunConfig(**base)
-    if n in (1, 2) and "sources" not in over:
+    if n in (1, 2, 3, 4) and "sources" not in over:
         src = dict(seed=cfg.seed, x_open=1, inflow_ppc=cfg.ppc, inflow_vth=cfg.vth, inflow_ux=cfg.u[0],
                    inflow_uy=cfg.u[1], inflow_uz=cfg.u[2])
-        if n == 2:
+        if n >= 2:
             cx, cy, cz = (c / 2.0 + 1.0 for c in cfg.cells)  # box centre (q(1) = 1 with unit spacing)
             src.update(cloud_N0=1000.0, cloud_r0=5.0, cloud_x=cx, cloud_y=cy, cloud_z=cz, nu_ion=1e-3,
                        mrat_heavy=1.0 / 16.0, beta_heavy=1.0, cx_a=1.0, cx_b=0.1)
@@ -103,7 +128,10 @@ class Hybrid:
     """One context on the current GPU with the reference's arrays bound."""
 
     def __init__(self, cfg: RunConfig, ni_max: int | None = None, coords: Coords | None = None,
-                 pinned: bool = False):
+                 pinned: bool = False, work_arrays: bool = True):
+        """work_arrays=False leaves out the arrays only the per-subroutine
+        entries take (Ep, vplus, vminus, ijkp) and their device mirrors: the
+        fused steps keep their own, which saves 84 B per particle on each side."""
         self.cfg = cfg
         self.lib = abi.load()
         nx, ny, nz = cfg.nodes
@@ -117,12 +145,13 @@ class Hybrid:
         # particle arrays (maind.f:54-59, global.f:44,96,100)
         f = (lambda: self._pinned((NM, 3))) if pinned else (lambda: np.zeros((NM, 3), dtype=np.float64, order="F"))
         self.xp, self.vp, self.vp1 = f(), f(), f()
-        self.Ep, self.vplus, self.vminus = f(), f(), f()
+        if work_arrays:
+            self.Ep, self.vplus, self.vminus = f(), f(), f()
         self.mrat = self._pinned((NM,)) if pinned else np.zeros(NM, dtype=np.float64)
         self.beta_p = self._pinned((NM,)) if pinned else np.zeros(NM, dtype=np.float64)
         self.mrat[:] = 1.0
         self.beta_p[:] = 1.0
-        self.ijkp = np.zeros((NM, 3), dtype=np.int32, order="F")
+        self.ijkp = np.zeros((NM, 3) if work_arrays else (1, 3), dtype=np.int32, order="F")
         self.ni_tot = np.zeros(1, dtype=np.int32)
         # fields (maind.f:38-70)
         flds = grd6_setup(self.coords, cfg.b0, cfg.nu)
@@ -138,11 +167,12 @@ class Hybrid:
                                                        C.byref(self._coords_c)))
         self.ctx = ctx
         self._check(self.lib.swap_bind_particles(ctx, abi.dptr(self.xp), abi.dptr(self.vp), abi.dptr(self.vp1),
-                                                 abi.dptr(self.mrat), abi.dptr(self.beta_p), abi.iptr(self.ijkp),
+                                                 abi.dptr(self.mrat), abi.dptr(self.beta_p),
+                                                 abi.iptr(self.ijkp) if work_arrays else None,
                                                  abi.iptr(self.ni_tot)))
         self._check(self.lib.swap_bind_fields(ctx, *[abi.dptr(getattr(self, n)) for n in (
             "b0", "b1", "b12", "b1p2", "bt", "btc", "np", "up", "aj", "E", "nu")]))
-        for a in (self.Ep, self.vplus, self.vminus, self.input_p):
+        for a in ((self.Ep, self.vplus, self.vminus) if work_arrays else ()) + (self.input_p,):
             self._check(self.lib.swap_bind_array(ctx, a.ctypes.data_as(C.c_void_p), a.nbytes))
 
     # ---- plumbing ----
@@ -365,6 +395,13 @@ class Hybrid:
         n = C.c_int64()
         self._check(self.lib.swap_f32_count(self.ctx, C.byref(n)))
         return n.value
+
+    def f32_key_starts(self) -> np.ndarray:
+        """starts[0..nkeys] of the FP32 state's sort keys (brick * 64 + cell in the brick)."""
+        nk = int(np.prod([c // 4 for c in self.cfg.cells])) * 64
+        out = np.zeros(nk + 1, dtype=np.int64)
+        self._check(self.lib.swap_f32_key_starts(self.ctx, out.ctypes.data_as(abi.c_int64_p), nk + 1))
+        return out
 
     def f32_energy(self):
         out = np.zeros(4)

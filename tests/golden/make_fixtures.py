@@ -11,6 +11,7 @@ from __future__ import annotations
 
 import hashlib
 import json
+import os
 import struct
 import sys
 from pathlib import Path
@@ -72,4 +73,7 @@ def main(ref: Path):
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))
+    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SWAP_REFERENCE")
+    if not src:
+        sys.exit("usage: make_fixtures.py REFERENCE_DIR (or set SWAP_REFERENCE): the SWAP source tree holding b0.dat")
+    main(Path(src))
