@@ -176,6 +176,31 @@ NODE_BYTES_F32 = {
 }
 
 
+def host_available() -> int:
+    """MemAvailable of /proc/meminfo in bytes (0 if unreadable)."""
+    try:
+        for line in Path("/proc/meminfo").read_text().splitlines():
+            if line.startswith("MemAvailable:"):
+                return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return 0
+
+
+def room_for(host_bytes: float, dev_bytes: float = 0.0):
+    """None if the host and the current GPU have the room, else the reason."""
+    avail = host_available()
+    if avail and avail < host_bytes:
+        return f"needs {host_bytes / 1e9:.0f} GB of host memory, {avail / 1e9:.0f} GB available"
+    if dev_bytes:
+        import torch
+
+        free, _ = torch.cuda.mem_get_info()
+        if free < dev_bytes:
+            return f"needs {dev_bytes / 1e9:.0f} GB of device memory, {free / 1e9:.0f} GB free"
+    return None
+
+
 def config_line(cfg, ions, f32=True):
     """The workload's description in a bench line."""
     return {"workload": cfg.name, "cells": list(cfg.cells), "ppc": cfg.ppc, "ions": int(ions),
@@ -196,6 +221,11 @@ def oracle_run(cfg, precision: str, warmup: int, steps: int, threads: int) -> di
         sys.path.insert(0, str(ROOT / "oracle"))
     import pyoracle
 
+    # bytes per ion of capacity: the bound particle arrays plus the oracle's
+    # ijkp, weights, scratch velocities and push work arrays
+    why = room_for(cfg.ni_max_hint() * (112 if precision == "f32" else 224) * 1.15)
+    if why:
+        return {"skipped": why, "precision": precision}
     t0 = time.perf_counter()
     o = pyoracle.standalone(cfg, precision=precision, nthreads=threads)
     t_load = time.perf_counter() - t0
@@ -234,6 +264,9 @@ def run_reference(args):
     cfg = config(args.config)
     threads = os.cpu_count() or 1
     r = oracle_run(cfg, "f32", args.warmup, args.steps, threads)
+    if "skipped" in r:
+        print(json.dumps({"impl": "reference", "unavailable": r["skipped"]}), flush=True)
+        return 0
     sample = (f"the whole workload ({r['ions']:,.0f} ions), one full FP32 ion step of the oracle per timed step "
               f"after {args.warmup} warm-up steps, OpenMP over {threads} host threads")
     line = {
@@ -401,6 +434,12 @@ def run_compare(n: int, steps: int, cx: bool = True) -> dict:
         src.update(cx_a=0.0, cx_b=0.0)
         cfg = config(n, sources=src)
     NM = cfg.ni_max_hint(steps + 4)
+    # the FP64 context holds 260 B of device memory per ion of capacity
+    # (particles, weights, cell indices, push and compaction work arrays);
+    # the host keeps 88 B (x, v, vp1, mrat, beta_p)
+    why = room_for(NM * 88 * 1.3, NM * 270)
+    if why:
+        return {"workload": cfg.name, "skipped": why}
 
     def fresh():
         h = Hybrid(cfg, ni_max=NM, work_arrays=False)
@@ -640,7 +679,7 @@ def run_ours(args):
         run_accuracy_legs(args, line)
     if rank == 0 and not args.no_cpu_baseline:
         r = oracle_run(cfg, "f32", 1, 1, os.cpu_count() or 1)
-        line["cpu_baseline"] = {"value": r["value"], "unit": UNIT, "cores": r["threads"], "kind": "port",
+        line["cpu_baseline"] = {"skipped": r["skipped"]} if "skipped" in r else {"value": r["value"], "unit": UNIT, "cores": r["threads"], "kind": "port",
                                 "sample": f"one full FP32 ion step of the oracle over the whole workload "
                                           f"({r['ions']:,.0f} ions) after one warm-up step"}
     if rank == 0:
