@@ -9,8 +9,17 @@
  * Data model.
  *   - Arrays are the caller's host arrays in Fortran layout: grids
  *     (nx,ny,nz[,3]) column-major, x fastest, component slowest; particles
- *     (ni_max,3) column-major.  Reals are IEEE double (the reference built with
- *     -real-size 64); indices are int32 (-i4, makefile:1).
+ *     (ni_max,3) column-major.  Indices are int32 (-i4, makefile:1).
+ *   - Reals are the caller's REAL: swap_dims.real_bytes = 4 for SWAP as its
+ *     makefile builds it (makefile:1, -real-size 32: every REAL array is
+ *     float), 8 (or 0) for IEEE double.  The device computes in FP64 either
+ *     way; with 4, each registered real array is widened on its way to the
+ *     device and rounded back to float on its way to the host.  The array
+ *     parameters below are declared double*: a caller with 4-byte reals
+ *     passes its float arrays there (the entries only use the address to find
+ *     the registered array).  Scalars passed by value or through a double*
+ *     to a single value (dtsub, ntf, energy sums) are double in both
+ *     settings, and so are the coordinate arrays of swap_coords.
  *   - Every host array an entry receives must first be registered
  *     (swap_bind_particles / swap_bind_fields / swap_bind_array).  The context
  *     keeps a device mirror of each and tracks which copy is current: an entry
@@ -52,7 +61,7 @@ typedef struct swap_ctx swap_ctx;
 /* Grid and particle capacity: dimensions.f:5,9 (nx,ny,nz,Ni_max). */
 typedef struct swap_dims {
   int32_t nx, ny, nz;
-  int32_t reserved;
+  int32_t real_bytes;  /* size of the caller's REAL: 4, or 8 (0 means 8) */
   int64_t ni_max;
 } swap_dims;
 
@@ -91,7 +100,8 @@ int swap_bind_particles(swap_ctx* ctx, double* xp, double* vp, double* vp1, doub
 /* The grid arrays of maind.f:38-70. */
 int swap_bind_fields(swap_ctx* ctx, double* b0, double* b1, double* b12, double* b1p2, double* bt, double* btc,
                      double* np, double* up, double* aj, double* E, double* nu);
-/* Any other array an entry is handed (e.g. Ep, vplus, vminus). */
+/* Any other real array an entry is handed (e.g. Ep, vplus, vminus): bytes
+ * is its size in the caller's memory (real_bytes per element). */
 int swap_bind_array(swap_ctx* ctx, void* host, int64_t bytes);
 /* host = NULL: every registered array. */
 int swap_sync_to_device(swap_ctx* ctx, const void* host);
@@ -102,7 +112,8 @@ int swap_mark_host_dirty(swap_ctx* ctx, const void* host);
  * xp, vp, vp1 in the caller's memory when the host copy is current, and
  * swap_f32_end writes xp, vp, vp1, mrat and beta_p straight back (the host
  * copy becomes current, the device copy stale).  0 = always stage through
- * the device mirrors.  SWAP_EINVAL if the device cannot. */
+ * the device mirrors.  SWAP_EINVAL if the device cannot, or if the context
+ * binds 4-byte reals (the direct conversions read doubles). */
 int swap_set_host_direct(swap_ctx* ctx, int on);
 /* Bytes moved from the caller's memory to the device (h2d) and back (d2h)
  * since the last reset: mirror copies and direct reads and writes. */

@@ -80,7 +80,7 @@ struct Api {
 // ../swap_gb300/csrc/philox.h).  Ions come out by bricks of 4x4x4 cells, each
 // brick's cells x fastest, when every axis has a multiple of 4 physical
 // cells, else by cell with x fastest.  Arithmetic is in double, then rounded
-// to R.
+// to R (kept above the cell's low node in x and z, see swo::above).
 template <class R>
 std::int64_t load_maxwellian(const swo::State<R>& s, std::uint64_t seed, std::uint32_t stream, int ppc, double vth,
                              double ux, double uy, double uz, double mrat, double beta_p, std::int64_t first, R* xp,
@@ -117,9 +117,9 @@ std::int64_t load_maxwellian(const swo::State<R>& s, std::uint64_t seed, std::ui
     const double v[3] = {ux + vth * std::sqrt(-std::log(u[3])) * std::cos(pi * u[4]),
                          uy + vth * std::sqrt(-std::log(u[5])) * std::cos(pi * u[6]),
                          uz + vth * std::sqrt(-std::log(u[7])) * std::cos(pi * u[8])};
-    xp[l] = (R)(x0 + u[0] * (x1 - x0));
+    xp[l] = swo::above<R>((R)(x0 + u[0] * (x1 - x0)), (R)x0);
     xp[l + NM] = (R)(y0 + u[1] * (y1 - y0));
-    xp[l + 2 * NM] = (R)(z0 + u[2] * (z1 - z0));
+    xp[l + 2 * NM] = swo::above<R>((R)(z0 + u[2] * (z1 - z0)), (R)z0);
     for (int m = 0; m < 3; ++m) {
       vp[l + m * NM] = (R)v[m];
       vp1[l + m * NM] = (R)v[m];

@@ -26,6 +26,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <stdexcept>
 #include <vector>
 
@@ -206,6 +207,7 @@ struct State {
   // locals of the subroutines that the reference allocates per call
   std::vector<R> ajc, upc, aa, btcl, curl_E, btp1, btp1mf, btc2, v_tmp;
   int nthreads = 1;                  // >1 only for the CPU baseline timing leg
+  std::vector<std::vector<R>> priv;  // per-thread deposit grids, kept between calls
 
   std::size_t C() const { return g.C; }
 };
@@ -676,12 +678,15 @@ void deposit_loop(State<R>& s, std::int64_t ni_tot, std::size_t len, R* out, F&&
     return;
   }
 #ifdef _OPENMP
-  std::vector<std::vector<R>> priv((std::size_t)T);
+  auto& priv = s.priv;
+  if (priv.size() < (std::size_t)T) priv.resize((std::size_t)T);
 #pragma omp parallel num_threads(T)
   {
     const int t = omp_get_thread_num();
-    priv[(std::size_t)t].assign(len, R(0));
-    R* mine = priv[(std::size_t)t].data();
+    auto& mine_v = priv[(std::size_t)t];
+    if (mine_v.size() < len) mine_v.resize(len);
+    std::fill(mine_v.begin(), mine_v.begin() + (std::ptrdiff_t)len, R(0));
+    R* mine = mine_v.data();
 #pragma omp for schedule(static)
     for (std::int64_t l = 0; l < ni_tot; ++l) body(l, mine);
 #pragma omp for schedule(static)
@@ -1135,6 +1140,17 @@ inline void draw4(const Sources& s, std::uint32_t stream, std::int64_t step, std
   swapk::source_uniforms(s.seed, stream, step, a, b, u);
 }
 
+// A position drawn inside a cell must lie strictly above the cell's low node
+// on the axes whose cell search is strict (x and z, gutsp.f:1396-1412), or
+// the search puts it one cell lower, outside the grid at q(1).  Drawn in
+// double it always does (the uniforms are at least 2^-33 above 0); rounded to
+// float, a draw within half an ulp of the node lands on it, and goes to the
+// next float above instead.
+template <class R>
+inline R above(R x, R lo) {
+  return x > lo ? x : std::nextafter(lo, std::numeric_limits<R>::infinity());
+}
+
 // Ionize_sw_mp (chem_rates.f:508-646): dNi = ndot*dt*beta*beta_pu*dx*dy*delz*nz
 // (:553), a Bernoulli trial when below one (:555-560), nint (:562); ring
 // ions v = (vsw + vsw cos th, vsw sin th, 0) placed uniformly in the box
@@ -1167,9 +1183,9 @@ std::int64_t ionize_sw(State<R>& s, const Sources& src, std::int64_t step, R* xp
     vp[l] = (R)src.vsw + (R)src.vsw * std::cos(th);
     vp[l + NM] = (R)src.vsw * std::sin(th);
     vp[l + 2 * NM] = R(0.0);
-    xp[l] = g.qx[1] + (R(1.0) - (R)u[1]) * (g.qx[g.nx - 1] - g.qx[1]);
+    xp[l] = above<R>(g.qx[1] + (R(1.0) - (R)u[1]) * (g.qx[g.nx - 1] - g.qx[1]), g.qx[1]);
     xp[l + NM] = g.qy[1] + (R(1.0) - (R)u[2]) * (g.qy[g.ny - 1] - g.qy[1]);
-    xp[l + 2 * NM] = g.qz[1] + (R(1.0) - (R)u[3]) * (g.qz[g.nz - 1] - g.qz[1]);
+    xp[l + 2 * NM] = above<R>(g.qz[1] + (R(1.0) - (R)u[3]) * (g.qz[g.nz - 1] - g.qz[1]), g.qz[1]);
     for (int m = 0; m < 3; ++m) vp1[l + m * NM] = vp[l + m * NM];
     mrat[l] = (R)src.mrat_pu;
     beta_p[l] = (R)src.beta_pu;
@@ -1276,7 +1292,7 @@ std::int64_t inflow_x(State<R>& s, const Sources& src, std::int64_t step, R* xp,
         if (w >= NM) throw std::runtime_error("inflow: Ni_max exceeded");
         xp[w] = xn;
         xp[w + NM] = g.qy[cj + 1] + (R)u[1] * (g.qy[cj + 2] - g.qy[cj + 1]);
-        xp[w + 2 * NM] = g.qz[ck + 1] + (R)u[2] * (g.qz[ck + 2] - g.qz[ck + 1]);
+        xp[w + 2 * NM] = above<R>(g.qz[ck + 1] + (R)u[2] * (g.qz[ck + 2] - g.qz[ck + 1]), g.qz[ck + 1]);
         vp[w] = vx; vp[w + NM] = vy; vp[w + 2 * NM] = vz;
         for (int m = 0; m < 3; ++m) vp1[w + m * NM] = vp[w + m * NM];
         mrat[w] = R(1.0);
@@ -1328,9 +1344,9 @@ std::int64_t ionize_cloud(State<R>& s, const Sources& src, std::int64_t step, R*
           if (w >= NM) throw std::runtime_error("cloud ionization: Ni_max exceeded");
           double u[4];
           draw4(src, RNG_CLOUD, step, cell, (std::uint32_t)(1 + q), u);
-          xp[w] = g.qx[ci + 1] + (R)u[0] * (g.qx[ci + 2] - g.qx[ci + 1]);
+          xp[w] = above<R>(g.qx[ci + 1] + (R)u[0] * (g.qx[ci + 2] - g.qx[ci + 1]), g.qx[ci + 1]);
           xp[w + NM] = g.qy[cj + 1] + (R)u[1] * (g.qy[cj + 2] - g.qy[cj + 1]);
-          xp[w + 2 * NM] = g.qz[ck + 1] + (R)u[2] * (g.qz[ck + 2] - g.qz[ck + 1]);
+          xp[w + 2 * NM] = above<R>(g.qz[ck + 1] + (R)u[2] * (g.qz[ck + 2] - g.qz[ck + 1]), g.qz[ck + 1]);
           for (int m = 0; m < 3; ++m) { vp[w + m * NM] = R(0); vp1[w + m * NM] = R(0); }
           mrat[w] = (R)src.mrat_heavy;
           beta_p[w] = (R)src.beta_heavy;

@@ -35,7 +35,8 @@ class SwapError(RuntimeError):
 
 
 class Dims(C.Structure):
-    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("reserved", C.c_int32), ("ni_max", C.c_int64)]
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("real_bytes", C.c_int32),
+                ("ni_max", C.c_int64)]
 
 
 class Params(C.Structure):
@@ -219,6 +220,14 @@ def load(build_if_missing: bool = True) -> C.CDLL:
 
 def dptr(a: np.ndarray):
     assert a.dtype == np.float64 and (a.flags.f_contiguous or a.ndim == 1), "need a float64 Fortran-ordered array"
+    return a.ctypes.data_as(c_double_p)
+
+
+def rptr(a: np.ndarray):
+    """A bound real array as the ABI's double*: float64, or float32 for a
+    context created with real_bytes = 4 (the reference's -real-size 32)."""
+    assert a.dtype in (np.float64, np.float32) and (a.flags.f_contiguous or a.ndim == 1), \
+        "need a float64/float32 Fortran-ordered array"
     return a.ctypes.data_as(c_double_p)
 
 

@@ -724,4 +724,26 @@ cudaError_t count_nonfinite(const double* x, long long n, unsigned long long* d_
   LAUNCH(k_nonfinite, n, x, n, d_cnt);
 }
 
+// ---- the caller's 4-byte reals ------------------------------------------------
+
+__global__ void k_widen(const float* __restrict__ in, double* __restrict__ out, long long n) {
+  GRID_STRIDE(i, n) out[i] = (double)in[i];
+}
+
+__global__ void k_narrow(const double* __restrict__ in, float* __restrict__ out, long long n) {
+  GRID_STRIDE(i, n) out[i] = (float)in[i];
+}
+
+cudaError_t widen_f32(const float* in, double* out, long long n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_widen<<<nblocks(n), TPB, 0, st>>>(in, out, n);
+  return cudaGetLastError();
+}
+
+cudaError_t narrow_f64(const double* in, float* out, long long n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_narrow<<<nblocks(n), TPB, 0, st>>>(in, out, n);
+  return cudaGetLastError();
+}
+
 }  // namespace swapk

@@ -71,5 +71,9 @@ cudaError_t energy_parts(const Geo& g, const PartDev& p, long long N, double bet
                          const double* b0, const double* b1, const double* E, double* d_acc4, cudaStream_t st);
 cudaError_t divb_max(const Geo& g, const double* b, double* d_max, cudaStream_t st);
 cudaError_t count_nonfinite(const double* x, long long n, unsigned long long* d_cnt, cudaStream_t st);
+// A caller's 4-byte reals to the device's doubles (exact) and back (rounded
+// to nearest).
+cudaError_t widen_f32(const float* in, double* out, long long n, cudaStream_t st);
+cudaError_t narrow_f64(const double* in, float* out, long long n, cudaStream_t st);
 
 }  // namespace swapk

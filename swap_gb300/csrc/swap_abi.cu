@@ -41,7 +41,7 @@ Mirror* swap_ctx::find(const void* host) {
   return it == reg.end() ? nullptr : &it->second;
 }
 
-int swap_ctx::add_mirror(void* host, std::size_t bytes, MirrorKind kind) {
+int swap_ctx::add_mirror(void* host, std::size_t bytes, MirrorKind kind, bool real) {
   if (!host) return SWAP_OK;  // optional array not supplied
   if (Mirror* m = find(host)) {
     if (m->bytes != bytes || m->kind != kind) return fail(SWAP_EINVAL, "array registered twice with another size");
@@ -51,6 +51,7 @@ int swap_ctx::add_mirror(void* host, std::size_t bytes, MirrorKind kind) {
   m.host = host;
   m.bytes = bytes;
   m.kind = kind;
+  m.host_f32 = real && real_bytes == 4;
   if (cudaMalloc(&m.dev, bytes) != cudaSuccess) return fail(SWAP_ECUDA, "device allocation of a mirror failed");
   cudaMemsetAsync(m.dev, 0, bytes, st);
   m.host_valid = true;
@@ -61,6 +62,31 @@ int swap_ctx::add_mirror(void* host, std::size_t bytes, MirrorKind kind) {
 
 long long swap_ctx::ntot() const { return ni_tot_ptr ? (long long)*ni_tot_ptr : 0; }
 
+// One segment of a 4-byte-real mirror: n floats at host element `off`
+// through the staging buffer, converted to or from the device's doubles.
+static cudaError_t convert_segment(swap_ctx* c, Mirror& m, std::size_t off, std::size_t n, bool to_dev) {
+  if (n == 0) return cudaSuccess;
+  if (c->stage32_n < n) {
+    if (c->stage32) cudaFree(c->stage32);
+    c->stage32 = nullptr;
+    c->stage32_n = 0;
+    cudaError_t e = cudaMalloc(&c->stage32, n * sizeof(float));
+    if (e != cudaSuccess) return e;
+    c->stage32_n = n;
+  }
+  float* h = static_cast<float*>(m.host) + off;
+  double* d = static_cast<double*>(m.dev) + off;
+  cudaError_t e;
+  if (to_dev) {
+    e = cudaMemcpyAsync(c->stage32, h, n * sizeof(float), cudaMemcpyHostToDevice, c->st);
+    if (e == cudaSuccess) e = swapk::widen_f32(c->stage32, d, (long long)n, c->st);
+  } else {
+    e = swapk::narrow_f64(d, c->stage32, (long long)n, c->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, c->stage32, n * sizeof(float), cudaMemcpyDeviceToHost, c->st);
+  }
+  return e;
+}
+
 // Copy the live part of a mirror: particle vectors move three ni_tot segments,
 // per-particle scalars one, grids everything.
 int swap_ctx::transfer(Mirror& m, bool to_dev) {
@@ -68,6 +94,18 @@ int swap_ctx::transfer(Mirror& m, bool to_dev) {
   char* d = static_cast<char*>(m.dev);
   char* h = static_cast<char*>(m.host);
   cudaError_t e = cudaSuccess;
+  if (m.host_f32) {
+    const bool part = m.kind == MirrorKind::Particle3 || m.kind == MirrorKind::Particle1;
+    const std::size_t N = part ? (std::size_t)std::max(0LL, ntot()) : m.bytes / sizeof(double);
+    const int ncomp = m.kind == MirrorKind::Particle3 ? 3 : 1;
+    for (int q = 0; q < ncomp && e == cudaSuccess; ++q)
+      e = convert_segment(this, m, part ? (std::size_t)q * (std::size_t)dims.ni_max : 0, N, to_dev);
+    if (e != cudaSuccess) return cuda_fail(e, "transfer (4-byte reals)");
+    (to_dev ? h2d_bytes : d2h_bytes) += (long long)(N * ncomp * sizeof(float));
+    if (to_dev) m.dev_valid = true;
+    else m.host_valid = true;
+    return SWAP_OK;
+  }
   if (m.kind == MirrorKind::Particle3 || m.kind == MirrorKind::Particle1 || m.kind == MirrorKind::ParticleI3) {
     const long long N = ntot();
     const std::size_t esz = m.kind == MirrorKind::ParticleI3 ? sizeof(int32_t) : sizeof(double);
@@ -107,7 +145,7 @@ int swap_ctx::use(const void* host, Access acc, double** dev) {
 
 int swap_ctx::use_host(const void* host, Access acc, double** ptr, bool* direct) {
   *direct = false;
-  if (!host_direct || acc == Access::InOut) return use(host, acc, ptr);
+  if (!host_direct || acc == Access::InOut || real_bytes != 8) return use(host, acc, ptr);
   if (!host) return fail(SWAP_EINVAL, "null array argument");
   Mirror* m = find(host);
   if (!m) return fail(SWAP_EINVAL, "array not registered with swap_bind_*");
@@ -418,6 +456,7 @@ extern "C" int swap_init(swap_ctx** out, const swap_dims* d, const swap_params* 
   if (!out || !d || !p || !co) return SWAP_EINVAL;
   *out = nullptr;
   if (d->nx < 3 || d->ny < 3 || d->nz < 3 || d->ni_max < 0 || p->ntsub < 1) return SWAP_EINVAL;
+  if (d->real_bytes != 0 && d->real_bytes != 4 && d->real_bytes != 8) return SWAP_EINVAL;
   const double* arrs[12] = {co->qx, co->qy, co->qz, co->dx_grid, co->dy_grid, co->dz_grid,
                             co->dx_cell, co->dy_cell, co->dz_cell, co->xrat, co->yrat, co->zrat};
   for (const double* a : arrs)
@@ -425,11 +464,13 @@ extern "C" int swap_init(swap_ctx** out, const swap_dims* d, const swap_params* 
   auto* c = new swap_ctx();
   c->dims = *d;
   c->prm = *p;
+  c->real_bytes = d->real_bytes == 4 ? 4 : 8;
+  c->dims.real_bytes = c->real_bytes;
   {
     int dev = 0, pageable = 0;
     if (cudaGetDevice(&dev) == cudaSuccess &&
         cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess)
-      c->host_direct = pageable != 0;
+      c->host_direct = pageable != 0 && c->real_bytes == 8;
   }
   if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
     delete c;
@@ -496,6 +537,7 @@ extern "C" int swap_finalize(swap_ctx* c) {
   srcops::free_all(c);
   for (auto& kv : c->reg) cudaFree(kv.second.dev);
   for (void* p : c->owned) cudaFree(p);
+  if (c->stage32) cudaFree(c->stage32);
   if (c->t0) cudaEventDestroy(c->t0);
   if (c->t1) cudaEventDestroy(c->t1);
   c->prof_free();
@@ -517,7 +559,7 @@ extern "C" int swap_bind_particles(swap_ctx* c, double* xp, double* vp, double* 
   TRY(c->add_mirror(vp1, 3 * NM * sizeof(double), MirrorKind::Particle3));
   TRY(c->add_mirror(mrat, NM * sizeof(double), MirrorKind::Particle1));
   TRY(c->add_mirror(beta_p, NM * sizeof(double), MirrorKind::Particle1));
-  if (ijkp) TRY(c->add_mirror(ijkp, 3 * NM * sizeof(int32_t), MirrorKind::ParticleI3));
+  if (ijkp) TRY(c->add_mirror(ijkp, 3 * NM * sizeof(int32_t), MirrorKind::ParticleI3, false));
   c->h_xp = xp; c->h_vp = vp; c->h_vp1 = vp1; c->h_mrat = mrat; c->h_beta_p = beta_p; c->h_ijkp = ijkp;
   c->ni_tot_ptr = ni_tot;
   c->d_mrat = static_cast<double*>(c->find(mrat)->dev);
@@ -551,10 +593,13 @@ extern "C" int swap_bind_fields(swap_ctx* c, double* b0, double* b1, double* b12
 
 extern "C" int swap_bind_array(swap_ctx* c, void* host, int64_t bytes) {
   if (!c || !host || bytes <= 0) return SWAP_EINVAL;
+  if (bytes % c->real_bytes) return c->fail(SWAP_EINVAL, "swap_bind_array: size is not a whole number of reals");
+  // the device mirror holds doubles whatever the caller's real size
+  const std::size_t dev_bytes = (std::size_t)bytes / (std::size_t)c->real_bytes * sizeof(double);
   const std::size_t NM3 = 3 * (std::size_t)c->dims.ni_max * sizeof(double);
   // a (ni_max,3) real array moves as particle segments
-  const MirrorKind k = (std::size_t)bytes == NM3 ? MirrorKind::Particle3 : MirrorKind::Grid;
-  return c->add_mirror(host, (std::size_t)bytes, k);
+  const MirrorKind k = dev_bytes == NM3 ? MirrorKind::Particle3 : MirrorKind::Grid;
+  return c->add_mirror(host, dev_bytes, k);
 }
 
 extern "C" int swap_sync_to_device(swap_ctx* c, const void* host) {
@@ -589,6 +634,8 @@ extern "C" int swap_sync_to_host(swap_ctx* c, void* host) {
 
 extern "C" int swap_set_host_direct(swap_ctx* c, int on) {
   if (!c) return SWAP_EINVAL;
+  if (on && c->real_bytes != 8)
+    return c->fail(SWAP_EINVAL, "host-direct mode reads 8-byte reals; this context binds 4-byte reals");
   if (on) {
     int dev = 0, pageable = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||

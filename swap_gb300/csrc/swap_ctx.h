@@ -24,6 +24,9 @@ struct Mirror {
   MirrorKind kind = MirrorKind::Grid;
   bool host_valid = true;
   bool dev_valid = false;
+  // a real array of a caller built with 4-byte reals: the host copy holds
+  // floats, the device mirror doubles; transfers convert (see real_bytes)
+  bool host_f32 = false;
 };
 
 struct ProfEntry {
@@ -49,6 +52,13 @@ struct swap_ctx {
   // conversions then read and write the FP64 particle arrays in place, with
   // no staging copy through the device mirror.
   bool host_direct = false;
+  // Size of the caller's REAL (swap_dims.real_bytes): 8, or 4 for the
+  // reference's own build (makefile:1, -real-size 32).  The device state is
+  // FP64 either way; with 4, every registered real array is converted on its
+  // way to and from the device.
+  int real_bytes = 8;
+  float* stage32 = nullptr;   // device staging of those conversions
+  std::size_t stage32_n = 0;  // its capacity in floats
   int64_t h2d_bytes = 0, d2h_bytes = 0;  // bytes moved between the caller's memory and the device
   std::vector<void*> owned;  // device buffers freed at finalize
 
@@ -103,7 +113,9 @@ struct swap_ctx {
   int cuda_fail(cudaError_t e, const char* where);
   double* dalloc(std::size_t n);
   Mirror* find(const void* host);
-  int add_mirror(void* host, std::size_t bytes, MirrorKind kind);
+  // bytes: the DEVICE mirror's size; real: a real array (float on the host
+  // when real_bytes is 4)
+  int add_mirror(void* host, std::size_t bytes, MirrorKind kind, bool real = true);
   int transfer(Mirror& m, bool to_dev);
   int use(const void* host, Access acc, double** dev);
   // As use(), but with host_direct an input whose host copy is current, and

@@ -84,6 +84,20 @@ int rec_mixed(swap_ctx* c, FILE* f, const char* kinds, const double* v, int real
   return rec_raw(c, f, buf.data(), buf.size());
 }
 
+// The same for a bound host array: float when the context binds 4-byte reals.
+int rec_host(swap_ctx* c, FILE* f, const double* a, std::size_t n, int real_bytes) {
+  if (c->real_bytes == 8) return rec_reals(c, f, a, n, real_bytes);
+  const float* x = reinterpret_cast<const float*>(a);
+  if (real_bytes == 4) return rec_raw(c, f, x, n * 4);
+  std::vector<double> t(x, x + n);
+  return rec_raw(c, f, t.data(), n * 8);
+}
+
+// Element i of a bound host real array, as a double.
+inline double hreal(const swap_ctx* c, const double* a, std::size_t i) {
+  return c->real_bytes == 4 ? (double)reinterpret_cast<const float*>(a)[i] : a[i];
+}
+
 FILE* unit(Diag* d, int number) {
   for (Unit& u : d->units)
     if (u.number == number) return u.f;
@@ -124,13 +138,13 @@ int dump(swap_ctx* c, Diag* d, int32_t m) {
   std::vector<double> zeros3(3 * C, 0.0), t(3 * C);
   if (sp.rank == 0) {
     TRY(rec_int(c, unit(d, 110), m));
-    TRY(rec_reals(c, unit(d, 110), c->h_np, C, rb));
+    TRY(rec_host(c, unit(d, 110), c->h_np, C, rb));
     TRY(rec_int(c, unit(d, 115), m));
     TRY(rec_reals(c, unit(d, 115), zeros3.data(), C, rb));  // np_b: separate_np is not called (maind.f:513)
     TRY(rec_int(c, unit(d, 120), m));
     TRY(rec_reals(c, unit(d, 120), zeros3.data(), C, rb));  // mixed: no mixing tags in this model
     TRY(rec_int(c, unit(d, 130), m));
-    TRY(rec_reals(c, unit(d, 130), c->h_bt, 3 * C, rb));
+    TRY(rec_host(c, unit(d, 130), c->h_bt, 3 * C, rb));
     // current density aj*alpha*np3, np3 the face-averaged density
     const int nx = c->dims.nx, ny = c->dims.ny, nz = c->dims.nz;
     for (int k = 0; k < nz; ++k)
@@ -140,28 +154,28 @@ int dump(swap_ctx* c, Diag* d, int32_t m) {
           const std::size_t s[3] = {1, (std::size_t)nx, (std::size_t)nx * ny};
           const bool last[3] = {i == nx - 1, j == ny - 1, k == nz - 1};
           for (int q = 0; q < 3; ++q) {
-            const double n3 = last[q] ? c->h_np[o] : 0.5 * (c->h_np[o] + c->h_np[o + s[q]]);
-            t[o + C * q] = c->h_aj[o + C * q] * c->prm.alpha * n3;
+            const double n3 = last[q] ? hreal(c, c->h_np, o) : 0.5 * (hreal(c, c->h_np, o) + hreal(c, c->h_np, o + s[q]));
+            t[o + C * q] = hreal(c, c->h_aj, o + C * q) * c->prm.alpha * n3;
           }
         }
     TRY(rec_int(c, unit(d, 140), m));
     TRY(rec_reals(c, unit(d, 140), t.data(), 3 * C, rb));
     TRY(rec_int(c, unit(d, 150), m));
-    TRY(rec_reals(c, unit(d, 150), c->h_E, 3 * C, rb));
+    TRY(rec_host(c, unit(d, 150), c->h_E, 3 * C, rb));
     TRY(rec_int(c, unit(d, 180), m));
-    TRY(rec_reals(c, unit(d, 180), c->h_up, 3 * C, rb));
+    TRY(rec_host(c, unit(d, 180), c->h_up, 3 * C, rb));
     for (std::size_t o = 0; o < C; ++o) t[o] = d->h_temp[o] / 1.6e-19;  // maind.f:546
     TRY(rec_int(c, unit(d, 300), m));
     TRY(rec_reals(c, unit(d, 300), t.data(), C, rb));
   }
   TRY(rec_int(c, unit(d, 305), m));
-  TRY(rec_reals(c, unit(d, 305), c->h_xp, 3 * NM, rb));
+  TRY(rec_host(c, unit(d, 305), c->h_xp, 3 * NM, rb));
   TRY(rec_int(c, unit(d, 310), m));
-  TRY(rec_reals(c, unit(d, 310), c->h_vp, 3 * NM, rb));
+  TRY(rec_host(c, unit(d, 310), c->h_vp, 3 * NM, rb));
   TRY(rec_int(c, unit(d, 315), m));
-  TRY(rec_reals(c, unit(d, 315), c->h_mrat, NM, rb));
+  TRY(rec_host(c, unit(d, 315), c->h_mrat, NM, rb));
   TRY(rec_int(c, unit(d, 317), m));
-  TRY(rec_reals(c, unit(d, 317), c->h_beta_p, NM, rb));
+  TRY(rec_host(c, unit(d, 317), c->h_beta_p, NM, rb));
   if (sp.rank == 0) {
     TRY(rec_int(c, unit(d, 330), m));
     TRY(rec_reals(c, unit(d, 330), zeros3.data(), 3 * C, rb));  // up_t, up_b: separate_up is not called
@@ -317,18 +331,20 @@ struct CkHead {
   swap_sources srcs;
 };
 
-// The bound FP64 arrays in a fixed order, with their element counts.
-std::vector<std::pair<double*, std::size_t>> fp64_arrays(swap_ctx* c, std::size_t N) {
-  const std::size_t C = (std::size_t)c->g.C, NM = (std::size_t)c->dims.ni_max;
-  std::vector<std::pair<double*, std::size_t>> v;
+// The bound host real arrays in a fixed order, as (start, element count);
+// elements are c->real_bytes wide.
+std::vector<std::pair<char*, std::size_t>> host_arrays(swap_ctx* c, std::size_t N) {
+  const std::size_t C = (std::size_t)c->g.C, NM = (std::size_t)c->dims.ni_max, rb = (std::size_t)c->real_bytes;
+  auto at = [rb](double* a, std::size_t off) { return reinterpret_cast<char*>(a) + off * rb; };
+  std::vector<std::pair<char*, std::size_t>> v;
   for (double* a : {c->h_xp, c->h_vp, c->h_vp1})
-    for (int m = 0; m < 3; ++m) v.push_back({a + m * NM, N});
-  v.push_back({c->h_mrat, N});
-  v.push_back({c->h_beta_p, N});
+    for (int m = 0; m < 3; ++m) v.push_back({at(a, m * NM), N});
+  v.push_back({at(c->h_mrat, 0), N});
+  v.push_back({at(c->h_beta_p, 0), N});
   for (double* a : {c->h_b0, c->h_b1, c->h_b12, c->h_b1p2, c->h_bt, c->h_btc, c->h_up, c->h_aj, c->h_E})
-    v.push_back({a, 3 * C});
-  v.push_back({c->h_np, C});
-  v.push_back({c->h_nu, C});
+    v.push_back({at(a, 0), 3 * C});
+  v.push_back({at(c->h_np, 0), C});
+  v.push_back({at(c->h_nu, 0), C});
   return v;
 }
 
@@ -353,8 +369,8 @@ extern "C" int swap_checkpoint_write(swap_ctx* c, const char* path) {
   std::FILE* f = std::fopen(path, "wb");
   if (!f) return c->fail(SWAP_EINVAL, std::string("cannot open ") + path);
   int r = std::fwrite(&h, sizeof(h), 1, f) == 1 ? SWAP_OK : c->fail(SWAP_EINVAL, "checkpoint write failed");
-  for (auto& a : fp64_arrays(c, (std::size_t)h.ni_tot))
-    if (!r && a.second && std::fwrite(a.first, 8, a.second, f) != a.second)
+  for (auto& a : host_arrays(c, (std::size_t)h.ni_tot))
+    if (!r && a.second && std::fwrite(a.first, (std::size_t)c->real_bytes, a.second, f) != a.second)
       r = c->fail(SWAP_EINVAL, "checkpoint write failed");
   if (!r && h.f32) r = swap_f32_checkpoint(c, f, true);
   if (std::fclose(f) != 0 && !r) r = c->fail(SWAP_EINVAL, "checkpoint close failed");
@@ -371,10 +387,12 @@ extern "C" int swap_checkpoint_read(swap_ctx* c, const char* path) {
   if (!r && std::memcmp(h.magic, CK_MAGIC, 8) != 0) r = c->fail(SWAP_EINVAL, "not a checkpoint of this library");
   if (!r && (h.dims.nx != c->dims.nx || h.dims.ny != c->dims.ny || h.dims.nz != c->dims.nz))
     r = c->fail(SWAP_EINVAL, "checkpoint grid differs from the context's");
+  if (!r && (h.dims.real_bytes == 4 ? 4 : 8) != c->real_bytes)
+    r = c->fail(SWAP_EINVAL, "checkpoint real size differs from the context's");
   if (!r && h.ni_tot > c->dims.ni_max) r = c->fail(SWAP_ECAPACITY, "checkpoint holds more ions than Ni_max");
   if (!r) {
-    for (auto& a : fp64_arrays(c, (std::size_t)h.ni_tot))
-      if (!r && a.second && std::fread(a.first, 8, a.second, f) != a.second)
+    for (auto& a : host_arrays(c, (std::size_t)h.ni_tot))
+      if (!r && a.second && std::fread(a.first, (std::size_t)c->real_bytes, a.second, f) != a.second)
         r = c->fail(SWAP_EINVAL, "checkpoint truncated");
   }
   if (!r) {

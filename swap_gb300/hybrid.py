@@ -128,27 +128,31 @@ class Hybrid:
     """One context on the current GPU with the reference's arrays bound."""
 
     def __init__(self, cfg: RunConfig, ni_max: int | None = None, coords: Coords | None = None,
-                 pinned: bool = False, work_arrays: bool = True):
+                 pinned: bool = False, work_arrays: bool = True, real_bytes: int = 8):
         """work_arrays=False leaves out the arrays only the per-subroutine
         entries take (Ep, vplus, vminus, ijkp) and their device mirrors: the
-        fused steps keep their own, which saves 84 B per particle on each side."""
+        fused steps keep their own, which saves 84 B per particle on each side.
+        real_bytes=4 holds every real array in float32, as SWAP built with
+        -real-size 32 (makefile:1) does; the context converts at the boundary."""
         self.cfg = cfg
         self.lib = abi.load()
         nx, ny, nz = cfg.nodes
         self.coords = coords or grd7(nx, ny, nz)
         self.ni_max = int(ni_max if ni_max is not None else cfg.n_particles)
         NM = self.ni_max
-        self.dims = abi.Dims(nx, ny, nz, 0, NM)
+        self.real_bytes = int(real_bytes)
+        self.rdtype = np.float32 if self.real_bytes == 4 else np.float64
+        self.dims = abi.Dims(nx, ny, nz, self.real_bytes, NM)
         self.params = abi.Params(cfg.dt, cfg.alpha, cfg.beta, self.coords.dx, self.coords.dy, cfg.grad_pe, cfg.ntsub, 0)
         self._coords_c = abi.Coords(*[abi.dptr(getattr(self.coords, n)) for n in Coords.ARRAYS])
         self._pins = []
         # particle arrays (maind.f:54-59, global.f:44,96,100)
-        f = (lambda: self._pinned((NM, 3))) if pinned else (lambda: np.zeros((NM, 3), dtype=np.float64, order="F"))
+        f = (lambda: self._pinned((NM, 3))) if pinned else (lambda: np.zeros((NM, 3), dtype=self.rdtype, order="F"))
         self.xp, self.vp, self.vp1 = f(), f(), f()
         if work_arrays:
             self.Ep, self.vplus, self.vminus = f(), f(), f()
-        self.mrat = self._pinned((NM,)) if pinned else np.zeros(NM, dtype=np.float64)
-        self.beta_p = self._pinned((NM,)) if pinned else np.zeros(NM, dtype=np.float64)
+        self.mrat = self._pinned((NM,)) if pinned else np.zeros(NM, dtype=self.rdtype)
+        self.beta_p = self._pinned((NM,)) if pinned else np.zeros(NM, dtype=self.rdtype)
         self.mrat[:] = 1.0
         self.beta_p[:] = 1.0
         self.ijkp = np.zeros((NM, 3) if work_arrays else (1, 3), dtype=np.int32, order="F")
@@ -160,29 +164,32 @@ class Hybrid:
                 pv = self._pinned(v.shape)
                 pv[...] = v
                 v = pv
+            elif v.dtype != self.rdtype:
+                v = np.asarray(v, dtype=self.rdtype, order="F")
             setattr(self, k, v)
-        self.input_p = np.zeros(3)
+        self.input_p = np.zeros(3, dtype=self.rdtype)
         ctx = C.c_void_p()
         abi.check(self.lib, None, self.lib.swap_init(C.byref(ctx), C.byref(self.dims), C.byref(self.params),
                                                        C.byref(self._coords_c)))
         self.ctx = ctx
-        self._check(self.lib.swap_bind_particles(ctx, abi.dptr(self.xp), abi.dptr(self.vp), abi.dptr(self.vp1),
-                                                 abi.dptr(self.mrat), abi.dptr(self.beta_p),
+        self._check(self.lib.swap_bind_particles(ctx, abi.rptr(self.xp), abi.rptr(self.vp), abi.rptr(self.vp1),
+                                                 abi.rptr(self.mrat), abi.rptr(self.beta_p),
                                                  abi.iptr(self.ijkp) if work_arrays else None,
                                                  abi.iptr(self.ni_tot)))
-        self._check(self.lib.swap_bind_fields(ctx, *[abi.dptr(getattr(self, n)) for n in (
+        self._check(self.lib.swap_bind_fields(ctx, *[abi.rptr(getattr(self, n)) for n in (
             "b0", "b1", "b12", "b1p2", "bt", "btc", "np", "up", "aj", "E", "nu")]))
         for a in ((self.Ep, self.vplus, self.vminus) if work_arrays else ()) + (self.input_p,):
             self._check(self.lib.swap_bind_array(ctx, a.ctypes.data_as(C.c_void_p), a.nbytes))
 
     # ---- plumbing ----
     def _pinned(self, shape):
-        """A zeroed float64 Fortran-ordered array in page-locked host memory."""
+        """A zeroed real Fortran-ordered array in page-locked host memory."""
         import torch
 
-        t = torch.zeros(int(np.prod(shape)), dtype=torch.float64, pin_memory=True)
+        t = torch.zeros(int(np.prod(shape)), dtype=torch.float32 if self.real_bytes == 4 else torch.float64,
+                        pin_memory=True)
         self._pins.append(t)
-        return np.ndarray(shape, dtype=np.float64, buffer=t.numpy(), order="F")
+        return np.ndarray(shape, dtype=self.rdtype, buffer=t.numpy(), order="F")
 
     def _check(self, code):
         abi.check(self.lib, self.ctx if hasattr(self, "ctx") else None, code)
@@ -205,9 +212,17 @@ class Hybrid:
         spec = abi.LoadSpec(cfg.seed if seed is None else seed, stream, cfg.ppc if ppc is None else ppc,
                             cfg.vth if vth is None else vth, ux, uy, uz, mrat, beta_p)
         cnt = C.c_int64()
+        if self.real_bytes == 4:  # the loader writes doubles: load into FP64 arrays and round
+            NM = self.ni_max
+            tmp = [np.zeros((NM, 3), order="F") for _ in range(3)] + [np.zeros(NM), np.zeros(NM)]
+            arrs = [abi.dptr(a) for a in tmp]
+        else:
+            arrs = [abi.dptr(a) for a in (self.xp, self.vp, self.vp1, self.mrat, self.beta_p)]
         abi.check(self.lib, None, self.lib.swap_load_maxwellian_host(
-            C.byref(self.dims), C.byref(self._coords_c), C.byref(spec), abi.dptr(self.xp), abi.dptr(self.vp),
-            abi.dptr(self.vp1), abi.dptr(self.mrat), abi.dptr(self.beta_p), first, C.byref(cnt)))
+            C.byref(self.dims), C.byref(self._coords_c), C.byref(spec), *arrs, first, C.byref(cnt)))
+        if self.real_bytes == 4:
+            for dst, src in zip((self.xp, self.vp, self.vp1, self.mrat, self.beta_p), tmp):
+                dst[first:first + cnt.value] = src[first:first + cnt.value]
         self.ni_tot[0] = first + cnt.value
         self.mark_host_dirty()
         return cnt.value
@@ -233,73 +248,73 @@ class Hybrid:
 
     # ---- gutsp.f ----
     def get_interp_weights(self, xp):
-        self._check(self.lib.swap_get_interp_weights(self.ctx, abi.dptr(xp)))
+        self._check(self.lib.swap_get_interp_weights(self.ctx, abi.rptr(xp)))
 
     def update_np(self, np_):
-        self._check(self.lib.swap_update_np(self.ctx, abi.dptr(np_)))
+        self._check(self.lib.swap_update_np(self.ctx, abi.rptr(np_)))
 
     def update_up(self, vp, np_, up):
-        self._check(self.lib.swap_update_up(self.ctx, abi.dptr(vp), abi.dptr(np_), abi.dptr(up)))
+        self._check(self.lib.swap_update_up(self.ctx, abi.rptr(vp), abi.rptr(np_), abi.rptr(up)))
 
     def extrapol_up(self, up, vp, vp1, np_):
-        self._check(self.lib.swap_extrapol_up(self.ctx, abi.dptr(up), abi.dptr(vp), abi.dptr(vp1), abi.dptr(np_)))
+        self._check(self.lib.swap_extrapol_up(self.ctx, abi.rptr(up), abi.rptr(vp), abi.rptr(vp1), abi.rptr(np_)))
 
     def get_Ep(self, Ep, aj, np_, up, btc, nu):
-        self._check(self.lib.swap_get_Ep(self.ctx, *map(abi.dptr, (Ep, aj, np_, up, btc, nu))))
+        self._check(self.lib.swap_get_Ep(self.ctx, *map(abi.rptr, (Ep, aj, np_, up, btc, nu))))
 
     def get_vplus_vminus(self, Ep, btc, vp, vplus, vminus):
-        self._check(self.lib.swap_get_vplus_vminus(self.ctx, *map(abi.dptr, (Ep, btc, vp, vplus, vminus))))
+        self._check(self.lib.swap_get_vplus_vminus(self.ctx, *map(abi.rptr, (Ep, btc, vp, vplus, vminus))))
 
     def improve_up(self, vp1, vplus, vminus, up, np_):
-        self._check(self.lib.swap_improve_up(self.ctx, *map(abi.dptr, (vp1, vplus, vminus, up, np_))))
+        self._check(self.lib.swap_improve_up(self.ctx, *map(abi.rptr, (vp1, vplus, vminus, up, np_))))
 
     def get_vp_final(self, Ep, vp, vp1, vplus):
-        self._check(self.lib.swap_get_vp_final(self.ctx, *map(abi.dptr, (Ep, vp, vp1, vplus))))
+        self._check(self.lib.swap_get_vp_final(self.ctx, *map(abi.rptr, (Ep, vp, vp1, vplus))))
 
     def move_ion_half(self, xp, vp, vp1, input_p):
-        self._check(self.lib.swap_move_ion_half(self.ctx, *map(abi.dptr, (xp, vp, vp1, input_p))))
+        self._check(self.lib.swap_move_ion_half(self.ctx, *map(abi.rptr, (xp, vp, vp1, input_p))))
 
     # ---- gutsf.f / grid_interp.f / boundary.f ----
     def curlB(self, bt, np_, aj):
-        self._check(self.lib.swap_curlB(self.ctx, *map(abi.dptr, (bt, np_, aj))))
+        self._check(self.lib.swap_curlB(self.ctx, *map(abi.rptr, (bt, np_, aj))))
 
     def edge_to_center(self, bt, btc):
-        self._check(self.lib.swap_edge_to_center(self.ctx, abi.dptr(bt), abi.dptr(btc)))
+        self._check(self.lib.swap_edge_to_center(self.ctx, abi.rptr(bt), abi.rptr(btc)))
 
     def face_to_center(self, v, vc):
-        self._check(self.lib.swap_face_to_center(self.ctx, abi.dptr(v), abi.dptr(vc)))
+        self._check(self.lib.swap_face_to_center(self.ctx, abi.rptr(v), abi.rptr(vc)))
 
     def get_E(self, E, b0, bt, aj, up, np_, nu):
-        self._check(self.lib.swap_get_E(self.ctx, *map(abi.dptr, (E, b0, bt, aj, up, np_, nu))))
+        self._check(self.lib.swap_get_E(self.ctx, *map(abi.rptr, (E, b0, bt, aj, up, np_, nu))))
 
     def predict_B(self, b0, b1, b12, b1p2, bt, E, aj, up, np_, nu, dtsub):
-        self._check(self.lib.swap_predict_B(self.ctx, *map(abi.dptr, (b0, b1, b12, b1p2, bt, E, aj, up, np_, nu)),
+        self._check(self.lib.swap_predict_B(self.ctx, *map(abi.rptr, (b0, b1, b12, b1p2, bt, E, aj, up, np_, nu)),
                                             float(dtsub)))
 
     def correct_B(self, b0, b1, b1p2, E, aj, up, np_, nu, dtsub):
-        self._check(self.lib.swap_correct_B(self.ctx, *map(abi.dptr, (b0, b1, b1p2, E, aj, up, np_, nu)),
+        self._check(self.lib.swap_correct_B(self.ctx, *map(abi.rptr, (b0, b1, b1p2, E, aj, up, np_, nu)),
                                             float(dtsub)))
 
     def f_update_tlev(self, b1, b12, b1p2, bt, b0):
-        self._check(self.lib.swap_f_update_tlev(self.ctx, *map(abi.dptr, (b1, b12, b1p2, bt, b0))))
+        self._check(self.lib.swap_f_update_tlev(self.ctx, *map(abi.rptr, (b1, b12, b1p2, bt, b0))))
 
     def check_time_step(self, bt, np_, dtsub, ntf):
         d = C.c_double(dtsub)
         n = C.c_double(ntf)
-        self._check(self.lib.swap_check_time_step(self.ctx, abi.dptr(bt), abi.dptr(np_), C.byref(d), C.byref(n)))
+        self._check(self.lib.swap_check_time_step(self.ctx, abi.rptr(bt), abi.rptr(np_), C.byref(d), C.byref(n)))
         return d.value, n.value
 
     def update_rho(self, mnp):
-        self._check(self.lib.swap_update_rho(self.ctx, abi.dptr(mnp)))
+        self._check(self.lib.swap_update_rho(self.ctx, abi.rptr(mnp)))
 
     def get_temperature(self, xp, vp, np_, temp_p):
-        self._check(self.lib.swap_get_temperature(self.ctx, *map(abi.dptr, (xp, vp, np_, temp_p))))
+        self._check(self.lib.swap_get_temperature(self.ctx, *map(abi.rptr, (xp, vp, np_, temp_p))))
 
     def set_mion(self, mion: float):
         self._check(self.lib.swap_set_mion(self.ctx, float(mion)))
 
     def periodic(self, b):
-        self._check(self.lib.swap_periodic(self.ctx, abi.dptr(b)))
+        self._check(self.lib.swap_periodic(self.ctx, abi.rptr(b)))
 
     # ---- sources and sinks (chem_rates.f, gutsp.f:12-46) ----
     def set_sources(self, src: "abi.Sources", step0: int = 0):
@@ -307,15 +322,15 @@ class Hybrid:
         self._check(self.lib.swap_set_sources(self.ctx, C.byref(src), int(step0)))
 
     def Ionize_sw_mp(self, np_, vp, vp1, xp, m_tstep, input_p, up):
-        self._check(self.lib.swap_Ionize_sw_mp(self.ctx, abi.dptr(np_), abi.dptr(vp), abi.dptr(vp1), abi.dptr(xp),
-                                               int(m_tstep), abi.dptr(input_p), abi.dptr(up)))
+        self._check(self.lib.swap_Ionize_sw_mp(self.ctx, abi.rptr(np_), abi.rptr(vp), abi.rptr(vp1), abi.rptr(xp),
+                                               int(m_tstep), abi.rptr(input_p), abi.rptr(up)))
 
     def remove_ion(self, xp, vp, vp1, ion_l):
-        self._check(self.lib.swap_remove_ion(self.ctx, abi.dptr(xp), abi.dptr(vp), abi.dptr(vp1), int(ion_l)))
+        self._check(self.lib.swap_remove_ion(self.ctx, abi.rptr(xp), abi.rptr(vp), abi.rptr(vp1), int(ion_l)))
 
     def res_chex(self, xp, vp, m_tstep) -> int:
         n = C.c_int64()
-        self._check(self.lib.swap_res_chex(self.ctx, abi.dptr(xp), abi.dptr(vp), int(m_tstep), C.byref(n)))
+        self._check(self.lib.swap_res_chex(self.ctx, abi.rptr(xp), abi.rptr(vp), int(m_tstep), C.byref(n)))
         return n.value
 
     def inflow_x(self, m_tstep):
@@ -346,7 +361,7 @@ class Hybrid:
 
     def max_abs_divB(self, b):
         out = C.c_double()
-        self._check(self.lib.swap_max_abs_divB(self.ctx, abi.dptr(b), C.byref(out)))
+        self._check(self.lib.swap_max_abs_divB(self.ctx, abi.rptr(b), C.byref(out)))
         return out.value
 
     def check_finite(self):
