@@ -741,7 +741,7 @@ def run_accuracy_legs(args, line):
             line["accuracy"] = {"error": f"{type(e).__name__}: {e}"}
     steps = {2: args.acc2_steps, 3: args.acc3_steps}
     for n in [int(x) for x in args.acc_configs.split(",") if x.strip()]:
-        for cx in ([True, False] if args.acc_cx_off else [True]):
+        for cx in {"both": [True, False], "on": [True], "off": [False]}[args.acc_cx]:
             key = f"config{n}" + ("" if cx else "_no_cx")
             try:
                 line.setdefault("accuracy_configs", {})[key] = run_compare(n, steps.get(n, 20), cx=cx)
@@ -773,8 +773,8 @@ def main():
                     help="workloads run at their stated size by both the FP64 drop-in and the FP32 form")
     ap.add_argument("--acc2-steps", type=int, default=100, help="ion steps of the 256x128x128 pickup-ion comparison")
     ap.add_argument("--acc3-steps", type=int, default=20, help="ion steps of the 512x256x256 pickup-ion comparison")
-    ap.add_argument("--acc-cx-off", action="store_true",
-                    help="also run each comparison with charge exchange off (no sampling difference)")
+    ap.add_argument("--acc-cx", default="both", choices=["both", "on", "off"],
+                    help="comparisons with charge exchange as stated (on), off (no sampling difference), or both")
     ap.add_argument("--only-accuracy", action="store_true", help="run the accuracy legs alone")
     ap.add_argument("--conv-only", type=int, nargs="+", default=None, metavar="N",
                     help="CIN COUT NX NY NZ [REPEATS]: the surrogate's convolution alone (profiling)")

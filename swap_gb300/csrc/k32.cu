@@ -8,6 +8,15 @@ namespace {
 
 constexpr int TPB = 256;
 constexpr int TPB_PASS = 128;  // particle passes: keeps the shared tiles under 48 KB
+// Chunk buffers of the particle passes: chunks k+1 .. k+PASS_STAGES-1 are in
+// flight while chunk k is processed (more bytes in flight per SM hides more
+// of the HBM latency; each stage costs one chunk of shared memory).
+#ifndef SWAP_PASS_STAGES
+#define SWAP_PASS_STAGES 2
+#endif
+constexpr int PASS_STAGES = SWAP_PASS_STAGES;
+// Polls of a chunk's mbarrier before a pass gives up (KERR_STAGE).
+constexpr uint32_t STAGE_WAIT_POLLS = 1u << 22;
 constexpr int KERR_DOMAIN = 3, KERR_CAPACITY = 4, KERR_MOVE = 7, KERR_STAGE = 8;
 
 inline unsigned nblk(long long n, int tpb = TPB) {
@@ -214,11 +223,11 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
                                               uint16_t* __restrict__ dep, int* err) {
   // the chunk's particles, copied in by the bulk-copy engine (double-buffered):
   // offsets and v, plus vp1 in P1; cell words; species bytes
-  constexpr int NF = PASS == 1 ? 9 : 6;
-  __shared__ __align__(128) float s_f[2][NF][TPB_PASS];
-  __shared__ __align__(128) int32_t s_c[2][TPB_PASS];
-  __shared__ __align__(128) uint8_t s_s[2][TPB_PASS];
-  __shared__ uint64_t s_full[2];
+  constexpr int NF = PASS == 1 ? 9 : 6, NS = PASS_STAGES;
+  __shared__ __align__(128) float s_f[NS][NF][TPB_PASS];
+  __shared__ __align__(128) int32_t s_c[NS][TPB_PASS];
+  __shared__ __align__(128) uint8_t s_s[NS][TPB_PASS];
+  __shared__ uint64_t s_full[NS];
   // the field-gather tile: (aj-up, B_x) and (B_y, B_z) per node
   // deposit tile: T nodes per axis; a cell rx of the brick (rx in [-1,4] for
   // pass 3's movers, [0,3] otherwise) has its lower corner at offset rx + O.
@@ -249,8 +258,7 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
   if (PASS == 3)
     for (int t = threadIdx.x; t < BCELLS * NDIR; t += blockDim.x) s_rank[t] = 0;
   if (threadIdx.x == 0) {
-    tc05::mbar_init(&s_full[0], 1);
-    tc05::mbar_init(&s_full[1], 1);
+    for (int q = 0; q < NS; ++q) tc05::mbar_init(&s_full[q], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -261,9 +269,11 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
   // on a 16-byte boundary); lanes outside [first, last) are masked
   const long long a0 = first & ~15LL;
   const int nchunk = last > first ? (int)((last - a0 + TPB_PASS - 1) / TPB_PASS) : 0;
-  // one thread copies chunk k's particle arrays into buffer k & 1
+  // one thread copies chunk k's particle arrays into buffer k % NS
+  int issued = 0;  // chunks whose copies thread 0 has started
   auto issue = [&](int k) {
-    const int u = k & 1;
+    const int u = k % NS;
+    issued = k + 1;
     const long long i0 = a0 + (long long)TPB_PASS * k;
     constexpr uint32_t FB = TPB_PASS * 4;
     tc05::mbar_expect_tx(&s_full[u], (NF + 1) * FB + (p.sp ? TPB_PASS : 0));
@@ -273,20 +283,25 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
     for (int f = 0; f < NF; ++f) tc05::bulk_g2s(s_f[u][f], src[f] + i0, FB, &s_full[u]);
     if (p.sp) tc05::bulk_g2s(s_s[u], p.sp + i0, TPB_PASS, &s_full[u]);
   };
-  if (threadIdx.x == 0 && nchunk > 0) issue(0);
+  if (threadIdx.x == 0)
+    for (int k = 0; k < NS - 1 && k < nchunk; ++k) issue(k);
   unsigned n_chex = 0;
   // warp-uniform trip count: every lane takes part in the deposit reduction
   for (int kc = 0; kc < nchunk; ++kc) {
-    const int u = kc & 1;
+    const int u = kc % NS;
     bool got = true;
-    if (threadIdx.x == 0) got = tc05::mbar_wait(&s_full[u], (kc >> 1) & 1, 1u << 22);
-    // the barrier publishes the chunk to every thread and frees the other
-    // buffer (chunk kc-1 is done): the next copy goes there
+    if (threadIdx.x == 0) got = tc05::mbar_wait(&s_full[u], (kc / NS) & 1, STAGE_WAIT_POLLS);
+    // the barrier publishes the chunk to every thread and frees the buffer of
+    // chunk kc-1, which every thread is done with: chunk kc+NS-1 goes there
     if (__syncthreads_or(!got)) {
       set_err(err, KERR_STAGE);
+      // let the copies still in flight land before the CTA's shared memory
+      // is released (each wait bounded)
+      if (threadIdx.x == 0)
+        for (int k = kc + 1; k < issued; ++k) tc05::mbar_wait(&s_full[k % NS], (k / NS) & 1, STAGE_WAIT_POLLS);
       break;
     }
-    if (threadIdx.x == 0 && kc + 1 < nchunk) issue(kc + 1);
+    if (threadIdx.x == 0 && kc + NS - 1 < nchunk) issue(kc + NS - 1);
     const long long l = a0 + (long long)TPB_PASS * kc + threadIdx.x;
     const bool mine = l >= first && l < last;
     const int32_t c = mine ? s_c[u][threadIdx.x] : CELL_DEAD;

@@ -71,15 +71,28 @@ class RunConfig:
         dens = float(np.sum(q["cloud_N0"] / (1.0 + r2)))
         return self.beta * q.get("beta_heavy", 1.0) * dens * q["nu_ion"] * self.dt
 
+    def inflow_ions_per_step(self) -> float:
+        """Ions entering through the open x face per step, at most: the
+        face's cells times inflow_ppc times (u_x + vth) dt (unit cells)."""
+        q = self.sources
+        if not q.get("x_open"):
+            return 0.0
+        face = self.cells[1] * self.cells[2] * q.get("inflow_ppc", 0)
+        return face * (abs(q.get("inflow_ux", 0.0)) + q.get("inflow_vth", 0.0)) * self.dt
+
     def ni_max_hint(self, steps: int | None = None) -> int:
         """Particle capacity with headroom for a workload whose count varies:
         5% for inflow and outflow, plus the cloud's new ions over `steps`
-        (default: the workload's step count)."""
+        (default: the workload's step count), plus, with charge exchange, every
+        ion that enters in that time: an exchanged ion is heavy and at rest,
+        and stays in the box far longer than the step count."""
         n = self.n_particles
         if not self.sources:
             return n
-        cloud = self.cloud_ions_per_step() * (self.steps if steps is None else steps)
-        return int(n * 1.05 + 1.1 * cloud) + 4096
+        per_step = self.cloud_ions_per_step()
+        if self.sources.get("cx_a"):
+            per_step += self.inflow_ions_per_step()
+        return int(n * 1.05 + 1.1 * per_step * (self.steps if steps is None else steps)) + 4096
 
 
 def config(n: int, **over) -> RunConfig:

@@ -1,0 +1,146 @@
+"""The electron-pressure term of the FP64 drop-in, and the FP32 form on a
+pickup-ion box (open x, neutral cloud, charge exchange) over many steps,
+against the FP64 oracle.
+
+grad_pe (the isothermal -grad(p_e)/(n e) term the reference keeps as a
+comment at gutsf.f:1083,1283): every operator that carries it is bit-exact
+on identical inputs, a fused step within rel 1e-12 on the particles, and 20
+steps within rel-L2 1e-9 on the fields.
+
+Pickup ions (chem_rates.f:346-432 cloud ionization and :805-843 charge
+exchange, on the 256x128x128 workload's physics at 32x16x16 cells): with
+charge exchange off the FP32 form and the FP64 oracle run the same
+deterministic step, so after 50 steps B, n_p, u_p and the energy agree to
+the FP32 form's rounding; with it on, the two draw the exchanges per sorted
+ion and per array index, so they agree in the statistics of the process.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_l2, relerr
+from helpers import make_hybrid, oracle_for
+from swap_gb300 import abi
+
+pytestmark = pytest.mark.gpu
+
+STEP_TOL = 1e-12
+
+
+def test_fp64_grad_pe_get_E_is_bit_exact():
+    h = make_hybrid(grad_pe=0.3)
+    o = oracle_for(h)
+    for obj in (h, o):
+        obj.get_interp_weights(obj.xp)
+        obj.update_np(obj.np)
+        obj.update_up(obj.vp, obj.np, obj.up)
+    h.sync_to_host()
+    # identical inputs from here on
+    h.np[...] = o.np
+    h.up[...] = o.up
+    h.mark_host_dirty()
+    for obj in (h, o):
+        obj.curlB(obj.bt, obj.np, obj.aj)
+        obj.get_E(obj.E, obj.b0, obj.bt, obj.aj, obj.up, obj.np, obj.nu)
+    h.sync_to_host()
+    assert np.array_equal(h.E, o.E)
+    # the term is live: the oracle without it gives another E
+    import dataclasses
+    import types
+
+    import pyoracle
+
+    plain = types.SimpleNamespace(**vars(h))
+    plain.cfg = dataclasses.replace(h.cfg, grad_pe=0.0)
+    o0 = pyoracle.from_hybrid_arrays(plain)
+    o0.curlB(o0.bt, o0.np, o0.aj)
+    o0.get_E(o0.E, o0.b0, o0.bt, o0.aj, o0.up, o0.np, o0.nu)
+    assert rel_l2(o0.E, o.E) > 1e-3
+    h.close()
+
+
+def test_fp64_grad_pe_fused_steps_match_oracle():
+    h = make_hybrid(cells=(12, 8, 8), ppc=6, grad_pe=0.3)
+    o = oracle_for(h)
+    N = int(h.ni_tot[0])
+    h.ion_step()
+    o.ion_step()
+    h.sync_to_host()
+    for name in ("xp", "vp", "vp1"):
+        assert relerr(getattr(h, name)[:N], getattr(o, name)[:N]) < STEP_TOL, name
+    h.run(19)
+    for _ in range(19):
+        o.ion_step()
+    h.sync_to_host()
+    for name in ("b1", "np", "up", "E"):
+        assert rel_l2(getattr(h, name), getattr(o, name)) < 1e-9, name
+    # the pressure term changed the run
+    h2 = make_hybrid(cells=(12, 8, 8), ppc=6, grad_pe=0.0)
+    h2.run(20)
+    h2.sync_to_host()
+    assert rel_l2(h2.b1 - h2.b0, h.b1 - h.b0) > 1e-3
+    h.close()
+    h2.close()
+
+
+def _pickup_sources(h, cx):
+    cfg = h.cfg
+    cells = cfg.cells
+    return abi.make_sources(seed=33, x_open=1, inflow_ppc=cfg.ppc, inflow_vth=cfg.vth, inflow_ux=cfg.u[0],
+                            cloud_N0=1000.0, cloud_r0=3.0, cloud_x=cells[0] / 2 + 1.0, cloud_y=cells[1] / 2 + 1.0,
+                            cloud_z=cells[2] / 2 + 1.0, nu_ion=1e-3, mrat_heavy=1.0 / 16.0, beta_heavy=1.0,
+                            cx_a=1.0 if cx else 0.0, cx_b=0.1 if cx else 0.0)
+
+
+def _pickup_pair(cx, steps=50):
+    h = make_hybrid(cells=(32, 16, 16), ppc=16, seed=9, db=0.0, extra=200000, u=(4.0, 0.0, 0.0))
+    o = oracle_for(h)
+    src = _pickup_sources(h, cx)
+    h.set_sources(src, 0)
+    o.set_sources(src, 0)
+    h.f32_begin()
+    e0 = h.f32_energy()
+    h.f32_run(steps)
+    e1 = h.f32_energy()
+    n32 = h.f32_count()
+    h.f32_end()
+    h.sync_to_host()
+    for _ in range(steps):
+        o.ion_step()
+    return h, o, e0, e1, n32
+
+
+def _heavy(obj, n):
+    return int(np.sum(np.isclose(obj.mrat[:n], 1.0 / 16.0)))
+
+
+def test_f32_pickup_box_50_steps_without_charge_exchange():
+    h, o, e0, e1, n32 = _pickup_pair(cx=False)
+    n, no = int(h.ni_tot[0]), int(o.ni_tot[0])
+    assert n == n32
+    assert abs(n - no) <= max(3, no // 20000), (n, no)  # outflow at FP32 positions
+    hv, hvo = _heavy(h, n), _heavy(o, no)
+    assert hvo > 1000 and abs(hv - hvo) <= 2, (hv, hvo)  # cloud ions: same draws
+    eb, ebo = rel_l2(h.b1, o.b1), rel_l2(h.b1 - h.b0, o.b1 - o.b0)
+    en, eu = rel_l2(h.np, o.np), rel_l2(h.up, o.up)
+    print(f"pickup, no cx, 50 steps: B {eb:.2e}  dB {ebo:.2e}  np {en:.2e}  up {eu:.2e}")
+    assert eb < 1e-4 and ebo < 3e-2 and en < 3e-3 and eu < 3e-2
+    eo = o.energy()
+    et, eto = e1[0] + e1[1], eo[0] + eo[1]
+    assert abs(et - eto) / eto < 1e-3
+    assert np.all(np.isfinite(h.b1))
+    h.close()
+
+
+def test_f32_pickup_box_50_steps_with_charge_exchange():
+    h, o, e0, e1, n32 = _pickup_pair(cx=True)
+    n, no = int(h.ni_tot[0]), int(o.ni_tot[0])
+    hv, hvo = _heavy(h, n), _heavy(o, no)
+    cx32, cxo = h.chex_count(), o.chex_count()
+    print(f"pickup, cx, 50 steps: exchanges {cx32} vs {cxo}; heavy {hv} vs {hvo}")
+    # the same process, different draws: within five standard deviations
+    assert cxo > 100
+    assert abs(cx32 - cxo) <= 5 * np.sqrt(cxo) + 5
+    assert abs(hv - hvo) <= 5 * np.sqrt(cxo) + 5
+    assert rel_l2(h.b1, o.b1) < 1e-3
+    assert rel_l2(h.np, o.np) < 5e-2
+    h.close()
