@@ -55,6 +55,7 @@ extern "C" {
 #define SWAP_ESUBCYCLE 6     /* subcycle count overflow in check_time_step     */
 #define SWAP_EMOVE 7         /* a particle moved more than one cell in a step  */
 #define SWAP_EWAIT 8         /* a device wait reached its iteration limit      */
+#define SWAP_EEXCHANGE 9     /* the caller's exchange callback returned nonzero */
 
 typedef struct swap_ctx swap_ctx;
 
@@ -91,6 +92,40 @@ int swap_init(swap_ctx** ctx, const swap_dims* dims, const swap_params* params, 
 int swap_finalize(swap_ctx* ctx);
 const char* swap_last_error(const swap_ctx* ctx);
 int swap_abi_version(void);
+
+/* ---- multi-rank particle decomposition ---- */
+/* The reference decomposes the ions over MPI ranks, each with a full copy of
+ * the grid, and sums every moment deposit over the ranks (MPI_ALLREDUCE,
+ * gutsp.f:1503,1812-1822; maind.f:140).  A context holds one rank's ions.
+ * With an exchange callback set, the fused entries (swap_ion_step_pre,
+ * swap_ion_step, swap_run, swap_f32_run) call it after every moment deposit
+ * with that rank's raw node sums -- the density and the velocity sums, before
+ * the division by the density -- and the callback must replace them in place
+ * by their sum over the ranks before it returns.
+ *   data:   device array of `count` reals; kind 8 (double, FP64 drop-in) or
+ *           4 (float, FP32 form);
+ *   stream: the cudaStream_t the deposit's kernels are queued on; the
+ *           reduction must come after them: queued on that stream
+ *           (ncclAllReduce(data, data, count, ..., stream)) or after
+ *           cudaStreamSynchronize(stream).
+ * A nonzero return ends the entry with SWAP_EEXCHANGE.  The per-subroutine
+ * entries never call it: their caller keeps its own MPI_ALLREDUCE.  With more
+ * than one rank, give the sources to one rank (inflow_ppc and nu_ion zero on
+ * the others, x_open on all so that every rank's ions flow out) and a
+ * different seed per rank for charge exchange.  swap_f32_energy's kinetic
+ * term is the rank's own: sum it over the ranks.  fn = NULL switches the
+ * exchange off (one rank). */
+typedef int (*swap_exchange_fn)(void* user, void* data, int64_t count, int32_t kind, void* stream);
+int swap_set_exchange(swap_ctx* ctx, swap_exchange_fn fn, void* user);
+
+/* ---- failure detection ---- */
+/* Every device wait of the FP32 form's particle passes (a chunk's bulk copy)
+ * polls at most `polls` times (default 4194304, about a second), then the
+ * pass stops, lets the copies already started land, and the entry returns
+ * SWAP_EWAIT; the context stays usable, the FP32 state does not (call
+ * swap_f32_begin again: the bound arrays still hold the state it began from).
+ * 0 makes every wait give up at once, to test that path. */
+int swap_set_wait_limit(swap_ctx* ctx, uint32_t polls);
 
 /* ---- array registration and data movement ---- */
 /* The particle arrays of maind.f:54-59 and global.f:44,96,100; ijkp may be
@@ -264,6 +299,12 @@ int swap_f32_count(swap_ctx* ctx, int64_t* n);
  * brick * 64 + cell in the brick (x fastest, bricks x fastest), so key q
  * holds starts[q+1] - starts[q] ions.  n = entries of starts (>= nkeys+1). */
 int swap_f32_key_starts(swap_ctx* ctx, int64_t* starts, int64_t n);
+/* Moment sums of the FP32 form: 1 (the default after swap_f32_begin) =
+ * compensated -- each warp's sum over a cell's ions is a Kahan sum, every
+ * shared-memory add keeps its rounding error in a bf16 compensation, and the
+ * brick partials are summed with their compensations by 2Sum; 0 = plain FP32
+ * sums, kept to measure what the compensation gains. */
+int swap_f32_set_compensated(swap_ctx* ctx, int on);
 /* Validation: move particles idx[q] of the current (sorted) order by one
  * cell step per axis (dcell[q] = (dx+1) | (dy+1)<<10 | (dz+1)<<20) and run
  * the stable incremental sort that follows each ion step. */

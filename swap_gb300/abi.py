@@ -25,6 +25,7 @@ SWAP_ERRORS = {
     6: "SWAP_ESUBCYCLE",
     7: "SWAP_EMOVE",
     8: "SWAP_EWAIT",
+    9: "SWAP_EEXCHANGE",
 }
 
 
@@ -104,6 +105,8 @@ def make_sources(**kw) -> Sources:
 
 # Every exported symbol declared in include/swap_gpu.h, with its argument types.
 P = C.c_void_p
+# swap_exchange_fn: int fn(void* user, void* data, int64 count, int32 kind, void* stream)
+EXCHANGE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p)
 SIGNATURES: dict[str, tuple] = {
     "swap_init": (C.c_int, [C.POINTER(P), C.POINTER(Dims), C.POINTER(Params), C.POINTER(Coords)]),
     "swap_finalize": (C.c_int, [P]),
@@ -117,6 +120,8 @@ SIGNATURES: dict[str, tuple] = {
     "swap_mark_host_dirty": (C.c_int, [P, P]),
     "swap_set_host_direct": (C.c_int, [P, C.c_int]),
     "swap_transfer_bytes": (C.c_int, [P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_int]),
+    "swap_set_exchange": (C.c_int, [P, EXCHANGE_FN, P]),
+    "swap_set_wait_limit": (C.c_int, [P, C.c_uint32]),
     "swap_get_interp_weights": (C.c_int, [P, c_double_p]),
     "swap_update_np": (C.c_int, [P, c_double_p]),
     "swap_update_up": (C.c_int, [P] + [c_double_p] * 3),
@@ -163,6 +168,7 @@ SIGNATURES: dict[str, tuple] = {
     "swap_f32_energy": (C.c_int, [P, c_double_p]),
     "swap_f32_count": (C.c_int, [P, c_int64_p]),
     "swap_f32_key_starts": (C.c_int, [P, c_int64_p, C.c_int64]),
+    "swap_f32_set_compensated": (C.c_int, [P, C.c_int]),
     "swap_f32_displace_resort": (C.c_int, [P, C.c_int64, c_int64_p, c_int32_p]),
     "swap_energy": (C.c_int, [P, c_double_p]),
     "swap_max_abs_divB": (C.c_int, [P, c_double_p, c_double_p]),

@@ -71,6 +71,7 @@ struct StepParams {
   float cx_a, cx_b, cloud_N0, inv_r0sq, cloud_x, cloud_y, cloud_z;
   uint8_t heavy_of[MAX_SPECIES];     // species after charge exchange
   unsigned long long* chex_count;    // exchanges, accumulated
+  uint32_t wait_polls;               // polls of a chunk's copy before a pass gives up
 };
 
 __host__ __device__ __forceinline__ int pk_i(int32_t c) { return c & 1023; }
@@ -133,12 +134,20 @@ __device__ __forceinline__ float offset_in_cell(double x, double q1, double d, i
 //     outflow and res_chex; writes each particle's sort direction and rank
 //     (dirrank) and the per-key direction counts (dep, direction-major:
 //     dep[dir * nkeys + key]) when those are given.
+// Moment sums (comp): each warp's sums over a cell's ions are compensated
+// (Kahan), each shared-memory add's rounding error goes to a bf16
+// compensation tile (2Sum of the value the atomic found and the addend), and
+// the brick partials are written as (float, bf16 compensation) pairs; with
+// comp = false the sums are plain FP32 (kept to measure what compensation
+// gains).
 cudaError_t pass(int which, const G32& g, const Part& p, const Species& sp, const StepParams& sprm,
-                 const int64_t* start, const float4* kit, float* partial, uint32_t* dirrank, uint16_t* dep, int* err,
-                 cudaStream_t st);
-// Sum the brick partial tiles into np and S (interior nodes, (nx,ny,nz) layout).
+                 const int64_t* start, const float4* kit, float* partial, uint16_t* partial_lo, uint32_t* dirrank,
+                 uint16_t* dep, int* err, bool comp, cudaStream_t st);
+// Sum the brick partial tiles into np and S (interior nodes, (nx,ny,nz) layout),
+// compensated (2Sum over the partials plus their compensations) when comp.
 // pass: the pass (1-3) whose tiles `partial` holds
-cudaError_t node_sum(const G32& g, int pass, const float* partial, int nq, float* np, float* S, cudaStream_t st);
+cudaError_t node_sum(const G32& g, int pass, const float* partial, const uint16_t* partial_lo, int nq, bool comp,
+                     float* np, float* S, cudaStream_t st);
 
 // ---- fields ----
 cudaError_t ct_and_up(const G32& g, const float* np, const float* S, float* up, cudaStream_t st);

@@ -193,6 +193,13 @@ int swap_ctx::finish() {
   return SWAP_OK;
 }
 
+int swap_ctx::exchange(void* data, long long count, int kind) {
+  if (!xfn) return SWAP_OK;
+  const int r = xfn(xuser, data, (int64_t)count, (int32_t)kind, static_cast<void*>(st));
+  if (r) return fail(SWAP_EEXCHANGE, "the exchange callback returned " + std::to_string(r));
+  return SWAP_OK;
+}
+
 PartDev swap_ctx::part_view() {
   PartDev p;
   p.xp = p.vp = p.vp1 = nullptr;
@@ -373,6 +380,7 @@ int update_np(swap_ctx* c, double* np) {
   TRY(need_weights(c));
   KL("cudaMemsetAsync", cudaMemsetAsync(np, 0, (std::size_t)c->g.C * sizeof(double), c->st));
   KL("deposit_np", deposit_np(c->g, c->part_view(), c->ntot(), c->prm.beta, np, c->d_err, c->st));
+  if (c->fused) TRY(c->exchange(np, c->g.C, 8));  // MPI_ALLREDUCE, gutsp.f:1503
   KL("periodic", periodic1(c->g, np, c->st));
   return 0;
 }
@@ -385,6 +393,7 @@ int update_up_mode(swap_ctx* c, int mode, const double* va, const double* vb, do
   const std::size_t b3 = 3 * (std::size_t)c->g.C * sizeof(double);
   KL("cudaMemsetAsync", cudaMemsetAsync(c->s_S, 0, b3, c->st));
   KL("deposit_u", deposit_u(c->g, c->part_view(), c->ntot(), c->prm.beta, mode, va, vb, out_v1, c->s_S, c->d_err, c->st));
+  if (c->fused) TRY(c->exchange(c->s_S, 3 * c->g.C, 8));  // MPI_ALLREDUCE, gutsp.f:1812-1822
   KL("ct_from_sums", ct_from_sums(c->g, c->s_S, np, c->s_ct, c->st));
   KL("periodic", periodic3(c->g, c->s_ct, c->st));
   KL("face_avg_int", face_avg_int(c->g, c->s_ct, up, c->st));
@@ -643,6 +652,19 @@ extern "C" int swap_set_host_direct(swap_ctx* c, int on) {
       return c->fail(SWAP_EINVAL, "this device cannot address host memory directly");
   }
   c->host_direct = on != 0;
+  return SWAP_OK;
+}
+
+extern "C" int swap_set_wait_limit(swap_ctx* c, uint32_t polls) {
+  if (!c) return SWAP_EINVAL;
+  c->wait_polls = polls;
+  return SWAP_OK;
+}
+
+extern "C" int swap_set_exchange(swap_ctx* c, swap_exchange_fn fn, void* user) {
+  if (!c) return SWAP_EINVAL;
+  c->xfn = fn;
+  c->xuser = user;
   return SWAP_OK;
 }
 
@@ -984,7 +1006,15 @@ int bound_inputs(swap_ctx* c, Bound& b) {
   return SWAP_OK;
 }
 
+// Marks the deposits made in its scope as the fused step's (exchanged).
+struct FusedScope {
+  swap_ctx* c;
+  explicit FusedScope(swap_ctx* cc) : c(cc) { c->fused = true; }
+  ~FusedScope() { c->fused = false; }
+};
+
 int step_pre(swap_ctx* c, Bound& b) {
+  FusedScope fs(c);
   TRY(srcops::step_begin(c, b.xp, b.vp, b.vp1));                            // sources
   TRY(ops::get_interp_weights(c, b.xp));                                     // maind.f:385
   TRY(ops::update_np(c, b.np));                                              // :386

@@ -57,6 +57,11 @@ struct swap_ctx {
   // FP64 either way; with 4, every registered real array is converted on its
   // way to and from the device.
   int real_bytes = 8;
+  // multi-rank exchange of the fused entries' deposits (swap_set_exchange)
+  swap_exchange_fn xfn = nullptr;
+  void* xuser = nullptr;
+  bool fused = false;  // inside a fused FP64 step: its deposits are exchanged
+  uint32_t wait_polls = 1u << 22;  // bound of the device waits (swap_set_wait_limit)
   float* stage32 = nullptr;   // device staging of those conversions
   std::size_t stage32_n = 0;  // its capacity in floats
   int64_t h2d_bytes = 0, d2h_bytes = 0;  // bytes moved between the caller's memory and the device
@@ -123,6 +128,9 @@ struct swap_ctx {
   int use_host(const void* host, Access acc, double** ptr, bool* direct);
   int begin();
   int finish();
+  // The rank sum of a deposit's raw node sums through the caller's callback
+  // (no-op without one).  kind: bytes per real of data.
+  int exchange(void* data, long long count, int kind);
   long long ntot() const;
   swapk::PartDev part_view();
   void prof_free();

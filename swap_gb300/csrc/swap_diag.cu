@@ -6,6 +6,7 @@
 // `write(unit)` produces and IDL's /f77_unformatted reads (read_para.pro,
 // get_fv.pro).  Reals are written at the reference's size (4 bytes, its
 // -real-size 32 build) unless 8 is asked for.
+#include <algorithm>
 #include <cerrno>
 #include <cstdio>
 #include <cstring>
@@ -319,7 +320,40 @@ extern "C" int swap_diag_close(swap_ctx* c) {
 
 namespace {
 
-constexpr char CK_MAGIC[8] = {'S', 'W', 'A', 'P', 'C', 'K', 'P', '1'};
+// Layout: header, the bound arrays, the FP32 state when one is running, then
+// an 8-byte checksum of everything before it.
+constexpr char CK_MAGIC[8] = {'S', 'W', 'A', 'P', 'C', 'K', 'P', '2'};
+
+// A 64-bit checksum of the first `len` bytes of a file, 8-byte words at a time
+// (xor, multiply by the FNV prime, fold the high bits down).  Detects a
+// truncated or altered checkpoint; not a cryptographic hash.
+bool file_checksum(const char* path, long long len, uint64_t* out) {
+  std::FILE* f = std::fopen(path, "rb");
+  if (!f) return false;
+  uint64_t h = 1469598103934665603ULL;
+  std::vector<unsigned char> buf((std::size_t)1 << 22);
+  long long left = len;
+  bool ok = true;
+  while (left > 0) {
+    const std::size_t want = (std::size_t)std::min<long long>(left, (long long)buf.size());
+    if (std::fread(buf.data(), 1, want, f) != want) {
+      ok = false;
+      break;
+    }
+    std::size_t i = 0;
+    for (; i + 8 <= want; i += 8) {
+      uint64_t w;
+      std::memcpy(&w, buf.data() + i, 8);
+      h = (h ^ w) * 1099511628211ULL;
+      h ^= h >> 29;
+    }
+    for (; i < want; ++i) h = (h ^ buf[i]) * 1099511628211ULL;
+    left -= (long long)want;
+  }
+  std::fclose(f);
+  *out = h;
+  return ok;
+}
 
 struct CkHead {
   char magic[8];
@@ -373,7 +407,16 @@ extern "C" int swap_checkpoint_write(swap_ctx* c, const char* path) {
     if (!r && a.second && std::fwrite(a.first, (std::size_t)c->real_bytes, a.second, f) != a.second)
       r = c->fail(SWAP_EINVAL, "checkpoint write failed");
   if (!r && h.f32) r = swap_f32_checkpoint(c, f, true);
+  long long len = r ? 0 : (long long)std::ftell(f);
   if (std::fclose(f) != 0 && !r) r = c->fail(SWAP_EINVAL, "checkpoint close failed");
+  if (!r) {  // the checksum trailer
+    uint64_t sum = 0;
+    std::FILE* g = nullptr;
+    if (len < 0 || !file_checksum(path, len, &sum) || !(g = std::fopen(path, "ab")) ||
+        std::fwrite(&sum, 8, 1, g) != 1)
+      r = c->fail(SWAP_EINVAL, "checkpoint checksum write failed");
+    if (g && std::fclose(g) != 0 && !r) r = c->fail(SWAP_EINVAL, "checkpoint close failed");
+  }
   return r;
 }
 
@@ -382,6 +425,17 @@ extern "C" int swap_checkpoint_read(swap_ctx* c, const char* path) {
   if (!c->h_xp || !c->h_b1) return c->fail(SWAP_EINVAL, "swap_bind_particles and swap_bind_fields are required");
   std::FILE* f = std::fopen(path, "rb");
   if (!f) return c->fail(SWAP_EINVAL, std::string("cannot open ") + path);
+  {  // the whole file against its checksum trailer, before anything is read
+    uint64_t want = 0, got = 1;
+    long long size = -1;
+    if (std::fseek(f, 0, SEEK_END) == 0) size = (long long)std::ftell(f);
+    const bool ok = size >= (long long)sizeof(CkHead) + 8 && std::fseek(f, size - 8, SEEK_SET) == 0 &&
+                    std::fread(&want, 8, 1, f) == 1 && file_checksum(path, size - 8, &got) && want == got;
+    if (!ok || std::fseek(f, 0, SEEK_SET) != 0) {
+      std::fclose(f);
+      return c->fail(SWAP_EINVAL, "checkpoint truncated or corrupted (checksum mismatch)");
+    }
+  }
   CkHead h{};
   int r = std::fread(&h, sizeof(h), 1, f) == 1 ? SWAP_OK : c->fail(SWAP_EINVAL, "not a checkpoint");
   if (!r && std::memcmp(h.magic, CK_MAGIC, 8) != 0) r = c->fail(SWAP_EINVAL, "not a checkpoint of this library");

@@ -34,8 +34,11 @@ struct F32State {
   uint16_t* dep = nullptr;
   uint16_t* pre = nullptr;
   float* partial = nullptr;
+  uint16_t* partial_lo = nullptr;  // bf16 compensations of the brick partials
+  bool comp = true;                // compensated moment sums (swap_f32_set_compensated)
   float4* kit = nullptr;
   float *np = nullptr, *S = nullptr, *up = nullptr, *aj = nullptr, *ct = nullptr, *E = nullptr, *nu = nullptr;
+  long long np_span = 0;  // floats from np to the end of S (one allocation)
   float *db1 = nullptr, *db1p2 = nullptr, *dbtp1 = nullptr;
   double* b0 = nullptr;  // FP64 b0, for the diagnostics
   // B levels in double-float: hi + lo float pairs (48 significant bits)
@@ -324,8 +327,18 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
       return c->fail(SWAP_ECUDA, "sort order table");
   }
   s->partial = s->alloc<float>((std::size_t)g.nbricks * 4 * TNODES);
+  s->partial_lo = s->alloc<uint16_t>((std::size_t)g.nbricks * 4 * TNODES);
   s->kit = s->alloc<float4>(2 * (std::size_t)ncx * ncy * ncz);
-  s->np = s->alloc<float>(C); s->S = s->alloc<float>(3 * C); s->up = s->alloc<float>(3 * C);
+  // np and the velocity sums S in one block (S 128-byte aligned after np), so
+  // that one exchange covers a deposit's node sums.  Zeroed once: the gap and
+  // S's ghost nodes are never written, and stay zero through the exchanges.
+  const std::size_t npad = ((std::size_t)C + 31) / 32 * 32;
+  float* nps = s->alloc<float>(npad + 3 * C);
+  s->np = nps;
+  s->S = nps ? nps + npad : nullptr;
+  s->np_span = (long long)(npad + 3 * C);
+  if (nps) CU(cudaMemsetAsync(nps, 0, (npad + 3 * C) * sizeof(float), c->st));
+  s->up = s->alloc<float>(3 * C);
   s->aj = s->alloc<float>(3 * C); s->ct = s->alloc<float>(3 * C); s->E = s->alloc<float>(3 * C);
   s->nu = s->alloc<float>(C);
   s->db1 = s->alloc<float>(3 * C); s->db1p2 = s->alloc<float>(3 * C); s->dbtp1 = s->alloc<float>(3 * C);
@@ -338,7 +351,7 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
   s->d_min = s->alloc<float>(4);
   s->dtn = s->alloc<float>(C);
   s->acc = s->alloc<double>(4);
-  if (!s->start || !s->start_new || !s->count || !s->sums || !s->dirrank || !s->dep || !s->pre || !s->partial || !s->kit ||
+  if (!s->start || !s->start_new || !s->count || !s->sums || !s->dirrank || !s->dep || !s->pre || !s->partial || !s->partial_lo || !s->kit ||
       !s->np || !s->S || !s->up || !s->aj || !s->ct || !s->E || !s->nu || !s->db1 || !s->db1p2 || !s->dbtp1 ||
       !s->b0 || !s->b1.l || !s->b12.l || !s->b1p2.l || !s->b0c || !s->d_min || !s->acc || !s->dtn)
     return c->fail(SWAP_ECUDA, "FP32 grid allocation failed");
@@ -405,7 +418,11 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
 
 // Deposit finish: node sums -> np (+ghosts) and up (maind.f:386-387 etc.).
 static int finish_deposit(swap_ctx* c, F32State* s, int pass, int nq) {
-  KL("f32_node_sum", node_sum(s->g, pass, s->partial, nq, s->np, s->S, c->st));
+  KL("f32_node_sum", node_sum(s->g, pass, s->partial, s->partial_lo, nq, s->comp, s->np, s->S, c->st));
+  // the rank sum of the raw node sums (MPI_ALLREDUCE, gutsp.f:1503,1812-1822);
+  // pass 2 deposits no density
+  if (nq == 4) TRY(c->exchange(s->np, s->np_span, 4));
+  else TRY(c->exchange(s->S, 3 * s->g.C, 4));
   KL("f32_ct_up", ct_and_up(s->g, s->np, s->S, s->up, c->st));
   return SWAP_OK;
 }
@@ -420,8 +437,13 @@ static int subcycles(swap_ctx* c, F32State* s, float* e_acc = nullptr) {
   // replayed on the host from the node values.
   KL("f32_courant", courant_min(g, s->db1, s->b0c, s->np, (float)c->prm.alpha, g.dx, s->dtn, s->d_min, c->st));
   float mn = 0;
+  int herr = 0;
   CU(cudaMemcpyAsync(&mn, s->d_min, sizeof(float), cudaMemcpyDeviceToHost, c->st));
+  CU(cudaMemcpyAsync(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->st));
   CU(cudaStreamSynchronize(c->st));
+  // a pass that failed (a wait that gave up, an ion outside the grid) ends
+  // the step here, before its moments reach the fields
+  if (herr) return check_err(c);
   if ((double)mn <= 2.0 * dtsub) {
     std::vector<float> h((std::size_t)g.C);
     CU(cudaMemcpy(h.data(), s->dtn, h.size() * sizeof(float), cudaMemcpyDeviceToHost));
@@ -516,6 +538,7 @@ static StepParams step_params(swap_ctx* c, F32State* s) {
   p.cloud_z = (float)q.cloud_z;
   for (int k = 0; k < MAX_SPECIES; ++k) p.heavy_of[k] = s->heavy_of[k];
   p.chex_count = p.chex ? srcops::counters(c) + 1 : nullptr;
+  p.wait_polls = c->wait_polls;
   return p;
 }
 
@@ -621,15 +644,18 @@ static int one_step(swap_ctx* c, F32State* s) {
   const G32& g = s->g;
   const StepParams sp = step_params(c, s);
   const Part& p = s->buf[s->cur];
-  KL("f32_P1", pass(1, g, p, s->sp, sp, s->start, s->kit, s->partial, nullptr, nullptr, c->d_err, c->st));  // :385-387,399
+  KL("f32_P1", pass(1, g, p, s->sp, sp, s->start, s->kit, s->partial, s->partial_lo, nullptr, nullptr, c->d_err,
+                    s->comp, c->st));  // :385-387,399
   TRY(finish_deposit(c, s, 1, 4));
   KL("f32_curlB", curlB32(g, s->db1, s->np, (float)c->prm.alpha, s->aj, c->st));  // :395
   KL("f32_kit", build_kit(g, s->aj, s->up, s->db1, s->b0c, s->kit, c->st));       // :398, get_Ep :183-184
-  KL("f32_P2", pass(2, g, p, s->sp, sp, s->start, s->kit, s->partial, nullptr, nullptr, c->d_err, c->st));  // :400-402
+  KL("f32_P2", pass(2, g, p, s->sp, sp, s->start, s->kit, s->partial, s->partial_lo, nullptr, nullptr, c->d_err,
+                    s->comp, c->st));  // :400-402
   TRY(finish_deposit(c, s, 2, 3));
   KL("f32_kit", build_kit(g, s->aj, s->up, s->db1, s->b0c, s->kit, c->st));       // :404
   // :404-413, the final half move of :479 and res_chex; prepares the sort
-  KL("f32_P3", pass(3, g, p, s->sp, sp, s->start, s->kit, s->partial, s->dirrank, s->dep, c->d_err, c->st));
+  KL("f32_P3", pass(3, g, p, s->sp, sp, s->start, s->kit, s->partial, s->partial_lo, s->dirrank, s->dep, c->d_err,
+                    s->comp, c->st));
   {  // pass 3 wrote the new v into the vp1 arrays and left the old v (the new vp1) in place
     Part& q = s->buf[s->cur];
     std::swap(q.vx, q.wx);
@@ -715,6 +741,14 @@ extern "C" int swap_f32_count(swap_ctx* c, int64_t* n) {
   // after swap_f32_end the state's ions are those written back (the buffer
   // still holds the next step's staged ions)
   *n = s->ended ? s->n_out : s->N;
+  return SWAP_OK;
+}
+
+extern "C" int swap_f32_set_compensated(swap_ctx* c, int on) {
+  if (!c) return SWAP_EINVAL;
+  F32State* s = f32(c);
+  if (!s) return c->fail(SWAP_EINVAL, "swap_f32_begin has not been called");
+  s->comp = on != 0;
   return SWAP_OK;
 }
 

@@ -253,6 +253,17 @@ class Hybrid:
         """Let the FP32 form's conversions read and write the FP64 particle arrays in host memory."""
         self._check(self.lib.swap_set_host_direct(self.ctx, int(bool(on))))
 
+    def set_exchange(self, fn):
+        """fn(data_ptr, count, kind, stream_ptr) -> int replaces the rank's raw
+        deposit sums at data_ptr (device, `count` reals of `kind` bytes) by
+        their sum over the ranks (swap_set_exchange); None switches it off."""
+        if fn is None:
+            self._xfn = None
+            self._check(self.lib.swap_set_exchange(self.ctx, abi.EXCHANGE_FN(), None))
+            return
+        self._xfn = abi.EXCHANGE_FN(lambda user, data, count, kind, stream: fn(data, count, kind, stream))
+        self._check(self.lib.swap_set_exchange(self.ctx, self._xfn, None))
+
     def transfer_bytes(self, reset=False):
         """(h2d, d2h) bytes moved between the bound host arrays and the device since the last reset."""
         h2d, d2h = C.c_int64(), C.c_int64()
