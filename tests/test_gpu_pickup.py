@@ -101,8 +101,8 @@ def _pickup_pair(cx, steps=50):
     e0 = h.f32_energy()
     h.f32_run(steps)
     e1 = h.f32_energy()
-    n32 = h.f32_count()
     h.f32_end()
+    n32 = h.f32_count()  # the ions written back (the running state also holds the next step's new ions)
     h.sync_to_host()
     for _ in range(steps):
         o.ion_step()
