@@ -558,6 +558,7 @@ def run_ours(args):
     f32 = args.precision == "f32"
     if f32:
         h.f32_begin()
+        h._check(h.lib.swap_f32_set_moment_sums(h.ctx, 1 if args.moment_sums == "exact" else 0))
         run, count = h.f32_run, h.f32_count
     else:
         run, count = h.run, (lambda: int(h.ni_tot[0]))
@@ -778,6 +779,8 @@ def main():
     ap.add_argument("--only-accuracy", action="store_true", help="run the accuracy legs alone")
     ap.add_argument("--conv-only", type=int, nargs="+", default=None, metavar="N",
                     help="CIN COUT NX NY NZ [REPEATS]: the surrogate's convolution alone (profiling)")
+    ap.add_argument("--moment-sums", default="exact", choices=["exact", "plain"],
+                    help="the FP32 form's moment sums: exact fixed-point accumulation, or plain FP32 atomics")
     ap.add_argument("--fp64-steps", type=int, default=5, help="timed steps of the FP64 GPU drop-in leg (0 skips)")
     ap.add_argument("--ref-fp64-steps", type=int, default=2,
                     help="reference arm: timed full-size steps of the FP64 oracle beside the FP32 one (0 skips)")

@@ -299,12 +299,15 @@ int swap_f32_count(swap_ctx* ctx, int64_t* n);
  * brick * 64 + cell in the brick (x fastest, bricks x fastest), so key q
  * holds starts[q+1] - starts[q] ions.  n = entries of starts (>= nkeys+1). */
 int swap_f32_key_starts(swap_ctx* ctx, int64_t* starts, int64_t n);
-/* Moment sums of the FP32 form: 1 (the default after swap_f32_begin) =
- * compensated -- each warp's sum over a cell's ions is a Kahan sum, every
- * shared-memory add keeps its rounding error in a bf16 compensation, and the
- * brick partials are summed with their compensations by 2Sum; 0 = plain FP32
- * sums, kept to measure what the compensation gains. */
-int swap_f32_set_compensated(swap_ctx* ctx, int on);
+/* Moment sums of the FP32 form.  exact = 1 (the default after
+ * swap_f32_begin): each warp sums a cell's ions in FP32, and those sums are
+ * accumulated per brick and over the bricks as 64-bit fixed-point integers
+ * (units of 2^-40) -- exact, so a node's moment is its warp sums' exact total
+ * rounded once to FP32, and the same whatever order the GPU adds in (the
+ * FP32 form's steps are then reproducible bit for bit).  A warp sum beyond
+ * 2^22 or not finite ends the step with SWAP_ENONFINITE.  exact = 0: FP32
+ * atomics, kept to measure what the exact sums gain. */
+int swap_f32_set_moment_sums(swap_ctx* ctx, int exact);
 /* Validation: move particles idx[q] of the current (sorted) order by one
  * cell step per axis (dcell[q] = (dx+1) | (dy+1)<<10 | (dz+1)<<20) and run
  * the stable incremental sort that follows each ion step. */

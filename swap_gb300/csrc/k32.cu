@@ -1,5 +1,5 @@
 // k32.cu -- kernels of the FP32 form (see k32.cuh for the data layout).
-#include <cuda_bf16.h>
+#include <type_traits>
 
 #include "k32.cuh"
 #include "philox.h"
@@ -21,7 +21,7 @@ constexpr int PASS_STAGES = SWAP_PASS_STAGES;
 // flight land before it exits (the wait itself is bounded by
 // StepParams::wait_polls).
 constexpr uint32_t STAGE_WAIT_POLLS = 1u << 22;
-constexpr int KERR_DOMAIN = 3, KERR_CAPACITY = 4, KERR_MOVE = 7, KERR_STAGE = 8;
+constexpr int KERR_DOMAIN = 3, KERR_CAPACITY = 4, KERR_MOVE = 7, KERR_STAGE = 8, KERR_RANGE = 10;
 
 inline unsigned nblk(long long n, int tpb = TPB) {
   const long long b = (n + tpb - 1) / tpb;
@@ -138,39 +138,36 @@ __device__ __forceinline__ int dir_index(int dx, int dy, int dz) { return (dx + 
 // the particle's cell before the move (sorted, so runs stay long), and the
 // few particles that changed cell (mover) take no part in them; each of
 // those then adds its 32 values to the tile directly, one per lane.
-// One term of a run sum: acc += x*m, with the Kahan compensation kc (the run
-// sum is acc - kc).  The product is exact inside the fma.
-template <bool COMP>
-__device__ __forceinline__ void run_add(float& acc, float& kc, float x, float m) {
-  if (COMP) {
-    const float y = fmaf(x, m, -kc);
-    const float t = acc + y;
-    kc = (t - acc) - y;
-    acc = t;
+// Exact moment sums (EXACT): a shared-memory add takes the run sum in fixed
+// point, units of 2^-40, as a 64-bit integer.  Integer adds are exact and do
+// not depend on their order, so a node's tile value is the exact sum of its
+// rounded run sums, whatever order the warps add in; the brick partials are
+// summed the same way and rounded to FP32 once per node (k_node_sum).  Every
+// run sum must satisfy |x| < 2^22 (node moments far above any density the
+// workloads reach); a larger or non-finite one is reported (KERR_RANGE).
+// Otherwise (plain): FP32 atomics, whose result depends on the order.
+constexpr float FIX_SCALE = 1099511627776.0f;       // 2^40
+constexpr double FIX_INV = 1.0 / 1099511627776.0;   // 2^-40
+constexpr float FIX_MAX = 4194304.0f;               // 2^22
+
+template <bool EXACT>
+__device__ __forceinline__ void tile_add(void* tile, int i, float x, int* err) {
+  if (EXACT) {
+    if (!(fabsf(x) < FIX_MAX)) {
+      set_err(err, KERR_RANGE);
+      return;
+    }
+    const long long q = __float2ll_rn(x * FIX_SCALE);  // x * 2^40 is exact; one rounding to an integer
+    atomicAdd(static_cast<unsigned long long*>(tile) + i, (unsigned long long)q);  // two's complement
   } else {
-    acc = fmaf(x, m, acc);
+    atomicAdd(static_cast<float*>(tile) + i, x);
   }
 }
 
-// Add x (with the low part xlo) to tile node i.  COMP: the rounding error of
-// the shared-memory add -- the 2Sum error of the value the atomic found and x,
-// which the atomic rounds to nearest just as this thread does -- joins xlo in
-// the node's bf16 compensation.
-template <bool COMP>
-__device__ __forceinline__ void tile_add(float* hi, __nv_bfloat16* lo, int i, float x, float xlo) {
-  const float old = atomicAdd(hi + i, x);
-  if (COMP) {
-    const float s = old + x;
-    const float bp = s - old;
-    const float e = ((old - (s - bp)) + (x - bp)) + xlo;
-    if (e != 0.0f) atomicAdd(lo + i, __float2bfloat16_rn(e));
-  }
-}
-
-template <bool ALL_Q, int T, bool MOVERS = false, bool COMP = true>
+template <bool ALL_Q, int T, bool MOVERS = false, bool EXACT = true>
 __device__ __forceinline__ void warp_deposit(float (*red)[36], bool live, int t0, const float (&w8)[8],
-                                             const float (&qdv)[4], float* tile, __nv_bfloat16* tlo, int lane,
-                                             int trun = -1, bool mover = false) {
+                                             const float (&qdv)[4], void* tile, int* err, int lane, int trun = -1,
+                                             bool mover = false) {
   const bool in_runs = live && !(MOVERS && mover);
 #pragma unroll
   for (int c8 = 0; c8 < 8; ++c8) red[c8][lane] = live ? w8[c8] : 0.0f;
@@ -186,7 +183,7 @@ __device__ __forceinline__ void warp_deposit(float (*red)[36], bool live, int t0
   const bool add_here = ALL_Q || qv != 0;
   const float4* wrow = reinterpret_cast<const float4*>(red[cv]);
   const float4* mrow = reinterpret_cast<const float4*>(red[8 + qv]);
-  float acc = 0.0f, kc = 0.0f;
+  float acc = 0.0f;
 #pragma unroll
   for (int h = 0; h < 2; ++h) {  // two halves of 16 particles, to bound the registers
     float x[16], m[16];
@@ -201,23 +198,22 @@ __device__ __forceinline__ void warp_deposit(float (*red)[36], bool live, int t0
       const unsigned e4 = (ends >> (16 * h + 4 * g4)) & 0xfu;
       if (e4 == 0u) {
 #pragma unroll
-        for (int r = 4 * g4; r < 4 * g4 + 4; ++r) run_add<COMP>(acc, kc, x[r], m[r]);
+        for (int r = 4 * g4; r < 4 * g4 + 4; ++r) acc = fmaf(x[r], m[r], acc);
       } else {
 #pragma unroll
         for (int r = 4 * g4; r < 4 * g4 + 4; ++r) {
-          run_add<COMP>(acc, kc, x[r], m[r]);
+          acc = fmaf(x[r], m[r], acc);
           if ((e4 >> (r - 4 * g4)) & 1u) {
             const int tr = __shfl_sync(0xffffffffu, key, 16 * h + r);
-            if (add_here && tr >= 0) tile_add<COMP>(tile, tlo, qv * T * T * T + tr + off, acc, -kc);
+            if (add_here && tr >= 0) tile_add<EXACT>(tile, qv * T * T * T + tr + off, acc, err);
             acc = 0.0f;
-            kc = 0.0f;
           }
         }
       }
     }
   }
   const int tr = __shfl_sync(0xffffffffu, key, 31);  // the run that ends at the last particle
-  if (add_here && tr >= 0) tile_add<COMP>(tile, tlo, qv * T * T * T + tr + off, acc, -kc);
+  if (add_here && tr >= 0) tile_add<EXACT>(tile, qv * T * T * T + tr + off, acc, err);
   if (MOVERS) {
     unsigned mv = __ballot_sync(0xffffffffu, live && mover);
     if (mv) {
@@ -231,7 +227,7 @@ __device__ __forceinline__ void warp_deposit(float (*red)[36], bool live, int t0
         const int m = __ffs(mv) - 1;
         mv &= mv - 1;
         const int tm = __shfl_sync(0xffffffffu, t0, m);
-        if (add_here) tile_add<COMP>(tile, tlo, qv * T * T * T + tm + off, red[cv][m] * red[8 + qv][m], 0.0f);
+        if (add_here) tile_add<EXACT>(tile, qv * T * T * T + tm + off, red[cv][m] * red[8 + qv][m], err);
       }
     }
   }
@@ -250,11 +246,11 @@ __device__ __forceinline__ void warp_deposit(float (*red)[36], bool live, int t0
 //       res_chex after the second (maind.f:484).  It also prepares the sort:
 //       the direction of every particle's new cell from its key's cell and
 //       its rank among the particles of that key and direction, in order.
-template <int PASS, bool CHEX = false, bool COMP = true>
+template <int PASS, bool CHEX = false, bool EXACT = true>
 __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Part p, Species sp, StepParams sprm,
                                               const int64_t* __restrict__ start, const float4* __restrict__ kit,
-                                              float* __restrict__ partial, __nv_bfloat16* __restrict__ partial_lo,
-                                              uint32_t* __restrict__ dirrank, uint16_t* __restrict__ dep, int* err) {
+                                              void* __restrict__ partial, uint32_t* __restrict__ dirrank,
+                                              uint16_t* __restrict__ dep, int* err) {
   // the chunk's particles, copied in by the bulk-copy engine (double-buffered):
   // offsets and v, plus vp1 in P1; cell words; species bytes
   constexpr int NF = PASS == 1 ? 9 : 6, NS = PASS_STAGES;
@@ -269,8 +265,9 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
   constexpr int T = pass_tile(PASS), TNOD = T * T * T, O = PASS == 3 ? 1 : 0;
   __shared__ float4 s_kitA[PASS == 1 ? 1 : TNODES_IN];
   __shared__ float2 s_kitB[PASS == 1 ? 1 : TNODES_IN];
-  __shared__ float s_dep[4 * TNOD];
-  __shared__ __nv_bfloat16 s_dlo[COMP ? 4 * TNOD : 2];  // compensation of s_dep
+  // the deposit tile: 64-bit fixed point (EXACT) or FP32 per node and moment
+  using dep_t = typename std::conditional<EXACT, unsigned long long, float>::type;
+  __shared__ dep_t s_dep[4 * TNOD];
   // per warp: [8 weights, 4 moments][particle]; rows padded to 36 floats so
   // that the 8 rows a reducing lane group reads start on different banks
   __shared__ __align__(16) float s_red[TPB_PASS / 32][12][36];
@@ -289,10 +286,7 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
       s_kitB[t] = make_float2(hi.x, hi.y);
     }
   }
-  for (int t = threadIdx.x; t < 4 * TNOD; t += blockDim.x) {
-    s_dep[t] = 0.0f;
-    if (COMP) s_dlo[t] = __float2bfloat16_rn(0.0f);
-  }
+  for (int t = threadIdx.x; t < 4 * TNOD; t += blockDim.x) s_dep[t] = 0;
   if (PASS == 3)
     for (int t = threadIdx.x; t < BCELLS * NDIR; t += blockDim.x) s_rank[t] = 0;
   if (threadIdx.x == 0) {
@@ -495,7 +489,7 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
         qdv[3] = qw * dvz;
       }
     }
-    warp_deposit<PASS != 2, T, PASS == 3, COMP>(s_red[warp], live, t0, w8, qdv, s_dep, s_dlo, lane, t0o, mover);
+    warp_deposit<PASS != 2, T, PASS == 3, EXACT>(s_red[warp], live, t0, w8, qdv, s_dep, err, lane, t0o, mover);
     if (PASS == 3 && dirrank) {
       // stable ranks per (key, direction): the warps of the CTA take their
       // turn in order, each adding its particles after the earlier ones
@@ -519,12 +513,8 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
     if (lane == 0 && n_chex) atomicAdd(sprm.chex_count, (unsigned long long)n_chex);
   }
   __syncthreads();
-  float* out = partial + b * (4 * TNOD);
+  dep_t* out = static_cast<dep_t*>(partial) + b * (4 * TNOD);
   for (int t = threadIdx.x; t < 4 * TNOD; t += blockDim.x) out[t] = s_dep[t];
-  if (COMP) {
-    __nv_bfloat16* out_lo = partial_lo + b * (4 * TNOD);
-    for (int t = threadIdx.x; t < 4 * TNOD; t += blockDim.x) out_lo[t] = s_dlo[t];
-  }
 
   if (PASS == 3 && dep)
     for (int t = threadIdx.x; t < BCELLS * NDIR; t += blockDim.x)  // direction-major: dep[dir][key]
@@ -538,8 +528,8 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
 // (O = 1 for the 7-node tiles, whose origin is one node lower).  The density
 // is stored with its ghost images (boundary.f:167-206 fused in).
 template <int T>
-__global__ void k_node_sum(G32 g, const float* __restrict__ partial, const __nv_bfloat16* __restrict__ partial_lo,
-                           int nq, int comp, float* __restrict__ np, float* __restrict__ S) {
+__global__ void k_node_sum(G32 g, const void* __restrict__ partial, int nq, int exact, float* __restrict__ np,
+                           float* __restrict__ S) {
   constexpr int O = T == TN ? 1 : 0, TNOD = T * T * T;
   GSTRIDE(t, n_int(g)) {
     int P, Q, R;
@@ -557,25 +547,23 @@ __global__ void k_node_sum(G32 g, const float* __restrict__ partial, const __nv_
     bz[0] = (R + 1 + O) >> 2; oz[0] = (R + 1 + O) & 3;
     if (bz[0] >= g.nbz) bz[0] -= g.nbz;
     if (oz[0] + 4 < T) { bz[1] = bz[0] == 0 ? g.nbz - 1 : bz[0] - 1; oz[1] = oz[0] + 4; nzc = 2; }
-    float acc[4] = {0.f, 0.f, 0.f, 0.f}, cmp[4] = {0.f, 0.f, 0.f, 0.f};
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    unsigned long long fix[4] = {0, 0, 0, 0};  // exact: the fixed-point sums, wrapping like two's complement
     for (int a = 0; a < nxc; ++a)
       for (int bb = 0; bb < nyc; ++bb)
         for (int cc = 0; cc < nzc; ++cc) {
           const long long brick = bx[a] + (long long)g.nbx * (by[bb] + (long long)g.nby * bz[cc]);
-          const int tt = ox[a] + T * (oy[bb] + T * oz[cc]);
-          const float* src = partial + brick * (4 * TNOD) + tt;
-          if (comp) {  // 2Sum over the partials, plus their own compensations
-            const __nv_bfloat16* lo = partial_lo + brick * (4 * TNOD) + tt;
-            for (int q = 4 - nq; q < 4; ++q) {
-              const float v = src[q * TNOD], s = acc[q] + v, bp = s - acc[q];
-              cmp[q] += ((acc[q] - (s - bp)) + (v - bp)) + __bfloat162float(lo[q * TNOD]);
-              acc[q] = s;
-            }
+          const long long at = brick * (4 * TNOD) + ox[a] + T * (oy[bb] + T * oz[cc]);
+          if (exact) {
+            const unsigned long long* src = static_cast<const unsigned long long*>(partial) + at;
+            for (int q = 4 - nq; q < 4; ++q) fix[q] += src[q * TNOD];
           } else {
+            const float* src = static_cast<const float*>(partial) + at;
             for (int q = 4 - nq; q < 4; ++q) acc[q] += src[q * TNOD];
           }
         }
-    for (int q = 0; q < 4; ++q) acc[q] += cmp[q];
+    if (exact)  // the one rounding of the exact sum
+      for (int q = 0; q < 4; ++q) acc[q] = (float)((double)(long long)fix[q] * FIX_INV);
     const long long o = pid(g, P, Q, R);
     if (nq == 4) store_img(g, np, P + 2, Q + 2, R + 2, acc[0]);  // np with its ghost images
     S[o] = acc[1];
@@ -1567,12 +1555,11 @@ __global__ void k_energy_f(G32 g, const double* __restrict__ b0, const float* __
   } while (0)
 
 cudaError_t pass(int which, const G32& g, const Part& p, const Species& sp, const StepParams& s, const int64_t* start,
-                 const float4* kit, float* partial, uint16_t* partial_lo, uint32_t* dirrank, uint16_t* dep, int* err,
-                 bool comp, cudaStream_t st) {
+                 const float4* kit, void* partial, uint32_t* dirrank, uint16_t* dep, int* err, bool exact,
+                 cudaStream_t st) {
   const unsigned grid = (unsigned)g.nbricks;
-  __nv_bfloat16* lo = reinterpret_cast<__nv_bfloat16*>(partial_lo);
-#define PASS_ARGS g, p, sp, s, start, kit, partial, lo, dirrank, dep, err
-  if (comp) {
+#define PASS_ARGS g, p, sp, s, start, kit, partial, dirrank, dep, err
+  if (exact) {
     if (which == 1) RET((k_pass<1, false, true><<<grid, TPB_PASS, 0, st>>>(PASS_ARGS)));
     if (which == 2) RET((k_pass<2, false, true><<<grid, TPB_PASS, 0, st>>>(PASS_ARGS)));
     if (s.chex) RET((k_pass<3, true, true><<<grid, TPB_PASS, 0, st>>>(PASS_ARGS)));
@@ -1584,12 +1571,11 @@ cudaError_t pass(int which, const G32& g, const Part& p, const Species& sp, cons
   RET((k_pass<3, false, false><<<grid, TPB_PASS, 0, st>>>(PASS_ARGS)));
 #undef PASS_ARGS
 }
-cudaError_t node_sum(const G32& g, int pass, const float* partial, const uint16_t* partial_lo, int nq, bool comp,
-                     float* np, float* S, cudaStream_t st) {
+cudaError_t node_sum(const G32& g, int pass, const void* partial, int nq, bool exact, float* np, float* S,
+                     cudaStream_t st) {
   const unsigned nb = nblk((long long)g.ncx * g.ncy * g.ncz);
-  const __nv_bfloat16* lo = reinterpret_cast<const __nv_bfloat16*>(partial_lo);
-  if (pass_tile(pass) == TN) RET((k_node_sum<TN><<<nb, TPB, 0, st>>>(g, partial, lo, nq, comp ? 1 : 0, np, S)));
-  RET((k_node_sum<TN_IN><<<nb, TPB, 0, st>>>(g, partial, lo, nq, comp ? 1 : 0, np, S)));
+  if (pass_tile(pass) == TN) RET((k_node_sum<TN><<<nb, TPB, 0, st>>>(g, partial, nq, exact ? 1 : 0, np, S)));
+  RET((k_node_sum<TN_IN><<<nb, TPB, 0, st>>>(g, partial, nq, exact ? 1 : 0, np, S)));
 }
 cudaError_t ct_and_up(const G32& g, const float* np, const float* S, float* up, cudaStream_t st) {
   RET((k_ct_up<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, const_cast<float*>(np), S, up)));

@@ -134,20 +134,18 @@ __device__ __forceinline__ float offset_in_cell(double x, double q1, double d, i
 //     outflow and res_chex; writes each particle's sort direction and rank
 //     (dirrank) and the per-key direction counts (dep, direction-major:
 //     dep[dir * nkeys + key]) when those are given.
-// Moment sums (comp): each warp's sums over a cell's ions are compensated
-// (Kahan), each shared-memory add's rounding error goes to a bf16
-// compensation tile (2Sum of the value the atomic found and the addend), and
-// the brick partials are written as (float, bf16 compensation) pairs; with
-// comp = false the sums are plain FP32 (kept to measure what compensation
-// gains).
+// Moment sums (exact): each warp sums a cell's ions in FP32, and those run
+// sums go into the brick tile, then the brick partials, as 64-bit fixed-point
+// integers (2^-40): exact and independent of the order of the adds, rounded
+// to FP32 once per node by node_sum.  exact = false: FP32 atomics (kept to
+// measure what the exact sums gain).  partial: 8 bytes per tile entry.
 cudaError_t pass(int which, const G32& g, const Part& p, const Species& sp, const StepParams& sprm,
-                 const int64_t* start, const float4* kit, float* partial, uint16_t* partial_lo, uint32_t* dirrank,
-                 uint16_t* dep, int* err, bool comp, cudaStream_t st);
-// Sum the brick partial tiles into np and S (interior nodes, (nx,ny,nz) layout),
-// compensated (2Sum over the partials plus their compensations) when comp.
+                 const int64_t* start, const float4* kit, void* partial, uint32_t* dirrank, uint16_t* dep, int* err,
+                 bool exact, cudaStream_t st);
+// Sum the brick partial tiles into np and S (interior nodes, (nx,ny,nz) layout).
 // pass: the pass (1-3) whose tiles `partial` holds
-cudaError_t node_sum(const G32& g, int pass, const float* partial, const uint16_t* partial_lo, int nq, bool comp,
-                     float* np, float* S, cudaStream_t st);
+cudaError_t node_sum(const G32& g, int pass, const void* partial, int nq, bool exact, float* np, float* S,
+                     cudaStream_t st);
 
 // ---- fields ----
 cudaError_t ct_and_up(const G32& g, const float* np, const float* S, float* up, cudaStream_t st);

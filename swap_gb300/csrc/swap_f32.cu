@@ -33,9 +33,8 @@ struct F32State {
   uint32_t* dirrank = nullptr;
   uint16_t* dep = nullptr;
   uint16_t* pre = nullptr;
-  float* partial = nullptr;
-  uint16_t* partial_lo = nullptr;  // bf16 compensations of the brick partials
-  bool comp = true;                // compensated moment sums (swap_f32_set_compensated)
+  void* partial = nullptr;  // brick partial tiles, 8 bytes per entry (fixed point or FP32)
+  bool exact = true;        // exact moment sums (swap_f32_set_moment_sums)
   float4* kit = nullptr;
   float *np = nullptr, *S = nullptr, *up = nullptr, *aj = nullptr, *ct = nullptr, *E = nullptr, *nu = nullptr;
   long long np_span = 0;  // floats from np to the end of S (one allocation)
@@ -153,6 +152,8 @@ static int check_err(swap_ctx* c) {
     if (herr == 7)
       return c->fail(SWAP_EMOVE, "a particle moved more than one cell per axis since the last sort (|v| dt > dx)");
     if (herr == 8) return c->fail(SWAP_EWAIT, "a particle chunk copy did not complete within its wait limit");
+    if (herr == 10)
+      return c->fail(SWAP_ENONFINITE, "a moment sum is not finite or beyond the exact sums' range (|sum| < 2^22)");
     return c->fail(SWAP_ECUDA, "device error flag " + std::to_string(herr));
   }
   return SWAP_OK;
@@ -326,8 +327,7 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
     if (!s->order || cudaMemcpy(s->order, ord, sizeof(ord), cudaMemcpyHostToDevice) != cudaSuccess)
       return c->fail(SWAP_ECUDA, "sort order table");
   }
-  s->partial = s->alloc<float>((std::size_t)g.nbricks * 4 * TNODES);
-  s->partial_lo = s->alloc<uint16_t>((std::size_t)g.nbricks * 4 * TNODES);
+  s->partial = s->alloc<unsigned long long>((std::size_t)g.nbricks * 4 * TNODES);
   s->kit = s->alloc<float4>(2 * (std::size_t)ncx * ncy * ncz);
   // np and the velocity sums S in one block (S 128-byte aligned after np), so
   // that one exchange covers a deposit's node sums.  Zeroed once: the gap and
@@ -351,7 +351,7 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
   s->d_min = s->alloc<float>(4);
   s->dtn = s->alloc<float>(C);
   s->acc = s->alloc<double>(4);
-  if (!s->start || !s->start_new || !s->count || !s->sums || !s->dirrank || !s->dep || !s->pre || !s->partial || !s->partial_lo || !s->kit ||
+  if (!s->start || !s->start_new || !s->count || !s->sums || !s->dirrank || !s->dep || !s->pre || !s->partial || !s->kit ||
       !s->np || !s->S || !s->up || !s->aj || !s->ct || !s->E || !s->nu || !s->db1 || !s->db1p2 || !s->dbtp1 ||
       !s->b0 || !s->b1.l || !s->b12.l || !s->b1p2.l || !s->b0c || !s->d_min || !s->acc || !s->dtn)
     return c->fail(SWAP_ECUDA, "FP32 grid allocation failed");
@@ -418,7 +418,7 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
 
 // Deposit finish: node sums -> np (+ghosts) and up (maind.f:386-387 etc.).
 static int finish_deposit(swap_ctx* c, F32State* s, int pass, int nq) {
-  KL("f32_node_sum", node_sum(s->g, pass, s->partial, s->partial_lo, nq, s->comp, s->np, s->S, c->st));
+  KL("f32_node_sum", node_sum(s->g, pass, s->partial, nq, s->exact, s->np, s->S, c->st));
   // the rank sum of the raw node sums (MPI_ALLREDUCE, gutsp.f:1503,1812-1822);
   // pass 2 deposits no density
   if (nq == 4) TRY(c->exchange(s->np, s->np_span, 4));
@@ -644,18 +644,16 @@ static int one_step(swap_ctx* c, F32State* s) {
   const G32& g = s->g;
   const StepParams sp = step_params(c, s);
   const Part& p = s->buf[s->cur];
-  KL("f32_P1", pass(1, g, p, s->sp, sp, s->start, s->kit, s->partial, s->partial_lo, nullptr, nullptr, c->d_err,
-                    s->comp, c->st));  // :385-387,399
+  KL("f32_P1", pass(1, g, p, s->sp, sp, s->start, s->kit, s->partial, nullptr, nullptr, c->d_err, s->exact, c->st));  // :385-387,399
   TRY(finish_deposit(c, s, 1, 4));
   KL("f32_curlB", curlB32(g, s->db1, s->np, (float)c->prm.alpha, s->aj, c->st));  // :395
   KL("f32_kit", build_kit(g, s->aj, s->up, s->db1, s->b0c, s->kit, c->st));       // :398, get_Ep :183-184
-  KL("f32_P2", pass(2, g, p, s->sp, sp, s->start, s->kit, s->partial, s->partial_lo, nullptr, nullptr, c->d_err,
-                    s->comp, c->st));  // :400-402
+  KL("f32_P2", pass(2, g, p, s->sp, sp, s->start, s->kit, s->partial, nullptr, nullptr, c->d_err, s->exact, c->st));  // :400-402
   TRY(finish_deposit(c, s, 2, 3));
   KL("f32_kit", build_kit(g, s->aj, s->up, s->db1, s->b0c, s->kit, c->st));       // :404
   // :404-413, the final half move of :479 and res_chex; prepares the sort
-  KL("f32_P3", pass(3, g, p, s->sp, sp, s->start, s->kit, s->partial, s->partial_lo, s->dirrank, s->dep, c->d_err,
-                    s->comp, c->st));
+  KL("f32_P3", pass(3, g, p, s->sp, sp, s->start, s->kit, s->partial, s->dirrank, s->dep, c->d_err, s->exact,
+                    c->st));
   {  // pass 3 wrote the new v into the vp1 arrays and left the old v (the new vp1) in place
     Part& q = s->buf[s->cur];
     std::swap(q.vx, q.wx);
@@ -744,11 +742,11 @@ extern "C" int swap_f32_count(swap_ctx* c, int64_t* n) {
   return SWAP_OK;
 }
 
-extern "C" int swap_f32_set_compensated(swap_ctx* c, int on) {
+extern "C" int swap_f32_set_moment_sums(swap_ctx* c, int exact) {
   if (!c) return SWAP_EINVAL;
   F32State* s = f32(c);
   if (!s) return c->fail(SWAP_EINVAL, "swap_f32_begin has not been called");
-  s->comp = on != 0;
+  s->exact = exact != 0;
   return SWAP_OK;
 }
 
