@@ -301,12 +301,13 @@ int swap_f32_count(swap_ctx* ctx, int64_t* n);
 int swap_f32_key_starts(swap_ctx* ctx, int64_t* starts, int64_t n);
 /* Moment sums of the FP32 form.  exact = 1 (the default after
  * swap_f32_begin): each warp sums a cell's ions in FP32, and those sums are
- * accumulated per brick and over the bricks as 64-bit fixed-point integers
- * (units of 2^-40) -- exact, so a node's moment is its warp sums' exact total
- * rounded once to FP32, and the same whatever order the GPU adds in (the
- * FP32 form's steps are then reproducible bit for bit).  A warp sum beyond
- * 2^22 or not finite ends the step with SWAP_ENONFINITE.  exact = 0: FP32
- * atomics, kept to measure what the exact sums gain. */
+ * accumulated per brick and over the bricks as fixed-point integers (units of
+ * 2^-32) -- exact, so a node's moment is its warp sums' exact total rounded
+ * once to FP32, and the same whatever order the GPU adds in (the FP32 form's
+ * steps are then reproducible bit for bit).  A warp sum or node moment of
+ * 2^15 or more, a non-finite one, or a brick of 4x4x4 cells holding 65536
+ * ions or more ends the step with SWAP_ENONFINITE.  exact = 0: FP32 atomics,
+ * kept to measure what the exact sums gain. */
 int swap_f32_set_moment_sums(swap_ctx* ctx, int exact);
 /* Validation: move particles idx[q] of the current (sorted) order by one
  * cell step per axis (dcell[q] = (dx+1) | (dy+1)<<10 | (dz+1)<<20) and run
@@ -410,13 +411,13 @@ int swap_surrogate_attach(swap_ctx* ctx, swap_surrogate* net, int32_t judge_ever
 /* [0] steps by the network, [1] judged steps, [2] fallbacks, [3] last judged
  * B rel-L2, [4] last judged (B - b0) rel-L2. */
 int swap_surrogate_stats(swap_ctx* ctx, double out[5]);
-/* Test access: normalisation (8 input means and stds, output scale) and
+/* Test access: normalisation (11 input means and stds, output scale) and
  * FP32 master weights of a layer ([27][cout][cin] with (cin, cout) = (16,32),
  * (32,32), (32,32), (32,16): padded channels zero) with its bias; get or set. */
 int swap_surrogate_norm(swap_surrogate* net, float* mean, float* stdv, float* out_mean, float* out_std,
                         int32_t set);
 int swap_surrogate_weights(swap_surrogate* net, int32_t layer, float* w, float* b, int32_t set);
-/* One forward and backward pass on device inputs [V][8] and targets [V][3]
+/* One forward and backward pass on device inputs [V][11] and targets [V][3]
  * of an nx*ny*nz box: loss = 0.5 mean((out - (tgt - out_mean)/out_std)^2), gradients of
  * every layer into grads as (gW0, gb0, gW1, gb1, gW2, gb2, gW3, gb3). */
 int swap_surrogate_grads(swap_surrogate* net, int32_t nx, int32_t ny, int32_t nz, const float* vin, const float* tgt,

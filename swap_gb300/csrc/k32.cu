@@ -1,4 +1,5 @@
 // k32.cu -- kernels of the FP32 form (see k32.cuh for the data layout).
+#include <mutex>
 #include <type_traits>
 
 #include "k32.cuh"
@@ -138,27 +139,36 @@ __device__ __forceinline__ int dir_index(int dx, int dy, int dz) { return (dx + 
 // the particle's cell before the move (sorted, so runs stay long), and the
 // few particles that changed cell (mover) take no part in them; each of
 // those then adds its 32 values to the tile directly, one per lane.
-// Exact moment sums (EXACT): a shared-memory add takes the run sum in fixed
-// point, units of 2^-40, as a 64-bit integer.  Integer adds are exact and do
-// not depend on their order, so a node's tile value is the exact sum of its
-// rounded run sums, whatever order the warps add in; the brick partials are
-// summed the same way and rounded to FP32 once per node (k_node_sum).  Every
-// run sum must satisfy |x| < 2^22 (node moments far above any density the
-// workloads reach); a larger or non-finite one is reported (KERR_RANGE).
+// Exact moment sums (EXACT): a run sum x goes into the tile in fixed point,
+// units of 2^-32, split over two 32-bit words per node (low words first, then
+// the high words of all nodes): the high word takes h = floor(x * 2^16), the
+// low word the rest, l = (x * 2^16 - h) * 2^16 rounded, in [0, 2^16].  Both
+// are plain integer reductions (no returned value), exact and commutative,
+// so a node's tile value sum(h) * 2^16 + sum(l) is the exact sum of its
+// rounded run sums whatever order the warps add in.  The brick partials are
+// written as 64-bit integers, summed the same way and rounded to FP32 once
+// per node (k_node_sum).  Bounds: |x| < 2^15 per run sum and per node (the
+// high words wrap, so only the total must fit), and fewer than 2^16 adds per
+// node in a brick, i.e. fewer than 65536 ions per brick; a larger or
+// non-finite run sum, or a fuller brick, is reported (KERR_RANGE).
 // Otherwise (plain): FP32 atomics, whose result depends on the order.
-constexpr float FIX_SCALE = 1099511627776.0f;       // 2^40
-constexpr double FIX_INV = 1.0 / 1099511627776.0;   // 2^-40
-constexpr float FIX_MAX = 4194304.0f;               // 2^22
+constexpr double FIX_INV = 1.0 / 4294967296.0;  // 2^-32
+constexpr float FIX_MAX = 32768.0f;             // 2^15
+constexpr long long FIX_MAX_IONS = 65535;       // ions per brick
 
-template <bool EXACT>
+template <bool EXACT, int NT>
 __device__ __forceinline__ void tile_add(void* tile, int i, float x, int* err) {
   if (EXACT) {
     if (!(fabsf(x) < FIX_MAX)) {
       set_err(err, KERR_RANGE);
       return;
     }
-    const long long q = __float2ll_rn(x * FIX_SCALE);  // x * 2^40 is exact; one rounding to an integer
-    atomicAdd(static_cast<unsigned long long*>(tile) + i, (unsigned long long)q);  // two's complement
+    // x * 2^16 and its floor are exact floats; their difference is exact and
+    // in [0, 1); only the low part rounds, below 2^-32
+    const float xs = x * 65536.0f, fh = floorf(xs);
+    unsigned* w = static_cast<unsigned*>(tile);
+    atomicAdd(w + i, __float2uint_rn((xs - fh) * 65536.0f));
+    atomicAdd(w + NT + i, (unsigned)__float2int_rn(fh));  // two's complement
   } else {
     atomicAdd(static_cast<float*>(tile) + i, x);
   }
@@ -205,7 +215,7 @@ __device__ __forceinline__ void warp_deposit(float (*red)[36], bool live, int t0
           acc = fmaf(x[r], m[r], acc);
           if ((e4 >> (r - 4 * g4)) & 1u) {
             const int tr = __shfl_sync(0xffffffffu, key, 16 * h + r);
-            if (add_here && tr >= 0) tile_add<EXACT>(tile, qv * T * T * T + tr + off, acc, err);
+            if (add_here && tr >= 0) tile_add<EXACT, 4 * T * T * T>(tile, qv * T * T * T + tr + off, acc, err);
             acc = 0.0f;
           }
         }
@@ -213,7 +223,7 @@ __device__ __forceinline__ void warp_deposit(float (*red)[36], bool live, int t0
     }
   }
   const int tr = __shfl_sync(0xffffffffu, key, 31);  // the run that ends at the last particle
-  if (add_here && tr >= 0) tile_add<EXACT>(tile, qv * T * T * T + tr + off, acc, err);
+  if (add_here && tr >= 0) tile_add<EXACT, 4 * T * T * T>(tile, qv * T * T * T + tr + off, acc, err);
   if (MOVERS) {
     unsigned mv = __ballot_sync(0xffffffffu, live && mover);
     if (mv) {
@@ -227,7 +237,8 @@ __device__ __forceinline__ void warp_deposit(float (*red)[36], bool live, int t0
         const int m = __ffs(mv) - 1;
         mv &= mv - 1;
         const int tm = __shfl_sync(0xffffffffu, t0, m);
-        if (add_here) tile_add<EXACT>(tile, qv * T * T * T + tm + off, red[cv][m] * red[8 + qv][m], err);
+        if (add_here)
+          tile_add<EXACT, 4 * T * T * T>(tile, qv * T * T * T + tm + off, red[cv][m] * red[8 + qv][m], err);
       }
     }
   }
@@ -265,9 +276,9 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
   constexpr int T = pass_tile(PASS), TNOD = T * T * T, O = PASS == 3 ? 1 : 0;
   __shared__ float4 s_kitA[PASS == 1 ? 1 : TNODES_IN];
   __shared__ float2 s_kitB[PASS == 1 ? 1 : TNODES_IN];
-  // the deposit tile: 64-bit fixed point (EXACT) or FP32 per node and moment
-  using dep_t = typename std::conditional<EXACT, unsigned long long, float>::type;
-  __shared__ dep_t s_dep[4 * TNOD];
+  // the deposit tile per node and moment: FP32, or (EXACT) fixed point as
+  // low words [4 * TNOD] then high words [4 * TNOD]
+  __shared__ __align__(8) unsigned s_dep[(EXACT ? 2 : 1) * 4 * TNOD];
   // per warp: [8 weights, 4 moments][particle]; rows padded to 36 floats so
   // that the 8 rows a reducing lane group reads start on different banks
   __shared__ __align__(16) float s_red[TPB_PASS / 32][12][36];
@@ -286,7 +297,7 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
       s_kitB[t] = make_float2(hi.x, hi.y);
     }
   }
-  for (int t = threadIdx.x; t < 4 * TNOD; t += blockDim.x) s_dep[t] = 0;
+  for (int t = threadIdx.x; t < (EXACT ? 2 : 1) * 4 * TNOD; t += blockDim.x) s_dep[t] = 0u;
   if (PASS == 3)
     for (int t = threadIdx.x; t < BCELLS * NDIR; t += blockDim.x) s_rank[t] = 0;
   if (threadIdx.x == 0) {
@@ -297,6 +308,7 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
 
   const float hdt = 0.5f * sprm.dt;
   const long long first = start[b * BCELLS], last = start[b * BCELLS + BCELLS];
+  if (EXACT && last - first > FIX_MAX_IONS && threadIdx.x == 0) set_err(err, KERR_RANGE);
   // chunks of 128 particles from a 16-aligned start (every copy then starts
   // on a 16-byte boundary); lanes outside [first, last) are masked
   const long long a0 = first & ~15LL;
@@ -513,8 +525,14 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
     if (lane == 0 && n_chex) atomicAdd(sprm.chex_count, (unsigned long long)n_chex);
   }
   __syncthreads();
-  dep_t* out = static_cast<dep_t*>(partial) + b * (4 * TNOD);
-  for (int t = threadIdx.x; t < 4 * TNOD; t += blockDim.x) out[t] = s_dep[t];
+  if (EXACT) {  // the node's fixed-point value: high words * 2^16 + low words
+    long long* out = static_cast<long long*>(partial) + b * (4 * TNOD);
+    for (int t = threadIdx.x; t < 4 * TNOD; t += blockDim.x)
+      out[t] = (long long)(int)s_dep[4 * TNOD + t] * 65536LL + (long long)s_dep[t];
+  } else {
+    float* out = static_cast<float*>(partial) + b * (4 * TNOD);
+    for (int t = threadIdx.x; t < 4 * TNOD; t += blockDim.x) out[t] = __uint_as_float(s_dep[t]);
+  }
 
   if (PASS == 3 && dep)
     for (int t = threadIdx.x; t < BCELLS * NDIR; t += blockDim.x)  // direction-major: dep[dir][key]
@@ -548,14 +566,14 @@ __global__ void k_node_sum(G32 g, const void* __restrict__ partial, int nq, int 
     if (bz[0] >= g.nbz) bz[0] -= g.nbz;
     if (oz[0] + 4 < T) { bz[1] = bz[0] == 0 ? g.nbz - 1 : bz[0] - 1; oz[1] = oz[0] + 4; nzc = 2; }
     float acc[4] = {0.f, 0.f, 0.f, 0.f};
-    unsigned long long fix[4] = {0, 0, 0, 0};  // exact: the fixed-point sums, wrapping like two's complement
+    long long fix[4] = {0, 0, 0, 0};  // exact: the fixed-point sums (units of 2^-32)
     for (int a = 0; a < nxc; ++a)
       for (int bb = 0; bb < nyc; ++bb)
         for (int cc = 0; cc < nzc; ++cc) {
           const long long brick = bx[a] + (long long)g.nbx * (by[bb] + (long long)g.nby * bz[cc]);
           const long long at = brick * (4 * TNOD) + ox[a] + T * (oy[bb] + T * oz[cc]);
           if (exact) {
-            const unsigned long long* src = static_cast<const unsigned long long*>(partial) + at;
+            const long long* src = static_cast<const long long*>(partial) + at;
             for (int q = 4 - nq; q < 4; ++q) fix[q] += src[q * TNOD];
           } else {
             const float* src = static_cast<const float*>(partial) + at;
@@ -563,7 +581,7 @@ __global__ void k_node_sum(G32 g, const void* __restrict__ partial, int nq, int 
           }
         }
     if (exact)  // the one rounding of the exact sum
-      for (int q = 0; q < 4; ++q) acc[q] = (float)((double)(long long)fix[q] * FIX_INV);
+      for (int q = 0; q < 4; ++q) acc[q] = (float)((double)fix[q] * FIX_INV);
     const long long o = pid(g, P, Q, R);
     if (nq == 4) store_img(g, np, P + 2, Q + 2, R + 2, acc[0]);  // np with its ghost images
     S[o] = acc[1];
@@ -1015,15 +1033,19 @@ __global__ void k_judge(G32 g, const float* __restrict__ ah, const float* __rest
 }
 
 // The surrogate's inputs at every interior node (voxel v = x + ncx*(y +
-// ncy*z)): B = dB + b0, u_p, n_p and p_e = te * n_p, FP32 [V][8].
+// Surrogate inputs per interior node (v = P + ncx*(Q + ncy*R)), FP32
+// [V][SUR_NIN]: B = dB + b0, u_p, n_p, p_e = te * n_p, and E0 = ct + nu aj at
+// the faces (the plain E of get_E from the predictor's aj and ct; zero when
+// ct is null).
 __global__ void k_grid_to_voxels(G32 g, const float* __restrict__ db, const float* __restrict__ b0c,
                                  const float* __restrict__ up, const float* __restrict__ np, float te,
-                                 float* __restrict__ out) {
+                                 const float* __restrict__ ct, const float* __restrict__ aj,
+                                 const float* __restrict__ nu, float* __restrict__ out) {
   GSTRIDE(v, n_int(g)) {
     int i, j, k;
     interior_of(g, v, i, j, k);
     const long long C = g.C, o = nid(g, i, j, k);
-    float* r = out + v * 8;
+    float* r = out + v * SUR_NIN;
     r[0] = db[o] + b0c[0];
     r[1] = db[o + C] + b0c[1];
     r[2] = db[o + 2 * C] + b0c[2];
@@ -1032,25 +1054,32 @@ __global__ void k_grid_to_voxels(G32 g, const float* __restrict__ db, const floa
     r[5] = up[o + 2 * C];
     r[6] = np[o];
     r[7] = te * np[o];
+    r[8] = ct ? e_o<0>(g, ct, nu, aj, o) : 0.0f;
+    r[9] = ct ? e_o<1>(g, ct, nu, aj, o) : 0.0f;
+    r[10] = ct ? e_o<2>(g, ct, nu, aj, o) : 0.0f;
   }
 }
 
-// An E predicted per voxel ([V][3]) into the field layout with ghost images.
-__global__ void k_voxels_to_grid(G32 g, const float* __restrict__ ev, float* __restrict__ E) {
+// E = E0 + the predicted correction ([V][3]) into the field layout with ghost
+// images (E0 from the inputs vin, none when vin is null).
+__global__ void k_voxels_to_grid(G32 g, const float* __restrict__ ev, const float* __restrict__ vin,
+                                 float* __restrict__ E) {
   GSTRIDE(v, n_int(g)) {
     int i, j, k;
     interior_of(g, v, i, j, k);
-    for (int m = 0; m < 3; ++m) store_img(g, E + g.C * m, i, j, k, ev[v * 3 + m]);
+    for (int m = 0; m < 3; ++m)
+      store_img(g, E + g.C * m, i, j, k, ev[v * 3 + m] + (vin ? vin[v * SUR_NIN + 8 + m] : 0.0f));
   }
 }
 
-// Grid E (interior) into [V][3] per voxel, times a factor.
-__global__ void k_grid_e_to_voxels(G32 g, const float* __restrict__ E, float f, float* __restrict__ ev) {
+// Grid E (interior) times f into [V][3] per voxel, less E0 from vin (when given).
+__global__ void k_grid_e_to_voxels(G32 g, const float* __restrict__ E, float f, const float* __restrict__ vin,
+                                   float* __restrict__ ev) {
   GSTRIDE(v, n_int(g)) {
     int i, j, k;
     interior_of(g, v, i, j, k);
     const long long o = nid(g, i, j, k);
-    for (int m = 0; m < 3; ++m) ev[v * 3 + m] = f * E[o + g.C * m];
+    for (int m = 0; m < 3; ++m) ev[v * 3 + m] = f * E[o + g.C * m] - (vin ? vin[v * SUR_NIN + 8 + m] : 0.0f);
   }
 }
 
@@ -1554,21 +1583,37 @@ __global__ void k_energy_f(G32 g, const double* __restrict__ b0, const float* __
     return cudaGetLastError();   \
   } while (0)
 
+// One pass launch; the first launch of each form asks for the largest
+// shared-memory carve-out, so that the occupancy the launch bounds name (7 or
+// 8 CTAs per SM) fits the CTAs' shared tiles.
+template <int PASS, bool CHEX, bool EXACT>
+cudaError_t launch_pass(unsigned grid, cudaStream_t st, const G32& g, const Part& p, const Species& sp,
+                        const StepParams& s, const int64_t* start, const float4* kit, void* partial,
+                        uint32_t* dirrank, uint16_t* dep, int* err) {
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaFuncSetAttribute(k_pass<PASS, CHEX, EXACT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
+  });
+  k_pass<PASS, CHEX, EXACT><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, partial, dirrank, dep, err);
+  return cudaGetLastError();
+}
+
 cudaError_t pass(int which, const G32& g, const Part& p, const Species& sp, const StepParams& s, const int64_t* start,
                  const float4* kit, void* partial, uint32_t* dirrank, uint16_t* dep, int* err, bool exact,
                  cudaStream_t st) {
   const unsigned grid = (unsigned)g.nbricks;
-#define PASS_ARGS g, p, sp, s, start, kit, partial, dirrank, dep, err
+#define PASS_ARGS grid, st, g, p, sp, s, start, kit, partial, dirrank, dep, err
   if (exact) {
-    if (which == 1) RET((k_pass<1, false, true><<<grid, TPB_PASS, 0, st>>>(PASS_ARGS)));
-    if (which == 2) RET((k_pass<2, false, true><<<grid, TPB_PASS, 0, st>>>(PASS_ARGS)));
-    if (s.chex) RET((k_pass<3, true, true><<<grid, TPB_PASS, 0, st>>>(PASS_ARGS)));
-    RET((k_pass<3, false, true><<<grid, TPB_PASS, 0, st>>>(PASS_ARGS)));
+    if (which == 1) return launch_pass<1, false, true>(PASS_ARGS);
+    if (which == 2) return launch_pass<2, false, true>(PASS_ARGS);
+    if (s.chex) return launch_pass<3, true, true>(PASS_ARGS);
+    return launch_pass<3, false, true>(PASS_ARGS);
   }
-  if (which == 1) RET((k_pass<1, false, false><<<grid, TPB_PASS, 0, st>>>(PASS_ARGS)));
-  if (which == 2) RET((k_pass<2, false, false><<<grid, TPB_PASS, 0, st>>>(PASS_ARGS)));
-  if (s.chex) RET((k_pass<3, true, false><<<grid, TPB_PASS, 0, st>>>(PASS_ARGS)));
-  RET((k_pass<3, false, false><<<grid, TPB_PASS, 0, st>>>(PASS_ARGS)));
+  if (which == 1) return launch_pass<1, false, false>(PASS_ARGS);
+  if (which == 2) return launch_pass<2, false, false>(PASS_ARGS);
+  if (s.chex) return launch_pass<3, true, false>(PASS_ARGS);
+  return launch_pass<3, false, false>(PASS_ARGS);
 #undef PASS_ARGS
 }
 cudaError_t node_sum(const G32& g, int pass, const void* partial, int nq, bool exact, float* np, float* S,
@@ -1622,8 +1667,8 @@ cudaError_t df_lerp(const G32& g, const float* nh, const float* nl, const float*
   RET((k_df_lerp<<<grid, blk, 0, st>>>(g, nh, nl, oh, f, rh, rl)));
 }
 cudaError_t grid_to_voxels(const G32& g, const float* db, const float* b0c, const float* up, const float* np,
-                           float te, float* out, cudaStream_t st) {
-  RET((k_grid_to_voxels<<<nblk(n_int(g)), TPB, 0, st>>>(g, db, b0c, up, np, te, out)));
+                           float te, const float* ct, const float* aj, const float* nu, float* out, cudaStream_t st) {
+  RET((k_grid_to_voxels<<<nblk(n_int(g)), TPB, 0, st>>>(g, db, b0c, up, np, te, ct, aj, nu, out)));
 }
 cudaError_t judge_sums(const G32& g, const float* ah, const float* al, const float* bh, const float* bl,
                        const float* b0c, double* acc3, cudaStream_t st) {
@@ -1632,11 +1677,11 @@ cudaError_t judge_sums(const G32& g, const float* ah, const float* al, const flo
   const unsigned nb = nblk(n_int(g)) < 152u * 8u ? nblk(n_int(g)) : 152u * 8u;
   RET((k_judge<<<nb, TPB, 0, st>>>(g, ah, al, bh, bl, b0c, acc3)));
 }
-cudaError_t voxels_to_grid(const G32& g, const float* ev, float* E, cudaStream_t st) {
-  RET((k_voxels_to_grid<<<nblk(n_int(g)), TPB, 0, st>>>(g, ev, E)));
+cudaError_t voxels_to_grid(const G32& g, const float* ev, const float* vin, float* E, cudaStream_t st) {
+  RET((k_voxels_to_grid<<<nblk(n_int(g)), TPB, 0, st>>>(g, ev, vin, E)));
 }
-cudaError_t grid_e_to_voxels(const G32& g, const float* E, float f, float* ev, cudaStream_t st) {
-  RET((k_grid_e_to_voxels<<<nblk(n_int(g)), TPB, 0, st>>>(g, E, f, ev)));
+cudaError_t grid_e_to_voxels(const G32& g, const float* E, float f, const float* vin, float* ev, cudaStream_t st) {
+  RET((k_grid_e_to_voxels<<<nblk(n_int(g)), TPB, 0, st>>>(g, E, f, vin, ev)));
 }
 cudaError_t split_df(long long n, const double* a, float* h, float* l, cudaStream_t st) {
   RET((k_split_df<<<nblk(n), TPB, 0, st>>>(n, a, h, l)));

@@ -26,6 +26,8 @@ constexpr int TNODES_IN = TN_IN * TN_IN * TN_IN;  // 125
 __host__ __device__ constexpr int pass_tile(int pass) { return pass == 3 ? TN : TN_IN; }
 constexpr int NDIR = 27;              // displacements in {-1,0,1}^3
 constexpr int MAX_SPECIES = 16;
+// Inputs per voxel of the field surrogate: B (3), u_p (3), n_p, p_e, E0 (3).
+constexpr int SUR_NIN = 11;
 
 struct G32 {
   int nx, ny, nz;     // nodes incl. ghosts
@@ -135,9 +137,10 @@ __device__ __forceinline__ float offset_in_cell(double x, double q1, double d, i
 //     (dirrank) and the per-key direction counts (dep, direction-major:
 //     dep[dir * nkeys + key]) when those are given.
 // Moment sums (exact): each warp sums a cell's ions in FP32, and those run
-// sums go into the brick tile, then the brick partials, as 64-bit fixed-point
-// integers (2^-40): exact and independent of the order of the adds, rounded
-// to FP32 once per node by node_sum.  exact = false: FP32 atomics (kept to
+// sums go into the brick tile (two 32-bit words per node), then the brick
+// partials (64-bit), as fixed-point integers in units of 2^-32: exact and
+// independent of the order of the adds, rounded to FP32 once per node by
+// node_sum.  exact = false: FP32 atomics (kept to
 // measure what the exact sums gain).  partial: 8 bytes per tile entry.
 cudaError_t pass(int which, const G32& g, const Part& p, const Species& sp, const StepParams& sprm,
                  const int64_t* start, const float4* kit, void* partial, uint32_t* dirrank, uint16_t* dep, int* err,
@@ -168,15 +171,17 @@ cudaError_t b_step_given_e(const G32& g, const float* E, const float* bh, const 
 // r = b_new + f*(b_old - b_new) (double-float, hi parts of b_old).
 cudaError_t df_lerp(const G32& g, const float* nh, const float* nl, const float* oh, float f, float* rh, float* rl,
                     cudaStream_t st);
-// Surrogate inputs per interior node, FP32 [V][8]: B, u_p, n_p, te*n_p.
+// Surrogate inputs per interior node, FP32 [V][SUR_NIN]: B, u_p, n_p,
+// te*n_p and E0 = ct + nu aj (zero when ct is null).
 cudaError_t grid_to_voxels(const G32& g, const float* db, const float* b0c, const float* up, const float* np,
-                           float te, float* out, cudaStream_t st);
+                           float te, const float* ct, const float* aj, const float* nu, float* out, cudaStream_t st);
 // Sums over the interior of |B_a - B_b|^2, |B_b|^2 and |B_b - b0|^2.
 cudaError_t judge_sums(const G32& g, const float* ah, const float* al, const float* bh, const float* bl,
                        const float* b0c, double* acc3, cudaStream_t st);
-// [V][3] <-> the field layout (ghost images written).
-cudaError_t voxels_to_grid(const G32& g, const float* ev, float* E, cudaStream_t st);
-cudaError_t grid_e_to_voxels(const G32& g, const float* E, float f, float* ev, cudaStream_t st);
+// [V][3] <-> the field layout (ghost images written): E = ev + E0 of vin,
+// and ev = f*E - E0 of vin (no E0 when vin is null).
+cudaError_t voxels_to_grid(const G32& g, const float* ev, const float* vin, float* E, cudaStream_t st);
+cudaError_t grid_e_to_voxels(const G32& g, const float* E, float f, const float* vin, float* ev, cudaStream_t st);
 // FP64 <-> double-float (hi + lo).
 cudaError_t split_df(long long n, const double* a, float* h, float* l, cudaStream_t st);
 cudaError_t join_df(long long n, const float* h, const float* l, double* a, cudaStream_t st);

@@ -504,16 +504,19 @@ extern "C" int swap_conv3_check(int32_t nx, int32_t ny, int32_t nz, int32_t cin,
 namespace {
 
 constexpr int NL = 4;
-constexpr int LCIN[NL] = {16, 32, 32, 32};   // layer 0: 8 input channels padded to 16
+constexpr int LCIN[NL] = {16, 32, 32, 32};   // layer 0: 11 input channels padded to 16
 constexpr int LCOUT[NL] = {32, 32, 32, 16};  // layer 3: 3 output channels padded to 16
-constexpr int NIN = 8, NOUT = 3;
+// Inputs per voxel: B (3), u_p (3), n_p, p_e, and E0 (3), the plain scheme's
+// E at the start of the field step (the layout k32's voxel kernels write);
+// output: the mean corrector E of the subcycles minus E0.
+constexpr int NIN = 11, NOUT = 3;
 
 __device__ __forceinline__ float gelu_grad(float x) {
   const float t = tanh_hw(GELU_K0 * fmaf(GELU_K1 * x, x * x, x));
   return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * GELU_K0 * fmaf(3.0f * GELU_K1, x * x, 1.0f);
 }
 
-// Normalised BF16 inputs [V][16] from FP32 [V][8].
+// Normalised BF16 inputs [V][16] from FP32 [V][NIN].
 __global__ void k_norm_inputs(long long V, const float* __restrict__ in, const float* __restrict__ mean,
                               const float* __restrict__ inv_std, __nv_bfloat16* __restrict__ x) {
   for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
@@ -683,16 +686,20 @@ struct swap_surrogate {
   float *gw[NL] = {}, *gb[NL] = {}, *mw[NL] = {}, *vw[NL] = {}, *mb[NL] = {}, *vb[NL] = {};
   long long adam_t = 0;
   // normalisation: inputs (x - mean) / std, outputs (E - mean) / std
-  float in_mean[NIN] = {}, in_std[NIN] = {1, 1, 1, 1, 1, 1, 1, 1};
+  float in_mean[NIN] = {}, in_std[NIN] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1};
   OutNorm on{{0, 0, 0}, {1, 1, 1}};
   bool normed = false;
   float *d_mean = nullptr, *d_istd = nullptr;
-  // dataset of one grid shape
+  // the dataset, all of one grid shape (the first sample's)
+  int ds_nx = 0, ds_ny = 0, ds_nz = 0;
+  long long ds_V = 0;
+  int max_samples = 0;
+  std::vector<float*> ds_in, ds_tgt;  // [ds_V][NIN], [ds_V][3]
+  // work buffers for the grid shape in use (nx, ny, nz; V voxels): the
+  // dataset's while training, the run's in the step; reallocated on a change
   int nx = 0, ny = 0, nz = 0;
   long long V = 0;
-  int max_samples = 0;
-  std::vector<float*> ds_in, ds_tgt;  // [V][8], [V][3]
-  // work buffers for V voxels
+  std::vector<void*> work;
   __nv_bfloat16* x0 = nullptr;             // [V][16]
   __nv_bfloat16 *Z[NL - 1] = {}, *Y[NL - 1] = {};  // [V][32]
   float* out = nullptr;                    // [V][3]
@@ -713,6 +720,7 @@ struct swap_surrogate {
   }
   ~swap_surrogate() {
     for (void* p : owned) cudaFree(p);
+    for (void* p : work) cudaFree(p);
   }
 };
 
@@ -729,26 +737,46 @@ int fail(swap_surrogate* n, int code, const std::string& m) {
     if (_e != cudaSuccess) return fail(net, SWAP_ECUDA, std::string(#x) + ": " + cudaGetErrorString(_e)); \
   } while (0)
 
-// Work buffers for a grid of nx*ny*nz voxels (the first call fixes it).
+// Work buffers for a grid of nx*ny*nz voxels; a network trained on one shape
+// (patches) runs on another (the whole box): the convolutions are periodic
+// and local, so the weights do not depend on the shape.
 int ensure_shape(swap_surrogate* net, int nx, int ny, int nz) {
   const long long V = (long long)nx * ny * nz;
   if (net->V == V && net->nx == nx && net->ny == ny && net->nz == nz) return SWAP_OK;
-  if (net->V != 0) return fail(net, SWAP_EINVAL, "the surrogate is bound to another grid shape");
   if (V % 128) return fail(net, SWAP_EINVAL, "the surrogate needs a voxel count that is a multiple of 128");
-  net->nx = nx; net->ny = ny; net->nz = nz; net->V = V;
-  net->x0 = net->alloc<__nv_bfloat16>(V * 16);
-  for (int l = 0; l < NL - 1; ++l) {
-    net->Z[l] = net->alloc<__nv_bfloat16>(V * 32);
-    net->Y[l] = net->alloc<__nv_bfloat16>(V * 32);
+  if (!net->work.empty()) {
+    cudaDeviceSynchronize();  // the old buffers may still be read by queued work
+    for (void* p : net->work) cudaFree(p);
+    net->work.clear();
   }
-  net->out = net->alloc<float>(V * NOUT);
-  net->d16 = net->alloc<__nv_bfloat16>(V * 16);
-  net->dy = net->alloc<float>(V * 32);
-  net->dzA = net->alloc<__nv_bfloat16>(V * 32);
-  net->dzB = net->alloc<__nv_bfloat16>(V * 32);
-  if (!net->x0 || !net->Z[2] || !net->out || !net->d16 || !net->dy || !net->dzB)
+  net->nx = nx; net->ny = ny; net->nz = nz; net->V = V;
+  auto take = [net](std::size_t bytes) -> void* {
+    void* p = nullptr;
+    if (cudaMalloc(&p, bytes + 16) != cudaSuccess) return nullptr;
+    net->work.push_back(p);
+    return p;
+  };
+  net->x0 = static_cast<__nv_bfloat16*>(take(V * 16 * 2));
+  for (int l = 0; l < NL - 1; ++l) {
+    net->Z[l] = static_cast<__nv_bfloat16*>(take(V * 32 * 2));
+    net->Y[l] = static_cast<__nv_bfloat16*>(take(V * 32 * 2));
+  }
+  net->out = static_cast<float*>(take(V * NOUT * 4));
+  net->d16 = static_cast<__nv_bfloat16*>(take(V * 16 * 2));
+  net->dy = static_cast<float*>(take(V * 32 * 4));
+  net->dzA = static_cast<__nv_bfloat16*>(take(V * 32 * 2));
+  net->dzB = static_cast<__nv_bfloat16*>(take(V * 32 * 2));
+  if (net->work.size() != 2 * (NL - 1) + 6) {  // x0, Z and Y per hidden layer, out, d16, dy, dzA, dzB
+    net->V = 0;
     return fail(net, SWAP_ECUDA, "surrogate work buffers");
+  }
   return SWAP_OK;
+}
+
+// The dataset's shape for the work buffers (training).
+int ensure_ds_shape(swap_surrogate* net) {
+  if (!net->ds_V) return fail(net, SWAP_EINVAL, "the surrogate has no training samples");
+  return ensure_shape(net, net->ds_nx, net->ds_ny, net->ds_nz);
 }
 
 ConvArgs conv_args(swap_surrogate* net) {
@@ -872,7 +900,7 @@ int check_err(swap_surrogate* net) {
 
 namespace surr {
 
-// E predicted for FP32 inputs [V][8] (device) into ve [V][3] (device).
+// The network's output for FP32 inputs [V][11] (device) into ve [V][3] (device).
 int predict_e(swap_surrogate* net, int nx, int ny, int nz, const float* vin, float* ve, cudaStream_t st) {
   if (!net->normed) return fail(net, SWAP_EINVAL, "the surrogate has not been trained");
   int r = ensure_shape(net, nx, ny, nz);
@@ -885,16 +913,21 @@ int predict_e(swap_surrogate* net, int nx, int ny, int nz, const float* vin, flo
   return SWAP_OK;
 }
 
-// Append a training pair: inputs [V][8] and the target E [V][3] (device).
+// Append a training pair: inputs [V][NIN] and the target [V][3] (device).
 int add_sample(swap_surrogate* net, int nx, int ny, int nz, const float* vin, const float* ve, cudaStream_t st) {
-  int r = ensure_shape(net, nx, ny, nz);
-  if (r) return r;
+  const long long V = (long long)nx * ny * nz;
+  if (!net->ds_V) {
+    if (V % 128) return fail(net, SWAP_EINVAL, "the surrogate needs a voxel count that is a multiple of 128");
+    net->ds_nx = nx; net->ds_ny = ny; net->ds_nz = nz; net->ds_V = V;
+  } else if (net->ds_nx != nx || net->ds_ny != ny || net->ds_nz != nz) {
+    return fail(net, SWAP_EINVAL, "every training pair must come from a grid of the first pair's shape");
+  }
   if ((int)net->ds_in.size() >= net->max_samples) return SWAP_OK;  // the dataset is full
-  float* a = net->alloc<float>(net->V * NIN);
-  float* t = net->alloc<float>(net->V * NOUT);
+  float* a = net->alloc<float>(V * NIN);
+  float* t = net->alloc<float>(V * NOUT);
   if (!a || !t) return fail(net, SWAP_ECUDA, "surrogate dataset allocation");
-  SCU(cudaMemcpyAsync(a, vin, net->V * NIN * sizeof(float), cudaMemcpyDeviceToDevice, st));
-  SCU(cudaMemcpyAsync(t, ve, net->V * NOUT * sizeof(float), cudaMemcpyDeviceToDevice, st));
+  SCU(cudaMemcpyAsync(a, vin, V * NIN * sizeof(float), cudaMemcpyDeviceToDevice, st));
+  SCU(cudaMemcpyAsync(t, ve, V * NOUT * sizeof(float), cudaMemcpyDeviceToDevice, st));
   net->ds_in.push_back(a);
   net->ds_tgt.push_back(t);
   return SWAP_OK;
@@ -1038,7 +1071,7 @@ extern "C" int swap_surrogate_weights(swap_surrogate* net, int32_t layer, float*
   return SWAP_OK;
 }
 
-// One forward and backward pass on device inputs vin [V][8] and targets tgt
+// One forward and backward pass on device inputs vin [V][11] and targets tgt
 // [V][3] (unnormalised) of an nx*ny*nz box: the loss 0.5*mean((out -
 // (tgt - out_mean)/out_std)^2) and the gradients of every layer, written to grads as
 // (gW[0], gb[0], gW[1], gb[1], ...).
@@ -1073,7 +1106,7 @@ extern "C" int swap_surrogate_grads(swap_surrogate* net, int32_t nx, int32_t ny,
 static int fit_norm(swap_surrogate* net) {
   const std::size_t n = net->ds_in.size();
   if (!n) return fail(net, SWAP_EINVAL, "the surrogate has no training samples");
-  const std::size_t take = std::min<std::size_t>(n, 16), V = (std::size_t)net->V;
+  const std::size_t take = std::min<std::size_t>(n, 16), V = (std::size_t)net->ds_V;
   std::vector<float> hi(V * NIN), ht(V * NOUT);
   double s[NIN] = {}, s2[NIN] = {}, e1[NOUT] = {}, e2[NOUT] = {};
   for (std::size_t q = 0; q < take; ++q) {
@@ -1114,6 +1147,7 @@ extern "C" int swap_surrogate_train(swap_surrogate* net, int32_t epochs, double 
   if (!net->normed && (r = fit_norm(net))) return r;
   const std::size_t n = net->ds_in.size();
   if (!n) return fail(net, SWAP_EINVAL, "the surrogate has no training samples");
+  if ((r = ensure_ds_shape(net))) return r;
   cudaStream_t st = nullptr;
   std::mt19937_64 rng(net->seed + 17 + (uint64_t)net->adam_t);
   std::vector<std::size_t> order(n);
@@ -1143,6 +1177,7 @@ extern "C" int swap_surrogate_loss(swap_surrogate* net, double* loss) {
   if (!net || !loss) return SWAP_EINVAL;
   int r;
   if (!net->normed && (r = fit_norm(net))) return r;
+  if ((r = ensure_ds_shape(net))) return r;
   double tot = 0;
   for (std::size_t k = 0; k < net->ds_in.size(); ++k) {
     k_norm_inputs<<<nblk(net->V), 256, 0, nullptr>>>(net->V, net->ds_in[k], net->d_mean, net->d_istd, net->x0);

@@ -153,7 +153,8 @@ static int check_err(swap_ctx* c) {
       return c->fail(SWAP_EMOVE, "a particle moved more than one cell per axis since the last sort (|v| dt > dx)");
     if (herr == 8) return c->fail(SWAP_EWAIT, "a particle chunk copy did not complete within its wait limit");
     if (herr == 10)
-      return c->fail(SWAP_ENONFINITE, "a moment sum is not finite or beyond the exact sums' range (|sum| < 2^22)");
+      return c->fail(SWAP_ENONFINITE,
+                     "a moment sum is not finite or beyond the exact sums' range (|sum| < 2^15, < 65536 ions per brick)");
     return c->fail(SWAP_ECUDA, "device error flag " + std::to_string(herr));
   }
   return SWAP_OK;
@@ -547,7 +548,7 @@ static int sur_buffers(swap_ctx* c, F32State* s) {
   if (s->e_sum) return SWAP_OK;
   const std::size_t C = (std::size_t)s->g.C, V = (std::size_t)s->g.ncx * s->g.ncy * s->g.ncz;
   s->e_sum = s->alloc<float>(3 * C);
-  s->vin = s->alloc<float>(8 * V);
+  s->vin = s->alloc<float>((std::size_t)SUR_NIN * V);
   s->ve = s->alloc<float>(3 * V);
   s->jh = s->alloc<float>(3 * C);
   s->jl = s->alloc<float>(3 * C);
@@ -558,17 +559,27 @@ static int sur_buffers(swap_ctx* c, F32State* s) {
   return SWAP_OK;
 }
 
+// The network's inputs at the start of the subcycles: B, u_p, n_p, p_e and
+// E0, the plain E from the first predictor's aj and ct (curlB and the cross
+// product of get_E, maind.f:430,457).
+static int sur_inputs(swap_ctx* c, F32State* s) {
+  const G32& g = s->g;
+  KL("f32_sur_inputs", aj_ct(g, false, s->db1, s->np, s->up, s->b0c, (float)c->prm.alpha, s->aj, s->ct, c->st));
+  KL("f32_sur_inputs", grid_to_voxels(g, s->db1, s->b0c, s->up, s->np, 1.0f, s->ct, s->aj, s->nu, s->vin, c->st));
+  return SWAP_OK;
+}
+
 // The network's field advance from the state at the start of the subcycles:
-// E predicted per node, B into (oh, ol) and its dB into odb as B - dt curl E.
+// E = E0 + the predicted correction per node, B into (oh, ol) and its dB
+// into odb as B - dt curl E.  The inputs are in s->vin.
 static int sur_predict(swap_ctx* c, F32State* s, float* oh, float* ol, float* odb) {
   const G32& g = s->g;
-  KL("f32_sur_inputs", grid_to_voxels(g, s->db1, s->b0c, s->up, s->np, 1.0f, s->vin, c->st));
   {
     ProfScope ps(c, "f32_sur_net", c->st, 6);  // the network's own launches (normalise, 4 convs, scale)
     if (surr::predict_e(s->sur, g.ncx, g.ncy, g.ncz, s->vin, s->ve, c->st))
       return c->fail(SWAP_EINVAL, std::string("surrogate: ") + surr::last_error(s->sur));
   }
-  KL("f32_sur_E", voxels_to_grid(g, s->ve, s->E, c->st));
+  KL("f32_sur_E", voxels_to_grid(g, s->ve, s->vin, s->E, c->st));
   KL("f32_sur_B", b_step_given_e(g, s->E, s->b1.h, s->b1.l, c->prm.dt, s->b0c, oh, ol, odb, c->st));
   return SWAP_OK;
 }
@@ -584,6 +595,8 @@ static int field_step(swap_ctx* c, F32State* s) {
   const bool use_net = s->sur && !judge && !s->sur_off;
   if (s->sur) ++s->sur_step;
   if (use_net) {
+    TRY(sur_buffers(c, s));
+    TRY(sur_inputs(c, s));
     TRY(sur_predict(c, s, s->b1p2.h, s->b1p2.l, s->db1p2));
     // b12: B one subcycle before the end of the step, the leapfrog base of the next predictor
     KL("f32_sur_B", df_lerp(g, s->b1p2.h, s->b1p2.l, s->b1.h, 1.0f / (float)c->prm.ntsub, s->b12.h, s->b12.l,
@@ -598,11 +611,11 @@ static int field_step(swap_ctx* c, F32State* s) {
     TRY(sur_buffers(c, s));
     CU(cudaMemsetAsync(s->e_sum, 0, 3 * (std::size_t)g.C * sizeof(float), c->st));
   }
+  if (collect || judge) TRY(sur_inputs(c, s));
   if (judge) TRY(sur_predict(c, s, s->jh, s->jl, s->jdb));
-  if (collect) KL("f32_sur_inputs", grid_to_voxels(g, s->db1, s->b0c, s->up, s->np, 1.0f, s->vin, c->st));
   TRY(subcycles(c, s, (collect || judge) ? s->e_sum : nullptr));
   if (collect) {
-    KL("f32_sur_target", grid_e_to_voxels(g, s->e_sum, (float)(1.0 / s->last_ntf), s->ve, c->st));
+    KL("f32_sur_target", grid_e_to_voxels(g, s->e_sum, (float)(1.0 / s->last_ntf), s->vin, s->ve, c->st));
     if (surr::add_sample(s->collect, g.ncx, g.ncy, g.ncz, s->vin, s->ve, c->st))
       return c->fail(SWAP_EINVAL, std::string("surrogate: ") + surr::last_error(s->collect));
   }

@@ -110,8 +110,9 @@ def config(n: int, **over) -> RunConfig:
        sigma = 1 - 0.1 ln v_rel; 300 steps, seed 3.
     3: the physics of 2 on 512x256x256 cells at 16 ppc (536,870,912 ions),
        1000 steps, seed 4 (the FP32 form against an FP64 run).
-    4: 3 with a stronger B0 (2, so Omega_i dt = 0.1) and 20 field subcycles
-       per ion step, seed 5 (the learned field surrogate's workload).
+    4: 3 with a stronger B0 (2: Omega_i = 2, v_A = 2), the ion step kept at
+       0.05 / Omega_i (dt = 0.025) and 20 field subcycles per ion step,
+       seed 5 (the learned field surrogate's workload).
     """
     base = {
         0: dict(name="uniform H+ 64x32x32, 16 ppc", cells=(64, 32, 32), ppc=16, steps=100, seed=1),
@@ -122,7 +123,7 @@ def config(n: int, **over) -> RunConfig:
         3: dict(name="pickup ions 512x256x256, 16 ppc, cloud + charge exchange", cells=(512, 256, 256), ppc=16,
                 u=(4.0, 0.0, 0.0), steps=1000, seed=4),
         4: dict(name="pickup ions 512x256x256, 16 ppc, strong B0, 20 subcycles", cells=(512, 256, 256), ppc=16,
-                u=(4.0, 0.0, 0.0), b0=2.0, ntsub=20, steps=1000, seed=5),
+                u=(8.0, 0.0, 0.0), b0=2.0, dt=0.025, ntsub=20, steps=1000, seed=5),
     }[n]
     base.update(over)
     cfg = RunConfig(**base)
@@ -458,6 +459,9 @@ class Surrogate:
     """The learned field-subcycle surrogate (a handle of the C-ABI)."""
 
     LAYERS = ((16, 32), (32, 32), (32, 32), (32, 16))  # (cin, cout) of the 4 conv layers, padded
+    # inputs per voxel: B (3), u_p (3), n_p, p_e, and E0 (3), the plain E at the
+    # start of the field step; the output is the mean corrector E minus E0
+    NIN = 11
 
     def __init__(self, seed: int = 1, max_samples: int = 4096):
         self.lib = abi.load()
@@ -503,8 +507,9 @@ class Surrogate:
 
     def norm(self, mean=None, std=None, out_mean=None, out_std=None):
         """Get (mean, std, out_mean, out_std) or set them: inputs are fed as
-        (x - mean)/std, the network predicts (E - out_mean)/out_std."""
-        a = [np.zeros(8, np.float32), np.ones(8, np.float32), np.zeros(3, np.float32), np.ones(3, np.float32)]
+        (x - mean)/std, the network predicts (E - E0 - out_mean)/out_std."""
+        a = [np.zeros(self.NIN, np.float32), np.ones(self.NIN, np.float32), np.zeros(3, np.float32),
+             np.ones(3, np.float32)]
         if mean is None:
             self._check(self.lib.swap_surrogate_norm(self.h, *(x.ctypes.data for x in a), 0))
             return tuple(a)
@@ -526,7 +531,7 @@ class Surrogate:
         return None
 
     def grads(self, dims, vin_dev_ptr: int, tgt_dev_ptr: int):
-        """Loss and per-layer (gW, gb) for device inputs [V][8] and targets [V][3]."""
+        """Loss and per-layer (gW, gb) for device inputs [V][NIN] and targets [V][3]."""
         n = sum(27 * ci * co + co for ci, co in self.LAYERS)
         g = np.zeros(n, dtype=np.float32)
         loss = C.c_double()

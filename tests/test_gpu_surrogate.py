@@ -79,7 +79,7 @@ def _ref_forward_backward(vin, tgt, layers, mean, std, out_mean, out_std, dims):
 
     nx, ny, nz = dims
     x = ((vin - mean) / std).float().to(torch.bfloat16).double()
-    x = torch.cat([x, torch.zeros(x.shape[0], 8, dtype=x.dtype)], 1)
+    x = torch.cat([x, torch.zeros(x.shape[0], 16 - x.shape[1], dtype=x.dtype)], 1)
     params = []
     h = x
     for l, (w, b) in enumerate(layers):
@@ -110,9 +110,9 @@ def test_surrogate_gradients_match_cpu(dims):
     V = dims[0] * dims[1] * dims[2]
     net = Surrogate(seed=5)
     g = torch.Generator().manual_seed(3)
-    vin = torch.randn(V, 8, generator=g, dtype=torch.float64)
+    vin = torch.randn(V, Surrogate.NIN, generator=g, dtype=torch.float64)
     tgt = torch.randn(V, 3, generator=g, dtype=torch.float64)
-    mean, std = np.full(8, 0.1), np.full(8, 1.5)
+    mean, std = np.full(Surrogate.NIN, 0.1), np.full(Surrogate.NIN, 1.5)
     out_mean, out_std = np.array([0.5, -0.25, 0.0]), np.array([0.75, 0.5, 2.0])
     net.norm(mean, std, out_mean, out_std)
     layers = [net.weights(l) for l in range(4)]
@@ -193,3 +193,44 @@ def test_surrogate_step_is_faster_than_the_subcycles():
     attach_surrogate(h, None)
     h.f32_end()
     assert fast < 0.85 * plain, (fast, plain)
+
+
+def test_surrogate_meets_the_bound_on_runs_it_was_not_trained_on():
+    """Trained on pairs from randomized runs (upstream speed 1-6 v_A, beta
+    0.1-2, cloud radius 2-10 cells), the network advances the field of new
+    runs within the stated bound: judged every other step at B rel-L2 1e-3,
+    more than half of the judged steps pass with no fallback, and the
+    network takes the steps in between."""
+    from swap_gb300.hybrid import Hybrid, Surrogate, attach_surrogate, config, surrogate_stats
+    from swap_gb300.surrogate_data import collect_randomized, run_config
+
+    cells = (32, 32, 32)
+    base = config(0, cells=cells, ppc=8)
+    net = Surrogate(seed=3, max_samples=48)
+    collect_randomized(net, base, runs=8, pairs_per_run=6, warmup=3, cells=cells, seed=1)
+    assert net.samples() == 48
+    l0 = net.loss()
+    l1 = net.train(30, lr=2e-3)
+    assert l1 < 0.3 * l0, (l0, l1)
+    for trial in range(2):
+        cfg = run_config(base, np.random.default_rng(90 + trial), cells, 90 + trial)
+        h = Hybrid(cfg, ni_max=cfg.ni_max_hint(40), work_arrays=False)
+        h.load_maxwellian()
+        h.set_sources(cfg.make_sources(), 0)
+        h.sync_to_device()
+        h.f32_begin()
+        h.f32_run(3)
+        attach_surrogate(h, net, judge_every=2, bound=1e-3)
+        h.f32_run(20)
+        st = surrogate_stats(h)
+        print(cfg.name, st)
+        assert st["judged"] == 10, st
+        assert st["judged"] - st["fallbacks"] > st["judged"] / 2, st
+        assert st["net_steps"] >= 5 and st["err_b"] < 1e-3, st
+        attach_surrogate(h, None)
+        h.f32_end()
+        h.sync_to_host()
+        assert np.all(np.isfinite(h.b1))
+        assert h.max_abs_divB(h.b1) < 1e-5
+        h.close()
+    net.close()
