@@ -296,23 +296,44 @@ def run_reference(args):
 # our arm
 # ---------------------------------------------------------------------------
 
-def run_surrogate(h, args, N, ws):
-    """The FP32 step with the learned field surrogate in place of the
-    subcycles: collect training pairs from plain steps, train, attach with a
-    judge every few steps, then time K steps the same way as the plain run."""
-    import ctypes as C
+def train_surrogate(args, base):
+    """The learned field surrogate, trained on pairs that the plain subcycles
+    produce in randomized runs (swap_gb300.surrogate_data: upstream speed
+    1-6 v_A, beta 0.1-2, a neutral cloud of radius 2-10 cells) of a box of
+    --sur-cells cells that keeps the workload's B0, ion step, subcycles and
+    particles per cell.  Returns the network and what the training did."""
+    from swap_gb300.hybrid import Surrogate
+    from swap_gb300.surrogate_data import collect_randomized
 
-    from swap_gb300.hybrid import Surrogate, attach_surrogate, surrogate_stats
-
-    lib, ctx = h.lib, h.ctx
-    h.f32_begin()
-    net = Surrogate(seed=11, max_samples=args.sur_collect)
+    cells = (args.sur_cells,) * 3
+    net = Surrogate(seed=11, max_samples=args.sur_runs * args.sur_pairs)
     t0 = time.perf_counter()
-    net.collect(h, args.sur_collect)
+    collect_randomized(net, base, runs=args.sur_runs, pairs_per_run=args.sur_pairs, warmup=3, cells=cells, seed=5)
     t_collect = time.perf_counter() - t0
+    l0 = net.loss()
     t0 = time.perf_counter()
     loss = net.train(args.sur_epochs, lr=2e-3)
     t_train = time.perf_counter() - t0
+    info = {"network": "4 periodic 3x3x3 conv layers 11-32-32-32-3, GELU, BF16 on tcgen05, FP32 accumulate; "
+                       "predicts the subcycles' mean E minus the plain E at the step's start",
+            "training": f"{args.sur_runs} randomized runs of {cells[0]}x{cells[1]}x{cells[2]} cells at "
+                        f"{base.ppc} ppc, {args.sur_pairs} pairs each (upstream speed 1-6 v_A, beta 0.1-2, "
+                        f"cloud radius 2-10 cells)",
+            "pairs": net.samples(), "collect_s": t_collect, "train_epochs": args.sur_epochs, "train_s": t_train,
+            "loss_before": l0, "train_loss": loss}
+    return net, info
+
+
+def run_surrogate(h, args, N, ws, net, info):
+    """The FP32 step with the learned field surrogate in place of the
+    subcycles, judged against them every --sur-judge steps: K steps timed the
+    same way as the plain run."""
+    import ctypes as C
+
+    from swap_gb300.hybrid import attach_surrogate, surrogate_stats
+
+    lib, ctx = h.lib, h.ctx
+    h.f32_begin()
     attach_surrogate(h, net, judge_every=args.sur_judge, bound=args.sur_bound)
     for _ in range(args.warmup):
         h.f32_run(1)
@@ -336,24 +357,22 @@ def run_surrogate(h, args, N, ws):
              if names[i].decode().startswith(("f32_sur", "f32_aj_ct", "f32_bstep", "f32_courant"))}
     attach_surrogate(h, None)
     h.f32_end()
-    net.close()
-    return {"ms_per_step": t_ms / args.steps, "value": N * args.steps * ws / (t_ms / 1e3), "unit": UNIT,
-            "network": "4 periodic 3x3x3 conv layers 8-32-32-32-3, GELU, BF16 on tcgen05, FP32 accumulate",
-            "collect_steps": args.sur_collect, "collect_s": t_collect, "train_epochs": args.sur_epochs,
-            "train_s": t_train, "train_loss": loss, "judge_every": args.sur_judge, "bound": args.sur_bound,
-            "net_steps": st["net_steps"] - before["net_steps"], "judged": st["judged"] - before["judged"],
-            "fallbacks": st["fallbacks"] - before["fallbacks"], "last_err_b": st["err_b"],
-            "last_err_db": st["err_db"], "field_ms_per_step": field}
+    return dict(info, ms_per_step=t_ms / args.steps, value=N * args.steps * ws / (t_ms / 1e3), unit=UNIT,
+                judge_every=args.sur_judge, bound=args.sur_bound,
+                net_steps=st["net_steps"] - before["net_steps"], judged=st["judged"] - before["judged"],
+                fallbacks=st["fallbacks"] - before["fallbacks"], last_err_b=st["err_b"], last_err_db=st["err_db"],
+                field_ms_per_step=field)
 
 
-def run_accuracy(args):
+def run_accuracy(args, net=None):
     """The error of the FP32 form and of the FP32 form with the surrogate
     against the FP64 GPU drop-in, after the same number of ion steps from the
     same seeded load: the periodic 64x32x32-cell box at 16 ppc (no sources,
-    so the total energy is conserved up to the scheme's own drift)."""
+    so the total energy is conserved up to the scheme's own drift).  net: the
+    trained surrogate (None skips that leg)."""
     import numpy as np
 
-    from swap_gb300.hybrid import Hybrid, Surrogate, attach_surrogate, config, surrogate_stats
+    from swap_gb300.hybrid import Hybrid, attach_surrogate, config, surrogate_stats
 
     cfg = config(0)
     S = args.acc_steps
@@ -381,30 +400,28 @@ def run_accuracy(args):
     out = {"workload": f"{cfg.name} (periodic, 1,048,576 ions), {S} ion steps from the same seeded load",
            "fp64_energy_drift": (total(e64) - total(e0)) / total(e0)}
     for form in ("fp32", "fp32_surrogate"):
+        if form == "fp32_surrogate" and net is None:
+            continue
         h = fresh()
         h.f32_begin()
         ea = h.f32_energy()
         if form == "fp32":
             h.f32_run(S)
         else:
-            ncol = min(24, S // 2)
-            net = Surrogate(seed=7, max_samples=ncol)
-            net.collect(h, ncol)
-            net.train(12, lr=2e-3)
-            attach_surrogate(h, net, judge_every=8, bound=1e-3)
-            h.f32_run(S - ncol)
+            attach_surrogate(h, net, judge_every=args.sur_judge, bound=args.sur_bound)
+            h.f32_run(S)
             st = surrogate_stats(h)
-            out["surrogate_steps"] = {"collected": ncol, "network": st["net_steps"], "judged": st["judged"],
-                                      "fallbacks": st["fallbacks"], "bound": 1e-3}
+            out["surrogate_steps"] = {"network": st["net_steps"], "judged": st["judged"],
+                                      "fallbacks": st["fallbacks"], "bound": args.sur_bound,
+                                      "judge_every": args.sur_judge, "last_err_b": st["err_b"],
+                                      "last_err_db": st["err_db"]}
+            attach_surrogate(h, None)
         eb = h.f32_energy()
         h.f32_end()
         h.sync_to_host()
         out[form] = {"b_rel_l2": rel(h.b1, ref["b1"]), "db_rel_l2": rel(h.b1 - h.b0, ref["b1"] - ref["b0"]),
                      "np_rel_l2": rel(h.np, ref["np"]), "energy_drift": (total(eb) - total(ea)) / total(ea),
                      "energy_vs_fp64": (total(eb) - total(e64)) / total(e64)}
-        if form == "fp32_surrogate":
-            attach_surrogate(h, None)
-            net.close()
         h.close()
     out["seconds"] = time.perf_counter() - t0
     return out
@@ -664,9 +681,11 @@ def run_ours(args):
                 "d2h_bytes_per_step": d2h_bytes / args.steps},
         "load_seconds": t_load,
     }
+    net = None
     if f32 and args.surrogate != "off":
         try:
-            line["surrogate"] = run_surrogate(h, args, N, ws)
+            net, info = train_surrogate(args, cfg)
+            line["surrogate"] = run_surrogate(h, args, N, ws, net, info)
         except Exception as e:  # the headline stands without it
             line["surrogate"] = {"error": f"{type(e).__name__}: {e}"}
     if f32 and args.fp64_steps > 0:
@@ -683,7 +702,9 @@ def run_ours(args):
 
     gc.collect()
     if rank == 0:
-        run_accuracy_legs(args, line)
+        run_accuracy_legs(args, line, net)
+    if net is not None:
+        net.close()
     if rank == 0 and not args.no_cpu_baseline:
         try:
             r = oracle_run(cfg, "f32", 1, 1, os.cpu_count() or 1)
@@ -732,12 +753,12 @@ def run_conv_only(spec) -> int:
     return 0
 
 
-def run_accuracy_legs(args, line):
+def run_accuracy_legs(args, line, net=None):
     """The error legs of the line: the 64x32x32 box (FP64, FP32, FP32 with
     the surrogate), then the configs --acc-configs at their stated sizes."""
     if args.precision == "f32" and args.acc_steps > 0:
         try:
-            line["accuracy"] = run_accuracy(args)
+            line["accuracy"] = run_accuracy(args, net)
         except Exception as e:  # the headline stands without it
             line["accuracy"] = {"error": f"{type(e).__name__}: {e}"}
     steps = {2: args.acc2_steps, 3: args.acc3_steps}
@@ -764,8 +785,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--surrogate", default="on", choices=["on", "off"],
                     help="also time the FP32 step with the learned field surrogate")
-    ap.add_argument("--sur-collect", type=int, default=24, help="plain steps collected as training pairs")
-    ap.add_argument("--sur-epochs", type=int, default=12)
+    ap.add_argument("--sur-runs", type=int, default=12, help="randomized runs that give the training pairs")
+    ap.add_argument("--sur-pairs", type=int, default=6, help="training pairs per run")
+    ap.add_argument("--sur-cells", type=int, default=64, help="cells per axis of the training runs' box")
+    ap.add_argument("--sur-epochs", type=int, default=20)
     ap.add_argument("--sur-judge", type=int, default=8, help="judge the surrogate every this many steps")
     ap.add_argument("--sur-bound", type=float, default=1e-3, help="judge bound on the relative B error")
     ap.add_argument("--acc-steps", type=int, default=1000,
