@@ -157,12 +157,12 @@ constexpr float FIX_MAX = 32768.0f;             // 2^15
 constexpr long long FIX_MAX_IONS = 65535;       // ions per brick
 
 template <bool EXACT, int NT>
-__device__ __forceinline__ void tile_add(void* tile, int i, float x, int* err) {
+__device__ __forceinline__ void tile_add(void* tile, int i, float x, unsigned& bad) {
   if (EXACT) {
-    if (!(fabsf(x) < FIX_MAX)) {
-      set_err(err, KERR_RANGE);
-      return;
-    }
+    // out of range or not finite: noted here, reported once at the pass's end
+    // (a branch to the error word in this loop costs the passes 10%); the
+    // conversions saturate, so the adds below stay defined
+    bad |= fabsf(x) < FIX_MAX ? 0u : 1u;
     // x * 2^16 and its floor are exact floats; their difference is exact and
     // in [0, 1); only the low part rounds, below 2^-32
     const float xs = x * 65536.0f, fh = floorf(xs);
@@ -176,8 +176,8 @@ __device__ __forceinline__ void tile_add(void* tile, int i, float x, int* err) {
 
 template <bool ALL_Q, int T, bool MOVERS = false, bool EXACT = true>
 __device__ __forceinline__ void warp_deposit(float (*red)[36], bool live, int t0, const float (&w8)[8],
-                                             const float (&qdv)[4], void* tile, int* err, int lane, int trun = -1,
-                                             bool mover = false) {
+                                             const float (&qdv)[4], void* tile, unsigned& bad, int lane,
+                                             int trun = -1, bool mover = false) {
   const bool in_runs = live && !(MOVERS && mover);
 #pragma unroll
   for (int c8 = 0; c8 < 8; ++c8) red[c8][lane] = live ? w8[c8] : 0.0f;
@@ -215,7 +215,7 @@ __device__ __forceinline__ void warp_deposit(float (*red)[36], bool live, int t0
           acc = fmaf(x[r], m[r], acc);
           if ((e4 >> (r - 4 * g4)) & 1u) {
             const int tr = __shfl_sync(0xffffffffu, key, 16 * h + r);
-            if (add_here && tr >= 0) tile_add<EXACT, 4 * T * T * T>(tile, qv * T * T * T + tr + off, acc, err);
+            if (add_here && tr >= 0) tile_add<EXACT, 4 * T * T * T>(tile, qv * T * T * T + tr + off, acc, bad);
             acc = 0.0f;
           }
         }
@@ -223,7 +223,7 @@ __device__ __forceinline__ void warp_deposit(float (*red)[36], bool live, int t0
     }
   }
   const int tr = __shfl_sync(0xffffffffu, key, 31);  // the run that ends at the last particle
-  if (add_here && tr >= 0) tile_add<EXACT, 4 * T * T * T>(tile, qv * T * T * T + tr + off, acc, err);
+  if (add_here && tr >= 0) tile_add<EXACT, 4 * T * T * T>(tile, qv * T * T * T + tr + off, acc, bad);
   if (MOVERS) {
     unsigned mv = __ballot_sync(0xffffffffu, live && mover);
     if (mv) {
@@ -238,7 +238,7 @@ __device__ __forceinline__ void warp_deposit(float (*red)[36], bool live, int t0
         mv &= mv - 1;
         const int tm = __shfl_sync(0xffffffffu, t0, m);
         if (add_here)
-          tile_add<EXACT, 4 * T * T * T>(tile, qv * T * T * T + tm + off, red[cv][m] * red[8 + qv][m], err);
+          tile_add<EXACT, 4 * T * T * T>(tile, qv * T * T * T + tm + off, red[cv][m] * red[8 + qv][m], bad);
       }
     }
   }
@@ -330,6 +330,7 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
   if (threadIdx.x == 0)
     for (int k = 0; k < NS - 1 && k < nchunk; ++k) issue(k);
   unsigned n_chex = 0;
+  unsigned bad = 0;  // EXACT: a run sum beyond the fixed-point range
   // warp-uniform trip count: every lane takes part in the deposit reduction
   for (int kc = 0; kc < nchunk; ++kc) {
     const int u = kc % NS;
@@ -501,7 +502,7 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
         qdv[3] = qw * dvz;
       }
     }
-    warp_deposit<PASS != 2, T, PASS == 3, EXACT>(s_red[warp], live, t0, w8, qdv, s_dep, err, lane, t0o, mover);
+    warp_deposit<PASS != 2, T, PASS == 3, EXACT>(s_red[warp], live, t0, w8, qdv, s_dep, bad, lane, t0o, mover);
     if (PASS == 3 && dirrank) {
       // stable ranks per (key, direction): the warps of the CTA take their
       // turn in order, each adding its particles after the earlier ones
@@ -520,6 +521,7 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
       }
     }
   }
+  if (EXACT && bad) set_err(err, KERR_RANGE);
   if (CHEX) {
     for (int o = 16; o > 0; o >>= 1) n_chex += __shfl_down_sync(0xffffffffu, n_chex, o);
     if (lane == 0 && n_chex) atomicAdd(sprm.chex_count, (unsigned long long)n_chex);
