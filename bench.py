@@ -299,8 +299,8 @@ def run_reference(args):
 def train_surrogate(args, base):
     """The learned field surrogate, trained on pairs that the plain subcycles
     produce in randomized runs (swap_gb300.surrogate_data: upstream speed
-    1-6 v_A, beta 0.1-2, open or periodic x, with or without a neutral cloud
-    of radius 2-10 cells) of a box of
+    1-6 v_A, beta 0.1-2, open x, a neutral cloud of radius 2-10 cells) of a
+    box of
     --sur-cells cells that keeps the workload's B0, ion step, subcycles and
     particles per cell.  Returns the network and what the training did."""
     from swap_gb300.hybrid import Surrogate
@@ -319,7 +319,7 @@ def train_surrogate(args, base):
                        "predicts the subcycles' mean E minus the plain E at the step's start",
             "training": f"{args.sur_runs} randomized runs of {cells[0]}x{cells[1]}x{cells[2]} cells at "
                         f"{base.ppc} ppc, {args.sur_pairs} pairs each (upstream speed 1-6 v_A, beta 0.1-2, "
-                        f"open or periodic x, with or without a cloud of radius 2-10 cells)",
+                        f"open x, cloud radius 2-10 cells)",
             "pairs": net.samples(), "collect_s": t_collect, "train_epochs": args.sur_epochs, "train_s": t_train,
             "loss_before": l0, "train_loss": loss}
     return net, info

@@ -285,7 +285,10 @@ int swap_checkpoint_read(swap_ctx* ctx, const char* path);
  * rate).  The sources and sinks of swap_set_sources apply, with new ions
  * drawn as in the FP64 path and charge exchange drawn per sorted ion.  Needs a uniform grid with
  * 8..1024 physical cells per axis in multiples of 4, a uniform b0, at most 16
- * (mrat, beta_p) species, and |v|*dt < dx per axis (SWAP_EMOVE otherwise).
+ * (mrat, beta_p) species.  An ion that moves more than one cell per axis in
+ * a step takes a slower path (listed by pass 3, deposited and sorted apart,
+ * at most 65536 per step); a half move that spans the grid less two cells,
+ * or more such ions, gives SWAP_EMOVE.
  * begin converts the bound FP64 state; end writes it back into the bound
  * arrays' device mirrors, with the particles in cell-sorted order. */
 int swap_f32_begin(swap_ctx* ctx);
@@ -294,6 +297,9 @@ int swap_f32_end(swap_ctx* ctx);
 int swap_f32_energy(swap_ctx* ctx, double out[4]);
 /* Ions in the FP32 state (sources and sinks change it step by step). */
 int swap_f32_count(swap_ctx* ctx, int64_t* n);
+/* Ions that moved more than one cell per axis in a step and took the slower
+ * path, summed since swap_f32_begin. */
+int swap_f32_far_movers(swap_ctx* ctx, int64_t* n);
 /* Where each sort key's ions start in the FP32 state's sorted order:
  * starts[0..nkeys], nkeys = (cells/4 per axis, multiplied) * 64, key =
  * brick * 64 + cell in the brick (x fastest, bricks x fastest), so key q

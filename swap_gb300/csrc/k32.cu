@@ -36,7 +36,9 @@ __device__ __forceinline__ void set_err(int* err, int code) {
   if (err) atomicCAS(err, 0, code);
 }
 
-constexpr uint32_t DR_BAD = 0xffffffffu, DR_DEAD = 0xfffffffeu;  // dirrank of unsorted ions
+// dirrank of ions the 27-direction sort does not place: a failed move,
+// removed, and moved more than one cell (placed from the far list)
+constexpr uint32_t DR_BAD = 0xffffffffu, DR_DEAD = 0xfffffffeu, DR_FAR = 0xfffffffdu;
 
 __device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
@@ -83,10 +85,11 @@ __host__ __device__ __forceinline__ long long n_int(const G32& g) { return (long
 // Move one axis of a (cell, offset) position by d cells.  upper_closed:
 // offsets in (0,1] (the '>' cell search of x and z, gutsp.f:1396-1412);
 // otherwise [0,1) (the floor of y, gutsp.f:1404).  Periodic in the cell
-// index (gutsp.f:490-510) when wrap; otherwise the cell may leave [0, n).
-// Returns false on a move of more than two cells.
+// index (gutsp.f:490-510, one wrap) when wrap; otherwise the cell may leave
+// [0, n).  Returns false on a move that is not finite or spans n - 2 cells
+// or more (one wrap then always lands in [0, n)).
 __device__ __forceinline__ bool move_axis(int& c, float& o, float d, int n, bool upper_closed, bool wrap = true) {
-  if (!(fabsf(d) < 2.0f)) return false;
+  if (!(fabsf(d) < (float)(n - 2))) return false;
   o += d;
   // carry whole cells: (0,1] keeps o = 1 in the cell, [0,1) moves it up
   const float k = upper_closed ? ceilf(o) - 1.0f : floorf(o);
@@ -155,6 +158,13 @@ __device__ __forceinline__ int dir_index(int dx, int dy, int dz) { return (dx + 
 constexpr double FIX_INV = 1.0 / 4294967296.0;  // 2^-32
 constexpr float FIX_MAX = 32768.0f;             // 2^15
 constexpr long long FIX_MAX_IONS = 65535;       // ions per brick
+
+// x in units of 2^-32 as the tile holds it: floor(x * 2^16) * 2^16 plus the
+// rounded rest (the same two conversions as tile_add).
+__device__ __forceinline__ long long to_fixed(float x) {
+  const float xs = x * 65536.0f, fh = floorf(xs);
+  return (long long)__float2int_rn(fh) * 65536LL + (long long)__float2uint_rn((xs - fh) * 65536.0f);
+}
 
 template <bool EXACT, int NT>
 __device__ __forceinline__ void tile_add(void* tile, int i, float x, unsigned& bad) {
@@ -261,7 +271,7 @@ template <int PASS, bool CHEX = false, bool EXACT = true>
 __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Part p, Species sp, StepParams sprm,
                                               const int64_t* __restrict__ start, const float4* __restrict__ kit,
                                               void* __restrict__ partial, uint32_t* __restrict__ dirrank,
-                                              uint16_t* __restrict__ dep, int* err) {
+                                              uint16_t* __restrict__ dep, int* err, FarList far) {
   // the chunk's particles, copied in by the bulk-copy engine (double-buffered):
   // offsets and v, plus vp1 in P1; cell words; species bytes
   constexpr int NF = PASS == 1 ? 9 : 6, NS = PASS_STAGES;
@@ -361,6 +371,7 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
     int t0o = -1;       // P3: tile index of the cell before the move
     bool mover = false;  // P3: deposits in another cell than its own
     int grp = -1;  // P3: local key * NDIR + direction for the sort, -1 when not sorted
+    bool far_ion = false;  // P3: moved more than one cell: placed through the far list
     float w8[8], qdv[4];
     if (live) {
       const bool fresh = (c & CELL_FRESH) != 0;
@@ -472,15 +483,33 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
             p.ox[l] = ox; p.oy[l] = oy; p.oz[l] = oz;
             const int sx = step_cell(ci2, c0x + (kl & 3), g.ncx), sy = step_cell(cj2, c0y + ((kl >> 2) & 3), g.ncy),
                       sz = step_cell(ck2, c0z + (kl >> 4), g.ncz);
-            if (sx < -1 || sx > 1 || sy < -1 || sy > 1 || sz < -1 || sz > 1) {
-              set_err(err, KERR_MOVE);
-              if (dirrank) dirrank[l] = DR_BAD;
-            } else {
+            if (sx < -1 || sx > 1 || sy < -1 || sy > 1 || sz < -1 || sz > 1)
+              far_ion = true;
+            else
               grp = kl * NDIR + dir_index(sx, sy, sz);
-            }
           }
           ox = dox; oy = doy; oz = doz;  // the deposit uses the maind.f:408 position
           if (out1) live = false;
+          // a deposit position outside the tile's window also takes the far path
+          if (live && (rx < -1 || rx > 4 || ry < -1 || ry > 4 || rz < -1 || rz > 4)) far_ion = true;
+          if (far_ion) {
+            const int slot = far.n ? atomicAdd(far.n, 1) : FAR_CAP;
+            if (slot < FAR_CAP) {
+              far.idx[slot] = l;
+              far.key[slot] = out2 ? -1LL : key_of(g, ci2, cj2, ck2);
+              far.dcell[slot] = live ? pk(ci, cj, ck) : -1;
+              far.o[slot] = ox; far.o[FAR_CAP + slot] = oy; far.o[2 * FAR_CAP + slot] = oz;
+              far.q[slot] = qw; far.q[FAR_CAP + slot] = qw * dvx;
+              far.q[2 * FAR_CAP + slot] = qw * dvy; far.q[3 * FAR_CAP + slot] = qw * dvz;
+              atomicAdd(far.total, 1ULL);
+              if (!out2 && dirrank) dirrank[l] = DR_FAR;
+            } else {
+              set_err(err, KERR_MOVE);
+              if (!out2 && dirrank) dirrank[l] = DR_BAD;
+            }
+            grp = -1;
+            live = false;  // neither in the tile nor in the ranks
+          }
         }
       }
       const bool inside = PASS == 3 ? !(rx < -1 || rx > 4 || ry < -1 || ry > 4 || rz < -1 || rz > 4)
@@ -1247,7 +1276,7 @@ __global__ void k_sort_scatter(G32 g, long long N, long long cap, const int32_t*
   GSTRIDE(l, N) {
     const int32_t c = cell[l];
     const uint32_t dr = dirrank[l];
-    if (dr == DR_DEAD) continue;
+    if (dr == DR_DEAD || dr == DR_FAR) continue;
     // every source field is read before the first store: the source and
     // destination buffers are distinct, and loading them together keeps the
     // ion's reads in flight at once instead of one per store
@@ -1591,21 +1620,24 @@ __global__ void k_energy_f(G32 g, const double* __restrict__ b0, const float* __
 template <int PASS, bool CHEX, bool EXACT>
 cudaError_t launch_pass(unsigned grid, cudaStream_t st, const G32& g, const Part& p, const Species& sp,
                         const StepParams& s, const int64_t* start, const float4* kit, void* partial,
-                        uint32_t* dirrank, uint16_t* dep, int* err) {
+                        uint32_t* dirrank, uint16_t* dep, int* err, const FarList& far) {
   static std::once_flag once;
   std::call_once(once, [] {
     cudaFuncSetAttribute(k_pass<PASS, CHEX, EXACT>, cudaFuncAttributePreferredSharedMemoryCarveout,
                          cudaSharedmemCarveoutMaxShared);
   });
-  k_pass<PASS, CHEX, EXACT><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, partial, dirrank, dep, err);
+  k_pass<PASS, CHEX, EXACT><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, partial, dirrank, dep, err, far);
   return cudaGetLastError();
 }
 
 cudaError_t pass(int which, const G32& g, const Part& p, const Species& sp, const StepParams& s, const int64_t* start,
                  const float4* kit, void* partial, uint32_t* dirrank, uint16_t* dep, int* err, bool exact,
-                 cudaStream_t st) {
+                 cudaStream_t st, const FarList* far) {
   const unsigned grid = (unsigned)g.nbricks;
-#define PASS_ARGS grid, st, g, p, sp, s, start, kit, partial, dirrank, dep, err
+  if (which == 3 && !far) return cudaErrorInvalidValue;
+  const FarList none{};
+  const FarList& fl = far ? *far : none;
+#define PASS_ARGS grid, st, g, p, sp, s, start, kit, partial, dirrank, dep, err, fl
   if (exact) {
     if (which == 1) return launch_pass<1, false, true>(PASS_ARGS);
     if (which == 2) return launch_pass<2, false, true>(PASS_ARGS);
@@ -1699,6 +1731,97 @@ cudaError_t courant_min(const G32& g, const float* dbt, const float* b0c, const 
   const unsigned nb = nblk(g.C) < 152u * 8u ? nblk(g.C) : 152u * 8u;
   RET((k_courant<<<nb, TPB, 0, st>>>(g, dbt, b0c, np, alpha, dx, dtn, reinterpret_cast<unsigned*>(d_min))));
 }
+// ---------------------------------------------------------------------------
+// ions that moved more than one cell in a step (pass 3's far list)
+// ---------------------------------------------------------------------------
+
+// Each listed ion's 8 corner weights times (qw, qw v) into the partial tile
+// of its deposit cell's brick, as that tile would hold a run of one ion
+// (fixed point: 64-bit integer adds, exact and order-independent).
+template <bool EXACT>
+__global__ void k_far_deposit(G32 g, FarList f, void* __restrict__ partial, int* err) {
+  const int n = min(*f.n, FAR_CAP);
+  unsigned bad = 0;
+  GSTRIDE(i, n) {
+    const int32_t c = f.dcell[i];
+    if (c < 0) continue;
+    const int ci = pk_i(c), cj = pk_j(c), ck = pk_k(c);
+    const long long b = (long long)(ci >> 2) + (long long)g.nbx * ((cj >> 2) + (long long)g.nby * (ck >> 2));
+    const int t0 = ((ci & 3) + 1) + TN * (((cj & 3) + 1) + TN * ((ck & 3) + 1));
+    const float ox = f.o[i], oy = f.o[FAR_CAP + i], oz = f.o[2 * FAR_CAP + i];
+    const float wxl = 1.0f - ox, wxu = ox, wyl = 1.0f - oy, wyu = oy, wzl = 1.0f - oz, wzu = oz;
+    float q[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) q[m] = f.q[m * FAR_CAP + i];
+#pragma unroll
+    for (int cc = 0; cc < 8; ++cc) {
+      const float w = ((cc & 1) ? wxu : wxl) * (((cc >> 1) & 1) ? wyu : wyl) * ((cc >> 2) ? wzu : wzl);
+      const int t = t0 + (cc & 1) + TN * (((cc >> 1) & 1) + TN * (cc >> 2));
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        const float x = w * q[m];
+        const long long at = b * (4 * TNODES) + m * TNODES + t;
+        if (EXACT) {
+          bad |= fabsf(x) < FIX_MAX ? 0u : 1u;
+          atomicAdd(static_cast<unsigned long long*>(partial) + at, (unsigned long long)to_fixed(x));
+        } else {
+          atomicAdd(static_cast<float*>(partial) + at, x);
+        }
+      }
+    }
+  }
+  if (bad) set_err(err, KERR_RANGE);
+}
+
+__global__ void k_far_count(FarList f, int64_t* __restrict__ count) {
+  const int n = min(*f.n, FAR_CAP);
+  GSTRIDE(i, n) {
+    const long long X = f.key[i];
+    if (X >= 0) atomicAdd(reinterpret_cast<unsigned long long*>(count + X), 1ULL);
+  }
+}
+
+// Each survivor's rank among the listed arrivals of its key by array index
+// (a scan of the whole list: the list is short, and this keeps the order
+// deterministic), then a copy after the near arrivals.
+__global__ void k_far_scatter(G32 g, FarList f, const int32_t* __restrict__ ncount,
+                              const int64_t* __restrict__ start_new, Part s, Part d, long long cap, int* err) {
+  const int n = min(*f.n, FAR_CAP);
+  GSTRIDE(i, n) {
+    const long long X = f.key[i];
+    if (X < 0) continue;
+    const long long li = f.idx[i];
+    int cnt = 0, r = 0;
+    for (int j = 0; j < n; ++j)
+      if (f.key[j] == X) {
+        ++cnt;
+        r += f.idx[j] < li ? 1 : 0;
+      }
+    const long long dst = start_new[X + 1] - (ncount ? ncount[X] : 0) - cnt + r;
+    if (dst < 0 || dst >= cap) {
+      set_err(err, KERR_CAPACITY);
+      continue;
+    }
+    d.cell[dst] = s.cell[li];
+    d.ox[dst] = s.ox[li]; d.oy[dst] = s.oy[li]; d.oz[dst] = s.oz[li];
+    d.vx[dst] = s.vx[li]; d.vy[dst] = s.vy[li]; d.vz[dst] = s.vz[li];
+    d.wx[dst] = s.wx[li]; d.wy[dst] = s.wy[li]; d.wz[dst] = s.wz[li];
+    if (s.sp) d.sp[dst] = s.sp[li];
+  }
+}
+
+cudaError_t far_deposit(const G32& g, const FarList& far, void* partial, bool exact, int* err, cudaStream_t st) {
+  if (exact) RET((k_far_deposit<true><<<64, TPB, 0, st>>>(g, far, partial, err)));
+  RET((k_far_deposit<false><<<64, TPB, 0, st>>>(g, far, partial, err)));
+}
+cudaError_t far_count(const FarList& far, int64_t* count, cudaStream_t st) {
+  RET((k_far_count<<<64, TPB, 0, st>>>(far, count)));
+}
+cudaError_t far_scatter(const G32& g, const FarList& far, const int32_t* ncount, const int64_t* start_new,
+                        const Part& src, const Part& dst, long long cap, int* err, cudaStream_t st) {
+  RET((k_far_scatter<<<FAR_CAP / TPB, TPB, 0, st>>>(g, far, ncount, start_new, src, dst, cap, err)));
+}
+
 cudaError_t sort_prep(const G32& g, const int64_t* start, const int32_t* cell, uint32_t* dirrank, uint16_t* dep,
                       int* err, cudaStream_t st) {
   const long long warps = g.nkeys;

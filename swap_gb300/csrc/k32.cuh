@@ -76,6 +76,23 @@ struct StepParams {
   uint32_t wait_polls;               // polls of a chunk's copy before a pass gives up
 };
 
+// Ions that moved more than one cell per axis in one step (|v| dt > dx: the
+// reference handles any move, gutsp.f:454-570, 1378-1435) leave the fast
+// path: pass 3 lists them, far_deposit adds their moments to the brick
+// partials, and the sort places them after the near arrivals of their new
+// key, in array order.  At most FAR_CAP per step; a larger number, or a
+// half move of more than the grid's extent less two cells, fails the step.
+constexpr int FAR_CAP = 1 << 16;
+struct FarList {
+  long long* idx;             // the ion's index in the pass's buffer
+  long long* key;             // its new key; -1 when it left the grid
+  int32_t* dcell;             // packed cell of its deposit position; -1: none
+  float* o;                   // deposit offsets, [3][FAR_CAP]
+  float* q;                   // qw and qw * v, [4][FAR_CAP]
+  int* n;                     // entries this step (above FAR_CAP: the step fails)
+  unsigned long long* total;  // ions that took this path since the state began
+};
+
 __host__ __device__ __forceinline__ int pk_i(int32_t c) { return c & 1023; }
 __host__ __device__ __forceinline__ int pk_j(int32_t c) { return (c >> 10) & 1023; }
 __host__ __device__ __forceinline__ int pk_k(int32_t c) { return (c >> 20) & 1023; }
@@ -135,7 +152,8 @@ __device__ __forceinline__ float offset_in_cell(double x, double q1, double d, i
 //     up there (maind.f:404-413), the second half move (maind.f:479),
 //     outflow and res_chex; writes each particle's sort direction and rank
 //     (dirrank) and the per-key direction counts (dep, direction-major:
-//     dep[dir * nkeys + key]) when those are given.
+//     dep[dir * nkeys + key]) when those are given, and lists the ions that
+//     moved more than one cell in `far` (required for pass 3).
 // Moment sums (exact): each warp sums a cell's ions in FP32, and those run
 // sums go into the brick tile (two 32-bit words per node), then the brick
 // partials (64-bit), as fixed-point integers in units of 2^-32: exact and
@@ -144,7 +162,15 @@ __device__ __forceinline__ float offset_in_cell(double x, double q1, double d, i
 // measure what the exact sums gain).  partial: 8 bytes per tile entry.
 cudaError_t pass(int which, const G32& g, const Part& p, const Species& sp, const StepParams& sprm,
                  const int64_t* start, const float4* kit, void* partial, uint32_t* dirrank, uint16_t* dep, int* err,
-                 bool exact, cudaStream_t st);
+                 bool exact, cudaStream_t st, const FarList* far = nullptr);
+// The moments of pass 3's far list into the brick partials (pass 3's tiles).
+cudaError_t far_deposit(const G32& g, const FarList& far, void* partial, bool exact, int* err, cudaStream_t st);
+// Add the far list's arrivals to the per-key counts (before the scan).
+cudaError_t far_count(const FarList& far, int64_t* count, cudaStream_t st);
+// The far list's survivors to start_new[X+1] - ncount[X] - (far arrivals of
+// X) + (their rank by array index); ncount may be null.
+cudaError_t far_scatter(const G32& g, const FarList& far, const int32_t* ncount, const int64_t* start_new,
+                        const Part& src, const Part& dst, long long cap, int* err, cudaStream_t st);
 // Sum the brick partial tiles into np and S (interior nodes, (nx,ny,nz) layout).
 // pass: the pass (1-3) whose tiles `partial` holds
 cudaError_t node_sum(const G32& g, int pass, const void* partial, int nq, bool exact, float* np, float* S,

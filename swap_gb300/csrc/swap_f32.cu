@@ -34,6 +34,7 @@ struct F32State {
   uint16_t* dep = nullptr;
   uint16_t* pre = nullptr;
   void* partial = nullptr;  // brick partial tiles, 8 bytes per entry (fixed point or FP32)
+  FarList far{};            // pass 3's ions that moved more than one cell
   bool exact = true;        // exact moment sums (swap_f32_set_moment_sums)
   float4* kit = nullptr;
   float *np = nullptr, *S = nullptr, *up = nullptr, *aj = nullptr, *ct = nullptr, *E = nullptr, *nu = nullptr;
@@ -150,7 +151,9 @@ static int check_err(swap_ctx* c) {
     if (herr == 3) return c->fail(SWAP_EDOMAIN, "a particle lies outside the grid");
     if (herr == 4) return c->fail(SWAP_ECAPACITY, "Ni_max exceeded by new ions");
     if (herr == 7)
-      return c->fail(SWAP_EMOVE, "a particle moved more than one cell per axis since the last sort (|v| dt > dx)");
+      return c->fail(SWAP_EMOVE,
+                     "a particle's half move spanned the grid less two cells, or more than 65536 particles "
+                     "moved more than one cell per axis in one step");
     if (herr == 8) return c->fail(SWAP_EWAIT, "a particle chunk copy did not complete within its wait limit");
     if (herr == 10)
       return c->fail(SWAP_ENONFINITE,
@@ -329,6 +332,13 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
       return c->fail(SWAP_ECUDA, "sort order table");
   }
   s->partial = s->alloc<unsigned long long>((std::size_t)g.nbricks * 4 * TNODES);
+  s->far.idx = s->alloc<long long>(FAR_CAP);
+  s->far.key = s->alloc<long long>(FAR_CAP);
+  s->far.dcell = s->alloc<int32_t>(FAR_CAP);
+  s->far.o = s->alloc<float>(3 * (std::size_t)FAR_CAP);
+  s->far.q = s->alloc<float>(4 * (std::size_t)FAR_CAP);
+  s->far.n = s->alloc<int>(1);
+  s->far.total = s->alloc<unsigned long long>(1);
   s->kit = s->alloc<float4>(2 * (std::size_t)ncx * ncy * ncz);
   // np and the velocity sums S in one block (S 128-byte aligned after np), so
   // that one exchange covers a deposit's node sums.  Zeroed once: the gap and
@@ -354,8 +364,11 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
   s->acc = s->alloc<double>(4);
   if (!s->start || !s->start_new || !s->count || !s->sums || !s->dirrank || !s->dep || !s->pre || !s->partial || !s->kit ||
       !s->np || !s->S || !s->up || !s->aj || !s->ct || !s->E || !s->nu || !s->db1 || !s->db1p2 || !s->dbtp1 ||
-      !s->b0 || !s->b1.l || !s->b12.l || !s->b1p2.l || !s->b0c || !s->d_min || !s->acc || !s->dtn)
+      !s->b0 || !s->b1.l || !s->b12.l || !s->b1p2.l || !s->b0c || !s->d_min || !s->acc || !s->dtn || !s->far.idx ||
+      !s->far.key || !s->far.dcell || !s->far.o || !s->far.q || !s->far.n || !s->far.total)
     return c->fail(SWAP_ECUDA, "FP32 grid allocation failed");
+  CU(cudaMemsetAsync(s->far.n, 0, sizeof(int), c->st));
+  CU(cudaMemsetAsync(s->far.total, 0, sizeof(unsigned long long), c->st));
   CU(cudaMemsetAsync(s->np, 0, C * sizeof(float), c->st));
   for (void* p : {(void*)s->S, (void*)s->up, (void*)s->aj, (void*)s->ct, (void*)s->E})
     CU(cudaMemsetAsync(p, 0, 3 * C * sizeof(float), c->st));
@@ -503,8 +516,12 @@ static int sort_step(swap_ctx* c, F32State* s, long long src_step, bool prepared
   if (!prepared) KL("f32_sort_prep", sort_prep(g, s->start, a.cell, s->dirrank, s->dep, c->d_err, c->st));
   KL("f32_sort_count", sort_count(g, s->dep, staged ? s->stage.ncount : nullptr, s->order, s->count, s->pre,
                                   c->d_err, c->st));
+  if (prepared) KL("f32_far_count", far_count(s->far, s->count, c->st));
   KLN("f32_sort_scan", 3, scan_exclusive(s->count, s->start_new, g.nkeys, s->sums, c->st));
   KL("f32_sort_scatter", sort_scatter(g, s->N, cap, a.cell, s->dirrank, s->pre, s->start_new, a, b, c->d_err, c->st));
+  if (prepared)
+    KL("f32_far_scatter", far_scatter(g, s->far, staged ? s->stage.ncount : nullptr, s->start_new, a, b, cap,
+                                      c->d_err, c->st));
   if (staged)
     KL("f32_new_scatter", new_scatter(g, n_host, n_dev, n_max, s->stage.part, s->stage.key, s->stage.rank,
                                       s->stage.ncount, s->start_new, b, cap, c->d_err, c->st));
@@ -665,8 +682,10 @@ static int one_step(swap_ctx* c, F32State* s) {
   TRY(finish_deposit(c, s, 2, 3));
   KL("f32_kit", build_kit(g, s->aj, s->up, s->db1, s->b0c, s->kit, c->st));       // :404
   // :404-413, the final half move of :479 and res_chex; prepares the sort
+  CU(cudaMemsetAsync(s->far.n, 0, sizeof(int), c->st));
   KL("f32_P3", pass(3, g, p, s->sp, sp, s->start, s->kit, s->partial, s->dirrank, s->dep, c->d_err, s->exact,
-                    c->st));
+                    c->st, &s->far));
+  KL("f32_far_deposit", far_deposit(g, s->far, s->partial, s->exact, c->d_err, c->st));
   {  // pass 3 wrote the new v into the vp1 arrays and left the old v (the new vp1) in place
     Part& q = s->buf[s->cur];
     std::swap(q.vx, q.wx);
@@ -752,6 +771,17 @@ extern "C" int swap_f32_count(swap_ctx* c, int64_t* n) {
   // after swap_f32_end the state's ions are those written back (the buffer
   // still holds the next step's staged ions)
   *n = s->ended ? s->n_out : s->N;
+  return SWAP_OK;
+}
+
+extern "C" int swap_f32_far_movers(swap_ctx* c, int64_t* n) {
+  if (!c || !n) return SWAP_EINVAL;
+  F32State* s = f32(c);
+  if (!s) return c->fail(SWAP_EINVAL, "swap_f32_begin has not been called");
+  unsigned long long h = 0;
+  CU(cudaMemcpyAsync(&h, s->far.total, sizeof(h), cudaMemcpyDeviceToHost, c->st));
+  CU(cudaStreamSynchronize(c->st));
+  *n = (int64_t)h;
   return SWAP_OK;
 }
 

@@ -443,6 +443,12 @@ class Hybrid:
         self._check(self.lib.swap_f32_key_starts(self.ctx, out.ctypes.data_as(abi.c_int64_p), nk + 1))
         return out
 
+    def f32_far_movers(self) -> int:
+        """Ions that moved more than one cell per axis in a step since f32_begin."""
+        n = C.c_int64()
+        self._check(self.lib.swap_f32_far_movers(self.ctx, C.byref(n)))
+        return n.value
+
     def f32_energy(self):
         out = np.zeros(4)
         self._check(self.lib.swap_f32_energy(self.ctx, abi.dptr(out)))
