@@ -359,10 +359,12 @@ int swap_load_maxwellian_host(const swap_dims* dims, const swap_coords* coords, 
  *   - It allocates nothing.  Its scratch is one file-scope device array of
  *     SWAP_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds
  *     until the process exits.
+ *   - No call can be captured in a CUDA graph: each call reads its flag
+ *     back and waits for its stream.
  *   - The first call on a device resolves that array's address
- *     (cudaGetSymbolAddress) and keeps it; make the first call before any
- *     stream capture, and make no call on a device after cudaDeviceReset
- *     there.  After an error the entry waits for its stream before returning.
+ *     (cudaGetSymbolAddress) and keeps it; make no call on a device after
+ *     cudaDeviceReset there.  After an error the entry waits for its stream
+ *     before returning.
  *   - All calls share the array and each call clears the part it uses first;
  *     calls that overlap on the GPU race, so serialize them.
  *   - More than SWAP_NOALLOC_MAX_NODES nodes, or more than
@@ -392,12 +394,13 @@ int swap_conv3_check(int32_t nx, int32_t ny, int32_t nz, int32_t cin, int32_t co
                      const float* bias, void* Y, float* Yf, int32_t gelu);
 
 /* ---- the learned field-subcycle surrogate (FP32 form) ----
- * A 3D convolutional network (4 periodic 3x3x3 layers, 8 -> 32 -> 32 -> 32
- * -> 3 channels, GELU; BF16 weights and activations, FP32 accumulation on
- * the tensor cores) maps the state at the start of the field subcycles (B,
- * u_p, n_p, p_e = n_p per node) to the step's mean corrector E; B then
- * advances as B - dt curl E, so div B stays where it was.  It is trained on
- * pairs the plain subcycles of swap_surrogate_collect produce, with Adam.
+ * A 3D convolutional network (swap_surrogate_layers periodic 3x3x3 layers,
+ * 11 -> 32 -> ... -> 32 -> 3 channels, GELU; BF16 weights and activations,
+ * FP32 accumulation on the tensor cores) maps the state at the start of the
+ * field subcycles (B, u_p, n_p, p_e, and E0, the plain E there) to the
+ * step's mean corrector E minus E0; B then advances as B - dt curl E, so
+ * div B stays where it was.  It is trained on pairs the plain subcycles of
+ * swap_surrogate_collect produce, with Adam.
  * Attached to a context, it replaces the subcycles; every judge_every-th
  * step both run, the plain result is kept, and a B rel-L2 difference above
  * bound switches the network off until a judged step passes. */
@@ -410,22 +413,29 @@ const char* swap_surrogate_last_error(const swap_surrogate* net);
 int swap_surrogate_collect(swap_surrogate* net, swap_ctx* ctx, int32_t nsteps);
 int swap_surrogate_samples(swap_surrogate* net, int32_t* n);
 /* epochs of Adam over the pairs; loss = mean squared normalised E error of
- * the last epoch. */
+ * the last epoch, plus curl_w * mean |curl e|^2 / kref2 when a curl weight is
+ * set (e the E error, so curl e is the B error per unit dt; kref2 = mean
+ * |curl target|^2 of the training pairs, or the value given). */
 int swap_surrogate_train(swap_surrogate* net, int32_t epochs, double lr, double* loss);
 int swap_surrogate_loss(swap_surrogate* net, double* loss);
+int swap_surrogate_set_curl_weight(swap_surrogate* net, double curl_w, double kref2);
+/* The network's depth (conv layers). */
+int swap_surrogate_layers(int32_t* n);
 int swap_surrogate_attach(swap_ctx* ctx, swap_surrogate* net, int32_t judge_every, double bound);
 /* [0] steps by the network, [1] judged steps, [2] fallbacks, [3] last judged
  * B rel-L2, [4] last judged (B - b0) rel-L2. */
 int swap_surrogate_stats(swap_ctx* ctx, double out[5]);
 /* Test access: normalisation (11 input means and stds, output scale) and
- * FP32 master weights of a layer ([27][cout][cin] with (cin, cout) = (16,32),
- * (32,32), (32,32), (32,16): padded channels zero) with its bias; get or set. */
+ * FP32 master weights of a layer ([27][cout][cin] with (cin, cout) = (16,32)
+ * for the first, (32,16) for the last and (32,32) between: padded channels
+ * zero) with its bias; get or set. */
 int swap_surrogate_norm(swap_surrogate* net, float* mean, float* stdv, float* out_mean, float* out_std,
                         int32_t set);
 int swap_surrogate_weights(swap_surrogate* net, int32_t layer, float* w, float* b, int32_t set);
 /* One forward and backward pass on device inputs [V][11] and targets [V][3]
- * of an nx*ny*nz box: loss = 0.5 mean((out - (tgt - out_mean)/out_std)^2), gradients of
- * every layer into grads as (gW0, gb0, gW1, gb1, gW2, gb2, gW3, gb3). */
+ * of an nx*ny*nz box: loss = 0.5 mean((out - (tgt - out_mean)/out_std)^2)
+ * (plus 0.5 curl_w mean |curl e|^2 / kref2 with a curl weight), gradients of
+ * every layer into grads as (gW0, gb0, gW1, gb1, ...). */
 int swap_surrogate_grads(swap_surrogate* net, int32_t nx, int32_t ny, int32_t nz, const float* vin, const float* tgt,
                          double* loss, float* grads);
 

@@ -267,11 +267,14 @@ __device__ __forceinline__ void warp_deposit(float (*red)[36], bool live, int t0
 //       res_chex after the second (maind.f:484).  It also prepares the sort:
 //       the direction of every particle's new cell from its key's cell and
 //       its rank among the particles of that key and direction, in order.
-template <int PASS, bool CHEX = false, bool EXACT = true>
+// PGRAD: the isothermal electron-pressure term in the gathered E (kitg:
+// its face gradient centred per node, as get_Ep's gradient extension).
+template <int PASS, bool CHEX = false, bool EXACT = true, bool PGRAD = false>
 __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Part p, Species sp, StepParams sprm,
                                               const int64_t* __restrict__ start, const float4* __restrict__ kit,
-                                              void* __restrict__ partial, uint32_t* __restrict__ dirrank,
-                                              uint16_t* __restrict__ dep, int* err, FarList far) {
+                                              const float4* __restrict__ kitg, void* __restrict__ partial,
+                                              uint32_t* __restrict__ dirrank, uint16_t* __restrict__ dep, int* err,
+                                              FarList far) {
   // the chunk's particles, copied in by the bulk-copy engine (double-buffered):
   // offsets and v, plus vp1 in P1; cell words; species bytes
   constexpr int NF = PASS == 1 ? 9 : 6, NS = PASS_STAGES;
@@ -286,6 +289,7 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
   constexpr int T = pass_tile(PASS), TNOD = T * T * T, O = PASS == 3 ? 1 : 0;
   __shared__ float4 s_kitA[PASS == 1 ? 1 : TNODES_IN];
   __shared__ float2 s_kitB[PASS == 1 ? 1 : TNODES_IN];
+  __shared__ float4 s_kitG[PGRAD && PASS != 1 ? TNODES_IN : 1];
   // the deposit tile per node and moment: FP32, or (EXACT) fixed point as
   // low words [4 * TNOD] then high words [4 * TNOD]
   __shared__ __align__(8) unsigned s_dep[(EXACT ? 2 : 1) * 4 * TNOD];
@@ -305,6 +309,7 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
       s_kitA[t] = kit[src];
       const float4 hi = kit[src + 1];
       s_kitB[t] = make_float2(hi.x, hi.y);
+      if (PGRAD) s_kitG[t] = kitg[src / 2];
     }
   }
   for (int t = threadIdx.x; t < (EXACT ? 2 : 1) * 4 * TNOD; t += blockDim.x) s_dep[t] = 0u;
@@ -397,7 +402,7 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
         // cannot index outside the tile: the checks below report it)
         const int gx = min(max(rx, 0), 3), gy = min(max(ry, 0), 3), gz = min(max(rz, 0), 3);
         const int tg = gx + TN_IN * (gy + TN_IN * gz);
-        float ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;
+        float ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0, qx = 0, qy = 0, qz = 0;
 #pragma unroll
         for (int cz = 0; cz < 2; ++cz)
 #pragma unroll
@@ -410,9 +415,14 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
               const float2 f1 = s_kitB[t];
               ax = fmaf(w, f0.x, ax); ay = fmaf(w, f0.y, ay); az = fmaf(w, f0.z, az);
               bx = fmaf(w, f0.w, bx); by = fmaf(w, f1.x, by); bz = fmaf(w, f1.y, bz);
+              if (PGRAD) {
+                const float4 f2 = s_kitG[t];
+                qx = fmaf(w, f2.x, qx); qy = fmaf(w, f2.y, qy); qz = fmaf(w, f2.z, qz);
+              }
             }
-        // Ep = ((aj-up) x B) * mrat (gutsp.f:260-270)
-        const float ex = (ay * bz - az * by) * mr, ey = (az * bx - ax * bz) * mr, ez = (ax * by - ay * bx) * mr;
+        // Ep = ((aj-up) x B - gradP) * mrat (gutsp.f:260-270; q: gradP, zero without PGRAD)
+        const float ex = ((ay * bz - az * by) - qx) * mr, ey = ((az * bx - ax * bz) - qy) * mr,
+                    ez = ((ax * by - ay * bx) - qz) * mr;
         // v- and the rotation of get_vplus_vminus (gutsp.f:302-397)
         const float mx = vx + hdt * ex, my = vy + hdt * ey, mz = vz + hdt * ez;
         const float Bx = bx * mr, By = by * mr, Bz = bz * mr;
@@ -681,15 +691,30 @@ __device__ __forceinline__ void e2c(const G32& g, const float* bt, int i, int j,
   e2c_o(g, bt, nid(g, i, j, k), c1, c2, c3);
 }
 
+// The isothermal electron-pressure gradient at the face of component m
+// (node o to o + e_m): grad_pe * (np(o+e_m) - np(o)) / d_m / n_face, n_face
+// the face average of np as in curlB.
+template <int m, class I = long long>
+__device__ __forceinline__ float gpe_face(const G32& g, const float* __restrict__ np, float gp, I o) {
+  const I s = m == 0 ? (I)1 : (m == 1 ? (I)g.nx : (I)g.nx * (I)g.ny);
+  const float inv = m == 0 ? g.inv_dx : (m == 1 ? g.inv_dy : g.inv_dz);
+  return gp * ((np[o + s] - np[o]) * inv) / (0.5f * (np[o] + np[o + s]));
+}
+
 // Gather kit per physical node: (ajc - upc, btc) with ajc/upc =
 // face_to_center (grid_interp.f:163-170) and btc = edge_to_center of
 // dB plus the centred b0.
 __global__ void k_kit(G32 g, const float* __restrict__ aj, const float* __restrict__ up,
-                      const float* __restrict__ dbt, const float* __restrict__ b0c, float4* __restrict__ kit) {
+                      const float* __restrict__ dbt, const float* __restrict__ b0c, const float* __restrict__ np,
+                      float gp, float4* __restrict__ kit, float4* __restrict__ kitg) {
   GSTRIDE(t, n_int(g)) {
     int i, j, k;
     interior_of(g, t, i, j, k);
     const long long C = g.C, o = nid(g, i, j, k), sx = 1, sy = g.nx, sz = (long long)g.nx * g.ny;
+    if (kitg)  // the pressure gradient centred like aj (face_to_center), for get_Ep
+      kitg[t] = make_float4(0.5f * (gpe_face<0>(g, np, gp, o) + gpe_face<0>(g, np, gp, o - sx)),
+                            0.5f * (gpe_face<1>(g, np, gp, o) + gpe_face<1>(g, np, gp, o - sy)),
+                            0.5f * (gpe_face<2>(g, np, gp, o) + gpe_face<2>(g, np, gp, o - sz)), 0.0f);
     const float ax = 0.5f * ((aj[o] - up[o]) + (aj[o - sx] - up[o - sx]));
     const float ay = 0.5f * ((aj[o + C] - up[o + C]) + (aj[o - sy + C] - up[o - sy + C]));
     const float az = 0.5f * ((aj[o + 2 * C] - up[o + 2 * C]) + (aj[o - sz + 2 * C] - up[o - sz + 2 * C]));
@@ -874,14 +899,17 @@ __global__ void __launch_bounds__(FBX * FBY) k_aj_ct(G32 g, const float* __restr
 }
 
 // Component m of E = face average of ct + nu*aj at node (i,j,k) (gutsf.f:
-// 94-96, 1082).
+// 94-96, 1082), less the electron-pressure face gradient gpf when given
+// (the isothermal extension of the commented "- gradP", gutsf.f:1083,1283).
 template <int m>
 __device__ __forceinline__ float e_o(const G32& g, const float* __restrict__ ct, const float* __restrict__ nu,
-                                     const float* __restrict__ aj, long long o) {
+                                     const float* __restrict__ aj, const float* __restrict__ gpf, long long o) {
   const long long C = g.C;
   const long long s = m == 0 ? 1 : (m == 1 ? (long long)g.nx : (long long)g.nx * g.ny);
-  return 0.5f * (ct[o + C * m] + ct[o + s + C * m]) + nu[o] * aj[o + C * m];
+  const float e = 0.5f * (ct[o + C * m] + ct[o + s + C * m]) + nu[o] * aj[o + C * m];
+  return gpf ? e - gpf[o + C * m] : e;
 }
+
 
 // Double-float arithmetic (a pair of floats carrying 48 significant bits):
 // the FP32 form accumulates B across subcycles in it, because GB300's FP64
@@ -912,7 +940,8 @@ __device__ __forceinline__ void df_sub_mul(float bh, float bl, float ch, float c
 // (the step's last corrector).
 template <bool PRED, bool WRITE_E, bool INNER>
 __device__ __forceinline__ void bstep_node(const G32& g, const float* __restrict__ ct, const float* __restrict__ nu,
-                                           const float* __restrict__ aj, const float* __restrict__ bh,
+                                           const float* __restrict__ aj, const float* __restrict__ gpf,
+                                           const float* __restrict__ bh,
                                            const float* __restrict__ bl, float ch, float cl,
                                            const float* __restrict__ b0c, float* __restrict__ oh,
                                            float* __restrict__ ol, float* __restrict__ dbo,
@@ -921,12 +950,12 @@ __device__ __forceinline__ void bstep_node(const G32& g, const float* __restrict
   const long long C = g.C, o = nid(g, i, j, k);
   const long long ox = nbr<INNER>(g, o, i, j, k, 1, 0, 0), oy = nbr<INNER>(g, o, i, j, k, 0, 1, 0),
                   oz = nbr<INNER>(g, o, i, j, k, 0, 0, 1);
-  const float e1 = e_o<0>(g, ct, nu, aj, o);
-  const float e2 = e_o<1>(g, ct, nu, aj, o);
-  const float e3 = e_o<2>(g, ct, nu, aj, o);
-  const float e1y = e_o<0>(g, ct, nu, aj, oy), e1z = e_o<0>(g, ct, nu, aj, oz);
-  const float e2x = e_o<1>(g, ct, nu, aj, ox), e2z = e_o<1>(g, ct, nu, aj, oz);
-  const float e3x = e_o<2>(g, ct, nu, aj, ox), e3y = e_o<2>(g, ct, nu, aj, oy);
+  const float e1 = e_o<0>(g, ct, nu, aj, gpf, o);
+  const float e2 = e_o<1>(g, ct, nu, aj, gpf, o);
+  const float e3 = e_o<2>(g, ct, nu, aj, gpf, o);
+  const float e1y = e_o<0>(g, ct, nu, aj, gpf, oy), e1z = e_o<0>(g, ct, nu, aj, gpf, oz);
+  const float e2x = e_o<1>(g, ct, nu, aj, gpf, ox), e2z = e_o<1>(g, ct, nu, aj, gpf, oz);
+  const float e3x = e_o<2>(g, ct, nu, aj, gpf, ox), e3y = e_o<2>(g, ct, nu, aj, gpf, oy);
   const float ce[3] = {(e3y - e3) * g.inv_dy + (e2 - e2z) * g.inv_dz,
                        (e3 - e3x) * g.inv_dx + (e1z - e1) * g.inv_dz,
                        (e1 - e1y) * g.inv_dy + (e2x - e2) * g.inv_dx};
@@ -960,6 +989,7 @@ __device__ __forceinline__ void bstep_node(const G32& g, const float* __restrict
 template <bool PRED, bool WRITE_E>
 __global__ void __launch_bounds__(FBX * FBY) k_bstep(G32 g, const float* __restrict__ ct,
                                                      const float* __restrict__ nu, const float* __restrict__ aj,
+                                                     const float* __restrict__ gpf,
                                                      const float* __restrict__ bh, const float* __restrict__ bl,
                                                      float ch, float cl, const float* __restrict__ b0c,
                                                      float* __restrict__ oh, float* __restrict__ ol,
@@ -968,10 +998,11 @@ __global__ void __launch_bounds__(FBX * FBY) k_bstep(G32 g, const float* __restr
                                                      float* __restrict__ e_acc) {
   FIELD_NODE(i, j, k);
   if (inner_node(g, i, j, k))
-    bstep_node<PRED, WRITE_E, true>(g, ct, nu, aj, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E, e_acc, i, j, k);
+    bstep_node<PRED, WRITE_E, true>(g, ct, nu, aj, gpf, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E, e_acc, i, j,
+                                    k);
   else
-    bstep_node<PRED, WRITE_E, false>(g, ct, nu, aj, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E, e_acc, i, j,
-                                     k);
+    bstep_node<PRED, WRITE_E, false>(g, ct, nu, aj, gpf, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E, e_acc, i,
+                                     j, k);
 }
 
 // B_new = base - coef * curl E for a given E (with ghost images), in
@@ -1071,7 +1102,8 @@ __global__ void k_judge(G32 g, const float* __restrict__ ah, const float* __rest
 __global__ void k_grid_to_voxels(G32 g, const float* __restrict__ db, const float* __restrict__ b0c,
                                  const float* __restrict__ up, const float* __restrict__ np, float te,
                                  const float* __restrict__ ct, const float* __restrict__ aj,
-                                 const float* __restrict__ nu, float* __restrict__ out) {
+                                 const float* __restrict__ nu, const float* __restrict__ gpf,
+                                 float* __restrict__ out) {
   GSTRIDE(v, n_int(g)) {
     int i, j, k;
     interior_of(g, v, i, j, k);
@@ -1085,9 +1117,9 @@ __global__ void k_grid_to_voxels(G32 g, const float* __restrict__ db, const floa
     r[5] = up[o + 2 * C];
     r[6] = np[o];
     r[7] = te * np[o];
-    r[8] = ct ? e_o<0>(g, ct, nu, aj, o) : 0.0f;
-    r[9] = ct ? e_o<1>(g, ct, nu, aj, o) : 0.0f;
-    r[10] = ct ? e_o<2>(g, ct, nu, aj, o) : 0.0f;
+    r[8] = ct ? e_o<0>(g, ct, nu, aj, gpf, o) : 0.0f;
+    r[9] = ct ? e_o<1>(g, ct, nu, aj, gpf, o) : 0.0f;
+    r[10] = ct ? e_o<2>(g, ct, nu, aj, gpf, o) : 0.0f;
   }
 }
 
@@ -1617,27 +1649,34 @@ __global__ void k_energy_f(G32 g, const double* __restrict__ b0, const float* __
 // One pass launch; the first launch of each form asks for the largest
 // shared-memory carve-out, so that the occupancy the launch bounds name (7 or
 // 8 CTAs per SM) fits the CTAs' shared tiles.
-template <int PASS, bool CHEX, bool EXACT>
+template <int PASS, bool CHEX, bool EXACT, bool PGRAD = false>
 cudaError_t launch_pass(unsigned grid, cudaStream_t st, const G32& g, const Part& p, const Species& sp,
-                        const StepParams& s, const int64_t* start, const float4* kit, void* partial,
-                        uint32_t* dirrank, uint16_t* dep, int* err, const FarList& far) {
+                        const StepParams& s, const int64_t* start, const float4* kit, const float4* kitg,
+                        void* partial, uint32_t* dirrank, uint16_t* dep, int* err, const FarList& far) {
   static std::once_flag once;
   std::call_once(once, [] {
-    cudaFuncSetAttribute(k_pass<PASS, CHEX, EXACT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+    cudaFuncSetAttribute(k_pass<PASS, CHEX, EXACT, PGRAD>, cudaFuncAttributePreferredSharedMemoryCarveout,
                          cudaSharedmemCarveoutMaxShared);
   });
-  k_pass<PASS, CHEX, EXACT><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, partial, dirrank, dep, err, far);
+  k_pass<PASS, CHEX, EXACT, PGRAD><<<grid, TPB_PASS, 0, st>>>(g, p, sp, s, start, kit, kitg, partial, dirrank, dep,
+                                                               err, far);
   return cudaGetLastError();
 }
 
 cudaError_t pass(int which, const G32& g, const Part& p, const Species& sp, const StepParams& s, const int64_t* start,
                  const float4* kit, void* partial, uint32_t* dirrank, uint16_t* dep, int* err, bool exact,
-                 cudaStream_t st, const FarList* far) {
+                 cudaStream_t st, const FarList* far, const float4* kitg) {
   const unsigned grid = (unsigned)g.nbricks;
   if (which == 3 && !far) return cudaErrorInvalidValue;
   const FarList none{};
   const FarList& fl = far ? *far : none;
-#define PASS_ARGS grid, st, g, p, sp, s, start, kit, partial, dirrank, dep, err, fl
+#define PASS_ARGS grid, st, g, p, sp, s, start, kit, kitg, partial, dirrank, dep, err, fl
+  if (kitg && which != 1) {  // the electron-pressure term: exact moment sums only
+    if (!exact) return cudaErrorInvalidValue;
+    if (which == 2) return launch_pass<2, false, true, true>(PASS_ARGS);
+    if (s.chex) return launch_pass<3, true, true, true>(PASS_ARGS);
+    return launch_pass<3, false, true, true>(PASS_ARGS);
+  }
   if (exact) {
     if (which == 1) return launch_pass<1, false, true>(PASS_ARGS);
     if (which == 2) return launch_pass<2, false, true>(PASS_ARGS);
@@ -1659,9 +1698,22 @@ cudaError_t node_sum(const G32& g, int pass, const void* partial, int nq, bool e
 cudaError_t ct_and_up(const G32& g, const float* np, const float* S, float* up, cudaStream_t st) {
   RET((k_ct_up<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, const_cast<float*>(np), S, up)));
 }
-cudaError_t build_kit(const G32& g, const float* aj, const float* up, const float* dbt, const float* b0c, float4* kit,
-                      cudaStream_t st) {
-  RET((k_kit<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, aj, up, dbt, b0c, kit)));
+cudaError_t build_kit(const G32& g, const float* aj, const float* up, const float* dbt, const float* b0c,
+                      const float* np, float gp, float4* kit, float4* kitg, cudaStream_t st) {
+  RET((k_kit<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, aj, up, dbt, b0c, np, gp, kit, kitg)));
+}
+__global__ void k_gpe(G32 g, const float* __restrict__ np, float gp, float* __restrict__ gpf) {
+  GSTRIDE(t, n_int(g)) {
+    int i, j, k;
+    interior_of(g, t, i, j, k);
+    const long long C = g.C, o = nid(g, i, j, k);
+    store_img(g, gpf, i, j, k, gpe_face<0>(g, np, gp, o));
+    store_img(g, gpf + C, i, j, k, gpe_face<1>(g, np, gp, o));
+    store_img(g, gpf + 2 * C, i, j, k, gpe_face<2>(g, np, gp, o));
+  }
+}
+cudaError_t gpe_faces(const G32& g, const float* np, float gp, float* gpf, cudaStream_t st) {
+  RET((k_gpe<<<nblk(n_int(g)), TPB, 0, st>>>(g, np, gp, gpf)));
 }
 cudaError_t curlB32(const G32& g, const float* dbt, const float* np, float alpha, float* aj, cudaStream_t st) {
   RET((k_curlB<<<nblk((long long)g.ncx * g.ncy * g.ncz), TPB, 0, st>>>(g, dbt, np, alpha, aj)));
@@ -1673,20 +1725,20 @@ cudaError_t aj_ct(const G32& g, bool corr, const float* db, const float* np, con
   RET((k_aj_ct<false><<<grid, blk, 0, st>>>(g, db, np, up, b0c, alpha, aj, ct)));
 }
 cudaError_t b_step(const G32& g, bool pred, bool write_e, const float* ct, const float* nu, const float* aj,
-                   const float* bh, const float* bl, double coef, const float* b0c, float* oh, float* ol, float* dbo,
-                   const float* db1, float* dbtp1, float* E, float* e_acc, cudaStream_t st) {
+                   const float* gpf, const float* bh, const float* bl, double coef, const float* b0c, float* oh,
+                   float* ol, float* dbo, const float* db1, float* dbtp1, float* E, float* e_acc, cudaStream_t st) {
   const dim3 grid((g.ncx + FBX - 1) / FBX, (g.ncy + FBY - 1) / FBY, g.ncz), blk(FBX, FBY);
   const float ch = (float)coef, cl = (float)(coef - (double)ch);
   if (pred && write_e)
-    RET((k_bstep<true, true><<<grid, blk, 0, st>>>(g, ct, nu, aj, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E,
+    RET((k_bstep<true, true><<<grid, blk, 0, st>>>(g, ct, nu, aj, gpf, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E,
                                                    e_acc)));
   if (pred)
-    RET((k_bstep<true, false><<<grid, blk, 0, st>>>(g, ct, nu, aj, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E,
+    RET((k_bstep<true, false><<<grid, blk, 0, st>>>(g, ct, nu, aj, gpf, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E,
                                                     e_acc)));
   if (write_e)
-    RET((k_bstep<false, true><<<grid, blk, 0, st>>>(g, ct, nu, aj, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E,
+    RET((k_bstep<false, true><<<grid, blk, 0, st>>>(g, ct, nu, aj, gpf, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E,
                                                     e_acc)));
-  RET((k_bstep<false, false><<<grid, blk, 0, st>>>(g, ct, nu, aj, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E,
+  RET((k_bstep<false, false><<<grid, blk, 0, st>>>(g, ct, nu, aj, gpf, bh, bl, ch, cl, b0c, oh, ol, dbo, db1, dbtp1, E,
                                                    e_acc)));
 }
 cudaError_t b_step_given_e(const G32& g, const float* E, const float* bh, const float* bl, double coef,
@@ -1701,8 +1753,9 @@ cudaError_t df_lerp(const G32& g, const float* nh, const float* nl, const float*
   RET((k_df_lerp<<<grid, blk, 0, st>>>(g, nh, nl, oh, f, rh, rl)));
 }
 cudaError_t grid_to_voxels(const G32& g, const float* db, const float* b0c, const float* up, const float* np,
-                           float te, const float* ct, const float* aj, const float* nu, float* out, cudaStream_t st) {
-  RET((k_grid_to_voxels<<<nblk(n_int(g)), TPB, 0, st>>>(g, db, b0c, up, np, te, ct, aj, nu, out)));
+                           float te, const float* ct, const float* aj, const float* nu, const float* gpf, float* out,
+                           cudaStream_t st) {
+  RET((k_grid_to_voxels<<<nblk(n_int(g)), TPB, 0, st>>>(g, db, b0c, up, np, te, ct, aj, nu, gpf, out)));
 }
 cudaError_t judge_sums(const G32& g, const float* ah, const float* al, const float* bh, const float* bl,
                        const float* b0c, double* acc3, cudaStream_t st) {

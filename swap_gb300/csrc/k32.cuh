@@ -162,7 +162,7 @@ __device__ __forceinline__ float offset_in_cell(double x, double q1, double d, i
 // measure what the exact sums gain).  partial: 8 bytes per tile entry.
 cudaError_t pass(int which, const G32& g, const Part& p, const Species& sp, const StepParams& sprm,
                  const int64_t* start, const float4* kit, void* partial, uint32_t* dirrank, uint16_t* dep, int* err,
-                 bool exact, cudaStream_t st, const FarList* far = nullptr);
+                 bool exact, cudaStream_t st, const FarList* far = nullptr, const float4* kitg = nullptr);
 // The moments of pass 3's far list into the brick partials (pass 3's tiles).
 cudaError_t far_deposit(const G32& g, const FarList& far, void* partial, bool exact, int* err, cudaStream_t st);
 // Add the far list's arrivals to the per-key counts (before the scan).
@@ -178,8 +178,13 @@ cudaError_t node_sum(const G32& g, int pass, const void* partial, int nq, bool e
 
 // ---- fields ----
 cudaError_t ct_and_up(const G32& g, const float* np, const float* S, float* up, cudaStream_t st);
+// kitg (may be null): the electron-pressure face gradient of np (grad_pe
+// gp) centred per node, for the passes' gathered E.
 cudaError_t build_kit(const G32& g, const float* aj, const float* up, const float* dbt, const float* b0c,
-                      float4* kit, cudaStream_t st);
+                      const float* np, float gp, float4* kit, float4* kitg, cudaStream_t st);
+// gpf: the electron-pressure gradient at every face (with ghost images),
+// which E subtracts (the isothermal extension of gutsf.f:1083,1283).
+cudaError_t gpe_faces(const G32& g, const float* np, float gp, float* gpf, cudaStream_t st);
 cudaError_t curlB32(const G32& g, const float* dbt, const float* np, float alpha, float* aj, cudaStream_t st);
 // One half of a field subcycle in two fused kernels: aj and the cross
 // product ct (predictor: B from dB; corrector: B at m+1/2), then E on the
@@ -188,9 +193,10 @@ cudaError_t curlB32(const G32& g, const float* dbt, const float* np, float alpha
 cudaError_t aj_ct(const G32& g, bool corr, const float* db, const float* np, const float* up, const float* b0c,
                   float alpha, float* aj, float* ct, cudaStream_t st);
 // e_acc (may be null): the step's E summed over the correctors.
+// gpf (may be null): the electron-pressure face gradient E subtracts.
 cudaError_t b_step(const G32& g, bool pred, bool write_e, const float* ct, const float* nu, const float* aj,
-                   const float* bh, const float* bl, double coef, const float* b0c, float* oh, float* ol, float* dbo,
-                   const float* db1, float* dbtp1, float* E, float* e_acc, cudaStream_t st);
+                   const float* gpf, const float* bh, const float* bl, double coef, const float* b0c, float* oh,
+                   float* ol, float* dbo, const float* db1, float* dbtp1, float* E, float* e_acc, cudaStream_t st);
 // The surrogate's field advance: B_new = base - coef * curl E for a given E.
 cudaError_t b_step_given_e(const G32& g, const float* E, const float* bh, const float* bl, double coef,
                            const float* b0c, float* oh, float* ol, float* dbo, cudaStream_t st);
@@ -200,7 +206,8 @@ cudaError_t df_lerp(const G32& g, const float* nh, const float* nl, const float*
 // Surrogate inputs per interior node, FP32 [V][SUR_NIN]: B, u_p, n_p,
 // te*n_p and E0 = ct + nu aj (zero when ct is null).
 cudaError_t grid_to_voxels(const G32& g, const float* db, const float* b0c, const float* up, const float* np,
-                           float te, const float* ct, const float* aj, const float* nu, float* out, cudaStream_t st);
+                           float te, const float* ct, const float* aj, const float* nu, const float* gpf, float* out,
+                           cudaStream_t st);
 // Sums over the interior of |B_a - B_b|^2, |B_b|^2 and |B_b - b0|^2.
 cudaError_t judge_sums(const G32& g, const float* ah, const float* al, const float* bh, const float* bl,
                        const float* b0c, double* acc3, cudaStream_t st);

@@ -496,16 +496,33 @@ extern "C" int swap_conv3_check(int32_t nx, int32_t ny, int32_t nz, int32_t cin,
 }
 
 // ---------------------------------------------------------------------------
-// the network: 4 periodic 3x3x3 conv layers, 8 -> 32 -> 32 -> 32 -> 3
+// the network: NL periodic 3x3x3 conv layers, 11 -> 32 -> ... -> 32 -> 3
 // channels, GELU between them; BF16 weights and activations, FP32
 // accumulation, FP32 master weights trained with Adam
 // ---------------------------------------------------------------------------
 
 namespace {
 
-constexpr int NL = 4;
-constexpr int LCIN[NL] = {16, 32, 32, 32};   // layer 0: 11 input channels padded to 16
-constexpr int LCOUT[NL] = {32, 32, 32, 16};  // layer 3: 3 output channels padded to 16
+// Depth: each layer widens the receptive field by one voxel per side.  The
+// subcycles move grid-scale whistler waves several cells within one ion
+// step, so the correction at a node depends on a wide neighbourhood.
+#ifndef SWAP_SUR_LAYERS
+#define SWAP_SUR_LAYERS 8
+#endif
+constexpr int NL = SWAP_SUR_LAYERS;
+constexpr double WARMUP = 200.0;  // Adam updates of the learning-rate warm-up
+static_assert(NL >= 2 && NL <= 16, "surrogate depth");
+struct LayerDims {
+  int v[NL];
+  constexpr int operator[](int l) const { return v[l]; }
+};
+constexpr LayerDims layer_dims(bool in) {
+  LayerDims d{};
+  for (int l = 0; l < NL; ++l) d.v[l] = in ? (l == 0 ? 16 : 32) : (l == NL - 1 ? 16 : 32);
+  return d;
+}
+constexpr LayerDims LCIN = layer_dims(true);    // layer 0: 11 input channels padded to 16
+constexpr LayerDims LCOUT = layer_dims(false);  // last layer: 3 output channels padded to 16
 // Inputs per voxel: B (3), u_p (3), n_p, p_e, and E0 (3), the plain scheme's
 // E at the start of the field step (the layout k32's voxel kernels write);
 // output: the mean corrector E of the subcycles minus E0.
@@ -548,6 +565,80 @@ __global__ void k_loss(long long V, const float* __restrict__ out, const float* 
       const float d = out[v * NOUT + c] - (tgt[v * NOUT + c] - on.mean[c]) / on.std[c];
       s += d * d;
       h[c] = __float2bfloat16(d * gscale);
+    }
+    uint4* dst = reinterpret_cast<uint4*>(d16 + v * 16);
+    dst[0] = reinterpret_cast<const uint4*>(h)[0];
+    dst[1] = reinterpret_cast<const uint4*>(h)[1];
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(acc, s);
+}
+
+// The B error a prediction makes is dt curl(E error) (B advances as
+// B - dt curl E), and curl weights an error by its wavenumber: the loss can
+// add lam * 0.5 sum |curl e|^2 of the physical error e = out*std + mean - tgt
+// (forward differences on the periodic voxel grid, as the B update's curl,
+// in voxel units).  k_err3: e [V][3].
+__global__ void k_err3(long long V, const float* __restrict__ out, const float* __restrict__ tgt, OutNorm on,
+                       float* __restrict__ e) {
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x)
+#pragma unroll
+    for (int c = 0; c < NOUT; ++c)
+      e[v * NOUT + c] = (out ? fmaf(out[v * NOUT + c], on.std[c], on.mean[c]) : 0.0f) - tgt[v * NOUT + c];
+}
+
+__device__ __forceinline__ long long vox(int i, int j, int k, int nx, int ny, int nz) {
+  i = i < 0 ? i + nx : (i >= nx ? i - nx : i);
+  j = j < 0 ? j + ny : (j >= ny ? j - ny : j);
+  k = k < 0 ? k + nz : (k >= nz ? k - nz : k);
+  return (long long)i + (long long)nx * ((long long)j + (long long)ny * k);
+}
+
+// kap = curl e (forward differences): kap_x = Dy e3 - Dz e2, kap_y = Dz e1 -
+// Dx e3, kap_z = Dx e2 - Dy e1; the sum of |kap|^2 into *acc.
+__global__ void k_curl3(int nx, int ny, int nz, const float* __restrict__ e, float* __restrict__ kap, float* acc) {
+  const long long V = (long long)nx * ny * nz;
+  float s = 0.0f;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(v % nx), j = (int)((v / nx) % ny), k = (int)(v / ((long long)nx * ny));
+    const float* o = e + v * 3;
+    const float* px = e + vox(i + 1, j, k, nx, ny, nz) * 3;
+    const float* py = e + vox(i, j + 1, k, nx, ny, nz) * 3;
+    const float* pz = e + vox(i, j, k + 1, nx, ny, nz) * 3;
+    const float kx = (py[2] - o[2]) - (pz[1] - o[1]);
+    const float ky = (pz[0] - o[0]) - (px[2] - o[2]);
+    const float kz = (px[1] - o[1]) - (py[0] - o[0]);
+    kap[v * 3] = kx; kap[v * 3 + 1] = ky; kap[v * 3 + 2] = kz;
+    s += kx * kx + ky * ky + kz * kz;
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(acc, s);
+}
+
+// The plain loss of k_loss plus lam * std_c * (curl^T kap)_c in the output
+// gradient (D_a^T g = g[o - s_a] - g[o]); the plain sum of squares to *acc.
+__global__ void k_loss_curl(int nx, int ny, int nz, const float* __restrict__ out, const float* __restrict__ tgt,
+                            OutNorm on, float gscale, float lam, const float* __restrict__ kap,
+                            __nv_bfloat16* __restrict__ d16, float* acc) {
+  const long long V = (long long)nx * ny * nz;
+  float s = 0.0f;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(v % nx), j = (int)((v / nx) % ny), k = (int)(v / ((long long)nx * ny));
+    const float* o = kap + v * 3;
+    const float* mx = kap + vox(i - 1, j, k, nx, ny, nz) * 3;
+    const float* my = kap + vox(i, j - 1, k, nx, ny, nz) * 3;
+    const float* mz = kap + vox(i, j, k - 1, nx, ny, nz) * 3;
+    // d/de1 = Dz^T kap_y - Dy^T kap_z, d/de2 = Dx^T kap_z - Dz^T kap_x, d/de3 = Dy^T kap_x - Dx^T kap_y
+    const float ct[3] = {(mz[1] - o[1]) - (my[2] - o[2]), (mx[2] - o[2]) - (mz[0] - o[0]),
+                         (my[0] - o[0]) - (mx[1] - o[1])};
+    alignas(16) __nv_bfloat16 h[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) h[c] = __float2bfloat16(0.0f);
+#pragma unroll
+    for (int c = 0; c < NOUT; ++c) {
+      const float d = out[v * NOUT + c] - (tgt[v * NOUT + c] - on.mean[c]) / on.std[c];
+      s += d * d;
+      h[c] = __float2bfloat16((d + lam * on.std[c] * ct[c]) * gscale);
     }
     uint4* dst = reinterpret_cast<uint4*>(d16 + v * 16);
     dst[0] = reinterpret_cast<const uint4*>(h)[0];
@@ -689,6 +780,10 @@ struct swap_surrogate {
   float in_mean[NIN] = {}, in_std[NIN] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1};
   OutNorm on{{0, 0, 0}, {1, 1, 1}};
   bool normed = false;
+  // loss: 0.5 mean r^2 + 0.5 curl_w * mean |curl e|^2 / kref2 (r the
+  // normalised error, e the physical one, kref2 = mean |curl tgt|^2)
+  float curl_w = 0.0f;
+  double kref2 = 0.0;
   float *d_mean = nullptr, *d_istd = nullptr;
   // the dataset, all of one grid shape (the first sample's)
   int ds_nx = 0, ds_ny = 0, ds_nz = 0;
@@ -823,24 +918,23 @@ int forward(swap_surrogate* net, bool train, cudaStream_t st) {
 int backward(swap_surrogate* net, cudaStream_t st) {
   const int nx = net->nx, ny = net->ny, nz = net->nz;
   const long long V = net->V;
-  SCU((conv3_dw<32, 16>(nx, ny, nz, V, net->Y[2], net->d16, net->gw[3], net->gb[3], st)));
+  constexpr int L = NL - 1;
+  SCU((conv3_dw<32, 16>(nx, ny, nz, V, net->Y[L - 1], net->d16, net->gw[L], net->gb[L], st)));
   ConvArgs a = conv_args(net);
   a.Y = nullptr; a.Z = nullptr; a.bias = nullptr; a.gelu = 0; a.ldf = 32; a.nstore = 32; a.Yf = net->dy;
-  // layer 3 -> 2
-  a.X = net->d16; a.W = net->wt[3];
+  // last layer -> the one before: the data gradient, then through its GELU
+  a.X = net->d16; a.W = net->wt[L];
   SCU(conv3(16, 32, a, st));
-  k_gelu_back<<<nblk(V * 32), 256, 0, st>>>(V * 32, net->dy, net->Z[2], net->dzA);
-  SCU((conv3_dw<32, 32>(nx, ny, nz, V, net->Y[1], net->dzA, net->gw[2], net->gb[2], st)));
-  // layer 2 -> 1
-  a.X = net->dzA; a.W = net->wt[2];
-  SCU(conv3(32, 32, a, st));
-  k_gelu_back<<<nblk(V * 32), 256, 0, st>>>(V * 32, net->dy, net->Z[1], net->dzB);
-  SCU((conv3_dw<32, 32>(nx, ny, nz, V, net->Y[0], net->dzB, net->gw[1], net->gb[1], st)));
-  // layer 1 -> 0
-  a.X = net->dzB; a.W = net->wt[1];
-  SCU(conv3(32, 32, a, st));
-  k_gelu_back<<<nblk(V * 32), 256, 0, st>>>(V * 32, net->dy, net->Z[0], net->dzA);
-  SCU((conv3_dw<16, 32>(nx, ny, nz, V, net->x0, net->dzA, net->gw[0], net->gb[0], st)));
+  __nv_bfloat16 *dz = net->dzA, *dz_next = net->dzB;
+  k_gelu_back<<<nblk(V * 32), 256, 0, st>>>(V * 32, net->dy, net->Z[L - 1], dz);
+  for (int l = L - 1; l >= 1; --l) {  // layer l -> l - 1
+    SCU((conv3_dw<32, 32>(nx, ny, nz, V, net->Y[l - 1], dz, net->gw[l], net->gb[l], st)));
+    a.X = dz; a.W = net->wt[l];
+    SCU(conv3(32, 32, a, st));
+    k_gelu_back<<<nblk(V * 32), 256, 0, st>>>(V * 32, net->dy, net->Z[l - 1], dz_next);
+    std::swap(dz, dz_next);
+  }
+  SCU((conv3_dw<16, 32>(nx, ny, nz, V, net->x0, dz, net->gw[0], net->gb[0], st)));
   return SWAP_OK;
 }
 
@@ -877,12 +971,22 @@ int adam_step(swap_surrogate* net, float lr, cudaStream_t st) {
 // Loss of the current x0 against target tgt ([V][3], unnormalised); the
 // output gradient goes to d16.  Returns the sum of squares in *sq.
 int loss_grad(swap_surrogate* net, const float* tgt, float gnorm, double* sq, cudaStream_t st) {
-  SCU(cudaMemsetAsync(net->acc, 0, sizeof(float), st));
-  k_loss<<<nblk(net->V), 256, 0, st>>>(net->V, net->out, tgt, net->on, gnorm, net->d16, net->acc);
-  float h = 0;
-  SCU(cudaMemcpyAsync(&h, net->acc, sizeof(float), cudaMemcpyDeviceToHost, st));
+  SCU(cudaMemsetAsync(net->acc, 0, 2 * sizeof(float), st));
+  const bool curl = net->curl_w > 0.0f && net->kref2 > 0.0;
+  if (curl) {  // e and curl e in the (free until the backward pass) dy buffer
+    float *e = net->dy, *kap = net->dy + 3 * net->V;
+    k_err3<<<nblk(net->V), 256, 0, st>>>(net->V, net->out, tgt, net->on, e);
+    k_curl3<<<nblk(net->V), 256, 0, st>>>(net->nx, net->ny, net->nz, e, kap, net->acc + 1);
+    k_loss_curl<<<nblk(net->V), 256, 0, st>>>(net->nx, net->ny, net->nz, net->out, tgt, net->on, gnorm,
+                                                (float)(3.0 * net->curl_w / net->kref2), kap, net->d16, net->acc);
+  } else {
+    k_loss<<<nblk(net->V), 256, 0, st>>>(net->V, net->out, tgt, net->on, gnorm, net->d16, net->acc);
+  }
+  float h[2] = {0, 0};
+  SCU(cudaMemcpyAsync(h, net->acc, sizeof(h), cudaMemcpyDeviceToHost, st));
   SCU(cudaStreamSynchronize(st));
-  *sq = h;
+  // in units of the plain term's sum over V*3 values
+  *sq = h[0] + (curl ? 3.0 * net->curl_w * (double)h[1] / net->kref2 : 0.0);
   return SWAP_OK;
 }
 
@@ -1135,8 +1239,36 @@ static int fit_norm(swap_surrogate* net) {
     net->on.mean[c] = (float)m;
     net->on.std[c] = (float)std::max(std::sqrt(var), 1e-6 * std::max(1.0, std::fabs(m)));
   }
+  // mean |curl tgt|^2 per voxel over the same samples: the curl term's scale
+  int r;
+  if ((r = ensure_ds_shape(net))) return r;
+  double k2 = 0;
+  for (std::size_t q = 0; q < take; ++q) {
+    const std::size_t k = q * n / take;
+    float* e = net->dy;
+    SCU(cudaMemsetAsync(net->acc, 0, 2 * sizeof(float), nullptr));
+    k_err3<<<nblk(net->V), 256>>>(net->V, nullptr, net->ds_tgt[k], net->on, e);
+    k_curl3<<<nblk(net->V), 256>>>(net->nx, net->ny, net->nz, e, e + 3 * net->V, net->acc + 1);
+    float h = 0;
+    SCU(cudaMemcpy(&h, net->acc + 1, sizeof(float), cudaMemcpyDeviceToHost));
+    k2 += h;
+  }
+  net->kref2 = k2 / cnt;
   net->normed = true;
   return upload_norm(net, nullptr);
+}
+
+extern "C" int swap_surrogate_layers(int32_t* n) {
+  if (!n) return SWAP_EINVAL;
+  *n = NL;
+  return SWAP_OK;
+}
+
+extern "C" int swap_surrogate_set_curl_weight(swap_surrogate* net, double w, double kref2) {
+  if (!net || !(w >= 0.0) || !(kref2 >= 0.0)) return SWAP_EINVAL;
+  net->curl_w = (float)w;
+  if (kref2 > 0.0) net->kref2 = kref2;
+  return SWAP_OK;
 }
 
 // Adam over the collected pairs for `epochs` passes in shuffled order; the
@@ -1162,7 +1294,12 @@ extern "C" int swap_surrogate_train(swap_surrogate* net, int32_t epochs, double 
       double sq = 0;
       if ((r = loss_grad(net, net->ds_tgt[k], 1.0f / (3.0f * (float)net->V), &sq, st))) return r;
       tot += sq / (3.0 * (double)net->V);
-      if ((r = zero_grads(net, st)) || (r = backward(net, st)) || (r = adam_step(net, (float)lr, st))) return r;
+      // linear warm-up over the first WARMUP updates: Adam's first steps move
+      // every weight by about lr at once, which can push a deep stack's
+      // pre-activations where GELU is flat, and it then stops learning
+      const double warm = std::min(1.0, (double)(net->adam_t + 1) / WARMUP);
+      if ((r = zero_grads(net, st)) || (r = backward(net, st)) || (r = adam_step(net, (float)(lr * warm), st)))
+        return r;
     }
     last = tot / (double)n;
   }

@@ -35,6 +35,11 @@ struct F32State {
   uint16_t* pre = nullptr;
   void* partial = nullptr;  // brick partial tiles, 8 bytes per entry (fixed point or FP32)
   FarList far{};            // pass 3's ions that moved more than one cell
+  // the isothermal electron-pressure term (grad_pe != 0): its face gradient
+  // for E, and centred per node for the passes' gather
+  float gp = 0.0f;
+  float* gpf = nullptr;
+  float4* kitg = nullptr;
   bool exact = true;        // exact moment sums (swap_f32_set_moment_sums)
   float4* kit = nullptr;
   float *np = nullptr, *S = nullptr, *up = nullptr, *aj = nullptr, *ct = nullptr, *E = nullptr, *nu = nullptr;
@@ -178,7 +183,6 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
   if (!c) return SWAP_EINVAL;
   TRY(c->begin());
   if (!c->h_xp || !c->h_b1) return c->fail(SWAP_EINVAL, "swap_bind_particles and swap_bind_fields are required");
-  if (c->prm.grad_pe != 0.0) return c->fail(SWAP_EINVAL, "the FP32 form has no electron-pressure term");
   const int nx = c->dims.nx, ny = c->dims.ny, nz = c->dims.nz;
   const int ncx = nx - 2, ncy = ny - 2, ncz = nz - 2;
   if (ncx % 4 || ncy % 4 || ncz % 4 || ncx < 8 || ncy < 8 || ncz < 8 || ncx > 1024 || ncy > 1024 || ncz > 1024)
@@ -340,6 +344,13 @@ extern "C" int swap_f32_begin(swap_ctx* c) {
   s->far.n = s->alloc<int>(1);
   s->far.total = s->alloc<unsigned long long>(1);
   s->kit = s->alloc<float4>(2 * (std::size_t)ncx * ncy * ncz);
+  s->gp = (float)c->prm.grad_pe;
+  if (s->gp != 0.0f) {
+    s->gpf = s->alloc<float>(3 * (std::size_t)C);
+    s->kitg = s->alloc<float4>((std::size_t)ncx * ncy * ncz);
+    if (!s->gpf || !s->kitg) return c->fail(SWAP_ECUDA, "FP32 grid allocation failed");
+    CU(cudaMemsetAsync(s->gpf, 0, 3 * (std::size_t)C * sizeof(float), c->st));
+  }
   // np and the velocity sums S in one block (S 128-byte aligned after np), so
   // that one exchange covers a deposit's node sums.  Zeroed once: the gap and
   // S's ghost nodes are never written, and stay zero through the exchanges.
@@ -478,11 +489,11 @@ static int subcycles(swap_ctx* c, F32State* s, float* e_acc = nullptr) {
     const bool last = it == n - 1;
     // predictor: curlB (maind.f:430) and predict_B with its get_E (maind.f:457), plus dB at m+1/2
     KL("f32_aj_ct_pred", aj_ct(g, false, s->db1, s->np, s->up, s->b0c, alpha, s->aj, s->ct, c->st));
-    KL("f32_bstep_pred", b_step(g, true, false, s->ct, s->nu, s->aj, s->b12.h, s->b12.l, 2.0 * dtsub, s->b0c,
+    KL("f32_bstep_pred", b_step(g, true, false, s->ct, s->nu, s->aj, s->gpf, s->b12.h, s->b12.l, 2.0 * dtsub, s->b0c,
                                 s->b1p2.h, s->b1p2.l, s->db1p2, s->db1, s->dbtp1, s->E, nullptr, c->st));
     // corrector: correct_B (maind.f:462) with its curlB and get_Ep1 at m+1/2
     KL("f32_aj_ct_corr", aj_ct(g, true, s->dbtp1, s->np, s->up, s->b0c, alpha, s->aj, s->ct, c->st));
-    KL("f32_bstep_corr", b_step(g, false, last, s->ct, s->nu, s->aj, s->b1.h, s->b1.l, dtsub, s->b0c, s->b1p2.h,
+    KL("f32_bstep_corr", b_step(g, false, last, s->ct, s->nu, s->aj, s->gpf, s->b1.h, s->b1.l, dtsub, s->b0c, s->b1p2.h,
                                 s->b1p2.l, s->db1p2, nullptr, nullptr, s->E, e_acc, c->st));
     // f_update_tlev (gutsf.f:10-35): b12 <- b1, b1 <- b1p2 (bt = b1)
     std::swap(s->b12, s->b1);
@@ -582,7 +593,8 @@ static int sur_buffers(swap_ctx* c, F32State* s) {
 static int sur_inputs(swap_ctx* c, F32State* s) {
   const G32& g = s->g;
   KL("f32_sur_inputs", aj_ct(g, false, s->db1, s->np, s->up, s->b0c, (float)c->prm.alpha, s->aj, s->ct, c->st));
-  KL("f32_sur_inputs", grid_to_voxels(g, s->db1, s->b0c, s->up, s->np, 1.0f, s->ct, s->aj, s->nu, s->vin, c->st));
+  KL("f32_sur_inputs",
+     grid_to_voxels(g, s->db1, s->b0c, s->up, s->np, 1.0f, s->ct, s->aj, s->nu, s->gpf, s->vin, c->st));
   return SWAP_OK;
 }
 
@@ -677,14 +689,15 @@ static int one_step(swap_ctx* c, F32State* s) {
   KL("f32_P1", pass(1, g, p, s->sp, sp, s->start, s->kit, s->partial, nullptr, nullptr, c->d_err, s->exact, c->st));  // :385-387,399
   TRY(finish_deposit(c, s, 1, 4));
   KL("f32_curlB", curlB32(g, s->db1, s->np, (float)c->prm.alpha, s->aj, c->st));  // :395
-  KL("f32_kit", build_kit(g, s->aj, s->up, s->db1, s->b0c, s->kit, c->st));       // :398, get_Ep :183-184
-  KL("f32_P2", pass(2, g, p, s->sp, sp, s->start, s->kit, s->partial, nullptr, nullptr, c->d_err, s->exact, c->st));  // :400-402
+  KL("f32_kit", build_kit(g, s->aj, s->up, s->db1, s->b0c, s->np, s->gp, s->kit, s->kitg, c->st));  // :398, :183-184
+  KL("f32_P2", pass(2, g, p, s->sp, sp, s->start, s->kit, s->partial, nullptr, nullptr, c->d_err, s->exact, c->st,
+                    nullptr, s->kitg));  // :400-402
   TRY(finish_deposit(c, s, 2, 3));
-  KL("f32_kit", build_kit(g, s->aj, s->up, s->db1, s->b0c, s->kit, c->st));       // :404
+  KL("f32_kit", build_kit(g, s->aj, s->up, s->db1, s->b0c, s->np, s->gp, s->kit, s->kitg, c->st));  // :404
   // :404-413, the final half move of :479 and res_chex; prepares the sort
   CU(cudaMemsetAsync(s->far.n, 0, sizeof(int), c->st));
   KL("f32_P3", pass(3, g, p, s->sp, sp, s->start, s->kit, s->partial, s->dirrank, s->dep, c->d_err, s->exact,
-                    c->st, &s->far));
+                    c->st, &s->far, s->kitg));
   KL("f32_far_deposit", far_deposit(g, s->far, s->partial, s->exact, c->d_err, c->st));
   {  // pass 3 wrote the new v into the vp1 arrays and left the old v (the new vp1) in place
     Part& q = s->buf[s->cur];
@@ -695,6 +708,7 @@ static int one_step(swap_ctx* c, F32State* s) {
   PreStaged pre;
   if (s->src_on) TRY(stage_ahead(c, s, c->src_step + 1, &pre));  // the sources of the next step
   TRY(finish_deposit(c, s, 3, 4));
+  if (s->gpf) KL("f32_gpe", gpe_faces(g, s->np, s->gp, s->gpf, c->st));  // E's pressure term at the new np
   TRY(field_step(c, s));                                                          // :420-476
   TRY(sort_step(c, s, c->src_step + 1, true, &pre));
   if (c->have_srcs) c->src_step++;
@@ -789,6 +803,8 @@ extern "C" int swap_f32_set_moment_sums(swap_ctx* c, int exact) {
   if (!c) return SWAP_EINVAL;
   F32State* s = f32(c);
   if (!s) return c->fail(SWAP_EINVAL, "swap_f32_begin has not been called");
+  if (!exact && s->gp != 0.0f)
+    return c->fail(SWAP_EINVAL, "the electron-pressure term runs with the exact moment sums only");
   s->exact = exact != 0;
   return SWAP_OK;
 }

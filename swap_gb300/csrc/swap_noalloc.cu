@@ -18,11 +18,12 @@
 // Properties:
 //  * scratch is static: every GPU that loads this library holds it
 //    (SWAP_NOALLOC_SCRATCH_BYTES) until the process exits;
+//  * no call can be captured in a CUDA graph: every call reads the flag back
+//    and waits for its stream, which a capture does not allow;
 //  * the first call on a device looks up the scratch address with
-//    cudaGetSymbolAddress (no allocation) and keeps it for the process; make
-//    that first call before any stream capture, and do not call the entry
-//    again on a device after cudaDeviceReset on it (the module is loaded
-//    anew and the kept address is stale);
+//    cudaGetSymbolAddress (no allocation) and keeps it for the process; do
+//    not call the entry again on a device after cudaDeviceReset on it (the
+//    module is loaded anew and the kept address is stale);
 //  * all calls share the scratch, so calls that overlap on the GPU (two
 //    streams, two threads) race; serialize them.  After an error the entry
 //    waits for its stream before it returns, so no work of the failed call

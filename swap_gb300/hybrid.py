@@ -464,16 +464,26 @@ class Hybrid:
 class Surrogate:
     """The learned field-subcycle surrogate (a handle of the C-ABI)."""
 
-    LAYERS = ((16, 32), (32, 32), (32, 32), (32, 16))  # (cin, cout) of the 4 conv layers, padded
     # inputs per voxel: B (3), u_p (3), n_p, p_e, and E0 (3), the plain E at the
     # start of the field step; the output is the mean corrector E minus E0
     NIN = 11
 
-    def __init__(self, seed: int = 1, max_samples: int = 4096):
+    def __init__(self, seed: int = 1, max_samples: int = 4096, curl_weight: float = 0.0):
         self.lib = abi.load()
+        n = C.c_int32()
+        abi.check(self.lib, None, self.lib.swap_surrogate_layers(C.byref(n)))
+        # (cin, cout) of the conv layers, padded
+        self.LAYERS = tuple([(16, 32)] + [(32, 32)] * (n.value - 2) + [(32, 16)])
         h = C.c_void_p()
         abi.check(self.lib, None, self.lib.swap_surrogate_create(C.byref(h), int(seed), int(max_samples)))
         self.h = h
+        if curl_weight:
+            self.set_curl_weight(curl_weight)
+
+    def set_curl_weight(self, w: float, kref2: float = 0.0):
+        """Add w * mean |curl e|^2 / kref2 to the loss (e the E error: curl e is
+        the B error per unit dt); kref2 = 0: mean |curl target|^2 of the pairs."""
+        self._check(self.lib.swap_surrogate_set_curl_weight(self.h, float(w), float(kref2)))
 
     def _check(self, code):
         if code:

@@ -71,9 +71,11 @@ def test_conv3_matches_cpu(cin, cout, dims):
     assert (Y.cpu().double() - gelu).abs().max().item() <= 1e-2 * gelu.abs().max().item()
 
 
-def _ref_forward_backward(vin, tgt, layers, mean, std, out_mean, out_std, dims):
+def _ref_forward_backward(vin, tgt, layers, mean, std, out_mean, out_std, dims, curl=None):
     """The network in float64 on the CPU with the GPU's BF16 roundings of the
-    inputs, weights and hidden activations; loss and weight gradients."""
+    inputs, weights and hidden activations; loss and weight gradients.
+    curl = (w, kref2): the loss adds 0.5 w mean_v |curl e|^2 / kref2 of the
+    physical error e (forward differences, periodic, voxel units)."""
     import torch
     import torch.nn.functional as F
 
@@ -97,32 +99,43 @@ def _ref_forward_backward(vin, tgt, layers, mean, std, out_mean, out_std, dims):
             h = z
     out = h[:, :3]
     loss = 0.5 * ((out - (tgt - out_mean) / out_std) ** 2).mean()
+    if curl:
+        w, kref2 = curl
+        e = (out * out_std + out_mean - tgt).reshape(nz, ny, nx, 3)
+        D = lambda f, dim: torch.roll(f, -1, dims=dim) - f  # f[i+1] - f[i]
+        e1, e2, e3 = e[..., 0], e[..., 1], e[..., 2]
+        kx = D(e3, 1) - D(e2, 0)
+        ky = D(e1, 0) - D(e3, 2)
+        kz = D(e2, 2) - D(e1, 1)
+        loss = loss + 0.5 * w * (kx**2 + ky**2 + kz**2).mean() / kref2
     loss.backward()
     return loss.item(), [(W.grad.numpy(), B.grad.numpy()) for W, B in params]
 
 
-@pytest.mark.parametrize("dims", [(8, 8, 4), (128, 2, 2)])
-def test_surrogate_gradients_match_cpu(dims):
+@pytest.mark.parametrize("dims,curl", [((8, 8, 4), None), ((128, 2, 2), None), ((8, 4, 8), (0.7, 2.5))])
+def test_surrogate_gradients_match_cpu(dims, curl):
     import torch
 
     from swap_gb300.hybrid import Surrogate
 
     V = dims[0] * dims[1] * dims[2]
     net = Surrogate(seed=5)
+    if curl:
+        net.set_curl_weight(*curl)
     g = torch.Generator().manual_seed(3)
     vin = torch.randn(V, Surrogate.NIN, generator=g, dtype=torch.float64)
     tgt = torch.randn(V, 3, generator=g, dtype=torch.float64)
     mean, std = np.full(Surrogate.NIN, 0.1), np.full(Surrogate.NIN, 1.5)
     out_mean, out_std = np.array([0.5, -0.25, 0.0]), np.array([0.75, 0.5, 2.0])
     net.norm(mean, std, out_mean, out_std)
-    layers = [net.weights(l) for l in range(4)]
+    layers = [net.weights(l) for l in range(len(net.LAYERS))]
     T = torch.tensor
-    loss_ref, g_ref = _ref_forward_backward(vin, tgt, layers, T(mean), T(std), T(out_mean), T(out_std), dims)
+    loss_ref, g_ref = _ref_forward_backward(vin, tgt, layers, T(mean), T(std), T(out_mean), T(out_std), dims, curl)
     dvin = vin.float().cuda()
     dtgt = tgt.float().cuda()
     loss, g_gpu = net.grads(dims, dvin.data_ptr(), dtgt.data_ptr())
     assert abs(loss - loss_ref) <= 2e-3 * loss_ref
-    for l in range(4):
+    for l in range(len(net.LAYERS)):
         for a, b in zip(g_gpu[l], g_ref[l]):
             err = np.linalg.norm(a - b) / np.linalg.norm(b)
             assert err < 3e-2, (l, err)  # BF16 activations and gradients against float64
