@@ -299,28 +299,39 @@ def run_reference(args):
 def train_surrogate(args, base):
     """The learned field surrogate, trained on pairs that the plain subcycles
     produce in randomized runs (swap_gb300.surrogate_data: upstream speed
-    1-6 v_A, beta 0.1-2, open x, a neutral cloud of radius 2-10 cells) of a
-    box of
-    --sur-cells cells that keeps the workload's B0, ion step, subcycles and
-    particles per cell.  Returns the network and what the training did."""
+    1-6 v_A, beta 0.1-2, an open x axis in half of the runs and a neutral
+    cloud of radius 2-10 cells in half) of a box of --sur-cells cells that
+    keeps the workload's B0, ion step, subcycles and particles per cell.
+    Adam with the library's warm-up, then --sur-epochs epochs in three stages
+    of falling learning rate.  Returns the network and what the training did."""
     from swap_gb300.hybrid import Surrogate
     from swap_gb300.surrogate_data import collect_randomized
 
     cells = (args.sur_cells,) * 3
-    net = Surrogate(seed=11, max_samples=args.sur_runs * args.sur_pairs)
+    net = Surrogate(seed=11, max_samples=args.sur_runs * args.sur_pairs, curl_weight=args.sur_curl)
     t0 = time.perf_counter()
-    collect_randomized(net, base, runs=args.sur_runs, pairs_per_run=args.sur_pairs, warmup=3, cells=cells, seed=5)
+    collect_randomized(net, base, runs=args.sur_runs, pairs_per_run=args.sur_pairs, warmup=3, cells=cells, seed=5,
+                       mixed=True)
     t_collect = time.perf_counter() - t0
     l0 = net.loss()
     t0 = time.perf_counter()
-    loss = net.train(args.sur_epochs, lr=2e-3)
+    E = max(args.sur_epochs, 3)
+    done, loss = 0, l0
+    for upto, lr in ((E // 4, 1e-3), (E * 5 // 8, 5e-4), (E, 1.5e-4)):
+        if upto > done:
+            loss = net.train(upto - done, lr=lr)
+            done = upto
     t_train = time.perf_counter() - t0
-    info = {"network": "4 periodic 3x3x3 conv layers 11-32-32-32-3, GELU, BF16 on tcgen05, FP32 accumulate; "
-                       "predicts the subcycles' mean E minus the plain E at the step's start",
+    nl = len(net.LAYERS)
+    info = {"network": f"{nl} periodic 3x3x3 conv layers {Surrogate.NIN}-" + "-".join(["32"] * (nl - 1))
+                       + "-3, GELU, BF16 on tcgen05, FP32 accumulate; predicts the subcycles' mean E minus the "
+                       "plain E at the step's start from B, u_p, n_p, p_e, that E and B - b12",
             "training": f"{args.sur_runs} randomized runs of {cells[0]}x{cells[1]}x{cells[2]} cells at "
                         f"{base.ppc} ppc, {args.sur_pairs} pairs each (upstream speed 1-6 v_A, beta 0.1-2, "
-                        f"open x, cloud radius 2-10 cells)",
-            "pairs": net.samples(), "collect_s": t_collect, "train_epochs": args.sur_epochs, "train_s": t_train,
+                        f"open or periodic x, with or without a cloud of radius 2-10 cells)",
+            "loss": "mean squared normalised E error" + (f" + {args.sur_curl} x relative curl error"
+                                                         if args.sur_curl else ""),
+            "pairs": net.samples(), "collect_s": t_collect, "train_epochs": E, "train_s": t_train,
             "loss_before": l0, "train_loss": loss}
     return net, info
 
@@ -439,7 +450,7 @@ def brick_load(starts: np.ndarray) -> dict:
             "cell_p99": float(np.percentile(per_cell, 99))}
 
 
-def run_compare(n: int, steps: int, cx: bool = True) -> dict:
+def run_compare(n: int, steps: int, cx: bool = True, marks=()) -> dict:
     """A named workload at its stated size, run `steps` ion steps from the
     same seeded load by the FP64 GPU drop-in and by the FP32 form: B, B - b0
     and n_p rel-L2 of the FP32 form against the FP64 run, each run's energy
@@ -447,7 +458,8 @@ def run_compare(n: int, steps: int, cx: bool = True) -> dict:
     brick.  With cx=False charge exchange is off: the FP32 form draws it per
     sorted ion and the FP64 path per array index, so with it on the two runs
     are different draws of the same process and their difference holds that
-    sampling noise as well as the FP32 rounding."""
+    sampling noise as well as the FP32 rounding.  marks: steps at which both
+    runs' total energies are also recorded."""
     import ctypes as C
 
     from swap_gb300.hybrid import Hybrid, config
@@ -485,11 +497,22 @@ def run_compare(n: int, steps: int, cx: bool = True) -> dict:
     def total(e):
         return float(e[0] + e[1])
 
+    marks = sorted(m for m in set(marks) if 0 < m < steps) + [steps]
+
+    def segments(run, energy):
+        """Run to each mark; the summed time and the total energy at each."""
+        ms, done, es = 0.0, 0, []
+        for m in marks:
+            ms += timed(h, lambda: run(m - done))
+            done = m
+            es.append(total(energy()))
+        return ms, es
+
     t0 = time.perf_counter()
     h = fresh()
     n0 = int(h.ni_tot[0])
     e0 = h.energy()
-    ms64 = timed(h, lambda: h.run(steps))
+    ms64, es64 = segments(h.run, h.energy)
     e64 = h.energy()
     h.sync_to_host()
     ref = {"b1": h.b1.copy(), "b0": h.b0.copy(), "np": h.np.copy()}
@@ -499,7 +522,7 @@ def run_compare(n: int, steps: int, cx: bool = True) -> dict:
     h = fresh()
     h.f32_begin()
     ea = h.f32_energy()
-    ms32 = timed(h, lambda: h.f32_run(steps))
+    ms32, es32 = segments(h.f32_run, h.f32_energy)
     eb = h.f32_energy()
     load = brick_load(h.f32_key_starts())
     n32 = h.f32_count()
@@ -514,6 +537,8 @@ def run_compare(n: int, steps: int, cx: bool = True) -> dict:
            "fp64_energy_drift": (total(e64) - total(e0)) / total(e0),
            "fp32_energy_drift": (total(eb) - total(ea)) / total(ea),
            "energy_vs_fp64": (total(eb) - total(e64)) / total(e64),
+           "energy_marks": [{"step": m, "fp64_drift": (a - total(e0)) / total(e0), "fp32_vs_fp64": (b - a) / a}
+                            for m, a, b in zip(marks, es64, es32)],
            "fp32_load_per_brick": load}
     h.close()
     del h
@@ -767,7 +792,8 @@ def run_accuracy_legs(args, line, net=None):
         for cx in {"both": [True, False], "on": [True], "off": [False]}[args.acc_cx]:
             key = f"config{n}" + ("" if cx else "_no_cx")
             try:
-                line.setdefault("accuracy_configs", {})[key] = run_compare(n, steps.get(n, 20), cx=cx)
+                line.setdefault("accuracy_configs", {})[key] = run_compare(
+                    n, steps.get(n, 20), cx=cx, marks=[int(x) for x in args.acc_marks.split(",") if x.strip()])
             except Exception as e:
                 line.setdefault("accuracy_configs", {})[key] = {"error": f"{type(e).__name__}: {e}"}
             import gc
@@ -789,7 +815,8 @@ def main():
     ap.add_argument("--sur-runs", type=int, default=12, help="randomized runs that give the training pairs")
     ap.add_argument("--sur-pairs", type=int, default=6, help="training pairs per run")
     ap.add_argument("--sur-cells", type=int, default=64, help="cells per axis of the training runs' box")
-    ap.add_argument("--sur-epochs", type=int, default=20)
+    ap.add_argument("--sur-epochs", type=int, default=80)
+    ap.add_argument("--sur-curl", type=float, default=1.0, help="weight of the curl term in the surrogate's loss")
     ap.add_argument("--sur-judge", type=int, default=8, help="judge the surrogate every this many steps")
     ap.add_argument("--sur-bound", type=float, default=1e-3, help="judge bound on the relative B error")
     ap.add_argument("--acc-steps", type=int, default=1000,
@@ -798,6 +825,7 @@ def main():
                     help="workloads run at their stated size by both the FP64 drop-in and the FP32 form")
     ap.add_argument("--acc2-steps", type=int, default=100, help="ion steps of the 256x128x128 pickup-ion comparison")
     ap.add_argument("--acc3-steps", type=int, default=20, help="ion steps of the 512x256x256 pickup-ion comparison")
+    ap.add_argument("--acc-marks", default="", help="steps at which the comparisons also record both energies")
     ap.add_argument("--acc-cx", default="both", choices=["both", "on", "off"],
                     help="comparisons with charge exchange as stated (on), off (no sampling difference), or both")
     ap.add_argument("--only-accuracy", action="store_true", help="run the accuracy legs alone")

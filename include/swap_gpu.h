@@ -395,9 +395,10 @@ int swap_conv3_check(int32_t nx, int32_t ny, int32_t nz, int32_t cin, int32_t co
 
 /* ---- the learned field-subcycle surrogate (FP32 form) ----
  * A 3D convolutional network (swap_surrogate_layers periodic 3x3x3 layers,
- * 11 -> 32 -> ... -> 32 -> 3 channels, GELU; BF16 weights and activations,
+ * 14 -> 32 -> ... -> 32 -> 3 channels, GELU; BF16 weights and activations,
  * FP32 accumulation on the tensor cores) maps the state at the start of the
- * field subcycles (B, u_p, n_p, p_e, and E0, the plain E there) to the
+ * field subcycles (B, u_p, n_p, p_e, E0, the plain E there, and B - b12,
+ * the change over the last subcycle that the leapfrog predictor starts from) to the
  * step's mean corrector E minus E0; B then advances as B - dt curl E, so
  * div B stays where it was.  It is trained on pairs the plain subcycles of
  * swap_surrogate_collect produce, with Adam.
@@ -419,20 +420,24 @@ int swap_surrogate_samples(swap_surrogate* net, int32_t* n);
 int swap_surrogate_train(swap_surrogate* net, int32_t epochs, double lr, double* loss);
 int swap_surrogate_loss(swap_surrogate* net, double* loss);
 int swap_surrogate_set_curl_weight(swap_surrogate* net, double curl_w, double kref2);
+/* relative != 0: each pair's loss and gradient scaled by kref2 over its own
+ * mean |curl target|^2 (clamped to [0.1, 100]), so every pair counts by its
+ * relative error. */
+int swap_surrogate_set_pair_weighting(swap_surrogate* net, int32_t relative);
 /* The network's depth (conv layers). */
 int swap_surrogate_layers(int32_t* n);
 int swap_surrogate_attach(swap_ctx* ctx, swap_surrogate* net, int32_t judge_every, double bound);
 /* [0] steps by the network, [1] judged steps, [2] fallbacks, [3] last judged
  * B rel-L2, [4] last judged (B - b0) rel-L2. */
 int swap_surrogate_stats(swap_ctx* ctx, double out[5]);
-/* Test access: normalisation (11 input means and stds, output scale) and
+/* Test access: normalisation (14 input means and stds, output scale) and
  * FP32 master weights of a layer ([27][cout][cin] with (cin, cout) = (16,32)
  * for the first, (32,16) for the last and (32,32) between: padded channels
  * zero) with its bias; get or set. */
 int swap_surrogate_norm(swap_surrogate* net, float* mean, float* stdv, float* out_mean, float* out_std,
                         int32_t set);
 int swap_surrogate_weights(swap_surrogate* net, int32_t layer, float* w, float* b, int32_t set);
-/* One forward and backward pass on device inputs [V][11] and targets [V][3]
+/* One forward and backward pass on device inputs [V][14] and targets [V][3]
  * of an nx*ny*nz box: loss = 0.5 mean((out - (tgt - out_mean)/out_std)^2)
  * (plus 0.5 curl_w mean |curl e|^2 / kref2 with a curl weight), gradients of
  * every layer into grads as (gW0, gb0, gW1, gb1, ...). */

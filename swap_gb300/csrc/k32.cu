@@ -1103,6 +1103,8 @@ __global__ void k_grid_to_voxels(G32 g, const float* __restrict__ db, const floa
                                  const float* __restrict__ up, const float* __restrict__ np, float te,
                                  const float* __restrict__ ct, const float* __restrict__ aj,
                                  const float* __restrict__ nu, const float* __restrict__ gpf,
+                                 const float* __restrict__ b1h, const float* __restrict__ b1l,
+                                 const float* __restrict__ b12h, const float* __restrict__ b12l,
                                  float* __restrict__ out) {
   GSTRIDE(v, n_int(g)) {
     int i, j, k;
@@ -1120,6 +1122,9 @@ __global__ void k_grid_to_voxels(G32 g, const float* __restrict__ db, const floa
     r[8] = ct ? e_o<0>(g, ct, nu, aj, gpf, o) : 0.0f;
     r[9] = ct ? e_o<1>(g, ct, nu, aj, gpf, o) : 0.0f;
     r[10] = ct ? e_o<2>(g, ct, nu, aj, gpf, o) : 0.0f;
+#pragma unroll
+    for (int m = 0; m < 3; ++m)
+      r[11 + m] = b12h ? (b1h[o + C * m] - b12h[o + C * m]) + (b1l[o + C * m] - b12l[o + C * m]) : 0.0f;
   }
 }
 
@@ -1753,9 +1758,11 @@ cudaError_t df_lerp(const G32& g, const float* nh, const float* nl, const float*
   RET((k_df_lerp<<<grid, blk, 0, st>>>(g, nh, nl, oh, f, rh, rl)));
 }
 cudaError_t grid_to_voxels(const G32& g, const float* db, const float* b0c, const float* up, const float* np,
-                           float te, const float* ct, const float* aj, const float* nu, const float* gpf, float* out,
+                           float te, const float* ct, const float* aj, const float* nu, const float* gpf,
+                           const float* b1h, const float* b1l, const float* b12h, const float* b12l, float* out,
                            cudaStream_t st) {
-  RET((k_grid_to_voxels<<<nblk(n_int(g)), TPB, 0, st>>>(g, db, b0c, up, np, te, ct, aj, nu, gpf, out)));
+  RET((k_grid_to_voxels<<<nblk(n_int(g)), TPB, 0, st>>>(g, db, b0c, up, np, te, ct, aj, nu, gpf, b1h, b1l, b12h,
+                                                         b12l, out)));
 }
 cudaError_t judge_sums(const G32& g, const float* ah, const float* al, const float* bh, const float* bl,
                        const float* b0c, double* acc3, cudaStream_t st) {

@@ -26,8 +26,10 @@ constexpr int TNODES_IN = TN_IN * TN_IN * TN_IN;  // 125
 __host__ __device__ constexpr int pass_tile(int pass) { return pass == 3 ? TN : TN_IN; }
 constexpr int NDIR = 27;              // displacements in {-1,0,1}^3
 constexpr int MAX_SPECIES = 16;
-// Inputs per voxel of the field surrogate: B (3), u_p (3), n_p, p_e, E0 (3).
-constexpr int SUR_NIN = 11;
+// Inputs per voxel of the field surrogate: B (3), u_p (3), n_p, p_e, E0 (3),
+// and B - b12 (3), the change over the last subcycle (the predictor is a
+// leapfrog from b12, so the subcycles depend on it as well as on B).
+constexpr int SUR_NIN = 14;
 
 struct G32 {
   int nx, ny, nz;     // nodes incl. ghosts
@@ -204,9 +206,11 @@ cudaError_t b_step_given_e(const G32& g, const float* E, const float* bh, const 
 cudaError_t df_lerp(const G32& g, const float* nh, const float* nl, const float* oh, float f, float* rh, float* rl,
                     cudaStream_t st);
 // Surrogate inputs per interior node, FP32 [V][SUR_NIN]: B, u_p, n_p,
-// te*n_p and E0 = ct + nu aj (zero when ct is null).
+// te*n_p, E0 = ct + nu aj (zero when ct is null) and B - b12 from the
+// double-float levels (b1h, b1l) and (b12h, b12l) (zero when b12h is null).
 cudaError_t grid_to_voxels(const G32& g, const float* db, const float* b0c, const float* up, const float* np,
-                           float te, const float* ct, const float* aj, const float* nu, const float* gpf, float* out,
+                           float te, const float* ct, const float* aj, const float* nu, const float* gpf,
+                           const float* b1h, const float* b1l, const float* b12h, const float* b12l, float* out,
                            cudaStream_t st);
 // Sums over the interior of |B_a - B_b|^2, |B_b|^2 and |B_b - b0|^2.
 cudaError_t judge_sums(const G32& g, const float* ah, const float* al, const float* bh, const float* bl,

@@ -496,7 +496,7 @@ extern "C" int swap_conv3_check(int32_t nx, int32_t ny, int32_t nz, int32_t cin,
 }
 
 // ---------------------------------------------------------------------------
-// the network: NL periodic 3x3x3 conv layers, 11 -> 32 -> ... -> 32 -> 3
+// the network: NL periodic 3x3x3 conv layers, 14 -> 32 -> ... -> 32 -> 3
 // channels, GELU between them; BF16 weights and activations, FP32
 // accumulation, FP32 master weights trained with Adam
 // ---------------------------------------------------------------------------
@@ -507,7 +507,7 @@ namespace {
 // subcycles move grid-scale whistler waves several cells within one ion
 // step, so the correction at a node depends on a wide neighbourhood.
 #ifndef SWAP_SUR_LAYERS
-#define SWAP_SUR_LAYERS 8
+#define SWAP_SUR_LAYERS 4
 #endif
 constexpr int NL = SWAP_SUR_LAYERS;
 constexpr double WARMUP = 200.0;  // Adam updates of the learning-rate warm-up
@@ -521,12 +521,13 @@ constexpr LayerDims layer_dims(bool in) {
   for (int l = 0; l < NL; ++l) d.v[l] = in ? (l == 0 ? 16 : 32) : (l == NL - 1 ? 16 : 32);
   return d;
 }
-constexpr LayerDims LCIN = layer_dims(true);    // layer 0: 11 input channels padded to 16
+constexpr LayerDims LCIN = layer_dims(true);    // layer 0: 14 input channels padded to 16
 constexpr LayerDims LCOUT = layer_dims(false);  // last layer: 3 output channels padded to 16
 // Inputs per voxel: B (3), u_p (3), n_p, p_e, and E0 (3), the plain scheme's
 // E at the start of the field step (the layout k32's voxel kernels write);
 // output: the mean corrector E of the subcycles minus E0.
-constexpr int NIN = 11, NOUT = 3;
+constexpr int NIN = 14, NOUT = 3;
+static_assert(NIN <= 16, "the first layer's input is padded to 16 channels");
 
 __device__ __forceinline__ float gelu_grad(float x) {
   const float t = tanh_hw(GELU_K0 * fmaf(GELU_K1 * x, x * x, x));
@@ -777,13 +778,18 @@ struct swap_surrogate {
   float *gw[NL] = {}, *gb[NL] = {}, *mw[NL] = {}, *vw[NL] = {}, *mb[NL] = {}, *vb[NL] = {};
   long long adam_t = 0;
   // normalisation: inputs (x - mean) / std, outputs (E - mean) / std
-  float in_mean[NIN] = {}, in_std[NIN] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1};
+  float in_mean[NIN] = {}, in_std[NIN] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1};
   OutNorm on{{0, 0, 0}, {1, 1, 1}};
   bool normed = false;
   // loss: 0.5 mean r^2 + 0.5 curl_w * mean |curl e|^2 / kref2 (r the
   // normalised error, e the physical one, kref2 = mean |curl tgt|^2)
   float curl_w = 0.0f;
   double kref2 = 0.0;
+  // per-pair weighting: pair k's loss and gradient scaled by kref2 / k2[k]
+  // (its own mean |curl tgt|^2, clamped to [0.1, 100]), so that each pair
+  // counts by its relative error, as the judge measures it
+  bool per_pair = false;
+  std::vector<double> ds_k2;
   float *d_mean = nullptr, *d_istd = nullptr;
   // the dataset, all of one grid shape (the first sample's)
   int ds_nx = 0, ds_ny = 0, ds_nz = 0;
@@ -1004,7 +1010,7 @@ int check_err(swap_surrogate* net) {
 
 namespace surr {
 
-// The network's output for FP32 inputs [V][11] (device) into ve [V][3] (device).
+// The network's output for FP32 inputs [V][14] (device) into ve [V][3] (device).
 int predict_e(swap_surrogate* net, int nx, int ny, int nz, const float* vin, float* ve, cudaStream_t st) {
   if (!net->normed) return fail(net, SWAP_EINVAL, "the surrogate has not been trained");
   int r = ensure_shape(net, nx, ny, nz);
@@ -1175,7 +1181,7 @@ extern "C" int swap_surrogate_weights(swap_surrogate* net, int32_t layer, float*
   return SWAP_OK;
 }
 
-// One forward and backward pass on device inputs vin [V][11] and targets tgt
+// One forward and backward pass on device inputs vin [V][14] and targets tgt
 // [V][3] (unnormalised) of an nx*ny*nz box: the loss 0.5*mean((out -
 // (tgt - out_mean)/out_std)^2) and the gradients of every layer, written to grads as
 // (gW[0], gb[0], gW[1], gb[1], ...).
@@ -1258,6 +1264,30 @@ static int fit_norm(swap_surrogate* net) {
   return upload_norm(net, nullptr);
 }
 
+// mean |curl tgt|^2 per voxel of every pair (once per dataset size)
+static int pair_k2(swap_surrogate* net) {
+  if (net->ds_k2.size() == net->ds_tgt.size()) return SWAP_OK;
+  int r;
+  if ((r = ensure_ds_shape(net))) return r;
+  net->ds_k2.clear();
+  for (float* t : net->ds_tgt) {
+    float* e = net->dy;
+    SCU(cudaMemsetAsync(net->acc, 0, 2 * sizeof(float), nullptr));
+    k_err3<<<nblk(net->V), 256>>>(net->V, nullptr, t, net->on, e);
+    k_curl3<<<nblk(net->V), 256>>>(net->nx, net->ny, net->nz, e, e + 3 * net->V, net->acc + 1);
+    float h = 0;
+    SCU(cudaMemcpy(&h, net->acc + 1, sizeof(float), cudaMemcpyDeviceToHost));
+    net->ds_k2.push_back((double)h / (double)net->V);
+  }
+  return SWAP_OK;
+}
+
+extern "C" int swap_surrogate_set_pair_weighting(swap_surrogate* net, int32_t relative) {
+  if (!net) return SWAP_EINVAL;
+  net->per_pair = relative != 0;
+  return SWAP_OK;
+}
+
 extern "C" int swap_surrogate_layers(int32_t* n) {
   if (!n) return SWAP_EINVAL;
   *n = NL;
@@ -1280,6 +1310,7 @@ extern "C" int swap_surrogate_train(swap_surrogate* net, int32_t epochs, double 
   const std::size_t n = net->ds_in.size();
   if (!n) return fail(net, SWAP_EINVAL, "the surrogate has no training samples");
   if ((r = ensure_ds_shape(net))) return r;
+  if (net->per_pair && (r = pair_k2(net))) return r;
   cudaStream_t st = nullptr;
   std::mt19937_64 rng(net->seed + 17 + (uint64_t)net->adam_t);
   std::vector<std::size_t> order(n);
@@ -1292,8 +1323,11 @@ extern "C" int swap_surrogate_train(swap_surrogate* net, int32_t epochs, double 
       k_norm_inputs<<<nblk(net->V), 256, 0, st>>>(net->V, net->ds_in[k], net->d_mean, net->d_istd, net->x0);
       if ((r = forward(net, true, st))) return r;
       double sq = 0;
-      if ((r = loss_grad(net, net->ds_tgt[k], 1.0f / (3.0f * (float)net->V), &sq, st))) return r;
-      tot += sq / (3.0 * (double)net->V);
+      const double wk = net->per_pair && net->ds_k2[k] > 0.0
+                            ? std::min(100.0, std::max(0.1, net->kref2 / net->ds_k2[k]))
+                            : 1.0;
+      if ((r = loss_grad(net, net->ds_tgt[k], (float)(wk / (3.0 * (double)net->V)), &sq, st))) return r;
+      tot += wk * sq / (3.0 * (double)net->V);
       // linear warm-up over the first WARMUP updates: Adam's first steps move
       // every weight by about lr at once, which can push a deep stack's
       // pre-activations where GELU is flat, and it then stops learning

@@ -594,7 +594,8 @@ static int sur_inputs(swap_ctx* c, F32State* s) {
   const G32& g = s->g;
   KL("f32_sur_inputs", aj_ct(g, false, s->db1, s->np, s->up, s->b0c, (float)c->prm.alpha, s->aj, s->ct, c->st));
   KL("f32_sur_inputs",
-     grid_to_voxels(g, s->db1, s->b0c, s->up, s->np, 1.0f, s->ct, s->aj, s->nu, s->gpf, s->vin, c->st));
+     grid_to_voxels(g, s->db1, s->b0c, s->up, s->np, 1.0f, s->ct, s->aj, s->nu, s->gpf, s->b1.h, s->b1.l, s->b12.h,
+                    s->b12.l, s->vin, c->st));
   return SWAP_OK;
 }
 

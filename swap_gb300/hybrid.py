@@ -466,9 +466,9 @@ class Surrogate:
 
     # inputs per voxel: B (3), u_p (3), n_p, p_e, and E0 (3), the plain E at the
     # start of the field step; the output is the mean corrector E minus E0
-    NIN = 11
+    NIN = 14
 
-    def __init__(self, seed: int = 1, max_samples: int = 4096, curl_weight: float = 0.0):
+    def __init__(self, seed: int = 1, max_samples: int = 4096, curl_weight: float = 0.0, per_pair: bool = False):
         self.lib = abi.load()
         n = C.c_int32()
         abi.check(self.lib, None, self.lib.swap_surrogate_layers(C.byref(n)))
@@ -479,6 +479,8 @@ class Surrogate:
         self.h = h
         if curl_weight:
             self.set_curl_weight(curl_weight)
+        if per_pair:
+            self._check(self.lib.swap_surrogate_set_pair_weighting(self.h, 1))
 
     def set_curl_weight(self, w: float, kref2: float = 0.0):
         """Add w * mean |curl e|^2 / kref2 to the loss (e the E error: curl e is

@@ -3,11 +3,13 @@
 The network stands in for the field subcycles of one ion step (maind.f:420-476)
 and is trained on pairs that the plain subcycles produce.  To cover the
 conditions it will meet, the pairs come from many short runs of a small
-box with an open x axis, each with its own upstream state: flow speed drawn
-uniform in 1-6 v_A and plasma beta in 0.1-2, and a neutral cloud (ionization
-and charge exchange, chem_rates.f:346-432, 805-843) of radius drawn in 2-10
-cells at the box centre (mixed=True: the cloud and the open x axis each in
-half of the runs).  Every run keeps the target
+box, each with its own upstream state: flow speed drawn uniform in 1-6 v_A
+and plasma beta in 0.1-2; an open x axis with inflow in half of the runs
+(periodic otherwise), and in half a neutral cloud (ionization and charge
+exchange, chem_rates.f:346-432, 805-843) of radius drawn in 2-10 cells at
+the box centre (mixed=False: every run has both).  The uniform, periodic
+boxes matter: trained on cloud runs alone, the network's judged B error on
+a source-free box was five times larger.  Every run keeps the target
 workload's B0, ion step, subcycle count and particles per cell, so the
 network learns the step it will replace.  All computation is the library's
 FP32 form on the GPU; this module only draws the parameters.
@@ -20,7 +22,7 @@ from .hybrid import Hybrid, RunConfig, config
 
 
 def run_config(base: RunConfig, rng: np.random.Generator, cells=(64, 64, 64), index: int = 0,
-               mixed: bool = False) -> RunConfig:
+               mixed: bool = True) -> RunConfig:
     """One randomized run around `base`: v_A = B0 (n0 = 1); the load's velocity
     spread sigma = vth/sqrt(2) per component gives beta = vth^2 / v_A^2.
     mixed: the cloud and the open x axis are each present in half of the
@@ -48,7 +50,7 @@ def run_config(base: RunConfig, rng: np.random.Generator, cells=(64, 64, 64), in
 
 
 def collect_randomized(net, base: RunConfig, runs: int, pairs_per_run: int, warmup: int = 4,
-                       cells=(64, 64, 64), seed: int = 0, mixed: bool = False) -> list:
+                       cells=(64, 64, 64), seed: int = 0, mixed: bool = True) -> list:
     """Add runs * pairs_per_run training pairs to `net` (a hybrid.Surrogate):
     each run loads its box, takes `warmup` plain FP32 steps so the upstream
     flow and the pickup ions develop, then collects one pair per step.
