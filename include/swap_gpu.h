@@ -126,6 +126,13 @@ int swap_set_exchange(swap_ctx* ctx, swap_exchange_fn fn, void* user);
  * swap_f32_begin again: the bound arrays still hold the state it began from).
  * 0 makes every wait give up at once, to test that path. */
 int swap_set_wait_limit(swap_ctx* ctx, uint32_t polls);
+/* on != 0: the FP64 drop-in's moment deposits (update_np, update_up and the
+ * fused steps') sum in 128-bit fixed point (units of 2^-60, |value| < 2^25
+ * per particle and corner, SWAP_ENONFINITE beyond) instead of FP64 atomics,
+ * then round once per node.  The result does not depend on the order of the
+ * GPU's adds: runs repeat bit for bit and a run resumed from a checkpoint
+ * equals the uninterrupted one.  Off by default (FP64 atomics). */
+int swap_set_deterministic(swap_ctx* ctx, int32_t on);
 
 /* ---- array registration and data movement ---- */
 /* The particle arrays of maind.f:54-59 and global.f:44,96,100; ijkp may be

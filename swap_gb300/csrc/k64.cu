@@ -274,7 +274,30 @@ __device__ __forceinline__ void corners(const Geo& g, int i, int j, int k, long 
 }
 
 // update_np deposit (gutsp.f:1461-1493) into the folded node.
-__global__ void k_deposit_np(Geo g, PartDev p, long long N, double beta, double* __restrict__ np, int* err) {
+// One value into a deterministic fixed-point sum (Fix64); a value out of
+// range or not finite is flagged instead (the conversions saturate).
+__device__ __forceinline__ void fix_add(const Fix64& f, long long t, double x, unsigned& bad) {
+  bad |= fabs(x) < 0x1p25 ? 0u : 1u;
+  const double xs = x * 0x1p28, h = floor(xs);
+  atomicAdd(reinterpret_cast<unsigned long long*>(f.h) + t, (unsigned long long)__double2ll_rn(h));
+  atomicAdd(f.l + t, __double2ull_rn((xs - h) * 0x1p32));
+}
+
+__global__ void k_fix_to_double(long long n, Fix64 f, double* __restrict__ out) {
+  GRID_STRIDE(t, n) {
+    const unsigned long long l = f.l[t];
+    // the sum is hh * 2^32 + (l mod 2^32) units of 2^-60
+    const long long hh = f.h[t] + (long long)(l >> 32);
+    const double a = (double)hh;            // rounds beyond 2^53
+    const long long r = hh - (long long)a;  // exact remainder
+    out[t] = fma(a, 0x1p-28, fma((double)r, 0x1p-28, (double)(l & 0xffffffffULL) * 0x1p-60));
+  }
+}
+
+template <bool DET>
+__global__ void k_deposit_np(Geo g, PartDev p, long long N, double beta, double* __restrict__ np, Fix64 fx,
+                             int* err) {
+  unsigned bad = 0;
   GRID_STRIDE(l, N) {
     const int i = p.ijk[l], j = p.ijk[l + p.NM], k = p.ijk[l + 2 * p.NM];
     if (!cell_ok(g, i, j, k)) {
@@ -284,17 +307,23 @@ __global__ void k_deposit_np(Geo g, PartDev p, long long N, double beta, double*
     const double volb = 1.0 / (g.dxg[i] * g.dyg[j] * g.dzg[k] * beta * p.beta_p[l]);
     long long tg[8];
     corner_targets(g, i, j, k, tg);
-    for (int c = 0; c < 8; ++c)
-      if (tg[c] >= 0) atomicAdd(np + tg[c], p.wght[l + c * p.NM] * volb);
+    for (int c = 0; c < 8; ++c) {
+      if (tg[c] < 0) continue;
+      if (DET) fix_add(fx, tg[c], p.wght[l + c * p.NM] * volb, bad);
+      else atomicAdd(np + tg[c], p.wght[l + c * p.NM] * volb);
+    }
   }
+  if (DET && bad) set_err(err, KERR_RANGE);
 }
 
 // update_up deposit (gutsp.f:1676-1800) without the per-node 1/np factor,
 // which ct_from_sums applies once per node: sum v*w/volb.
+template <bool DET>
 __global__ void k_deposit_u(Geo g, PartDev p, long long N, double beta, int mode, const double* __restrict__ va,
                             const double* __restrict__ vb, double* __restrict__ out_v1, double* __restrict__ S,
-                            int* err) {
+                            Fix64 fx, int* err) {
   const long long C = g.C;
+  unsigned bad = 0;
   GRID_STRIDE(l, N) {
     double v[3];
     const double sq = mode >= 3 ? sqrt(p.mrat[l]) : 1.0;
@@ -323,11 +352,18 @@ __global__ void k_deposit_u(Geo g, PartDev p, long long N, double beta, int mode
     for (int c = 0; c < 8; ++c) {
       if (tg[c] < 0) continue;
       const double w = p.wght[l + c * p.NM] * ivolb;
-      atomicAdd(S + tg[c], v[0] * w);
-      atomicAdd(S + tg[c] + C, v[1] * w);
-      atomicAdd(S + tg[c] + 2 * C, v[2] * w);
+      if (DET) {
+        fix_add(fx, tg[c], v[0] * w, bad);
+        fix_add(fx, tg[c] + C, v[1] * w, bad);
+        fix_add(fx, tg[c] + 2 * C, v[2] * w, bad);
+      } else {
+        atomicAdd(S + tg[c], v[0] * w);
+        atomicAdd(S + tg[c] + C, v[1] * w);
+        atomicAdd(S + tg[c] + 2 * C, v[2] * w);
+      }
     }
   }
+  if (DET && bad) set_err(err, KERR_RANGE);
 }
 
 // update_rho deposit (gutsp.f:1543-1567): (w/mrat)/volb.
@@ -653,14 +689,19 @@ cudaError_t interp_weights(const Geo& g, const PartDev& p, long long N, int* err
   LAUNCH(k_weights, N, g, p, N, err);
 }
 cudaError_t deposit_np(const Geo& g, const PartDev& p, long long N, double beta, double* np, int* err,
-                       cudaStream_t st) {
+                       cudaStream_t st, Fix64 fix) {
   if (N <= 0) return cudaSuccess;
-  LAUNCH(k_deposit_np, N, g, p, N, beta, np, err);
+  if (fix.h) LAUNCH(k_deposit_np<true>, N, g, p, N, beta, np, fix, err);
+  LAUNCH(k_deposit_np<false>, N, g, p, N, beta, np, fix, err);
 }
 cudaError_t deposit_u(const Geo& g, const PartDev& p, long long N, double beta, int mode, const double* va,
-                      const double* vb, double* out_v1, double* S, int* err, cudaStream_t st) {
+                      const double* vb, double* out_v1, double* S, int* err, cudaStream_t st, Fix64 fix) {
   if (N <= 0) return cudaSuccess;
-  LAUNCH(k_deposit_u, N, g, p, N, beta, mode, va, vb, out_v1, S, err);
+  if (fix.h) LAUNCH(k_deposit_u<true>, N, g, p, N, beta, mode, va, vb, out_v1, S, fix, err);
+  LAUNCH(k_deposit_u<false>, N, g, p, N, beta, mode, va, vb, out_v1, S, fix, err);
+}
+cudaError_t fix_to_double(long long n, Fix64 fix, double* out, cudaStream_t st) {
+  LAUNCH(k_fix_to_double, n, n, fix, out);
 }
 cudaError_t deposit_rho(const Geo& g, const PartDev& p, long long N, double beta, double* mnp, int* err,
                         cudaStream_t st) {

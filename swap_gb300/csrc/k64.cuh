@@ -39,12 +39,25 @@ cudaError_t grad_pe_face_int(const Geo& g, const double* np, double grad_pe, dou
 
 // gutsp.f particle operators
 cudaError_t interp_weights(const Geo& g, const PartDev& p, long long N, int* err, cudaStream_t st);
+// Deterministic deposits: each added value x goes into a 128-bit fixed-point
+// sum in units of 2^-60, as floor(x * 2^28) into a signed 64-bit word (h)
+// and the rest * 2^32, rounded, into an unsigned one (l).  Integer adds are
+// exact and commutative, so the sum does not depend on the order of the
+// GPU's atomics; |x| < 2^25 per value (SWAP_ENONFINITE otherwise).
+struct Fix64 {
+  long long* h;
+  unsigned long long* l;
+};
+// fix (h, l null: plain FP64 atomics into np) ...
 cudaError_t deposit_np(const Geo& g, const PartDev& p, long long N, double beta, double* np, int* err,
-                       cudaStream_t st);
+                       cudaStream_t st, Fix64 fix = Fix64{nullptr, nullptr});
+// out[t] = the fixed-point sums (h[t], l[t]) rounded to FP64, t < n.
+cudaError_t fix_to_double(long long n, Fix64 fix, double* out, cudaStream_t st);
 // mode: 0 = v, 1 = 1.5 v - 0.5 v1 (extrapol_up), 2 = 0.5 (a + b) (improve_up, also stores into out_v1),
 // 3 = (v/sqrt(mrat))^2 and 4 = v/sqrt(mrat) per component (get_temperature)
 cudaError_t deposit_u(const Geo& g, const PartDev& p, long long N, double beta, int mode, const double* va,
-                      const double* vb, double* out_v1, double* S, int* err, cudaStream_t st);
+                      const double* vb, double* out_v1, double* S, int* err, cudaStream_t st,
+                      Fix64 fix = Fix64{nullptr, nullptr});
 cudaError_t ct_from_sums(const Geo& g, const double* S, const double* np, double* ct, cudaStream_t st);
 // update_rho deposit (folded into the interior), interior scaling, and the
 // temperature of get_temperature from the two face moments.

@@ -188,6 +188,8 @@ int swap_ctx::finish() {
     if (herr == KERR_DOMAIN) return fail(SWAP_EDOMAIN, "a particle lies outside the grid");
     if (herr == KERR_MOVE) return fail(SWAP_EMOVE, "a particle moved more than one cell in one step");
     if (herr == KERR_WAIT) return fail(SWAP_EWAIT, "a device wait reached its iteration limit");
+    if (herr == KERR_RANGE)
+      return fail(SWAP_ENONFINITE, "a deposited value is not finite or beyond the deterministic sums' range (2^25)");
     return fail(SWAP_ECUDA, "device error flag " + std::to_string(herr));
   }
   return SWAP_OK;
@@ -376,10 +378,34 @@ int need_weights(swap_ctx* c) {
 }
 
 // update_np (gutsp.f:1441-1512)
+// The fixed-point sums of the deterministic deposits, n values, zeroed.
+static int fix_sums(swap_ctx* c, long long n, swapk::Fix64* f) {
+  if (!c->fix.h) {
+    void *h = nullptr, *l = nullptr;
+    const std::size_t b = 3 * (std::size_t)c->g.C * 8;
+    if (cudaMalloc(&h, b) != cudaSuccess) return c->fail(SWAP_ECUDA, "deterministic deposit sums");
+    c->owned.push_back(h);
+    if (cudaMalloc(&l, b) != cudaSuccess) return c->fail(SWAP_ECUDA, "deterministic deposit sums");
+    c->owned.push_back(l);
+    c->fix = swapk::Fix64{static_cast<long long*>(h), static_cast<unsigned long long*>(l)};
+  }
+  KL("cudaMemsetAsync", cudaMemsetAsync(c->fix.h, 0, (std::size_t)n * 8, c->st));
+  KL("cudaMemsetAsync", cudaMemsetAsync(c->fix.l, 0, (std::size_t)n * 8, c->st));
+  *f = c->fix;
+  return 0;
+}
+
 int update_np(swap_ctx* c, double* np) {
   TRY(need_weights(c));
-  KL("cudaMemsetAsync", cudaMemsetAsync(np, 0, (std::size_t)c->g.C * sizeof(double), c->st));
-  KL("deposit_np", deposit_np(c->g, c->part_view(), c->ntot(), c->prm.beta, np, c->d_err, c->st));
+  if (c->deterministic) {
+    swapk::Fix64 f;
+    TRY(fix_sums(c, c->g.C, &f));
+    KL("deposit_np", deposit_np(c->g, c->part_view(), c->ntot(), c->prm.beta, np, c->d_err, c->st, f));
+    KL("fix_to_double", fix_to_double(c->g.C, f, np, c->st));
+  } else {
+    KL("cudaMemsetAsync", cudaMemsetAsync(np, 0, (std::size_t)c->g.C * sizeof(double), c->st));
+    KL("deposit_np", deposit_np(c->g, c->part_view(), c->ntot(), c->prm.beta, np, c->d_err, c->st));
+  }
   if (c->fused) TRY(c->exchange(np, c->g.C, 8));  // MPI_ALLREDUCE, gutsp.f:1503
   KL("periodic", periodic1(c->g, np, c->st));
   return 0;
@@ -391,8 +417,17 @@ int update_up_mode(swap_ctx* c, int mode, const double* va, const double* vb, do
                    double* up) {
   TRY(need_weights(c));
   const std::size_t b3 = 3 * (std::size_t)c->g.C * sizeof(double);
-  KL("cudaMemsetAsync", cudaMemsetAsync(c->s_S, 0, b3, c->st));
-  KL("deposit_u", deposit_u(c->g, c->part_view(), c->ntot(), c->prm.beta, mode, va, vb, out_v1, c->s_S, c->d_err, c->st));
+  if (c->deterministic) {
+    swapk::Fix64 f;
+    TRY(fix_sums(c, 3 * c->g.C, &f));
+    KL("deposit_u",
+       deposit_u(c->g, c->part_view(), c->ntot(), c->prm.beta, mode, va, vb, out_v1, c->s_S, c->d_err, c->st, f));
+    KL("fix_to_double", fix_to_double(3 * c->g.C, f, c->s_S, c->st));
+  } else {
+    KL("cudaMemsetAsync", cudaMemsetAsync(c->s_S, 0, b3, c->st));
+    KL("deposit_u",
+       deposit_u(c->g, c->part_view(), c->ntot(), c->prm.beta, mode, va, vb, out_v1, c->s_S, c->d_err, c->st));
+  }
   if (c->fused) TRY(c->exchange(c->s_S, 3 * c->g.C, 8));  // MPI_ALLREDUCE, gutsp.f:1812-1822
   KL("ct_from_sums", ct_from_sums(c->g, c->s_S, np, c->s_ct, c->st));
   KL("periodic", periodic3(c->g, c->s_ct, c->st));
@@ -652,6 +687,12 @@ extern "C" int swap_set_host_direct(swap_ctx* c, int on) {
       return c->fail(SWAP_EINVAL, "this device cannot address host memory directly");
   }
   c->host_direct = on != 0;
+  return SWAP_OK;
+}
+
+extern "C" int swap_set_deterministic(swap_ctx* c, int32_t on) {
+  if (!c) return SWAP_EINVAL;
+  c->deterministic = on != 0;
   return SWAP_OK;
 }
 

@@ -62,6 +62,10 @@ struct swap_ctx {
   void* xuser = nullptr;
   bool fused = false;  // inside a fused FP64 step: its deposits are exchanged
   uint32_t wait_polls = 1u << 22;  // bound of the device waits (swap_set_wait_limit)
+  // deterministic FP64 deposits (swap_set_deterministic): fixed-point sums
+  // for up to 3 C values, allocated on first use
+  bool deterministic = false;
+  swapk::Fix64 fix{nullptr, nullptr};
   float* stage32 = nullptr;   // device staging of those conversions
   std::size_t stage32_n = 0;  // its capacity in floats
   int64_t h2d_bytes = 0, d2h_bytes = 0;  // bytes moved between the caller's memory and the device

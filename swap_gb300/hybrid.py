@@ -443,6 +443,10 @@ class Hybrid:
         self._check(self.lib.swap_f32_key_starts(self.ctx, out.ctypes.data_as(abi.c_int64_p), nk + 1))
         return out
 
+    def set_deterministic(self, on: bool = True):
+        """FP64 deposits in fixed point: order-independent, bit-reproducible."""
+        self._check(self.lib.swap_set_deterministic(self.ctx, 1 if on else 0))
+
     def f32_far_movers(self) -> int:
         """Ions that moved more than one cell per axis in a step since f32_begin."""
         n = C.c_int64()
