@@ -82,7 +82,7 @@ class RunConfig:
 
     def ni_max_hint(self, steps: int | None = None) -> int:
         """Particle capacity with headroom for a workload whose count varies:
-        5% for inflow and outflow, plus the cloud's new ions over `steps`
+        10% for inflow and outflow, plus the cloud's new ions over `steps`
         (default: the workload's step count), plus, with charge exchange, every
         ion that enters in that time: an exchanged ion is heavy and at rest,
         and stays in the box far longer than the step count."""
@@ -92,7 +92,7 @@ class RunConfig:
         per_step = self.cloud_ions_per_step()
         if self.sources.get("cx_a"):
             per_step += self.inflow_ions_per_step()
-        return int(n * 1.05 + 1.1 * per_step * (self.steps if steps is None else steps)) + 4096
+        return int(n * 1.10 + 1.1 * per_step * (self.steps if steps is None else steps)) + 4096
 
 
 def config(n: int, **over) -> RunConfig:
