@@ -162,7 +162,7 @@ KERNEL_BYTES_F32 = {
 # (dram__bytes_read.sum + dram__bytes_write.sum over one launch at 128x64x64
 # cells, 16 ppc, 8.4M particles); the roofline's traffic is this figure times
 # the particles of a launch.
-KERNEL_TRAFFIC_F32 = {"f32_P1": 42.8, "f32_P2": 32.4, "f32_P3": 64.8, "f32_sort_scatter": 86.0}
+KERNEL_TRAFFIC_F32 = {"f32_P1": 44.4, "f32_P2": 34.1, "f32_P3": 70.5, "f32_sort_scatter": 86.0}
 # per interior node (FP32 fields, double-float B levels of 8 B per component)
 NODE_BYTES_F32 = {
     "f32_curlB": 12 + 4 + 12,
