@@ -898,130 +898,6 @@ __global__ void __launch_bounds__(FBX * FBY) k_aj_ct(G32 g, const float* __restr
   store_img(g, ct + 2 * C, i, j, k, ax * by - ay * bx);
 }
 
-// The three components of edge_to_center one at a time (the arithmetic of
-// e2c_o, which the corrector's 1-2-1 averages need at different neighbours).
-__device__ __forceinline__ float e2c_x(const G32& g, const float* __restrict__ bt, long long o) {
-  const long long sy = g.nx, sz = (long long)g.nx * g.ny;
-  const float b2 = 0.5f * (bt[o] + bt[o - sy]);
-  const float b1 = 0.5f * (bt[o - sz] + bt[o - sy - sz]);
-  return 0.5f * (b1 + b2);
-}
-__device__ __forceinline__ float e2c_y(const G32& g, const float* __restrict__ bt, long long o) {
-  const long long sz = (long long)g.nx * g.ny;
-  const float* B = bt + g.C;
-  const float b2 = 0.5f * (B[o] + B[o - 1]);
-  const float b1 = 0.5f * (B[o - sz] + B[o - 1 - sz]);
-  return 0.5f * (b1 + b2);
-}
-__device__ __forceinline__ float e2c_z(const G32& g, const float* __restrict__ bt, long long o) {
-  const long long sy = g.nx;
-  const float* B = bt + 2 * g.C;
-  const float b2 = 0.5f * (B[o] + B[o - sy]);
-  const float b1 = 0.5f * (B[o - 1] + B[o - 1 - sy]);
-  return 0.5f * (b1 + b2);
-}
-
-// k_aj_ct with each aj and edge-to-centre value computed once: a block of
-// 32 x 4 nodes marches along z through AJCT_KZ planes; the x neighbours come
-// from the next lane (shuffles), the y neighbours from the next warp (shared
-// memory, double-buffered by plane), the z neighbours from the previous or
-// next plane (carried in registers).  Lanes at a tile edge compute their
-// neighbour themselves, at its interior image (periodic).  The same
-// arithmetic as k_aj_ct, so the same bits.
-constexpr int AJCT_KZ = 16;
-template <bool CORR>
-__global__ void __launch_bounds__(FBX * FBY, 8) k_aj_ct_z(G32 g, const float* __restrict__ db,
-                                                       const float* __restrict__ np, const float* __restrict__ up,
-                                                       const float* __restrict__ b0c, float alpha,
-                                                       float* __restrict__ aj, float* __restrict__ ct) {
-  __shared__ float s_a2[2][FBY][FBX];
-  __shared__ float s_c2[2][FBY][FBX];
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int iv = blockIdx.x * FBX + tx + 2, jv = blockIdx.y * FBY + ty + 2;
-  const bool valid = iv <= g.ncx + 1 && jv <= g.ncy + 1;
-  // lanes past the grid work on the last node, so that every lane takes part
-  // in the shuffles with a defined value
-  const int i = min(iv, g.ncx + 1), j = min(jv, g.ncy + 1);
-  const int k0 = 2 + (int)blockIdx.z * AJCT_KZ, k1 = min(k0 + AJCT_KZ, g.ncz + 2);
-  const int im = img(i - 1, g.nx), ip = img(i + 1, g.nx), jm = img(j - 1, g.ny), jp = img(j + 1, g.ny);
-  const bool self_right = tx == FBX - 1 || iv + 1 > g.ncx + 1;  // the next lane is not node i+1
-  const bool self_up = ty == FBY - 1 || jv + 1 > g.ncy + 1;     // the next warp is not node j+1
-  const long long C = g.C, sy = g.nx, sz = (long long)g.nx * g.ny;
-  float a3m = aj_o<2>(g, db, np, alpha, nid(g, i, j, img(k0 - 1, g.nz)));  // aj_z one plane below
-  float c3m = 0.f, c3 = 0.f;
-  if (CORR) {
-    c3m = e2c_z(g, db, nid(g, i, j, img(k0 - 1, g.nz)));
-    c3 = e2c_z(g, db, nid(g, i, j, k0));
-  }
-  for (int k = k0; k < k1; ++k) {
-    const int buf = k & 1;
-    const long long o = nid(g, i, j, k);
-    const float a1 = aj_o<0>(g, db, np, alpha, o);
-    const float a2 = aj_o<1>(g, db, np, alpha, o);
-    const float a3 = aj_o<2>(g, db, np, alpha, o);
-    float c1 = 0.f, c2 = 0.f, c3p = 0.f;
-    s_a2[buf][ty][tx] = a2;
-    if (CORR) {
-      c1 = e2c_x(g, db, o);
-      c2 = e2c_y(g, db, o);
-      c3p = e2c_z(g, db, nid(g, i, j, img(k + 1, g.nz)));
-      s_c2[buf][ty][tx] = c2;
-    }
-    float a1m = __shfl_up_sync(0xffffffffu, a1, 1);
-    float c1m = 0.f, c1p = 0.f;
-    if (CORR) {
-      c1m = __shfl_up_sync(0xffffffffu, c1, 1);
-      c1p = __shfl_down_sync(0xffffffffu, c1, 1);
-    }
-    if (tx == 0) {
-      const long long om = nid(g, im, j, k);
-      a1m = aj_o<0>(g, db, np, alpha, om);
-      if (CORR) c1m = e2c_x(g, db, om);
-    }
-    if (CORR && self_right) c1p = e2c_x(g, db, nid(g, ip, j, k));
-    __syncthreads();
-    const float a2m = ty > 0 ? s_a2[buf][ty - 1][tx] : aj_o<1>(g, db, np, alpha, nid(g, i, jm, k));
-    float bx, by, bz;
-    if (CORR) {
-      const float c2m = ty > 0 ? s_c2[buf][ty - 1][tx] : e2c_y(g, db, nid(g, i, jm, k));
-      const float c2p = !self_up ? s_c2[buf][ty + 1][tx] : e2c_y(g, db, nid(g, i, jp, k));
-      bx = 0.25f * (c1m + 2.0f * c1 + c1p);
-      by = 0.25f * (c2m + 2.0f * c2 + c2p);
-      bz = 0.25f * (c3m + 2.0f * c3 + c3p);
-    } else {
-      e2c_o(g, db, o, bx, by, bz);
-    }
-    bx += b0c[0];
-    by += b0c[1];
-    bz += b0c[2];
-    const float ax = 0.5f * ((a1 - up[o]) + (a1m - up[o - 1]));
-    const float ay = 0.5f * ((a2 - up[o + C]) + (a2m - up[o - sy + C]));
-    const float az = 0.5f * ((a3 - up[o + 2 * C]) + (a3m - up[o - sz + 2 * C]));
-    if (valid) {
-      if (inner_node(g, i, j, k)) {
-        aj[o] = a1;
-        aj[o + C] = a2;
-        aj[o + 2 * C] = a3;
-        ct[o] = ay * bz - az * by;
-        ct[o + C] = az * bx - ax * bz;
-        ct[o + 2 * C] = ax * by - ay * bx;
-      } else {
-        store_img(g, aj, i, j, k, a1);
-        store_img(g, aj + C, i, j, k, a2);
-        store_img(g, aj + 2 * C, i, j, k, a3);
-        store_img(g, ct, i, j, k, ay * bz - az * by);
-        store_img(g, ct + C, i, j, k, az * bx - ax * bz);
-        store_img(g, ct + 2 * C, i, j, k, ax * by - ay * bx);
-      }
-    }
-    a3m = a3;
-    if (CORR) {
-      c3m = c3;
-      c3 = c3p;
-    }
-  }
-}
-
 // Component m of E = face average of ct + nu*aj at node (i,j,k) (gutsf.f:
 // 94-96, 1082), less the electron-pressure face gradient gpf when given
 // (the isothermal extension of the commented "- gradP", gutsf.f:1083,1283).
@@ -1849,9 +1725,9 @@ cudaError_t curlB32(const G32& g, const float* dbt, const float* np, float alpha
 }
 cudaError_t aj_ct(const G32& g, bool corr, const float* db, const float* np, const float* up, const float* b0c,
                   float alpha, float* aj, float* ct, cudaStream_t st) {
-  const dim3 grid((g.ncx + FBX - 1) / FBX, (g.ncy + FBY - 1) / FBY, (g.ncz + AJCT_KZ - 1) / AJCT_KZ), blk(FBX, FBY);
-  if (corr) RET((k_aj_ct_z<true><<<grid, blk, 0, st>>>(g, db, np, up, b0c, alpha, aj, ct)));
-  RET((k_aj_ct_z<false><<<grid, blk, 0, st>>>(g, db, np, up, b0c, alpha, aj, ct)));
+  const dim3 grid((g.ncx + FBX - 1) / FBX, (g.ncy + FBY - 1) / FBY, g.ncz), blk(FBX, FBY);
+  if (corr) RET((k_aj_ct<true><<<grid, blk, 0, st>>>(g, db, np, up, b0c, alpha, aj, ct)));
+  RET((k_aj_ct<false><<<grid, blk, 0, st>>>(g, db, np, up, b0c, alpha, aj, ct)));
 }
 cudaError_t b_step(const G32& g, bool pred, bool write_e, const float* ct, const float* nu, const float* aj,
                    const float* gpf, const float* bh, const float* bl, double coef, const float* b0c, float* oh,
