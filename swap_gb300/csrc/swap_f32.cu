@@ -78,10 +78,18 @@ struct F32State {
   // fields advance (the staging draws in FP64, the field kernels stream HBM)
   cudaStream_t side = nullptr;
   cudaEvent_t ev_main = nullptr, ev_side = nullptr;
+  // the step's sort runs on the second stream too, beside the field
+  // subcycles (it reads only pass 3's outputs and the staging): its end, and
+  // the new ion count it copies to pinned host memory
+  cudaEvent_t ev_sort = nullptr;
+  int64_t* h_n = nullptr;
+  bool sort_pending = false;
   ~F32State() {
     if (side) cudaStreamSynchronize(side);
     if (ev_main) cudaEventDestroy(ev_main);
     if (ev_side) cudaEventDestroy(ev_side);
+    if (ev_sort) cudaEventDestroy(ev_sort);
+    if (h_n) cudaFreeHost(h_n);
     if (side) cudaStreamDestroy(side);
     srcops::stage_free(stage);
     for (void* p : owned) cudaFree(p);
@@ -175,7 +183,7 @@ struct PreStaged {
   const int64_t* n_dev = nullptr;
 };
 static int sort_step(swap_ctx* c, F32State* s, long long src_step, bool prepared = false,
-                     const PreStaged* pre = nullptr);
+                     const PreStaged* pre = nullptr, bool on_side = false);
 
 // ---------------------------------------------------------------------------
 
@@ -508,14 +516,52 @@ static int subcycles(swap_ctx* c, F32State* s, float* e_acc = nullptr) {
 // with src_step >= 0 the new ions of that step's sources are placed after the
 // arrivals of their cell, flagged fresh.  prepared: pass 3 already wrote the
 // directions, ranks and per-key counts.
-static int sort_step(swap_ctx* c, F32State* s, long long src_step, bool prepared, const PreStaged* pre) {
+static int sort_body(swap_ctx* c, F32State* s, long long src_step, bool prepared, const PreStaged* pre,
+                     bool on_side);
+static int side_stream(swap_ctx* c, F32State* s);
+// on_side: the sort goes to the second stream after the main stream's work
+// so far and the staging; sort_join (after the field step) waits for it and
+// takes the new count.
+static int sort_step(swap_ctx* c, F32State* s, long long src_step, bool prepared, const PreStaged* pre,
+                     bool on_side) {
+  if (!on_side) return sort_body(c, s, src_step, prepared, pre, false);
+  TRY(side_stream(c, s));
+  if (!(pre && pre->valid)) {  // no staging ahead of it: order after the main stream here
+    CU(cudaEventRecord(s->ev_main, c->st));
+    CU(cudaStreamWaitEvent(s->side, s->ev_main, 0));
+  }
+  cudaStream_t main = c->st;
+  c->st = s->side;
+  const int r = sort_body(c, s, src_step, prepared, pre, true);
+  c->st = main;
+  if (r) return r;
+  CU(cudaEventRecord(s->ev_sort, s->side));
+  s->sort_pending = true;
+  return SWAP_OK;
+}
+
+static int sort_join(swap_ctx* c, F32State* s) {
+  if (!s->sort_pending) return SWAP_OK;
+  s->sort_pending = false;
+  CU(cudaStreamWaitEvent(c->st, s->ev_sort, 0));
+  if (s->src_on) {
+    CU(cudaEventSynchronize(s->ev_sort));
+    const int64_t n = *s->h_n;
+    if (n > c->dims.ni_max) return c->fail(SWAP_ECAPACITY, "Ni_max exceeded by new ions");
+    s->N = n;
+  }
+  return SWAP_OK;
+}
+
+static int sort_body(swap_ctx* c, F32State* s, long long src_step, bool prepared, const PreStaged* pre,
+                     bool on_side) {
   const G32& g = s->g;
   Part& a = s->buf[s->cur];
   Part& b = s->buf[1 - s->cur];
   long long n_host = 0, n_max = 0;
   const int64_t* n_dev = nullptr;
   if (pre && pre->valid) {
-    CU(cudaStreamWaitEvent(c->st, s->ev_side, 0));
+    if (!on_side) CU(cudaStreamWaitEvent(c->st, s->ev_side, 0));
     n_host = pre->n_host;
     n_max = pre->n_max;
     n_dev = pre->n_dev;
@@ -538,6 +584,10 @@ static int sort_step(swap_ctx* c, F32State* s, long long src_step, bool prepared
                                       s->stage.ncount, s->start_new, b, cap, c->d_err, c->st));
   std::swap(s->start, s->start_new);
   s->cur = 1 - s->cur;
+  if (on_side) {  // the count, for sort_join
+    if (s->src_on) CU(cudaMemcpyAsync(s->h_n, s->start + g.nkeys, sizeof(int64_t), cudaMemcpyDeviceToHost, c->st));
+    return SWAP_OK;
+  }
   if (s->src_on) {  // the count changed: the host needs it for the next launches
     int64_t n = 0;
     CU(cudaMemcpyAsync(&n, s->start + g.nkeys, sizeof(int64_t), cudaMemcpyDeviceToHost, c->st));
@@ -663,14 +713,21 @@ static int field_step(swap_ctx* c, F32State* s) {
   return SWAP_OK;
 }
 
+// The second stream, its events and the pinned count, made once.
+static int side_stream(swap_ctx* c, F32State* s) {
+  if (s->side) return SWAP_OK;
+  CU(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+  CU(cudaEventCreateWithFlags(&s->ev_main, cudaEventDisableTiming));
+  CU(cudaEventCreateWithFlags(&s->ev_side, cudaEventDisableTiming));
+  CU(cudaEventCreateWithFlags(&s->ev_sort, cudaEventDisableTiming));
+  CU(cudaMallocHost(&s->h_n, sizeof(int64_t)));
+  return SWAP_OK;
+}
+
 // Stage the new ions of step m on the second stream, after the main stream's
 // work so far (the last sort read the previous staging's buffers).
 static int stage_ahead(swap_ctx* c, F32State* s, long long m, PreStaged* pre) {
-  if (!s->side) {
-    CU(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
-    CU(cudaEventCreateWithFlags(&s->ev_main, cudaEventDisableTiming));
-    CU(cudaEventCreateWithFlags(&s->ev_side, cudaEventDisableTiming));
-  }
+  TRY(side_stream(c, s));
   CU(cudaEventRecord(s->ev_main, c->st));
   CU(cudaStreamWaitEvent(s->side, s->ev_main, 0));
   cudaStream_t main = c->st;
@@ -683,7 +740,19 @@ static int stage_ahead(swap_ctx* c, F32State* s, long long m, PreStaged* pre) {
   return SWAP_OK;
 }
 
+static int one_step_body(swap_ctx* c, F32State* s);
+// A step; after a failure the second stream's work (a sort already queued)
+// is drained, so that nothing of the step runs on when the caller goes on.
 static int one_step(swap_ctx* c, F32State* s) {
+  const int r = one_step_body(c, s);
+  if (r && s->sort_pending) {
+    cudaStreamSynchronize(s->side);
+    s->sort_pending = false;
+  }
+  return r;
+}
+
+static int one_step_body(swap_ctx* c, F32State* s) {
   const G32& g = s->g;
   const StepParams sp = step_params(c, s);
   const Part& p = s->buf[s->cur];
@@ -708,10 +777,13 @@ static int one_step(swap_ctx* c, F32State* s) {
   }
   PreStaged pre;
   if (s->src_on) TRY(stage_ahead(c, s, c->src_step + 1, &pre));  // the sources of the next step
+  // the sort on the second stream, beside the moments' sums and the field
+  // subcycles: it reads pass 3's outputs and the staging, they the grids
+  TRY(sort_step(c, s, c->src_step + 1, true, &pre, true));
   TRY(finish_deposit(c, s, 3, 4));
   if (s->gpf) KL("f32_gpe", gpe_faces(g, s->np, s->gp, s->gpf, c->st));  // E's pressure term at the new np
   TRY(field_step(c, s));                                                          // :420-476
-  TRY(sort_step(c, s, c->src_step + 1, true, &pre));
+  TRY(sort_join(c, s));
   if (c->have_srcs) c->src_step++;
   return SWAP_OK;
 }
