@@ -431,6 +431,9 @@ int swap_surrogate_set_curl_weight(swap_surrogate* net, double curl_w, double kr
  * mean |curl target|^2 (clamped to [0.1, 100]), so every pair counts by its
  * relative error. */
 int swap_surrogate_set_pair_weighting(swap_surrogate* net, int32_t relative);
+/* cuda_cores != 0: the training's weight gradients on the CUDA cores instead
+ * of the tensor cores (the same sums in another order; kept for checking). */
+int swap_surrogate_set_weight_grad_cores(swap_surrogate* net, int32_t cuda_cores);
 /* The network's depth (conv layers). */
 int swap_surrogate_layers(int32_t* n);
 int swap_surrogate_attach(swap_ctx* ctx, swap_surrogate* net, int32_t judge_every, double bound);

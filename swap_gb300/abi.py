@@ -172,6 +172,7 @@ SIGNATURES: dict[str, tuple] = {
     "swap_surrogate_layers": (C.c_int, [c_int32_p]),
     "swap_surrogate_set_curl_weight": (C.c_int, [P, C.c_double, C.c_double]),
     "swap_surrogate_set_pair_weighting": (C.c_int, [P, C.c_int32]),
+    "swap_surrogate_set_weight_grad_cores": (C.c_int, [P, C.c_int32]),
     "swap_f32_key_starts": (C.c_int, [P, c_int64_p, C.c_int64]),
     "swap_f32_set_moment_sums": (C.c_int, [P, C.c_int]),
     "swap_f32_displace_resort": (C.c_int, [P, C.c_int64, c_int64_p, c_int32_p]),

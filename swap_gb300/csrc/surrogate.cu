@@ -715,6 +715,134 @@ __global__ void __launch_bounds__(256) k_conv3_dw(int nx, int ny, int nz, long l
   }
 }
 
+// Weight gradient on the tensor cores.  For a group of TPG = 128 / CIN taps,
+// D[(tap, ci)][co] = sum_v X[v + tap][ci] * dZ[v][co] is one MMA chain with
+// M = 128 rows (tap, ci), N = COUT, K = the voxels: A[(tap, ci)][v] and
+// B[co][v] are the voxel-major transposes of the gathered inputs and of dZ,
+// written into the K-major core layout 64 voxels (4 MMAs of K = 16) per
+// stage, two stages, while the tensor core works on the other.  A block
+// (voxel chunk, tap group) adds its 128 x COUT sums to gW with FP32 atomics;
+// gb is k_bias_grad's.  The accumulator lives in tensor memory.
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(128) k_conv3_dw_tc(int nx, int ny, int nz, long long V,
+                                                     const __nv_bfloat16* __restrict__ X,
+                                                     const __nv_bfloat16* __restrict__ dZ, float* __restrict__ gW,
+                                                     int vchunk, int* err) {
+  static_assert((CIN == 16 || CIN == 32) && (COUT == 16 || COUT == 32), "operand shapes");
+  constexpr int TPG = 128 / CIN, KS = 64;
+  constexpr int ABYTES = 128 * KS * 2, BBYTES = COUT * KS * 2;
+  __shared__ __align__(1024) uint8_t sA[2][ABYTES];
+  __shared__ __align__(1024) uint8_t sB[2][BBYTES];
+  __shared__ uint64_t mbar[2];
+  __shared__ uint32_t tslot;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tap0 = blockIdx.y * TPG;
+  if (warp == 0) tc05::tmem_alloc(&tslot, 32);
+  if (tid == 0) {
+    tc05::mbar_init(&mbar[0], 1);
+    tc05::mbar_init(&mbar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc05::fence_before_sync();
+  __syncthreads();
+  tc05::fence_after_sync();
+  const uint32_t tmem = tslot;
+  constexpr uint32_t idesc = tc05::idesc_bf16_f32(128, COUT);
+  uint32_t issued[2] = {0, 0}, waited[2] = {0, 0};
+  bool ok = true;
+  const long long v0 = (long long)blockIdx.x * vchunk;
+  const long long v1 = v0 + vchunk < V ? v0 + vchunk : V;  // V and vchunk are multiples of KS
+  int stage = 0;
+  for (long long vb = v0; vb < v1; vb += KS, ++stage) {
+    const int b = stage & 1;
+    if (issued[b] > waited[b]) {  // the MMAs that read this buffer are done
+      ok &= tc05::mbar_wait(&mbar[b], waited[b] & 1, WAIT_LIMIT);
+      ++waited[b];
+    }
+    // A: item (voxel k, tap t, 8 channels) -> rows t*CIN + c0 .. +7 at column k
+    for (int it = tid; it < KS * TPG * (CIN / 8); it += 128) {
+      const int k = it % KS, r = it / KS, t = r / (CIN / 8), c0 = (r % (CIN / 8)) * 8;
+      const int tap = tap0 + t;
+      uint4 val = make_uint4(0u, 0u, 0u, 0u);
+      if (tap < 27) {
+        const long long v = vb + k;
+        const int x = (int)(v % nx), y = (int)((v / nx) % ny), z = (int)(v / ((long long)nx * ny));
+        int xn = x + tap % 3 - 1, yn = y + (tap / 3) % 3 - 1, zn = z + tap / 9 - 1;
+        xn = xn < 0 ? xn + nx : (xn >= nx ? xn - nx : xn);
+        yn = yn < 0 ? yn + ny : (yn >= ny ? yn - ny : yn);
+        zn = zn < 0 ? zn + nz : (zn >= nz ? zn - nz : zn);
+        val = *reinterpret_cast<const uint4*>(X + (xn + (long long)nx * (yn + (long long)ny * zn)) * CIN + c0);
+      }
+      const __nv_bfloat16* h = reinterpret_cast<const __nv_bfloat16*>(&val);
+#pragma unroll
+      for (int e = 0; e < 8; ++e)
+        *reinterpret_cast<__nv_bfloat16*>(sA[b] + tc05::core_offset(t * CIN + c0 + e, k, 128)) = h[e];
+    }
+    // B: item (voxel k, 8 output channels) -> rows c0 .. +7 at column k
+    for (int it = tid; it < KS * (COUT / 8); it += 128) {
+      const int k = it % KS, c0 = (it / KS) * 8;
+      const uint4 val = *reinterpret_cast<const uint4*>(dZ + (vb + k) * COUT + c0);
+      const __nv_bfloat16* h = reinterpret_cast<const __nv_bfloat16*>(&val);
+#pragma unroll
+      for (int e = 0; e < 8; ++e)
+        *reinterpret_cast<__nv_bfloat16*>(sB[b] + tc05::core_offset(c0 + e, k, COUT)) = h[e];
+    }
+    tc05::fence_async_smem();
+    tc05::fence_before_sync();
+    __syncthreads();
+    tc05::fence_after_sync();
+    if (tid == 0) {
+      const uint32_t a0 = tc05::smem_u32(sA[b]), b0 = tc05::smem_u32(sB[b]);
+#pragma unroll
+      for (int kk = 0; kk < KS / 16; ++kk) {
+        const uint64_t ad = tc05::desc_noswizzle(a0 + kk * 2 * (16 * 128), 16 * 128, 128);
+        const uint64_t bd = tc05::desc_noswizzle(b0 + kk * 2 * ((COUT / 8) * 128), (COUT / 8) * 128, 128);
+        tc05::mma_bf16(tmem, ad, bd, idesc, stage > 0 || kk > 0);
+      }
+      tc05::mma_commit(&mbar[b]);
+    }
+    ++issued[b];
+  }
+  for (int b = 0; b < 2; ++b)
+    if (issued[b] > waited[b]) {
+      ok &= tc05::mbar_wait(&mbar[b], waited[b] & 1, WAIT_LIMIT);
+      ++waited[b];
+    }
+  tc05::fence_after_sync();
+  if (stage > 0) {  // row 32 w + lane of the accumulator: (tap, ci)
+    float acc[COUT];
+    if (COUT == 32) tc05::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16), acc);
+    else tc05::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16), acc);
+    const int r = warp * 32 + lane, tap = tap0 + r / CIN, ci = r % CIN;
+    if (ok && tap < 27) {
+      float* w = gW + (long long)tap * COUT * CIN + ci;
+#pragma unroll
+      for (int co = 0; co < COUT; ++co) atomicAdd(w + co * CIN, acc[co]);
+    }
+  }
+  if (!ok) atomicCAS(err, 0, SWAP_EWAIT);
+  tc05::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc05::tmem_free(tmem, 32);
+}
+
+// gb[co] += sum_v dZ[v][co].
+template <int COUT>
+__global__ void __launch_bounds__(256) k_bias_grad(long long V, const __nv_bfloat16* __restrict__ dZ,
+                                                   float* __restrict__ gb) {
+  __shared__ float s[256 / COUT][COUT];
+  const int c = threadIdx.x % COUT, row = threadIdx.x / COUT;
+  float a = 0.0f;
+  for (long long v = blockIdx.x * (long long)(256 / COUT) + row; v < V; v += (long long)gridDim.x * (256 / COUT))
+    a += __bfloat162float(dZ[v * COUT + c]);
+  s[row][c] = a;
+  __syncthreads();
+  if (row == 0) {
+    for (int q = 1; q < 256 / COUT; ++q) a += s[q][c];
+    atomicAdd(gb + c, a);
+  }
+}
+
 // Adam on n parameters; BF16 copy refreshed.
 __global__ void k_adam(long long n, float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
                        float* __restrict__ vv, float lr, float b1, float b2, float c1, float c2, float eps,
@@ -752,14 +880,29 @@ inline unsigned nblk(long long n, int tpb = 256) {
   return (unsigned)(b < 1 ? 1 : (b > 65535LL * 8 ? 65535LL * 8 : b));
 }
 
+// Weight and bias gradients of a conv layer: the tensor-core form, or with
+// cuda_cores the CUDA-core form (kept to check the other against).
 template <int CIN, int COUT>
 cudaError_t conv3_dw(int nx, int ny, int nz, long long V, const __nv_bfloat16* X, const __nv_bfloat16* dZ, float* gW,
-                     float* gb, cudaStream_t st) {
-  // at most 64 voxel chunks per tap: few enough atomic adds per weight
-  const long long nchunk = std::min<long long>((V + 2047) / 2048, 64);
-  const int vchunk = (int)(((V + nchunk - 1) / nchunk + 63) / 64 * 64);
-  const dim3 grid((unsigned)((V + vchunk - 1) / vchunk), 27);
-  k_conv3_dw<CIN, COUT><<<grid, 256, 0, st>>>(nx, ny, nz, V, X, dZ, gW, gb, vchunk);
+                     float* gb, int* err, bool cuda_cores, cudaStream_t st) {
+  if (cuda_cores) {
+    // at most 64 voxel chunks per tap: few enough atomic adds per weight
+    const long long nchunk = std::min<long long>((V + 2047) / 2048, 64);
+    const int vchunk = (int)(((V + nchunk - 1) / nchunk + 63) / 64 * 64);
+    const dim3 grid((unsigned)((V + vchunk - 1) / vchunk), 27);
+    k_conv3_dw<CIN, COUT><<<grid, 256, 0, st>>>(nx, ny, nz, V, X, dZ, gW, gb, vchunk);
+    return cudaGetLastError();
+  }
+  // voxel chunks of a multiple of 64 (V is a multiple of 128), about 152 x 4
+  // blocks over all tap groups
+  constexpr int TPG = 128 / CIN, NG = (27 + TPG - 1) / TPG;
+  const long long want = std::max<long long>(1, 608 / NG);
+  const int vchunk = (int)std::max<long long>(64, ((V + want - 1) / want + 63) / 64 * 64);
+  const dim3 grid((unsigned)((V + vchunk - 1) / vchunk), NG);
+  k_conv3_dw_tc<CIN, COUT><<<grid, 128, 0, st>>>(nx, ny, nz, V, X, dZ, gW, vchunk, err);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_bias_grad<COUT><<<std::min<long long>((V + 255) / 256, 1216), 256, 0, st>>>(V, dZ, gb);
   return cudaGetLastError();
 }
 
@@ -790,6 +933,8 @@ struct swap_surrogate {
   // counts by its relative error, as the judge measures it
   bool per_pair = false;
   std::vector<double> ds_k2;
+  // the weight gradient on the CUDA cores instead of the tensor cores
+  bool dw_cores = false;
   float *d_mean = nullptr, *d_istd = nullptr;
   // the dataset, all of one grid shape (the first sample's)
   int ds_nx = 0, ds_ny = 0, ds_nz = 0;
@@ -925,7 +1070,7 @@ int backward(swap_surrogate* net, cudaStream_t st) {
   const int nx = net->nx, ny = net->ny, nz = net->nz;
   const long long V = net->V;
   constexpr int L = NL - 1;
-  SCU((conv3_dw<32, 16>(nx, ny, nz, V, net->Y[L - 1], net->d16, net->gw[L], net->gb[L], st)));
+  SCU((conv3_dw<32, 16>(nx, ny, nz, V, net->Y[L - 1], net->d16, net->gw[L], net->gb[L], net->err, net->dw_cores, st)));
   ConvArgs a = conv_args(net);
   a.Y = nullptr; a.Z = nullptr; a.bias = nullptr; a.gelu = 0; a.ldf = 32; a.nstore = 32; a.Yf = net->dy;
   // last layer -> the one before: the data gradient, then through its GELU
@@ -934,13 +1079,13 @@ int backward(swap_surrogate* net, cudaStream_t st) {
   __nv_bfloat16 *dz = net->dzA, *dz_next = net->dzB;
   k_gelu_back<<<nblk(V * 32), 256, 0, st>>>(V * 32, net->dy, net->Z[L - 1], dz);
   for (int l = L - 1; l >= 1; --l) {  // layer l -> l - 1
-    SCU((conv3_dw<32, 32>(nx, ny, nz, V, net->Y[l - 1], dz, net->gw[l], net->gb[l], st)));
+    SCU((conv3_dw<32, 32>(nx, ny, nz, V, net->Y[l - 1], dz, net->gw[l], net->gb[l], net->err, net->dw_cores, st)));
     a.X = dz; a.W = net->wt[l];
     SCU(conv3(32, 32, a, st));
     k_gelu_back<<<nblk(V * 32), 256, 0, st>>>(V * 32, net->dy, net->Z[l - 1], dz_next);
     std::swap(dz, dz_next);
   }
-  SCU((conv3_dw<16, 32>(nx, ny, nz, V, net->x0, dz, net->gw[0], net->gb[0], st)));
+  SCU((conv3_dw<16, 32>(nx, ny, nz, V, net->x0, dz, net->gw[0], net->gb[0], net->err, net->dw_cores, st)));
   return SWAP_OK;
 }
 
@@ -1279,6 +1424,12 @@ static int pair_k2(swap_surrogate* net) {
     SCU(cudaMemcpy(&h, net->acc + 1, sizeof(float), cudaMemcpyDeviceToHost));
     net->ds_k2.push_back((double)h / (double)net->V);
   }
+  return SWAP_OK;
+}
+
+extern "C" int swap_surrogate_set_weight_grad_cores(swap_surrogate* net, int32_t cuda_cores) {
+  if (!net) return SWAP_EINVAL;
+  net->dw_cores = cuda_cores != 0;
   return SWAP_OK;
 }
 

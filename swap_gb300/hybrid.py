@@ -486,6 +486,10 @@ class Surrogate:
         if per_pair:
             self._check(self.lib.swap_surrogate_set_pair_weighting(self.h, 1))
 
+    def set_weight_grad_cores(self, cuda_cores: bool):
+        """Weight gradients on the CUDA cores (True) or the tensor cores (False, the default)."""
+        self._check(self.lib.swap_surrogate_set_weight_grad_cores(self.h, 1 if cuda_cores else 0))
+
     def set_curl_weight(self, w: float, kref2: float = 0.0):
         """Add w * mean |curl e|^2 / kref2 to the loss (e the E error: curl e is
         the B error per unit dt); kref2 = 0: mean |curl target|^2 of the pairs."""

@@ -141,6 +141,31 @@ def test_surrogate_gradients_match_cpu(dims, curl):
             assert err < 3e-2, (l, err)  # BF16 activations and gradients against float64
 
 
+@pytest.mark.parametrize("dims", [(8, 8, 4), (128, 4, 2)])
+def test_weight_gradient_on_tensor_cores_matches_cuda_cores(dims):
+    """The tcgen05 weight gradient (voxel-major operands, K = the voxels)
+    against the CUDA-core one on the same BF16 values: the same sums in
+    another order, so within FP32 summation error."""
+    import torch
+
+    from swap_gb300.hybrid import Surrogate
+
+    V = dims[0] * dims[1] * dims[2]
+    net = Surrogate(seed=5)
+    net.norm(np.full(Surrogate.NIN, 0.1), np.full(Surrogate.NIN, 1.5), np.array([0.5, -0.25, 0.0]),
+             np.array([0.75, 0.5, 2.0]))
+    g = torch.Generator().manual_seed(8)
+    dvin = torch.randn(V, Surrogate.NIN, generator=g).float().cuda()
+    dtgt = torch.randn(V, 3, generator=g).float().cuda()
+    _, g_tc = net.grads(dims, dvin.data_ptr(), dtgt.data_ptr())
+    net.set_weight_grad_cores(True)
+    _, g_cc = net.grads(dims, dvin.data_ptr(), dtgt.data_ptr())
+    for l in range(len(net.LAYERS)):
+        for a, b in zip(g_tc[l], g_cc[l]):
+            assert np.linalg.norm(a - b) <= 1e-4 * np.linalg.norm(b), l
+    net.close()
+
+
 def _trained(cells, ppc, collect, epochs, seed=3):
     from helpers import make_hybrid
     from swap_gb300.hybrid import Surrogate
