@@ -322,7 +322,7 @@ def train_surrogate(args, base):
             loss = net.train(upto - done, lr=lr)
             done = upto
     t_train = time.perf_counter() - t0
-    nl = len(net.LAYERS)
+    nl = len(net.layers)
     info = {"network": f"{nl} periodic 3x3x3 conv layers {Surrogate.NIN}-" + "-".join(["32"] * (nl - 1))
                        + "-3, GELU, BF16 on tcgen05, FP32 accumulate; predicts the subcycles' mean E minus the "
                        "plain E at the step's start from B, u_p, n_p, p_e, that E and B - b12",

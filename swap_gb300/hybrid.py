@@ -477,7 +477,7 @@ class Surrogate:
         n = C.c_int32()
         abi.check(self.lib, None, self.lib.swap_surrogate_layers(C.byref(n)))
         # (cin, cout) of the conv layers, padded
-        self.LAYERS = tuple([(16, 32)] + [(32, 32)] * (n.value - 2) + [(32, 16)])
+        self.layers = tuple([(16, 32)] + [(32, 32)] * (n.value - 2) + [(32, 16)])
         h = C.c_void_p()
         abi.check(self.lib, None, self.lib.swap_surrogate_create(C.byref(h), int(seed), int(max_samples)))
         self.h = h
@@ -545,7 +545,7 @@ class Surrogate:
         return None
 
     def weights(self, layer: int, w=None, b=None):
-        cin, cout = self.LAYERS[layer]
+        cin, cout = self.layers[layer]
         if w is None:
             w = np.zeros((27, cout, cin), dtype=np.float32)
             b = np.zeros(cout, dtype=np.float32)
@@ -558,12 +558,12 @@ class Surrogate:
 
     def grads(self, dims, vin_dev_ptr: int, tgt_dev_ptr: int):
         """Loss and per-layer (gW, gb) for device inputs [V][NIN] and targets [V][3]."""
-        n = sum(27 * ci * co + co for ci, co in self.LAYERS)
+        n = sum(27 * ci * co + co for ci, co in self.layers)
         g = np.zeros(n, dtype=np.float32)
         loss = C.c_double()
         self._check(self.lib.swap_surrogate_grads(self.h, *dims, vin_dev_ptr, tgt_dev_ptr, C.byref(loss), g.ctypes.data))
         out, o = [], 0
-        for ci, co in self.LAYERS:
+        for ci, co in self.layers:
             gw = g[o:o + 27 * ci * co].reshape(27, co, ci)
             o += 27 * ci * co
             out.append((gw, g[o:o + co].copy()))

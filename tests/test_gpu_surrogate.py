@@ -128,14 +128,14 @@ def test_surrogate_gradients_match_cpu(dims, curl):
     mean, std = np.full(Surrogate.NIN, 0.1), np.full(Surrogate.NIN, 1.5)
     out_mean, out_std = np.array([0.5, -0.25, 0.0]), np.array([0.75, 0.5, 2.0])
     net.norm(mean, std, out_mean, out_std)
-    layers = [net.weights(l) for l in range(len(net.LAYERS))]
+    layers = [net.weights(l) for l in range(len(net.layers))]
     T = torch.tensor
     loss_ref, g_ref = _ref_forward_backward(vin, tgt, layers, T(mean), T(std), T(out_mean), T(out_std), dims, curl)
     dvin = vin.float().cuda()
     dtgt = tgt.float().cuda()
     loss, g_gpu = net.grads(dims, dvin.data_ptr(), dtgt.data_ptr())
     assert abs(loss - loss_ref) <= 2e-3 * loss_ref
-    for l in range(len(net.LAYERS)):
+    for l in range(len(net.layers)):
         for a, b in zip(g_gpu[l], g_ref[l]):
             err = np.linalg.norm(a - b) / np.linalg.norm(b)
             assert err < 3e-2, (l, err)  # BF16 activations and gradients against float64
@@ -160,7 +160,7 @@ def test_weight_gradient_on_tensor_cores_matches_cuda_cores(dims):
     _, g_tc = net.grads(dims, dvin.data_ptr(), dtgt.data_ptr())
     net.set_weight_grad_cores(True)
     _, g_cc = net.grads(dims, dvin.data_ptr(), dtgt.data_ptr())
-    for l in range(len(net.LAYERS)):
+    for l in range(len(net.layers)):
         for a, b in zip(g_tc[l], g_cc[l]):
             assert np.linalg.norm(a - b) <= 1e-4 * np.linalg.norm(b), l
     net.close()
