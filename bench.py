@@ -323,7 +323,7 @@ def train_surrogate(args, base):
             done = upto
     t_train = time.perf_counter() - t0
     nl = len(net.layers)
-    info = {"network": f"{nl} periodic 3x3x3 conv layers {Surrogate.NIN}-" + "-".join(["32"] * (nl - 1))
+    info = {"network": f"{nl} periodic 3x3x3 conv layers {Surrogate.NIN}-" + "-".join([str(net.layers[0][1])] * (nl - 1))
                        + "-3, GELU, BF16 on tcgen05, FP32 accumulate; predicts the subcycles' mean E minus the "
                        "plain E at the step's start from B, u_p, n_p, p_e, that E and B - b12",
             "training": f"{args.sur_runs} randomized runs of {cells[0]}x{cells[1]}x{cells[2]} cells at "

@@ -434,8 +434,9 @@ int swap_surrogate_set_pair_weighting(swap_surrogate* net, int32_t relative);
 /* cuda_cores != 0: the training's weight gradients on the CUDA cores instead
  * of the tensor cores (the same sums in another order; kept for checking). */
 int swap_surrogate_set_weight_grad_cores(swap_surrogate* net, int32_t cuda_cores);
-/* The network's depth (conv layers). */
+/* The network's depth (conv layers) and the channels of its hidden layers. */
 int swap_surrogate_layers(int32_t* n);
+int swap_surrogate_width(int32_t* w);
 int swap_surrogate_attach(swap_ctx* ctx, swap_surrogate* net, int32_t judge_every, double bound);
 /* [0] steps by the network, [1] judged steps, [2] fallbacks, [3] last judged
  * B rel-L2, [4] last judged (B - b0) rel-L2. */

@@ -170,6 +170,7 @@ SIGNATURES: dict[str, tuple] = {
     "swap_f32_far_movers": (C.c_int, [P, c_int64_p]),
     "swap_set_deterministic": (C.c_int, [P, C.c_int32]),
     "swap_surrogate_layers": (C.c_int, [c_int32_p]),
+    "swap_surrogate_width": (C.c_int, [c_int32_p]),
     "swap_surrogate_set_curl_weight": (C.c_int, [P, C.c_double, C.c_double]),
     "swap_surrogate_set_pair_weighting": (C.c_int, [P, C.c_int32]),
     "swap_surrogate_set_weight_grad_cores": (C.c_int, [P, C.c_int32]),

@@ -510,6 +510,12 @@ namespace {
 #define SWAP_SUR_LAYERS 4
 #endif
 constexpr int NL = SWAP_SUR_LAYERS;
+// Channels of the hidden layers (16 or 32).
+#ifndef SWAP_SUR_WIDTH
+#define SWAP_SUR_WIDTH 16
+#endif
+constexpr int HID = SWAP_SUR_WIDTH;
+static_assert(HID == 16 || HID == 32, "hidden width");
 constexpr double WARMUP = 200.0;  // Adam updates of the learning-rate warm-up
 static_assert(NL >= 2 && NL <= 16, "surrogate depth");
 struct LayerDims {
@@ -518,7 +524,7 @@ struct LayerDims {
 };
 constexpr LayerDims layer_dims(bool in) {
   LayerDims d{};
-  for (int l = 0; l < NL; ++l) d.v[l] = in ? (l == 0 ? 16 : 32) : (l == NL - 1 ? 16 : 32);
+  for (int l = 0; l < NL; ++l) d.v[l] = in ? (l == 0 ? 16 : HID) : (l == NL - 1 ? 16 : HID);
   return d;
 }
 constexpr LayerDims LCIN = layer_dims(true);    // layer 0: 14 input channels padded to 16
@@ -1004,14 +1010,14 @@ int ensure_shape(swap_surrogate* net, int nx, int ny, int nz) {
   };
   net->x0 = static_cast<__nv_bfloat16*>(take(V * 16 * 2));
   for (int l = 0; l < NL - 1; ++l) {
-    net->Z[l] = static_cast<__nv_bfloat16*>(take(V * 32 * 2));
-    net->Y[l] = static_cast<__nv_bfloat16*>(take(V * 32 * 2));
+    net->Z[l] = static_cast<__nv_bfloat16*>(take(V * HID * 2));
+    net->Y[l] = static_cast<__nv_bfloat16*>(take(V * HID * 2));
   }
   net->out = static_cast<float*>(take(V * NOUT * 4));
   net->d16 = static_cast<__nv_bfloat16*>(take(V * 16 * 2));
-  net->dy = static_cast<float*>(take(V * 32 * 4));
-  net->dzA = static_cast<__nv_bfloat16*>(take(V * 32 * 2));
-  net->dzB = static_cast<__nv_bfloat16*>(take(V * 32 * 2));
+  net->dy = static_cast<float*>(take(V * (HID > 6 ? HID : 6) * 4));  // also the curl loss's scratch (6 V)
+  net->dzA = static_cast<__nv_bfloat16*>(take(V * HID * 2));
+  net->dzB = static_cast<__nv_bfloat16*>(take(V * HID * 2));
   if (net->work.size() != 2 * (NL - 1) + 6) {  // x0, Z and Y per hidden layer, out, d16, dy, dzA, dzB
     net->V = 0;
     return fail(net, SWAP_ECUDA, "surrogate work buffers");
@@ -1070,22 +1076,23 @@ int backward(swap_surrogate* net, cudaStream_t st) {
   const int nx = net->nx, ny = net->ny, nz = net->nz;
   const long long V = net->V;
   constexpr int L = NL - 1;
-  SCU((conv3_dw<32, 16>(nx, ny, nz, V, net->Y[L - 1], net->d16, net->gw[L], net->gb[L], net->err, net->dw_cores, st)));
+  SCU((conv3_dw<HID, 16>(nx, ny, nz, V, net->Y[L - 1], net->d16, net->gw[L], net->gb[L], net->err, net->dw_cores,
+                          st)));
   ConvArgs a = conv_args(net);
-  a.Y = nullptr; a.Z = nullptr; a.bias = nullptr; a.gelu = 0; a.ldf = 32; a.nstore = 32; a.Yf = net->dy;
+  a.Y = nullptr; a.Z = nullptr; a.bias = nullptr; a.gelu = 0; a.ldf = HID; a.nstore = HID; a.Yf = net->dy;
   // last layer -> the one before: the data gradient, then through its GELU
   a.X = net->d16; a.W = net->wt[L];
-  SCU(conv3(16, 32, a, st));
+  SCU(conv3(16, HID, a, st));
   __nv_bfloat16 *dz = net->dzA, *dz_next = net->dzB;
-  k_gelu_back<<<nblk(V * 32), 256, 0, st>>>(V * 32, net->dy, net->Z[L - 1], dz);
+  k_gelu_back<<<nblk(V * HID), 256, 0, st>>>(V * HID, net->dy, net->Z[L - 1], dz);
   for (int l = L - 1; l >= 1; --l) {  // layer l -> l - 1
-    SCU((conv3_dw<32, 32>(nx, ny, nz, V, net->Y[l - 1], dz, net->gw[l], net->gb[l], net->err, net->dw_cores, st)));
+    SCU((conv3_dw<HID, HID>(nx, ny, nz, V, net->Y[l - 1], dz, net->gw[l], net->gb[l], net->err, net->dw_cores, st)));
     a.X = dz; a.W = net->wt[l];
-    SCU(conv3(32, 32, a, st));
-    k_gelu_back<<<nblk(V * 32), 256, 0, st>>>(V * 32, net->dy, net->Z[l - 1], dz_next);
+    SCU(conv3(HID, HID, a, st));
+    k_gelu_back<<<nblk(V * HID), 256, 0, st>>>(V * HID, net->dy, net->Z[l - 1], dz_next);
     std::swap(dz, dz_next);
   }
-  SCU((conv3_dw<16, 32>(nx, ny, nz, V, net->x0, dz, net->gw[0], net->gb[0], net->err, net->dw_cores, st)));
+  SCU((conv3_dw<16, HID>(nx, ny, nz, V, net->x0, dz, net->gw[0], net->gb[0], net->err, net->dw_cores, st)));
   return SWAP_OK;
 }
 
@@ -1442,6 +1449,12 @@ extern "C" int swap_surrogate_set_pair_weighting(swap_surrogate* net, int32_t re
 extern "C" int swap_surrogate_layers(int32_t* n) {
   if (!n) return SWAP_EINVAL;
   *n = NL;
+  return SWAP_OK;
+}
+
+extern "C" int swap_surrogate_width(int32_t* w) {
+  if (!w) return SWAP_EINVAL;
+  *w = HID;
   return SWAP_OK;
 }
 

@@ -474,10 +474,12 @@ class Surrogate:
 
     def __init__(self, seed: int = 1, max_samples: int = 4096, curl_weight: float = 0.0, per_pair: bool = False):
         self.lib = abi.load()
-        n = C.c_int32()
+        n, w = C.c_int32(), C.c_int32()
         abi.check(self.lib, None, self.lib.swap_surrogate_layers(C.byref(n)))
+        abi.check(self.lib, None, self.lib.swap_surrogate_width(C.byref(w)))
         # (cin, cout) of the conv layers, padded
-        self.layers = tuple([(16, 32)] + [(32, 32)] * (n.value - 2) + [(32, 16)])
+        W = w.value
+        self.layers = tuple([(16, W)] + [(W, W)] * (n.value - 2) + [(W, 16)])
         h = C.c_void_p()
         abi.check(self.lib, None, self.lib.swap_surrogate_create(C.byref(h), int(seed), int(max_samples)))
         self.h = h
