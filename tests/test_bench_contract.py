@@ -41,3 +41,18 @@ def test_reference_arm_prints_the_contract_line():
     assert abs(d["ms_per_step"] - 1e3 * sum(d["step_s"]) / 2) <= 0.01 * d["ms_per_step"] + 2
     tail = r.stdout.strip().splitlines()[-1].split()
     assert tail == ["ORACLE_ONLY", "True"], tail
+
+
+def test_reference_arm_under_torchrun_prints_one_line():
+    """Launched as the multi-GPU bench is (torchrun, two ranks on 127.0.0.1),
+    the reference arm runs on rank 0 alone and prints one line; the other
+    rank exits 0 without work."""
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", "29611", str(ROOT / "bench.py"), "--impl", "reference",
+           "--config", "0", "--steps", "1", "--warmup", "0", "--ref-fp64-steps", "0", "--gpus", "2"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=900, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.strip().startswith("{")]
+    assert len(lines) == 1, r.stdout[-2000:]
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
