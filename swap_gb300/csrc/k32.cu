@@ -151,13 +151,14 @@ __device__ __forceinline__ int dir_index(int dx, int dy, int dz) { return (dx + 
 // rounded run sums whatever order the warps add in.  The brick partials are
 // written as 64-bit integers, summed the same way and rounded to FP32 once
 // per node (k_node_sum).  Bounds: |x| < 2^15 per run sum and per node (the
-// high words wrap, so only the total must fit), and fewer than 2^16 adds per
-// node in a brick, i.e. fewer than 65536 ions per brick; a larger or
-// non-finite run sum, or a fuller brick, is reported (KERR_RANGE).
+// high words wrap, so only the total must fit); a larger or non-finite run
+// sum is reported (KERR_RANGE).  A low word takes at most 2^16 per add and
+// an ion adds at most once per node, so every CARRY_CHUNKS chunks of a brick
+// the low words carry into the high words and any number of ions fits.
 // Otherwise (plain): FP32 atomics, whose result depends on the order.
 constexpr double FIX_INV = 1.0 / 4294967296.0;  // 2^-32
 constexpr float FIX_MAX = 32768.0f;             // 2^15
-constexpr long long FIX_MAX_IONS = 65535;       // ions per brick
+constexpr int CARRY_CHUNKS = 256;               // 32768 ions: the low words stay below 2^32
 
 // x in units of 2^-32 as the tile holds it: floor(x * 2^16) * 2^16 plus the
 // rounded rest (the same two conversions as tile_add).
@@ -323,7 +324,6 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
 
   const float hdt = 0.5f * sprm.dt;
   const long long first = start[b * BCELLS], last = start[b * BCELLS + BCELLS];
-  if (EXACT && last - first > FIX_MAX_IONS && threadIdx.x == 0) set_err(err, KERR_RANGE);
   // chunks of 128 particles from a 16-aligned start (every copy then starts
   // on a 16-byte boundary); lanes outside [first, last) are masked
   const long long a0 = first & ~15LL;
@@ -558,6 +558,17 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
         }
         __syncthreads();
       }
+    }
+    if (EXACT && (kc + 1) % CARRY_CHUNKS == 0 && kc + 1 < nchunk) {
+      // a crowded brick: carry the low words into the high words (exact:
+      // 2^16 low units are one high unit), so that they never wrap
+      __syncthreads();
+      for (int t = threadIdx.x; t < 4 * TNOD; t += blockDim.x) {
+        const unsigned lo = s_dep[t];
+        s_dep[t] = lo & 0xFFFFu;
+        s_dep[4 * TNOD + t] += lo >> 16;
+      }
+      __syncthreads();
     }
   }
   if (EXACT && bad) set_err(err, KERR_RANGE);

@@ -170,7 +170,7 @@ static int check_err(swap_ctx* c) {
     if (herr == 8) return c->fail(SWAP_EWAIT, "a particle chunk copy did not complete within its wait limit");
     if (herr == 10)
       return c->fail(SWAP_ENONFINITE,
-                     "a moment sum is not finite or beyond the exact sums' range (|sum| < 2^15, < 65536 ions per brick)");
+                     "a moment sum is not finite or beyond the exact sums' range (|sum| < 2^15)");
     return c->fail(SWAP_ECUDA, "device error flag " + std::to_string(herr));
   }
   return SWAP_OK;
