@@ -318,9 +318,9 @@ int swap_f32_key_starts(swap_ctx* ctx, int64_t* starts, int64_t n);
  * 2^-32) -- exact, so a node's moment is its warp sums' exact total rounded
  * once to FP32, and the same whatever order the GPU adds in (the FP32 form's
  * steps are then reproducible bit for bit).  A warp sum or node moment of
- * 2^15 or more, a non-finite one, or a brick of 4x4x4 cells holding 65536
- * ions or more ends the step with SWAP_ENONFINITE.  exact = 0: FP32 atomics,
- * kept to measure what the exact sums gain. */
+ * 2^15 or more, or a non-finite one, ends the step with SWAP_ENONFINITE; a
+ * brick may hold any number of ions.  exact = 0: FP32 atomics, kept to
+ * measure what the exact sums gain. */
 int swap_f32_set_moment_sums(swap_ctx* ctx, int exact);
 /* Validation: move particles idx[q] of the current (sorted) order by one
  * cell step per axis (dcell[q] = (dx+1) | (dy+1)<<10 | (dz+1)<<20) and run
