@@ -316,6 +316,17 @@ module swap_gpu_iface
        type(c_ptr), value :: ctx
        integer(c_int64_t) :: n
      end function swap_f32_count
+     integer(c_int) function swap_f32_far_movers(ctx, n) bind(C, name="swap_f32_far_movers")
+       import :: c_int, c_ptr, c_int64_t
+       type(c_ptr), value :: ctx
+       integer(c_int64_t) :: n
+     end function swap_f32_far_movers
+     ! ---- reproducible FP64 runs (fixed-point deposits), e.g. around a restart
+     integer(c_int) function swap_set_deterministic(ctx, on) bind(C, name="swap_set_deterministic")
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), value :: on
+     end function swap_set_deterministic
      ! ---- sources and sinks without a reference argument list of their own
      integer(c_int) function swap_inflow_x(ctx, m_tstep) bind(C, name="swap_inflow_x")
        import :: c_int, c_ptr, c_int32_t
