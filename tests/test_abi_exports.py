@@ -42,3 +42,13 @@ def test_kernels_compiled_for_sm103a_only():
     flags = " ".join(build.ARCH)
     assert "compute_103a" in flags and "sm_103a" in flags
     assert "sm_100" not in flags and "sm_90" not in flags
+
+
+def test_fortran_module_binds_declared_symbols():
+    """Every bind(C) name of the Fortran interface module is an entry the
+    header declares (so a SWAP build that uses the module links)."""
+    text = (ROOT / "swap_gb300" / "fortran" / "swap_gpu_iface.f90").read_text()
+    names = set(re.findall(r'bind\(C,\s*name="(swap_[A-Za-z0-9_]+)"\)', text))
+    assert len(names) > 30
+    missing = names - set(header_symbols())
+    assert not missing, missing
