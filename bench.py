@@ -787,7 +787,7 @@ def run_accuracy_legs(args, line, net=None):
             line["accuracy"] = run_accuracy(args, net)
         except Exception as e:  # the headline stands without it
             line["accuracy"] = {"error": f"{type(e).__name__}: {e}"}
-    steps = {2: args.acc2_steps, 3: args.acc3_steps}
+    steps = {1: args.acc1_steps, 2: args.acc2_steps, 3: args.acc3_steps}
     for n in [int(x) for x in args.acc_configs.split(",") if x.strip()]:
         for cx in {"both": [True, False], "on": [True], "off": [False]}[args.acc_cx]:
             key = f"config{n}" + ("" if cx else "_no_cx")
@@ -823,6 +823,7 @@ def main():
                     help="ion steps of the accuracy comparison against the FP64 drop-in (0 skips it)")
     ap.add_argument("--acc-configs", default="2,3",
                     help="workloads run at their stated size by both the FP64 drop-in and the FP32 form")
+    ap.add_argument("--acc1-steps", type=int, default=20, help="ion steps of the 256x128x128 H+ comparison")
     ap.add_argument("--acc2-steps", type=int, default=100, help="ion steps of the 256x128x128 pickup-ion comparison")
     ap.add_argument("--acc3-steps", type=int, default=20, help="ion steps of the 512x256x256 pickup-ion comparison")
     ap.add_argument("--acc-marks", default="", help="steps at which the comparisons also record both energies")
