@@ -452,7 +452,7 @@ module swap_gpu_calls
 contains
   ! Create the context from the reference's modules: dimensions.f (nx, ny,
   ! nz, Ni_max), inputs.f (dt, alpha, dx, dy, ntsub) and global.f (beta and
-  ! the /coords/ arrays), with real_bytes = the size of this build's REAL.
+  ! the /coords/ arrays), with real_bytes = the size of the REAL this module is compiled with.
   ! Call after grd7 and initparameters, before the main loop (maind.f:372).
   subroutine swap_gpu_init()
     use dimensions, only: nx, ny, nz, Ni_max
