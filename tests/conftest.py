@@ -12,7 +12,7 @@ for p in (ROOT, ROOT / "oracle"):
 
 
 def pytest_configure(config):
-    config.addinivalue_line("markers", "gpu: needs a GB300 (run on the GPU box)")
+    config.addinivalue_line("markers", "gpu: needs a GB300")
     config.addinivalue_line("markers", "slow: full-size workloads")
 
 
