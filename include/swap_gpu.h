@@ -438,13 +438,17 @@ int swap_surrogate_set_weight_grad_cores(swap_surrogate* net, int32_t cuda_cores
 int swap_surrogate_layers(int32_t* n);
 int swap_surrogate_width(int32_t* w);
 int swap_surrogate_attach(swap_ctx* ctx, swap_surrogate* net, int32_t judge_every, double bound);
+/* bound_db > 0: a judged step also falls back when the network's B differs
+ * from the subcycles' by more than bound_db relative to the plain B - b0
+ * (the field's perturbation, not the field); 0 (the default): B alone. */
+int swap_surrogate_set_db_bound(swap_ctx* ctx, double bound_db);
 /* [0] steps by the network, [1] judged steps, [2] fallbacks, [3] last judged
  * B rel-L2, [4] last judged (B - b0) rel-L2. */
 int swap_surrogate_stats(swap_ctx* ctx, double out[5]);
 /* Test access: normalisation (14 input means and stds, output scale) and
- * FP32 master weights of a layer ([27][cout][cin] with (cin, cout) = (16,32)
- * for the first, (32,16) for the last and (32,32) between: padded channels
- * zero) with its bias; get or set. */
+ * FP32 master weights of a layer ([27][cout][cin] with (cin, cout) = (16,W)
+ * for the first, (W,16) for the last and (W,W) between, W the hidden width
+ * of swap_surrogate_width: padded channels zero) with its bias; get or set. */
 int swap_surrogate_norm(swap_surrogate* net, float* mean, float* stdv, float* out_mean, float* out_std,
                         int32_t set);
 int swap_surrogate_weights(swap_surrogate* net, int32_t layer, float* w, float* b, int32_t set);

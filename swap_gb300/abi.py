@@ -194,6 +194,7 @@ SIGNATURES: dict[str, tuple] = {
     "swap_surrogate_train": (C.c_int, [P, C.c_int32, C.c_double, c_double_p]),
     "swap_surrogate_loss": (C.c_int, [P, c_double_p]),
     "swap_surrogate_attach": (C.c_int, [P, P, C.c_int32, C.c_double]),
+    "swap_surrogate_set_db_bound": (C.c_int, [P, C.c_double]),
     "swap_surrogate_stats": (C.c_int, [P, c_double_p]),
     "swap_surrogate_norm": (C.c_int, [P, P, P, P, P, C.c_int32]),
     "swap_surrogate_weights": (C.c_int, [P, C.c_int32, P, P, C.c_int32]),

@@ -68,6 +68,7 @@ struct F32State {
   swap_surrogate* collect = nullptr;  // network collecting training pairs
   int sur_every = 8;
   double sur_bound = 1e-3;
+  double sur_bound_db = 0;             // bound on the (B - b0) error too; 0: none
   bool sur_off = false;               // the last judge failed: plain until one passes
   long long sur_step = 0, sur_used = 0, sur_judged = 0, sur_fallbacks = 0;
   double sur_err_b = 0, sur_err_db = 0;
@@ -707,7 +708,7 @@ static int field_step(swap_ctx* c, F32State* s) {
     s->sur_err_b = std::sqrt(h[0] / std::max(h[1], 1e-300));
     s->sur_err_db = std::sqrt(h[0] / std::max(h[2], 1e-300));
     ++s->sur_judged;
-    s->sur_off = s->sur_err_b > s->sur_bound;
+    s->sur_off = s->sur_err_b > s->sur_bound || (s->sur_bound_db > 0 && s->sur_err_db > s->sur_bound_db);
     if (s->sur_off) ++s->sur_fallbacks;
   }
   return SWAP_OK;
@@ -1042,6 +1043,15 @@ extern "C" int swap_surrogate_attach(swap_ctx* c, swap_surrogate* net, int32_t j
   s->sur_off = false;
   s->sur_step = 0;
   if (net) TRY(sur_buffers(c, s));
+  return SWAP_OK;
+}
+
+extern "C" int swap_surrogate_set_db_bound(swap_ctx* c, double bound_db) {
+  if (!c) return SWAP_EINVAL;
+  F32State* s = f32(c);
+  if (!s) return c->fail(SWAP_EINVAL, "swap_f32_begin has not been called");
+  if (!(bound_db >= 0)) return c->fail(SWAP_EINVAL, "bound_db >= 0");
+  s->sur_bound_db = bound_db;
   return SWAP_OK;
 }
 

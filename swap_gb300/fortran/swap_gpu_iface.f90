@@ -397,6 +397,11 @@ module swap_gpu_iface
        integer(c_int32_t), value :: judge_every
        real(c_double), value :: bound
      end function swap_surrogate_attach
+     integer(c_int) function swap_surrogate_set_db_bound(ctx, bound_db) bind(C, name="swap_surrogate_set_db_bound")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), value :: bound_db
+     end function swap_surrogate_set_db_bound
      integer(c_int) function swap_surrogate_stats(ctx, out) bind(C, name="swap_surrogate_stats")
        import :: c_int, c_ptr, c_double
        type(c_ptr), value :: ctx

@@ -573,9 +573,14 @@ class Surrogate:
         return loss.value, out
 
 
-def attach_surrogate(h: "Hybrid", net, judge_every: int = 8, bound: float = 1e-3):
-    """Use `net` for the field subcycles of h's FP32 steps (None detaches)."""
+def attach_surrogate(h: "Hybrid", net, judge_every: int = 8, bound: float = 1e-3, bound_db: float = 0.0):
+    """Use `net` for the field subcycles of h's FP32 steps (None detaches).
+
+    A judged step falls back when the network's B is more than `bound` from
+    the subcycles' relative to B, or, with bound_db > 0, more than bound_db
+    relative to the plain B - b0."""
     h._check(h.lib.swap_surrogate_attach(h.ctx, None if net is None else net.h, int(judge_every), float(bound)))
+    h._check(h.lib.swap_surrogate_set_db_bound(h.ctx, float(bound_db)))
 
 
 def surrogate_stats(h: "Hybrid") -> dict:

@@ -197,6 +197,12 @@ def test_surrogate_in_the_step_is_judged_and_falls_back():
     st = surrogate_stats(h)
     # judged at steps 0, 2, 4, each above the bound: the network never runs
     assert (st["net_steps"], st["judged"], st["fallbacks"]) == (9, 6, 3), st
+    # the B bound met, an impossible bound on the (B - b0) error: the same
+    attach_surrogate(h, net, judge_every=2, bound=1e-2, bound_db=1e-12)
+    h.f32_run(6)
+    st = surrogate_stats(h)
+    assert (st["net_steps"], st["judged"], st["fallbacks"]) == (9, 9, 6), st
+    assert 0 < st["err_b"] < 1e-2 and st["err_db"] > st["err_b"]  # |B - b0| < |B|
     attach_surrogate(h, None)
     h.f32_end()
     h.sync_to_host()
