@@ -4,6 +4,7 @@
 
 #include "k32.cuh"
 #include "philox.h"
+#include "swap_dev.cuh"
 #include "tc05.cuh"
 
 namespace swapk32 {
@@ -22,7 +23,9 @@ constexpr int PASS_STAGES = SWAP_PASS_STAGES;
 // flight land before it exits (the wait itself is bounded by
 // StepParams::wait_polls).
 constexpr uint32_t STAGE_WAIT_POLLS = 1u << 22;
-constexpr int KERR_DOMAIN = 3, KERR_CAPACITY = 4, KERR_MOVE = 7, KERR_STAGE = 8, KERR_RANGE = 10;
+// the device error codes of every kernel (swap_dev.cuh), as ints
+constexpr int KERR_DOMAIN = swapk::KERR_DOMAIN, KERR_CAPACITY = swapk::KERR_CAPACITY, KERR_MOVE = swapk::KERR_MOVE,
+              KERR_WAIT = swapk::KERR_WAIT, KERR_RANGE = swapk::KERR_RANGE;
 
 inline unsigned nblk(long long n, int tpb = TPB) {
   const long long b = (n + tpb - 1) / tpb;
@@ -354,7 +357,7 @@ __global__ void __launch_bounds__(TPB_PASS, PASS == 3 ? 7 : 8) k_pass(G32 g, Par
     // the barrier publishes the chunk to every thread and frees the buffer of
     // chunk kc-1, which every thread is done with: chunk kc+NS-1 goes there
     if (__syncthreads_or(!got)) {
-      set_err(err, KERR_STAGE);
+      set_err(err, KERR_WAIT);
       // let the copies still in flight land before the CTA's shared memory
       // is released (each wait bounded)
       if (threadIdx.x == 0)

@@ -8,7 +8,7 @@ namespace swapk {
 
 // Error codes written by kernels into the context's device flag (first
 // writer wins); the host maps them to SWAP_E* status codes.
-enum : int { KERR_NONE = 0, KERR_DOMAIN = 3, KERR_MOVE = 7, KERR_WAIT = 8, KERR_RANGE = 10 };
+enum : int { KERR_NONE = 0, KERR_DOMAIN = 3, KERR_CAPACITY = 4, KERR_MOVE = 7, KERR_WAIT = 8, KERR_RANGE = 10 };
 
 // Grid geometry on the device.  Node arrays are 1-based (element 0 unused)
 // so kernel code reads like the reference: qx[i] is qx(i).

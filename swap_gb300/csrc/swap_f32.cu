@@ -16,6 +16,7 @@
 
 #include "../../include/swap_gpu.h"
 #include "k32.cuh"
+#include "swap_dev.cuh"
 #include "swap_ctx.h"
 #include "swap_ops.h"
 #include "swap_prof.h"
@@ -162,14 +163,14 @@ static int check_err(swap_ctx* c) {
   CU(cudaStreamSynchronize(c->st));
   if (herr) {
     cudaMemset(c->d_err, 0, sizeof(int));
-    if (herr == 3) return c->fail(SWAP_EDOMAIN, "a particle lies outside the grid");
-    if (herr == 4) return c->fail(SWAP_ECAPACITY, "Ni_max exceeded by new ions");
-    if (herr == 7)
+    if (herr == swapk::KERR_DOMAIN) return c->fail(SWAP_EDOMAIN, "a particle lies outside the grid");
+    if (herr == swapk::KERR_CAPACITY) return c->fail(SWAP_ECAPACITY, "Ni_max exceeded by new ions");
+    if (herr == swapk::KERR_MOVE)
       return c->fail(SWAP_EMOVE,
                      "a particle's half move spanned the grid less two cells, or more than 65536 particles "
                      "moved more than one cell per axis in one step");
-    if (herr == 8) return c->fail(SWAP_EWAIT, "a particle chunk copy did not complete within its wait limit");
-    if (herr == 10)
+    if (herr == swapk::KERR_WAIT) return c->fail(SWAP_EWAIT, "a particle chunk copy did not complete within its wait limit");
+    if (herr == swapk::KERR_RANGE)
       return c->fail(SWAP_ENONFINITE,
                      "a moment sum is not finite or beyond the exact sums' range (|sum| < 2^15)");
     return c->fail(SWAP_ECUDA, "device error flag " + std::to_string(herr));
