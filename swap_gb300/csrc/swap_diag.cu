@@ -443,6 +443,7 @@ extern "C" int swap_checkpoint_read(swap_ctx* c, const char* path) {
     r = c->fail(SWAP_EINVAL, "checkpoint grid differs from the context's");
   if (!r && (h.dims.real_bytes == 4 ? 4 : 8) != c->real_bytes)
     r = c->fail(SWAP_EINVAL, "checkpoint real size differs from the context's");
+  if (!r && h.ni_tot < 0) r = c->fail(SWAP_EINVAL, "checkpoint holds a negative ion count");
   if (!r && h.ni_tot > c->dims.ni_max) r = c->fail(SWAP_ECAPACITY, "checkpoint holds more ions than Ni_max");
   if (!r) {
     for (auto& a : host_arrays(c, (std::size_t)h.ni_tot))
@@ -451,10 +452,10 @@ extern "C" int swap_checkpoint_read(swap_ctx* c, const char* path) {
   }
   if (!r) {
     *c->ni_tot_ptr = (int32_t)h.ni_tot;
-    TRY(swap_mark_host_dirty(c, nullptr));
+    r = swap_mark_host_dirty(c, nullptr);  // (each failure below still closes the file)
     c->weights_valid = false;
-    if (h.have_srcs) {
-      TRY(swap_set_sources(c, &h.srcs, h.src_step));
+    if (!r && h.have_srcs) r = swap_set_sources(c, &h.srcs, h.src_step);
+    if (!r && h.have_srcs) {
       unsigned long long* cnt = srcops::counters(c);
       if (!cnt || cudaMemcpy(cnt + 1, &h.chex_total, 8, cudaMemcpyHostToDevice) != cudaSuccess)
         r = c->fail(SWAP_ECUDA, "checkpoint counters");
