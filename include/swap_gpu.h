@@ -402,16 +402,18 @@ int swap_conv3_check(int32_t nx, int32_t ny, int32_t nz, int32_t cin, int32_t co
 
 /* ---- the learned field-subcycle surrogate (FP32 form) ----
  * A 3D convolutional network (swap_surrogate_layers periodic 3x3x3 layers,
- * 14 -> 32 -> ... -> 32 -> 3 channels, GELU; BF16 weights and activations,
- * FP32 accumulation on the tensor cores) maps the state at the start of the
- * field subcycles (B, u_p, n_p, p_e, E0, the plain E there, and B - b12,
- * the change over the last subcycle that the leapfrog predictor starts from) to the
- * step's mean corrector E minus E0; B then advances as B - dt curl E, so
+ * 14 -> W -> ... -> W -> 3 channels with W = swap_surrogate_width, GELU;
+ * BF16 weights and activations, FP32 accumulation on the tensor cores) maps
+ * the state at the start of the field subcycles (B, u_p, n_p, p_e, E0, the
+ * plain E there, and B - b12, the change over the last subcycle that the
+ * leapfrog predictor starts from) to the step's mean corrector E minus E0; B then advances as B - dt curl E, so
  * div B stays where it was.  It is trained on pairs the plain subcycles of
  * swap_surrogate_collect produce, with Adam.
  * Attached to a context, it replaces the subcycles; every judge_every-th
  * step both run, the plain result is kept, and a B rel-L2 difference above
- * bound switches the network off until a judged step passes. */
+ * bound (or, with swap_surrogate_set_db_bound, a difference relative to
+ * B - b0 above that bound) switches the network off until a judged step
+ * passes. */
 typedef struct swap_surrogate swap_surrogate;
 int swap_surrogate_create(swap_surrogate** net, uint64_t seed, int32_t max_samples);
 int swap_surrogate_destroy(swap_surrogate* net);

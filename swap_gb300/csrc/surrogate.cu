@@ -496,7 +496,7 @@ extern "C" int swap_conv3_check(int32_t nx, int32_t ny, int32_t nz, int32_t cin,
 }
 
 // ---------------------------------------------------------------------------
-// the network: NL periodic 3x3x3 conv layers, 14 -> 32 -> ... -> 32 -> 3
+// the network: NL periodic 3x3x3 conv layers, 14 -> HID -> ... -> HID -> 3
 // channels, GELU between them; BF16 weights and activations, FP32
 // accumulation, FP32 master weights trained with Adam
 // ---------------------------------------------------------------------------
