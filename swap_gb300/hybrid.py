@@ -468,8 +468,9 @@ class Hybrid:
 class Surrogate:
     """The learned field-subcycle surrogate (a handle of the C-ABI)."""
 
-    # inputs per voxel: B (3), u_p (3), n_p, p_e, and E0 (3), the plain E at the
-    # start of the field step; the output is the mean corrector E minus E0
+    # inputs per voxel: B (3), u_p (3), n_p, p_e, E0 (3), the plain E at the
+    # start of the field step, and B - b12 (3), the change over the last
+    # subcycle; the output is the mean corrector E minus E0
     NIN = 14
 
     def __init__(self, seed: int = 1, max_samples: int = 4096, curl_weight: float = 0.0, per_pair: bool = False):
