@@ -4,8 +4,9 @@
 // plus FP32 offsets inside the cell, FP32 v and vp1, a species byte.  They
 // are kept sorted by a brick-major key (bricks of 4x4x4 cells), so one CTA
 // owns one brick's particles as a contiguous range.  Grids keep the
-// reference's (nx,ny,nz[,3]) layout with ghosts; B is accumulated in FP64
-// and its perturbation dB = B - b0 is mirrored in FP32 for the stencils.
+// reference's (nx,ny,nz[,3]) layout with ghosts; B is accumulated in
+// double-float (float hi + lo pairs) and its perturbation dB = B - b0 is
+// mirrored in FP32 for the stencils.
 #pragma once
 
 #include <cmath>
