@@ -52,3 +52,37 @@ def test_fortran_module_binds_declared_symbols():
     assert len(names) > 30
     missing = names - set(header_symbols())
     assert not missing, missing
+
+
+def test_header_compiles_as_c_and_links(tmp_path):
+    """A C caller (what a Fortran ISO_C_BINDING build links like) compiles
+    against the header with every warning an error, links every declared
+    entry from the library, and runs without a GPU."""
+    import shutil
+    import subprocess
+
+    from swap_gb300 import build
+
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        import pytest
+
+        pytest.skip("no C compiler")
+    lib_path = build.build()
+    syms = header_symbols()
+    src = tmp_path / "caller.c"
+    src.write_text(
+        '#include <stdio.h>\n#include "swap_gpu.h"\n'
+        "typedef void (*entry)(void);\n"
+        "static const entry entries[] = {\n" + "".join(f"  (entry){s},\n" for s in syms) + "};\n"
+        "int main(void) {\n"
+        '  printf("%d %d\\n", (int)(sizeof entries / sizeof entries[0]), swap_abi_version());\n'
+        "  return 0;\n}\n")
+    exe = tmp_path / "caller"
+    r = subprocess.run([gcc, "-std=c11", "-Wall", "-Wextra", "-Wpedantic", "-Werror", f"-I{ROOT / 'include'}",
+                        str(src), f"-L{lib_path.parent}", f"-l:{lib_path.name}", f"-Wl,-rpath,{lib_path.parent}",
+                        "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.split() == [str(len(syms)), "1"]
