@@ -86,3 +86,95 @@ def test_header_compiles_as_c_and_links(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert out.returncode == 0, out.stderr
     assert out.stdout.split() == [str(len(syms)), "1"]
+
+
+# ---- the Fortran interfaces against the header's prototypes ----
+
+def _header_prototypes():
+    """{name: (return type, [parameter types])} with pointer and array
+    parameters written as 'T*'."""
+    text = (ROOT / "include" / "swap_gpu.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    out = {}
+    for ret, name, args in re.findall(r"^([A-Za-z_][A-Za-z0-9_ *]*?)\b(swap_\w+)\s*\(([^;]*?)\)\s*;", text,
+                                      flags=re.M | re.S):
+        types = []
+        for a in (x.strip() for x in args.replace("\n", " ").split(",")):
+            if not a or a == "void":
+                continue
+            arr = a.endswith("]")
+            a = re.sub(r"\[[^\]]*\]$", "", a).strip()
+            t = re.match(r"^(.*?)\w+$", a).group(1)
+            types.append(re.sub(r"\s+", " ", t).strip().replace(" *", "*").replace("const ", "") + ("*" if arr else ""))
+        out[name] = (re.sub(r"\s+", " ", ret).strip().replace(" *", "*"), types)
+    return out
+
+
+def _fortran_interfaces():
+    """{bind name: (result type, [(dummy, type spec with attributes)])} of the
+    interface blocks, continuation lines joined and comments dropped."""
+    lines, buf = [], ""
+    for raw in (ROOT / "swap_gb300" / "fortran" / "swap_gpu_iface.f90").read_text().splitlines():
+        s = raw.split("!")[0].rstrip()
+        if not s.strip():
+            continue
+        s = (buf + " " + s.strip().lstrip("&").strip()) if buf else s.strip()
+        if s.endswith("&"):
+            buf = s[:-1].rstrip()
+            continue
+        buf = ""
+        lines.append(s)
+    out, i = {}, 0
+    while i < len(lines):
+        m = re.match(r'^(.*?)\bfunction\s+\w+\s*\(([^)]*)\)\s*bind\(C,\s*name="(\w+)"\)', lines[i], re.I)
+        if m:
+            decl, i = {}, i + 1
+            while not re.match(r"^end\s+function", lines[i], re.I):
+                d = re.match(r"^(?!import)(.*?)::(.*)$", lines[i], re.I)
+                if d:
+                    for nm in re.findall(r"(\w+)\s*(?:\([^)]*\))?", d.group(2)):
+                        decl[nm.lower()] = d.group(1).strip().lower()
+                i += 1
+            dummies = [a.strip().lower() for a in m.group(2).split(",") if a.strip()]
+            out[m.group(3)] = (m.group(1).strip().lower(), [(a, decl.get(a, "")) for a in dummies])
+        i += 1
+    return out
+
+
+_BY_VALUE = {"int32_t": {"integer(c_int32_t)", "integer(c_int)"}, "int": {"integer(c_int)", "integer(c_int32_t)"},
+             "uint32_t": {"integer(c_int32_t)"}, "int64_t": {"integer(c_int64_t)"},
+             "uint64_t": {"integer(c_int64_t)"}, "double": {"real(c_double)"}, "float": {"real(c_float)"},
+             "swap_exchange_fn": {"type(c_funptr)"}}
+_BY_REFERENCE = {"double": {"real(c_double)", "real(wp)"}, "float": {"real(c_float)", "real(wp)"},
+                 "int32_t": {"integer(c_int32_t)", "integer(c_int)"}, "int64_t": {"integer(c_int64_t)"},
+                 "char": {"character(kind=c_char)"}, "swap_ctx*": {"type(c_ptr)"},
+                 "swap_surrogate*": {"type(c_ptr)"}}
+
+
+def test_fortran_interfaces_match_the_header_prototypes():
+    """Every bind(C) interface passes each argument as the C prototype takes
+    it: scalars by value with the same kind, pointers as `type(c_ptr),
+    value` or by reference to an object of the pointed-to type (real(wp)
+    arrays for the real arrays, whose width swap_dims.real_bytes gives)."""
+    protos, ifaces = _header_prototypes(), _fortran_interfaces()
+    assert len(ifaces) > 30
+    bad = []
+    for name, (result, dummies) in ifaces.items():
+        ret, types = protos[name]
+        if len(types) != len(dummies):
+            bad.append((name, "takes", len(types), "arguments, the interface", len(dummies)))
+            continue
+        if not result.startswith({"int": "integer(c_int)", "const char*": "type(c_ptr)"}[ret]):
+            bad.append((name, "returns", ret, result))
+        for ctype, (dummy, spec) in zip(types, dummies):
+            by_value = "value" in spec
+            base = spec.split(",")[0].replace(" ", "")
+            if ctype.endswith("*"):
+                pointee = ctype[:-1]
+                ok = base == "type(c_ptr)" if by_value else (
+                    pointee == "void" or base in _BY_REFERENCE.get(pointee, {f"type({pointee}_t)"}))
+            else:
+                ok = by_value and base in _BY_VALUE.get(ctype, ())
+            if not ok:
+                bad.append((name, dummy, ctype, spec))
+    assert not bad, bad
