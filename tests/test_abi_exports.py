@@ -178,3 +178,73 @@ def test_fortran_interfaces_match_the_header_prototypes():
             if not ok:
                 bad.append((name, dummy, ctype, spec))
     assert not bad, bad
+
+
+# ---- the argument structs: C, ctypes and Fortran layouts ----
+
+_STRUCTS = {"swap_dims": ("Dims", "swap_dims_t"), "swap_params": ("Params", "swap_params_t"),
+            "swap_coords": ("Coords", "swap_coords_t"), "swap_sources": ("Sources", "swap_sources_t"),
+            "swap_diag_spec": ("DiagSpec", "swap_diag_spec_t"), "swap_load_spec": ("LoadSpec", None)}
+
+
+def _c_struct_fields():
+    """{struct: [(field, C type)]} from the header's typedefs."""
+    text = re.sub(r"/\*.*?\*/", "", (ROOT / "include" / "swap_gpu.h").read_text(), flags=re.S)
+    out = {}
+    for name, body in re.findall(r"typedef struct (swap_\w+) \{(.*?)\}", text, flags=re.S):
+        fields = []
+        for decl in (d.strip() for d in body.split(";") if d.strip()):
+            m = re.match(r"^((?:const )?\w+)\s*(.*)$", " ".join(decl.split()))
+            for f in m.group(2).split(","):
+                f = f.strip()
+                fields.append((f.lstrip("*"), m.group(1) + "*" * f.count("*")))
+        out[name] = fields
+    return out
+
+
+def test_struct_layouts_agree_in_c_ctypes_and_fortran(tmp_path):
+    """The C compiler's offsets and sizes of every argument struct equal the
+    ctypes mirrors', and each Fortran bind(C) type lists the same fields in
+    the same order with interoperable kinds."""
+    import shutil
+    import subprocess
+
+    from swap_gb300 import abi
+
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        import pytest
+
+        pytest.skip("no C compiler")
+    cfields = _c_struct_fields()
+    assert set(_STRUCTS) <= set(cfields)
+    prog = ['#include <stddef.h>', '#include <stdio.h>', '#include "swap_gpu.h"', "int main(void) {"]
+    for s in _STRUCTS:
+        prog.append(f'  printf("{s} %zu\\n", sizeof({s}));')
+        prog += [f'  printf("{s}.{f} %zu\\n", offsetof({s}, {f}));' for f, _ in cfields[s]]
+    prog += ["  return 0;", "}"]
+    src, exe = tmp_path / "layout.c", tmp_path / "layout"
+    src.write_text("\n".join(prog) + "\n")
+    r = subprocess.run([gcc, "-std=c11", "-Wall", "-Werror", f"-I{ROOT / 'include'}", str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    c_layout = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                             check=True).stdout.splitlines())
+    ftext = (ROOT / "swap_gb300" / "fortran" / "swap_gpu_iface.f90").read_text()
+    fkind = {"int32_t": "integer(c_int32_t)", "uint32_t": "integer(c_int32_t)", "int64_t": "integer(c_int64_t)",
+             "uint64_t": "integer(c_int64_t)", "double": "real(c_double)", "const double*": "type(c_ptr)"}
+    for s, (py, ftype) in _STRUCTS.items():
+        cls = getattr(abi, py)
+        assert [f for f, _ in cls._fields_] == [f for f, _ in cfields[s]], s
+        assert ctypes.sizeof(cls) == int(c_layout[s]), s
+        for f, _ in cfields[s]:
+            assert getattr(cls, f).offset == int(c_layout[f"{s}.{f}"]), (s, f)
+        if ftype is None:
+            continue
+        body = re.search(rf"type, bind\(C\) :: {ftype}\n(.*?)end type {ftype}", ftext, flags=re.S).group(1)
+        flist = []
+        for line in filter(str.strip, body.replace("&\n", " ").splitlines()):
+            spec, names = line.split("::")
+            flist += [(n.strip().lower(), spec.strip().lower()) for n in names.split(",")]
+        assert [f for f, _ in flist] == [f.lower() for f, _ in cfields[s]], s
+        assert [k for _, k in flist] == [fkind[t] for _, t in cfields[s]], s
