@@ -248,3 +248,25 @@ def test_struct_layouts_agree_in_c_ctypes_and_fortran(tmp_path):
             flist += [(n.strip().lower(), spec.strip().lower()) for n in names.split(",")]
         assert [f for f, _ in flist] == [f.lower() for f, _ in cfields[s]], s
         assert [k for _, k in flist] == [fkind[t] for _, t in cfields[s]], s
+
+
+def test_python_signatures_match_the_header_prototypes():
+    """The ctypes signature of every entry has the prototype's argument count,
+    the same scalar types, and a pointer wherever the prototype takes one."""
+    from swap_gb300 import abi
+
+    scalar = {"int32_t": ctypes.c_int32, "int": ctypes.c_int, "uint32_t": ctypes.c_uint32,
+              "int64_t": ctypes.c_int64, "uint64_t": ctypes.c_uint64, "double": ctypes.c_double,
+              "float": ctypes.c_float, "swap_exchange_fn": abi.EXCHANGE_FN}
+    pointers = (ctypes.c_void_p, ctypes.c_char_p, ctypes._Pointer)
+    bad = []
+    for name, (ret, types) in _header_prototypes().items():
+        res, args = abi.SIGNATURES[name]
+        if res is not {"int": ctypes.c_int, "const char*": ctypes.c_char_p}[ret] or len(args) != len(types):
+            bad.append((name, ret, len(types), res, len(args)))
+            continue
+        for k, (ctype, py) in enumerate(zip(types, args)):
+            ok = (isinstance(py, type) and issubclass(py, pointers)) if ctype.endswith("*") else py is scalar[ctype]
+            if not ok:
+                bad.append((name, k, ctype, py))
+    assert not bad, bad
