@@ -524,9 +524,9 @@ contains
     real(wp) :: xp(*), vp(*), vp1(*), input_p(*)
     call swap_check(c_move_ion_half(swap_gpu_ctx, xp, vp, vp1, input_p), 'move_ion_half')
   end subroutine move_ion_half
-  subroutine curlB(bt, np, aj)
-    real(wp) :: bt(*), np(*), aj(*)
-    call swap_check(c_curlB(swap_gpu_ctx, bt, np, aj), 'curlB')
+  subroutine curlB(b1, np, aj)
+    real(wp) :: b1(*), np(*), aj(*)
+    call swap_check(c_curlB(swap_gpu_ctx, b1, np, aj), 'curlB')
   end subroutine curlB
   subroutine edge_to_center(bt, btc)
     real(wp) :: bt(*), btc(*)

@@ -1,17 +1,25 @@
-"""Generate tests/golden/b0_dat.json from the reference's own golden file.
+"""Generate the fixtures of tests/golden from the reference's source tree.
 
+b0_dat.json -- the reference's own golden vector.
 The reference ships one golden vector, b0.dat, written by grd6_setup
 (initial.f:136-139) as a Fortran unformatted sequential file with two
 records: nz (int32) and b0(nx,ny,nz,3) (float32).  This script decodes it and
 the run-time inputs it was made from (inputs.dat, read by inputs.f:84-119)
 into a small JSON fixture, so that tests need nothing from the reference at
-run time.  Usage: python tests/golden/make_fixtures.py [reference_dir]
+run time.
+
+reference_interfaces.json -- the argument lists of the reference subroutines
+that the Fortran wrappers replace, with the file and line of each header,
+so that a test can hold the wrappers to the reference's interfaces.
+
+Usage: python tests/golden/make_fixtures.py REFERENCE_DIR
 """
 from __future__ import annotations
 
 import hashlib
 import json
 import os
+import re
 import struct
 import sys
 from pathlib import Path
@@ -69,6 +77,36 @@ def main(ref: Path):
     }
     out = HERE / "b0_dat.json"
     out.write_text(json.dumps(fx, indent=1) + "\n")
+    print("wrote", out)
+    interfaces(ref)
+
+
+# The subroutines of the ion step that the Fortran wrappers stand in for.
+WRAPPED = ["get_interp_weights", "update_np", "update_up", "extrapol_up", "get_Ep", "get_vplus_vminus",
+           "improve_up", "get_vp_final", "move_ion_half", "curlB", "edge_to_center", "face_to_center", "get_E",
+           "predict_B", "correct_B", "f_update_tlev", "check_time_step", "periodic", "periodic_scalar",
+           "Ionize_sw_mp", "remove_ion", "res_chex", "update_rho", "get_temperature"]
+
+
+def interfaces(ref: Path):
+    """Each wrapped subroutine's header line in the fixed-form sources:
+    its dummy arguments in order, and where it stands."""
+    found = {}
+    for f in sorted(ref.glob("*.f")):
+        if f.name == "old_routines.f":  # superseded copies, not compiled by the makefile
+            continue
+        for ln, line in enumerate(f.read_text(errors="replace").splitlines(), 1):
+            if line[:1] in "cC*!":
+                continue
+            m = re.match(r"^\s+subroutine\s+(\w+)\s*\(([^)]*)\)", line, re.I)
+            if m and m.group(1) in WRAPPED:
+                assert m.group(1) not in found, ("defined twice", m.group(1))
+                found[m.group(1)] = {"args": [a.strip() for a in m.group(2).split(",")], "at": f"{f.name}:{ln}"}
+    missing = sorted(set(WRAPPED) - set(found))
+    assert not missing, missing
+    out = HERE / "reference_interfaces.json"
+    out.write_text(json.dumps({"source": "SUBROUTINE headers of pdelamere/SWAP", "subroutines": found},
+                              indent=1, sort_keys=True) + "\n")
     print("wrote", out)
 
 

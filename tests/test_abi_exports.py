@@ -270,3 +270,19 @@ def test_python_signatures_match_the_header_prototypes():
             if not ok:
                 bad.append((name, k, ctype, py))
     assert not bad, bad
+
+
+def test_fortran_wrappers_keep_the_reference_argument_lists():
+    """The wrappers of module swap_gpu_calls carry each replaced reference
+    subroutine's name and dummy arguments in order (Fortran is not case
+    sensitive), against the headers recorded in tests/golden."""
+    import json
+
+    ref = json.loads((ROOT / "tests" / "golden" / "reference_interfaces.json").read_text())["subroutines"]
+    text = (ROOT / "swap_gb300" / "fortran" / "swap_gpu_iface.f90").read_text()
+    calls = text[text.index("module swap_gpu_calls"):]
+    ours = {m.group(1).lower(): [a.strip().lower() for a in m.group(2).split(",")]
+            for m in re.finditer(r"^\s*subroutine\s+(\w+)\s*\(([^)]*)\)", calls, flags=re.M)}
+    assert len(ref) >= 20
+    for name, sub in ref.items():
+        assert ours.get(name.lower()) == [a.lower() for a in sub["args"]], (name, sub["at"], ours.get(name.lower()))
