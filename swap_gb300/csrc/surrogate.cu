@@ -432,9 +432,10 @@ cudaError_t launch_conv3(const ConvArgs& a, int nsm, cudaStream_t st) {
 }
 
 cudaError_t conv3(int cin, int cout, const ConvArgs& a, cudaStream_t st) {
-  int dev = 0, nsm = 148;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  int dev = 0, nsm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
   if (cin == 16 && cout == 32) return launch_conv3<16, 32>(a, nsm, st);
   if (cin == 32 && cout == 32) return launch_conv3<32, 32>(a, nsm, st);
   if (cin == 32 && cout == 16) return launch_conv3<32, 16>(a, nsm, st);
@@ -1241,11 +1242,15 @@ extern "C" int swap_surrogate_create(swap_surrogate** out, uint64_t seed, int32_
       for (int o = 0; o < co_real; ++o)
         for (int i = 0; i < ci_real; ++i) hw[((std::size_t)t * co + o) * ci + i] = (float)nd(rng);
     for (std::size_t i = 0; i < nw; ++i) hh[i] = __float2bfloat16(hw[i]);
-    cudaMemcpy(net->w[l], hw.data(), nw * sizeof(float), cudaMemcpyHostToDevice);
-    cudaMemcpy(net->wh[l], hh.data(), nw * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice);
-    cudaMemset(net->b[l], 0, co * sizeof(float));
-    for (float* p : {net->mw[l], net->vw[l]}) cudaMemset(p, 0, nw * sizeof(float));
-    for (float* p : {net->mb[l], net->vb[l]}) cudaMemset(p, 0, co * sizeof(float));
+    bool ok = cudaMemcpy(net->w[l], hw.data(), nw * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(net->wh[l], hh.data(), nw * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemset(net->b[l], 0, co * sizeof(float)) == cudaSuccess;
+    for (float* p : {net->mw[l], net->vw[l]}) ok = ok && cudaMemset(p, 0, nw * sizeof(float)) == cudaSuccess;
+    for (float* p : {net->mb[l], net->vb[l]}) ok = ok && cudaMemset(p, 0, co * sizeof(float)) == cudaSuccess;
+    if (!ok) {
+      delete net;
+      return SWAP_ECUDA;
+    }
   }
   net->d_mean = net->alloc<float>(NIN);
   net->d_istd = net->alloc<float>(NIN);
@@ -1255,8 +1260,8 @@ extern "C" int swap_surrogate_create(swap_surrogate** out, uint64_t seed, int32_
     delete net;
     return SWAP_ECUDA;
   }
-  cudaMemset(net->err, 0, sizeof(int));
-  if (upload_norm(net, nullptr) || refresh_flips(net, nullptr) || cudaDeviceSynchronize() != cudaSuccess) {
+  if (cudaMemset(net->err, 0, sizeof(int)) != cudaSuccess || upload_norm(net, nullptr) ||
+      refresh_flips(net, nullptr) || cudaDeviceSynchronize() != cudaSuccess) {
     delete net;
     return SWAP_ECUDA;
   }

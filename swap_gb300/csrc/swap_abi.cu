@@ -760,10 +760,13 @@ extern "C" int swap_get_interp_weights(swap_ctx* c, const double* xp) {
   if (r == SWAP_OK && c->h_ijkp) {  // the COMMON ijkp mirror now holds new indices
     Mirror* m = c->find(c->h_ijkp);
     const std::size_t NM = (std::size_t)c->dims.ni_max;
-    for (int k = 0; k < 3; ++k)
-      cudaMemcpyAsync(static_cast<int32_t*>(m->dev) + k * NM, c->d_ijk + k * NM, (std::size_t)c->ntot() * 4,
-                      cudaMemcpyDeviceToDevice, c->st);
-    cudaStreamSynchronize(c->st);
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k)
+      e = cudaMemcpyAsync(static_cast<int32_t*>(m->dev) + k * NM, c->d_ijk + k * NM, (std::size_t)c->ntot() * 4,
+                          cudaMemcpyDeviceToDevice, c->st);
+    const cudaError_t e2 = cudaStreamSynchronize(c->st);  // also after a failed copy: nothing stays queued
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return c->cuda_fail(e, "ijkp mirror");
     m->dev_valid = true;
     m->host_valid = false;
   }
