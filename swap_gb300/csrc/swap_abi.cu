@@ -53,7 +53,10 @@ int swap_ctx::add_mirror(void* host, std::size_t bytes, MirrorKind kind, bool re
   m.kind = kind;
   m.host_f32 = real && real_bytes == 4;
   if (cudaMalloc(&m.dev, bytes) != cudaSuccess) return fail(SWAP_ECUDA, "device allocation of a mirror failed");
-  cudaMemsetAsync(m.dev, 0, bytes, st);
+  if (cudaMemsetAsync(m.dev, 0, bytes, st) != cudaSuccess) {
+    cudaFree(m.dev);
+    return fail(SWAP_ECUDA, "clearing a mirror failed");
+  }
   m.host_valid = true;
   m.dev_valid = false;
   reg.emplace(host, m);
@@ -551,11 +554,10 @@ extern "C" int swap_init(swap_ctx** out, const swap_dims* d, const swap_params* 
                      &c->s_upc, &c->s_btp1, &c->s_S, &c->s_gf, &c->s_gpc};
   for (double** b : bufs) {
     *b = c->dalloc(C3);
-    if (!*b) {
+    if (!*b || cudaMemset(*b, 0, C3 * sizeof(double)) != cudaSuccess) {
       swap_finalize(c);
       return SWAP_ECUDA;
     }
-    cudaMemset(*b, 0, C3 * sizeof(double));
   }
   c->s_dtn = c->dalloc((std::size_t)g.C);
   c->s_red = c->dalloc(8);
@@ -566,9 +568,11 @@ extern "C" int swap_init(swap_ctx** out, const swap_dims* d, const swap_params* 
   }
   c->owned.push_back(e);
   c->d_err = e;
-  cudaMemset(e, 0, sizeof(int));
-  cudaEventCreate(&c->t0);
-  cudaEventCreate(&c->t1);
+  if (cudaMemset(e, 0, sizeof(int)) != cudaSuccess || cudaEventCreate(&c->t0) != cudaSuccess ||
+      cudaEventCreate(&c->t1) != cudaSuccess) {
+    swap_finalize(c);
+    return SWAP_ECUDA;
+  }
   *out = c;
   return SWAP_OK;
 }
