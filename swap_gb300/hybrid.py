@@ -300,8 +300,8 @@ class Hybrid:
         self._check(self.lib.swap_move_ion_half(self.ctx, *map(abi.rptr, (xp, vp, vp1, input_p))))
 
     # ---- gutsf.f / grid_interp.f / boundary.f ----
-    def curlB(self, bt, np_, aj):
-        self._check(self.lib.swap_curlB(self.ctx, *map(abi.rptr, (bt, np_, aj))))
+    def curlB(self, b1, np_, aj):
+        self._check(self.lib.swap_curlB(self.ctx, *map(abi.rptr, (b1, np_, aj))))
 
     def edge_to_center(self, bt, btc):
         self._check(self.lib.swap_edge_to_center(self.ctx, abi.rptr(bt), abi.rptr(btc)))
@@ -340,6 +340,9 @@ class Hybrid:
 
     def periodic(self, b):
         self._check(self.lib.swap_periodic(self.ctx, abi.rptr(b)))
+
+    def periodic_scalar(self, b):
+        self._check(self.lib.swap_periodic_scalar(self.ctx, abi.rptr(b)))
 
     # ---- sources and sinks (chem_rates.f, gutsp.f:12-46) ----
     def set_sources(self, src: "abi.Sources", step0: int = 0):

@@ -286,3 +286,34 @@ def test_fortran_wrappers_keep_the_reference_argument_lists():
     assert len(ref) >= 20
     for name, sub in ref.items():
         assert ours.get(name.lower()) == [a.lower() for a in sub["args"]], (name, sub["at"], ours.get(name.lower()))
+
+
+# The module state a reference subroutine reads from its modules, which the
+# Python mirror takes as trailing arguments instead (the Fortran wrappers read
+# it from their module): the subcycle step and count (inputs.f, gutsf.f:1776,
+# 1115, 1309) and the ion step of res_chex's draws.
+_MODULE_STATE = {"check_time_step": ["dtsub", "ntf"], "predict_B": ["dtsub"], "correct_B": ["dtsub"],
+                 "res_chex": ["m_tstep"]}
+
+
+def test_python_mirror_keeps_the_reference_argument_lists():
+    """swap_gb300.hybrid.Hybrid has a method per replaced reference
+    subroutine with its dummy arguments in order (np spelled np_, which
+    would shadow numpy), then only the module state named above."""
+    import inspect
+    import json
+
+    from swap_gb300.hybrid import Hybrid
+
+    ref = json.loads((ROOT / "tests" / "golden" / "reference_interfaces.json").read_text())["subroutines"]
+    bad = []
+    for name, sub in ref.items():
+        method = getattr(Hybrid, name, None)
+        if method is None:
+            bad.append((name, "missing"))
+            continue
+        got = [p.rstrip("_").lower() for p in inspect.signature(method).parameters if p != "self"]
+        want = [a.lower() for a in sub["args"]] + _MODULE_STATE.get(name, [])
+        if got != want:
+            bad.append((name, sub["at"], want, got))
+    assert not bad, bad
