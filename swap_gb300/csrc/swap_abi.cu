@@ -53,7 +53,7 @@ int swap_ctx::add_mirror(void* host, std::size_t bytes, MirrorKind kind, bool re
   m.kind = kind;
   m.host_f32 = real && real_bytes == 4;
   if (cudaMalloc(&m.dev, bytes) != cudaSuccess) return fail(SWAP_ECUDA, "device allocation of a mirror failed");
-  if (cudaMemsetAsync(m.dev, 0, bytes, st) != cudaSuccess) {
+  if (bytes && cudaMemsetAsync(m.dev, 0, bytes, st) != cudaSuccess) {  // (ni_max = 0: no memory to clear)
     cudaFree(m.dev);
     return fail(SWAP_ECUDA, "clearing a mirror failed");
   }
