@@ -765,7 +765,7 @@ extern "C" int swap_get_interp_weights(swap_ctx* c, const double* xp) {
     Mirror* m = c->find(c->h_ijkp);
     const std::size_t NM = (std::size_t)c->dims.ni_max;
     cudaError_t e = cudaSuccess;
-    for (int k = 0; k < 3 && e == cudaSuccess; ++k)
+    for (int k = 0; k < 3 && e == cudaSuccess && c->ntot() > 0; ++k)
       e = cudaMemcpyAsync(static_cast<int32_t*>(m->dev) + k * NM, c->d_ijk + k * NM, (std::size_t)c->ntot() * 4,
                           cudaMemcpyDeviceToDevice, c->st);
     const cudaError_t e2 = cudaStreamSynchronize(c->st);  // also after a failed copy: nothing stays queued
