@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 from conftest import rel_l2, relerr
-from helpers import copy_state, fortran_records, make_hybrid, oracle_for
+from helpers import fortran_records, make_hybrid, oracle_for
 
 pytestmark = pytest.mark.gpu
 

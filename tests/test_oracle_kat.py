@@ -2,7 +2,6 @@
 b0.dat).  Each checks a property the reference algorithm has exactly or to
 roundoff."""
 import numpy as np
-import pytest
 
 from helpers import Host, oracle, small
 
