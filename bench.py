@@ -713,7 +713,9 @@ def run_ours(args):
             line["surrogate"] = run_surrogate(h, args, N, ws, net, info)
         except Exception as e:  # the headline stands without it
             line["surrogate"] = {"error": f"{type(e).__name__}: {e}"}
-    if f32 and args.fp64_steps > 0:
+    if ws > 1:  # per-GPU characterisations: the 1-GPU line carries them
+        line["single_gpu_legs"] = "the FP64, accuracy and CPU-baseline legs run in the 1-GPU line only"
+    if f32 and args.fp64_steps > 0 and ws == 1:
         # the plain FP64 GPU drop-in on the same workload: the other side of
         # the metric's FP32-versus-FP64 comparison
         try:
@@ -726,11 +728,11 @@ def run_ours(args):
     import gc
 
     gc.collect()
-    if rank == 0:
+    if ws == 1:
         run_accuracy_legs(args, line, net)
     if net is not None:
         net.close()
-    if rank == 0 and not args.no_cpu_baseline:
+    if ws == 1 and not args.no_cpu_baseline:
         try:
             r = oracle_run(cfg, "f32", 1, 1, os.cpu_count() or 1)
         except Exception as e:  # the headline stands without it
